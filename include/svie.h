@@ -1,0 +1,299 @@
+/*
+ * svie.h -- C ABI of the GB300 (sm_103a) narrow-band level-set erosion library.
+ *
+ * Every function takes plain device pointers, sizes and a cudaStream_t passed as
+ * `void* stream` (NULL = legacy default stream), returns an int status
+ * (SVIE_OK = 0) and allocates no device memory: scratch space is a
+ * caller-provided workspace whose size the matching *_workspace_bytes() query
+ * reports.  svie_last_error() returns the message of the last failure on the
+ * calling thread.  Grids are dense float32 arrays in C order with axes (x, y, z)
+ * (strides ny*nz, nz, 1); node lists are sorted int32 flat indices.
+ *
+ * Each declaration names the reference interface it replaces (paths within the
+ * SVIErosion project).  The reference binds nothing natively: its hot path is
+ * PyTorch functions compiled by torch.compile, so the "binding" is the Python
+ * module svierosion_gb300 (ctypes), whose functions keep the reference's names
+ * and argument orders.
+ */
+#ifndef SVIE_H
+#define SVIE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+#define SVIE_OK 0
+#define SVIE_ERR_ARG 1          /* bad argument / shape                        */
+#define SVIE_ERR_LAUNCH 2       /* CUDA launch or runtime error                */
+#define SVIE_ERR_WORKSPACE 3    /* workspace too small                         */
+#define SVIE_ERR_MARGIN 4       /* narrow band reaches the grid boundary       */
+#define SVIE_ERR_UNSUPPORTED 5  /* size outside what the kernels support      */
+#define SVIE_ERR_CAPACITY 6     /* output capacity too small                   */
+
+const char* svie_last_error(void);
+int svie_version(void);
+
+/* ---------------------------------------------------------------- structs */
+/* Speed law and integrator constants (reference svierosion/flows.py:51-213,
+ * svierosion/evolve.py:70-112).  kind: 0 = SVI power law, 1 = mean curvature,
+ * 2 = Gauss curvature. */
+typedef struct svie_law {
+  int32_t kind;
+  int32_t k;             /* SVI exponent                                   */
+  int32_t s;             /* SVI geometric switch (0/1)                     */
+  int32_t pad0;
+  double t;              /* SVI singularity                                */
+  double eps;            /* additive grassfire term                        */
+  double n_cap;          /* SVI cap on N (1.0 when s == 0)                 */
+  double radius;         /* SVI ball radius                                */
+  double alpha;          /* curvature exponent                             */
+  double delta;          /* curvature regularisation                       */
+  double cfl;
+  double feedback_cfl;
+  double parabolic_cfl;
+  double h;              /* grid spacing                                   */
+  double cut_a;          /* cutoff[0] * h                                  */
+  double cut_b;          /* cutoff[1] * h                                  */
+} svie_law;
+
+/* Per-step statistics and scalars, written on the device and read back once
+ * per step (reference svierosion/evolve.py:118-170, levelset.py:93-95,123-126).
+ * Float maxima of non-negative values are stored as IEEE bits; signed minima
+ * and maxima as order-preserving keys (see svierosion_gb300/_native.py). */
+typedef struct svie_stats {
+  double vsum_near;      /* sum of V (before cutoff) over |phi| < h       */
+  double vsum_all;       /* sum of V (before cutoff) over the band        */
+  double fsum;           /* sum of band cell fractions (float64)          */
+  double dt;             /* stable time step computed on the device        */
+  double dt_cap;         /* upper bound for dt (max_time - time or +inf)   */
+  double reserved_d[3];
+  uint32_t vmax;         /* max V after cutoff (float bits)               */
+  uint32_t qmin_near, qmax_near, qmin_all, qmax_all;   /* ordered keys    */
+  uint32_t dvmax_near, dvmax_all;                      /* float bits      */
+  uint32_t dmax_near, dmax_all;                        /* float bits      */
+  uint32_t capped_near, capped_all;
+  uint32_t n_near;
+  uint32_t any_neg, any_pos;   /* band has phi < 0 / phi > 0               */
+  uint32_t n_band;
+  uint32_t reserved_u;
+} svie_stats;
+
+/* Band bookkeeping written by svie_band_write (reference levelset.py:70-86,
+ * evolve.py:96-105). */
+typedef struct svie_band_info {
+  int64_t count;             /* band size                                   */
+  int64_t static_inside;     /* nodes outside the band with phi < 0          */
+  int32_t lo[3], hi[3];      /* min / max band coordinate per axis           */
+  int32_t ilo[3], ihi[3];    /* min / max coordinate of phi < 0 nodes        */
+} svie_band_info;
+
+/* ----------------------------------------------------- band construction */
+/* LevelSet.rebuild_band (svierosion/levelset.py:70-77): clamp phi to
+ * [-cap, cap] in place, then list the nodes with |phi| < thresh in ascending
+ * flat order.  Two calls: svie_band_scan clamps and counts (writing the count
+ * to info->count on the device); the caller reads it, sizes `band` and calls
+ * svie_band_write, which also writes occ[i] = (phi[i] < 0) for every node when
+ * occ is non-NULL, and fills the rest of *info (margin check data,
+ * levelset.py:79-86). */
+size_t svie_band_workspace_bytes(int64_t n);
+int svie_band_scan(float* phi, int64_t n, float cap, float thresh, void* ws, size_t ws_bytes,
+                   svie_band_info* info, void* stream);
+int svie_band_write(const float* phi, int nx, int ny, int nz, float thresh, const void* ws,
+                    size_t ws_bytes, int32_t* band, int64_t capacity, float* occ,
+                    svie_band_info* info, void* stream);
+
+/* Generic order-preserving compaction of mask[i] != 0 (torch.nonzero on a
+ * bool mask, as in levelset.py:173).  Same two-call protocol; `count` is a
+ * device int64. */
+int svie_mask_scan(const uint8_t* mask, int64_t n, void* ws, size_t ws_bytes, int64_t* count,
+                   void* stream);
+int svie_mask_write(const uint8_t* mask, int64_t n, const void* ws, size_t ws_bytes, int32_t* out,
+                    int64_t capacity, void* stream);
+
+/* ------------------------------------------------- stencil kernels (API) */
+/* svierosion/kernels.py:146 godunov_inward(flat, idx, sx, sy, sz, inv_h) */
+int svie_godunov_inward(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                        int64_t sz, float inv_h, float* out, void* stream);
+/* svierosion/kernels.py:173 cell_fractions(flat, idx, sx, sy, sz) */
+int svie_cell_fractions(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                        int64_t sz, float* out, void* stream);
+/* svierosion/kernels.py:185 closest_points(flat, idx, ny, nz, hi_x, hi_y, hi_z, h); out (m,3) */
+int svie_closest_points(const float* flat, const int32_t* idx, int64_t m, int ny, int nz, float hi_x,
+                        float hi_y, float hi_z, float h, float* out, void* stream);
+/* svierosion/kernels.py:212 tricubic(flat, ny, nz, p) */
+int svie_tricubic(const float* flat, int ny, int nz, const float* p, int64_t m, float* out,
+                  void* stream);
+/* svierosion/kernels.py:232 tricubic_with_gradient(flat, ny, nz, p); grad (m,3) */
+int svie_tricubic_with_gradient(const float* flat, int ny, int nz, const float* p, int64_t m,
+                                float* val, float* grad, void* stream);
+/* svierosion/kernels.py:257 trilinear(flat, ny, nz, p) */
+int svie_trilinear(const float* flat, int ny, int nz, const float* p, int64_t m, float* out,
+                   void* stream);
+/* svierosion/kernels.py:274 principal_curvatures(flat, idx, sx, sy, sz, h) */
+int svie_principal_curvatures(const float* flat, const int32_t* idx, int64_t m, int64_t sx,
+                              int64_t sy, int64_t sz, float h, float* k1, float* k2, void* stream);
+/* svierosion/kernels.py:303 interface_mask(flat, idx, sx, sy, sz) */
+int svie_interface_mask(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                        int64_t sz, uint8_t* out, void* stream);
+/* svierosion/kernels.py:382-427 _point_triangle_distance2 for m (point, triangle) pairs;
+ * p (m,3), a, b, c (m,3) */
+int svie_point_triangle_distance2(const float* p, const float* a, const float* b, const float* c,
+                                  int64_t m, float* out, void* stream);
+
+/* ------------------------------------------- occupancy and solid volume */
+/* LevelSet.dense_fractions (svierosion/levelset.py:117-121): occ[band[i]] =
+ * cell fraction; occ elsewhere must already hold (phi < 0). */
+int svie_scatter_fractions(const float* phi, const int32_t* band, int64_t m, int64_t sx, int64_t sy,
+                           int64_t sz, float* occ, void* stream);
+/* LevelSet.volume (svierosion/levelset.py:123-126) minus the static count:
+ * stats->fsum = float64 sum of the band cell fractions (deterministic order),
+ * stats->any_neg / any_pos = has_interface flags (levelset.py:93-95); when occ
+ * is non-NULL the fractions are also scattered into it. */
+size_t svie_volume_workspace_bytes(int64_t m);
+int svie_band_volume(const float* phi, const int32_t* band, int64_t m, int64_t sx, int64_t sy,
+                     int64_t sz, float* occ, void* ws, size_t ws_bytes, svie_stats* stats,
+                     void* stream);
+
+/* ------------------------------------------------------ SVI convolution */
+/* svierosion/svi.py:24 ball_cell_weights(radius, spacing, quad): half-width
+ * m = floor(r/h + 1/2) + 1, weights (2m+1)^3 float64 on the device. */
+int svie_ball_half_width(double radius, double spacing);
+int svie_ball_weights(double radius, double spacing, int quad, double* w, void* stream);
+
+/* BallConvolution (svierosion/svi.py:58-93).  The plan holds the FFT twiddle
+ * tables and the real, axis-even kernel spectrum K^ computed in float64 from
+ * the float64 weights and rounded to float32, stored for
+ * kx <= nx/2, ky <= ny/2, kz <= nz/2.  The workspace holds one complex64
+ * padded half spectrum nx*ny*svie_conv_spectrum_row(nz). */
+size_t svie_conv_plan_bytes(int nx, int ny, int nz);
+size_t svie_conv_workspace_bytes(int nx, int ny, int nz);
+int svie_conv_supported(int n);
+/* The float64 intermediates of the K^ sums use a temporary workspace of
+ * svie_conv_init_workspace_bytes() bytes. */
+size_t svie_conv_init_workspace_bytes(int nx, int ny, int nz, int m);
+int svie_conv_plan_init(void* plan, int nx, int ny, int nz, const double* w, int m, void* ws,
+                        size_t ws_bytes, void* stream);
+/* out = beta + alpha * (w (*) f) with unnormalised circular convolution:
+ * interior_volume uses alpha = h^3, beta = 0; exterior_fraction uses
+ * alpha = -h^3/|B_r|, beta = 1 (svi.py:84-93). */
+int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, float* out,
+                    double alpha, double beta, void* ws, size_t ws_bytes, void* stream);
+/* Row length (complex values) of the padded half spectrum used by the
+ * workspace and by svie_rfft3 / svie_irfft3: nz/2+1 rounded up to a multiple
+ * of 8, so every row starts on a 64-byte boundary.  The spectrum is
+ * [nx][ny][row]; entries kz >= nz/2+1 are padding. */
+int svie_conv_spectrum_row(int nz);
+/* Full complex64 half spectrum K^ (rfftn of the wrapped kernel, svi.py:76-81). */
+int svie_conv_kernel_hat(const void* plan, int nx, int ny, int nz, void* out_c64, void* stream);
+/* Forward rfftn (complex64 nx*ny*(nz/2+1)) and inverse irfftn with
+ * out = beta + alpha * irfftn_unnormalised(spec); spec is overwritten. */
+int svie_rfft3(const void* plan, int nx, int ny, int nz, const float* f, void* spec, void* stream);
+int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out, double alpha,
+                double beta, void* stream);
+
+/* ---------------------------------------------------- fused RK3 stages */
+/* ErosionSimulation._rhs for the SVI law (svierosion/evolve.py:118-160):
+ * closest point -> tricubic N -> speed law -> cutoff -> WENO5/Godunov ->
+ * L = V |grad phi|.  u0 (phi at the band, optional) and V (after cutoff,
+ * optional) are also written.  When stats is non-NULL the stage-0 statistics
+ * are accumulated (the struct must be cleared first with svie_stats_reset). */
+size_t svie_stage_workspace_bytes(int64_t m);
+int svie_stats_reset(svie_stats* stats, double dt_cap, void* stream);
+int svie_stage_svi(const float* phi, const int32_t* band, int64_t m, int nx, int ny, int nz,
+                   const float* N, const svie_law* law, float* L, float* u0, float* V,
+                   svie_stats* stats, void* ws, size_t ws_bytes, void* stream);
+/* Curvature laws: principal curvatures into an interleaved (k1, k2) dense
+ * field (zero off the band), then trilinear at closest points
+ * (evolve.py:137-151). */
+int svie_curvature_scatter(const float* phi, const int32_t* band, int64_t m, int nx, int ny, int nz,
+                           float h, float* kdense, void* stream);
+int svie_stage_curvature(const float* phi, const int32_t* band, int64_t m, int nx, int ny, int nz,
+                         const float* kdense, const svie_law* law, float* L, float* u0, float* V,
+                         svie_stats* stats, void* ws, size_t ws_bytes, void* stream);
+/* stable_dt (evolve.py:162-170) on the device: stats->dt. */
+int svie_stats_finalize(svie_stats* stats, const svie_law* law, const void* ws, size_t ws_bytes,
+                        int64_t m, void* stream);
+/* _rk3 stage updates (evolve.py:172-179); stage 1: phi = u0 + dt L;
+ * 2: phi = 3/4 u0 + 1/4 (phi + dt L); 3: phi = u0/3 + 2/3 (phi + dt L).
+ * dt is read from *dt on the device; nothing is written unless dt is finite
+ * and positive.  stage 0 restores phi[band] = u0. */
+int svie_rk_stage(float* phi, const int32_t* band, int64_t m, const float* u0, const float* L,
+                  const double* dt, int stage, void* stream);
+int svie_set_f64(double* dst, double value, void* stream);
+
+/* ------------------------------------------------------ reinitialisation */
+/* LevelSet.reinitialize (svierosion/levelset.py:154-183): work mask = band
+ * dilated by `dilation` cells with the `margin` outer layers cleared. */
+int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin,
+                     uint8_t* mask, uint8_t* tmp, void* stream);
+/* reinit_geometry (kernels.py:335-359) packed per node: 4 floats
+ * (sgn, dtau, flags, pad) + 6 floats (xp, xm per axis). */
+size_t svie_reinit_geometry_bytes(int64_t m);
+int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                         int64_t sz, float h, float cfl, void* geo, void* stream);
+/* `iterations` TVD-RK2 pseudo-time steps (levelset.py:178-182); phi_tmp is a
+ * dense grid used as the second buffer (it is overwritten). */
+int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* idx, int64_t m,
+                        int64_t sx, int64_t sy, int64_t sz, float h, const void* geo, int iterations,
+                        void* stream);
+/* kernels.reinit_rhs (kernels.py:363-379) for API parity. */
+int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz,
+                    float h, const void* geo, float* out, void* stream);
+/* Unpack geometry into the 14 arrays of kernels.reinit_geometry. */
+int svie_reinit_geometry_unpack(const void* geo, int64_t m, float* sgn, float* dtau, uint8_t* flags,
+                                float* dist6, void* stream);
+
+/* ------------------------------------------------------------------ SDF */
+/* mesh_to_sdf (svierosion/sdf.py:365-415).  tri: (T,3,3) float32 and tri64:
+ * (T,3,3) float64 triangle vertices in index coordinates (after
+ * split_long_triangles).  keys: dense int64 (dist bits << 32 | id),
+ * initialised to INT64_MAX by svie_sdf_keys_init. */
+int svie_sdf_keys_init(int64_t* keys, int64_t n, void* stream);
+/* _exact_near_field (sdf.py:100-145): nodes within exact_band cells of a
+ * triangle's bounding box, kept when dist <= eb_keep. */
+int svie_sdf_near_field(const float* tri, const double* tri64, int64_t ntri, int nx, int ny, int nz,
+                        double exact_band, float eb_keep, int64_t* keys, void* stream);
+/* keys -> dist (inf where empty), tid (-1 where empty), known mask */
+int svie_sdf_unpack(const int64_t* keys, int64_t n, float* dist, int32_t* tid, uint8_t* known,
+                    void* stream);
+/* _propagate (sdf.py:163-202), one ring: ring = dilate26(known) & ~known
+ * without the outer grid layer; update = best over the neighbours' closest
+ * triangles (new values into new_dist/new_tid); scatter writes them back and
+ * marks the nodes known. */
+int svie_sdf_ring_mask(const uint8_t* known, int nx, int ny, int nz, uint8_t* ring, void* stream);
+int svie_sdf_ring_update(const int32_t* upd, int64_t m, int nx, int ny, int nz, const float* tri,
+                         const float* dist, const int32_t* tid, float* new_dist, int32_t* new_tid,
+                         void* stream);
+int svie_sdf_scatter(const int32_t* upd, int64_t m, const float* new_dist, const int32_t* new_tid,
+                     float* dist, int32_t* tid, uint8_t* known, void* stream);
+/* mask = (dist > lo) & (dist <= hi)  (sdf.py:403) */
+int svie_sdf_outer_mask(const float* dist, int64_t n, float lo, float hi, uint8_t* mask, void* stream);
+/* _refine_with_stars, one pass (sdf.py:211-265); star CSR: first/deg per
+ * vertex, star = triangle ids grouped by vertex; vid (T,3); changed: device
+ * int64 counter (accumulated). */
+int svie_sdf_star_pass(const int32_t* nodes, int64_t m, int nx, int ny, int nz, const float* tri,
+                       const int32_t* vid, const int32_t* first, const int32_t* deg,
+                       const int32_t* star, float* dist, int32_t* tid, int64_t* changed,
+                       void* stream);
+/* _crossings_along_axis (sdf.py:285-340): acc int32 (n_axis+1) x n_b x n_c,
+ * zeroed by the caller, accumulates the crossings of the grid lines parallel
+ * to `axis`; svie_sdf_inside adds 1 to votes[x,y,z] where the prefix sum says
+ * inside (signed_rule = winding number, else parity). */
+int svie_sdf_crossings(const double* tri64, int64_t ntri, int nx, int ny, int nz, int axis,
+                       int signed_rule, int32_t* acc, void* stream);
+int svie_sdf_inside(const int32_t* acc, int nx, int ny, int nz, int axis, int signed_rule,
+                    uint8_t* votes, void* stream);
+/* phi = inside ? -(min(dist, band) * h) : +(...), inside = 2*votes > naxes
+ * (sdf.py:361, 409-410). */
+int svie_sdf_finalize(const float* dist, const uint8_t* votes, int64_t n, int naxes, float band,
+                      float h, float* phi, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVIE_H */

@@ -1,0 +1,282 @@
+// Narrow-band construction: order-preserving stream compaction.
+//
+// Replaces LevelSet.rebuild_band / _check_margin (reference
+// svierosion/levelset.py:70-86) and the torch.nonzero calls on dense masks
+// (levelset.py:173, evolve.py:100).  The output is the ascending list of flat
+// indices, bit-identical to torch.nonzero given the same phi.
+//
+// Layout: each CTA owns a tile of TILE = THREADS * IPT consecutive nodes and
+// each thread IPT consecutive nodes of it.  Pass 1 counts selected nodes per
+// CTA; a one-CTA scan turns the counts into offsets (workspace: one int32 per
+// CTA); pass 2 recomputes the predicate, scans the per-thread counts inside the
+// CTA and writes the indices in order.  Both passes read the grid once
+// (HBM-bound, 4 B/node each for phi).
+#include <limits.h>
+
+#include "common.cuh"
+
+namespace svie {
+
+constexpr int CMP_THREADS = 256;
+constexpr int CMP_IPT = 16;
+constexpr int CMP_TILE = CMP_THREADS * CMP_IPT;
+
+inline long long cmp_blocks(long long n) { return (n + CMP_TILE - 1) / CMP_TILE; }
+
+// Exclusive scan of one int per thread across the CTA; returns the prefix and
+// writes the CTA total to *total.
+SVIE_DEV int block_exclusive_scan(int v, int* sh, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < nw ? sh[lane] : 0;
+    int s = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < nw) sh[lane] = s - w;  // exclusive warp offsets
+    if (lane == nw - 1) sh[32] = s;
+  }
+  __syncthreads();
+  int r = sh[wid] + x - v;
+  *total = sh[32];
+  __syncthreads();
+  return r;
+}
+
+// ------------------------------------------------------------ predicates
+struct BandPred {
+  float* phi;
+  float cap, thresh;
+  bool clamp;
+  SVIE_DEV bool operator()(long long e) const {
+    float v = phi[e];
+    if (clamp) {
+      float c = fminf(fmaxf(v, -cap), cap);
+      if (c != v) phi[e] = c;  // torch clamp_ semantics (NaN stays NaN)
+      v = c;
+    }
+    return fabsf(v) < thresh;
+  }
+};
+
+struct MaskPred {
+  const uint8_t* mask;
+  SVIE_DEV bool operator()(long long e) const { return mask[e] != 0; }
+};
+
+template <class Pred>
+__global__ void __launch_bounds__(CMP_THREADS) k_count(Pred pred, long long n, int* counts) {
+  __shared__ int sh[CMP_THREADS / 32];
+  const long long t0 = (long long)blockIdx.x * CMP_TILE + (long long)threadIdx.x * CMP_IPT;
+  int c = 0;
+#pragma unroll 4
+  for (int j = 0; j < CMP_IPT; ++j) {
+    long long e = t0 + j;
+    if (e < n && pred(e)) ++c;
+  }
+  int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
+  if (threadIdx.x == 0) counts[blockIdx.x] = tot;
+}
+
+// Single-CTA exclusive scan of nb block counts in place; total -> *total64.
+__global__ void __launch_bounds__(1024) k_scan_counts(int* counts, long long nb, long long* total64) {
+  __shared__ int sh[33];
+  const long long per = (nb + blockDim.x - 1) / blockDim.x;
+  const long long s0 = (long long)threadIdx.x * per;
+  long long s1 = s0 + per;
+  if (s1 > nb) s1 = nb;
+  long long local = 0;
+  for (long long i = s0; i < s1; ++i) local += counts[i];
+  int tot;
+  int off = block_exclusive_scan((int)local, sh, &tot);
+  long long run = off;
+  for (long long i = s0; i < s1; ++i) {
+    int c = counts[i];
+    counts[i] = (int)run;
+    run += c;
+  }
+  if (threadIdx.x == 0) *total64 = tot;
+}
+
+template <class Pred>
+__global__ void __launch_bounds__(CMP_THREADS) k_write(Pred pred, long long n, const int* offsets,
+                                                       int32_t* out, long long capacity) {
+  __shared__ int sh[33];
+  const long long t0 = (long long)blockIdx.x * CMP_TILE + (long long)threadIdx.x * CMP_IPT;
+  unsigned int bits = 0;
+#pragma unroll 4
+  for (int j = 0; j < CMP_IPT; ++j) {
+    long long e = t0 + j;
+    if (e < n && pred(e)) bits |= 1u << j;
+  }
+  int tot;
+  long long o = (long long)offsets[blockIdx.x] + block_exclusive_scan(__popc(bits), sh, &tot);
+  while (bits) {
+    int j = __ffs(bits) - 1;
+    bits &= bits - 1;
+    if (o < capacity) out[o] = (int32_t)(t0 + j);
+    ++o;
+  }
+}
+
+// Band write pass: indices + dense occupancy + margin / static-count data.
+__global__ void __launch_bounds__(CMP_THREADS) k_band_write(const float* __restrict__ phi, int nx, int ny,
+                                                            int nz, float thresh, const int* offsets,
+                                                            int32_t* out, long long capacity,
+                                                            float* occ, svie_band_info* info) {
+  __shared__ int sh[33];
+  __shared__ long long shl[CMP_THREADS / 32];
+  __shared__ int shi[CMP_THREADS / 32];
+  const long long n = (long long)nx * ny * nz;
+  const long long syz = (long long)ny * nz;
+  const long long t0 = (long long)blockIdx.x * CMP_TILE + (long long)threadIdx.x * CMP_IPT;
+  unsigned int bits = 0;
+  int inside_static = 0;
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
+  int ilo[3] = {INT_MAX, INT_MAX, INT_MAX}, ihi[3] = {-1, -1, -1};
+  for (int j = 0; j < CMP_IPT; ++j) {
+    long long e = t0 + j;
+    if (e >= n) break;
+    float v = phi[e];
+    bool sel = fabsf(v) < thresh;
+    bool neg = v < 0.0f;
+    if (occ) occ[e] = neg ? 1.0f : 0.0f;
+    if (sel || neg) {
+      int c[3] = {(int)(e / syz), (int)((e / nz) % ny), (int)(e % nz)};
+      if (sel) {
+        bits |= 1u << j;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
+      }
+      if (neg) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { ilo[a] = min(ilo[a], c[a]); ihi[a] = max(ihi[a], c[a]); }
+        if (!sel) ++inside_static;
+      }
+    }
+  }
+  int tot;
+  long long o = (long long)offsets[blockIdx.x] + block_exclusive_scan(__popc(bits), sh, &tot);
+  while (bits) {
+    int j = __ffs(bits) - 1;
+    bits &= bits - 1;
+    if (o < capacity) out[o] = (int32_t)(t0 + j);
+    ++o;
+  }
+  long long st = block_reduce((long long)inside_static, shl, OpSumLL(), 0LL);
+  if (threadIdx.x == 0 && st) atomicAdd((unsigned long long*)&info->static_inside, (unsigned long long)st);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    int v;
+    v = block_reduce(lo[a], shi, OpMinI(), INT_MAX);
+    if (threadIdx.x == 0 && v != INT_MAX) atomicMin(&info->lo[a], v);
+    v = block_reduce(hi[a], shi, OpMaxI(), -1);
+    if (threadIdx.x == 0 && v >= 0) atomicMax(&info->hi[a], v);
+    v = block_reduce(ilo[a], shi, OpMinI(), INT_MAX);
+    if (threadIdx.x == 0 && v != INT_MAX) atomicMin(&info->ilo[a], v);
+    v = block_reduce(ihi[a], shi, OpMaxI(), -1);
+    if (threadIdx.x == 0 && v >= 0) atomicMax(&info->ihi[a], v);
+  }
+}
+
+__global__ void k_info_init(svie_band_info* info) {
+  info->static_inside = 0;
+  for (int a = 0; a < 3; ++a) {
+    info->lo[a] = INT_MAX;
+    info->hi[a] = -1;
+    info->ilo[a] = INT_MAX;
+    info->ihi[a] = -1;
+  }
+}
+
+}  // namespace svie
+
+using namespace svie;
+
+extern "C" {
+
+size_t svie_band_workspace_bytes(int64_t n) {
+  long long nb = cmp_blocks(n < 1 ? 1 : n);
+  return (size_t)(nb * sizeof(int) + 256);
+}
+
+int svie_band_scan(float* phi, int64_t n, float cap, float thresh, void* ws, size_t ws_bytes,
+                   svie_band_info* info, void* stream) {
+  if (!phi || !info || n <= 0 || n >= (1LL << 31)) {
+    set_error("svie_band_scan: bad arguments (n=%lld)", (long long)n);
+    return SVIE_ERR_ARG;
+  }
+  if (ws_bytes < svie_band_workspace_bytes(n) || !ws) {
+    set_error("svie_band_scan: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  long long nb = cmp_blocks(n);
+  BandPred p{phi, cap, thresh, true};
+  k_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(p, n, (int*)ws);
+  k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)&info->count);
+  k_info_init<<<1, 1, 0, s>>>(info);
+  return launch_status("svie_band_scan");
+}
+
+int svie_band_write(const float* phi, int nx, int ny, int nz, float thresh, const void* ws,
+                    size_t ws_bytes, int32_t* band, int64_t capacity, float* occ,
+                    svie_band_info* info, void* stream) {
+  long long n = (long long)nx * ny * nz;
+  if (!phi || !info || n <= 0 || n >= (1LL << 31) || (capacity > 0 && !band)) {
+    set_error("svie_band_write: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (ws_bytes < svie_band_workspace_bytes(n) || !ws) {
+    set_error("svie_band_write: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  long long nb = cmp_blocks(n);
+  k_band_write<<<(unsigned)nb, CMP_THREADS, 0, (cudaStream_t)stream>>>(
+      phi, nx, ny, nz, thresh, (const int*)ws, band, capacity, occ, info);
+  return launch_status("svie_band_write");
+}
+
+int svie_mask_scan(const uint8_t* mask, int64_t n, void* ws, size_t ws_bytes, int64_t* count,
+                   void* stream) {
+  if (!mask || !count || n <= 0 || n >= (1LL << 31)) {
+    set_error("svie_mask_scan: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (ws_bytes < svie_band_workspace_bytes(n) || !ws) {
+    set_error("svie_mask_scan: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  long long nb = cmp_blocks(n);
+  MaskPred p{mask};
+  k_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(p, n, (int*)ws);
+  k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)count);
+  return launch_status("svie_mask_scan");
+}
+
+int svie_mask_write(const uint8_t* mask, int64_t n, const void* ws, size_t ws_bytes, int32_t* out,
+                    int64_t capacity, void* stream) {
+  if (!mask || n <= 0 || n >= (1LL << 31) || (capacity > 0 && !out)) {
+    set_error("svie_mask_write: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (ws_bytes < svie_band_workspace_bytes(n) || !ws) {
+    set_error("svie_mask_write: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  long long nb = cmp_blocks(n);
+  MaskPred p{mask};
+  k_write<<<(unsigned)nb, CMP_THREADS, 0, (cudaStream_t)stream>>>(p, n, (const int*)ws, out, capacity);
+  return launch_status("svie_mask_write");
+}
+
+}  // extern "C"

@@ -1,0 +1,301 @@
+// Shared device helpers for the narrow-band level-set erosion kernels.
+//
+// Conventions (the same as the reference's kernels, svierosion/kernels.py:11-13):
+//   * phi is a dense float32 grid in C order with axes (x, y, z); strides (ny*nz, nz, 1);
+//   * band / node lists are sorted int32 flat indices (grids have < 2^31 nodes);
+//   * points are in index (cell) coordinates.
+// Every entry point returns an int status (0 = ok) and never allocates: scratch
+// memory comes from a caller-provided workspace whose size a *_workspace_bytes()
+// query reports.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#include "../../include/svie.h"
+
+#define SVIE_DEV __device__ __forceinline__
+
+namespace svie {
+
+// Records a message for svie_last_error(); defined in capi.cu.
+void set_error(const char* fmt, ...);
+
+// Status from the most recent launch on the calling thread.
+inline int launch_status(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("%s: launch failed: %s", what, cudaGetErrorString(e));
+    return SVIE_ERR_LAUNCH;
+  }
+  return SVIE_OK;
+}
+
+inline int blocks_for(long long n, int threads, long long cap = 1LL << 30) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (int)b;
+}
+
+// -------------------------------------------------------------- float keys
+// Monotone map float -> uint32 so that unsigned atomicMin/Max order floats.
+SVIE_DEV unsigned int float_to_ordered(float f) {
+  unsigned int u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+SVIE_DEV float ordered_to_float(unsigned int u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// ------------------------------------------------------- warp reductions
+SVIE_DEV float warp_max(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+SVIE_DEV float warp_min(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+SVIE_DEV double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+SVIE_DEV unsigned int warp_sum_u(unsigned int v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+SVIE_DEV int warp_min_i(int v) {
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+SVIE_DEV int warp_max_i(int v) {
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide reduction through shared memory; every thread gets the result.
+// `scratch` needs blockDim.x/32 entries; the block size is a multiple of 32.
+template <typename T, typename Op>
+SVIE_DEV T block_reduce(T v, T* scratch, Op op, T identity) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  T r = identity;
+  for (int i = 0; i < nw; ++i) r = op(r, scratch[i]);
+  return r;
+}
+
+struct OpMaxF { SVIE_DEV float operator()(float a, float b) const { return fmaxf(a, b); } };
+struct OpMinF { SVIE_DEV float operator()(float a, float b) const { return fminf(a, b); } };
+struct OpSumD { SVIE_DEV double operator()(double a, double b) const { return a + b; } };
+struct OpSumU { SVIE_DEV unsigned int operator()(unsigned int a, unsigned int b) const { return a + b; } };
+struct OpSumLL { SVIE_DEV long long operator()(long long a, long long b) const { return a + b; } };
+struct OpMinI { SVIE_DEV int operator()(int a, int b) const { return min(a, b); } };
+struct OpMaxI { SVIE_DEV int operator()(int a, int b) const { return max(a, b); } };
+
+// ----------------------------------------------------------- stencil maths
+// Jiang-Peng WENO5 derivative from five differences (reference kernels.py:83-97).
+SVIE_DEV float weno5(float v1, float v2, float v3, float v4, float v5) {
+  const float c1312 = (float)(13.0 / 12.0);
+  float p1 = v1 / 3.0f - 7.0f * v2 / 6.0f + 11.0f * v3 / 6.0f;
+  float p2 = -v2 / 6.0f + 5.0f * v3 / 6.0f + v4 / 3.0f;
+  float p3 = v3 / 3.0f + 5.0f * v4 / 6.0f - v5 / 6.0f;
+  float e1 = v1 - 2.0f * v2 + v3, f1 = v1 - 4.0f * v2 + 3.0f * v3;
+  float e2 = v2 - 2.0f * v3 + v4, f2 = v2 - v4;
+  float e3 = v3 - 2.0f * v4 + v5, f3 = 3.0f * v3 - 4.0f * v4 + v5;
+  float s1 = c1312 * (e1 * e1) + 0.25f * (f1 * f1);
+  float s2 = c1312 * (e2 * e2) + 0.25f * (f2 * f2);
+  float s3 = c1312 * (e3 * e3) + 0.25f * (f3 * f3);
+  float vmax = fmaxf(fmaxf(fmaxf(v1 * v1, v2 * v2), fmaxf(v3 * v3, v4 * v4)), v5 * v5);
+  float eps = 1e-6f * vmax + 1e-10f;
+  float d1 = s1 + eps, d2 = s2 + eps, d3 = s3 + eps;
+  float a1 = 0.1f / (d1 * d1);
+  float a2 = 0.6f / (d2 * d2);
+  float a3 = 0.3f / (d3 * d3);
+  return (a1 * p1 + a2 * p2 + a3 * p3) / (a1 + a2 + a3);
+}
+
+// Godunov |grad phi| for inward motion at flat node i (reference kernels.py:146-169).
+SVIE_DEV float godunov_at(const float* __restrict__ f, long long i, long long sx, long long sy,
+                          long long sz, float inv_h) {
+  const float c = __ldg(f + i);
+  float g2 = 0.0f;
+  const long long st[3] = {sx, sy, sz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const long long s = st[a];
+    float m3 = __ldg(f + i - 3 * s), m2 = __ldg(f + i - 2 * s), m1 = __ldg(f + i - s);
+    float p1 = __ldg(f + i + s), p2 = __ldg(f + i + 2 * s), p3 = __ldg(f + i + 3 * s);
+    float d0 = (m2 - m3) * inv_h, d1 = (m1 - m2) * inv_h, d2 = (c - m1) * inv_h;
+    float d3 = (p1 - c) * inv_h, d4 = (p2 - p1) * inv_h, d5 = (p3 - p2) * inv_h;
+    float dm = weno5(d0, d1, d2, d3, d4);
+    float dp = weno5(d5, d4, d3, d2, d1);
+    float lo = fminf(dm, 0.0f), hi = fmaxf(dp, 0.0f);
+    g2 = g2 + fmaxf(lo * lo, hi * hi);
+  }
+  return sqrtf(g2);
+}
+
+// Volume fraction of the unit cube below a plane (reference kernels.py:104-122):
+// s = signed distance in cells, a >= b >= c >= 0 the sorted |normal| components.
+SVIE_DEV float cube_plane_fraction(float s, float a, float b, float c) {
+  float M = 0.5f * (a + b + c);
+  float y = M - s;
+  bool flip = y > M;
+  y = flip ? 2.0f * M - y : y;
+  y = fmaxf(y, 0.0f);
+  const float tiny = 1e-12f;
+  float bs = fmaxf(b, tiny), cs = fmaxf(c, tiny);
+  float q = 3.0f * y * y - 3.0f * y * c + c * c;
+  float H;
+  if (y <= c) {
+    H = (y * y * y) / (bs * cs);
+  } else if (y <= b) {
+    H = q / bs;
+  } else if (y <= b + c) {
+    float u = fmaxf(y - b, 0.0f);
+    H = (q - (u * u * u) / cs) / bs;
+  } else {
+    H = 3.0f * (2.0f * y - b - c);
+  }
+  float ua = fmaxf(y - a, 0.0f);
+  float F = H / (6.0f * a) - (ua * ua * ua) / (6.0f * a * bs * cs);
+  F = flip ? 1.0f - F : F;
+  return fminf(fmaxf(F, 0.0f), 1.0f);
+}
+
+// Tangent-plane cell fraction at node i (reference kernels.py:173-181).
+SVIE_DEV float cell_fraction_at(const float* __restrict__ f, long long i, long long sx, long long sy,
+                                long long sz) {
+  float c = __ldg(f + i);
+  float gx = 0.5f * (__ldg(f + i + sx) - __ldg(f + i - sx));
+  float gy = 0.5f * (__ldg(f + i + sy) - __ldg(f + i - sy));
+  float gz = 0.5f * (__ldg(f + i + sz) - __ldg(f + i - sz));
+  float gn = fmaxf(sqrtf(gx * gx + gy * gy + gz * gz), 1e-30f);
+  float x = fabsf(gx / gn), y = fabsf(gy / gn), z = fabsf(gz / gn);
+  float hi = fmaxf(fmaxf(x, y), z);
+  float lo = fminf(fminf(x, y), z);
+  float mid = x + y + z - hi - lo;
+  return cube_plane_fraction(c / gn, hi, mid, lo);
+}
+
+// First Newton projection to the zero set (reference kernels.py:185-208).
+// hi = (nx-3.001, ny-3.001, nz-3.001) rounded to float.
+SVIE_DEV float3 closest_point_at(const float* __restrict__ f, long long i, int ny, int nz, float hx,
+                                 float hy, float hz, float h) {
+  const long long sx = (long long)ny * nz, sy = nz;
+  float c = __ldg(f + i);
+  float gx = 0.5f * (__ldg(f + i + sx) - __ldg(f + i - sx));
+  float gy = 0.5f * (__ldg(f + i + sy) - __ldg(f + i - sy));
+  float gz = 0.5f * (__ldg(f + i + 1) - __ldg(f + i - 1));
+  float g2 = fmaxf(gx * gx + gy * gy + gz * gz, 1e-30f);
+  float ac = fabsf(c);
+  float length = ac / sqrtf(g2);
+  float cap = 1.25f * ac / h + 0.25f;
+  float scale = (c / g2) * fminf(cap / fmaxf(length, 1e-30f), 1.0f);
+  float fi = (float)(i / sx);
+  float fj = (float)((i / sy) % ny);
+  float fk = (float)(i % nz);
+  float3 p;
+  p.x = fminf(fmaxf(fi - scale * gx, 1.0f), hx);
+  p.y = fminf(fmaxf(fj - scale * gy, 1.0f), hy);
+  p.z = fminf(fmaxf(fk - scale * gz, 1.0f), hz);
+  return p;
+}
+
+// Cubic Lagrange weights on nodes -1, 0, 1, 2 (reference kernels.py:134-136).
+SVIE_DEV void cubic_w(float t, float w[4]) {
+  w[0] = -t * (t - 1.0f) * (t - 2.0f) / 6.0f;
+  w[1] = (t + 1.0f) * (t - 1.0f) * (t - 2.0f) / 2.0f;
+  w[2] = -(t + 1.0f) * t * (t - 2.0f) / 2.0f;
+  w[3] = (t + 1.0f) * t * (t - 1.0f) / 6.0f;
+}
+// Their derivatives (reference kernels.py:139-141).
+SVIE_DEV void cubic_dw(float t, float w[4]) {
+  w[0] = -(3.0f * t * t - 6.0f * t + 2.0f) / 6.0f;
+  w[1] = (3.0f * t * t - 4.0f * t - 1.0f) / 2.0f;
+  w[2] = -(3.0f * t * t - 2.0f * t - 2.0f) / 2.0f;
+  w[3] = (3.0f * t * t - 1.0f) / 6.0f;
+}
+
+// Tricubic interpolation at index coordinates p (reference kernels.py:212-228).
+SVIE_DEV float tricubic_at(const float* __restrict__ g, int ny, int nz, float3 p) {
+  float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
+  float wx[4], wy[4], wz[4];
+  cubic_w(p.x - fx, wx);
+  cubic_w(p.y - fy, wy);
+  cubic_w(p.z - fz, wz);
+  const long long syz = (long long)ny * nz;
+  const long long b0 = ((long long)fx - 1) * syz + ((long long)fy - 1) * nz + ((long long)fz - 1);
+  float out = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const float wab = wx[a] * wy[b];
+      const float* row = g + b0 + a * syz + b * nz;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) out = out + (wab * wz[c]) * __ldg(row + c);
+    }
+  }
+  return out;
+}
+
+// Trilinear interpolation (reference kernels.py:257-270); `comp` selects a
+// component of an interleaved field with `ncomp` floats per node.
+SVIE_DEV float trilinear_at(const float* __restrict__ g, int ny, int nz, float3 p, int ncomp, int comp) {
+  float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
+  float tx = p.x - fx, ty = p.y - fy, tz = p.z - fz;
+  const long long syz = (long long)ny * nz;
+  const long long b0 = (long long)fx * syz + (long long)fy * nz + (long long)fz;
+  float out = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    float wa = a ? tx : 1.0f - tx;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      float wb = wa * (b ? ty : 1.0f - ty);
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        long long o = b0 + a * syz + b * nz + c;
+        out = out + wb * (c ? tz : 1.0f - tz) * __ldg(g + o * ncomp + comp);
+      }
+    }
+  }
+  return out;
+}
+
+// Principal curvatures k1 >= k2 of the level sets at node i (reference kernels.py:274-299).
+SVIE_DEV float2 principal_curvatures_at(const float* __restrict__ f, long long i, long long sx,
+                                        long long sy, long long sz, float h) {
+  float c = __ldg(f + i);
+  float xp = __ldg(f + i + sx), xm = __ldg(f + i - sx);
+  float yp = __ldg(f + i + sy), ym = __ldg(f + i - sy);
+  float zp = __ldg(f + i + sz), zm = __ldg(f + i - sz);
+  float h2 = 2.0f * h, hh = h * h, h4 = 4.0f * h * h;
+  float px = (xp - xm) / h2, py = (yp - ym) / h2, pz = (zp - zm) / h2;
+  float pxx = (xp - 2.0f * c + xm) / hh;
+  float pyy = (yp - 2.0f * c + ym) / hh;
+  float pzz = (zp - 2.0f * c + zm) / hh;
+  auto mixed = [&](long long a, long long b) {
+    return (__ldg(f + i + a + b) - __ldg(f + i + a - b) - __ldg(f + i - a + b) + __ldg(f + i - a - b)) / h4;
+  };
+  float pxy = mixed(sx, sy), pxz = mixed(sx, sz), pyz = mixed(sy, sz);
+  float g2 = fmaxf(px * px + py * py + pz * pz, 1e-30f);
+  float gn = sqrtf(g2);
+  float ksum = ((pyy + pzz) * px * px + (pxx + pzz) * py * py + (pxx + pyy) * pz * pz -
+                2.0f * (px * py * pxy + px * pz * pxz + py * pz * pyz)) / (g2 * gn);
+  float K = (px * px * (pyy * pzz - pyz * pyz) + py * py * (pxx * pzz - pxz * pxz) +
+             pz * pz * (pxx * pyy - pxy * pxy) + 2.0f * px * py * (pxz * pyz - pxy * pzz) +
+             2.0f * py * pz * (pxy * pxz - pyz * pxx) + 2.0f * px * pz * (pxy * pyz - pxz * pyy)) /
+            (g2 * g2);
+  float H = 0.5f * ksum;
+  float r = sqrtf(fmaxf(H * H - K, 0.0f));
+  return make_float2(H + r, H - r);
+}
+
+}  // namespace svie

@@ -1,0 +1,731 @@
+// Ball-convolution evaluation of N_r (reference svierosion/svi.py:24-93).
+//
+// The grid sizes are 2^a 3^b 5^c 7^d (Grid.around rounds up to them,
+// svierosion/grid.py:18-28), so every axis FFT is a mixed-radix Stockham
+// transform with radices 8, 7, 6, 5, 4, 3, 2 computed on lines staged in shared
+// memory.  The 3-D real transform runs as five HBM passes over the complex64
+// half spectrum S[x][y][kz] (kz = 0..nz/2, the rfftn layout):
+//
+//   1. z  R2C: two real lines packed into one complex line per FFT;
+//   2. y  C2C forward on [ny x W] tiles of consecutive kz;
+//   3. x  C2C forward, multiply by the real kernel spectrum K^, C2C inverse, all
+//      while the lines are in shared memory;
+//   4. y  C2C inverse;
+//   5. z  C2R with the epilogue out = beta + alpha * value fused in.
+//
+// The ball weights w are even in each axis, so K^ is real and even in each
+// frequency; it is computed once in float64 directly from w (three separable
+// cosine sums) and stored for kx <= nx/2, ky <= ny/2, kz <= nz/2 only.
+// Inverse transforms use conj(FFT(conj(x))).  All arithmetic is float32 with
+// float64-accurate twiddle tables.
+#include <math.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace svie {
+
+constexpr int FFT_T = 256;      // threads per CTA
+constexpr int FFT_MAXST = 14;   // radix stages per axis
+constexpr int FFT_MAXN = 8192;  // longest supported axis
+
+struct AxisPlan {
+  int n;
+  int nst;
+  int radix[FFT_MAXST];
+  const float2* tw;  // tw[k] = exp(-2 pi i k / n), k < n
+};
+
+static bool factor_axis(int n, AxisPlan* p) {
+  if (n < 1 || n > FFT_MAXN) return false;
+  static const int rs[] = {8, 7, 6, 5, 4, 3, 2};
+  int m = n, st = 0;
+  for (int r : rs) {
+    while (m % r == 0) {
+      if (st >= FFT_MAXST) return false;
+      p->radix[st++] = r;
+      m /= r;
+    }
+  }
+  if (m != 1) return false;
+  p->n = n;
+  p->nst = st;
+  return true;
+}
+
+SVIE_DEV float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+SVIE_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+SVIE_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+SVIE_DEV float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+SVIE_DEV float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // -i * a
+
+// cos / sin of 2 pi t / R for the odd radices (values of the trigonometric
+// functions at rational multiples of pi, to float precision).
+__constant__ float c_cos3[3] = {1.0f, -0.5f, -0.5f};
+__constant__ float c_sin3[3] = {0.0f, 0.86602540378443865f, -0.86602540378443865f};
+__constant__ float c_cos5[5] = {1.0f, 0.30901699437494742f, -0.80901699437494742f, -0.80901699437494742f,
+                                0.30901699437494742f};
+__constant__ float c_sin5[5] = {0.0f, 0.95105651629515357f, 0.58778525229247313f, -0.58778525229247313f,
+                                -0.95105651629515357f};
+__constant__ float c_cos7[7] = {1.0f, 0.62348980185873353f, -0.22252093395631440f, -0.90096886790241913f,
+                                -0.90096886790241913f, -0.22252093395631440f, 0.62348980185873353f};
+__constant__ float c_sin7[7] = {0.0f, 0.78183148246802981f, 0.97492791218182361f, 0.43388373911755812f,
+                                -0.43388373911755812f, -0.97492791218182361f, -0.78183148246802981f};
+__constant__ float c_cos6[6] = {1.0f, 0.5f, -0.5f, -1.0f, -0.5f, 0.5f};
+__constant__ float c_sin6[6] = {0.0f, 0.86602540378443865f, 0.86602540378443865f, 0.0f,
+                                -0.86602540378443865f, -0.86602540378443865f};
+
+// Forward DFT of R points in place: y_p = sum_q x_q exp(-2 pi i p q / R).
+template <int R>
+SVIE_DEV void dft(float2* x);
+
+template <>
+SVIE_DEV void dft<2>(float2* x) {
+  float2 a = x[0], b = x[1];
+  x[0] = cadd(a, b);
+  x[1] = csub(a, b);
+}
+
+template <>
+SVIE_DEV void dft<4>(float2* x) {
+  float2 t0 = cadd(x[0], x[2]), t1 = csub(x[0], x[2]);
+  float2 t2 = cadd(x[1], x[3]), t3 = csub(x[1], x[3]);
+  x[0] = cadd(t0, t2);
+  x[2] = csub(t0, t2);
+  x[1] = cadd(t1, mul_mi(t3));
+  x[3] = csub(t1, mul_mi(t3));
+}
+
+template <>
+SVIE_DEV void dft<8>(float2* x) {
+  float2 e[4] = {x[0], x[2], x[4], x[6]};
+  float2 o[4] = {x[1], x[3], x[5], x[7]};
+  dft<4>(e);
+  dft<4>(o);
+  const float r = 0.70710678118654752f;
+  float2 w1 = make_float2(r * (o[1].x + o[1].y), r * (o[1].y - o[1].x));    // o1 * (r - ir)
+  float2 w2 = mul_mi(o[2]);                                                  // o2 * (-i)
+  float2 w3 = make_float2(r * (o[3].y - o[3].x), -r * (o[3].x + o[3].y));   // o3 * (-r - ir)
+  x[0] = cadd(e[0], o[0]);
+  x[4] = csub(e[0], o[0]);
+  x[1] = cadd(e[1], w1);
+  x[5] = csub(e[1], w1);
+  x[2] = cadd(e[2], w2);
+  x[6] = csub(e[2], w2);
+  x[3] = cadd(e[3], w3);
+  x[7] = csub(e[3], w3);
+}
+
+// Odd radix with the symmetric pairing of q and R-q.
+template <int R>
+SVIE_DEV void dft_odd(float2* x, const float* C, const float* S) {
+  constexpr int H = (R - 1) / 2;
+  float2 a[H], b[H];
+#pragma unroll
+  for (int q = 1; q <= H; ++q) {
+    a[q - 1] = cadd(x[q], x[R - q]);
+    b[q - 1] = csub(x[q], x[R - q]);
+  }
+  float2 x0 = x[0];
+  float2 y0 = x0;
+#pragma unroll
+  for (int q = 0; q < H; ++q) y0 = cadd(y0, a[q]);
+#pragma unroll
+  for (int p = 1; p <= H; ++p) {
+    float2 re = x0, im = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 1; q <= H; ++q) {
+      const int t = (p * q) % R;
+      re.x += a[q - 1].x * C[t];
+      re.y += a[q - 1].y * C[t];
+      im.x += b[q - 1].x * S[t];
+      im.y += b[q - 1].y * S[t];
+    }
+    // y_p = re - i*im ; y_{R-p} = re + i*im
+    x[p] = make_float2(re.x + im.y, re.y - im.x);
+    x[R - p] = make_float2(re.x - im.y, re.y + im.x);
+  }
+  x[0] = y0;
+}
+
+template <>
+SVIE_DEV void dft<3>(float2* x) { dft_odd<3>(x, c_cos3, c_sin3); }
+template <>
+SVIE_DEV void dft<5>(float2* x) { dft_odd<5>(x, c_cos5, c_sin5); }
+template <>
+SVIE_DEV void dft<7>(float2* x) { dft_odd<7>(x, c_cos7, c_sin7); }
+
+template <>
+SVIE_DEV void dft<6>(float2* x) {
+  float2 y[6];
+#pragma unroll
+  for (int p = 0; p < 6; ++p) {
+    float2 acc = x[0];
+#pragma unroll
+    for (int q = 1; q < 6; ++q) {
+      const int t = (p * q) % 6;
+      const float c = c_cos6[t], s = c_sin6[t];
+      acc.x += x[q].x * c + x[q].y * s;
+      acc.y += x[q].y * c - x[q].x * s;
+    }
+    y[p] = acc;
+  }
+#pragma unroll
+  for (int p = 0; p < 6; ++p) x[p] = y[p];
+}
+
+// One Stockham radix-R stage over `nlines` lines of length n, reading
+// src[line*LS + k] and writing dst (ping-pong buffers, so a thread holds one
+// butterfly at a time).  p = product of the radices already applied.
+template <int R>
+SVIE_DEV void fft_stage(const float2* __restrict__ src, float2* __restrict__ dst, int LS, int n, int nlines, int p,
+                        const float2* __restrict__ tw) {
+  const int m = n / R;
+  const int total = m * nlines;
+  const int twstep = n / (p * R);
+  for (int b = threadIdx.x; b < total; b += FFT_T) {
+    const int line = b / m, i = b - line * m;
+    const int k = i % p;
+    float2 v[R];
+    const float2* s = src + line * LS + i;
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = s[q * m];
+    if (k) {
+#pragma unroll
+      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], __ldg(tw + q * k * twstep));
+    }
+    dft<R>(v);
+    float2* d = dst + line * LS + (i - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) d[q * p] = v[q];
+  }
+  __syncthreads();
+}
+
+// Runs all stages; the data starts in a and the result pointer is returned
+// (a or b).
+SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPlan& P) {
+  int p = 1;
+  for (int st = 0; st < P.nst; ++st) {
+    const int R = P.radix[st];
+    switch (R) {
+      case 8: fft_stage<8>(a, b, LS, P.n, nlines, p, P.tw); break;
+      case 7: fft_stage<7>(a, b, LS, P.n, nlines, p, P.tw); break;
+      case 6: fft_stage<6>(a, b, LS, P.n, nlines, p, P.tw); break;
+      case 5: fft_stage<5>(a, b, LS, P.n, nlines, p, P.tw); break;
+      case 4: fft_stage<4>(a, b, LS, P.n, nlines, p, P.tw); break;
+      case 3: fft_stage<3>(a, b, LS, P.n, nlines, p, P.tw); break;
+      default: fft_stage<2>(a, b, LS, P.n, nlines, p, P.tw); break;
+    }
+    float2* t = a; a = b; b = t;
+    p *= R;
+  }
+  return a;
+}
+
+__host__ __device__ inline int line_stride(int n) { return (n & 1) ? n : n + 1; }  // odd -> conflict-free columns
+__host__ __device__ inline int padded_nzh(int nz) { return ((nz / 2 + 1) + 7) & ~7; }  // 64-byte rows
+
+// ----------------------------------------------------------------- z passes
+// Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
+__global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ in, float2* __restrict__ out,
+                                                     AxisPlan P, long long nlines, int W, int nzp) {
+  extern __shared__ float2 sm[];
+  const int n = P.n, LS = line_stride(n), nh = n / 2 + 1;
+  float2* sa = sm;
+  float2* sb = sm + W * LS;
+  const long long line0 = (long long)blockIdx.x * 2 * W;
+  const int nl = (int)min((long long)2 * W, nlines - line0);
+  const int np = (nl + 1) >> 1;
+  const float* src = in + line0 * n;
+  float* smf = reinterpret_cast<float*>(sa);
+  for (int e = threadIdx.x; e < np * 2 * n; e += FFT_T) {
+    const int l = e / n, z = e - l * n;
+    smf[2 * ((l >> 1) * LS + z) + (l & 1)] = (l < nl) ? __ldg(src + e) : 0.0f;
+  }
+  __syncthreads();
+  const float2* r = run_fft(sa, sb, LS, np, P);
+  float2* dst = out + line0 * nzp;
+  for (int e = threadIdx.x; e < nl * nh; e += FFT_T) {
+    const int l = e / nh, k = e - l * nh;
+    const int w = l >> 1;
+    const float2 a = r[w * LS + k];
+    const float2 b = r[w * LS + (k == 0 ? 0 : n - k)];
+    float2 v;
+    if ((l & 1) == 0) v = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+    else v = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
+    dst[(long long)l * nzp + k] = v;
+  }
+}
+
+// Inverse: half spectra -> real lines, out = beta + alpha * irfft_unnormalised.
+__global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ in, float* __restrict__ out,
+                                                     AxisPlan P, long long nlines, int W, int nzp, float alpha,
+                                                     float beta) {
+  extern __shared__ float2 sm[];
+  const int n = P.n, LS = line_stride(n);
+  float2* sa = sm;
+  float2* sb = sm + W * LS;
+  const long long line0 = (long long)blockIdx.x * 2 * W;
+  const int nl = (int)min((long long)2 * W, nlines - line0);
+  const int np = (nl + 1) >> 1;
+  const float2* src = in + line0 * nzp;
+  const bool even = (n & 1) == 0;
+  for (int e = threadIdx.x; e < np * n; e += FFT_T) {
+    const int w = e / n, k = e - w * n;
+    const bool mirror = k > n / 2;
+    const int kk = mirror ? n - k : k;
+    float2 x1 = make_float2(0.f, 0.f), x2 = make_float2(0.f, 0.f);
+    if (2 * w < nl) x1 = __ldg(src + (long long)(2 * w) * nzp + kk);
+    if (2 * w + 1 < nl) x2 = __ldg(src + (long long)(2 * w + 1) * nzp + kk);
+    if (kk == 0 || (even && kk == n / 2)) { x1.y = 0.f; x2.y = 0.f; }
+    if (mirror) { x1.y = -x1.y; x2.y = -x2.y; }
+    // C = X1 + i X2, stored conjugated for the inverse-by-forward transform
+    sa[w * LS + k] = make_float2(x1.x - x2.y, -(x1.y + x2.x));
+  }
+  __syncthreads();
+  const float2* r = run_fft(sa, sb, LS, np, P);
+  float* dst = out + line0 * n;
+  for (int e = threadIdx.x; e < nl * n; e += FFT_T) {
+    const int l = e / n, z = e - l * n;
+    const float2 v = r[(l >> 1) * LS + z];
+    dst[e] = beta + alpha * ((l & 1) ? -v.y : v.x);
+  }
+}
+
+// ------------------------------------------------------------ strided passes
+// Lines along an axis with element stride `stride`; a CTA takes W consecutive
+// lines (contiguous in memory) of one outer slab: base = data +
+// blockIdx.y * outer_stride + blockIdx.x * W.  mode 0 = forward, 1 = inverse,
+// 2 = forward * K^ then inverse (x axis only; the outer index is y and the
+// line index kz).
+struct KGeom {
+  const float* kred;  // [(nx/2+1)][(ny/2+1)][nzh]
+  int ny, nzh;
+};
+
+__global__ void __launch_bounds__(FFT_T) k_fft_strided(float2* __restrict__ data, AxisPlan P, long long stride,
+                                                       int ninner, long long outer_stride, int W, int mode, KGeom K) {
+  extern __shared__ float2 sm[];
+  const int n = P.n, LS = line_stride(n);
+  float2* sa = sm;
+  float2* sb = sm + W * LS;
+  const int c0 = blockIdx.x * W;
+  const int nl = min(W, ninner - c0);
+  float2* base = data + (long long)blockIdx.y * outer_stride + c0;
+  const bool conj_in = (mode == 1);
+  for (int e = threadIdx.x; e < n * nl; e += FFT_T) {
+    const int k = e / nl, c = e - k * nl;
+    float2 v = base[(long long)k * stride + c];
+    if (conj_in) v.y = -v.y;
+    sa[c * LS + k] = v;
+  }
+  __syncthreads();
+  float2* r = run_fft(sa, sb, LS, nl, P);
+  if (mode == 2) {
+    const int nyh = K.ny / 2 + 1;
+    const int y = blockIdx.y, yr = min(y, K.ny - y);
+    for (int e = threadIdx.x; e < n * nl; e += FFT_T) {
+      const int k = e / nl, c = e - k * nl;
+      const int kr = min(k, n - k);
+      const float kv = __ldg(K.kred + ((long long)kr * nyh + yr) * K.nzh + (c0 + c));
+      const float2 v = r[c * LS + k];
+      r[c * LS + k] = make_float2(v.x * kv, -(v.y * kv));  // conj for the inverse
+    }
+    __syncthreads();
+    float2* other = (r == sa) ? sb : sa;
+    r = run_fft(r, other, LS, nl, P);
+  }
+  const bool conj_out = (mode != 0);
+  for (int e = threadIdx.x; e < n * nl; e += FFT_T) {
+    const int k = e / nl, c = e - k * nl;
+    float2 v = r[c * LS + k];
+    if (conj_out) v.y = -v.y;
+    base[(long long)k * stride + c] = v;
+  }
+}
+
+// ------------------------------------------------------ plan construction
+__global__ void k_twiddles(float2* tw, int n) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double s, c;
+  sincospi(2.0 * (double)k / (double)n, &s, &c);
+  tw[k] = make_float2((float)c, (float)(-s));
+}
+
+struct GL32 {
+  double x[64], w[64];
+};
+
+// Ball/cell overlap fractions (reference svi.py:24-55) in float64.
+__global__ void k_ball_weights(double R, int m, int quad, GL32 gl, double* __restrict__ w) {
+  const int side = 2 * m + 1;
+  const long long tot = (long long)side * side * side;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tot) return;
+  const int i = (int)(t / ((long long)side * side)) - m;
+  const int j = (int)((t / side) % side) - m;
+  const int k = (int)(t % side) - m;
+  const double ci = i, cj = j, ck = k;
+  auto nr = [](double c) { double v = fabs(c) - 0.5; return v > 0 ? v : 0.0; };
+  double a0 = nr(ci), a1 = nr(cj), a2 = nr(ck);
+  double near = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+  double b0 = fabs(ci) + 0.5, b1 = fabs(cj) + 0.5, b2 = fabs(ck) + 0.5;
+  double far = sqrt(b0 * b0 + b1 * b1 + b2 * b2);
+  double v = 0.0;
+  if (far <= R) {
+    v = 1.0;
+  } else if (near < R && far > R) {
+    const double lo = ck - 0.5, hi = ck + 0.5;
+    double acc = 0.0;
+    for (int a = 0; a < quad; ++a) {
+      const double X = ci + gl.x[a];
+      double row = 0.0;
+      for (int b = 0; b < quad; ++b) {
+        const double Y = cj + gl.x[b];
+        double r2 = R * R - X * X - Y * Y;
+        double zr = sqrt(r2 > 0 ? r2 : 0.0);
+        double L = fmin(hi, zr) - fmax(lo, -zr);
+        if (L < 0) L = 0;
+        row += L * gl.w[b];
+      }
+      acc += row * gl.w[a];
+    }
+    v = acc;
+  }
+  w[t] = v;
+}
+
+// K^ step A: A[(i,j)][kz] = sum_k w[i][j][k] cos(2 pi kz k / nz), i, j in [-m, m].
+__global__ void k_khat_a(const double* __restrict__ w, int m, int nz, int nzh, double* __restrict__ A) {
+  extern __shared__ double ctab[];
+  for (int t = threadIdx.x; t < nz; t += blockDim.x) ctab[t] = cospi(2.0 * t / nz);
+  __syncthreads();
+  const int side = 2 * m + 1;
+  const long long tot = (long long)side * side * nzh;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+    const long long ij = t / nzh;
+    const int kz = (int)(t - ij * nzh);
+    const double* row = w + ij * side;
+    double acc = 0.0;
+    for (int k = -m; k <= m; ++k) {
+      long long ph = ((long long)kz * k) % nz;
+      if (ph < 0) ph += nz;
+      acc += row[k + m] * ctab[ph];
+    }
+    A[t] = acc;
+  }
+}
+
+// step B: Bq[i][ky][kz] = sum_j A[i][j][kz] cos(2 pi ky j / ny), ky <= ny/2.
+__global__ void k_khat_b(const double* __restrict__ A, int m, int ny, int nzh, double* __restrict__ Bq) {
+  extern __shared__ double ctab[];
+  for (int t = threadIdx.x; t < ny; t += blockDim.x) ctab[t] = cospi(2.0 * t / ny);
+  __syncthreads();
+  const int side = 2 * m + 1, nyh = ny / 2 + 1;
+  const long long tot = (long long)side * nyh * nzh;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+    const int kz = (int)(t % nzh);
+    const int ky = (int)((t / nzh) % nyh);
+    const int i = (int)(t / ((long long)nzh * nyh));
+    double acc = 0.0;
+    for (int j = -m; j <= m; ++j) {
+      long long ph = ((long long)ky * j) % ny;
+      if (ph < 0) ph += ny;
+      acc += A[((long long)i * side + (j + m)) * nzh + kz] * ctab[ph];
+    }
+    Bq[t] = acc;
+  }
+}
+
+// step C: K[kx][ky][kz] = sum_i Bq[i][ky][kz] cos(2 pi kx i / nx), kx <= nx/2 -> float.
+__global__ void k_khat_c(const double* __restrict__ Bq, int m, int nx, int ny, int nzh, float* __restrict__ K) {
+  extern __shared__ double ctab[];
+  for (int t = threadIdx.x; t < nx; t += blockDim.x) ctab[t] = cospi(2.0 * t / nx);
+  __syncthreads();
+  const int nxh = nx / 2 + 1, nyh = ny / 2 + 1;
+  const long long plane = (long long)nyh * nzh;
+  const long long tot = (long long)nxh * plane;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(t / plane);
+    const long long r = t - (long long)kx * plane;
+    double acc = 0.0;
+    for (int i = -m; i <= m; ++i) {
+      long long ph = ((long long)kx * i) % nx;
+      if (ph < 0) ph += nx;
+      acc += Bq[(long long)(i + m) * plane + r] * ctab[ph];
+    }
+    K[t] = (float)acc;
+  }
+}
+
+// Full complex64 half spectrum from the reduced real one.
+__global__ void k_khat_expand(const float* __restrict__ K, int nx, int ny, int nzh, float2* __restrict__ out) {
+  const long long tot = (long long)nx * ny * nzh;
+  const int nyh = ny / 2 + 1;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+    const int kz = (int)(t % nzh);
+    const int y = (int)((t / nzh) % ny);
+    const int x = (int)(t / ((long long)nzh * ny));
+    const int xr = min(x, nx - x), yr = min(y, ny - y);
+    out[t] = make_float2(K[((long long)xr * nyh + yr) * nzh + kz], 0.0f);
+  }
+}
+
+// ------------------------------------------------------------ plan layout
+inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct PlanLayout {
+  size_t tw_x, tw_y, tw_z, kred, total;
+};
+
+static PlanLayout plan_layout(int nx, int ny, int nz) {
+  PlanLayout L;
+  size_t off = 0;
+  L.tw_x = off; off += align256((size_t)nx * sizeof(float2));
+  L.tw_y = off; off += align256((size_t)ny * sizeof(float2));
+  L.tw_z = off; off += align256((size_t)nz * sizeof(float2));
+  L.kred = off; off += align256((size_t)(nx / 2 + 1) * (ny / 2 + 1) * (nz / 2 + 1) * sizeof(float));
+  L.total = off;
+  return L;
+}
+
+// Lines per CTA: shared memory holds two buffers of W lines (<= 64 KB, so three
+// CTAs fit on an SM).  Strided passes use W = 8 complex (one aligned 64-byte
+// segment per row of the padded spectrum).
+static int strided_width(int n) {
+  int w = 4096 / n;
+  return w > 8 ? 8 : (w < 1 ? 1 : w);
+}
+static int z_width(int n) {  // complex (paired) lines per CTA
+  int w = 4096 / n;
+  return w > 16 ? 16 : (w < 1 ? 1 : w);
+}
+
+static int ensure_smem_attr() {
+  static unsigned long long done = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return SVIE_ERR_LAUNCH;
+  if (dev < 64 && (done >> dev) & 1ULL) return SVIE_OK;
+  const int bytes = 227 * 1024;
+  cudaError_t e1 = cudaFuncSetAttribute(k_fft_z_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e2 = cudaFuncSetAttribute(k_fft_z_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e3 = cudaFuncSetAttribute(k_fft_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+    set_error("fft: cudaFuncSetAttribute failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  if (dev < 64) done |= 1ULL << dev;
+  return SVIE_OK;
+}
+
+struct Plans {
+  AxisPlan x, y, z;
+  const float* kred;
+};
+
+static int make_plans(const void* plan, int nx, int ny, int nz, Plans* P) {
+  if (!plan) {
+    set_error("fft: null plan");
+    return SVIE_ERR_ARG;
+  }
+  PlanLayout L = plan_layout(nx, ny, nz);
+  const char* b = (const char*)plan;
+  if (!factor_axis(nx, &P->x) || !factor_axis(ny, &P->y) || !factor_axis(nz, &P->z)) {
+    set_error("fft: axis sizes %d x %d x %d must be 2^a 3^b 5^c 7^d and <= %d", nx, ny, nz, FFT_MAXN);
+    return SVIE_ERR_UNSUPPORTED;
+  }
+  P->x.tw = (const float2*)(b + L.tw_x);
+  P->y.tw = (const float2*)(b + L.tw_y);
+  P->z.tw = (const float2*)(b + L.tw_z);
+  P->kred = (const float*)(b + L.kred);
+  return SVIE_OK;
+}
+
+static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, float2* spec, float* out, bool fwd,
+                     float alpha, float beta, cudaStream_t s) {
+  const long long nlines = (long long)nx * ny;
+  const int W = z_width(nz), nzp = padded_nzh(nz);
+  const size_t smem = 2 * (size_t)W * line_stride(nz) * sizeof(float2);
+  const long long nb = (nlines + 2 * W - 1) / (2 * W);
+  if (fwd) k_fft_z_r2c<<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, W, nzp);
+  else k_fft_z_c2r<<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, W, nzp, alpha, beta);
+}
+
+// y lines: outer index x, line index kz, element stride nzp.
+static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
+  const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
+  const int W = strided_width(ny);
+  const size_t smem = 2 * (size_t)W * line_stride(ny) * sizeof(float2);
+  dim3 g((unsigned)((nzh + W - 1) / W), (unsigned)nx);
+  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, W, mode, KGeom{nullptr, ny, nzh});
+}
+
+// x lines: outer index y, line index kz, element stride ny * nzp.
+static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
+  const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
+  const int W = strided_width(nx);
+  const size_t smem = 2 * (size_t)W * line_stride(nx) * sizeof(float2);
+  dim3 g((unsigned)((nzh + W - 1) / W), (unsigned)ny);
+  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, W, mode, KGeom{P.kred, ny, nzh});
+}
+
+static void gauss_legendre(int n, double* x, double* w) {
+  // Newton iteration on the Legendre polynomial P_n from the Chebyshev-like
+  // initial guesses cos(pi (i - 1/4) / (n + 1/2)); nodes returned ascending,
+  // scaled to [-1/2, 1/2] with weights summing to 1.
+  for (int i = 0; i < n; ++i) {
+    double z = cos(M_PI * (i + 0.75) / (n + 0.5)), pp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p1 = 1.0, p2 = 0.0;
+      for (int j = 1; j <= n; ++j) {
+        double p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1.0);
+      double z1 = z;
+      z = z1 - p1 / pp;
+      if (fabs(z - z1) < 1e-16) break;
+    }
+    x[n - 1 - i] = 0.5 * z;
+    w[n - 1 - i] = 0.5 * 2.0 / ((1.0 - z * z) * pp * pp);
+  }
+}
+
+}  // namespace svie
+
+using namespace svie;
+
+extern "C" {
+
+int svie_ball_half_width(double radius, double spacing) {
+  if (!(radius > 0) || !(spacing > 0)) return -1;
+  double R = radius / spacing;
+  return (int)floor(R + 0.5) + 1;
+}
+
+int svie_ball_weights(double radius, double spacing, int quad, double* w, void* stream) {
+  int m = svie_ball_half_width(radius, spacing);
+  if (m < 1 || !w || quad < 1 || quad > 64) {
+    set_error("svie_ball_weights: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  GL32 gl;
+  memset(&gl, 0, sizeof(gl));
+  gauss_legendre(quad, gl.x, gl.w);
+  const long long side = 2 * m + 1, tot = side * side * side;
+  k_ball_weights<<<blocks_for(tot, 128), 128, 0, (cudaStream_t)stream>>>(radius / spacing, m, quad, gl, w);
+  return launch_status("svie_ball_weights");
+}
+
+int svie_conv_supported(int n) {
+  AxisPlan p;
+  return factor_axis(n, &p) ? 1 : 0;
+}
+
+size_t svie_conv_plan_bytes(int nx, int ny, int nz) { return plan_layout(nx, ny, nz).total; }
+
+size_t svie_conv_workspace_bytes(int nx, int ny, int nz) {
+  return align256((size_t)nx * ny * padded_nzh(nz) * sizeof(float2));
+}
+
+int svie_conv_spectrum_row(int nz) { return padded_nzh(nz); }
+
+size_t svie_conv_init_workspace_bytes(int nx, int ny, int nz, int m) {
+  const size_t side = 2 * (size_t)m + 1, nzh = nz / 2 + 1, nyh = ny / 2 + 1;
+  (void)nx;
+  return align256(side * side * nzh * sizeof(double)) + align256(side * nyh * nzh * sizeof(double));
+}
+
+int svie_conv_plan_init(void* plan, int nx, int ny, int nz, const double* w, int m, void* ws, size_t ws_bytes,
+                           void* stream) {
+  if (!plan || !w || m < 1 || 2 * m + 1 > nx || 2 * m + 1 > ny || 2 * m + 1 > nz) {
+    set_error("svie_conv_plan_init: ball kernel larger than the grid or bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_conv_init_workspace_bytes(nx, ny, nz, m)) {
+    set_error("svie_conv_plan_init: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  Plans P;
+  int st = make_plans(plan, nx, ny, nz, &P);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  PlanLayout L = plan_layout(nx, ny, nz);
+  char* b = (char*)plan;
+  k_twiddles<<<blocks_for(nx, 256), 256, 0, s>>>((float2*)(b + L.tw_x), nx);
+  k_twiddles<<<blocks_for(ny, 256), 256, 0, s>>>((float2*)(b + L.tw_y), ny);
+  k_twiddles<<<blocks_for(nz, 256), 256, 0, s>>>((float2*)(b + L.tw_z), nz);
+  const int side = 2 * m + 1, nzh = nz / 2 + 1, nyh = ny / 2 + 1, nxh = nx / 2 + 1;
+  double* A = (double*)ws;
+  double* Bq = (double*)((char*)ws + align256((size_t)side * side * nzh * sizeof(double)));
+  const int TB = 256;
+  k_khat_a<<<blocks_for((long long)side * side * nzh, TB, 4096), TB, nz * sizeof(double), s>>>(w, m, nz, nzh, A);
+  k_khat_b<<<blocks_for((long long)side * nyh * nzh, TB, 4096), TB, ny * sizeof(double), s>>>(A, m, ny, nzh, Bq);
+  k_khat_c<<<blocks_for((long long)nxh * nyh * nzh, TB, 8192), TB, nx * sizeof(double), s>>>(
+      Bq, m, nx, ny, nzh, (float*)(b + L.kred));
+  return launch_status("svie_conv_plan_init");
+}
+
+int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, float* out, double alpha,
+                    double beta, void* ws, size_t ws_bytes, void* stream) {
+  Plans P;
+  int st = make_plans(plan, nx, ny, nz, &P);
+  if (st) return st;
+  if (!f || !out) {
+    set_error("svie_conv_apply: null input/output");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_conv_workspace_bytes(nx, ny, nz)) {
+    set_error("svie_conv_apply: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  if ((st = ensure_smem_attr())) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  float2* spec = (float2*)ws;
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s);
+  launch_y(P, nx, ny, nz, spec, 0, s);
+  launch_x(P, nx, ny, nz, spec, 2, s);
+  launch_y(P, nx, ny, nz, spec, 1, s);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s);
+  return launch_status("svie_conv_apply");
+}
+
+int svie_conv_kernel_hat(const void* plan, int nx, int ny, int nz, void* out_c64, void* stream) {
+  Plans P;
+  int st = make_plans(plan, nx, ny, nz, &P);
+  if (st) return st;
+  const long long tot = (long long)nx * ny * (nz / 2 + 1);
+  k_khat_expand<<<blocks_for(tot, 256, 8192), 256, 0, (cudaStream_t)stream>>>(P.kred, nx, ny, nz / 2 + 1,
+                                                                             (float2*)out_c64);
+  return launch_status("svie_conv_kernel_hat");
+}
+
+int svie_rfft3(const void* plan, int nx, int ny, int nz, const float* f, void* spec, void* stream) {
+  Plans P;
+  int st = make_plans(plan, nx, ny, nz, &P);
+  if (st) return st;
+  if ((st = ensure_smem_attr())) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s);
+  launch_y(P, nx, ny, nz, (float2*)spec, 0, s);
+  launch_x(P, nx, ny, nz, (float2*)spec, 0, s);
+  return launch_status("svie_rfft3");
+}
+
+int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out, double alpha, double beta,
+                void* stream) {
+  Plans P;
+  int st = make_plans(plan, nx, ny, nz, &P);
+  if (st) return st;
+  if ((st = ensure_smem_attr())) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  launch_x(P, nx, ny, nz, (float2*)spec, 1, s);
+  launch_y(P, nx, ny, nz, (float2*)spec, 1, s);
+  launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s);
+  return launch_status("svie_irfft3");
+}
+
+}  // extern "C"

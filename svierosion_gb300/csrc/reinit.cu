@@ -1,0 +1,278 @@
+// PDE reinitialisation with subcell fix (Min 2010), reference
+// svierosion/levelset.py:154-183 and svierosion/kernels.py:312-379.
+//
+// Work set: band dilated by `dilation` cells (box), outer `margin` layers
+// cleared, compacted in flat order.  Geometry (sign, local pseudo-time step,
+// per-axis crossing flags and subcell interface distances) is computed once
+// from the initial phi and stored structure-of-arrays:
+//   [sgn m][dtau m][flags m (uint32: bit 2a = cp, bit 2a+1 = cm)][xp_x xm_x xp_y xm_y xp_z xm_z : 6 m]
+// Each TVD-RK2 iteration is two Jacobi sweeps between the level-set grid A and
+// a second dense grid B that mirrors A off the work set:
+//   B[idx] = u0 + dtau rhs(A);   A[idx] = (u0 + B[idx] + dtau rhs(B)) / 2.
+#include "common.cuh"
+
+namespace svie {
+
+constexpr int RI_THREADS = 256;
+
+SVIE_DEV float minmod(float a, float b) {
+  return (a * b > 0.0f) ? (fabsf(a) < fabsf(b) ? a : b) : 0.0f;
+}
+
+// _interface_distance (kernels.py:312-331)
+SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
+  float den = p0 - p1;
+  float lin = h * p0 / (den != 0.0f ? den : 1e-30f);
+  float c2 = 0.5f * dd / (h * h);
+  float c1 = (p1 - p0) / h;
+  float c0 = 0.5f * (p0 + p1) - c2 * h * h / 4.0f;
+  float disc = c1 * c1 - 4.0f * c2 * c0;
+  float sq = sqrtf(fmaxf(disc, 0.0f));
+  float q = -0.5f * (c1 + (c1 >= 0.0f ? sq : -sq));
+  float xi = c0 / (q != 0.0f ? q : 1e-30f);
+  float quad = h / 2.0f + xi;
+  bool ok = (disc >= 0.0f) && (fabsf(dd) > 1e-10f * h * h) && (quad >= 0.0f) && (quad <= h);
+  return fminf(fmaxf(ok ? quad : lin, 0.0f), h);
+}
+
+struct Geo {
+  float* sgn;
+  float* dtau;
+  uint32_t* flags;
+  float* dist;  // 6 arrays of m
+  long long m;
+};
+
+SVIE_DEV Geo geo_view(void* base, long long m) {
+  Geo g;
+  float* f = (float*)base;
+  g.sgn = f;
+  g.dtau = f + m;
+  g.flags = (uint32_t*)(f + 2 * m);
+  g.dist = f + 3 * m;
+  g.m = m;
+  return g;
+}
+
+__global__ void k_reinit_geometry(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
+                                  long long sx, long long sy, long long sz, float h, float cfl, void* geo) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  Geo g = geo_view(geo, m);
+  const long long i = idx[t];
+  const float c = __ldg(f + i);
+  float hmin = h;
+  uint32_t flags = 0;
+  const long long st[3] = {sx, sy, sz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const long long s = st[a];
+    float m2 = __ldg(f + i - 2 * s), m1 = __ldg(f + i - s), p1 = __ldg(f + i + s), p2 = __ldg(f + i + 2 * s);
+    float d_m1 = c - 2.0f * m1 + m2;
+    float d_0 = p1 - 2.0f * c + m1;
+    float d_p1 = p2 - 2.0f * p1 + c;
+    bool cp = (c * p1) < 0.0f;
+    bool cm = (c * m1) < 0.0f;
+    float xp = interface_distance(c, p1, minmod(d_0, d_p1), h);
+    float xm = interface_distance(c, m1, minmod(d_0, d_m1), h);
+    hmin = fminf(hmin, cp ? xp : hmin);
+    hmin = fminf(hmin, cm ? xm : hmin);
+    flags |= (cp ? 1u : 0u) << (2 * a);
+    flags |= (cm ? 1u : 0u) << (2 * a + 1);
+    g.dist[(2 * a) * m + t] = fmaxf(xp, 1e-6f * h);
+    g.dist[(2 * a + 1) * m + t] = fmaxf(xm, 1e-6f * h);
+  }
+  g.sgn[t] = (c > 0.0f) ? 1.0f : ((c < 0.0f) ? -1.0f : 0.0f);
+  g.dtau[t] = cfl * fmaxf(hmin, 1e-3f * h);
+  g.flags[t] = flags;
+}
+
+// reinit_rhs (kernels.py:363-379) at work-set entry t.
+SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, long long i, long long t, const Geo& g, long long sx,
+                             long long sy, long long sz, float h) {
+  const float c = __ldg(f + i);
+  const float sgn = g.sgn[t];
+  const uint32_t flags = g.flags[t];
+  const bool outside = sgn > 0.0f;
+  const float hh = h * h;
+  float g2 = 0.0f;
+  const long long st[3] = {sx, sy, sz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const long long s = st[a];
+    float m2 = __ldg(f + i - 2 * s), m1 = __ldg(f + i - s), p1 = __ldg(f + i + s), p2 = __ldg(f + i + 2 * s);
+    float mm_p = minmod(p1 - 2.0f * c + m1, p2 - 2.0f * p1 + c);
+    float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
+    const bool cp = (flags >> (2 * a)) & 1u, cm = (flags >> (2 * a + 1)) & 1u;
+    float Dp, Dm;
+    if (cp) {
+      const float xp = g.dist[(2 * a) * g.m + t];
+      Dp = -c / xp - 0.5f * xp * mm_p / hh;
+    } else {
+      Dp = (p1 - c - 0.5f * mm_p) / h;
+    }
+    if (cm) {
+      const float xm = g.dist[(2 * a + 1) * g.m + t];
+      Dm = c / xm + 0.5f * xm * mm_m / hh;
+    } else {
+      Dm = (c - m1 + 0.5f * mm_m) / h;
+    }
+    float v;
+    if (outside) {
+      float a1 = fmaxf(Dm, 0.0f), b1 = fminf(Dp, 0.0f);
+      v = fmaxf(a1 * a1, b1 * b1);
+    } else {
+      float a1 = fminf(Dm, 0.0f), b1 = fmaxf(Dp, 0.0f);
+      v = fmaxf(a1 * a1, b1 * b1);
+    }
+    g2 = g2 + v;
+  }
+  return -sgn * (sqrtf(g2) - 1.0f);
+}
+
+__global__ void __launch_bounds__(RI_THREADS) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
+                                                             const int32_t* __restrict__ idx, long long m, long long sx,
+                                                             long long sy, long long sz, float h, void* geo,
+                                                             int second) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  Geo g = geo_view(geo, m);
+  const long long i = idx[t];
+  const float r = reinit_rhs_at(src, i, t, g, sx, sy, sz, h);
+  const float dtau = g.dtau[t];
+  if (!second) {
+    dst[i] = src[i] + dtau * r;  // u0 + dtau rhs(A)
+  } else {
+    const float u0 = dst[i], u1 = src[i];
+    dst[i] = 0.5f * (u0 + u1 + dtau * r);
+  }
+}
+
+__global__ void k_reinit_rhs(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, long long sx,
+                             long long sy, long long sz, float h, void* geo, float* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  Geo g = geo_view(geo, m);
+  out[t] = reinit_rhs_at(f, idx[t], t, g, sx, sy, sz, h);
+}
+
+__global__ void k_geo_unpack(const void* geo, long long m, float* sgn, float* dtau, uint8_t* flags, float* dist6) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  Geo g = geo_view(const_cast<void*>(geo), m);
+  sgn[t] = g.sgn[t];
+  dtau[t] = g.dtau[t];
+  for (int a = 0; a < 6; ++a) {
+    flags[a * m + t] = (g.flags[t] >> a) & 1u;
+    dist6[a * m + t] = g.dist[a * m + t];
+  }
+}
+
+__global__ void k_mark(const int32_t* __restrict__ band, long long m, uint8_t* __restrict__ mask) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m) mask[band[t]] = 1;
+}
+
+// dst = src dilated by `r` cells along one axis (box, clipped at the borders);
+// margin > 0 also clears the outer layers on every axis (last pass only).
+__global__ void k_dilate_axis(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, int nx, int ny, int nz,
+                              int axis, int r, int margin) {
+  const long long n = (long long)nx * ny * nz;
+  const long long syz = (long long)ny * nz;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(e / syz), y = (int)((e / nz) % ny), z = (int)(e % nz);
+    const int c = axis == 0 ? x : (axis == 1 ? y : z);
+    const int len = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    const long long st = axis == 0 ? syz : (axis == 1 ? nz : 1);
+    uint8_t v = 0;
+    const int lo = max(c - r, 0), hi = min(c + r, len - 1);
+    for (int d = lo; d <= hi && !v; ++d) v = src[e + (long long)(d - c) * st];
+    if (margin > 0 && (x < margin || y < margin || z < margin || x >= nx - margin || y >= ny - margin ||
+                       z >= nz - margin))
+      v = 0;
+    dst[e] = v;
+  }
+}
+
+inline size_t geo_bytes(long long m) { return (size_t)(m < 1 ? 1 : m) * 9 * sizeof(float) + 256; }
+
+}  // namespace svie
+
+using namespace svie;
+
+extern "C" {
+
+int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin, uint8_t* mask,
+                     uint8_t* tmp, void* stream) {
+  const long long n = (long long)nx * ny * nz;
+  if (!mask || !tmp || n <= 0 || dilation < 0 || margin < 0 || m < 0) {
+    set_error("svie_reinit_mask: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(mask, 0, (size_t)n, s) != cudaSuccess) {
+    set_error("svie_reinit_mask: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  if (m > 0) k_mark<<<blocks_for(m, 256), 256, 0, s>>>(band, m, mask);
+  const int nb = blocks_for(n, 256, 152 * 16);
+  k_dilate_axis<<<nb, 256, 0, s>>>(mask, tmp, nx, ny, nz, 0, dilation, 0);
+  k_dilate_axis<<<nb, 256, 0, s>>>(tmp, mask, nx, ny, nz, 1, dilation, 0);
+  k_dilate_axis<<<nb, 256, 0, s>>>(mask, tmp, nx, ny, nz, 2, dilation, margin);
+  if (cudaMemcpyAsync(mask, tmp, (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+    set_error("svie_reinit_mask: copy failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  return launch_status("svie_reinit_mask");
+}
+
+size_t svie_reinit_geometry_bytes(int64_t m) { return geo_bytes(m); }
+
+int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz,
+                         float h, float cfl, void* geo, void* stream) {
+  if (m < 0 || (m > 0 && (!phi || !idx || !geo))) {
+    set_error("svie_reinit_geometry: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (m == 0) return SVIE_OK;
+  k_reinit_geometry<<<blocks_for(m, RI_THREADS), RI_THREADS, 0, (cudaStream_t)stream>>>(phi, idx, m, sx, sy, sz, h,
+                                                                                        cfl, geo);
+  return launch_status("svie_reinit_geometry");
+}
+
+int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                        int64_t sz, float h, const void* geo, int iterations, void* stream) {
+  if (!phi || !phi_tmp || n <= 0 || m < 0 || iterations < 0) {
+    set_error("svie_reinit_iterate: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (m == 0 || iterations == 0) return SVIE_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(phi_tmp, phi, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+    set_error("svie_reinit_iterate: copy failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  const int nb = blocks_for(m, RI_THREADS);
+  for (int it = 0; it < iterations; ++it) {
+    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, const_cast<void*>(geo), 0);
+    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, const_cast<void*>(geo), 1);
+  }
+  return launch_status("svie_reinit_iterate");
+}
+
+int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz, float h,
+                    const void* geo, float* out, void* stream) {
+  if (m <= 0) return m < 0 ? SVIE_ERR_ARG : SVIE_OK;
+  k_reinit_rhs<<<blocks_for(m, RI_THREADS), RI_THREADS, 0, (cudaStream_t)stream>>>(phi, idx, m, sx, sy, sz, h,
+                                                                                   const_cast<void*>(geo), out);
+  return launch_status("svie_reinit_rhs");
+}
+
+int svie_reinit_geometry_unpack(const void* geo, int64_t m, float* sgn, float* dtau, uint8_t* flags, float* dist6,
+                                void* stream) {
+  if (m <= 0) return m < 0 ? SVIE_ERR_ARG : SVIE_OK;
+  k_geo_unpack<<<blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(geo, m, sgn, dtau, flags, dist6);
+  return launch_status("svie_reinit_geometry_unpack");
+}
+
+}  // extern "C"

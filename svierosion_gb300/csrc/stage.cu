@@ -1,0 +1,394 @@
+// Fused right-hand side of one TVD-RK3 stage on the narrow band
+// (reference svierosion/evolve.py:118-179).
+//
+// SVI law, one thread per band node:
+//   closest point (7-point stencil) -> tricubic N at it (64 taps of the dense N
+//   field) -> speed law (t - N in float64 when s = 1) -> statistics ->
+//   smoothstep cutoff -> WENO5/Godunov |grad phi| (19 taps) -> L = V |grad phi|.
+// Curvature laws replace the N lookup by principal curvatures scattered into an
+// interleaved dense (k1, k2) field and trilinear lookups at the closest point.
+//
+// Statistics: maxima/minima with one atomic per CTA on order-preserving
+// integer keys (exact, order independent); sums as per-CTA float64 partials
+// reduced in a fixed order, so every run gives the same bits.
+#include "common.cuh"
+
+namespace svie {
+
+constexpr int SG_THREADS = 256;
+
+struct LawF {
+  // float copies of the law constants as the reference's float32 kernels see them
+  float hf, cut_b, cut_ba, n_cap_f;
+};
+
+SVIE_DEV float powk(float x, int k) {
+  if (k == 0) return 1.0f;
+  if (k == 1) return x;
+  if (k == 2) return x * x;
+  if (k == 3) return x * x * x;
+  return powf(x, (float)k);
+}
+
+// SVIPowerLaw.speed (flows.py:89-96)
+SVIE_DEV float svi_speed(float N, const svie_law& L) {
+  N = fminf(fmaxf(N, 0.0f), 1.0f);
+  float V;
+  if (L.s) {
+    N = fminf(N, (float)L.n_cap);
+    V = (float)((double)powk(N, L.k) / (L.t - (double)N));
+  } else {
+    V = L.k ? powk(N, L.k) : 1.0f;
+  }
+  return L.eps != 0.0 ? V + (float)L.eps : V;
+}
+
+// SVIPowerLaw.dspeed (flows.py:98-108)
+SVIE_DEV float svi_dspeed(float N, const svie_law& L) {
+  N = fminf(fmaxf(N, 1e-12f), 1.0f);
+  if (L.s) {
+    N = fminf(N, (float)L.n_cap);
+    double d = L.t - (double)N;
+    float V = (float)((double)powk(N, L.k) / d);
+    return V * ((float)L.k / N + (float)(1.0 / d));
+  }
+  if (L.k == 0) return 0.0f;
+  return (float)L.k * powk(N, L.k - 1);
+}
+
+// _CurvatureLaw._power / _dpower (flows.py:139-158)
+SVIE_DEV float curv_power(float x, const svie_law& L) {
+  if (L.alpha == 1.0) return x;
+  if (L.alpha < 1.0) return x * powf(x + (float)L.delta, (float)(L.alpha - 1.0));
+  return powf(x, (float)L.alpha);
+}
+SVIE_DEV float curv_dpower(float x, const svie_law& L) {
+  const double a = L.alpha;
+  if (a == 1.0) return 1.0f;
+  if (a < 1.0) {
+    float y = x + (float)L.delta;
+    return powf(y, (float)(a - 2.0)) * ((float)a * x + (float)L.delta);
+  }
+  return (float)a * powf(fmaxf(x, 0.0f), (float)(a - 1.0));
+}
+
+// Speed and diffusivity of the curvature laws (flows.py:170-206).
+SVIE_DEV void curv_speed(float k1, float k2, const svie_law& L, float* V, float* D) {
+  if (L.kind == 1) {
+    float H = 0.5f * (k1 + k2);
+    float Hp = fmaxf(H, 0.0f);
+    *V = curv_power(Hp, L) + (float)L.eps;
+    *D = H > 0.0f ? curv_dpower(Hp, L) : 0.0f;
+  } else {
+    float a = fmaxf(k1, 0.0f), b = fmaxf(k2, 0.0f);
+    float Kc = a * b;
+    *V = curv_power(Kc, L) + (float)L.eps;
+    float dF = curv_dpower(Kc, L);
+    *D = Kc > 0.0f ? dF * (a + b) : dF * 0.0f;
+  }
+}
+
+// Smoothstep cutoff (evolve.py:108-112): t = clamp((b - |phi|)/(b - a), 0, 1).
+SVIE_DEV float cutoff(float phi, const svie_law& L) {
+  float x = fabsf(phi);
+  float t = ((float)L.cut_b - x) / (float)(L.cut_b - L.cut_a);
+  t = fminf(fmaxf(t, 0.0f), 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+
+struct StatAcc {
+  float vmax;          // after cutoff, all nodes
+  float qmin_n, qmax_n, qmin_a, qmax_a;
+  float dv_n, dv_a;    // dspeed (svi) or diffusivity (curvature)
+  unsigned int cap_n, cap_a, n_near;
+  double vs_n, vs_a;
+};
+
+SVIE_DEV void stat_init(StatAcc& s) {
+  s.vmax = 0.0f;
+  s.qmin_n = s.qmin_a = INFINITY;
+  s.qmax_n = s.qmax_a = -INFINITY;
+  s.dv_n = s.dv_a = 0.0f;
+  s.cap_n = s.cap_a = s.n_near = 0;
+  s.vs_n = s.vs_a = 0.0;
+}
+
+// Per-CTA reduction of the statistics and one atomic / partial write per CTA.
+SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
+  __shared__ float shf[SG_THREADS / 32];
+  __shared__ double shd[SG_THREADS / 32];
+  __shared__ unsigned int shu[SG_THREADS / 32];
+  float v;
+  v = block_reduce(a.vmax, shf, OpMaxF(), 0.0f);
+  if (threadIdx.x == 0 && v > 0.0f) atomicMax(&st->vmax, __float_as_uint(v));
+  v = block_reduce(a.qmin_n, shf, OpMinF(), INFINITY);
+  if (threadIdx.x == 0 && v < INFINITY) atomicMin(&st->qmin_near, float_to_ordered(v));
+  v = block_reduce(a.qmax_n, shf, OpMaxF(), -INFINITY);
+  if (threadIdx.x == 0 && v > -INFINITY) atomicMax(&st->qmax_near, float_to_ordered(v));
+  v = block_reduce(a.qmin_a, shf, OpMinF(), INFINITY);
+  if (threadIdx.x == 0 && v < INFINITY) atomicMin(&st->qmin_all, float_to_ordered(v));
+  v = block_reduce(a.qmax_a, shf, OpMaxF(), -INFINITY);
+  if (threadIdx.x == 0 && v > -INFINITY) atomicMax(&st->qmax_all, float_to_ordered(v));
+  v = block_reduce(a.dv_n, shf, OpMaxF(), 0.0f);
+  if (threadIdx.x == 0 && v > 0.0f) atomicMax(&st->dvmax_near, __float_as_uint(v));
+  v = block_reduce(a.dv_a, shf, OpMaxF(), 0.0f);
+  if (threadIdx.x == 0 && v > 0.0f) atomicMax(&st->dvmax_all, __float_as_uint(v));
+  unsigned int u;
+  u = block_reduce(a.cap_n, shu, OpSumU(), 0u);
+  if (threadIdx.x == 0 && u) atomicAdd(&st->capped_near, u);
+  u = block_reduce(a.cap_a, shu, OpSumU(), 0u);
+  if (threadIdx.x == 0 && u) atomicAdd(&st->capped_all, u);
+  u = block_reduce(a.n_near, shu, OpSumU(), 0u);
+  if (threadIdx.x == 0 && u) atomicAdd(&st->n_near, u);
+  double d;
+  d = block_reduce(a.vs_n, shd, OpSumD(), 0.0);
+  if (threadIdx.x == 0) partial[2 * blockIdx.x] = d;
+  d = block_reduce(a.vs_a, shd, OpSumD(), 0.0);
+  if (threadIdx.x == 0) partial[2 * blockIdx.x + 1] = d;
+}
+
+__global__ void __launch_bounds__(SG_THREADS) k_stage_svi(const float* __restrict__ phi,
+                                                          const int32_t* __restrict__ band, long long m, int nx,
+                                                          int ny, int nz, const float* __restrict__ Nd,
+                                                          svie_law L, float* __restrict__ Lout,
+                                                          float* __restrict__ u0, float* __restrict__ Vout,
+                                                          svie_stats* st, double* partial) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long syz = (long long)ny * nz;
+  const float h = (float)L.h;
+  StatAcc acc;
+  if (st) stat_init(acc);
+  if (t < m) {
+    const long long i = band[t];
+    const float c = __ldg(phi + i);
+    const float3 p = closest_point_at(phi, i, ny, nz, (float)(nx - 3.001), (float)(ny - 3.001),
+                                      (float)(nz - 3.001), h);
+    const float N = tricubic_at(Nd, ny, nz, p);
+    float V = svi_speed(N, L);
+    if (st) {
+      const bool near = fabsf(c) < h;
+      const float dv = svi_dspeed(N, L);
+      const bool capped = N > (float)L.n_cap;
+      acc.qmin_a = N; acc.qmax_a = N; acc.dv_a = dv; acc.cap_a = capped; acc.vs_a = V;
+      if (near) {
+        acc.qmin_n = N; acc.qmax_n = N; acc.dv_n = dv; acc.cap_n = capped; acc.vs_n = V; acc.n_near = 1;
+      }
+    }
+    V = V * cutoff(c, L);
+    const float G = godunov_at(phi, i, syz, nz, 1, (float)(1.0 / L.h));
+    Lout[t] = V * G;
+    if (u0) u0[t] = c;
+    if (Vout) Vout[t] = V;
+    if (st) acc.vmax = V;
+  }
+  if (st) stat_commit(acc, st, partial);
+}
+
+__global__ void k_curv_scatter(const float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
+                               int ny, int nz, float h, float* __restrict__ kd) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const long long i = band[t];
+  const float2 k = principal_curvatures_at(phi, i, (long long)ny * nz, nz, 1, h);
+  kd[2 * i] = k.x;
+  kd[2 * i + 1] = k.y;
+}
+
+__global__ void __launch_bounds__(SG_THREADS) k_stage_curv(const float* __restrict__ phi,
+                                                           const int32_t* __restrict__ band, long long m, int nx,
+                                                           int ny, int nz, const float* __restrict__ kd,
+                                                           svie_law L, float* __restrict__ Lout,
+                                                           float* __restrict__ u0, float* __restrict__ Vout,
+                                                           svie_stats* st, double* partial) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long syz = (long long)ny * nz;
+  const float h = (float)L.h;
+  StatAcc acc;
+  if (st) stat_init(acc);
+  if (t < m) {
+    const long long i = band[t];
+    const float c = __ldg(phi + i);
+    const float3 p = closest_point_at(phi, i, ny, nz, (float)(nx - 3.001), (float)(ny - 3.001),
+                                      (float)(nz - 3.001), h);
+    const float k1 = trilinear_at(kd, ny, nz, p, 2, 0);
+    const float k2 = trilinear_at(kd, ny, nz, p, 2, 1);
+    float V, D;
+    curv_speed(k1, k2, L, &V, &D);
+    if (st) {
+      const bool near = fabsf(c) < h;
+      const float H = 0.5f * (k1 + k2);
+      acc.qmin_a = H; acc.qmax_a = H; acc.dv_a = D; acc.vs_a = V;
+      if (near) { acc.qmin_n = H; acc.qmax_n = H; acc.dv_n = D; acc.vs_n = V; acc.n_near = 1; }
+    }
+    V = V * cutoff(c, L);
+    const float G = godunov_at(phi, i, syz, nz, 1, (float)(1.0 / L.h));
+    Lout[t] = V * G;
+    if (u0) u0[t] = c;
+    if (Vout) Vout[t] = V;
+    if (st) acc.vmax = V;
+  }
+  if (st) stat_commit(acc, st, partial);
+}
+
+__global__ void k_stats_reset(svie_stats* st, double dt_cap) {
+  st->vsum_near = st->vsum_all = 0.0;
+  st->dt = 0.0;
+  st->dt_cap = dt_cap;
+  st->vmax = 0u;
+  st->qmin_near = st->qmin_all = 0xffffffffu;
+  st->qmax_near = st->qmax_all = 0u;
+  st->dvmax_near = st->dvmax_all = 0u;
+  st->dmax_near = st->dmax_all = 0u;
+  st->capped_near = st->capped_all = 0u;
+  st->n_near = 0u;
+}
+
+// stable_dt (evolve.py:162-170) plus the float64 sums of V.
+__global__ void __launch_bounds__(1024) k_stats_finalize(svie_stats* st, svie_law L, const double* partial,
+                                                         long long nb, long long m) {
+  __shared__ double sh[32];
+  double a = 0.0, b = 0.0;
+  for (long long i = threadIdx.x; i < nb; i += blockDim.x) {
+    a += partial[2 * i];
+    b += partial[2 * i + 1];
+  }
+  a = block_reduce(a, sh, OpSumD(), 0.0);
+  b = block_reduce(b, sh, OpSumD(), 0.0);
+  if (threadIdx.x != 0) return;
+  st->vsum_near = a;
+  st->vsum_all = b;
+  const bool any_near = st->n_near > 0;
+  const double vmax = m > 0 ? (double)__uint_as_float(st->vmax) : 0.0;
+  const double h = L.h;
+  double dt = vmax > 0 ? L.cfl * h / vmax : INFINITY;
+  if (L.kind == 0) {
+    const double dv = (double)__uint_as_float(any_near ? st->dvmax_near : st->dvmax_all);
+    if (dv > 0) dt = fmin(dt, L.feedback_cfl * (4.0 * L.radius / 3.0) / dv);
+  } else {
+    const double dm = (double)__uint_as_float(any_near ? st->dvmax_near : st->dvmax_all);
+    st->dmax_near = st->dvmax_near;
+    st->dmax_all = st->dvmax_all;
+    if (dm > 0) dt = fmin(dt, L.parabolic_cfl * h * h / dm);
+  }
+  dt = fmin(dt, st->dt_cap);
+  st->dt = dt;
+}
+
+// TVD-RK3 stage combinations (evolve.py:175-179) with the reference's float32
+// operation order; dt read from the device.
+__global__ void k_rk(float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
+                     const float* __restrict__ u0, const float* __restrict__ L, const double* dtp, int stage) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const long long i = band[t];
+  if (stage == 0) {
+    phi[i] = u0[t];
+    return;
+  }
+  const double dtd = *dtp;
+  if (!(dtd > 0.0) || !isfinite(dtd)) return;
+  const float dt = (float)dtd;
+  const float a = u0[t], dl = dt * L[t];
+  if (stage == 1) {
+    phi[i] = a + dl;
+  } else if (stage == 2) {
+    phi[i] = 0.75f * a + 0.25f * (phi[i] + dl);
+  } else {
+    phi[i] = a / 3.0f + (float)(2.0 / 3.0) * (phi[i] + dl);
+  }
+}
+
+}  // namespace svie
+
+using namespace svie;
+
+extern "C" {
+
+size_t svie_stage_workspace_bytes(int64_t m) {
+  long long nb = (m + SG_THREADS - 1) / SG_THREADS;
+  if (nb < 1) nb = 1;
+  return (size_t)nb * 2 * sizeof(double) + 256;
+}
+
+int svie_stats_reset(svie_stats* stats, double dt_cap, void* stream) {
+  if (!stats) {
+    set_error("svie_stats_reset: null stats");
+    return SVIE_ERR_ARG;
+  }
+  k_stats_reset<<<1, 1, 0, (cudaStream_t)stream>>>(stats, dt_cap);
+  return launch_status("svie_stats_reset");
+}
+
+static int stage_check(const char* name, int64_t m, int nx, int ny, int nz, const svie_law* law, svie_stats* st,
+                       void* ws, size_t ws_bytes) {
+  if (m < 0 || m >= (1LL << 31) || nx < 8 || ny < 8 || nz < 8 || !law) {
+    set_error("%s: bad arguments", name);
+    return SVIE_ERR_ARG;
+  }
+  if (st && (!ws || ws_bytes < svie_stage_workspace_bytes(m))) {
+    set_error("%s: workspace too small", name);
+    return SVIE_ERR_WORKSPACE;
+  }
+  return SVIE_OK;
+}
+
+int svie_stage_svi(const float* phi, const int32_t* band, int64_t m, int nx, int ny, int nz, const float* N,
+                   const svie_law* law, float* L, float* u0, float* V, svie_stats* stats, void* ws,
+                   size_t ws_bytes, void* stream) {
+  int s = stage_check("svie_stage_svi", m, nx, ny, nz, law, stats, ws, ws_bytes);
+  if (s) return s;
+  const long long nb = (m + SG_THREADS - 1) / SG_THREADS;
+  if (nb == 0) return SVIE_OK;
+  k_stage_svi<<<(unsigned)nb, SG_THREADS, 0, (cudaStream_t)stream>>>(phi, band, m, nx, ny, nz, N, *law, L, u0, V,
+                                                                     stats, (double*)ws);
+  return launch_status("svie_stage_svi");
+}
+
+int svie_curvature_scatter(const float* phi, const int32_t* band, int64_t m, int nx, int ny, int nz, float h,
+                           float* kdense, void* stream) {
+  (void)nx;
+  if (m <= 0) return m < 0 ? SVIE_ERR_ARG : SVIE_OK;
+  k_curv_scatter<<<blocks_for(m, SG_THREADS), SG_THREADS, 0, (cudaStream_t)stream>>>(phi, band, m, ny, nz, h,
+                                                                                      kdense);
+  return launch_status("svie_curvature_scatter");
+}
+
+int svie_stage_curvature(const float* phi, const int32_t* band, int64_t m, int nx, int ny, int nz,
+                         const float* kdense, const svie_law* law, float* L, float* u0, float* V,
+                         svie_stats* stats, void* ws, size_t ws_bytes, void* stream) {
+  int s = stage_check("svie_stage_curvature", m, nx, ny, nz, law, stats, ws, ws_bytes);
+  if (s) return s;
+  const long long nb = (m + SG_THREADS - 1) / SG_THREADS;
+  if (nb == 0) return SVIE_OK;
+  k_stage_curv<<<(unsigned)nb, SG_THREADS, 0, (cudaStream_t)stream>>>(phi, band, m, nx, ny, nz, kdense, *law, L,
+                                                                      u0, V, stats, (double*)ws);
+  return launch_status("svie_stage_curvature");
+}
+
+int svie_stats_finalize(svie_stats* stats, const svie_law* law, const void* ws, size_t ws_bytes, int64_t m,
+                        void* stream) {
+  if (!stats || !law || m < 0) {
+    set_error("svie_stats_finalize: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_stage_workspace_bytes(m)) {
+    set_error("svie_stats_finalize: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  const long long nb = (m + SG_THREADS - 1) / SG_THREADS;
+  k_stats_finalize<<<1, 1024, 0, (cudaStream_t)stream>>>(stats, *law, (const double*)ws, nb, m);
+  return launch_status("svie_stats_finalize");
+}
+
+int svie_rk_stage(float* phi, const int32_t* band, int64_t m, const float* u0, const float* L, const double* dt,
+                  int stage, void* stream) {
+  if (m < 0 || stage < 0 || stage > 3 || (stage > 0 && (!L || !dt))) {
+    set_error("svie_rk_stage: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (m == 0) return SVIE_OK;
+  k_rk<<<blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(phi, band, m, u0, L, dt, stage);
+  return launch_status("svie_rk_stage");
+}
+
+}  // extern "C"

@@ -1,0 +1,318 @@
+// Per-node stencil and interpolation kernels behind svierosion_gb300.kernels,
+// plus the band occupancy scatter and the float64 solid-volume reduction.
+//
+// One thread per listed node; the node list is sorted, so neighbouring threads
+// read neighbouring phi values and the +-stride stencil taps of a warp fall in
+// the same few cache lines.  All of these are gather-bound (L2/HBM).
+#include "common.cuh"
+
+namespace svie {
+
+constexpr int ST_THREADS = 256;
+
+__global__ void k_godunov(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
+                          long long sx, long long sy, long long sz, float inv_h, float* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  out[t] = godunov_at(f, idx[t], sx, sy, sz, inv_h);
+}
+
+__global__ void k_fractions(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
+                            long long sx, long long sy, long long sz, float* __restrict__ out,
+                            int scatter) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  long long i = idx[t];
+  float v = cell_fraction_at(f, i, sx, sy, sz);
+  if (scatter) out[i] = v; else out[t] = v;
+}
+
+__global__ void k_closest(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int ny,
+                          int nz, float hx, float hy, float hz, float h, float* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  float3 p = closest_point_at(f, idx[t], ny, nz, hx, hy, hz, h);
+  out[3 * t] = p.x;
+  out[3 * t + 1] = p.y;
+  out[3 * t + 2] = p.z;
+}
+
+__global__ void k_tricubic(const float* __restrict__ g, int ny, int nz, const float* __restrict__ p,
+                           long long m, float* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  out[t] = tricubic_at(g, ny, nz, make_float3(p[3 * t], p[3 * t + 1], p[3 * t + 2]));
+}
+
+__global__ void k_tricubic_grad(const float* __restrict__ g, int ny, int nz, const float* __restrict__ p,
+                                long long m, float* __restrict__ val, float* __restrict__ grad) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  float px = p[3 * t], py = p[3 * t + 1], pz = p[3 * t + 2];
+  float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+  float tx = px - fx, ty = py - fy, tz = pz - fz;
+  float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
+  cubic_w(tx, wx); cubic_w(ty, wy); cubic_w(tz, wz);
+  cubic_dw(tx, dx); cubic_dw(ty, dy); cubic_dw(tz, dz);
+  const long long syz = (long long)ny * nz;
+  const long long b0 = ((long long)fx - 1) * syz + ((long long)fy - 1) * nz + ((long long)fz - 1);
+  float v = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b)
+      for (int c = 0; c < 4; ++c) {
+        float s = __ldg(g + b0 + a * syz + b * nz + c);
+        v = v + wx[a] * wy[b] * wz[c] * s;
+        gx = gx + dx[a] * wy[b] * wz[c] * s;
+        gy = gy + wx[a] * dy[b] * wz[c] * s;
+        gz = gz + wx[a] * wy[b] * dz[c] * s;
+      }
+  val[t] = v;
+  grad[3 * t] = gx;
+  grad[3 * t + 1] = gy;
+  grad[3 * t + 2] = gz;
+}
+
+__global__ void k_trilinear(const float* __restrict__ g, int ny, int nz, const float* __restrict__ p,
+                            long long m, float* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  out[t] = trilinear_at(g, ny, nz, make_float3(p[3 * t], p[3 * t + 1], p[3 * t + 2]), 1, 0);
+}
+
+__global__ void k_curvatures(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
+                             long long sx, long long sy, long long sz, float h, float* __restrict__ k1,
+                             float* __restrict__ k2) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  float2 k = principal_curvatures_at(f, idx[t], sx, sy, sz, h);
+  k1[t] = k.x;
+  k2[t] = k.y;
+}
+
+__global__ void k_interface(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
+                            long long sx, long long sy, long long sz, uint8_t* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  long long i = idx[t];
+  float c = __ldg(f + i);
+  bool hit = false;
+  const long long st[3] = {sx, sy, sz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    hit = hit || (__ldg(f + i + st[a]) * c <= 0.0f) || (__ldg(f + i - st[a]) * c <= 0.0f);
+  }
+  out[t] = hit ? 1 : 0;
+}
+
+// Squared point-triangle distance with Ericson's region classification in the
+// priority order of the reference (kernels.py:382-427).
+SVIE_DEV float point_triangle_d2(float3 p, float3 a, float3 b, float3 c) {
+  float3 ab = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+  float3 ac = make_float3(c.x - a.x, c.y - a.y, c.z - a.z);
+  float3 ap = make_float3(p.x - a.x, p.y - a.y, p.z - a.z);
+  float3 bp = make_float3(p.x - b.x, p.y - b.y, p.z - b.z);
+  float3 cp = make_float3(p.x - c.x, p.y - c.y, p.z - c.z);
+  float d1 = ab.x * ap.x + ab.y * ap.y + ab.z * ap.z;
+  float d2 = ac.x * ap.x + ac.y * ap.y + ac.z * ap.z;
+  float d3 = ab.x * bp.x + ab.y * bp.y + ab.z * bp.z;
+  float d4 = ac.x * bp.x + ac.y * bp.y + ac.z * bp.z;
+  float d5 = ab.x * cp.x + ab.y * cp.y + ab.z * cp.z;
+  float d6 = ac.x * cp.x + ac.y * cp.y + ac.z * cp.z;
+  float va = d3 * d6 - d5 * d4;
+  float vb = d5 * d2 - d1 * d6;
+  float vc = d1 * d4 - d3 * d2;
+  const float tiny = 1e-30f;
+  float denom = va + vb + vc;
+  denom = fabsf(denom) > tiny ? denom : tiny;
+  float v = vb / denom, w = vc / denom;
+  float e1 = d4 - d3, e2 = d5 - d6;
+  if (d1 <= 0.f && d2 <= 0.f) {                 // vertex a
+    v = 0.f; w = 0.f;
+  } else if (d3 >= 0.f && d4 <= d3) {           // vertex b
+    v = 1.f; w = 0.f;
+  } else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {  // edge ab
+    v = d1 / fmaxf(d1 - d3, tiny); w = 0.f;
+  } else if (d6 >= 0.f && d5 <= d6) {           // vertex c
+    v = 0.f; w = 1.f;
+  } else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {  // edge ac
+    v = 0.f; w = d2 / fmaxf(d2 - d6, tiny);
+  } else if (va <= 0.f && e1 >= 0.f && e2 >= 0.f) {  // edge bc
+    float wbc = e1 / fmaxf(e1 + e2, tiny);
+    v = 1.f - wbc; w = wbc;
+  }
+  float qx = a.x + v * ab.x + w * ac.x;
+  float qy = a.y + v * ab.y + w * ac.y;
+  float qz = a.z + v * ab.z + w * ac.z;
+  float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+  return dx * dx + dy * dy + dz * dz;
+}
+
+__global__ void k_pt_tri(const float* __restrict__ p, const float* __restrict__ a, const float* __restrict__ b,
+                         const float* __restrict__ c, long long m, float* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  auto ld = [&](const float* q) { return make_float3(q[3 * t], q[3 * t + 1], q[3 * t + 2]); };
+  out[t] = point_triangle_d2(ld(p), ld(a), ld(b), ld(c));
+}
+
+// Band volume: per-CTA float64 partial sums of the cell fractions, reduced in a
+// fixed order by a second one-CTA kernel (deterministic); also the
+// has_interface flags and (optionally) the occupancy scatter.
+__global__ void __launch_bounds__(ST_THREADS) k_volume_partial(const float* __restrict__ f,
+                                                               const int32_t* __restrict__ idx, long long m,
+                                                               long long sx, long long sy, long long sz,
+                                                               float* __restrict__ occ, double* partial,
+                                                               svie_stats* stats) {
+  __shared__ double shd[ST_THREADS / 32];
+  __shared__ unsigned int shu[ST_THREADS / 32];
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  unsigned int neg = 0, pos = 0;
+  if (t < m) {
+    long long i = idx[t];
+    float fr = cell_fraction_at(f, i, sx, sy, sz);
+    if (occ) occ[i] = fr;
+    v = (double)fr;
+    float c = __ldg(f + i);
+    neg = c < 0.0f;
+    pos = c > 0.0f;
+  }
+  double s = block_reduce(v, shd, OpSumD(), 0.0);
+  unsigned int an = block_reduce(neg, shu, OpSumU(), 0u);
+  unsigned int ap = block_reduce(pos, shu, OpSumU(), 0u);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = s;
+    if (an) atomicOr(&stats->any_neg, 1u);
+    if (ap) atomicOr(&stats->any_pos, 1u);
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_sum_partials(const double* partial, long long nb, double* out) {
+  __shared__ double sh[32];
+  double v = 0.0;
+  // fixed assignment of partials to threads -> deterministic result
+  for (long long i = threadIdx.x; i < nb; i += blockDim.x) v += partial[i];
+  double s = block_reduce(v, sh, OpSumD(), 0.0);
+  if (threadIdx.x == 0) *out = s;
+}
+
+__global__ void k_clear_flags(svie_stats* stats, unsigned int n_band) {
+  stats->any_neg = 0;
+  stats->any_pos = 0;
+  stats->n_band = n_band;
+}
+
+}  // namespace svie
+
+using namespace svie;
+
+#define SVIE_CHECK_M(name, m)                                 \
+  if ((m) < 0) {                                              \
+    set_error("%s: negative size", name);                     \
+    return SVIE_ERR_ARG;                                      \
+  }                                                           \
+  if ((m) == 0) return SVIE_OK;
+
+extern "C" {
+
+int svie_godunov_inward(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                        int64_t sz, float inv_h, float* out, void* stream) {
+  SVIE_CHECK_M("svie_godunov_inward", m);
+  k_godunov<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, idx, m, sx, sy, sz,
+                                                                                 inv_h, out);
+  return launch_status("svie_godunov_inward");
+}
+
+int svie_cell_fractions(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                        int64_t sz, float* out, void* stream) {
+  SVIE_CHECK_M("svie_cell_fractions", m);
+  k_fractions<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, idx, m, sx, sy, sz,
+                                                                                   out, 0);
+  return launch_status("svie_cell_fractions");
+}
+
+int svie_scatter_fractions(const float* phi, const int32_t* band, int64_t m, int64_t sx, int64_t sy,
+                           int64_t sz, float* occ, void* stream) {
+  SVIE_CHECK_M("svie_scatter_fractions", m);
+  k_fractions<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(phi, band, m, sx, sy, sz,
+                                                                                   occ, 1);
+  return launch_status("svie_scatter_fractions");
+}
+
+int svie_closest_points(const float* flat, const int32_t* idx, int64_t m, int ny, int nz, float hi_x,
+                        float hi_y, float hi_z, float h, float* out, void* stream) {
+  SVIE_CHECK_M("svie_closest_points", m);
+  k_closest<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, idx, m, ny, nz, hi_x,
+                                                                                 hi_y, hi_z, h, out);
+  return launch_status("svie_closest_points");
+}
+
+int svie_tricubic(const float* flat, int ny, int nz, const float* p, int64_t m, float* out, void* stream) {
+  SVIE_CHECK_M("svie_tricubic", m);
+  k_tricubic<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, ny, nz, p, m, out);
+  return launch_status("svie_tricubic");
+}
+
+int svie_tricubic_with_gradient(const float* flat, int ny, int nz, const float* p, int64_t m, float* val,
+                                float* grad, void* stream) {
+  SVIE_CHECK_M("svie_tricubic_with_gradient", m);
+  k_tricubic_grad<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, ny, nz, p, m,
+                                                                                       val, grad);
+  return launch_status("svie_tricubic_with_gradient");
+}
+
+int svie_trilinear(const float* flat, int ny, int nz, const float* p, int64_t m, float* out, void* stream) {
+  SVIE_CHECK_M("svie_trilinear", m);
+  k_trilinear<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, ny, nz, p, m, out);
+  return launch_status("svie_trilinear");
+}
+
+int svie_principal_curvatures(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                              int64_t sz, float h, float* k1, float* k2, void* stream) {
+  SVIE_CHECK_M("svie_principal_curvatures", m);
+  k_curvatures<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, idx, m, sx, sy, sz,
+                                                                                    h, k1, k2);
+  return launch_status("svie_principal_curvatures");
+}
+
+int svie_interface_mask(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                        int64_t sz, uint8_t* out, void* stream) {
+  SVIE_CHECK_M("svie_interface_mask", m);
+  k_interface<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, idx, m, sx, sy, sz,
+                                                                                   out);
+  return launch_status("svie_interface_mask");
+}
+
+int svie_point_triangle_distance2(const float* p, const float* a, const float* b, const float* c, int64_t m,
+                                  float* out, void* stream) {
+  SVIE_CHECK_M("svie_point_triangle_distance2", m);
+  k_pt_tri<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(p, a, b, c, m, out);
+  return launch_status("svie_point_triangle_distance2");
+}
+
+size_t svie_volume_workspace_bytes(int64_t m) {
+  long long nb = (m + ST_THREADS - 1) / ST_THREADS;
+  if (nb < 1) nb = 1;
+  return (size_t)nb * sizeof(double) + 256;
+}
+
+int svie_band_volume(const float* phi, const int32_t* band, int64_t m, int64_t sx, int64_t sy, int64_t sz,
+                     float* occ, void* ws, size_t ws_bytes, svie_stats* stats, void* stream) {
+  if (m < 0 || !stats || m >= (1LL << 31)) {
+    set_error("svie_band_volume: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_volume_workspace_bytes(m)) {
+    set_error("svie_band_volume: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  long long nb = (m + ST_THREADS - 1) / ST_THREADS;
+  k_clear_flags<<<1, 1, 0, s>>>(stats, (unsigned)m);
+  if (nb > 0)
+    k_volume_partial<<<(unsigned)nb, ST_THREADS, 0, s>>>(phi, band, m, sx, sy, sz, occ, (double*)ws, stats);
+  k_sum_partials<<<1, 1024, 0, s>>>((const double*)ws, nb, &stats->fsum);
+  return launch_status("svie_band_volume");
+}
+
+}  // extern "C"
