@@ -36,6 +36,8 @@ extern "C" {
 
 const char* svie_last_error(void);
 int svie_version(void);
+/* Number of kernels launched through this library so far (all threads). */
+unsigned long long svie_launch_count(void);
 
 /* ---------------------------------------------------------------- structs */
 /* Speed law and integrator constants (reference svierosion/flows.py:51-213,
@@ -113,6 +115,11 @@ int svie_mask_scan(const uint8_t* mask, int64_t n, void* ws, size_t ws_bytes, in
                    void* stream);
 int svie_mask_write(const uint8_t* mask, int64_t n, const void* ws, size_t ws_bytes, int32_t* out,
                     int64_t capacity, void* stream);
+/* idx[mask] for an int32 index list (LevelSet.interface_nodes,
+ * levelset.py:88-91): out[k] = vals[e] for the k-th e with mask[e] != 0.  Uses
+ * the workspace of a preceding svie_mask_scan over the same mask. */
+int svie_mask_select(const uint8_t* mask, const int32_t* vals, int64_t n, const void* ws,
+                     size_t ws_bytes, int32_t* out, int64_t capacity, void* stream);
 
 /* ------------------------------------------------- stencil kernels (API) */
 /* svierosion/kernels.py:146 godunov_inward(flat, idx, sx, sy, sz, inv_h) */
@@ -143,12 +150,28 @@ int svie_interface_mask(const float* flat, const int32_t* idx, int64_t m, int64_
  * p (m,3), a, b, c (m,3) */
 int svie_point_triangle_distance2(const float* p, const float* a, const float* b, const float* c,
                                   int64_t m, float* out, void* stream);
+/* LevelSet.central_gradient (levelset.py:98-101); out (m,3) */
+int svie_central_gradient(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                          int64_t sz, float* out, void* stream);
+/* LevelSet.closest_points(idx, newton_steps) (levelset.py:129-151); out (m,3) */
+int svie_closest_points_newton(const float* flat, const int32_t* idx, int64_t m, int ny, int nz,
+                               float hi_x, float hi_y, float hi_z, float h, int newton_steps,
+                               float* out, void* stream);
+/* levelset.cube_plane_fraction (levelset.py:37-48, kernels.py:104-122) */
+int svie_cube_plane_fraction(const float* s, const float* a, const float* b, const float* c,
+                             int64_t m, float* out, void* stream);
+/* SVIPowerLaw.speed/dspeed (flows.py:89-108) or the curvature laws'
+ * speed_and_diffusivity (flows.py:170-206): x2 is k2 for curvature laws. */
+int svie_law_eval(const float* x1, const float* x2, int64_t m, const svie_law* law, float* V,
+                  float* D, void* stream);
 
 /* ------------------------------------------- occupancy and solid volume */
 /* LevelSet.dense_fractions (svierosion/levelset.py:117-121): occ[band[i]] =
  * cell fraction; occ elsewhere must already hold (phi < 0). */
 int svie_scatter_fractions(const float* phi, const int32_t* band, int64_t m, int64_t sx, int64_t sy,
                            int64_t sz, float* occ, void* stream);
+/* occ[i] = (phi[i] < 0) on every node (levelset.py:119). */
+int svie_dense_occupancy(const float* phi, int64_t n, float* occ, void* stream);
 /* LevelSet.volume (svierosion/levelset.py:123-126) minus the static count:
  * stats->fsum = float64 sum of the band cell fractions (deterministic order),
  * stats->any_neg / any_pos = has_interface flags (levelset.py:93-95); when occ
@@ -187,6 +210,12 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
  * of 8, so every row starts on a 64-byte boundary.  The spectrum is
  * [nx][ny][row]; entries kz >= nz/2+1 are padding. */
 int svie_conv_spectrum_row(int nz);
+/* svie_conv_apply that also records events[0..5] (cudaEvent_t, created by
+ * the caller) on the stream before, between and after its five passes:
+ * z R2C, y forward, x forward*K^*inverse, y inverse, z C2R. */
+int svie_conv_apply_events(const void* plan, int nx, int ny, int nz, const float* f, float* out,
+                           double alpha, double beta, void* ws, size_t ws_bytes,
+                           void* const* events, void* stream);
 /* Full complex64 half spectrum K^ (rfftn of the wrapped kernel, svi.py:76-81). */
 int svie_conv_kernel_hat(const void* plan, int nx, int ny, int nz, void* out_c64, void* stream);
 /* Forward rfftn (complex64 nx*ny*(nz/2+1)) and inverse irfftn with
@@ -246,6 +275,9 @@ int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx,
 /* Unpack geometry into the 14 arrays of kernels.reinit_geometry. */
 int svie_reinit_geometry_unpack(const void* geo, int64_t m, float* sgn, float* dtau, uint8_t* flags,
                                 float* dist6, void* stream);
+/* levelset.dilate (levelset.py:25-34); tmp is a same-size scratch grid. */
+int svie_dilate(const uint8_t* mask, int nx, int ny, int nz, int steps, uint8_t* out, uint8_t* tmp,
+                void* stream);
 
 /* ------------------------------------------------------------------ SDF */
 /* mesh_to_sdf (svierosion/sdf.py:365-415).  tri: (T,3,3) float32 and tri64:

@@ -1,0 +1,258 @@
+"""ctypes binding of ``libsvie.so`` (the C ABI declared in include/svie.h).
+
+The library is loaded from the package directory.  There is no fallback: if it
+is missing, or a tensor is not on a CUDA device, the call raises.  Helpers here
+turn torch tensors into raw pointers, pick the current torch stream and turn
+non-zero status codes into Python exceptions.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_size_t, c_void_p
+from pathlib import Path
+
+import numpy as np
+import torch
+
+LIB_PATH = Path(__file__).resolve().parent / "libsvie.so"
+
+_lib = None
+
+
+class SvieError(RuntimeError):
+    """A failure reported by the CUDA library (status code + message)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"libsvie error {code}: {msg}")
+        self.code = code
+
+
+class Law(ctypes.Structure):
+    """svie_law (include/svie.h)."""
+    _fields_ = [("kind", c_int32), ("k", c_int32), ("s", c_int32), ("pad0", c_int32),
+                ("t", c_double), ("eps", c_double), ("n_cap", c_double), ("radius", c_double),
+                ("alpha", c_double), ("delta", c_double), ("cfl", c_double), ("feedback_cfl", c_double),
+                ("parabolic_cfl", c_double), ("h", c_double), ("cut_a", c_double), ("cut_b", c_double)]
+
+
+STATS_DTYPE = np.dtype([
+    ("vsum_near", "<f8"), ("vsum_all", "<f8"), ("fsum", "<f8"), ("dt", "<f8"), ("dt_cap", "<f8"),
+    ("reserved_d", "<f8", (3,)), ("vmax", "<u4"), ("qmin_near", "<u4"), ("qmax_near", "<u4"),
+    ("qmin_all", "<u4"), ("qmax_all", "<u4"), ("dvmax_near", "<u4"), ("dvmax_all", "<u4"),
+    ("dmax_near", "<u4"), ("dmax_all", "<u4"), ("capped_near", "<u4"), ("capped_all", "<u4"),
+    ("n_near", "<u4"), ("any_neg", "<u4"), ("any_pos", "<u4"), ("n_band", "<u4"), ("reserved_u", "<u4")])
+STATS_BYTES = STATS_DTYPE.itemsize  # 128
+DT_OFFSET = STATS_DTYPE.fields["dt"][1]
+
+BAND_INFO_DTYPE = np.dtype([("count", "<i8"), ("static_inside", "<i8"), ("lo", "<i4", (3,)), ("hi", "<i4", (3,)),
+                            ("ilo", "<i4", (3,)), ("ihi", "<i4", (3,))])
+BAND_INFO_BYTES = BAND_INFO_DTYPE.itemsize  # 64
+
+assert STATS_BYTES == 128 and BAND_INFO_BYTES == 64
+
+
+def bits_to_float(u) -> float:
+    return float(np.array([u], dtype=np.uint32).view(np.float32)[0])
+
+
+def ordered_to_float(u) -> float:
+    """Inverse of the device's order-preserving float -> uint32 map."""
+    u = int(u) & 0xFFFFFFFF
+    b = (u & 0x7FFFFFFF) if (u & 0x80000000) else (~u & 0xFFFFFFFF)
+    return float(np.array([b], dtype=np.uint32).view(np.float32)[0])
+
+
+# name -> (restype, argtypes)
+V, I64, I, F, D, Z = c_void_p, c_int64, c_int, c_float, c_double, c_size_t
+_SIGS = {
+    "svie_last_error": (c_char_p, []),
+    "svie_version": (I, []),
+    "svie_launch_count": (ctypes.c_ulonglong, []),
+    "svie_set_f64": (I, [V, D, V]),
+    "svie_band_workspace_bytes": (Z, [I64]),
+    "svie_band_scan": (I, [V, I64, F, F, V, Z, V, V]),
+    "svie_band_write": (I, [V, I, I, I, F, V, Z, V, I64, V, V, V]),
+    "svie_mask_scan": (I, [V, I64, V, Z, V, V]),
+    "svie_mask_write": (I, [V, I64, V, Z, V, I64, V]),
+    "svie_mask_select": (I, [V, V, I64, V, Z, V, I64, V]),
+    "svie_godunov_inward": (I, [V, V, I64, I64, I64, I64, F, V, V]),
+    "svie_cell_fractions": (I, [V, V, I64, I64, I64, I64, V, V]),
+    "svie_closest_points": (I, [V, V, I64, I, I, F, F, F, F, V, V]),
+    "svie_closest_points_newton": (I, [V, V, I64, I, I, F, F, F, F, I, V, V]),
+    "svie_tricubic": (I, [V, I, I, V, I64, V, V]),
+    "svie_tricubic_with_gradient": (I, [V, I, I, V, I64, V, V, V]),
+    "svie_trilinear": (I, [V, I, I, V, I64, V, V]),
+    "svie_principal_curvatures": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),
+    "svie_interface_mask": (I, [V, V, I64, I64, I64, I64, V, V]),
+    "svie_point_triangle_distance2": (I, [V, V, V, V, I64, V, V]),
+    "svie_central_gradient": (I, [V, V, I64, I64, I64, I64, V, V]),
+    "svie_cube_plane_fraction": (I, [V, V, V, V, I64, V, V]),
+    "svie_law_eval": (I, [V, V, I64, POINTER(Law), V, V, V]),
+    "svie_scatter_fractions": (I, [V, V, I64, I64, I64, I64, V, V]),
+    "svie_dense_occupancy": (I, [V, I64, V, V]),
+    "svie_volume_workspace_bytes": (Z, [I64]),
+    "svie_band_volume": (I, [V, V, I64, I64, I64, I64, V, V, Z, V, V]),
+    "svie_ball_half_width": (I, [D, D]),
+    "svie_ball_weights": (I, [D, D, I, V, V]),
+    "svie_conv_plan_bytes": (Z, [I, I, I]),
+    "svie_conv_workspace_bytes": (Z, [I, I, I]),
+    "svie_conv_init_workspace_bytes": (Z, [I, I, I, I]),
+    "svie_conv_spectrum_row": (I, [I]),
+    "svie_conv_supported": (I, [I]),
+    "svie_conv_plan_init": (I, [V, I, I, I, V, I, V, Z, V]),
+    "svie_conv_apply": (I, [V, I, I, I, V, V, D, D, V, Z, V]),
+    "svie_conv_apply_events": (I, [V, I, I, I, V, V, D, D, V, Z, V, V]),
+    "svie_conv_kernel_hat": (I, [V, I, I, I, V, V]),
+    "svie_rfft3": (I, [V, I, I, I, V, V, V]),
+    "svie_irfft3": (I, [V, I, I, I, V, V, D, D, V]),
+    "svie_stage_workspace_bytes": (Z, [I64]),
+    "svie_stats_reset": (I, [V, D, V]),
+    "svie_stage_svi": (I, [V, V, I64, I, I, I, V, POINTER(Law), V, V, V, V, V, Z, V]),
+    "svie_curvature_scatter": (I, [V, V, I64, I, I, I, F, V, V]),
+    "svie_stage_curvature": (I, [V, V, I64, I, I, I, V, POINTER(Law), V, V, V, V, V, Z, V]),
+    "svie_stats_finalize": (I, [V, POINTER(Law), V, Z, I64, V]),
+    "svie_rk_stage": (I, [V, V, I64, V, V, V, I, V]),
+    "svie_reinit_mask": (I, [V, I64, I, I, I, I, I, V, V, V]),
+    "svie_reinit_geometry_bytes": (Z, [I64]),
+    "svie_reinit_geometry": (I, [V, V, I64, I64, I64, I64, F, F, V, V]),
+    "svie_reinit_iterate": (I, [V, V, I64, V, I64, I64, I64, I64, F, V, I, V]),
+    "svie_reinit_rhs": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),
+    "svie_reinit_geometry_unpack": (I, [V, I64, V, V, V, V, V]),
+    "svie_dilate": (I, [V, I, I, I, I, V, V, V]),
+    "svie_sdf_keys_init": (I, [V, I64, V]),
+    "svie_sdf_near_field": (I, [V, V, I64, I, I, I, D, F, V, V]),
+    "svie_sdf_unpack": (I, [V, I64, V, V, V, V]),
+    "svie_sdf_ring_mask": (I, [V, I, I, I, V, V]),
+    "svie_sdf_ring_update": (I, [V, I64, I, I, I, V, V, V, V, V, V]),
+    "svie_sdf_scatter": (I, [V, I64, V, V, V, V, V, V]),
+    "svie_sdf_outer_mask": (I, [V, I64, F, F, V, V]),
+    "svie_sdf_star_pass": (I, [V, I64, I, I, I, V, V, V, V, V, V, V, V, V]),
+    "svie_sdf_crossings": (I, [V, I64, I, I, I, I, I, V, V]),
+    "svie_sdf_inside": (I, [V, I, I, I, I, I, V, V]),
+    "svie_sdf_finalize": (I, [V, V, I64, I, F, F, V, V]),
+}
+
+
+def exported_names() -> list[str]:
+    return list(_SIGS)
+
+
+def load(path: str | os.PathLike | None = None):
+    """Load (once) and return the library; raises if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is not built: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                           "(or svierosion_gb300.build.build()); there is no CPU fallback")
+    lib = ctypes.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def lib():
+    return _lib if _lib is not None else load()
+
+
+def check(status: int) -> None:
+    if status != 0:
+        msg = lib().svie_last_error().decode(errors="replace")
+        raise SvieError(status, msg)
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args))
+
+
+def ptr(t: torch.Tensor | None):
+    """Raw device pointer of a CUDA tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("svierosion_gb300 runs on CUDA tensors only (no CPU fallback); got a tensor on "
+                         f"{t.device}")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def require_cuda() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("svierosion_gb300 needs a CUDA GPU (GB300 / sm_103a); no CPU fallback exists")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+class Scratch:
+    """Grow-only device byte buffers, one per name (the caller-provided
+    workspaces of the C ABI)."""
+
+    def __init__(self, device):
+        self.device = device
+        self._buf: dict[str, torch.Tensor] = {}
+
+    def get(self, name: str, nbytes: int) -> torch.Tensor:
+        nbytes = max(int(nbytes), 256)
+        b = self._buf.get(name)
+        if b is None or b.numel() < nbytes:
+            b = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self._buf[name] = b
+        return b
+
+
+_scratch: dict[int, Scratch] = {}
+
+
+def scratch(device) -> Scratch:
+    d = torch.device(device)
+    key = d.index if d.index is not None else torch.cuda.current_device()
+    if key not in _scratch:
+        _scratch[key] = Scratch(torch.device("cuda", key))
+    return _scratch[key]
+
+
+_h2d_bytes = 0
+_d2h_bytes = 0
+
+
+def reset_transfer_counters() -> None:
+    global _h2d_bytes, _d2h_bytes
+    _h2d_bytes = _d2h_bytes = 0
+
+
+def transfer_counters() -> tuple[int, int]:
+    """Bytes copied host->device and device->host by the package since the last reset."""
+    return _h2d_bytes, _d2h_bytes
+
+
+def h2d(array, dtype: torch.dtype, device) -> torch.Tensor:
+    """Copy a host array to the device (counted)."""
+    global _h2d_bytes
+    t = torch.as_tensor(np.ascontiguousarray(array)).to(dtype)
+    _h2d_bytes += t.numel() * t.element_size()
+    return t.to(device, non_blocking=False).contiguous()
+
+
+def d2h(t: torch.Tensor) -> np.ndarray:
+    """Copy a device tensor to a host numpy array (counted)."""
+    global _d2h_bytes
+    _d2h_bytes += t.numel() * t.element_size()
+    return t.cpu().numpy()
+
+
+def f32(x) -> float:
+    """Round a Python float to float32 (how torch applies a Python scalar to a
+    float32 tensor)."""
+    return float(np.float32(x))
+
+
+INF = math.inf

@@ -224,7 +224,7 @@ int svie_band_scan(float* phi, int64_t n, float cap, float thresh, void* ws, siz
   k_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(p, n, (int*)ws);
   k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)&info->count);
   k_info_init<<<1, 1, 0, s>>>(info);
-  return launch_status("svie_band_scan");
+  return launch_status("svie_band_scan", 3);
 }
 
 int svie_band_write(const float* phi, int nx, int ny, int nz, float thresh, const void* ws,
@@ -260,7 +260,7 @@ int svie_mask_scan(const uint8_t* mask, int64_t n, void* ws, size_t ws_bytes, in
   MaskPred p{mask};
   k_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(p, n, (int*)ws);
   k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)count);
-  return launch_status("svie_mask_scan");
+  return launch_status("svie_mask_scan", 2);
 }
 
 int svie_mask_write(const uint8_t* mask, int64_t n, const void* ws, size_t ws_bytes, int32_t* out,
@@ -280,3 +280,42 @@ int svie_mask_write(const uint8_t* mask, int64_t n, const void* ws, size_t ws_by
 }
 
 }  // extern "C"
+
+namespace svie {
+// out[k] = vals[e] for the k-th e with mask[e] != 0 (order preserved).
+__global__ void __launch_bounds__(CMP_THREADS) k_select(const uint8_t* __restrict__ mask, const int32_t* __restrict__ vals,
+                                                        long long n, const int* offsets, int32_t* out,
+                                                        long long capacity) {
+  __shared__ int sh[33];
+  const long long t0 = (long long)blockIdx.x * CMP_TILE + (long long)threadIdx.x * CMP_IPT;
+  unsigned int bits = 0;
+  for (int j = 0; j < CMP_IPT; ++j) {
+    long long e = t0 + j;
+    if (e < n && mask[e]) bits |= 1u << j;
+  }
+  int tot;
+  long long o = (long long)offsets[blockIdx.x] + block_exclusive_scan(__popc(bits), sh, &tot);
+  while (bits) {
+    int j = __ffs(bits) - 1;
+    bits &= bits - 1;
+    if (o < capacity) out[o] = vals[t0 + j];
+    ++o;
+  }
+}
+}  // namespace svie
+
+extern "C" int svie_mask_select(const uint8_t* mask, const int32_t* vals, int64_t n, const void* ws, size_t ws_bytes,
+                                int32_t* out, int64_t capacity, void* stream) {
+  if (!mask || !vals || n <= 0 || n >= (1LL << 31) || (capacity > 0 && !out)) {
+    svie::set_error("svie_mask_select: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (ws_bytes < svie_band_workspace_bytes(n) || !ws) {
+    svie::set_error("svie_mask_select: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  long long nb = svie::cmp_blocks(n);
+  svie::k_select<<<(unsigned)nb, svie::CMP_THREADS, 0, (cudaStream_t)stream>>>(mask, vals, n, (const int*)ws, out,
+                                                                              capacity);
+  return svie::launch_status("svie_mask_select");
+}

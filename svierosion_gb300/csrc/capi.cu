@@ -2,11 +2,16 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <atomic>
+
 #include "common.cuh"
 
 namespace svie {
 
 static thread_local char g_err[512] = "";
+static std::atomic<unsigned long long> g_launches{0};
+
+void note_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
   va_list ap;
@@ -24,6 +29,8 @@ extern "C" {
 const char* svie_last_error(void) { return svie::g_err; }
 
 int svie_version(void) { return 1; }
+
+unsigned long long svie_launch_count(void) { return svie::g_launches.load(std::memory_order_relaxed); }
 
 int svie_set_f64(double* dst, double value, void* stream) {
   if (!dst) {

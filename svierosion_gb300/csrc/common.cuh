@@ -22,8 +22,13 @@ namespace svie {
 // Records a message for svie_last_error(); defined in capi.cu.
 void set_error(const char* fmt, ...);
 
-// Status from the most recent launch on the calling thread.
-inline int launch_status(const char* what) {
+// Counts kernel launches made through the C ABI (svie_launch_count).
+void note_launches(int n);
+
+// Status from the most recent launches on the calling thread; `n` is the number
+// of kernels the entry point launched.
+inline int launch_status(const char* what, int n = 1) {
+  note_launches(n);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("%s: launch failed: %s", what, cudaGetErrorString(e));

@@ -666,7 +666,7 @@ int svie_conv_plan_init(void* plan, int nx, int ny, int nz, const double* w, int
   k_khat_b<<<blocks_for((long long)side * nyh * nzh, TB, 4096), TB, ny * sizeof(double), s>>>(A, m, ny, nzh, Bq);
   k_khat_c<<<blocks_for((long long)nxh * nyh * nzh, TB, 8192), TB, nx * sizeof(double), s>>>(
       Bq, m, nx, ny, nzh, (float*)(b + L.kred));
-  return launch_status("svie_conv_plan_init");
+  return launch_status("svie_conv_plan_init", 6);
 }
 
 int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, float* out, double alpha,
@@ -690,7 +690,38 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
   launch_x(P, nx, ny, nz, spec, 2, s);
   launch_y(P, nx, ny, nz, spec, 1, s);
   launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s);
-  return launch_status("svie_conv_apply");
+  return launch_status("svie_conv_apply", 5);
+}
+
+int svie_conv_apply_events(const void* plan, int nx, int ny, int nz, const float* f, float* out, double alpha,
+                           double beta, void* ws, size_t ws_bytes, void* const* events, void* stream) {
+  Plans P;
+  int st = make_plans(plan, nx, ny, nz, &P);
+  if (st) return st;
+  if (!f || !out || !events) {
+    set_error("svie_conv_apply_events: null argument");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_conv_workspace_bytes(nx, ny, nz)) {
+    set_error("svie_conv_apply_events: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  if ((st = ensure_smem_attr())) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  float2* spec = (float2*)ws;
+  cudaEvent_t* ev = (cudaEvent_t*)events;
+  cudaEventRecord(ev[0], s);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s);
+  cudaEventRecord(ev[1], s);
+  launch_y(P, nx, ny, nz, spec, 0, s);
+  cudaEventRecord(ev[2], s);
+  launch_x(P, nx, ny, nz, spec, 2, s);
+  cudaEventRecord(ev[3], s);
+  launch_y(P, nx, ny, nz, spec, 1, s);
+  cudaEventRecord(ev[4], s);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s);
+  cudaEventRecord(ev[5], s);
+  return launch_status("svie_conv_apply_events", 5);
 }
 
 int svie_conv_kernel_hat(const void* plan, int nx, int ny, int nz, void* out_c64, void* stream) {
@@ -712,7 +743,7 @@ int svie_rfft3(const void* plan, int nx, int ny, int nz, const float* f, void* s
   launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s);
   launch_y(P, nx, ny, nz, (float2*)spec, 0, s);
   launch_x(P, nx, ny, nz, (float2*)spec, 0, s);
-  return launch_status("svie_rfft3");
+  return launch_status("svie_rfft3", 3);
 }
 
 int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out, double alpha, double beta,
@@ -725,7 +756,7 @@ int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out
   launch_x(P, nx, ny, nz, (float2*)spec, 1, s);
   launch_y(P, nx, ny, nz, (float2*)spec, 1, s);
   launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s);
-  return launch_status("svie_irfft3");
+  return launch_status("svie_irfft3", 3);
 }
 
 }  // extern "C"

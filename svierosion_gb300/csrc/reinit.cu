@@ -223,7 +223,7 @@ int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int
     set_error("svie_reinit_mask: copy failed");
     return SVIE_ERR_LAUNCH;
   }
-  return launch_status("svie_reinit_mask");
+  return launch_status("svie_reinit_mask", m > 0 ? 4 : 3);
 }
 
 size_t svie_reinit_geometry_bytes(int64_t m) { return geo_bytes(m); }
@@ -257,7 +257,7 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
     k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, const_cast<void*>(geo), 0);
     k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, const_cast<void*>(geo), 1);
   }
-  return launch_status("svie_reinit_iterate");
+  return launch_status("svie_reinit_iterate", 2 * iterations);
 }
 
 int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz, float h,
@@ -276,3 +276,24 @@ int svie_reinit_geometry_unpack(const void* geo, int64_t m, float* sgn, float* d
 }
 
 }  // extern "C"
+
+// levelset.dilate (levelset.py:25-34): out = mask dilated by the
+// (2 steps + 1)^3 box, clipped at the borders; tmp is a same-size scratch grid.
+extern "C" int svie_dilate(const uint8_t* mask, int nx, int ny, int nz, int steps, uint8_t* out, uint8_t* tmp,
+                           void* stream) {
+  const long long n = (long long)nx * ny * nz;
+  if (!mask || !out || !tmp || n <= 0 || steps < 0) {
+    svie::set_error("svie_dilate: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = svie::blocks_for(n, 256, 152 * 16);
+  svie::k_dilate_axis<<<nb, 256, 0, s>>>(mask, tmp, nx, ny, nz, 0, steps, 0);
+  svie::k_dilate_axis<<<nb, 256, 0, s>>>(tmp, out, nx, ny, nz, 1, steps, 0);
+  svie::k_dilate_axis<<<nb, 256, 0, s>>>(out, tmp, nx, ny, nz, 2, steps, 0);
+  if (cudaMemcpyAsync(out, tmp, (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+    svie::set_error("svie_dilate: copy failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  return svie::launch_status("svie_dilate", 3);
+}

@@ -392,3 +392,33 @@ int svie_rk_stage(float* phi, const int32_t* band, int64_t m, const float* u0, c
 }
 
 }  // extern "C"
+
+namespace svie {
+// Elementwise law evaluation: SVI: V = speed(x1), D = dspeed(x1); curvature
+// laws: V, D = speed_and_diffusivity(x1 = k1, x2 = k2).
+__global__ void k_law_eval(const float* __restrict__ x1, const float* __restrict__ x2, long long m, svie_law L,
+                           float* __restrict__ V, float* __restrict__ D) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  if (L.kind == 0) {
+    if (V) V[t] = svi_speed(x1[t], L);
+    if (D) D[t] = svi_dspeed(x1[t], L);
+  } else {
+    float v, d;
+    curv_speed(x1[t], x2[t], L, &v, &d);
+    if (V) V[t] = v;
+    if (D) D[t] = d;
+  }
+}
+}  // namespace svie
+
+extern "C" int svie_law_eval(const float* x1, const float* x2, int64_t m, const svie_law* law, float* V, float* D,
+                             void* stream) {
+  if (m < 0 || !law || (m > 0 && !x1) || (law->kind != 0 && m > 0 && !x2)) {
+    svie::set_error("svie_law_eval: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (m == 0) return SVIE_OK;
+  svie::k_law_eval<<<svie::blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(x1, x2, m, *law, V, D);
+  return svie::launch_status("svie_law_eval");
+}

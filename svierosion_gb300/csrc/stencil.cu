@@ -312,7 +312,115 @@ int svie_band_volume(const float* phi, const int32_t* band, int64_t m, int64_t s
   if (nb > 0)
     k_volume_partial<<<(unsigned)nb, ST_THREADS, 0, s>>>(phi, band, m, sx, sy, sz, occ, (double*)ws, stats);
   k_sum_partials<<<1, 1024, 0, s>>>((const double*)ws, nb, &stats->fsum);
-  return launch_status("svie_band_volume");
+  return launch_status("svie_band_volume", nb > 0 ? 3 : 2);
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ API helpers
+namespace svie {
+
+__global__ void k_central_gradient(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
+                                   long long sx, long long sy, long long sz, float* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  long long i = idx[t];
+  out[3 * t] = 0.5f * (__ldg(f + i + sx) - __ldg(f + i - sx));
+  out[3 * t + 1] = 0.5f * (__ldg(f + i + sy) - __ldg(f + i - sy));
+  out[3 * t + 2] = 0.5f * (__ldg(f + i + sz) - __ldg(f + i - sz));
+}
+
+// LevelSet.closest_points with newton_steps >= 1 (levelset.py:129-151): the
+// first projection from the central gradient, then Newton steps on the
+// tricubic interpolant with the same step cap, clamped to [1, n - 3.001].
+__global__ void k_closest_newton(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int ny,
+                                 int nz, float hx, float hy, float hz, float h, int steps, float* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  float3 p = closest_point_at(f, idx[t], ny, nz, hx, hy, hz, h);
+  const long long syz = (long long)ny * nz;
+  for (int s = 1; s < steps; ++s) {
+    float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
+    float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
+    cubic_w(p.x - fx, wx); cubic_w(p.y - fy, wy); cubic_w(p.z - fz, wz);
+    cubic_dw(p.x - fx, dx); cubic_dw(p.y - fy, dy); cubic_dw(p.z - fz, dz);
+    const long long b0 = ((long long)fx - 1) * syz + ((long long)fy - 1) * nz + ((long long)fz - 1);
+    float v = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int a = 0; a < 4; ++a)
+      for (int b = 0; b < 4; ++b)
+        for (int c = 0; c < 4; ++c) {
+          float q = __ldg(f + b0 + a * syz + b * nz + c);
+          v = v + wx[a] * wy[b] * wz[c] * q;
+          gx = gx + dx[a] * wy[b] * wz[c] * q;
+          gy = gy + wx[a] * dy[b] * wz[c] * q;
+          gz = gz + wx[a] * wy[b] * dz[c] * q;
+        }
+    float g2 = fmaxf(gx * gx + gy * gy + gz * gz, 1e-30f);
+    float length = fabsf(v) / sqrtf(g2);
+    float cap = 1.25f * fabsf(v) / h + 0.25f;
+    float sc = v / g2 * fminf(cap / fmaxf(length, 1e-30f), 1.0f);
+    p.x = fminf(fmaxf(p.x - sc * gx, 1.0f), hx);
+    p.y = fminf(fmaxf(p.y - sc * gy, 1.0f), hy);
+    p.z = fminf(fmaxf(p.z - sc * gz, 1.0f), hz);
+  }
+  out[3 * t] = p.x;
+  out[3 * t + 1] = p.y;
+  out[3 * t + 2] = p.z;
+}
+
+__global__ void k_cube_plane(const float* __restrict__ s, const float* __restrict__ a, const float* __restrict__ b,
+                             const float* __restrict__ c, long long m, float* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  out[t] = cube_plane_fraction(s[t], a[t], b[t], c[t]);
+}
+
+}  // namespace svie
+
+extern "C" {
+
+int svie_central_gradient(const float* flat, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz,
+                          float* out, void* stream) {
+  SVIE_CHECK_M("svie_central_gradient", m);
+  k_central_gradient<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, idx, m, sx, sy, sz,
+                                                                                          out);
+  return launch_status("svie_central_gradient");
+}
+
+int svie_closest_points_newton(const float* flat, const int32_t* idx, int64_t m, int ny, int nz, float hi_x,
+                               float hi_y, float hi_z, float h, int newton_steps, float* out, void* stream) {
+  SVIE_CHECK_M("svie_closest_points_newton", m);
+  if (newton_steps < 1) {
+    set_error("svie_closest_points_newton: newton_steps must be >= 1");
+    return SVIE_ERR_ARG;
+  }
+  k_closest_newton<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(
+      flat, idx, m, ny, nz, hi_x, hi_y, hi_z, h, newton_steps, out);
+  return launch_status("svie_closest_points_newton");
+}
+
+int svie_cube_plane_fraction(const float* s, const float* a, const float* b, const float* c, int64_t m, float* out,
+                             void* stream) {
+  SVIE_CHECK_M("svie_cube_plane_fraction", m);
+  k_cube_plane<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(s, a, b, c, m, out);
+  return launch_status("svie_cube_plane_fraction");
+}
+
+}  // extern "C"
+
+namespace svie {
+__global__ void k_dense_occ(const float* __restrict__ phi, long long n, float* __restrict__ occ) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    occ[e] = phi[e] < 0.0f ? 1.0f : 0.0f;
+}
+}  // namespace svie
+
+// occ = (phi < 0) on every node (the dense part of levelset.py:119).
+extern "C" int svie_dense_occupancy(const float* phi, int64_t n, float* occ, void* stream) {
+  if (!phi || !occ || n <= 0) {
+    svie::set_error("svie_dense_occupancy: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  svie::k_dense_occ<<<svie::blocks_for(n, 256, 152 * 32), 256, 0, (cudaStream_t)stream>>>(phi, n, occ);
+  return svie::launch_status("svie_dense_occupancy");
+}

@@ -1,0 +1,265 @@
+"""Narrow-band level set on a CUDA device (reference svierosion/levelset.py).
+
+``phi`` is a dense float32 CUDA tensor (negative inside), the band is the
+ascending list of flat indices with ``|phi| < width * h`` (clamped to
+``+-width * h`` elsewhere), at least :data:`MARGIN` cells from the boundary.
+Besides the reference's state the level set keeps, for the fused stages:
+
+* ``band32`` -- the band as int32 (``band`` is the int64 view of the API);
+* ``occ``    -- the dense occupancy ``(phi < 0)`` with the band's cell
+  fractions, maintained incrementally: off the band phi only changes at a
+  band rebuild, so only band entries are rewritten between rebuilds;
+* ``static_inside`` -- the number of nodes off the band with ``phi < 0``,
+  which turns the solid volume into a band-only float64 reduction.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .grid import Grid, get_device
+
+MARGIN = 4  # cells between any band node and the grid boundary (levelset.py:22)
+
+
+def dilate(mask: torch.Tensor, steps: int = 1) -> torch.Tensor:
+    """Binary dilation by the (2 steps + 1)^3 box (levelset.py:25-34)."""
+    m = mask.to(torch.uint8).contiguous()
+    out = torch.empty_like(m)
+    tmp = torch.empty_like(m)
+    nx, ny, nz = m.shape
+    nat.call("svie_dilate", nat.ptr(m), nx, ny, nz, int(steps), nat.ptr(out), nat.ptr(tmp), nat.stream())
+    return out.view(torch.bool)
+
+
+def cube_plane_fraction(s, a, b, c):
+    """Volume fraction of the unit cube below a plane (levelset.py:37-48)."""
+    from .kernels import cube_plane_fraction as f
+    return f(s, a, b, c)
+
+
+def _read(t: torch.Tensor, dtype: np.dtype):
+    return np.frombuffer(t.cpu().numpy().tobytes(), dtype=dtype)[0]
+
+
+class LevelSet:
+    """A level set function with an explicitly stored narrow band (levelset.py:51-183)."""
+
+    def __init__(self, phi: torch.Tensor, grid: Grid, width: float = 6.0):
+        if tuple(phi.shape) != tuple(grid.shape):
+            raise ValueError("phi shape does not match grid")
+        if grid.size >= 2 ** 31:
+            raise ValueError("grids are limited to 2^31 nodes (int32 node indices)")
+        self.grid = grid
+        self.h = float(grid.spacing)
+        self.width = float(width)
+        dev = phi.device if phi.is_cuda else get_device()
+        self.phi = phi.to(device=dev, dtype=torch.float32).contiguous()
+        self.device = self.phi.device
+        self.strides = tuple(int(s) for s in grid.strides)
+        self.occ = torch.empty(grid.size, dtype=torch.float32, device=self.device)
+        self.occ_current = False
+        self._info = torch.zeros(nat.BAND_INFO_BYTES, dtype=torch.uint8, device=self.device)
+        self._vstats = torch.zeros(nat.STATS_BYTES, dtype=torch.uint8, device=self.device)
+        self._band64 = None
+        self.last_flags = (1, 1)
+        self.rebuild_band()
+
+    # ------------------------------------------------------------ band
+    @property
+    def flat(self) -> torch.Tensor:
+        return self.phi.view(-1)
+
+    @property
+    def band(self) -> torch.Tensor:
+        """Band as int64 flat indices (the reference's dtype)."""
+        if self._band64 is None:
+            self._band64 = self.band32.to(torch.int64)
+        return self._band64
+
+    @band.setter
+    def band(self, idx: torch.Tensor) -> None:
+        self.band32 = idx.to(device=self.device, dtype=torch.int32).contiguous()
+        self._band64 = None
+        self.occ_current = False
+
+    def rebuild_band(self) -> None:
+        """Clamp phi to +-width*h and list |phi| < width*h (1 - 1e-5) (levelset.py:70-77)."""
+        cap = self.width * self.h
+        n = self.grid.size
+        nx, ny, nz = self.grid.shape
+        sc = nat.scratch(self.device)
+        wsb = nat.lib().svie_band_workspace_bytes(n)
+        ws = sc.get("band", wsb)
+        thresh = nat.f32(cap * (1 - 1e-5))
+        nat.call("svie_band_scan", nat.ptr(self.flat), n, nat.f32(cap), thresh, nat.ptr(ws), ws.numel(),
+                 nat.ptr(self._info), nat.stream())
+        count = int(_read(self._info, nat.BAND_INFO_DTYPE)["count"])
+        band = torch.empty(count, dtype=torch.int32, device=self.device)
+        nat.call("svie_band_write", nat.ptr(self.flat), nx, ny, nz, thresh, nat.ptr(ws), ws.numel(), nat.ptr(band),
+                 count, nat.ptr(self.occ), nat.ptr(self._info), nat.stream())
+        info = _read(self._info, nat.BAND_INFO_DTYPE)
+        self.band32 = band
+        self._band64 = None
+        self.static_inside = int(info["static_inside"])
+        self.band_lo = tuple(int(v) for v in info["lo"])
+        self.band_hi = tuple(int(v) for v in info["hi"])
+        self.inside_lo = tuple(int(v) for v in info["ilo"])
+        self.inside_hi = tuple(int(v) for v in info["ihi"])
+        self.occ_current = False
+        if count:
+            shape = self.grid.shape
+            for ax in range(3):
+                if self.band_lo[ax] < MARGIN or self.band_hi[ax] > shape[ax] - 1 - MARGIN:
+                    raise RuntimeError("narrow band reaches the grid boundary; enlarge the padding")
+
+    def _check_margin(self, idx: torch.Tensor) -> None:
+        """levelset.py:79-86 for an arbitrary index list."""
+        if idx.numel() == 0:
+            return
+        shape = self.grid.shape
+        for ax, s in enumerate(self.strides):
+            coord = (idx // s) % shape[ax]
+            if int(coord.min()) < MARGIN or int(coord.max()) > shape[ax] - 1 - MARGIN:
+                raise RuntimeError("narrow band reaches the grid boundary; enlarge the padding")
+
+    def interface_nodes(self, idx: torch.Tensor | None = None) -> torch.Tensor:
+        """Band nodes having a 6-neighbour of the opposite sign (levelset.py:88-91)."""
+        from .kernels import interface_mask
+        idx32 = self.band32 if idx is None else idx.to(torch.int32).contiguous()
+        m = idx32.numel()
+        if m == 0:
+            return torch.empty(0, dtype=torch.int64, device=self.device)
+        mask = interface_mask(self.flat, idx32, *self.strides).view(torch.uint8)
+        sc = nat.scratch(self.device)
+        ws = sc.get("select", nat.lib().svie_band_workspace_bytes(m))
+        cnt = sc.get("select_count", 8)
+        nat.call("svie_mask_scan", nat.ptr(mask), m, nat.ptr(ws), ws.numel(), nat.ptr(cnt), nat.stream())
+        k = int(cnt[:8].cpu().view(torch.int64)[0])
+        out = torch.empty(k, dtype=torch.int32, device=self.device)
+        nat.call("svie_mask_select", nat.ptr(mask), nat.ptr(idx32), m, nat.ptr(ws), ws.numel(), nat.ptr(out), k,
+                 nat.stream())
+        return out.to(torch.int64)
+
+    def _volume_kernel(self, write_occ: bool):
+        sc = nat.scratch(self.device)
+        m = self.band32.numel()
+        ws = sc.get("volume", nat.lib().svie_volume_workspace_bytes(m))
+        nat.call("svie_band_volume", nat.ptr(self.flat), nat.ptr(self.band32), m, *self.strides,
+                 nat.ptr(self.occ) if write_occ else None, nat.ptr(ws), ws.numel(), nat.ptr(self._vstats),
+                 nat.stream())
+        if write_occ:
+            self.occ_current = True
+
+    def has_interface(self) -> bool:
+        """Band has both signs (levelset.py:93-95)."""
+        self._volume_kernel(False)
+        st = _read(self._vstats, nat.STATS_DTYPE)
+        return bool(st["any_neg"]) and bool(st["any_pos"])
+
+    # ---------------------------------------------------- derivatives
+    def central_gradient(self, idx: torch.Tensor) -> torch.Tensor:
+        """Second-order central gradient in phi per cell, (m, 3) (levelset.py:98-101)."""
+        i = idx.to(torch.int32).contiguous()
+        out = torch.empty((i.numel(), 3), dtype=torch.float32, device=self.device)
+        nat.call("svie_central_gradient", nat.ptr(self.flat), nat.ptr(i), i.numel(), *self.strides, nat.ptr(out),
+                 nat.stream())
+        return out
+
+    def godunov_norm_inward(self, idx: torch.Tensor) -> torch.Tensor:
+        from .kernels import godunov_inward
+        return godunov_inward(self.flat, idx, *self.strides, 1.0 / self.h)
+
+    def principal_curvatures(self, idx: torch.Tensor):
+        from .kernels import principal_curvatures
+        return principal_curvatures(self.flat, idx, *self.strides, self.h)
+
+    # ------------------------------------------------- volume fractions
+    def cell_fractions(self, idx: torch.Tensor | None = None) -> torch.Tensor:
+        from .kernels import cell_fractions
+        return cell_fractions(self.flat, self.band32 if idx is None else idx, *self.strides)
+
+    def dense_fractions(self) -> torch.Tensor:
+        """Dense occupancy field (levelset.py:117-121), recomputed from phi."""
+        f = torch.empty(self.grid.size, dtype=torch.float32, device=self.device)
+        nat.call("svie_dense_occupancy", nat.ptr(self.flat), self.grid.size, nat.ptr(f), nat.stream())
+        nat.call("svie_scatter_fractions", nat.ptr(self.flat), nat.ptr(self.band32), self.band32.numel(),
+                 *self.strides, nat.ptr(f), nat.stream())
+        return f.view(self.grid.shape)
+
+    def refresh_occupancy(self) -> None:
+        """Bring the maintained occupancy up to date with the band values."""
+        if not self.occ_current:
+            nat.call("svie_scatter_fractions", nat.ptr(self.flat), nat.ptr(self.band32), self.band32.numel(),
+                     *self.strides, nat.ptr(self.occ), nat.stream())
+            self.occ_current = True
+
+    def volume_async(self) -> None:
+        """Launch the band volume reduction (result in the volume stats)."""
+        self._volume_kernel(True)
+
+    def volume_from_stats(self, st) -> float:
+        return (self.static_inside + float(st["fsum"])) * self.h ** 3
+
+    def volume(self) -> float:
+        """Solid volume (levelset.py:123-126): off-band inside count + float64 sum of band fractions."""
+        self._volume_kernel(True)
+        st = _read(self._vstats, nat.STATS_DTYPE)
+        self.last_flags = (int(st["any_neg"]), int(st["any_pos"]))
+        return self.volume_from_stats(st)
+
+    # ----------------------------------------------------- projection
+    def closest_points(self, idx: torch.Tensor, newton_steps: int = 1) -> torch.Tensor:
+        """Projection of nodes onto the zero level set, index coordinates (levelset.py:129-146)."""
+        nx, ny, nz = self.grid.shape
+        i = idx.to(torch.int32).contiguous()
+        out = torch.empty((i.numel(), 3), dtype=torch.float32, device=self.device)
+        nat.call("svie_closest_points_newton", nat.ptr(self.flat), nat.ptr(i), i.numel(), ny, nz, nx - 3.001,
+                 ny - 3.001, nz - 3.001, self.h, int(newton_steps), nat.ptr(out), nat.stream())
+        return out
+
+    def clamp_to_interior(self, p: torch.Tensor) -> torch.Tensor:
+        hi = torch.tensor([n - 3.001 for n in self.grid.shape], device=p.device, dtype=p.dtype)
+        return torch.minimum(p.clamp_min(1.0), hi)
+
+    # --------------------------------------------------- reinitialisation
+    def reinitialize(self, iterations: int = 12, cfl: float = 0.45, dilation: int = 3) -> None:
+        """Subcell-fixed PDE reinitialisation (Min 2010) on the dilated band (levelset.py:154-183)."""
+        n = self.grid.size
+        nx, ny, nz = self.grid.shape
+        sc = nat.scratch(self.device)
+        mask = sc.get("reinit_mask", n)
+        tmp = sc.get("reinit_tmp", n)
+        nat.call("svie_reinit_mask", nat.ptr(self.band32), self.band32.numel(), nx, ny, nz, int(dilation), MARGIN,
+                 nat.ptr(mask), nat.ptr(tmp), nat.stream())
+        ws = sc.get("band", nat.lib().svie_band_workspace_bytes(n))
+        cnt = sc.get("reinit_count", 8)
+        nat.call("svie_mask_scan", nat.ptr(mask), n, nat.ptr(ws), ws.numel(), nat.ptr(cnt), nat.stream())
+        m = int(cnt[:8].cpu().view(torch.int64)[0])
+        idx = sc.get("reinit_idx", 4 * max(m, 1))[:4 * m].view(torch.int32)
+        nat.call("svie_mask_write", nat.ptr(mask), n, nat.ptr(ws), ws.numel(), nat.ptr(idx), m, nat.stream())
+        geo = sc.get("reinit_geo", nat.lib().svie_reinit_geometry_bytes(m))
+        nat.call("svie_reinit_geometry", nat.ptr(self.flat), nat.ptr(idx), m, *self.strides, self.h, cfl,
+                 nat.ptr(geo), nat.stream())
+        phi_tmp = sc.get("reinit_phi", 4 * n)
+        nat.call("svie_reinit_iterate", nat.ptr(self.flat), nat.ptr(phi_tmp), n, nat.ptr(idx), m, *self.strides,
+                 self.h, nat.ptr(geo), int(iterations), nat.stream())
+        self.rebuild_band()
+
+
+# ------------------------------------------------------------- interpolation
+def tricubic(flat: torch.Tensor, shape, p: torch.Tensor) -> torch.Tensor:
+    from . import kernels as K
+    return K.tricubic(flat, int(shape[1]), int(shape[2]), p)
+
+
+def tricubic_with_gradient(flat: torch.Tensor, shape, p: torch.Tensor):
+    from . import kernels as K
+    return K.tricubic_with_gradient(flat, int(shape[1]), int(shape[2]), p)
+
+
+def trilinear(flat: torch.Tensor, shape, p: torch.Tensor) -> torch.Tensor:
+    from . import kernels as K
+    return K.trilinear(flat, int(shape[1]), int(shape[2]), p)

@@ -1,0 +1,133 @@
+"""Spherical volume invariant N_r by FFT convolution (reference svierosion/svi.py).
+
+``N_r(x) = 1 - h^3 (w * f)(x) / |B_r|`` with ``w`` the exact ball/cell overlap
+fractions (float64, computed on the GPU) and ``f`` the cell occupancy.  The
+convolution is the package's own mixed-radix R2C/C2R FFT with the kernel
+spectrum multiply fused into the x pass (csrc/fft.cu).
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .grid import Grid, get_device
+
+
+def ball_cell_weights(radius: float, spacing: float, quad: int = 32) -> np.ndarray:
+    """Exact fractions |B_r(0) cap cell(i,j,k)| / h^3 for |i|,|j|,|k| <= m (svi.py:24-55)."""
+    w = _ball_weights_device(radius, spacing, quad, get_device())
+    return w.cpu().numpy()
+
+
+def _ball_weights_device(radius, spacing, quad, device) -> torch.Tensor:
+    m = nat.lib().svie_ball_half_width(float(radius), float(spacing))
+    if m < 1:
+        raise ValueError("radius and spacing must be positive")
+    side = 2 * m + 1
+    w = torch.empty((side, side, side), dtype=torch.float64, device=device)
+    nat.call("svie_ball_weights", float(radius), float(spacing), int(quad), nat.ptr(w), nat.stream())
+    return w
+
+
+class BallConvolution:
+    """Cached kernel spectrum on a grid; evaluates interior ball volumes (svi.py:58-93)."""
+
+    def __init__(self, grid: Grid, radius: float, device=None, quad: int = 32):
+        self.grid = grid
+        self.radius = float(radius)
+        self.device = get_device(device)
+        w = _ball_weights_device(radius, grid.spacing, quad, self.device)
+        self.m = (w.shape[0] - 1) // 2
+        self.ball_volume = 4.0 / 3.0 * math.pi * radius ** 3
+        self.quadrature_volume = float(w.sum()) * grid.spacing ** 3
+        if any(2 * self.m + 1 > n for n in grid.shape):
+            raise ValueError("ball kernel larger than the grid")
+        L = nat.lib()
+        if not all(L.svie_conv_supported(int(n)) for n in grid.shape):
+            raise ValueError(f"grid {grid.shape}: every dimension must be 2^a 3^b 5^c 7^d and <= 8192 "
+                             "(use Grid.around(..., fast=True))")
+        nx, ny, nz = grid.shape
+        self.plan = torch.empty(L.svie_conv_plan_bytes(nx, ny, nz), dtype=torch.uint8, device=self.device)
+        init_ws = torch.empty(L.svie_conv_init_workspace_bytes(nx, ny, nz, self.m), dtype=torch.uint8,
+                              device=self.device)
+        nat.call("svie_conv_plan_init", nat.ptr(self.plan), nx, ny, nz, nat.ptr(w), self.m, nat.ptr(init_ws),
+                 init_ws.numel(), nat.stream())
+        del init_ws
+        self.workspace_bytes = L.svie_conv_workspace_bytes(nx, ny, nz)
+        self._khat = None
+
+    @property
+    def kernel_hat(self) -> torch.Tensor:
+        """complex64 [nx, ny, nz/2+1] spectrum of the wrapped kernel (svi.py:76-81)."""
+        if self._khat is None:
+            nx, ny, nz = self.grid.shape
+            k = torch.empty((nx, ny, nz // 2 + 1), dtype=torch.complex64, device=self.device)
+            nat.call("svie_conv_kernel_hat", nat.ptr(self.plan), nx, ny, nz, nat.ptr(k), nat.stream())
+            self._khat = k
+        return self._khat
+
+    def apply_into(self, f: torch.Tensor, out: torch.Tensor, alpha: float, beta: float, events=None) -> torch.Tensor:
+        """out = beta + alpha * G * (w (*) f), G = number of nodes (unnormalised FFT pair).
+
+        ``events``: optional six timing events recorded around the five passes."""
+        nx, ny, nz = self.grid.shape
+        f = f.reshape(-1)
+        if f.dtype != torch.float32 or not f.is_contiguous():
+            f = f.to(torch.float32).contiguous()
+        ws = nat.scratch(self.device).get("conv", self.workspace_bytes)
+        if events is None:
+            nat.call("svie_conv_apply", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)),
+                     float(alpha), float(beta), nat.ptr(ws), ws.numel(), nat.stream())
+        else:
+            from .profiling import KernelTimer
+            nat.call("svie_conv_apply_events", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)),
+                     float(alpha), float(beta), nat.ptr(ws), ws.numel(), KernelTimer.handles(events), nat.stream())
+        return out
+
+    def interior_volume(self, fractions: torch.Tensor) -> torch.Tensor:
+        """Dense |B_r(x) cap Omega| (svi.py:84-88)."""
+        out = torch.empty(self.grid.shape, dtype=torch.float32, device=self.device)
+        return self.apply_into(fractions, out, self.grid.spacing ** 3 / self.grid.size, 0.0)
+
+    def exterior_fraction(self, fractions: torch.Tensor) -> torch.Tensor:
+        """Dense N_r(x) = 1 - |B_r(x) cap Omega| / |B_r| (svi.py:90-93)."""
+        out = torch.empty(self.grid.shape, dtype=torch.float32, device=self.device)
+        return self.exterior_fraction_into(fractions, out)
+
+    def exterior_fraction_into(self, fractions: torch.Tensor, out: torch.Tensor, events=None) -> torch.Tensor:
+        a = -self.grid.spacing ** 3 / (self.ball_volume * self.grid.size)
+        return self.apply_into(fractions, out, a, 1.0, events=events)
+
+
+def sphere_exterior_fraction(radius_ball: float, radius_sphere: float) -> float:
+    """Exact N_r at a point of a sphere of radius R (svi.py:96-101)."""
+    r, R = radius_ball, radius_sphere
+    if r > 2 * R:
+        return 1.0 - (R / r) ** 3
+    return 0.5 + 3.0 * r / (16.0 * R)
+
+
+def rfftn(f: torch.Tensor, conv: BallConvolution) -> torch.Tensor:
+    """Forward 3-D real FFT with the package's kernels; complex64 [nx, ny, nz/2+1]."""
+    nx, ny, nz = conv.grid.shape
+    row = nat.lib().svie_conv_spectrum_row(nz)
+    spec = torch.empty((nx, ny, row), dtype=torch.complex64, device=conv.device)
+    f = f.reshape(-1).to(torch.float32).contiguous()
+    nat.call("svie_rfft3", nat.ptr(conv.plan), nx, ny, nz, nat.ptr(f), nat.ptr(spec), nat.stream())
+    return spec[:, :, : nz // 2 + 1]
+
+
+def irfftn(spec: torch.Tensor, conv: BallConvolution) -> torch.Tensor:
+    """Inverse of :func:`rfftn` (normalised like torch.fft.irfftn)."""
+    nx, ny, nz = conv.grid.shape
+    row = nat.lib().svie_conv_spectrum_row(nz)
+    buf = torch.zeros((nx, ny, row), dtype=torch.complex64, device=conv.device)
+    buf[:, :, : nz // 2 + 1] = spec
+    out = torch.empty(conv.grid.shape, dtype=torch.float32, device=conv.device)
+    nat.call("svie_irfft3", nat.ptr(conv.plan), nx, ny, nz, nat.ptr(buf), nat.ptr(out), 1.0 / conv.grid.size, 0.0,
+             nat.stream())
+    return out

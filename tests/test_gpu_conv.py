@@ -1,0 +1,115 @@
+"""Ball weights, the hand-written 3-D FFT and the N_r convolution."""
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+if torch.cuda.is_available():
+    import svierosion_gb300 as S
+    from svierosion_gb300 import svi
+    from svierosion_gb300.grid import Grid
+
+
+def test_ball_weights(golden):
+    s = golden("svi_conv")
+    np.testing.assert_allclose(svi.ball_cell_weights(1.0, 1 / 3.3), s["w_r33"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(svi.ball_cell_weights(0.1, 1 / 64), s["w_r64"], rtol=0, atol=1e-12)
+    for ratio in (3.3, 8.0, 12.7):  # test_flows.py:41-44
+        w = svi.ball_cell_weights(1.0, 1.0 / ratio)
+        assert abs(w.sum() / ratio ** 3 / (4 * math.pi / 3) - 1.0) < 1e-4
+
+
+@pytest.mark.parametrize("shape", [(16, 18, 20), (20, 21, 25), (27, 28, 30), (90, 90, 90), (45, 60, 49),
+                                   (64, 48, 35), (40, 42, 36)])
+def test_rfft_matches_numpy(shape):
+    rng = np.random.default_rng(sum(shape))
+    f = rng.standard_normal(shape).astype(np.float32)
+    g = Grid((0.0, 0.0, 0.0), 1.0, shape)
+    conv = S.BallConvolution(g, 2.0)
+    spec = svi.rfftn(torch.from_numpy(f).cuda(), conv)
+    ref = np.fft.rfftn(f.astype(np.float64))
+    scale = np.abs(ref).max()
+    assert np.abs(spec.cpu().numpy() - ref).max() < 2e-6 * scale * math.log2(f.size)
+    back = svi.irfftn(spec, conv)
+    assert np.abs(back.cpu().numpy() - f).max() < 2e-6 * math.log2(f.size) * np.abs(f).max()
+
+
+def test_kernel_hat_and_exterior_fraction(golden):
+    s = golden("svi_conv")
+    shape = tuple(int(v) for v in s["shape"])
+    g = Grid((0.0, 0.0, 0.0), float(s["h"]), shape)
+    conv = S.BallConvolution(g, float(s["radius"]))
+    assert conv.m == int(s["m"])
+    assert abs(conv.quadrature_volume - float(s["quadrature_volume"])) < 1e-10
+    kh = conv.kernel_hat.cpu().numpy()
+    np.testing.assert_allclose(kh.real, s["khat_re"], atol=1e-4 * np.abs(s["khat_re"]).max())
+    N = conv.exterior_fraction(torch.from_numpy(s["fractions"]).cuda())
+    assert float(np.abs(N.cpu().numpy() - s["N"]).max()) < 2e-6
+    # interior volume + exterior fraction consistency
+    iv = conv.interior_volume(torch.from_numpy(s["fractions"]).cuda())
+    np.testing.assert_allclose(1 - iv.cpu().numpy() / conv.ball_volume, N.cpu().numpy(), atol=2e-6)
+
+
+@pytest.mark.parametrize("ratio,tol", [(8, 3e-4), (16, 6e-5)])
+def test_sphere_exterior_fraction(ratio, tol):
+    # known answer N_r = 1/2 + 3r/(16R) on a sphere (test_flows.py:46-56)
+    R, r = 1.0, 0.4
+    h = r / ratio
+    ctr = np.array([0.0123, -0.0311, 0.0217])
+    g = Grid.around([-R] * 3, [R] * 3, h, padding=r + 10 * h)
+    X, Y, Z = [torch.tensor(a, device="cuda") for a in np.meshgrid(*g.axes(), indexing="ij")]
+    phi = torch.sqrt((X - ctr[0]) ** 2 + (Y - ctr[1]) ** 2 + (Z - ctr[2]) ** 2) - R
+    ls = S.LevelSet(phi.float(), g, width=6)
+    conv = S.BallConvolution(g, r)
+    N = conv.exterior_fraction(ls.dense_fractions())
+    pts = ls.closest_points(ls.interface_nodes())
+    from svierosion_gb300.levelset import tricubic
+    vals = tricubic(N.view(-1), g.shape, pts)
+    err = (vals - svi.sphere_exterior_fraction(r, R)).abs().max().item()
+    assert err < tol
+
+
+def test_flat_plane_is_one_half():
+    # test_flows.py:58-75
+    h, r = 0.05, 0.3
+    g = Grid.around([-1] * 3, [1] * 3, h, padding=r + 10 * h)
+    X, Y, Z = [torch.tensor(a, device="cuda") for a in np.meshgrid(*g.axes(), indexing="ij")]
+    n = torch.tensor([0.3, -0.5, 0.81], dtype=torch.float64)
+    n /= n.norm()
+    lin = n[0] * X + n[1] * Y + n[2] * Z - 0.0131
+    phi = torch.maximum(lin, torch.sqrt(X * X + Y * Y + Z * Z) - 0.9).float()
+    ls = S.LevelSet(phi, g)
+    conv = S.BallConvolution(g, r)
+    N = conv.exterior_fraction(ls.dense_fractions())
+    idx = ls.interface_nodes()
+    x = g.node_coords(idx).cpu()
+    keep = ((x @ n - 0.0131).abs() < 2 * h) & (x.norm(dim=1) < 0.45)
+    from svierosion_gb300.levelset import tricubic
+    vals = tricubic(N.view(-1), g.shape, ls.closest_points(idx[keep.to(idx.device)]))
+    assert (vals - 0.5).abs().max().item() < 2e-4
+
+
+def test_convolution_vs_oracle_float64():
+    """N_r error of the float32 path against a float64 evaluation of the same discrete convolution."""
+    R, h, r = 1.0, 0.05, 0.4
+    g = Grid.around([-R] * 3, [R] * 3, h, padding=r + 10 * h)
+    X, Y, Z = np.meshgrid(*g.axes(), indexing="ij")
+    phi = (np.sqrt(X ** 2 + Y ** 2 + (Z / 0.8) ** 2) - R).astype(np.float32)
+    band = O.rebuild_band(phi.reshape(-1).copy(), 6.0, h)
+    f = O.dense_fractions(np.clip(phi.reshape(-1), -6 * h, 6 * h).astype(np.float32), band, g.shape).reshape(g.shape)
+    w = O.ball_cell_weights(r, h)
+    m = (w.shape[0] - 1) // 2
+    kern = np.zeros(g.shape)
+    ii = np.arange(-m, m + 1)
+    kern[(ii % g.shape[0])[:, None, None], (ii % g.shape[1])[None, :, None], (ii % g.shape[2])[None, None, :]] = w
+    g64 = np.fft.irfftn(np.fft.rfftn(f.astype(np.float64)) * np.fft.rfftn(kern), s=g.shape) * h ** 3
+    N64 = 1 - g64 / (4 / 3 * np.pi * r ** 3)
+    conv = S.BallConvolution(g, r)
+    N = conv.exterior_fraction(torch.from_numpy(f).cuda()).cpu().numpy()
+    assert np.abs(N - N64).max() < 1e-5

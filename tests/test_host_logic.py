@@ -1,0 +1,64 @@
+"""Host-side logic that needs no GPU: grids, law parameters, workload generators."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from svierosion_gb300 import shapes
+from svierosion_gb300.api import ErosionParams, make_grid
+from svierosion_gb300.flows import GaussCurvatureLaw, MeanCurvatureLaw, SVIPowerLaw
+from svierosion_gb300.grid import Grid, next_fast_size
+
+
+def test_next_fast_size_and_grid():
+    for n in range(1, 600):
+        assert next_fast_size(n) == O.next_fast_size(n)
+    g = Grid.around([-0.5] * 3, [0.5] * 3, 1 / 64, 12 / 64)
+    assert g.shape == O.grid_around([-0.5] * 3, [0.5] * 3, 1 / 64, 12 / 64)[2] == (90, 90, 90)
+
+
+def test_cube_matches_reference_fixture(golden):
+    d = golden("sdf")
+    c = shapes.cube(1.0)
+    assert np.array_equal(c.faces, d["cube_f"]) and np.allclose(c.vertices, d["cube_v"])
+
+
+def test_make_grid_configs():
+    p = ErosionParams(law="svi", radius=0.1, k=1, s=1, t=0.93, resolution=64)
+    assert make_grid(shapes.cube(1.0), p).shape == (90, 90, 90)
+    m = shapes.fragment(4, seed=0)
+    L = float((m.bounds[1] - m.bounds[0]).max())
+    assert abs(L - 2.077) < 2e-3
+    p = ErosionParams(law="svi", radius=0.05 * L, k=1, s=1, t=0.93, resolution=400)
+    g = make_grid(m, p)
+    assert all(next_fast_size(n) == n for n in g.shape)
+
+
+def test_fragment_generator():
+    m = shapes.fragment(6, seed=0)
+    assert len(m.faces) == 81920 and m.is_watertight() and m.is_consistently_oriented()
+    assert abs(m.volume() - 1.6556) < 1e-3
+    L = float((m.bounds[1] - m.bounds[0]).max())
+    assert abs(L - 2.078) < 1e-3
+
+
+def test_law_parameters_match_oracle():
+    for k, s, t in ((1, 1, 0.93), (2, 1, 0.95), (0, 0, None), (1, 0, None)):
+        a = SVIPowerLaw(0.1, k, s, t)
+        b = O.SVILaw(0.1, k, s, t)
+        assert a.n_cap == b.n_cap
+    with pytest.raises(ValueError):
+        SVIPowerLaw(0.1, 1, 1, 0.4)
+    with pytest.raises(ValueError):
+        SVIPowerLaw(-1.0)
+    with pytest.raises(ValueError):
+        GaussCurvatureLaw(0.25)
+    assert MeanCurvatureLaw(1.0).params()["law"] == "mean_curvature"
+
+
+def test_params_make_law_auto_delta():
+    p = ErosionParams(law="gauss", alpha=0.25)
+    law = p.make_law(length_scale=2.0)
+    assert law.delta == 0.25
+    p = ErosionParams(law="mean", alpha=0.5)
+    assert p.make_law(length_scale=2.0).delta == 0.5

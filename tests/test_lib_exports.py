@@ -1,0 +1,65 @@
+"""CPU checks of the C ABI: the library builds, loads and exports every symbol
+that include/svie.h declares (no compute calls without a GPU)."""
+
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from svierosion_gb300 import _native, build
+
+    if not _native.LIB_PATH.exists():
+        build.build()
+    return _native.load()
+
+
+def declared_functions():
+    text = (ROOT / "include" / "svie.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(svie_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    assert "svie_stage_svi" in names and "svie_conv_apply" in names and "svie_band_scan" in names
+    assert len(names) >= 50
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_table_matches_header(lib):
+    from svierosion_gb300 import _native
+
+    declared = set(declared_functions())
+    bound = set(_native.exported_names())
+    assert bound <= declared, bound - declared
+
+
+def test_size_queries_without_gpu(lib):
+    assert lib.svie_version() == 1
+    assert lib.svie_conv_spectrum_row(245) == 128
+    assert lib.svie_conv_supported(448) == 1 and lib.svie_conv_supported(11) == 0
+    assert lib.svie_ball_half_width(0.1, 1 / 64) == 7
+    assert lib.svie_conv_workspace_bytes(448, 336, 245) >= 448 * 336 * 123 * 8
+    assert lib.svie_band_workspace_bytes(1 << 20) > 0
+
+
+def test_no_cpu_fallback():
+    import torch
+    import svierosion_gb300 as S
+    from svierosion_gb300 import kernels as K
+
+    flat = torch.zeros(1000)
+    with pytest.raises((ValueError, RuntimeError)):
+        K.godunov_inward(flat, torch.arange(10), 100, 10, 1, 1.0)
+    if not torch.cuda.is_available():
+        with pytest.raises(RuntimeError):
+            S.get_device()
