@@ -130,6 +130,8 @@ def algorithmic_bytes(shape, band: int) -> dict:
         # idx 4 + phi 4 + N at the closest point 4 + write L 4 (+ u0 4 in stage 0)
         "stage_svi": 16 * band,
         "scatter_fractions": 8 * band,
+        "rk_stage": 16 * band,       # idx, u0, L read, phi written
+        "volume": 8 * band,          # idx + phi (fractions recomputed)
     }
 
 

@@ -104,11 +104,16 @@ struct OpMaxI { SVIE_DEV int operator()(int a, int b) const { return max(a, b); 
 
 // ----------------------------------------------------------- stencil maths
 // Jiang-Peng WENO5 derivative from five differences (reference kernels.py:83-97).
+// Divisions by constants are multiplications by their float reciprocals and
+// the three weights use IEEE reciprocals: the result differs from the
+// reference's division form by a few float32 ulps.
 SVIE_DEV float weno5(float v1, float v2, float v3, float v4, float v5) {
   const float c1312 = (float)(13.0 / 12.0);
-  float p1 = v1 / 3.0f - 7.0f * v2 / 6.0f + 11.0f * v3 / 6.0f;
-  float p2 = -v2 / 6.0f + 5.0f * v3 / 6.0f + v4 / 3.0f;
-  float p3 = v3 / 3.0f + 5.0f * v4 / 6.0f - v5 / 6.0f;
+  const float r3 = (float)(1.0 / 3.0), r6 = (float)(1.0 / 6.0), c76 = (float)(7.0 / 6.0);
+  const float c116 = (float)(11.0 / 6.0), c56 = (float)(5.0 / 6.0);
+  float p1 = v1 * r3 - v2 * c76 + v3 * c116;
+  float p2 = -v2 * r6 + v3 * c56 + v4 * r3;
+  float p3 = v3 * r3 + v4 * c56 - v5 * r6;
   float e1 = v1 - 2.0f * v2 + v3, f1 = v1 - 4.0f * v2 + 3.0f * v3;
   float e2 = v2 - 2.0f * v3 + v4, f2 = v2 - v4;
   float e3 = v3 - 2.0f * v4 + v5, f3 = 3.0f * v3 - 4.0f * v4 + v5;
@@ -118,9 +123,9 @@ SVIE_DEV float weno5(float v1, float v2, float v3, float v4, float v5) {
   float vmax = fmaxf(fmaxf(fmaxf(v1 * v1, v2 * v2), fmaxf(v3 * v3, v4 * v4)), v5 * v5);
   float eps = 1e-6f * vmax + 1e-10f;
   float d1 = s1 + eps, d2 = s2 + eps, d3 = s3 + eps;
-  float a1 = 0.1f / (d1 * d1);
-  float a2 = 0.6f / (d2 * d2);
-  float a3 = 0.3f / (d3 * d3);
+  float a1 = 0.1f * __frcp_rn(d1 * d1);
+  float a2 = 0.6f * __frcp_rn(d2 * d2);
+  float a3 = 0.3f * __frcp_rn(d3 * d3);
   return (a1 * p1 + a2 * p2 + a3 * p3) / (a1 + a2 + a3);
 }
 
@@ -155,20 +160,21 @@ SVIE_DEV float cube_plane_fraction(float s, float a, float b, float c) {
   y = fmaxf(y, 0.0f);
   const float tiny = 1e-12f;
   float bs = fmaxf(b, tiny), cs = fmaxf(c, tiny);
+  float rb = __frcp_rn(bs), rc = __frcp_rn(cs), ra6 = __frcp_rn(6.0f * a);
   float q = 3.0f * y * y - 3.0f * y * c + c * c;
   float H;
   if (y <= c) {
-    H = (y * y * y) / (bs * cs);
+    H = (y * y * y) * (rb * rc);
   } else if (y <= b) {
-    H = q / bs;
+    H = q * rb;
   } else if (y <= b + c) {
     float u = fmaxf(y - b, 0.0f);
-    H = (q - (u * u * u) / cs) / bs;
+    H = (q - (u * u * u) * rc) * rb;
   } else {
     H = 3.0f * (2.0f * y - b - c);
   }
   float ua = fmaxf(y - a, 0.0f);
-  float F = H / (6.0f * a) - (ua * ua * ua) / (6.0f * a * bs * cs);
+  float F = H * ra6 - (ua * ua * ua) * (ra6 * rb * rc);
   F = flip ? 1.0f - F : F;
   return fminf(fmaxf(F, 0.0f), 1.0f);
 }
@@ -181,11 +187,12 @@ SVIE_DEV float cell_fraction_at(const float* __restrict__ f, long long i, long l
   float gy = 0.5f * (__ldg(f + i + sy) - __ldg(f + i - sy));
   float gz = 0.5f * (__ldg(f + i + sz) - __ldg(f + i - sz));
   float gn = fmaxf(sqrtf(gx * gx + gy * gy + gz * gz), 1e-30f);
-  float x = fabsf(gx / gn), y = fabsf(gy / gn), z = fabsf(gz / gn);
+  float rg = __frcp_rn(gn);
+  float x = fabsf(gx * rg), y = fabsf(gy * rg), z = fabsf(gz * rg);
   float hi = fmaxf(fmaxf(x, y), z);
   float lo = fminf(fminf(x, y), z);
   float mid = x + y + z - hi - lo;
-  return cube_plane_fraction(c / gn, hi, mid, lo);
+  return cube_plane_fraction(c * rg, hi, mid, lo);
 }
 
 // First Newton projection to the zero set (reference kernels.py:185-208).
@@ -214,10 +221,11 @@ SVIE_DEV float3 closest_point_at(const float* __restrict__ f, long long i, int n
 
 // Cubic Lagrange weights on nodes -1, 0, 1, 2 (reference kernels.py:134-136).
 SVIE_DEV void cubic_w(float t, float w[4]) {
-  w[0] = -t * (t - 1.0f) * (t - 2.0f) / 6.0f;
-  w[1] = (t + 1.0f) * (t - 1.0f) * (t - 2.0f) / 2.0f;
-  w[2] = -(t + 1.0f) * t * (t - 2.0f) / 2.0f;
-  w[3] = (t + 1.0f) * t * (t - 1.0f) / 6.0f;
+  const float r6 = (float)(1.0 / 6.0);
+  w[0] = -t * (t - 1.0f) * (t - 2.0f) * r6;
+  w[1] = (t + 1.0f) * (t - 1.0f) * (t - 2.0f) * 0.5f;
+  w[2] = -(t + 1.0f) * t * (t - 2.0f) * 0.5f;
+  w[3] = (t + 1.0f) * t * (t - 1.0f) * r6;
 }
 // Their derivatives (reference kernels.py:139-141).
 SVIE_DEV void cubic_dw(float t, float w[4]) {

@@ -32,24 +32,26 @@ constexpr int FFT_MAXN = 8192;  // longest supported axis
 struct AxisPlan {
   int n;
   int nst;
-  int radix[FFT_MAXST];
-  const float2* tw;  // tw[k] = exp(-2 pi i k / n), k < n
+  unsigned long long radices;  // radix of stage s in bits [4s, 4s+4) (no arrays: no local-memory copy)
+  const float2* tw;            // tw[k] = exp(-2 pi i k / n), k < n
 };
 
 static bool factor_axis(int n, AxisPlan* p) {
   if (n < 1 || n > FFT_MAXN) return false;
   static const int rs[] = {8, 7, 6, 5, 4, 3, 2};
   int m = n, st = 0;
+  unsigned long long packed = 0;
   for (int r : rs) {
     while (m % r == 0) {
       if (st >= FFT_MAXST) return false;
-      p->radix[st++] = r;
+      packed |= (unsigned long long)r << (4 * st++);
       m /= r;
     }
   }
   if (m != 1) return false;
   p->n = n;
   p->nst = st;
+  p->radices = packed;
   return true;
 }
 
@@ -174,30 +176,39 @@ SVIE_DEV void dft<6>(float2* x) {
   for (int p = 0; p < 6; ++p) x[p] = y[p];
 }
 
+// Shared-memory index with one pad slot every 16 complex values: the stride-R
+// writes of the early Stockham stages then fall on distinct banks.
+SVIE_DEV int px(int a) { return a + (a >> 4); }
+__host__ __device__ inline int padded_len(int a) { return a + (a >> 4) + 1; }
+
 // One Stockham radix-R stage over `nlines` lines of length n, reading
-// src[line*LS + k] and writing dst (ping-pong buffers, so a thread holds one
-// butterfly at a time).  p = product of the radices already applied.
+// src[line*LS + k] and writing dst (ping-pong buffers).  Warp w takes lines
+// w, w + 8, ...; its lanes take butterflies i = lane, lane + 32, ... of the
+// line, so no division is needed; k = i mod p uses the stage's magic
+// multiplier.  p = product of the radices already applied.
 template <int R>
 SVIE_DEV void fft_stage(const float2* __restrict__ src, float2* __restrict__ dst, int LS, int n, int nlines, int p,
-                        const float2* __restrict__ tw) {
+                        unsigned int pmagic, const float2* __restrict__ tw) {
   const int m = n / R;
-  const int total = m * nlines;
   const int twstep = n / (p * R);
-  for (int b = threadIdx.x; b < total; b += FFT_T) {
-    const int line = b / m, i = b - line * m;
-    const int k = i % p;
-    float2 v[R];
-    const float2* s = src + line * LS + i;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int line = warp; line < nlines; line += FFT_T / 32) {
+    const int base = line * LS;
+    for (int i = lane; i < m; i += 32) {
+      const int k = (p == 1) ? 0 : i - (int)__umulhi((unsigned)i, pmagic) * p;
+      float2 v[R];
 #pragma unroll
-    for (int q = 0; q < R; ++q) v[q] = s[q * m];
-    if (k) {
+      for (int q = 0; q < R; ++q) v[q] = src[px(base + i + q * m)];
+      if (k) {
+        const int tq = k * twstep;
 #pragma unroll
-      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], __ldg(tw + q * k * twstep));
+        for (int q = 1; q < R; ++q) v[q] = cmul(v[q], __ldg(tw + q * tq));
+      }
+      dft<R>(v);
+      const int o = base + (i - k) * R + k;
+#pragma unroll
+      for (int q = 0; q < R; ++q) dst[px(o + q * p)] = v[q];
     }
-    dft<R>(v);
-    float2* d = dst + line * LS + (i - k) * R + k;
-#pragma unroll
-    for (int q = 0; q < R; ++q) d[q * p] = v[q];
   }
   __syncthreads();
 }
@@ -207,15 +218,17 @@ SVIE_DEV void fft_stage(const float2* __restrict__ src, float2* __restrict__ dst
 SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPlan& P) {
   int p = 1;
   for (int st = 0; st < P.nst; ++st) {
-    const int R = P.radix[st];
+    const int R = (int)((P.radices >> (4 * st)) & 15ULL);
+    // ceil(2^32 / p): exact i / p = umulhi(i, mg) for i * p < 2^32
+    const unsigned int mg = p > 1 ? 0xFFFFFFFFu / (unsigned)p + 1u : 0u;
     switch (R) {
-      case 8: fft_stage<8>(a, b, LS, P.n, nlines, p, P.tw); break;
-      case 7: fft_stage<7>(a, b, LS, P.n, nlines, p, P.tw); break;
-      case 6: fft_stage<6>(a, b, LS, P.n, nlines, p, P.tw); break;
-      case 5: fft_stage<5>(a, b, LS, P.n, nlines, p, P.tw); break;
-      case 4: fft_stage<4>(a, b, LS, P.n, nlines, p, P.tw); break;
-      case 3: fft_stage<3>(a, b, LS, P.n, nlines, p, P.tw); break;
-      default: fft_stage<2>(a, b, LS, P.n, nlines, p, P.tw); break;
+      case 8: fft_stage<8>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
+      case 7: fft_stage<7>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
+      case 6: fft_stage<6>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
+      case 5: fft_stage<5>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
+      case 4: fft_stage<4>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
+      case 3: fft_stage<3>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
+      default: fft_stage<2>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
     }
     float2* t = a; a = b; b = t;
     p *= R;
@@ -225,36 +238,40 @@ SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPla
 
 __host__ __device__ inline int line_stride(int n) { return (n & 1) ? n : n + 1; }  // odd -> conflict-free columns
 __host__ __device__ inline int padded_nzh(int nz) { return ((nz / 2 + 1) + 7) & ~7; }  // 64-byte rows
+__host__ __device__ inline int smem_buffer(int W, int n) { return padded_len(W * line_stride(n)); }
 
 // ----------------------------------------------------------------- z passes
 // Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
+// W complex (paired) lines per CTA; the tile is one contiguous chunk.
 __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ in, float2* __restrict__ out,
                                                      AxisPlan P, long long nlines, int W, int nzp) {
   extern __shared__ float2 sm[];
   const int n = P.n, LS = line_stride(n), nh = n / 2 + 1;
   float2* sa = sm;
-  float2* sb = sm + W * LS;
+  float2* sb = sm + smem_buffer(W, n);
   const long long line0 = (long long)blockIdx.x * 2 * W;
   const int nl = (int)min((long long)2 * W, nlines - line0);
   const int np = (nl + 1) >> 1;
   const float* src = in + line0 * n;
-  float* smf = reinterpret_cast<float*>(sa);
-  for (int e = threadIdx.x; e < np * 2 * n; e += FFT_T) {
-    const int l = e / n, z = e - l * n;
-    smf[2 * ((l >> 1) * LS + z) + (l & 1)] = (l < nl) ? __ldg(src + e) : 0.0f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int l = warp; l < 2 * np; l += FFT_T / 32) {
+    const bool ok = l < nl;
+    float* row = reinterpret_cast<float*>(sa);
+    for (int z = lane; z < n; z += 32) row[2 * px((l >> 1) * LS + z) + (l & 1)] = ok ? __ldg(src + l * n + z) : 0.0f;
   }
   __syncthreads();
   const float2* r = run_fft(sa, sb, LS, np, P);
   float2* dst = out + line0 * nzp;
-  for (int e = threadIdx.x; e < nl * nh; e += FFT_T) {
-    const int l = e / nh, k = e - l * nh;
+  for (int l = warp; l < nl; l += FFT_T / 32) {
     const int w = l >> 1;
-    const float2 a = r[w * LS + k];
-    const float2 b = r[w * LS + (k == 0 ? 0 : n - k)];
-    float2 v;
-    if ((l & 1) == 0) v = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
-    else v = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
-    dst[(long long)l * nzp + k] = v;
+    for (int k = lane; k < nh; k += 32) {
+      const float2 a = r[px(w * LS + k)];
+      const float2 b = r[px(w * LS + (k == 0 ? 0 : n - k))];
+      float2 v;
+      if ((l & 1) == 0) v = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+      else v = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
+      dst[(long long)l * nzp + k] = v;
+    }
   }
 }
 
@@ -265,83 +282,98 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
   extern __shared__ float2 sm[];
   const int n = P.n, LS = line_stride(n);
   float2* sa = sm;
-  float2* sb = sm + W * LS;
+  float2* sb = sm + smem_buffer(W, n);
   const long long line0 = (long long)blockIdx.x * 2 * W;
   const int nl = (int)min((long long)2 * W, nlines - line0);
   const int np = (nl + 1) >> 1;
   const float2* src = in + line0 * nzp;
   const bool even = (n & 1) == 0;
-  for (int e = threadIdx.x; e < np * n; e += FFT_T) {
-    const int w = e / n, k = e - w * n;
-    const bool mirror = k > n / 2;
-    const int kk = mirror ? n - k : k;
-    float2 x1 = make_float2(0.f, 0.f), x2 = make_float2(0.f, 0.f);
-    if (2 * w < nl) x1 = __ldg(src + (long long)(2 * w) * nzp + kk);
-    if (2 * w + 1 < nl) x2 = __ldg(src + (long long)(2 * w + 1) * nzp + kk);
-    if (kk == 0 || (even && kk == n / 2)) { x1.y = 0.f; x2.y = 0.f; }
-    if (mirror) { x1.y = -x1.y; x2.y = -x2.y; }
-    // C = X1 + i X2, stored conjugated for the inverse-by-forward transform
-    sa[w * LS + k] = make_float2(x1.x - x2.y, -(x1.y + x2.x));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int w = warp; w < np; w += FFT_T / 32) {
+    const bool has2 = 2 * w + 1 < nl;
+    const float2* s1 = src + (long long)(2 * w) * nzp;
+    const float2* s2 = s1 + nzp;
+    for (int k = lane; k < n; k += 32) {
+      const bool mirror = k > n / 2;
+      const int kk = mirror ? n - k : k;
+      float2 x1 = __ldg(s1 + kk);
+      float2 x2 = has2 ? __ldg(s2 + kk) : make_float2(0.f, 0.f);
+      if (kk == 0 || (even && kk == n / 2)) { x1.y = 0.f; x2.y = 0.f; }
+      if (mirror) { x1.y = -x1.y; x2.y = -x2.y; }
+      // C = X1 + i X2, stored conjugated for the inverse-by-forward transform
+      sa[px(w * LS + k)] = make_float2(x1.x - x2.y, -(x1.y + x2.x));
+    }
   }
   __syncthreads();
   const float2* r = run_fft(sa, sb, LS, np, P);
   float* dst = out + line0 * n;
-  for (int e = threadIdx.x; e < nl * n; e += FFT_T) {
-    const int l = e / n, z = e - l * n;
-    const float2 v = r[(l >> 1) * LS + z];
-    dst[e] = beta + alpha * ((l & 1) ? -v.y : v.x);
+  for (int l = warp; l < nl; l += FFT_T / 32) {
+    const int w = l >> 1;
+    for (int z = lane; z < n; z += 32) {
+      const float2 v = r[px(w * LS + z)];
+      dst[l * n + z] = beta + alpha * ((l & 1) ? -v.y : v.x);
+    }
   }
 }
 
 // ------------------------------------------------------------ strided passes
-// Lines along an axis with element stride `stride`; a CTA takes W consecutive
-// lines (contiguous in memory) of one outer slab: base = data +
-// blockIdx.y * outer_stride + blockIdx.x * W.  mode 0 = forward, 1 = inverse,
-// 2 = forward * K^ then inverse (x axis only; the outer index is y and the
-// line index kz).
+// Lines along an axis with element stride `stride`; a CTA takes SW = 8
+// consecutive lines (one aligned 64-byte row segment of the padded spectrum)
+// of one outer slab: base = data + blockIdx.y * outer_stride + blockIdx.x * 8.
+// mode 0 = forward, 1 = inverse, 2 = forward * K^ then inverse (x axis only;
+// the outer index is y and the line index kz).
+constexpr int SW = 8;
+
 struct KGeom {
   const float* kred;  // [(nx/2+1)][(ny/2+1)][nzh]
   int ny, nzh;
 };
 
 __global__ void __launch_bounds__(FFT_T) k_fft_strided(float2* __restrict__ data, AxisPlan P, long long stride,
-                                                       int ninner, long long outer_stride, int W, int mode, KGeom K) {
+                                                       int ninner, long long outer_stride, int mode, KGeom K) {
   extern __shared__ float2 sm[];
   const int n = P.n, LS = line_stride(n);
   float2* sa = sm;
-  float2* sb = sm + W * LS;
-  const int c0 = blockIdx.x * W;
-  const int nl = min(W, ninner - c0);
+  float2* sb = sm + smem_buffer(SW, n);
+  const int c0 = blockIdx.x * SW;
+  const int nl = min(SW, ninner - c0);
   float2* base = data + (long long)blockIdx.y * outer_stride + c0;
   const bool conj_in = (mode == 1);
-  for (int e = threadIdx.x; e < n * nl; e += FFT_T) {
-    const int k = e / nl, c = e - k * nl;
-    float2 v = base[(long long)k * stride + c];
-    if (conj_in) v.y = -v.y;
-    sa[c * LS + k] = v;
+  for (int e = threadIdx.x; e < n * SW; e += FFT_T) {
+    const int k = e >> 3, c = e & 7;
+    if (c < nl) {
+      float2 v = base[(long long)k * stride + c];
+      if (conj_in) v.y = -v.y;
+      sa[px(c * LS + k)] = v;
+    }
   }
   __syncthreads();
   float2* r = run_fft(sa, sb, LS, nl, P);
   if (mode == 2) {
     const int nyh = K.ny / 2 + 1;
     const int y = blockIdx.y, yr = min(y, K.ny - y);
-    for (int e = threadIdx.x; e < n * nl; e += FFT_T) {
-      const int k = e / nl, c = e - k * nl;
-      const int kr = min(k, n - k);
-      const float kv = __ldg(K.kred + ((long long)kr * nyh + yr) * K.nzh + (c0 + c));
-      const float2 v = r[c * LS + k];
-      r[c * LS + k] = make_float2(v.x * kv, -(v.y * kv));  // conj for the inverse
+    const float* krow = K.kred + (long long)yr * K.nzh + c0;
+    for (int e = threadIdx.x; e < n * SW; e += FFT_T) {
+      const int k = e >> 3, c = e & 7;
+      if (c < nl) {
+        const int kr = min(k, n - k);
+        const float kv = __ldg(krow + (long long)kr * nyh * K.nzh + c);
+        const float2 v = r[px(c * LS + k)];
+        r[px(c * LS + k)] = make_float2(v.x * kv, -(v.y * kv));  // conj for the inverse
+      }
     }
     __syncthreads();
     float2* other = (r == sa) ? sb : sa;
     r = run_fft(r, other, LS, nl, P);
   }
   const bool conj_out = (mode != 0);
-  for (int e = threadIdx.x; e < n * nl; e += FFT_T) {
-    const int k = e / nl, c = e - k * nl;
-    float2 v = r[c * LS + k];
-    if (conj_out) v.y = -v.y;
-    base[(long long)k * stride + c] = v;
+  for (int e = threadIdx.x; e < n * SW; e += FFT_T) {
+    const int k = e >> 3, c = e & 7;
+    if (c < nl) {
+      float2 v = r[px(c * LS + k)];
+      if (conj_out) v.y = -v.y;
+      base[(long long)k * stride + c] = v;
+    }
   }
 }
 
@@ -491,14 +523,9 @@ static PlanLayout plan_layout(int nx, int ny, int nz) {
   return L;
 }
 
-// Lines per CTA: shared memory holds two buffers of W lines (<= 64 KB, so three
-// CTAs fit on an SM).  Strided passes use W = 8 complex (one aligned 64-byte
-// segment per row of the padded spectrum).
-static int strided_width(int n) {
-  int w = 4096 / n;
-  return w > 8 ? 8 : (w < 1 ? 1 : w);
-}
-static int z_width(int n) {  // complex (paired) lines per CTA
+// Complex lines per CTA of the z passes: two shared buffers of W lines stay
+// under ~64 KB, so three CTAs fit on an SM.
+static int z_width(int n) {
   int w = 4096 / n;
   return w > 16 ? 16 : (w < 1 ? 1 : w);
 }
@@ -547,7 +574,7 @@ static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, flo
                      float alpha, float beta, cudaStream_t s) {
   const long long nlines = (long long)nx * ny;
   const int W = z_width(nz), nzp = padded_nzh(nz);
-  const size_t smem = 2 * (size_t)W * line_stride(nz) * sizeof(float2);
+  const size_t smem = 2 * (size_t)smem_buffer(W, nz) * sizeof(float2);
   const long long nb = (nlines + 2 * W - 1) / (2 * W);
   if (fwd) k_fft_z_r2c<<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, W, nzp);
   else k_fft_z_c2r<<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, W, nzp, alpha, beta);
@@ -556,19 +583,17 @@ static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, flo
 // y lines: outer index x, line index kz, element stride nzp.
 static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
-  const int W = strided_width(ny);
-  const size_t smem = 2 * (size_t)W * line_stride(ny) * sizeof(float2);
-  dim3 g((unsigned)((nzh + W - 1) / W), (unsigned)nx);
-  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, W, mode, KGeom{nullptr, ny, nzh});
+  const size_t smem = 2 * (size_t)smem_buffer(SW, ny) * sizeof(float2);
+  dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)nx);
+  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, KGeom{nullptr, ny, nzh});
 }
 
 // x lines: outer index y, line index kz, element stride ny * nzp.
 static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
-  const int W = strided_width(nx);
-  const size_t smem = 2 * (size_t)W * line_stride(nx) * sizeof(float2);
-  dim3 g((unsigned)((nzh + W - 1) / W), (unsigned)ny);
-  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, W, mode, KGeom{P.kred, ny, nzh});
+  const size_t smem = 2 * (size_t)smem_buffer(SW, nx) * sizeof(float2);
+  dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)ny);
+  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, KGeom{P.kred, ny, nzh});
 }
 
 static void gauss_legendre(int n, double* x, double* w) {

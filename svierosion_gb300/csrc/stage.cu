@@ -17,11 +17,6 @@ namespace svie {
 
 constexpr int SG_THREADS = 256;
 
-struct LawF {
-  // float copies of the law constants as the reference's float32 kernels see them
-  float hf, cut_b, cut_ba, n_cap_f;
-};
-
 SVIE_DEV float powk(float x, int k) {
   if (k == 0) return 1.0f;
   if (k == 1) return x;
@@ -30,13 +25,15 @@ SVIE_DEV float powk(float x, int k) {
   return powf(x, (float)k);
 }
 
-// SVIPowerLaw.speed (flows.py:89-96)
+// SVIPowerLaw.speed (flows.py:89-96).  t - N is formed in float64 (exact for
+// float N) and rounded once: N approaches t at edges and corners, where the
+// float32 difference would lose relative accuracy.
 SVIE_DEV float svi_speed(float N, const svie_law& L) {
   N = fminf(fmaxf(N, 0.0f), 1.0f);
   float V;
   if (L.s) {
     N = fminf(N, (float)L.n_cap);
-    V = (float)((double)powk(N, L.k) / (L.t - (double)N));
+    V = powk(N, L.k) / (float)(L.t - (double)N);
   } else {
     V = L.k ? powk(N, L.k) : 1.0f;
   }
@@ -48,9 +45,9 @@ SVIE_DEV float svi_dspeed(float N, const svie_law& L) {
   N = fminf(fmaxf(N, 1e-12f), 1.0f);
   if (L.s) {
     N = fminf(N, (float)L.n_cap);
-    double d = L.t - (double)N;
-    float V = (float)((double)powk(N, L.k) / d);
-    return V * ((float)L.k / N + (float)(1.0 / d));
+    const float d = (float)(L.t - (double)N);
+    const float V = powk(N, L.k) / d;
+    return V * ((float)L.k / N + 1.0f / d);
   }
   if (L.k == 0) return 0.0f;
   return (float)L.k * powk(N, L.k - 1);
@@ -91,7 +88,7 @@ SVIE_DEV void curv_speed(float k1, float k2, const svie_law& L, float* V, float*
 // Smoothstep cutoff (evolve.py:108-112): t = clamp((b - |phi|)/(b - a), 0, 1).
 SVIE_DEV float cutoff(float phi, const svie_law& L) {
   float x = fabsf(phi);
-  float t = ((float)L.cut_b - x) / (float)(L.cut_b - L.cut_a);
+  float t = ((float)L.cut_b - x) * (float)(1.0 / (L.cut_b - L.cut_a));
   t = fminf(fmaxf(t, 0.0f), 1.0f);
   return t * t * (3.0f - 2.0f * t);
 }

@@ -111,8 +111,14 @@ def test_stencil_kernels(sphere):
     _close(g, d["tricubic_grad"], 2e-6)
     _close(K.trilinear(flat, ny, nz, ref_cp), d["trilinear"], 2e-6)
     k1, k2 = K.principal_curvatures(flat, idx, *st, h)
-    _close(k1, d["k1"], 1e-4, 1e-4)
-    _close(k2, d["k2"], 1e-4, 1e-4)
+    # H and K are well conditioned; k1,2 = H +- sqrt(H^2 - K) lose digits near
+    # umbilic points (on this near-sphere), so they are checked against their scale
+    H, Kg = 0.5 * (k1 + k2), k1 * k2
+    _close(H, 0.5 * (d["k1"] + d["k2"]), 1e-4, 1e-5)
+    _close(Kg, d["k1"] * d["k2"], 1e-3, 1e-5)
+    kscale = float(np.abs(d["k1"]).max())
+    _close(k1, d["k1"], 1e-4 * kscale)
+    _close(k2, d["k2"], 1e-4 * kscale)
     assert np.array_equal(K.interface_mask(flat, idx, *st).cpu().numpy(), d["interface"])
     geo = K.reinit_geometry(flat, idx, *st, h, 0.45)
     _close(geo[0], d["geo_sgn"], 0)
@@ -130,7 +136,7 @@ def test_interface_nodes_and_dense_fractions(sphere):
     ls = S.LevelSet(_cuda(d["phi"]), grid, width=6)
     ref = d["band"][d["interface"]]
     assert np.array_equal(ls.interface_nodes().cpu().numpy(), ref)
-    _close(ls.dense_fractions().view(-1), d["dense_fractions"], 2e-6)
+    _close(ls.dense_fractions().view(-1), d["dense_fractions"].reshape(-1), 2e-6)
 
 
 def test_cube_plane_fraction(golden):
