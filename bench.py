@@ -200,7 +200,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         peak, peak_src = 6800.0, "fallback"
     band_mean = updates / max(args.steps, 1)
     abytes = algorithmic_bytes(grid.shape, int(band_mean))
-    dom = max(kt.items(), key=lambda kv: kv[1]["total_ms"])[0] if kt else None
+    single = {k: v for k, v in kt.items() if k in abytes}
+    dom = max(single.items(), key=lambda kv: kv[1]["total_ms"])[0] if single else None
     kern = {}
     for k, v in kt.items():
         b = abytes.get(k)

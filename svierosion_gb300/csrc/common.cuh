@@ -130,16 +130,16 @@ SVIE_DEV float weno5(float v1, float v2, float v3, float v4, float v5) {
 }
 
 // Godunov |grad phi| for inward motion at flat node i (reference kernels.py:146-169).
-SVIE_DEV float godunov_at(const float* __restrict__ f, long long i, long long sx, long long sy,
-                          long long sz, float inv_h) {
-  const float c = __ldg(f + i);
+SVIE_DEV float godunov_at(const float* __restrict__ f, int i, int sx, int sy, int sz, float inv_h) {
+  const float* q = f + i;
+  const float c = __ldg(q);
   float g2 = 0.0f;
-  const long long st[3] = {sx, sy, sz};
+  const int st[3] = {sx, sy, sz};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const long long s = st[a];
-    float m3 = __ldg(f + i - 3 * s), m2 = __ldg(f + i - 2 * s), m1 = __ldg(f + i - s);
-    float p1 = __ldg(f + i + s), p2 = __ldg(f + i + 2 * s), p3 = __ldg(f + i + 3 * s);
+    const int s = st[a];
+    float m3 = __ldg(q - 3 * s), m2 = __ldg(q - 2 * s), m1 = __ldg(q - s);
+    float p1 = __ldg(q + s), p2 = __ldg(q + 2 * s), p3 = __ldg(q + 3 * s);
     float d0 = (m2 - m3) * inv_h, d1 = (m1 - m2) * inv_h, d2 = (c - m1) * inv_h;
     float d3 = (p1 - c) * inv_h, d4 = (p2 - p1) * inv_h, d5 = (p3 - p2) * inv_h;
     float dm = weno5(d0, d1, d2, d3, d4);
@@ -180,12 +180,12 @@ SVIE_DEV float cube_plane_fraction(float s, float a, float b, float c) {
 }
 
 // Tangent-plane cell fraction at node i (reference kernels.py:173-181).
-SVIE_DEV float cell_fraction_at(const float* __restrict__ f, long long i, long long sx, long long sy,
-                                long long sz) {
-  float c = __ldg(f + i);
-  float gx = 0.5f * (__ldg(f + i + sx) - __ldg(f + i - sx));
-  float gy = 0.5f * (__ldg(f + i + sy) - __ldg(f + i - sy));
-  float gz = 0.5f * (__ldg(f + i + sz) - __ldg(f + i - sz));
+SVIE_DEV float cell_fraction_at(const float* __restrict__ f, int i, int sx, int sy, int sz) {
+  const float* q = f + i;
+  float c = __ldg(q);
+  float gx = 0.5f * (__ldg(q + sx) - __ldg(q - sx));
+  float gy = 0.5f * (__ldg(q + sy) - __ldg(q - sy));
+  float gz = 0.5f * (__ldg(q + sz) - __ldg(q - sz));
   float gn = fmaxf(sqrtf(gx * gx + gy * gy + gz * gz), 1e-30f);
   float rg = __frcp_rn(gn);
   float x = fabsf(gx * rg), y = fabsf(gy * rg), z = fabsf(gz * rg);
@@ -197,21 +197,23 @@ SVIE_DEV float cell_fraction_at(const float* __restrict__ f, long long i, long l
 
 // First Newton projection to the zero set (reference kernels.py:185-208).
 // hi = (nx-3.001, ny-3.001, nz-3.001) rounded to float.
-SVIE_DEV float3 closest_point_at(const float* __restrict__ f, long long i, int ny, int nz, float hx,
-                                 float hy, float hz, float h) {
-  const long long sx = (long long)ny * nz, sy = nz;
-  float c = __ldg(f + i);
-  float gx = 0.5f * (__ldg(f + i + sx) - __ldg(f + i - sx));
-  float gy = 0.5f * (__ldg(f + i + sy) - __ldg(f + i - sy));
-  float gz = 0.5f * (__ldg(f + i + 1) - __ldg(f + i - 1));
+SVIE_DEV float3 closest_point_at(const float* __restrict__ f, int i, int ny, int nz, float hx, float hy,
+                                 float hz, float h) {
+  const int sx = ny * nz, sy = nz;
+  const float* q = f + i;
+  float c = __ldg(q);
+  float gx = 0.5f * (__ldg(q + sx) - __ldg(q - sx));
+  float gy = 0.5f * (__ldg(q + sy) - __ldg(q - sy));
+  float gz = 0.5f * (__ldg(q + 1) - __ldg(q - 1));
   float g2 = fmaxf(gx * gx + gy * gy + gz * gz, 1e-30f);
   float ac = fabsf(c);
   float length = ac / sqrtf(g2);
   float cap = 1.25f * ac / h + 0.25f;
   float scale = (c / g2) * fminf(cap / fmaxf(length, 1e-30f), 1.0f);
-  float fi = (float)(i / sx);
-  float fj = (float)((i / sy) % ny);
-  float fk = (float)(i % nz);
+  const int ii = i / sx, rem = i - ii * sx, jj = rem / sy;
+  float fi = (float)ii;
+  float fj = (float)jj;
+  float fk = (float)(rem - jj * sy);
   float3 p;
   p.x = fminf(fmaxf(fi - scale * gx, 1.0f), hx);
   p.y = fminf(fmaxf(fj - scale * gy, 1.0f), hy);
@@ -242,15 +244,15 @@ SVIE_DEV float tricubic_at(const float* __restrict__ g, int ny, int nz, float3 p
   cubic_w(p.x - fx, wx);
   cubic_w(p.y - fy, wy);
   cubic_w(p.z - fz, wz);
-  const long long syz = (long long)ny * nz;
-  const long long b0 = ((long long)fx - 1) * syz + ((long long)fy - 1) * nz + ((long long)fz - 1);
+  const int syz = ny * nz;
+  const float* b0 = g + (((int)fx - 1) * syz + ((int)fy - 1) * nz + ((int)fz - 1));
   float out = 0.0f;
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
       const float wab = wx[a] * wy[b];
-      const float* row = g + b0 + a * syz + b * nz;
+      const float* row = b0 + (a * syz + b * nz);
 #pragma unroll
       for (int c = 0; c < 4; ++c) out = out + (wab * wz[c]) * __ldg(row + c);
     }
@@ -264,7 +266,7 @@ SVIE_DEV float trilinear_at(const float* __restrict__ g, int ny, int nz, float3 
   float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
   float tx = p.x - fx, ty = p.y - fy, tz = p.z - fz;
   const long long syz = (long long)ny * nz;
-  const long long b0 = (long long)fx * syz + (long long)fy * nz + (long long)fz;
+  const long long b0 = (long long)fx * syz + (long long)fy * nz + (long long)fz;  // 64-bit: ncomp * index may exceed 2^31
   float out = 0.0f;
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
@@ -283,8 +285,7 @@ SVIE_DEV float trilinear_at(const float* __restrict__ g, int ny, int nz, float3 
 }
 
 // Principal curvatures k1 >= k2 of the level sets at node i (reference kernels.py:274-299).
-SVIE_DEV float2 principal_curvatures_at(const float* __restrict__ f, long long i, long long sx,
-                                        long long sy, long long sz, float h) {
+SVIE_DEV float2 principal_curvatures_at(const float* __restrict__ f, int i, int sx, int sy, int sz, float h) {
   float c = __ldg(f + i);
   float xp = __ldg(f + i + sx), xm = __ldg(f + i - sx);
   float yp = __ldg(f + i + sy), ym = __ldg(f + i - sy);
@@ -294,7 +295,7 @@ SVIE_DEV float2 principal_curvatures_at(const float* __restrict__ f, long long i
   float pxx = (xp - 2.0f * c + xm) / hh;
   float pyy = (yp - 2.0f * c + ym) / hh;
   float pzz = (zp - 2.0f * c + zm) / hh;
-  auto mixed = [&](long long a, long long b) {
+  auto mixed = [&](int a, int b) {
     return (__ldg(f + i + a + b) - __ldg(f + i + a - b) - __ldg(f + i - a + b) + __ldg(f + i - a - b)) / h4;
   };
   float pxy = mixed(sx, sy), pxz = mixed(sx, sz), pyz = mixed(sy, sz);

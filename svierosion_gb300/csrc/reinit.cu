@@ -88,19 +88,20 @@ __global__ void k_reinit_geometry(const float* __restrict__ f, const int32_t* __
 }
 
 // reinit_rhs (kernels.py:363-379) at work-set entry t.
-SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, long long i, long long t, const Geo& g, long long sx,
-                             long long sy, long long sz, float h) {
-  const float c = __ldg(f + i);
+SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, const Geo& g, int sx, int sy, int sz,
+                             float h) {
+  const float* qp = f + i;
+  const float c = __ldg(qp);
   const float sgn = g.sgn[t];
   const uint32_t flags = g.flags[t];
   const bool outside = sgn > 0.0f;
   const float hh = h * h;
   float g2 = 0.0f;
-  const long long st[3] = {sx, sy, sz};
+  const int st[3] = {sx, sy, sz};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const long long s = st[a];
-    float m2 = __ldg(f + i - 2 * s), m1 = __ldg(f + i - s), p1 = __ldg(f + i + s), p2 = __ldg(f + i + 2 * s);
+    const int s = st[a];
+    float m2 = __ldg(qp - 2 * s), m1 = __ldg(qp - s), p1 = __ldg(qp + s), p2 = __ldg(qp + 2 * s);
     float mm_p = minmod(p1 - 2.0f * c + m1, p2 - 2.0f * p1 + c);
     float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
     const bool cp = (flags >> (2 * a)) & 1u, cm = (flags >> (2 * a + 1)) & 1u;
