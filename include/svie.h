@@ -259,8 +259,10 @@ int svie_set_f64(double* dst, double value, void* stream);
  * dilated by `dilation` cells with the `margin` outer layers cleared. */
 int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin,
                      uint8_t* mask, uint8_t* tmp, void* stream);
-/* reinit_geometry (kernels.py:335-359) packed per node: 4 floats
- * (sgn, dtau, flags, pad) + 6 floats (xp, xm per axis). */
+/* reinit_geometry (kernels.py:335-359) packed structure-of-arrays over the
+ * m work-set nodes: dtau float[m], dist float[6m] (xp_x xm_x xp_y xm_y xp_z
+ * xm_z), meta uint8[m] (bits 0-5 crossing flags cp/cm per axis, bit 6
+ * phi0 > 0, bit 7 phi0 < 0). */
 size_t svie_reinit_geometry_bytes(int64_t m);
 int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
                          int64_t sz, float h, float cfl, void* geo, void* stream);

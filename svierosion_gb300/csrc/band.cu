@@ -142,6 +142,14 @@ __global__ void __launch_bounds__(CMP_THREADS) k_band_write(const float* __restr
   int inside_static = 0;
   int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
   int ilo[3] = {INT_MAX, INT_MAX, INT_MAX}, ihi[3] = {-1, -1, -1};
+  // coordinates of the first node, then advanced incrementally (no division per node)
+  int c[3];
+  if (t0 < n) {
+    const int e0 = (int)t0, yz = e0 % (int)syz;
+    c[0] = e0 / (int)syz;
+    c[1] = yz / nz;
+    c[2] = yz - c[1] * nz;
+  }
   for (int j = 0; j < CMP_IPT; ++j) {
     long long e = t0 + j;
     if (e >= n) break;
@@ -149,18 +157,19 @@ __global__ void __launch_bounds__(CMP_THREADS) k_band_write(const float* __restr
     bool sel = fabsf(v) < thresh;
     bool neg = v < 0.0f;
     if (occ) occ[e] = neg ? 1.0f : 0.0f;
-    if (sel || neg) {
-      int c[3] = {(int)(e / syz), (int)((e / nz) % ny), (int)(e % nz)};
-      if (sel) {
-        bits |= 1u << j;
+    if (sel) {
+      bits |= 1u << j;
 #pragma unroll
-        for (int a = 0; a < 3; ++a) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
-      }
-      if (neg) {
+      for (int a = 0; a < 3; ++a) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
+    }
+    if (neg) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) { ilo[a] = min(ilo[a], c[a]); ihi[a] = max(ihi[a], c[a]); }
-        if (!sel) ++inside_static;
-      }
+      for (int a = 0; a < 3; ++a) { ilo[a] = min(ilo[a], c[a]); ihi[a] = max(ihi[a], c[a]); }
+      if (!sel) ++inside_static;
+    }
+    if (++c[2] == nz) {
+      c[2] = 0;
+      if (++c[1] == ny) { c[1] = 0; ++c[0]; }
     }
   }
   int tot;

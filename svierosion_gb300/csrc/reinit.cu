@@ -35,39 +35,44 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
   return fminf(fmaxf(ok ? quad : lin, 0.0f), h);
 }
 
+// Geometry record, structure of arrays over the work set (m entries):
+//   dtau  float [m]
+//   meta  uint8 [m]   bits 0-5: crossing flags cp_x cm_x cp_y cm_y cp_z cm_z,
+//                     bit 6: phi0 > 0, bit 7: phi0 < 0
+//   dist  float [6m]  xp_x xm_x xp_y xm_y xp_z xm_z, read only where the flag is set
+// so a sweep streams 5 bytes of geometry per node instead of 36.
 struct Geo {
-  float* sgn;
   float* dtau;
-  uint32_t* flags;
-  float* dist;  // 6 arrays of m
+  uint8_t* meta;
+  float* dist;
   long long m;
 };
 
 SVIE_DEV Geo geo_view(void* base, long long m) {
   Geo g;
-  float* f = (float*)base;
-  g.sgn = f;
-  g.dtau = f + m;
-  g.flags = (uint32_t*)(f + 2 * m);
-  g.dist = f + 3 * m;
+  char* b = (char*)base;
+  g.dtau = (float*)b;
+  g.dist = (float*)(b + 4 * m);
+  g.meta = (uint8_t*)(b + 28 * m);
   g.m = m;
   return g;
 }
 
 __global__ void k_reinit_geometry(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
-                                  long long sx, long long sy, long long sz, float h, float cfl, void* geo) {
+                                  int sx, int sy, int sz, float h, float cfl, void* geo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
   Geo g = geo_view(geo, m);
-  const long long i = idx[t];
-  const float c = __ldg(f + i);
+  const int i = idx[t];
+  const float* qp = f + i;
+  const float c = __ldg(qp);
   float hmin = h;
   uint32_t flags = 0;
-  const long long st[3] = {sx, sy, sz};
+  const int st[3] = {sx, sy, sz};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const long long s = st[a];
-    float m2 = __ldg(f + i - 2 * s), m1 = __ldg(f + i - s), p1 = __ldg(f + i + s), p2 = __ldg(f + i + 2 * s);
+    const int s = st[a];
+    float m2 = __ldg(qp - 2 * s), m1 = __ldg(qp - s), p1 = __ldg(qp + s), p2 = __ldg(qp + 2 * s);
     float d_m1 = c - 2.0f * m1 + m2;
     float d_0 = p1 - 2.0f * c + m1;
     float d_p1 = p2 - 2.0f * p1 + c;
@@ -82,18 +87,20 @@ __global__ void k_reinit_geometry(const float* __restrict__ f, const int32_t* __
     g.dist[(2 * a) * m + t] = fmaxf(xp, 1e-6f * h);
     g.dist[(2 * a + 1) * m + t] = fmaxf(xm, 1e-6f * h);
   }
-  g.sgn[t] = (c > 0.0f) ? 1.0f : ((c < 0.0f) ? -1.0f : 0.0f);
+  flags |= (c > 0.0f ? 1u : 0u) << 6;
+  flags |= (c < 0.0f ? 1u : 0u) << 7;
   g.dtau[t] = cfl * fmaxf(hmin, 1e-3f * h);
-  g.flags[t] = flags;
+  g.meta[t] = (uint8_t)flags;
 }
 
+SVIE_DEV float meta_sgn(uint32_t meta) { return (meta & 64u) ? 1.0f : ((meta & 128u) ? -1.0f : 0.0f); }
+
 // reinit_rhs (kernels.py:363-379) at work-set entry t.
-SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, const Geo& g, int sx, int sy, int sz,
-                             float h) {
+SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, const Geo& g, uint32_t flags, int sx,
+                             int sy, int sz, float h) {
   const float* qp = f + i;
   const float c = __ldg(qp);
-  const float sgn = g.sgn[t];
-  const uint32_t flags = g.flags[t];
+  const float sgn = meta_sgn(flags);
   const bool outside = sgn > 0.0f;
   const float hh = h * h;
   float g2 = 0.0f;
@@ -132,14 +139,13 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, co
 }
 
 __global__ void __launch_bounds__(RI_THREADS) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
-                                                             const int32_t* __restrict__ idx, long long m, long long sx,
-                                                             long long sy, long long sz, float h, void* geo,
-                                                             int second) {
+                                                             const int32_t* __restrict__ idx, long long m, int sx,
+                                                             int sy, int sz, float h, void* geo, int second) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
   Geo g = geo_view(geo, m);
-  const long long i = idx[t];
-  const float r = reinit_rhs_at(src, i, t, g, sx, sy, sz, h);
+  const int i = idx[t];
+  const float r = reinit_rhs_at(src, i, t, g, g.meta[t], sx, sy, sz, h);
   const float dtau = g.dtau[t];
   if (!second) {
     dst[i] = src[i] + dtau * r;  // u0 + dtau rhs(A)
@@ -149,22 +155,23 @@ __global__ void __launch_bounds__(RI_THREADS) k_reinit_sweep(const float* __rest
   }
 }
 
-__global__ void k_reinit_rhs(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, long long sx,
-                             long long sy, long long sz, float h, void* geo, float* out) {
+__global__ void k_reinit_rhs(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx, int sy,
+                             int sz, float h, void* geo, float* out) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
   Geo g = geo_view(geo, m);
-  out[t] = reinit_rhs_at(f, idx[t], t, g, sx, sy, sz, h);
+  out[t] = reinit_rhs_at(f, idx[t], t, g, g.meta[t], sx, sy, sz, h);
 }
 
 __global__ void k_geo_unpack(const void* geo, long long m, float* sgn, float* dtau, uint8_t* flags, float* dist6) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
   Geo g = geo_view(const_cast<void*>(geo), m);
-  sgn[t] = g.sgn[t];
+  const uint32_t meta = g.meta[t];
+  sgn[t] = meta_sgn(meta);
   dtau[t] = g.dtau[t];
   for (int a = 0; a < 6; ++a) {
-    flags[a * m + t] = (g.flags[t] >> a) & 1u;
+    flags[a * m + t] = (meta >> a) & 1u;
     dist6[a * m + t] = g.dist[a * m + t];
   }
 }
@@ -178,10 +185,11 @@ __global__ void k_mark(const int32_t* __restrict__ band, long long m, uint8_t* _
 // margin > 0 also clears the outer layers on every axis (last pass only).
 __global__ void k_dilate_axis(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst, int nx, int ny, int nz,
                               int axis, int r, int margin) {
-  const long long n = (long long)nx * ny * nz;
   const long long syz = (long long)ny * nz;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(e / syz), y = (int)((e / nz) % ny), z = (int)(e % nz);
+  const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
+  if (z >= nz) return;
+  {
+    const long long e = (long long)x * syz + (long long)y * nz + z;
     const int c = axis == 0 ? x : (axis == 1 ? y : z);
     const int len = axis == 0 ? nx : (axis == 1 ? ny : nz);
     const long long st = axis == 0 ? syz : (axis == 1 ? nz : 1);
@@ -195,7 +203,7 @@ __global__ void k_dilate_axis(const uint8_t* __restrict__ src, uint8_t* __restri
   }
 }
 
-inline size_t geo_bytes(long long m) { return (size_t)(m < 1 ? 1 : m) * 9 * sizeof(float) + 256; }
+inline size_t geo_bytes(long long m) { return (size_t)(m < 1 ? 1 : m) * 29 + 256; }
 
 }  // namespace svie
 
@@ -216,10 +224,10 @@ int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int
     return SVIE_ERR_LAUNCH;
   }
   if (m > 0) k_mark<<<blocks_for(m, 256), 256, 0, s>>>(band, m, mask);
-  const int nb = blocks_for(n, 256, 152 * 16);
-  k_dilate_axis<<<nb, 256, 0, s>>>(mask, tmp, nx, ny, nz, 0, dilation, 0);
-  k_dilate_axis<<<nb, 256, 0, s>>>(tmp, mask, nx, ny, nz, 1, dilation, 0);
-  k_dilate_axis<<<nb, 256, 0, s>>>(mask, tmp, nx, ny, nz, 2, dilation, margin);
+  const dim3 gd((nz + 127) / 128, ny, nx);
+  k_dilate_axis<<<gd, 128, 0, s>>>(mask, tmp, nx, ny, nz, 0, dilation, 0);
+  k_dilate_axis<<<gd, 128, 0, s>>>(tmp, mask, nx, ny, nz, 1, dilation, 0);
+  k_dilate_axis<<<gd, 128, 0, s>>>(mask, tmp, nx, ny, nz, 2, dilation, margin);
   if (cudaMemcpyAsync(mask, tmp, (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
     set_error("svie_reinit_mask: copy failed");
     return SVIE_ERR_LAUNCH;
@@ -288,10 +296,10 @@ extern "C" int svie_dilate(const uint8_t* mask, int nx, int ny, int nz, int step
     return SVIE_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  const int nb = svie::blocks_for(n, 256, 152 * 16);
-  svie::k_dilate_axis<<<nb, 256, 0, s>>>(mask, tmp, nx, ny, nz, 0, steps, 0);
-  svie::k_dilate_axis<<<nb, 256, 0, s>>>(tmp, out, nx, ny, nz, 1, steps, 0);
-  svie::k_dilate_axis<<<nb, 256, 0, s>>>(out, tmp, nx, ny, nz, 2, steps, 0);
+  const dim3 gd((nz + 127) / 128, ny, nx);
+  svie::k_dilate_axis<<<gd, 128, 0, s>>>(mask, tmp, nx, ny, nz, 0, steps, 0);
+  svie::k_dilate_axis<<<gd, 128, 0, s>>>(tmp, out, nx, ny, nz, 1, steps, 0);
+  svie::k_dilate_axis<<<gd, 128, 0, s>>>(out, tmp, nx, ny, nz, 2, steps, 0);
   if (cudaMemcpyAsync(out, tmp, (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
     svie::set_error("svie_dilate: copy failed");
     return SVIE_ERR_LAUNCH;

@@ -119,10 +119,11 @@ __global__ void k_unpack(const long long* __restrict__ keys, long long n, float*
 }
 
 __global__ void k_ring_mask(const uint8_t* __restrict__ known, int nx, int ny, int nz, uint8_t* ring) {
-  const long long n = (long long)nx * ny * nz;
   const long long syz = (long long)ny * nz;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(e / syz), y = (int)((e / nz) % ny), z = (int)(e % nz);
+  const int z = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, x = blockIdx.z;
+  if (z >= nz) return;
+  {
+    const long long e = (long long)x * syz + (long long)y * nz + z;
     uint8_t r = 0;
     if (!known[e] && x > 0 && y > 0 && z > 0 && x < nx - 1 && y < ny - 1 && z < nz - 1) {
       for (int dx = -1; dx <= 1 && !r; ++dx)
@@ -338,7 +339,8 @@ int svie_sdf_ring_mask(const uint8_t* known, int nx, int ny, int nz, uint8_t* ri
     set_error("svie_sdf_ring_mask: bad arguments");
     return SVIE_ERR_ARG;
   }
-  k_ring_mask<<<blocks_for(n, 256, 152 * 32), 256, 0, (cudaStream_t)stream>>>(known, nx, ny, nz, ring);
+  const dim3 gd((nz + 127) / 128, ny, nx);
+  k_ring_mask<<<gd, 128, 0, (cudaStream_t)stream>>>(known, nx, ny, nz, ring);
   return launch_status("svie_sdf_ring_mask");
 }
 

@@ -167,15 +167,18 @@ def reinit_rhs(flat, idx, sx, sy, sz, h, sgn, cpx, cmx, xpx, xmx, cpy, cmy, xpy,
 
 
 def _pack_geometry(sgn, flags6, dist6, m, device):
-    """Structure-of-arrays layout of svie_reinit_geometry (plumbing copies)."""
-    geo = torch.zeros(nat.lib().svie_reinit_geometry_bytes(m) // 4, dtype=torch.float32, device=device)
-    geo[:m] = sgn.to(torch.float32)
-    bits = torch.zeros(m, dtype=torch.int32, device=device)
-    for a, f in enumerate(flags6):
-        bits |= f.to(torch.int32) << a
-    geo[2 * m:3 * m] = bits.view(torch.float32)
+    """Byte layout of svie_reinit_geometry: dtau float[m] (unused by reinit_rhs),
+    dist float[6m], meta uint8[m] (crossing flags, sign bits)."""
+    geo = torch.zeros(nat.lib().svie_reinit_geometry_bytes(m), dtype=torch.uint8, device=device)
+    dist = geo[4 * m:28 * m].view(torch.float32).view(6, m)
     for a, d in enumerate(dist6):
-        geo[(3 + a) * m:(4 + a) * m] = d.to(torch.float32)
+        dist[a] = d.to(torch.float32)
+    meta = torch.zeros(m, dtype=torch.int32, device=device)
+    for a, f in enumerate(flags6):
+        meta |= f.to(torch.int32) << a
+    meta |= (sgn > 0).to(torch.int32) << 6
+    meta |= (sgn < 0).to(torch.int32) << 7
+    geo[28 * m:29 * m] = meta.to(torch.uint8)
     return geo
 
 
