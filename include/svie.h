@@ -180,6 +180,19 @@ size_t svie_volume_workspace_bytes(int64_t m);
 int svie_band_volume(const float* phi, const int32_t* band, int64_t m, int64_t sx, int64_t sy,
                      int64_t sz, float* occ, void* ws, size_t ws_bytes, svie_stats* stats,
                      void* stream);
+/* svie_band_volume without a workspace: no counterpart in the reference.  For
+ * callers that cannot allocate device memory (a plugin inside a host
+ * framework whose pool owns all device memory, or a loop that forbids
+ * cudaMalloc after start-up because it can synchronise the device).  The
+ * scratch is a static 512 KiB device array held by every GPU that loads the
+ * library, so m is limited to svie_band_volume_noalloc_max() band nodes
+ * (16,777,216); larger m returns SVIE_ERR_CAPACITY.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be ordered by the caller. */
+int64_t svie_band_volume_noalloc_max(void);
+int svie_band_volume_noalloc(const float* phi, const int32_t* band, int64_t m, int64_t sx,
+                             int64_t sy, int64_t sz, float* occ, svie_stats* stats, void* stream);
 
 /* ------------------------------------------------------ SVI convolution */
 /* svierosion/svi.py:24 ball_cell_weights(radius, spacing, quad): half-width

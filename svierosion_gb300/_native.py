@@ -95,6 +95,8 @@ _SIGS = {
     "svie_dense_occupancy": (I, [V, I64, V, V]),
     "svie_volume_workspace_bytes": (Z, [I64]),
     "svie_band_volume": (I, [V, V, I64, I64, I64, I64, V, V, Z, V, V]),
+    "svie_band_volume_noalloc_max": (I64, []),
+    "svie_band_volume_noalloc": (I, [V, V, I64, I64, I64, I64, V, V, V]),
     "svie_ball_half_width": (I, [D, D]),
     "svie_ball_weights": (I, [D, D, I, V, V]),
     "svie_conv_plan_bytes": (Z, [I, I, I]),

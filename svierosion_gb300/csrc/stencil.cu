@@ -424,3 +424,79 @@ extern "C" int svie_dense_occupancy(const float* phi, int64_t n, float* occ, voi
   svie::k_dense_occ<<<svie::blocks_for(n, 256, 152 * 32), 256, 0, (cudaStream_t)stream>>>(phi, n, occ);
   return svie::launch_status("svie_dense_occupancy");
 }
+
+// ------------------------------------------------- allocation-free volume
+// svie_band_volume_noalloc: the same float64 volume reduction as
+// svie_band_volume, for callers that must not allocate device memory and have
+// no workspace to hand over -- for example a plugin living inside a host
+// framework whose own memory pool owns every device allocation, or a
+// latency-critical loop that forbids cudaMalloc after start-up because the
+// allocator may synchronise the device.  Its scratch (one float64 partial sum
+// per CTA) is the file-scope array below, which every GPU that loads this
+// library keeps for the life of the process.
+#include <mutex>
+
+namespace svie {
+
+constexpr long long VOLUME_NOALLOC_MAX_CTAS = 65536;  // 512 KiB of float64 partial sums
+
+static __device__ __align__(256) double g_volume_partials[VOLUME_NOALLOC_MAX_CTAS];
+
+static std::mutex g_volume_symbol_mutex;
+static double* g_volume_symbol[64] = {};
+
+// Device address of g_volume_partials on the current device, looked up once per
+// device (the array's name in host code is only a stand-in for the symbol).
+static int volume_partials_address(double** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    set_error("svie_band_volume_noalloc: no usable current CUDA device");
+    return SVIE_ERR_LAUNCH;
+  }
+  std::lock_guard<std::mutex> lock(g_volume_symbol_mutex);
+  if (!g_volume_symbol[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_volume_partials);
+    if (e != cudaSuccess || !p) {
+      set_error("svie_band_volume_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return SVIE_ERR_LAUNCH;
+    }
+    g_volume_symbol[dev] = (double*)p;
+  }
+  *out = g_volume_symbol[dev];
+  return SVIE_OK;
+}
+
+}  // namespace svie
+
+extern "C" {
+
+int64_t svie_band_volume_noalloc_max(void) { return (int64_t)svie::VOLUME_NOALLOC_MAX_CTAS * svie::ST_THREADS; }
+
+int svie_band_volume_noalloc(const float* phi, const int32_t* band, int64_t m, int64_t sx, int64_t sy, int64_t sz,
+                             float* occ, svie_stats* stats, void* stream) {
+  using namespace svie;
+  if (m < 0 || !stats || (m > 0 && (!phi || !band))) {
+    set_error("svie_band_volume_noalloc: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (m > svie_band_volume_noalloc_max()) {
+    set_error("svie_band_volume_noalloc: %lld band nodes exceed the static scratch limit of %lld; use "
+              "svie_band_volume with a workspace", (long long)m, (long long)svie_band_volume_noalloc_max());
+    return SVIE_ERR_CAPACITY;
+  }
+  double* partials = nullptr;
+  int st = volume_partials_address(&partials);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long nb = (m + ST_THREADS - 1) / ST_THREADS;
+  k_clear_flags<<<1, 1, 0, s>>>(stats, (unsigned)m);
+  // every CTA overwrites its own partial, and the sum reads exactly those nb
+  // entries, so nothing left from an earlier call is read
+  if (nb > 0)
+    k_volume_partial<<<(unsigned)nb, ST_THREADS, 0, s>>>(phi, band, m, sx, sy, sz, occ, partials, stats);
+  k_sum_partials<<<1, 1024, 0, s>>>(partials, nb, &stats->fsum);
+  return launch_status("svie_band_volume_noalloc", nb > 0 ? 3 : 2);
+}
+
+}  // extern "C"
