@@ -120,6 +120,16 @@ int svie_mask_write(const uint8_t* mask, int64_t n, const void* ws, size_t ws_by
  * the workspace of a preceding svie_mask_scan over the same mask. */
 int svie_mask_select(const uint8_t* mask, const int32_t* vals, int64_t n, const void* ws,
                      size_t ws_bytes, int32_t* out, int64_t capacity, void* stream);
+/* The same node sets in brick order (bricks of 4 x 4 x 16 nodes, x-major
+ * brick order, z fastest inside a row): kind 0 selects mask[i] != 0 (uint8
+ * src), kind 1 selects |phi[i]| < thresh (float src).  Same two-call
+ * protocol; the brick-ordered lists drive the stencil kernels, the ascending
+ * lists stay the API's node lists. */
+size_t svie_brick_workspace_bytes(int nx, int ny, int nz);
+int svie_brick_scan(int kind, const void* src, int nx, int ny, int nz, float thresh, void* ws,
+                    size_t ws_bytes, int64_t* count, void* stream);
+int svie_brick_write(int kind, const void* src, int nx, int ny, int nz, float thresh,
+                     const void* ws, size_t ws_bytes, int32_t* out, int64_t capacity, void* stream);
 
 /* ------------------------------------------------- stencil kernels (API) */
 /* svierosion/kernels.py:146 godunov_inward(flat, idx, sx, sy, sz, inv_h) */

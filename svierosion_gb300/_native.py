@@ -78,6 +78,9 @@ _SIGS = {
     "svie_mask_scan": (I, [V, I64, V, Z, V, V]),
     "svie_mask_write": (I, [V, I64, V, Z, V, I64, V]),
     "svie_mask_select": (I, [V, V, I64, V, Z, V, I64, V]),
+    "svie_brick_workspace_bytes": (Z, [I, I, I]),
+    "svie_brick_scan": (I, [I, V, I, I, I, F, V, Z, V, V]),
+    "svie_brick_write": (I, [I, V, I, I, I, F, V, Z, V, I64, V]),
     "svie_godunov_inward": (I, [V, V, I64, I64, I64, I64, F, V, V]),
     "svie_cell_fractions": (I, [V, V, I64, I64, I64, I64, V, V]),
     "svie_closest_points": (I, [V, V, I64, I, I, F, F, F, F, V, V]),

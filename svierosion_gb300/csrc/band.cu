@@ -328,3 +328,141 @@ extern "C" int svie_mask_select(const uint8_t* mask, const int32_t* vals, int64_
                                                                               capacity);
   return svie::launch_status("svie_mask_select");
 }
+
+// ------------------------------------------------- brick-ordered compaction
+// The same selections (mask[i] != 0, or |phi[i]| < thresh) listed brick by
+// brick: bricks of 4 x 4 x 16 nodes in x-major brick order, inside a brick the
+// 16 rows (x, y) in order and z fastest.  A CTA of the stencil kernels then
+// covers one or two bricks, so the x/y taps of its warps land on rows that
+// neighbouring warps of the same CTA load, instead of on new cache lines.
+// Node lists in this order drive the RK stages and the reinitialisation
+// sweeps; the sorted list stays the API's `band`.
+namespace svie {
+
+constexpr int BRX = 4, BRY = 4, BRZ = 16;
+constexpr int BRICK = BRX * BRY * BRZ;  // 256 = CMP_TILE / CMP_IPT rows of 16
+
+struct BrickGeom {
+  int nx, ny, nz, nbx, nby, nbz;
+  SVIE_DEV long long total() const { return (long long)nbx * nby * nbz * BRICK; }
+  // first flat index of the z-row handled by row id r (one row = CMP_IPT nodes),
+  // or -1 if the row is outside the grid; *zlen = nodes of the row inside it.
+  SVIE_DEV long long row(long long r, int* zlen) const {
+    const long long b = r >> 4;  // 16 rows per brick
+    const int lr = (int)(r & 15);
+    const int bz = (int)(b % nbz);
+    const long long bxy = b / nbz;
+    const int by = (int)(bxy % nby), bx = (int)(bxy / nby);
+    const int x = bx * BRX + (lr >> 2), y = by * BRY + (lr & 3), z0 = bz * BRZ;
+    if (x >= nx || y >= ny) return -1;
+    *zlen = min(BRZ, nz - z0);
+    return ((long long)x * ny + y) * nz + z0;
+  }
+};
+
+template <class Pred>
+__global__ void __launch_bounds__(CMP_THREADS) k_brick_count(Pred pred, BrickGeom G, int* counts) {
+  __shared__ int sh[CMP_THREADS / 32];
+  const long long r = (long long)blockIdx.x * CMP_THREADS + threadIdx.x;
+  int c = 0, zlen = 0;
+  if (r * CMP_IPT < G.total()) {
+    const long long f0 = G.row(r, &zlen);
+    if (f0 >= 0)
+      for (int j = 0; j < zlen; ++j) c += pred(f0 + j) ? 1 : 0;
+  }
+  int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
+  if (threadIdx.x == 0) counts[blockIdx.x] = tot;
+}
+
+template <class Pred>
+__global__ void __launch_bounds__(CMP_THREADS) k_brick_write(Pred pred, BrickGeom G, const int* offsets, int32_t* out,
+                                                             long long capacity) {
+  __shared__ int sh[33];
+  const long long r = (long long)blockIdx.x * CMP_THREADS + threadIdx.x;
+  unsigned int bits = 0;
+  long long f0 = -1;
+  int zlen = 0;
+  if (r * CMP_IPT < G.total()) {
+    f0 = G.row(r, &zlen);
+    if (f0 >= 0)
+      for (int j = 0; j < zlen; ++j)
+        if (pred(f0 + j)) bits |= 1u << j;
+  }
+  int tot;
+  long long o = (long long)offsets[blockIdx.x] + block_exclusive_scan(__popc(bits), sh, &tot);
+  while (bits) {
+    int j = __ffs(bits) - 1;
+    bits &= bits - 1;
+    if (o < capacity) out[o] = (int32_t)(f0 + j);
+    ++o;
+  }
+}
+
+struct AbsLessPred {
+  const float* phi;
+  float thresh;
+  SVIE_DEV bool operator()(long long e) const { return fabsf(phi[e]) < thresh; }
+};
+
+static BrickGeom brick_geom(int nx, int ny, int nz) {
+  return BrickGeom{nx, ny, nz, (nx + BRX - 1) / BRX, (ny + BRY - 1) / BRY, (nz + BRZ - 1) / BRZ};
+}
+
+static long long brick_blocks(const BrickGeom& G) {
+  const long long rows = (long long)G.nbx * G.nby * G.nbz * (BRICK / CMP_IPT);
+  return (rows + CMP_THREADS - 1) / CMP_THREADS;
+}
+
+}  // namespace svie
+
+extern "C" {
+
+size_t svie_brick_workspace_bytes(int nx, int ny, int nz) {
+  return (size_t)svie::brick_blocks(svie::brick_geom(nx, ny, nz)) * sizeof(int) + 256;
+}
+
+int svie_brick_scan(int kind, const void* src, int nx, int ny, int nz, float thresh, void* ws, size_t ws_bytes,
+                    int64_t* count, void* stream) {
+  using namespace svie;
+  const long long n = (long long)nx * ny * nz;
+  if (!src || !count || n <= 0 || n >= (1LL << 31) || (kind != 0 && kind != 1)) {
+    set_error("svie_brick_scan: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_brick_workspace_bytes(nx, ny, nz)) {
+    set_error("svie_brick_scan: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const BrickGeom G = brick_geom(nx, ny, nz);
+  const long long nb = brick_blocks(G);
+  if (kind == 0) k_brick_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(MaskPred{(const uint8_t*)src}, G, (int*)ws);
+  else k_brick_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(AbsLessPred{(const float*)src, thresh}, G, (int*)ws);
+  k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)count);
+  return launch_status("svie_brick_scan", 2);
+}
+
+int svie_brick_write(int kind, const void* src, int nx, int ny, int nz, float thresh, const void* ws, size_t ws_bytes,
+                     int32_t* out, int64_t capacity, void* stream) {
+  using namespace svie;
+  const long long n = (long long)nx * ny * nz;
+  if (!src || n <= 0 || n >= (1LL << 31) || (kind != 0 && kind != 1) || (capacity > 0 && !out)) {
+    set_error("svie_brick_write: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_brick_workspace_bytes(nx, ny, nz)) {
+    set_error("svie_brick_write: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const BrickGeom G = brick_geom(nx, ny, nz);
+  const long long nb = brick_blocks(G);
+  if (kind == 0)
+    k_brick_write<<<(unsigned)nb, CMP_THREADS, 0, s>>>(MaskPred{(const uint8_t*)src}, G, (const int*)ws, out, capacity);
+  else
+    k_brick_write<<<(unsigned)nb, CMP_THREADS, 0, s>>>(AbsLessPred{(const float*)src, thresh}, G, (const int*)ws, out,
+                                                       capacity);
+  return launch_status("svie_brick_write");
+}
+
+}  // extern "C"

@@ -80,6 +80,44 @@ SVIE_DEV int warp_max_i(int v) {
   return v;
 }
 
+// Warp sum of float values returned as a double in every lane.  The tree runs
+// on (hi, lo) float pairs combined with Knuth's error-free TwoSum, so the warp
+// total is exact to ~2^-46 relative while the FP64 pipe (slow on GB300) is used
+// once per warp instead of five times per thread.
+SVIE_DEV void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+SVIE_DEV double warp_sum_compensated(float v) {
+  float hi = v, lo = 0.0f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    float s, e;
+    two_sum(hi, h2, s, e);
+    e += lo + l2;
+    hi = s + e;
+    lo = e - (hi - s);
+  }
+  return (double)hi + (double)lo;
+}
+
+// Block sum of one float per thread as a double (compensated warp sums, FP64
+// across the warps); the result is valid in thread 0.
+SVIE_DEV double block_sum_compensated(float v, double* scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const double w = warp_sum_compensated(v);
+  __syncthreads();
+  if (lane == 0) scratch[wid] = w;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nw; ++i) r += scratch[i];
+  return r;
+}
+
 // Block-wide reduction through shared memory; every thread gets the result.
 // `scratch` needs blockDim.x/32 entries; the block size is a multiple of 32.
 template <typename T, typename Op>

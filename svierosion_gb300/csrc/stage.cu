@@ -17,6 +17,27 @@ namespace svie {
 
 constexpr int SG_THREADS = 256;
 
+// Float constants of a stage, rounded once on the host: the kernels then do no
+// float64 work per node except the t - N difference of the SVI law.
+struct StageConst {
+  float h, inv_h, hx, hy, hz;  // spacing, 1/h, clamp bounds n - 3.001
+  float n_cap, eps, cut_b, cut_scale;
+};
+
+static StageConst stage_const(const svie_law& L, int nx, int ny, int nz) {
+  StageConst c;
+  c.h = (float)L.h;
+  c.inv_h = (float)(1.0 / L.h);
+  c.hx = (float)(nx - 3.001);
+  c.hy = (float)(ny - 3.001);
+  c.hz = (float)(nz - 3.001);
+  c.n_cap = (float)L.n_cap;
+  c.eps = (float)L.eps;
+  c.cut_b = (float)L.cut_b;
+  c.cut_scale = (float)(1.0 / (L.cut_b - L.cut_a));
+  return c;
+}
+
 SVIE_DEV float powk(float x, int k) {
   if (k == 0) return 1.0f;
   if (k == 1) return x;
@@ -28,23 +49,23 @@ SVIE_DEV float powk(float x, int k) {
 // SVIPowerLaw.speed (flows.py:89-96).  t - N is formed in float64 (exact for
 // float N) and rounded once: N approaches t at edges and corners, where the
 // float32 difference would lose relative accuracy.
-SVIE_DEV float svi_speed(float N, const svie_law& L) {
+SVIE_DEV float svi_speed(float N, const svie_law& L, const StageConst& C) {
   N = fminf(fmaxf(N, 0.0f), 1.0f);
   float V;
   if (L.s) {
-    N = fminf(N, (float)L.n_cap);
+    N = fminf(N, C.n_cap);
     V = powk(N, L.k) / (float)(L.t - (double)N);
   } else {
     V = L.k ? powk(N, L.k) : 1.0f;
   }
-  return L.eps != 0.0 ? V + (float)L.eps : V;
+  return C.eps != 0.0f ? V + C.eps : V;
 }
 
 // SVIPowerLaw.dspeed (flows.py:98-108)
-SVIE_DEV float svi_dspeed(float N, const svie_law& L) {
+SVIE_DEV float svi_dspeed(float N, const svie_law& L, const StageConst& C) {
   N = fminf(fmaxf(N, 1e-12f), 1.0f);
   if (L.s) {
-    N = fminf(N, (float)L.n_cap);
+    N = fminf(N, C.n_cap);
     const float d = (float)(L.t - (double)N);
     const float V = powk(N, L.k) / d;
     return V * ((float)L.k / N + 1.0f / d);
@@ -86,9 +107,9 @@ SVIE_DEV void curv_speed(float k1, float k2, const svie_law& L, float* V, float*
 }
 
 // Smoothstep cutoff (evolve.py:108-112): t = clamp((b - |phi|)/(b - a), 0, 1).
-SVIE_DEV float cutoff(float phi, const svie_law& L) {
+SVIE_DEV float cutoff(float phi, const StageConst& C) {
   float x = fabsf(phi);
-  float t = ((float)L.cut_b - x) * (float)(1.0 / (L.cut_b - L.cut_a));
+  float t = (C.cut_b - x) * C.cut_scale;
   t = fminf(fmaxf(t, 0.0f), 1.0f);
   return t * t * (3.0f - 2.0f * t);
 }
@@ -98,7 +119,7 @@ struct StatAcc {
   float qmin_n, qmax_n, qmin_a, qmax_a;
   float dv_n, dv_a;    // dspeed (svi) or diffusivity (curvature)
   unsigned int cap_n, cap_a, n_near;
-  double vs_n, vs_a;
+  float vs_n, vs_a;    // V of this node (summed with compensated block sums)
 };
 
 SVIE_DEV void stat_init(StatAcc& s) {
@@ -107,7 +128,7 @@ SVIE_DEV void stat_init(StatAcc& s) {
   s.qmax_n = s.qmax_a = -INFINITY;
   s.dv_n = s.dv_a = 0.0f;
   s.cap_n = s.cap_a = s.n_near = 0;
-  s.vs_n = s.vs_a = 0.0;
+  s.vs_n = s.vs_a = 0.0f;
 }
 
 // Per-CTA reduction of the statistics and one atomic / partial write per CTA.
@@ -138,41 +159,39 @@ SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
   u = block_reduce(a.n_near, shu, OpSumU(), 0u);
   if (threadIdx.x == 0 && u) atomicAdd(&st->n_near, u);
   double d;
-  d = block_reduce(a.vs_n, shd, OpSumD(), 0.0);
+  d = block_sum_compensated(a.vs_n, shd);
   if (threadIdx.x == 0) partial[2 * blockIdx.x] = d;
-  d = block_reduce(a.vs_a, shd, OpSumD(), 0.0);
+  d = block_sum_compensated(a.vs_a, shd);
   if (threadIdx.x == 0) partial[2 * blockIdx.x + 1] = d;
 }
 
 __global__ void __launch_bounds__(SG_THREADS) k_stage_svi(const float* __restrict__ phi,
                                                           const int32_t* __restrict__ band, long long m, int nx,
                                                           int ny, int nz, const float* __restrict__ Nd,
-                                                          svie_law L, float* __restrict__ Lout,
+                                                          svie_law L, StageConst C, float* __restrict__ Lout,
                                                           float* __restrict__ u0, float* __restrict__ Vout,
                                                           svie_stats* st, double* partial) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long syz = (long long)ny * nz;
-  const float h = (float)L.h;
+  const int syz = ny * nz;
   StatAcc acc;
   if (st) stat_init(acc);
   if (t < m) {
-    const long long i = band[t];
+    const int i = band[t];
     const float c = __ldg(phi + i);
-    const float3 p = closest_point_at(phi, i, ny, nz, (float)(nx - 3.001), (float)(ny - 3.001),
-                                      (float)(nz - 3.001), h);
+    const float3 p = closest_point_at(phi, i, ny, nz, C.hx, C.hy, C.hz, C.h);
     const float N = tricubic_at(Nd, ny, nz, p);
-    float V = svi_speed(N, L);
+    float V = svi_speed(N, L, C);
     if (st) {
-      const bool near = fabsf(c) < h;
-      const float dv = svi_dspeed(N, L);
-      const bool capped = N > (float)L.n_cap;
+      const bool near = fabsf(c) < C.h;
+      const float dv = svi_dspeed(N, L, C);
+      const bool capped = N > C.n_cap;
       acc.qmin_a = N; acc.qmax_a = N; acc.dv_a = dv; acc.cap_a = capped; acc.vs_a = V;
       if (near) {
         acc.qmin_n = N; acc.qmax_n = N; acc.dv_n = dv; acc.cap_n = capped; acc.vs_n = V; acc.n_near = 1;
       }
     }
-    V = V * cutoff(c, L);
-    const float G = godunov_at(phi, i, syz, nz, 1, (float)(1.0 / L.h));
+    V = V * cutoff(c, C);
+    const float G = godunov_at(phi, i, syz, nz, 1, C.inv_h);
     Lout[t] = V * G;
     if (u0) u0[t] = c;
     if (Vout) Vout[t] = V;
@@ -185,8 +204,8 @@ __global__ void k_curv_scatter(const float* __restrict__ phi, const int32_t* __r
                                int ny, int nz, float h, float* __restrict__ kd) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  const long long i = band[t];
-  const float2 k = principal_curvatures_at(phi, i, (long long)ny * nz, nz, 1, h);
+  const int i = band[t];
+  const float2 k = principal_curvatures_at(phi, i, ny * nz, nz, 1, h);
   kd[2 * i] = k.x;
   kd[2 * i + 1] = k.y;
 }
@@ -194,31 +213,29 @@ __global__ void k_curv_scatter(const float* __restrict__ phi, const int32_t* __r
 __global__ void __launch_bounds__(SG_THREADS) k_stage_curv(const float* __restrict__ phi,
                                                            const int32_t* __restrict__ band, long long m, int nx,
                                                            int ny, int nz, const float* __restrict__ kd,
-                                                           svie_law L, float* __restrict__ Lout,
+                                                           svie_law L, StageConst C, float* __restrict__ Lout,
                                                            float* __restrict__ u0, float* __restrict__ Vout,
                                                            svie_stats* st, double* partial) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long syz = (long long)ny * nz;
-  const float h = (float)L.h;
+  const int syz = ny * nz;
   StatAcc acc;
   if (st) stat_init(acc);
   if (t < m) {
-    const long long i = band[t];
+    const int i = band[t];
     const float c = __ldg(phi + i);
-    const float3 p = closest_point_at(phi, i, ny, nz, (float)(nx - 3.001), (float)(ny - 3.001),
-                                      (float)(nz - 3.001), h);
+    const float3 p = closest_point_at(phi, i, ny, nz, C.hx, C.hy, C.hz, C.h);
     const float k1 = trilinear_at(kd, ny, nz, p, 2, 0);
     const float k2 = trilinear_at(kd, ny, nz, p, 2, 1);
     float V, D;
     curv_speed(k1, k2, L, &V, &D);
     if (st) {
-      const bool near = fabsf(c) < h;
+      const bool near = fabsf(c) < C.h;
       const float H = 0.5f * (k1 + k2);
       acc.qmin_a = H; acc.qmax_a = H; acc.dv_a = D; acc.vs_a = V;
       if (near) { acc.qmin_n = H; acc.qmax_n = H; acc.dv_n = D; acc.vs_n = V; acc.n_near = 1; }
     }
-    V = V * cutoff(c, L);
-    const float G = godunov_at(phi, i, syz, nz, 1, (float)(1.0 / L.h));
+    V = V * cutoff(c, C);
+    const float G = godunov_at(phi, i, syz, nz, 1, C.inv_h);
     Lout[t] = V * G;
     if (u0) u0[t] = c;
     if (Vout) Vout[t] = V;
@@ -336,8 +353,9 @@ int svie_stage_svi(const float* phi, const int32_t* band, int64_t m, int nx, int
   if (s) return s;
   const long long nb = (m + SG_THREADS - 1) / SG_THREADS;
   if (nb == 0) return SVIE_OK;
-  k_stage_svi<<<(unsigned)nb, SG_THREADS, 0, (cudaStream_t)stream>>>(phi, band, m, nx, ny, nz, N, *law, L, u0, V,
-                                                                     stats, (double*)ws);
+  k_stage_svi<<<(unsigned)nb, SG_THREADS, 0, (cudaStream_t)stream>>>(phi, band, m, nx, ny, nz, N, *law,
+                                                                     stage_const(*law, nx, ny, nz), L, u0, V, stats,
+                                                                     (double*)ws);
   return launch_status("svie_stage_svi");
 }
 
@@ -357,8 +375,9 @@ int svie_stage_curvature(const float* phi, const int32_t* band, int64_t m, int n
   if (s) return s;
   const long long nb = (m + SG_THREADS - 1) / SG_THREADS;
   if (nb == 0) return SVIE_OK;
-  k_stage_curv<<<(unsigned)nb, SG_THREADS, 0, (cudaStream_t)stream>>>(phi, band, m, nx, ny, nz, kdense, *law, L,
-                                                                      u0, V, stats, (double*)ws);
+  k_stage_curv<<<(unsigned)nb, SG_THREADS, 0, (cudaStream_t)stream>>>(phi, band, m, nx, ny, nz, kdense, *law,
+                                                                      stage_const(*law, nx, ny, nz), L, u0, V, stats,
+                                                                      (double*)ws);
   return launch_status("svie_stage_curvature");
 }
 
@@ -397,9 +416,10 @@ __global__ void k_law_eval(const float* __restrict__ x1, const float* __restrict
                            float* __restrict__ V, float* __restrict__ D) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
+  const StageConst C = {0.f, 0.f, 0.f, 0.f, 0.f, (float)L.n_cap, (float)L.eps, 0.f, 0.f};
   if (L.kind == 0) {
-    if (V) V[t] = svi_speed(x1[t], L);
-    if (D) D[t] = svi_dspeed(x1[t], L);
+    if (V) V[t] = svi_speed(x1[t], L, C);
+    if (D) D[t] = svi_dspeed(x1[t], L, C);
   } else {
     float v, d;
     curv_speed(x1[t], x2[t], L, &v, &d);

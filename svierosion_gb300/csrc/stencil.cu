@@ -164,22 +164,20 @@ __global__ void __launch_bounds__(ST_THREADS) k_volume_partial(const float* __re
                                                                float* __restrict__ occ, double* partial,
                                                                svie_stats* stats) {
   __shared__ double shd[ST_THREADS / 32];
-  __shared__ unsigned int shu[ST_THREADS / 32];
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double v = 0.0;
-  unsigned int neg = 0, pos = 0;
+  float v = 0.0f;
+  int neg = 0, pos = 0;
   if (t < m) {
-    long long i = idx[t];
-    float fr = cell_fraction_at(f, i, sx, sy, sz);
+    const int i = idx[t];
+    const float fr = cell_fraction_at(f, i, (int)sx, (int)sy, (int)sz);
     if (occ) occ[i] = fr;
-    v = (double)fr;
-    float c = __ldg(f + i);
+    v = fr;
+    const float c = __ldg(f + i);
     neg = c < 0.0f;
     pos = c > 0.0f;
   }
-  double s = block_reduce(v, shd, OpSumD(), 0.0);
-  unsigned int an = block_reduce(neg, shu, OpSumU(), 0u);
-  unsigned int ap = block_reduce(pos, shu, OpSumU(), 0u);
+  const double s = block_sum_compensated(v, shd);
+  const int an = __syncthreads_or(neg), ap = __syncthreads_or(pos);
   if (threadIdx.x == 0) {
     partial[blockIdx.x] = s;
     if (an) atomicOr(&stats->any_neg, 1u);

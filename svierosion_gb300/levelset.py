@@ -6,6 +6,8 @@ ascending list of flat indices with ``|phi| < width * h`` (clamped to
 Besides the reference's state the level set keeps, for the fused stages:
 
 * ``band32`` -- the band as int32 (``band`` is the int64 view of the API);
+* ``work32`` -- the same nodes in brick order (4 x 4 x 16 bricks), the order
+  in which the stencil kernels visit them;
 * ``occ``    -- the dense occupancy ``(phi < 0)`` with the band's cell
   fractions, maintained incrementally: off the band phi only changes at a
   band rebuild, so only band entries are rewritten between rebuilds;
@@ -82,6 +84,7 @@ class LevelSet:
     @band.setter
     def band(self, idx: torch.Tensor) -> None:
         self.band32 = idx.to(device=self.device, dtype=torch.int32).contiguous()
+        self.work32 = self.band32
         self._band64 = None
         self.occ_current = False
 
@@ -100,8 +103,16 @@ class LevelSet:
         band = torch.empty(count, dtype=torch.int32, device=self.device)
         nat.call("svie_band_write", nat.ptr(self.flat), nx, ny, nz, thresh, nat.ptr(ws), ws.numel(), nat.ptr(band),
                  count, nat.ptr(self.occ), nat.ptr(self._info), nat.stream())
+        bws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
+        bcnt = sc.get("brick_count", 8)
+        work = torch.empty(count, dtype=torch.int32, device=self.device)
+        nat.call("svie_brick_scan", 1, nat.ptr(self.flat), nx, ny, nz, thresh, nat.ptr(bws), bws.numel(), nat.ptr(bcnt),
+                 nat.stream())
+        nat.call("svie_brick_write", 1, nat.ptr(self.flat), nx, ny, nz, thresh, nat.ptr(bws), bws.numel(),
+                 nat.ptr(work), count, nat.stream())
         info = _read(self._info, nat.BAND_INFO_DTYPE)
         self.band32 = band
+        self.work32 = work
         self._band64 = None
         self.static_inside = int(info["static_inside"])
         self.band_lo = tuple(int(v) for v in info["lo"])
@@ -145,9 +156,9 @@ class LevelSet:
 
     def _volume_kernel(self, write_occ: bool):
         sc = nat.scratch(self.device)
-        m = self.band32.numel()
+        m = self.work32.numel()
         ws = sc.get("volume", nat.lib().svie_volume_workspace_bytes(m))
-        nat.call("svie_band_volume", nat.ptr(self.flat), nat.ptr(self.band32), m, *self.strides,
+        nat.call("svie_band_volume", nat.ptr(self.flat), nat.ptr(self.work32), m, *self.strides,
                  nat.ptr(self.occ) if write_occ else None, nat.ptr(ws), ws.numel(), nat.ptr(self._vstats),
                  nat.stream())
         if write_occ:
@@ -192,7 +203,7 @@ class LevelSet:
     def refresh_occupancy(self) -> None:
         """Bring the maintained occupancy up to date with the band values."""
         if not self.occ_current:
-            nat.call("svie_scatter_fractions", nat.ptr(self.flat), nat.ptr(self.band32), self.band32.numel(),
+            nat.call("svie_scatter_fractions", nat.ptr(self.flat), nat.ptr(self.work32), self.work32.numel(),
                      *self.strides, nat.ptr(self.occ), nat.stream())
             self.occ_current = True
 
@@ -234,12 +245,14 @@ class LevelSet:
         tmp = sc.get("reinit_tmp", n)
         nat.call("svie_reinit_mask", nat.ptr(self.band32), self.band32.numel(), nx, ny, nz, int(dilation), MARGIN,
                  nat.ptr(mask), nat.ptr(tmp), nat.stream())
-        ws = sc.get("band", nat.lib().svie_band_workspace_bytes(n))
+        ws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
         cnt = sc.get("reinit_count", 8)
-        nat.call("svie_mask_scan", nat.ptr(mask), n, nat.ptr(ws), ws.numel(), nat.ptr(cnt), nat.stream())
+        nat.call("svie_brick_scan", 0, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
+                 nat.stream())
         m = int(cnt[:8].cpu().view(torch.int64)[0])
         idx = sc.get("reinit_idx", 4 * max(m, 1))[:4 * m].view(torch.int32)
-        nat.call("svie_mask_write", nat.ptr(mask), n, nat.ptr(ws), ws.numel(), nat.ptr(idx), m, nat.stream())
+        nat.call("svie_brick_write", 0, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
+                 nat.stream())
         geo = sc.get("reinit_geo", nat.lib().svie_reinit_geometry_bytes(m))
         nat.call("svie_reinit_geometry", nat.ptr(self.flat), nat.ptr(idx), m, *self.strides, self.h, cfl,
                  nat.ptr(geo), nat.stream())
