@@ -233,11 +233,26 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
  * of 8, so every row starts on a 64-byte boundary.  The spectrum is
  * [nx][ny][row]; entries kz >= nz/2+1 are padding. */
 int svie_conv_spectrum_row(int nz);
-/* svie_conv_apply that also records events[0..5] (cudaEvent_t, created by
- * the caller) on the stream before, between and after its five passes:
- * z R2C, y forward, x forward*K^*inverse, y inverse, z C2R. */
-int svie_conv_apply_events(const void* plan, int nx, int ny, int nz, const float* f, float* out,
+/* Line flags for the masked convolution over the (x, y) lines of the grid
+ * (lineflag: nx*ny bytes, slabflag: nx bytes, tmp: nx*ny bytes scratch):
+ * bit 0 marks lines holding band nodes -- every line with solid, since the
+ * padding keeps the grid boundary outside -- and bit 1 those lines dilated by
+ * `dilation` lines in x and y, which covers every tricubic stencil at the
+ * closest point of a band node when dilation >= 10 (the projection moves at
+ * most 1.25 * 6 + 0.25 cells, the stencil reaches 2 more).  slabflag[x] ORs
+ * the bits of slab x. */
+int svie_conv_line_flags(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation,
+                         uint8_t* lineflag, uint8_t* slabflag, uint8_t* tmp, void* stream);
+/* svie_conv_apply that skips provably unneeded work: z lines without bit 0
+ * are zero on input (only zeros are written for them), y slabs without bit 0
+ * stay zero in the forward pass, and in the inverse passes only slabs / lines
+ * with bit 1 are computed -- the other values of `out` are left unchanged and
+ * must not be read.  events (optional): six cudaEvent_t recorded before,
+ * between and after the five passes (z R2C, y forward, x forward*K^*inverse,
+ * y inverse, z C2R). */
+int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float* f, float* out,
                            double alpha, double beta, void* ws, size_t ws_bytes,
+                           const uint8_t* lineflag, const uint8_t* slabflag,
                            void* const* events, void* stream);
 /* Full complex64 half spectrum K^ (rfftn of the wrapped kernel, svi.py:76-81). */
 int svie_conv_kernel_hat(const void* plan, int nx, int ny, int nz, void* out_c64, void* stream);

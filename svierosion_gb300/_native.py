@@ -109,7 +109,8 @@ _SIGS = {
     "svie_conv_supported": (I, [I]),
     "svie_conv_plan_init": (I, [V, I, I, I, V, I, V, Z, V]),
     "svie_conv_apply": (I, [V, I, I, I, V, V, D, D, V, Z, V]),
-    "svie_conv_apply_events": (I, [V, I, I, I, V, V, D, D, V, Z, V, V]),
+    "svie_conv_apply_masked": (I, [V, I, I, I, V, V, D, D, V, Z, V, V, V, V]),
+    "svie_conv_line_flags": (I, [V, I64, I, I, I, I, V, V, V, V]),
     "svie_conv_kernel_hat": (I, [V, I, I, I, V, V]),
     "svie_rfft3": (I, [V, I, I, I, V, V, V]),
     "svie_irfft3": (I, [V, I, I, I, V, V, D, D, V]),

@@ -73,9 +73,6 @@ __constant__ float c_cos7[7] = {1.0f, 0.62348980185873353f, -0.22252093395631440
                                 -0.90096886790241913f, -0.22252093395631440f, 0.62348980185873353f};
 __constant__ float c_sin7[7] = {0.0f, 0.78183148246802981f, 0.97492791218182361f, 0.43388373911755812f,
                                 -0.43388373911755812f, -0.97492791218182361f, -0.78183148246802981f};
-__constant__ float c_cos6[6] = {1.0f, 0.5f, -0.5f, -1.0f, -0.5f, 0.5f};
-__constant__ float c_sin6[6] = {0.0f, 0.86602540378443865f, 0.86602540378443865f, 0.0f,
-                                -0.86602540378443865f, -0.86602540378443865f};
 
 // Forward DFT of R points in place: y_p = sum_q x_q exp(-2 pi i p q / R).
 template <int R>
@@ -157,23 +154,23 @@ SVIE_DEV void dft<5>(float2* x) { dft_odd<5>(x, c_cos5, c_sin5); }
 template <>
 SVIE_DEV void dft<7>(float2* x) { dft_odd<7>(x, c_cos7, c_sin7); }
 
+// 6 = 2 x 3: two 3-point DFTs on the even / odd samples, then twiddles
+// w6^k = exp(-2 pi i k / 6) and a final radix-2 combination.
 template <>
 SVIE_DEV void dft<6>(float2* x) {
-  float2 y[6];
-#pragma unroll
-  for (int p = 0; p < 6; ++p) {
-    float2 acc = x[0];
-#pragma unroll
-    for (int q = 1; q < 6; ++q) {
-      const int t = (p * q) % 6;
-      const float c = c_cos6[t], s = c_sin6[t];
-      acc.x += x[q].x * c + x[q].y * s;
-      acc.y += x[q].y * c - x[q].x * s;
-    }
-    y[p] = acc;
-  }
-#pragma unroll
-  for (int p = 0; p < 6; ++p) x[p] = y[p];
+  float2 e[3] = {x[0], x[2], x[4]};
+  float2 o[3] = {x[1], x[3], x[5]};
+  dft<3>(e);
+  dft<3>(o);
+  const float h = 0.86602540378443865f;
+  const float2 o1 = make_float2(0.5f * o[1].x + h * o[1].y, 0.5f * o[1].y - h * o[1].x);    // o1 * (1/2 - i h)
+  const float2 o2 = make_float2(-0.5f * o[2].x + h * o[2].y, -0.5f * o[2].y - h * o[2].x);  // o2 * (-1/2 - i h)
+  x[0] = cadd(e[0], o[0]);
+  x[3] = csub(e[0], o[0]);
+  x[1] = cadd(e[1], o1);
+  x[4] = csub(e[1], o1);
+  x[2] = cadd(e[2], o2);
+  x[5] = csub(e[2], o2);
 }
 
 // Shared-memory index with one pad slot every 16 complex values: the stride-R
@@ -243,8 +240,11 @@ __host__ __device__ inline int smem_buffer(int W, int n) { return padded_len(W *
 // ----------------------------------------------------------------- z passes
 // Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
 // W complex (paired) lines per CTA; the tile is one contiguous chunk.
+// `lineflag` (optional): lines whose flag lacks bit 0 hold no solid, so their
+// input is zero; a tile without any such line only writes zeros.
 __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ in, float2* __restrict__ out,
-                                                     AxisPlan P, long long nlines, int W, int nzp) {
+                                                     AxisPlan P, long long nlines, int W, int nzp,
+                                                     const uint8_t* __restrict__ lineflag) {
   extern __shared__ float2 sm[];
   const int n = P.n, LS = line_stride(n), nh = n / 2 + 1;
   float2* sa = sm;
@@ -254,8 +254,17 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ i
   const int np = (nl + 1) >> 1;
   const float* src = in + line0 * n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lineflag) {
+    const int any = __syncthreads_or(threadIdx.x < nl ? (__ldg(lineflag + line0 + threadIdx.x) & 1) : 0);
+    if (!any) {
+      float2* dst = out + line0 * nzp;
+      for (int l = warp; l < nl; l += FFT_T / 32)
+        for (int k = lane; k < nh; k += 32) dst[(long long)l * nzp + k] = make_float2(0.f, 0.f);
+      return;
+    }
+  }
   for (int l = warp; l < 2 * np; l += FFT_T / 32) {
-    const bool ok = l < nl;
+    const bool ok = l < nl && (!lineflag || (__ldg(lineflag + line0 + l) & 1));
     float* row = reinterpret_cast<float*>(sa);
     for (int z = lane; z < n; z += 32) row[2 * px((l >> 1) * LS + z) + (l & 1)] = ok ? __ldg(src + l * n + z) : 0.0f;
   }
@@ -276,9 +285,11 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ i
 }
 
 // Inverse: half spectra -> real lines, out = beta + alpha * irfft_unnormalised.
+// `lineflag` (optional): only lines with bit 1 set are written (the others
+// are never read); a tile without such lines returns at once.
 __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ in, float* __restrict__ out,
                                                      AxisPlan P, long long nlines, int W, int nzp, float alpha,
-                                                     float beta) {
+                                                     float beta, const uint8_t* __restrict__ lineflag) {
   extern __shared__ float2 sm[];
   const int n = P.n, LS = line_stride(n);
   float2* sa = sm;
@@ -286,6 +297,10 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
   const long long line0 = (long long)blockIdx.x * 2 * W;
   const int nl = (int)min((long long)2 * W, nlines - line0);
   const int np = (nl + 1) >> 1;
+  if (lineflag) {
+    const int any = __syncthreads_or(threadIdx.x < nl ? (__ldg(lineflag + line0 + threadIdx.x) & 2) : 0);
+    if (!any) return;
+  }
   const float2* src = in + line0 * nzp;
   const bool even = (n & 1) == 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -308,6 +323,7 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
   const float2* r = run_fft(sa, sb, LS, np, P);
   float* dst = out + line0 * n;
   for (int l = warp; l < nl; l += FFT_T / 32) {
+    if (lineflag && !(__ldg(lineflag + line0 + l) & 2)) continue;
     const int w = l >> 1;
     for (int z = lane; z < n; z += 32) {
       const float2 v = r[px(w * LS + z)];
@@ -329,8 +345,13 @@ struct KGeom {
   int ny, nzh;
 };
 
+// Slab skipping: when `slabflag` is given, a CTA returns at once for an outer
+// slab whose flag lacks `need` (bit 0: the forward data of the slab is zero,
+// bit 1: no N value of the slab is read afterwards).
 __global__ void __launch_bounds__(FFT_T) k_fft_strided(float2* __restrict__ data, AxisPlan P, long long stride,
-                                                       int ninner, long long outer_stride, int mode, KGeom K) {
+                                                       int ninner, long long outer_stride, int mode, KGeom K,
+                                                       const uint8_t* __restrict__ slabflag, int need) {
+  if (slabflag && !(__ldg(slabflag + blockIdx.y) & need)) return;
   extern __shared__ float2 sm[];
   const int n = P.n, LS = line_stride(n);
   float2* sa = sm;
@@ -338,12 +359,15 @@ __global__ void __launch_bounds__(FFT_T) k_fft_strided(float2* __restrict__ data
   const int c0 = blockIdx.x * SW;
   const int nl = min(SW, ninner - c0);
   float2* base = data + (long long)blockIdx.y * outer_stride + c0;
-  const bool conj_in = (mode == 1);
-  for (int e = threadIdx.x; e < n * SW; e += FFT_T) {
-    const int k = e >> 3, c = e & 7;
-    if (c < nl) {
-      float2 v = base[(long long)k * stride + c];
-      if (conj_in) v.y = -v.y;
+  // each thread owns column c = tid & 7 and rows k = tid >> 3, + 32, ...
+  const int c = threadIdx.x & 7, k0 = threadIdx.x >> 3;
+  const bool col = c < nl;
+  const long long rstep = 32 * stride;
+  if (col) {
+    const float2* g = base + (long long)k0 * stride + c;
+    for (int k = k0; k < n; k += 32, g += rstep) {
+      float2 v = *g;
+      if (mode == 1) v.y = -v.y;
       sa[px(c * LS + k)] = v;
     }
   }
@@ -352,12 +376,12 @@ __global__ void __launch_bounds__(FFT_T) k_fft_strided(float2* __restrict__ data
   if (mode == 2) {
     const int nyh = K.ny / 2 + 1;
     const int y = blockIdx.y, yr = min(y, K.ny - y);
-    const float* krow = K.kred + (long long)yr * K.nzh + c0;
-    for (int e = threadIdx.x; e < n * SW; e += FFT_T) {
-      const int k = e >> 3, c = e & 7;
-      if (c < nl) {
+    if (col) {
+      const float* krow = K.kred + (long long)yr * K.nzh + c0 + c;
+      const long long kst = (long long)nyh * K.nzh;
+      for (int k = k0; k < n; k += 32) {
         const int kr = min(k, n - k);
-        const float kv = __ldg(krow + (long long)kr * nyh * K.nzh + c);
+        const float kv = __ldg(krow + kr * kst);
         const float2 v = r[px(c * LS + k)];
         r[px(c * LS + k)] = make_float2(v.x * kv, -(v.y * kv));  // conj for the inverse
       }
@@ -366,13 +390,13 @@ __global__ void __launch_bounds__(FFT_T) k_fft_strided(float2* __restrict__ data
     float2* other = (r == sa) ? sb : sa;
     r = run_fft(r, other, LS, nl, P);
   }
-  const bool conj_out = (mode != 0);
-  for (int e = threadIdx.x; e < n * SW; e += FFT_T) {
-    const int k = e >> 3, c = e & 7;
-    if (c < nl) {
+  if (col) {
+    const bool conj_out = (mode != 0);
+    float2* g = base + (long long)k0 * stride + c;
+    for (int k = k0; k < n; k += 32, g += rstep) {
       float2 v = r[px(c * LS + k)];
       if (conj_out) v.y = -v.y;
-      base[(long long)k * stride + c] = v;
+      *g = v;
     }
   }
 }
@@ -492,6 +516,44 @@ __global__ void k_khat_c(const double* __restrict__ Bq, int m, int nx, int ny, i
   }
 }
 
+// Line flags for the masked convolution: bit 0 on (x, y) lines holding band
+// nodes (all solid lines: the padding keeps the grid boundary outside), then
+// bit 1 on those lines dilated by `dil` lines in x and y (every tricubic
+// stencil at a closest point of a band node).
+__global__ void k_mark_lines(const int32_t* __restrict__ band, long long m, int nz, uint8_t* flags) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m) flags[band[t] / nz] = 1;
+}
+
+// tmp[x, y] = any band line within dil lines along x.
+__global__ void k_dilate_lines_x(const uint8_t* __restrict__ flags, uint8_t* __restrict__ tmp, int nx, int ny,
+                                 int dil) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x, x = blockIdx.y;
+  if (y >= ny) return;
+  uint8_t v = 0;
+  for (int d = max(x - dil, 0); d <= min(x + dil, nx - 1) && !v; ++d) v = flags[d * ny + y] & 1;
+  tmp[x * ny + y] = v;
+}
+
+// flags[x, y] |= 2 if tmp has a line within dil lines along y (bit 0 kept).
+__global__ void k_dilate_lines_y(const uint8_t* __restrict__ tmp, uint8_t* __restrict__ flags, int nx, int ny,
+                                 int dil) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x, x = blockIdx.y;
+  if (y >= ny) return;
+  uint8_t v = 0;
+  for (int d = max(y - dil, 0); d <= min(y + dil, ny - 1) && !v; ++d) v = tmp[x * ny + d];
+  if (v) flags[x * ny + y] |= 2;
+}
+
+__global__ void k_slab_flags(const uint8_t* __restrict__ lines, int nx, int ny, uint8_t* slabs) {
+  const int x = blockIdx.x;
+  uint8_t v = 0;
+  for (int y = threadIdx.x; y < ny; y += blockDim.x) v |= lines[x * ny + y];
+  // OR-reduce the two flag bits across the CTA
+  const int b0 = __syncthreads_or(v & 1), b1 = __syncthreads_or(v & 2);
+  if (threadIdx.x == 0) slabs[x] = (uint8_t)((b0 ? 1 : 0) | (b1 ? 2 : 0));
+}
+
 // Full complex64 half spectrum from the reduced real one.
 __global__ void k_khat_expand(const float* __restrict__ K, int nx, int ny, int nzh, float2* __restrict__ out) {
   const long long tot = (long long)nx * ny * nzh;
@@ -571,21 +633,23 @@ static int make_plans(const void* plan, int nx, int ny, int nz, Plans* P) {
 }
 
 static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, float2* spec, float* out, bool fwd,
-                     float alpha, float beta, cudaStream_t s) {
+                     float alpha, float beta, cudaStream_t s, const uint8_t* lineflag = nullptr) {
   const long long nlines = (long long)nx * ny;
   const int W = z_width(nz), nzp = padded_nzh(nz);
   const size_t smem = 2 * (size_t)smem_buffer(W, nz) * sizeof(float2);
   const long long nb = (nlines + 2 * W - 1) / (2 * W);
-  if (fwd) k_fft_z_r2c<<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, W, nzp);
-  else k_fft_z_c2r<<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, W, nzp, alpha, beta);
+  if (fwd) k_fft_z_r2c<<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, W, nzp, lineflag);
+  else k_fft_z_c2r<<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, W, nzp, alpha, beta, lineflag);
 }
 
 // y lines: outer index x, line index kz, element stride nzp.
-static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
+static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s,
+                     const uint8_t* slabflag = nullptr) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const size_t smem = 2 * (size_t)smem_buffer(SW, ny) * sizeof(float2);
   dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)nx);
-  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, KGeom{nullptr, ny, nzh});
+  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, KGeom{nullptr, ny, nzh},
+                                       slabflag, mode == 1 ? 2 : 1);
 }
 
 // x lines: outer index y, line index kz, element stride ny * nzp.
@@ -593,7 +657,8 @@ static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int m
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const size_t smem = 2 * (size_t)smem_buffer(SW, nx) * sizeof(float2);
   dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)ny);
-  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, KGeom{P.kred, ny, nzh});
+  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, KGeom{P.kred, ny, nzh},
+                                       nullptr, 0);
 }
 
 static void gauss_legendre(int n, double* x, double* w) {
@@ -718,35 +783,55 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
   return launch_status("svie_conv_apply", 5);
 }
 
-int svie_conv_apply_events(const void* plan, int nx, int ny, int nz, const float* f, float* out, double alpha,
-                           double beta, void* ws, size_t ws_bytes, void* const* events, void* stream) {
+int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float* f, float* out, double alpha,
+                           double beta, void* ws, size_t ws_bytes, const uint8_t* lineflag, const uint8_t* slabflag,
+                           void* const* events, void* stream) {
   Plans P;
   int st = make_plans(plan, nx, ny, nz, &P);
   if (st) return st;
-  if (!f || !out || !events) {
-    set_error("svie_conv_apply_events: null argument");
+  if (!f || !out || (!lineflag) != (!slabflag)) {
+    set_error("svie_conv_apply_masked: null input/output, or only one of the two flag arrays");
     return SVIE_ERR_ARG;
   }
   if (!ws || ws_bytes < svie_conv_workspace_bytes(nx, ny, nz)) {
-    set_error("svie_conv_apply_events: workspace too small");
+    set_error("svie_conv_apply_masked: workspace too small");
     return SVIE_ERR_WORKSPACE;
   }
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
   float2* spec = (float2*)ws;
   cudaEvent_t* ev = (cudaEvent_t*)events;
-  cudaEventRecord(ev[0], s);
-  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s);
-  cudaEventRecord(ev[1], s);
-  launch_y(P, nx, ny, nz, spec, 0, s);
-  cudaEventRecord(ev[2], s);
+  if (ev) cudaEventRecord(ev[0], s);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, lineflag);
+  if (ev) cudaEventRecord(ev[1], s);
+  launch_y(P, nx, ny, nz, spec, 0, s, slabflag);
+  if (ev) cudaEventRecord(ev[2], s);
   launch_x(P, nx, ny, nz, spec, 2, s);
-  cudaEventRecord(ev[3], s);
-  launch_y(P, nx, ny, nz, spec, 1, s);
-  cudaEventRecord(ev[4], s);
-  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s);
-  cudaEventRecord(ev[5], s);
-  return launch_status("svie_conv_apply_events", 5);
+  if (ev) cudaEventRecord(ev[3], s);
+  launch_y(P, nx, ny, nz, spec, 1, s, slabflag);
+  if (ev) cudaEventRecord(ev[4], s);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag);
+  if (ev) cudaEventRecord(ev[5], s);
+  return launch_status("svie_conv_apply_masked", 5);
+}
+
+int svie_conv_line_flags(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, uint8_t* lineflag,
+                         uint8_t* slabflag, uint8_t* tmp, void* stream) {
+  if (!lineflag || !slabflag || !tmp || m < 0 || (m > 0 && !band) || dilation < 0) {
+    set_error("svie_conv_line_flags: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(lineflag, 0, (size_t)nx * ny, s) != cudaSuccess) {
+    set_error("svie_conv_line_flags: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  if (m > 0) k_mark_lines<<<blocks_for(m, 256), 256, 0, s>>>(band, m, nz, lineflag);
+  const dim3 g((ny + 127) / 128, nx);
+  k_dilate_lines_x<<<g, 128, 0, s>>>(lineflag, tmp, nx, ny, dilation);
+  k_dilate_lines_y<<<g, 128, 0, s>>>(tmp, lineflag, nx, ny, dilation);
+  k_slab_flags<<<nx, 256, 0, s>>>(lineflag, nx, ny, slabflag);
+  return launch_status("svie_conv_line_flags", m > 0 ? 4 : 3);
 }
 
 int svie_conv_kernel_hat(const void* plan, int nx, int ny, int nz, void* out_c64, void* stream) {

@@ -70,22 +70,27 @@ class BallConvolution:
             self._khat = k
         return self._khat
 
-    def apply_into(self, f: torch.Tensor, out: torch.Tensor, alpha: float, beta: float, events=None) -> torch.Tensor:
+    def apply_into(self, f: torch.Tensor, out: torch.Tensor, alpha: float, beta: float, events=None,
+                   flags=None) -> torch.Tensor:
         """out = beta + alpha * G * (w (*) f), G = number of nodes (unnormalised FFT pair).
 
-        ``events``: optional six timing events recorded around the five passes."""
+        ``events``: optional six timing events recorded around the five passes;
+        ``flags``: optional (lineflag, slabflag) from svie_conv_line_flags -- then
+        only the N values that stencils at band closest points read are valid."""
         nx, ny, nz = self.grid.shape
         f = f.reshape(-1)
         if f.dtype != torch.float32 or not f.is_contiguous():
             f = f.to(torch.float32).contiguous()
         ws = nat.scratch(self.device).get("conv", self.workspace_bytes)
-        if events is None:
+        if events is None and flags is None:
             nat.call("svie_conv_apply", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)),
                      float(alpha), float(beta), nat.ptr(ws), ws.numel(), nat.stream())
         else:
             from .profiling import KernelTimer
-            nat.call("svie_conv_apply_events", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)),
-                     float(alpha), float(beta), nat.ptr(ws), ws.numel(), KernelTimer.handles(events), nat.stream())
+            lf, sf = flags if flags is not None else (None, None)
+            ev = KernelTimer.handles(events) if events is not None else None
+            nat.call("svie_conv_apply_masked", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)),
+                     float(alpha), float(beta), nat.ptr(ws), ws.numel(), nat.ptr(lf), nat.ptr(sf), ev, nat.stream())
         return out
 
     def interior_volume(self, fractions: torch.Tensor) -> torch.Tensor:
@@ -98,9 +103,10 @@ class BallConvolution:
         out = torch.empty(self.grid.shape, dtype=torch.float32, device=self.device)
         return self.exterior_fraction_into(fractions, out)
 
-    def exterior_fraction_into(self, fractions: torch.Tensor, out: torch.Tensor, events=None) -> torch.Tensor:
+    def exterior_fraction_into(self, fractions: torch.Tensor, out: torch.Tensor, events=None,
+                               flags=None) -> torch.Tensor:
         a = -self.grid.spacing ** 3 / (self.ball_volume * self.grid.size)
-        return self.apply_into(fractions, out, a, 1.0, events=events)
+        return self.apply_into(fractions, out, a, 1.0, events=events, flags=flags)
 
 
 def sphere_exterior_fraction(radius_ball: float, radius_sphere: float) -> float:

@@ -113,3 +113,36 @@ def test_convolution_vs_oracle_float64():
     conv = S.BallConvolution(g, r)
     N = conv.exterior_fraction(torch.from_numpy(f).cuda()).cpu().numpy()
     assert np.abs(N - N64).max() < 1e-5
+
+
+def test_masked_convolution_matches_on_needed_lines():
+    """The convolution that skips empty and unread lines gives bit-identical N
+    on every (x, y) line a closest-point stencil can read."""
+    from svierosion_gb300 import _native as nat
+    from svierosion_gb300.evolve import LINE_DILATION
+    R, h, r = 0.8, 0.04, 0.2
+    g = Grid.around([-R, -R * 0.6, -R * 0.5], [R, R * 0.6, R * 0.5], h, padding=r + 12 * h)
+    X, Y, Z = [torch.tensor(a, device="cuda") for a in np.meshgrid(*g.axes(), indexing="ij")]
+    phi = (torch.sqrt(X ** 2 + (Y / 0.6) ** 2 + (Z / 0.5) ** 2) - R).float()
+    ls = S.LevelSet(phi, g, width=6)
+    conv = S.BallConvolution(g, r)
+    nx, ny, nz = g.shape
+    lf = torch.empty(nx * ny, dtype=torch.uint8, device="cuda")
+    sf = torch.empty(nx, dtype=torch.uint8, device="cuda")
+    tmp = torch.empty(nx * ny, dtype=torch.uint8, device="cuda")
+    nat.call("svie_conv_line_flags", nat.ptr(ls.work32), ls.work32.numel(), nx, ny, nz, LINE_DILATION, nat.ptr(lf),
+             nat.ptr(sf), nat.ptr(tmp), nat.stream())
+    f = ls.dense_fractions()
+    full = conv.exterior_fraction(f)
+    masked = torch.full(g.shape, float("nan"), device="cuda")
+    conv.exterior_fraction_into(f, masked, flags=(lf, sf))
+    need = (lf.view(nx, ny) & 2).bool()
+    band_lines = (lf.view(nx, ny) & 1).bool()
+    assert need.any() and (~need).any() and bool((need | ~band_lines).all())
+    assert torch.equal(masked[need], full[need])
+    # every line holding a band node's closest-point stencil is flagged
+    cp = ls.closest_points(ls.band)
+    base = torch.floor(cp).long() - 1
+    for dx in range(4):
+        for dy in range(4):
+            assert bool(need[base[:, 0] + dx, base[:, 1] + dy].all())
