@@ -359,6 +359,32 @@ int svie_sdf_crossings(const double* tri64, int64_t ntri, int nx, int ny, int nz
                        int signed_rule, int32_t* acc, void* stream);
 int svie_sdf_inside(const int32_t* acc, int nx, int ny, int nz, int axis, int signed_rule,
                     uint8_t* votes, void* stream);
+/* Mesh preprocessing (the host numpy work of sdf.py:205-208,385,398-402
+ * and meshio.py:80-105).  svie_mesh_tri_index: triangle soup in index
+ * coordinates (T,3,3) float64 and float32 and the longest edge (float bits,
+ * atomically maxed into *max_edge_bits, which the caller zeroes). */
+int svie_mesh_tri_index(const double* vertices, const int32_t* faces, int64_t T, double ox, double oy,
+                        double oz, double h, double* tri64, float* tri32, uint32_t* max_edge_bits,
+                        void* stream);
+/* Vertex welding (np.unique over rows): ids[i] = representative index of the
+ * points exactly equal to point i (-0.0 == +0.0).  *overflow is set if the
+ * table is too full (it is sized by svie_mesh_weld_table_bytes). */
+size_t svie_mesh_weld_table_bytes(int64_t n);
+int svie_mesh_weld(const double* points, int64_t n, void* table, size_t table_bytes, int32_t* ids,
+                   int* overflow, void* stream);
+/* Vertex stars as CSR over nv vertex ids: vid = weld[faces] (faces NULL: weld
+ * is per soup corner), deg, first (exclusive scan), star = triangle ids
+ * grouped by vertex; cursor is nv ints of scratch. */
+int svie_mesh_stars(const int32_t* faces, const int32_t* weld, int64_t T, int64_t nv, int32_t* vid,
+                    int32_t* deg, int32_t* first, int32_t* cursor, int32_t* star, void* stream);
+/* Edge topology of the faces as given: out4 = {edges, boundary, non-manifold,
+ * misoriented}. */
+size_t svie_mesh_edge_table_bytes(int64_t T);
+int svie_mesh_edge_topology(const int32_t* faces, int64_t T, void* table, size_t table_bytes,
+                            uint64_t* out4, int* overflow, void* stream);
+/* Signed volume about the point c (meshio.py:80-83), float64. */
+int svie_mesh_signed_volume(const double* vertices, const int32_t* faces, int64_t T, double cx,
+                            double cy, double cz, double* out, void* stream);
 /* phi = inside ? -(min(dist, band) * h) : +(...), inside = 2*votes > naxes
  * (sdf.py:361, 409-410). */
 int svie_sdf_finalize(const float* dist, const uint8_t* votes, int64_t n, int naxes, float band,

@@ -128,6 +128,13 @@ _SIGS = {
     "svie_reinit_rhs": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),
     "svie_reinit_geometry_unpack": (I, [V, I64, V, V, V, V, V]),
     "svie_dilate": (I, [V, I, I, I, I, V, V, V]),
+    "svie_mesh_tri_index": (I, [V, V, I64, D, D, D, D, V, V, V, V]),
+    "svie_mesh_weld_table_bytes": (Z, [I64]),
+    "svie_mesh_weld": (I, [V, I64, V, Z, V, V, V]),
+    "svie_mesh_stars": (I, [V, V, I64, I64, V, V, V, V, V, V]),
+    "svie_mesh_edge_table_bytes": (Z, [I64]),
+    "svie_mesh_edge_topology": (I, [V, I64, V, Z, V, V, V]),
+    "svie_mesh_signed_volume": (I, [V, V, I64, D, D, D, V, V]),
     "svie_sdf_keys_init": (I, [V, I64, V]),
     "svie_sdf_near_field": (I, [V, V, I64, I, I, I, D, F, V, V]),
     "svie_sdf_unpack": (I, [V, I64, V, V, V, V]),
@@ -213,17 +220,6 @@ class Scratch:
             b = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
             self._buf[name] = b
         return b
-
-
-_scratch: dict[int, Scratch] = {}
-
-
-def scratch(device) -> Scratch:
-    d = torch.device(device)
-    key = d.index if d.index is not None else torch.cuda.current_device()
-    if key not in _scratch:
-        _scratch[key] = Scratch(torch.device("cuda", key))
-    return _scratch[key]
 
 
 _h2d_bytes = 0

@@ -1,0 +1,259 @@
+"""Batched and served erosion: many independent solids on one GPU.
+
+Every solid (an :class:`ErosionJob`) owns its level set, simulation,
+workspaces and CUDA stream.  The scheduler advances all active jobs in
+rounds: it enqueues one TVD-RK3 step of every job on that job's stream (no
+host synchronisation), then finishes the steps job by job (one 256-byte read
+back each, plus the reference's rare extra work: regula falsi on the last
+step, reinitialisation).  Kernels of different jobs overlap on the GPU, so
+small grids that cannot fill 152 SMs alone fill them together, and each job
+stops independently.  A job's arithmetic is exactly the plain path's, so its
+result is the same alone and in the mix.
+
+:class:`ErosionServer` runs an open-loop request stream on top: requests are
+admitted as slots and HBM (estimated footprint) free up, folded into the
+running batch at step boundaries, and their latency (arrival to result) is
+recorded.
+"""
+
+from __future__ import annotations
+
+import math
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .api import ErosionParams, make_grid
+from .evolve import ErosionSimulation
+from .grid import get_device
+from .levelset import LevelSet, tricubic
+from .meshio import TriMesh
+from .sdf import mesh_to_sdf
+
+# Device bytes per grid node while a job runs: phi, occupancy, N field,
+# padded half spectrum, the reinitialisation copy of phi and its two masks,
+# the maintained (k1, k2) field of curvature laws, plus the transient SDF
+# arrays (keys, distance, triangle ids, masks) during set-up.
+BYTES_PER_NODE = 48
+BYTES_PER_BAND_NODE = 40
+
+
+def footprint_bytes(grid_nodes: int, band_nodes: int | None = None) -> int:
+    """Estimated peak device memory of one job."""
+    band = band_nodes if band_nodes is not None else grid_nodes // 8
+    return int(BYTES_PER_NODE * grid_nodes + BYTES_PER_BAND_NODE * band + (64 << 20))
+
+
+@dataclass
+class JobResult:
+    name: str
+    stop_reason: str
+    fraction: float
+    time: float
+    steps: int
+    band_updates: int
+    history: list = field(default_factory=list)
+    snapshots: list = field(default_factory=list)      # [(fraction, time, band phi on the host)]
+    grid_shape: tuple = ()
+    setup_s: float = 0.0
+    wall_s: float = 0.0
+
+
+class ErosionJob:
+    """One erosion solve that can be advanced a step at a time."""
+
+    def __init__(self, mesh: TriMesh, params: ErosionParams, name: str = "", device=None, stream=None,
+                 keep_snapshot_phi: bool = False):
+        self.mesh = mesh
+        self.params = params
+        self.name = name
+        self.device = get_device(device if device is not None else params.device)
+        self.stream = stream if stream is not None else torch.cuda.Stream(device=self.device)
+        self.keep_snapshot_phi = keep_snapshot_phi
+        self.grid = make_grid(mesh, params)
+        self.done = False
+        self.result: JobResult | None = None
+        self.sim: ErosionSimulation | None = None
+
+    @property
+    def grid_nodes(self) -> int:
+        return self.grid.size
+
+    def footprint(self) -> int:
+        return footprint_bytes(self.grid.size)
+
+    def setup(self) -> None:
+        """SDF, narrow band and simulation on the job's stream (erode(), api.py:200-233)."""
+        t0 = time.time()
+        p = self.params
+        lo, hi = self.mesh.bounds
+        self.law = p.make_law(length_scale=float((hi - lo).max()))
+        with torch.cuda.stream(self.stream):
+            phi = mesh_to_sdf(self.mesh, self.grid, band=p.band, device=self.device)
+            self.ls = LevelSet(phi, self.grid, width=p.band)
+            self.sim = ErosionSimulation(self.ls, self.law, cfl=p.cfl, feedback_cfl=p.feedback_cfl,
+                                         parabolic_cfl=p.parabolic_cfl, reinit_distance=p.reinit_distance,
+                                         reinit_iterations=p.reinit_iterations)
+            if self.law.requires_svi and self.law.s == 1:
+                n0 = self.sim.svi_field()
+                nmax = float(tricubic(n0.view(-1), self.grid.shape,
+                                      self.ls.closest_points(self.ls.interface_nodes())).max())
+                if nmax >= self.law.t:
+                    raise ValueError(f"max N_r on the initial surface is {nmax:.4f} >= t = {self.law.t}")
+            self.targets = sorted({float(f) for f in p.snapshots if f > p.target_fraction},
+                                  reverse=True) + [p.target_fraction]
+            self.snapshots = []
+            self.sim.begin_run(self.targets[0], max_steps=p.max_steps)
+        self.setup_s = time.time() - t0
+        self.t_start = time.time()
+
+    def launch(self) -> bool:
+        """Enqueue the next step; False once the job has finished."""
+        if self.done:
+            return False
+        with torch.cuda.stream(self.stream):
+            while not self.sim.step_launch():
+                res = self.sim.end_run()
+                snap_phi = None
+                if self.keep_snapshot_phi:
+                    snap_phi = nat.d2h(self.ls.flat[self.ls.band32])
+                self.snapshots.append((res.fraction, self.sim.time, snap_phi))
+                self.targets.pop(0)
+                if res.stop_reason != "target_volume" or not self.targets:
+                    self._complete(res)
+                    return False
+                self.sim.begin_run(self.targets[0], max_steps=self.params.max_steps)
+        return True
+
+    def finish(self) -> None:
+        with torch.cuda.stream(self.stream):
+            self.sim.step_finish()
+
+    def _complete(self, res) -> None:
+        self.done = True
+        self.result = JobResult(self.name, res.stop_reason, res.fraction, self.sim.time, self.sim.steps,
+                                self.sim.band_updates, list(self.sim.history), self.snapshots[:-1],
+                                tuple(self.grid.shape), self.setup_s, time.time() - self.t_start)
+
+    def release(self) -> None:
+        """Drop device state (the result stays)."""
+        self.sim = None
+        self.ls = None
+
+
+class BatchedErosion:
+    """Advance many solids together; each stops independently (spec batched form)."""
+
+    def __init__(self, jobs: list[ErosionJob]):
+        self.jobs = list(jobs)
+
+    def run(self, release: bool = True) -> list[JobResult]:
+        for j in self.jobs:
+            j.setup()
+        active = list(self.jobs)
+        while active:
+            launched = [j for j in active if j.launch()]
+            for j in launched:
+                j.finish()
+            still = []
+            for j in active:
+                if j.done:
+                    if release:
+                        j.release()
+                else:
+                    still.append(j)
+            active = still
+        torch.cuda.synchronize()
+        return [j.result for j in self.jobs]
+
+
+def run_plain(jobs: list[ErosionJob]) -> list[JobResult]:
+    """The same jobs one at a time (the plain form)."""
+    out = []
+    for j in jobs:
+        j.setup()
+        while not j.done:
+            if j.launch():
+                j.finish()
+        torch.cuda.synchronize()
+        out.append(j.result)
+        j.release()
+    return out
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds after the start of the stream
+    mesh: TriMesh
+    params: ErosionParams
+    admitted: float = math.nan
+    completed: float = math.nan
+    result: JobResult | None = None
+
+
+class ErosionServer:
+    """Continuous batching of erosion requests under an HBM budget."""
+
+    def __init__(self, hbm_budget_bytes: int = 150 << 30, max_active: int = 64, device=None):
+        self.budget = int(hbm_budget_bytes)
+        self.max_active = int(max_active)
+        self.device = get_device(device)
+        self.queue: deque[Request] = deque()
+        self.active: list[tuple[Request, ErosionJob]] = []
+        self.in_use = 0
+        self.done: list[Request] = []
+
+    def submit(self, req: Request) -> None:
+        self.queue.append(req)
+
+    def _admit(self, now: float) -> None:
+        while self.queue and len(self.active) < self.max_active and self.queue[0].arrival <= now:
+            req = self.queue[0]
+            job = ErosionJob(req.mesh, req.params, name=str(req.rid), device=self.device)
+            need = job.footprint()
+            if self.active and self.in_use + need > self.budget:
+                return  # wait for memory (first-come first-served)
+            self.queue.popleft()
+            job.setup()
+            req.admitted = now
+            self.in_use += need
+            self.active.append((req, job))
+
+    def run(self, requests: list[Request]) -> dict:
+        """Open-loop: request i becomes visible at t0 + arrival_i."""
+        for r in sorted(requests, key=lambda r: r.arrival):
+            self.submit(r)
+        t0 = time.time()
+        updates = 0
+        while self.queue or self.active:
+            now = time.time() - t0
+            self._admit(now)
+            if not self.active:
+                time.sleep(max(0.0, min(self.queue[0].arrival - now, 0.01)))
+                continue
+            launched = [(r, j) for r, j in self.active if j.launch()]
+            for _, j in launched:
+                j.finish()
+            still = []
+            for r, j in self.active:
+                if j.done:
+                    r.completed = time.time() - t0
+                    r.result = j.result
+                    updates += j.result.band_updates
+                    self.in_use -= j.footprint()
+                    j.release()
+                    self.done.append(r)
+                else:
+                    still.append((r, j))
+            self.active = still
+        wall = time.time() - t0
+        lat = np.array([r.completed - r.arrival for r in self.done])
+        return {"requests": len(self.done), "wall_s": wall, "solves_per_s": len(self.done) / wall,
+                "band_updates_per_s": updates / wall,
+                "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                              "p99": float(np.percentile(lat, 99)), "max": float(lat.max())}}

@@ -49,7 +49,7 @@ def _read(t: torch.Tensor, dtype: np.dtype):
 class LevelSet:
     """A level set function with an explicitly stored narrow band (levelset.py:51-183)."""
 
-    def __init__(self, phi: torch.Tensor, grid: Grid, width: float = 6.0):
+    def __init__(self, phi: torch.Tensor, grid: Grid, width: float = 6.0, scratch: nat.Scratch | None = None):
         if tuple(phi.shape) != tuple(grid.shape):
             raise ValueError("phi shape does not match grid")
         if grid.size >= 2 ** 31:
@@ -60,6 +60,9 @@ class LevelSet:
         dev = phi.device if phi.is_cuda else get_device()
         self.phi = phi.to(device=dev, dtype=torch.float32).contiguous()
         self.device = self.phi.device
+        # workspaces of this level set (and of the simulation that evolves it):
+        # one set per instance, so that solids on different streams never share
+        self.scratch = scratch if scratch is not None else nat.Scratch(self.device)
         self.strides = tuple(int(s) for s in grid.strides)
         self.occ = torch.empty(grid.size, dtype=torch.float32, device=self.device)
         self.occ_current = False
@@ -93,7 +96,7 @@ class LevelSet:
         cap = self.width * self.h
         n = self.grid.size
         nx, ny, nz = self.grid.shape
-        sc = nat.scratch(self.device)
+        sc = self.scratch
         wsb = nat.lib().svie_band_workspace_bytes(n)
         ws = sc.get("band", wsb)
         thresh = nat.f32(cap * (1 - 1e-5))
@@ -144,7 +147,7 @@ class LevelSet:
         if m == 0:
             return torch.empty(0, dtype=torch.int64, device=self.device)
         mask = interface_mask(self.flat, idx32, *self.strides).view(torch.uint8)
-        sc = nat.scratch(self.device)
+        sc = self.scratch
         ws = sc.get("select", nat.lib().svie_band_workspace_bytes(m))
         cnt = sc.get("select_count", 8)
         nat.call("svie_mask_scan", nat.ptr(mask), m, nat.ptr(ws), ws.numel(), nat.ptr(cnt), nat.stream())
@@ -155,7 +158,7 @@ class LevelSet:
         return out.to(torch.int64)
 
     def _volume_kernel(self, write_occ: bool):
-        sc = nat.scratch(self.device)
+        sc = self.scratch
         m = self.work32.numel()
         ws = sc.get("volume", nat.lib().svie_volume_workspace_bytes(m))
         nat.call("svie_band_volume", nat.ptr(self.flat), nat.ptr(self.work32), m, *self.strides,
@@ -240,7 +243,7 @@ class LevelSet:
         """Subcell-fixed PDE reinitialisation (Min 2010) on the dilated band (levelset.py:154-183)."""
         n = self.grid.size
         nx, ny, nz = self.grid.shape
-        sc = nat.scratch(self.device)
+        sc = self.scratch
         mask = sc.get("reinit_mask", n)
         tmp = sc.get("reinit_tmp", n)
         nat.call("svie_reinit_mask", nat.ptr(self.band32), self.band32.numel(), nx, ny, nz, int(dilation), MARGIN,

@@ -36,7 +36,7 @@ def _ball_weights_device(radius, spacing, quad, device) -> torch.Tensor:
 class BallConvolution:
     """Cached kernel spectrum on a grid; evaluates interior ball volumes (svi.py:58-93)."""
 
-    def __init__(self, grid: Grid, radius: float, device=None, quad: int = 32):
+    def __init__(self, grid: Grid, radius: float, device=None, quad: int = 32, scratch=None):
         self.grid = grid
         self.radius = float(radius)
         self.device = get_device(device)
@@ -58,6 +58,7 @@ class BallConvolution:
                  init_ws.numel(), nat.stream())
         del init_ws
         self.workspace_bytes = L.svie_conv_workspace_bytes(nx, ny, nz)
+        self.scratch = scratch if scratch is not None else nat.Scratch(self.device)
         self._khat = None
 
     @property
@@ -81,7 +82,7 @@ class BallConvolution:
         f = f.reshape(-1)
         if f.dtype != torch.float32 or not f.is_contiguous():
             f = f.to(torch.float32).contiguous()
-        ws = nat.scratch(self.device).get("conv", self.workspace_bytes)
+        ws = self.scratch.get("conv", self.workspace_bytes)
         if events is None and flags is None:
             nat.call("svie_conv_apply", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)),
                      float(alpha), float(beta), nat.ptr(ws), ws.numel(), nat.stream())

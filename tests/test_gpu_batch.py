@@ -1,0 +1,73 @@
+"""Batched and served forms: every job gives the same result alone and in the mix."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+if torch.cuda.is_available():
+    import svierosion_gb300 as S
+    from svierosion_gb300 import shapes
+    from svierosion_gb300.batch import BatchedErosion, ErosionJob, ErosionServer, Request, run_plain
+
+
+def _jobs():
+    frag = shapes.fragment(3, seed=5)
+    L = float((frag.bounds[1] - frag.bounds[0]).max())
+    specs = [
+        (shapes.cube(1.0), S.ErosionParams(law="svi", radius=0.15, k=1, s=1, t=0.93, resolution=24,
+                                           target_fraction=0.9, snapshots=(0.95,))),
+        (frag, S.ErosionParams(law="svi", radius=0.08 * L, k=0, s=0, resolution=32, target_fraction=0.93)),
+        (shapes.cube(1.0), S.ErosionParams(law="mean", alpha=1.0, resolution=24, target_fraction=0.97,
+                                           max_steps=25)),
+        (frag, S.ErosionParams(law="gauss", alpha=0.25, resolution=28, target_fraction=0.98, max_steps=15)),
+    ]
+    return [ErosionJob(m, p, name=str(i)) for i, (m, p) in enumerate(specs)]
+
+
+def _same(a, b):
+    assert a.stop_reason == b.stop_reason and a.steps == b.steps
+    fa = np.array([r.fraction for r in a.history])
+    fb = np.array([r.fraction for r in b.history])
+    np.testing.assert_array_equal(fa, fb)
+    np.testing.assert_array_equal([r.dt for r in a.history], [r.dt for r in b.history])
+    assert [s[:2] for s in a.snapshots] == [s[:2] for s in b.snapshots]
+
+
+def test_batched_equals_plain():
+    plain = run_plain(_jobs())
+    batched = BatchedErosion(_jobs()).run()
+    for a, b in zip(plain, batched):
+        _same(a, b)
+    assert plain[0].stop_reason == "target_volume" and len(plain[0].snapshots) == 1
+    assert abs(plain[0].fraction - 0.9) < 1e-5
+
+
+def test_served_equals_plain_and_reports_latency():
+    plain = run_plain(_jobs())
+    reqs = [Request(i, arr, j.mesh, j.params) for i, (arr, j) in enumerate(zip([0.0, 0.0, 0.02, 0.05], _jobs()))]
+    srv = ErosionServer(hbm_budget_bytes=8 << 30, max_active=3)
+    stats = srv.run(reqs)
+    assert stats["requests"] == 4
+    assert stats["latency_s"]["p99"] >= stats["latency_s"]["p50"] > 0
+    by_id = {r.rid: r.result for r in srv.done}
+    for i, a in enumerate(plain):
+        _same(a, by_id[i])
+
+
+def test_admission_respects_the_budget():
+    jobs = _jobs()
+    reqs = [Request(i, 0.0, j.mesh, j.params) for i, j in enumerate(jobs)]
+    one = max(j.footprint() for j in jobs)
+    srv = ErosionServer(hbm_budget_bytes=one, max_active=8)
+    peak = []
+    orig = srv._admit
+
+    def admit(now):
+        orig(now)
+        peak.append(len(srv.active))
+
+    srv._admit = admit
+    stats = srv.run(reqs)
+    assert stats["requests"] == 4 and max(peak) == 1
