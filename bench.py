@@ -263,13 +263,14 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     e1 = torch.cuda.Event(enable_timing=True)
     u0 = sim.band_updates
     l0 = lib.svie_launch_count()
+    g0 = sim.kernel_launches
     e0.record()
     sim.run(target_fraction=None, max_steps=args.steps)
     e1.record()
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    launches = lib.svie_launch_count() - l0
+    launches = lib.svie_launch_count() - l0 + (sim.kernel_launches - g0)
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     updates = sim.band_updates - u0

@@ -50,3 +50,82 @@ class KernelTimer:
                 acc[nm].append(evs[i].elapsed_time(evs[i + 1]))
         return {k: {"launches": len(v), "total_ms": float(sum(v)), "mean_ms": float(sum(v) / len(v))}
                 for k, v in acc.items()}
+
+
+def _synthetic_levelset(shape, h):
+    """Analytic ellipsoid (semi-axes 1, 0.7, 0.5) level set on a grid of `shape`."""
+    import svierosion_gb300 as S
+
+    g = S.Grid(tuple(-0.5 * (n - 1) * h for n in shape), h, tuple(shape))
+    ax = [torch.tensor(a, device="cuda", dtype=torch.float32) for a in g.axes()]
+    X, Y, Z = torch.meshgrid(*ax, indexing="ij")
+    phi = (torch.sqrt(X ** 2 + (Y / 0.7) ** 2 + (Z / 0.5) ** 2) - 1.0) * 0.6
+    del X, Y, Z
+    return S.LevelSet(phi.float(), g, width=6)
+
+
+def main(argv=None) -> int:
+    """Profiling driver for ncu captures of the step kernels on a synthetic level set.
+
+        python -m svierosion_gb300.profiling --grid 448x336x245 --steps 2     # RK3 steps (FFT + stages)
+        python -m svierosion_gb300.profiling --grid 448x336x245 --reinit 3    # reinitialisation sub-steps
+    """
+    import argparse
+    import time
+
+    import svierosion_gb300 as S
+    from svierosion_gb300 import _native as nat
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--grid", default="448x336x245")
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--reinit", type=int, default=0)
+    a = ap.parse_args(argv)
+    shape = tuple(int(v) for v in a.grid.split("x"))
+    h = 2.078 / 400
+    ls = _synthetic_levelset(shape, h)
+    print("grid", shape, "band", ls.band32.numel(), flush=True)
+    if a.reinit:
+        n = ls.grid.size
+        nx, ny, nz = shape
+        sc = ls.scratch
+        for _ in range(a.reinit):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+            ev[0].record()
+            mask, tmp = sc.get("reinit_mask", n), sc.get("reinit_tmp", n)
+            nat.call("svie_reinit_mask", nat.ptr(ls.band32), ls.band32.numel(), nx, ny, nz, 3, 4, nat.ptr(mask),
+                     nat.ptr(tmp), nat.stream())
+            ev[1].record()
+            ws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
+            cnt = sc.get("reinit_count", 8)
+            nat.call("svie_brick_scan", 0, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
+                     nat.stream())
+            m = int(cnt[:8].cpu().view(torch.int64)[0])
+            idx = sc.get("reinit_idx", 4 * m)[:4 * m].view(torch.int32)
+            nat.call("svie_brick_write", 0, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
+                     nat.stream())
+            geo = sc.get("reinit_geo", nat.lib().svie_reinit_geometry_bytes(m))
+            nat.call("svie_reinit_geometry", nat.ptr(ls.flat), nat.ptr(idx), m, *ls.strides, ls.h, 0.45, nat.ptr(geo),
+                     nat.stream())
+            ev[2].record()
+            pt = sc.get("reinit_phi", 4 * n)
+            nat.call("svie_reinit_iterate", nat.ptr(ls.flat), nat.ptr(pt), n, nat.ptr(idx), m, *ls.strides, ls.h,
+                     nat.ptr(geo), 20, nat.stream())
+            ev[3].record()
+            ls.rebuild_band()
+            ev[4].record()
+            torch.cuda.synchronize()
+            t = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
+            print("work set %d mask %.3f compact+geometry %.3f 40 sweeps %.3f rebuild %.3f ms" % (m, *t), flush=True)
+        return 0
+    law = S.SVIPowerLaw(0.05 * 2.078, 1, 1, 0.93)
+    sim = S.ErosionSimulation(ls, law)
+    t0 = time.time()
+    res = sim.run(target_fraction=None, max_steps=a.steps)
+    torch.cuda.synchronize()
+    print("steps", len(res.history), "time", round(time.time() - t0, 4), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

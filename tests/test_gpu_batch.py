@@ -71,3 +71,20 @@ def test_admission_respects_the_budget():
     srv._admit = admit
     stats = srv.run(reqs)
     assert stats["requests"] == 4 and max(peak) == 1
+
+
+def test_cuda_graph_replay_matches_eager_launches():
+    res = {}
+    for graphs in (False, True):
+        m = shapes.cube(1.0)
+        p = S.ErosionParams(law="svi", radius=0.15, k=1, s=1, t=0.93, resolution=24)
+        g = S.make_grid(m, p)
+        ls = S.LevelSet(S.mesh_to_sdf(m, g), g)
+        sim = S.ErosionSimulation(ls, p.make_law())
+        sim.use_graphs = graphs
+        res[graphs] = sim.run(target_fraction=0.85)
+        if graphs:
+            assert sim.graph_replays > 0
+    a, b = res[False], res[True]
+    assert a.stop_reason == b.stop_reason and a.steps == b.steps
+    np.testing.assert_array_equal([r.fraction for r in a.history], [r.fraction for r in b.history])
