@@ -496,7 +496,7 @@ def exterior_fraction(fractions3, khat, radius, spacing):
     """svi.py:84-93."""
     fh = np.fft.rfftn(fractions3.astype(F32)).astype(np.complex64)
     fh *= khat
-    g = np.fft.irfftn(fh, s=fractions3.shape).astype(F32) * F32(spacing ** 3)
+    g = np.fft.irfftn(fh, s=fractions3.shape, axes=(0, 1, 2)).astype(F32) * F32(spacing ** 3)
     ball_volume = 4.0 / 3.0 * math.pi * radius ** 3
     return (g * F32(-1.0 / ball_volume) + F32(1.0)).astype(F32)
 
