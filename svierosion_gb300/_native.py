@@ -22,6 +22,11 @@ LIB_PATH = Path(__file__).resolve().parent / "libsvie.so"
 _lib = None
 
 
+# status codes (include/svie.h)
+SVIE_OK, SVIE_ERR_ARG, SVIE_ERR_LAUNCH, SVIE_ERR_WORKSPACE, SVIE_ERR_MARGIN, SVIE_ERR_UNSUPPORTED, \
+    SVIE_ERR_CAPACITY = range(7)
+
+
 class SvieError(RuntimeError):
     """A failure reported by the CUDA library (status code + message)."""
 

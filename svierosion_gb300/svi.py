@@ -9,6 +9,7 @@ spectrum multiply fused into the x pass (csrc/fft.cu).
 from __future__ import annotations
 
 import math
+from collections import OrderedDict
 
 import numpy as np
 import torch
@@ -23,13 +24,34 @@ def ball_cell_weights(radius: float, spacing: float, quad: int = 32) -> np.ndarr
     return w.cpu().numpy()
 
 
+_WEIGHTS_CACHE: "OrderedDict[tuple, tuple]" = OrderedDict()
+_WEIGHTS_CACHE_SIZE = 16
+
+
 def _ball_weights_device(radius, spacing, quad, device) -> torch.Tensor:
+    """Device ball weights, computed once per (radius, spacing, quad, device) and kept read-only.
+
+    Solids of one served stream share the same few radii and spacings; the
+    cache entry carries an event so that a reader on another stream waits
+    for the producing kernel."""
+    key = (float(radius), float(spacing), int(quad), torch.device(device).index)
+    hit = _WEIGHTS_CACHE.get(key)
+    if hit is not None:
+        _WEIGHTS_CACHE.move_to_end(key)
+        w, ev = hit
+        torch.cuda.current_stream(w.device).wait_event(ev)
+        return w
     m = nat.lib().svie_ball_half_width(float(radius), float(spacing))
     if m < 1:
         raise ValueError("radius and spacing must be positive")
     side = 2 * m + 1
     w = torch.empty((side, side, side), dtype=torch.float64, device=device)
     nat.call("svie_ball_weights", float(radius), float(spacing), int(quad), nat.ptr(w), nat.stream())
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream(w.device))
+    _WEIGHTS_CACHE[key] = (w, ev)
+    while len(_WEIGHTS_CACHE) > _WEIGHTS_CACHE_SIZE:
+        _WEIGHTS_CACHE.popitem(last=False)
     return w
 
 

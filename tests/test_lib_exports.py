@@ -63,3 +63,15 @@ def test_no_cpu_fallback():
     if not torch.cuda.is_available():
         with pytest.raises(RuntimeError):
             S.get_device()
+
+
+def test_status_codes_match_header():
+    import re
+
+    from svierosion_gb300 import _native as nat
+
+    text = (ROOT / "include" / "svie.h").read_text()
+    codes = dict(re.findall(r"#define (SVIE_(?:OK|ERR_[A-Z]+)) (\d+)", text))
+    assert len(codes) == 7
+    for name, value in codes.items():
+        assert getattr(nat, name) == int(value), name
