@@ -44,6 +44,36 @@ inline int blocks_for(long long n, int threads, long long cap = 1LL << 30) {
   return (int)b;
 }
 
+// ------------------------------------------------- division by a constant
+// Correctly rounded float reciprocal of d (normal, positive), on the host:
+// the double quotient rounded to float, then whichever float neighbour has
+// the product with d closest to 1 (a product of two floats is exact in
+// double, and so is 1 minus it).  1/d is never halfway between two floats
+// unless it is exact.
+inline float rn_reciprocal(float d) {
+  float r = (float)(1.0 / (double)d);
+  float best = r;
+  double err = fabs(1.0 - (double)d * (double)r);
+  const float cand[2] = {nextafterf(r, 0.0f), nextafterf(r, INFINITY)};
+  for (float c : cand) {
+    const double e = fabs(1.0 - (double)d * (double)c);
+    if (e < err) { err = e; best = c; }
+  }
+  return best;
+}
+
+// Correctly rounded x / d given rd = RN(1/d): q = RN(x rd) is within one ulp
+// of x / d, the remainder r = x - d q is exact in one fused multiply-add, and
+// RN(q + r rd) is the correctly rounded quotient (P. Markstein, "Computation
+// of elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Dev. 34(1), 1990, Theorem 1), for normal x and d and a normal quotient.
+// Three operations in place of a general division; a -0 quotient comes out +0.
+SVIE_DEV float div_by(float x, float d, float rd) {
+  const float q = __fmul_rn(x, rd);
+  const float r = __fmaf_rn(-q, d, x);
+  return __fmaf_rn(r, rd, q);
+}
+
 // -------------------------------------------------------------- float keys
 // Monotone map float -> uint32 so that unsigned atomicMin/Max order floats.
 SVIE_DEV unsigned int float_to_ordered(float f) {

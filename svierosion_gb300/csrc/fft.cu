@@ -179,39 +179,40 @@ SVIE_DEV int px(int a) { return a + (a >> 4); }
 __host__ __device__ inline int padded_len(int a) { return a + (a >> 4) + 1; }
 
 // One Stockham radix-R stage over `nlines` lines of length n, reading
-// src[line*LS + k] and writing dst (ping-pong buffers).  Warp w takes lines
-// w, w + 8, ...; its lanes take butterflies i = lane, lane + 32, ... of the
-// line, so no division is needed; k = i mod p uses the stage's magic
-// multiplier.  p = product of the radices already applied.
+// src[line*LS + k] and writing dst (ping-pong buffers).  The nlines * n / R
+// butterflies of the stage are spread over all threads of the CTA (thread j
+// takes butterflies j, j + FFT_T, ...), so lanes stay busy when n / R is not
+// a multiple of 32; line = j / m and k = i mod p use magic multipliers
+// (exact: j * m and i * p stay below 2^32).  p = product of the radices
+// already applied.
 template <int R>
 SVIE_DEV void fft_stage(const float2* __restrict__ src, float2* __restrict__ dst, int LS, int n, int nlines, int p,
                         unsigned int pmagic, const float2* __restrict__ tw) {
   const int m = n / R;
   const int twstep = n / (p * R);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int line = warp; line < nlines; line += FFT_T / 32) {
+  const int total = nlines * m;
+  const unsigned int mmagic = m > 1 ? 0xFFFFFFFFu / (unsigned)m + 1u : 0u;
+  for (int j = threadIdx.x; j < total; j += FFT_T) {
+    const int line = m > 1 ? (int)__umulhi((unsigned)j, mmagic) : j;
+    const int i = j - line * m;
     const int base = line * LS;
-    for (int i = lane; i < m; i += 32) {
-      const int k = (p == 1) ? 0 : i - (int)__umulhi((unsigned)i, pmagic) * p;
-      float2 v[R];
+    const int k = (p == 1) ? 0 : i - (int)__umulhi((unsigned)i, pmagic) * p;
+    float2 v[R];
 #pragma unroll
-      for (int q = 0; q < R; ++q) v[q] = src[px(base + i + q * m)];
-      if (k) {
-        const int tq = k * twstep;
+    for (int q = 0; q < R; ++q) v[q] = src[px(base + i + q * m)];
+    if (k) {
+      const int tq = k * twstep;
 #pragma unroll
-        for (int q = 1; q < R; ++q) v[q] = cmul(v[q], __ldg(tw + q * tq));
-      }
-      dft<R>(v);
-      const int o = base + (i - k) * R + k;
-#pragma unroll
-      for (int q = 0; q < R; ++q) dst[px(o + q * p)] = v[q];
+      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], __ldg(tw + q * tq));
     }
+    dft<R>(v);
+    const int o = base + (i - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) dst[px(o + q * p)] = v[q];
   }
   __syncthreads();
 }
 
-// Runs all stages; the data starts in a and the result pointer is returned
-// (a or b).
 SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPlan& P) {
   int p = 1;
   for (int st = 0; st < P.nst; ++st) {
@@ -233,7 +234,8 @@ SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPla
   return a;
 }
 
-__host__ __device__ inline int line_stride(int n) { return (n & 1) ? n : n + 1; }  // odd -> conflict-free columns
+// line stride in shared memory: odd -> conflict-free columns
+__host__ __device__ inline int line_stride(int n) { return (n & 1) ? n : n + 1; }
 __host__ __device__ inline int padded_nzh(int nz) { return ((nz / 2 + 1) + 7) & ~7; }  // 64-byte rows
 __host__ __device__ inline int smem_buffer(int W, int n) { return padded_len(W * line_stride(n)); }
 
@@ -266,7 +268,17 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ i
   for (int l = warp; l < 2 * np; l += FFT_T / 32) {
     const bool ok = l < nl && (!lineflag || (__ldg(lineflag + line0 + l) & 1));
     float* row = reinterpret_cast<float*>(sa);
-    for (int z = lane; z < n; z += 32) row[2 * px((l >> 1) * LS + z) + (l & 1)] = ok ? __ldg(src + l * n + z) : 0.0f;
+    const float* g = src + l * n;
+    int z = lane;
+    // eight loads in flight per thread before the shared-memory stores
+    for (; z + 7 * 32 < n; z += 8 * 32) {
+      float t[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) t[u] = ok ? __ldg(g + z + 32 * u) : 0.0f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) row[2 * px((l >> 1) * LS + z + 32 * u) + (l & 1)] = t[u];
+    }
+    for (; z < n; z += 32) row[2 * px((l >> 1) * LS + z) + (l & 1)] = ok ? __ldg(g + z) : 0.0f;
   }
   __syncthreads();
   const float2* r = run_fft(sa, sb, LS, np, P);
@@ -308,15 +320,28 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
     const bool has2 = 2 * w + 1 < nl;
     const float2* s1 = src + (long long)(2 * w) * nzp;
     const float2* s2 = s1 + nzp;
-    for (int k = lane; k < n; k += 32) {
-      const bool mirror = k > n / 2;
-      const int kk = mirror ? n - k : k;
-      float2 x1 = __ldg(s1 + kk);
-      float2 x2 = has2 ? __ldg(s2 + kk) : make_float2(0.f, 0.f);
-      if (kk == 0 || (even && kk == n / 2)) { x1.y = 0.f; x2.y = 0.f; }
-      if (mirror) { x1.y = -x1.y; x2.y = -x2.y; }
-      // C = X1 + i X2, stored conjugated for the inverse-by-forward transform
-      sa[px(w * LS + k)] = make_float2(x1.x - x2.y, -(x1.y + x2.x));
+    // four (k, line pair) loads in flight per thread before the stores
+    for (int k0 = lane; k0 < n; k0 += 4 * 32) {
+      float2 x1[4], x2[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + 32 * u;
+        const int kk = k > n / 2 ? n - k : k;
+        x1[u] = k < n ? __ldg(s1 + kk) : make_float2(0.f, 0.f);
+        x2[u] = (has2 && k < n) ? __ldg(s2 + kk) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + 32 * u;
+        if (k >= n) break;
+        const bool mirror = k > n / 2;
+        const int kk = mirror ? n - k : k;
+        float2 a = x1[u], b = x2[u];
+        if (kk == 0 || (even && kk == n / 2)) { a.y = 0.f; b.y = 0.f; }
+        if (mirror) { a.y = -a.y; b.y = -b.y; }
+        // C = X1 + i X2, stored conjugated for the inverse-by-forward transform
+        sa[px(w * LS + k)] = make_float2(a.x - b.y, -(a.y + b.x));
+      }
     }
   }
   __syncthreads();
@@ -365,7 +390,19 @@ __global__ void __launch_bounds__(FFT_T) k_fft_strided(float2* __restrict__ data
   const long long rstep = 32 * stride;
   if (col) {
     const float2* g = base + (long long)k0 * stride + c;
-    for (int k = k0; k < n; k += 32, g += rstep) {
+    int k = k0;
+    // eight loads in flight per thread before the shared-memory stores
+    for (; k + 7 * 32 < n; k += 8 * 32, g += 8 * rstep) {
+      float2 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = g[u * rstep];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (mode == 1) v[u].y = -v[u].y;
+        sa[px(c * LS + k + 32 * u)] = v[u];
+      }
+    }
+    for (; k < n; k += 32, g += rstep) {
       float2 v = *g;
       if (mode == 1) v.y = -v.y;
       sa[px(c * LS + k)] = v;
@@ -586,9 +623,9 @@ static PlanLayout plan_layout(int nx, int ny, int nz) {
 }
 
 // Complex lines per CTA of the z passes: two shared buffers of W lines stay
-// under ~64 KB, so three CTAs fit on an SM.
+// under ~56 KB, so four CTAs fit on an SM.
 static int z_width(int n) {
-  int w = 4096 / n;
+  int w = 3290 / line_stride(n);
   return w > 16 ? 16 : (w < 1 ? 1 : w);
 }
 

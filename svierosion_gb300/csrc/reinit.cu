@@ -2,10 +2,9 @@
 // svierosion/levelset.py:154-183 and svierosion/kernels.py:312-379.
 //
 // Work set: band dilated by `dilation` cells (box), outer `margin` layers
-// cleared, compacted in flat order.  Geometry (sign, local pseudo-time step,
+// cleared, compacted in brick order.  Geometry (sign, local pseudo-time step,
 // per-axis crossing flags and subcell interface distances) is computed once
-// from the initial phi and stored structure-of-arrays:
-//   [sgn m][dtau m][flags m (uint32: bit 2a = cp, bit 2a+1 = cm)][xp_x xm_x xp_y xm_y xp_z xm_z : 6 m]
+// from the initial phi (layout at struct Geo below).
 // Each TVD-RK2 iteration is two Jacobi sweeps between the level-set grid A and
 // a second dense grid B that mirrors A off the work set:
 //   B[idx] = u0 + dtau rhs(A);   A[idx] = (u0 + B[idx] + dtau rhs(B)) / 2.
@@ -40,13 +39,22 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
 //   meta  uint8 [m]   bits 0-5: crossing flags cp_x cm_x cp_y cm_y cp_z cm_z,
 //                     bit 6: phi0 > 0, bit 7: phi0 < 0
 //   dist  float [6m]  xp_x xm_x xp_y xm_y xp_z xm_z, read only where the flag is set
-// so a sweep streams 5 bytes of geometry per node instead of 36.
+//   cfl   float       at geo_cfl_offset(m)
+// A sweep streams 1 byte of geometry per node (the flags) and rebuilds dtau
+// from the distances it reads anyway; dtau is stored for
+// svie_reinit_geometry_unpack.
 struct Geo {
   float* dtau;
   uint8_t* meta;
   float* dist;
   long long m;
 };
+
+// cfl of the geometry, stored after the arrays (16-byte aligned).
+__host__ __device__ inline long long geo_cfl_offset(long long m) { return (29 * m + 15) & ~15LL; }
+SVIE_DEV float geo_cfl(const void* base, long long m) {
+  return __ldg(reinterpret_cast<const float*>(static_cast<const char*>(base) + geo_cfl_offset(m)));
+}
 
 SVIE_DEV Geo geo_view(void* base, long long m) {
   Geo g;
@@ -91,62 +99,71 @@ __global__ void k_reinit_geometry(const float* __restrict__ f, const int32_t* __
   flags |= (c < 0.0f ? 1u : 0u) << 7;
   g.dtau[t] = cfl * fmaxf(hmin, 1e-3f * h);
   g.meta[t] = (uint8_t)flags;
+  if (t == 0) *reinterpret_cast<float*>(static_cast<char*>(geo) + geo_cfl_offset(m)) = cfl;
 }
 
 SVIE_DEV float meta_sgn(uint32_t meta) { return (meta & 64u) ? 1.0f : ((meta & 128u) ? -1.0f : 0.0f); }
 
-// reinit_rhs (kernels.py:363-379) at work-set entry t.
+// reinit_rhs (kernels.py:363-379) at work-set entry t.  Divisions by h use
+// the correctly rounded reciprocal rh (div_by); hh = RN(h * h).  Also returns
+// hmin = min(h, stored distances of the flagged crossings), from which
+// dtau = cfl * max(hmin, 1e-3 h) is rebuilt exactly as k_reinit_geometry
+// computed it (a distance below 1e-6 h, stored clamped to 1e-6 h, gives the
+// same 1e-3 h either way).
 SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, const Geo& g, uint32_t flags, int sx,
-                             int sy, int sz, float h) {
+                             int sy, int sz, float h, float rh, float hh, float& hmin) {
   const float* qp = f + i;
   const float c = __ldg(qp);
   const float sgn = meta_sgn(flags);
   const bool outside = sgn > 0.0f;
-  const float hh = h * h;
   float g2 = 0.0f;
+  hmin = h;
   const int st[3] = {sx, sy, sz};
+  float v3[3][4];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const int s = st[a];
-    float m2 = __ldg(qp - 2 * s), m1 = __ldg(qp - s), p1 = __ldg(qp + s), p2 = __ldg(qp + 2 * s);
-    float mm_p = minmod(p1 - 2.0f * c + m1, p2 - 2.0f * p1 + c);
-    float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
-    const bool cp = (flags >> (2 * a)) & 1u, cm = (flags >> (2 * a + 1)) & 1u;
-    float Dp, Dm;
-    if (cp) {
+    v3[a][0] = __ldg(qp - 2 * s);
+    v3[a][1] = __ldg(qp - s);
+    v3[a][2] = __ldg(qp + s);
+    v3[a][3] = __ldg(qp + 2 * s);
+  }
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float m2 = v3[a][0], m1 = v3[a][1], p1 = v3[a][2], p2 = v3[a][3];
+    const float mm_p = minmod(p1 - 2.0f * c + m1, p2 - 2.0f * p1 + c);
+    const float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
+    float Dp = div_by(p1 - c - 0.5f * mm_p, h, rh);
+    float Dm = div_by(c - m1 + 0.5f * mm_m, h, rh);
+    if ((flags >> (2 * a)) & 1u) {
       const float xp = g.dist[(2 * a) * g.m + t];
       Dp = -c / xp - 0.5f * xp * mm_p / hh;
-    } else {
-      Dp = (p1 - c - 0.5f * mm_p) / h;
+      hmin = fminf(hmin, xp);
     }
-    if (cm) {
+    if ((flags >> (2 * a + 1)) & 1u) {
       const float xm = g.dist[(2 * a + 1) * g.m + t];
       Dm = c / xm + 0.5f * xm * mm_m / hh;
-    } else {
-      Dm = (c - m1 + 0.5f * mm_m) / h;
+      hmin = fminf(hmin, xm);
     }
-    float v;
-    if (outside) {
-      float a1 = fmaxf(Dm, 0.0f), b1 = fminf(Dp, 0.0f);
-      v = fmaxf(a1 * a1, b1 * b1);
-    } else {
-      float a1 = fminf(Dm, 0.0f), b1 = fmaxf(Dp, 0.0f);
-      v = fmaxf(a1 * a1, b1 * b1);
-    }
-    g2 = g2 + v;
+    const float a1 = outside ? fmaxf(Dm, 0.0f) : fminf(Dm, 0.0f);
+    const float b1 = outside ? fminf(Dp, 0.0f) : fmaxf(Dp, 0.0f);
+    g2 = g2 + fmaxf(a1 * a1, b1 * b1);
   }
   return -sgn * (sqrtf(g2) - 1.0f);
 }
 
 __global__ void __launch_bounds__(RI_THREADS) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
                                                              const int32_t* __restrict__ idx, long long m, int sx,
-                                                             int sy, int sz, float h, void* geo, int second) {
+                                                             int sy, int sz, float h, float rh, void* geo,
+                                                             int second) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
   Geo g = geo_view(geo, m);
+  const float cfl = geo_cfl(geo, m);
   const int i = idx[t];
-  const float r = reinit_rhs_at(src, i, t, g, g.meta[t], sx, sy, sz, h);
-  const float dtau = g.dtau[t];
+  float hmin;
+  const float r = reinit_rhs_at(src, i, t, g, g.meta[t], sx, sy, sz, h, rh, h * h, hmin);
+  const float dtau = cfl * fmaxf(hmin, 1e-3f * h);
   if (!second) {
     dst[i] = src[i] + dtau * r;  // u0 + dtau rhs(A)
   } else {
@@ -156,11 +173,12 @@ __global__ void __launch_bounds__(RI_THREADS) k_reinit_sweep(const float* __rest
 }
 
 __global__ void k_reinit_rhs(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx, int sy,
-                             int sz, float h, void* geo, float* out) {
+                             int sz, float h, float rh, void* geo, float* out) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
   Geo g = geo_view(geo, m);
-  out[t] = reinit_rhs_at(f, idx[t], t, g, g.meta[t], sx, sy, sz, h);
+  float hmin;
+  out[t] = reinit_rhs_at(f, idx[t], t, g, g.meta[t], sx, sy, sz, h, rh, h * h, hmin);
 }
 
 __global__ void k_geo_unpack(const void* geo, long long m, float* sgn, float* dtau, uint8_t* flags, float* dist6) {
@@ -262,9 +280,10 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
     return SVIE_ERR_LAUNCH;
   }
   const int nb = blocks_for(m, RI_THREADS);
+  const float rh = rn_reciprocal(h);
   for (int it = 0; it < iterations; ++it) {
-    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, const_cast<void*>(geo), 0);
-    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, const_cast<void*>(geo), 1);
+    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, const_cast<void*>(geo), 0);
+    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, const_cast<void*>(geo), 1);
   }
   return launch_status("svie_reinit_iterate", 2 * iterations);
 }
@@ -272,8 +291,8 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
 int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz, float h,
                     const void* geo, float* out, void* stream) {
   if (m <= 0) return m < 0 ? SVIE_ERR_ARG : SVIE_OK;
-  k_reinit_rhs<<<blocks_for(m, RI_THREADS), RI_THREADS, 0, (cudaStream_t)stream>>>(phi, idx, m, sx, sy, sz, h,
-                                                                                   const_cast<void*>(geo), out);
+  k_reinit_rhs<<<blocks_for(m, RI_THREADS), RI_THREADS, 0, (cudaStream_t)stream>>>(
+      phi, idx, m, sx, sy, sz, h, rn_reciprocal(h), const_cast<void*>(geo), out);
   return launch_status("svie_reinit_rhs");
 }
 
