@@ -5,12 +5,14 @@
 // (levelset.py:173, evolve.py:100).  The output is the ascending list of flat
 // indices, bit-identical to torch.nonzero given the same phi.
 //
-// Layout: each CTA owns a tile of TILE = THREADS * IPT consecutive nodes and
-// each thread IPT consecutive nodes of it.  Pass 1 counts selected nodes per
-// CTA; a one-CTA scan turns the counts into offsets (workspace: one int32 per
-// CTA); pass 2 recomputes the predicate, scans the per-thread counts inside the
-// CTA and writes the indices in order.  Both passes read the grid once
-// (HBM-bound, 4 B/node each for phi).
+// Layout: each CTA owns a tile of TILE = THREADS * IPT consecutive nodes;
+// warp w of the CTA owns IPT chunks of 32 consecutive nodes, chunk j being
+// nodes tile0 + w * 32 * IPT + 32 j + lane, so every load and store is
+// coalesced.  Pass 1 counts selected nodes per CTA; a one-CTA scan turns the
+// counts into offsets (workspace: one int32 per CTA); pass 2 recomputes the
+// predicate as one ballot per chunk, and popcounts of the ballots give each
+// selected node its position, so the output keeps the flat order.  Both
+// passes read the grid once (HBM-bound, 4 B/node each for phi).
 #include <limits.h>
 
 #include "common.cuh"
@@ -72,14 +74,56 @@ struct MaskPred {
   SVIE_DEV bool operator()(long long e) const { return mask[e] != 0; }
 };
 
+// First node of this warp's chunks.
+SVIE_DEV long long warp_base() {
+  return (long long)blockIdx.x * CMP_TILE + (long long)(threadIdx.x >> 5) * (32 * CMP_IPT);
+}
+
+// Exclusive offsets of the CTA's warps from their totals; CTA total -> *total.
+SVIE_DEV int warp_offsets(int wt, int* sh, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) sh[wid] = wt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int w = 0; w < nw; ++w) {
+      const int c = sh[w];
+      sh[w] = run;
+      run += c;
+    }
+    sh[32] = run;
+  }
+  __syncthreads();
+  const int r = sh[wid];
+  *total = sh[32];
+  __syncthreads();
+  return r;
+}
+
+// Writes the selected nodes of the warp's chunks (ballots bal[j]) in order
+// from position o; value(j) gives what to store for the lane's node of chunk j.
+template <class Value>
+SVIE_DEV void write_selected(const unsigned int* bal, long long o, int32_t* out, long long capacity, Value value) {
+  const int lane = threadIdx.x & 31;
+  const unsigned int lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    if ((bal[j] >> lane) & 1u) {
+      const long long pos = o + __popc(bal[j] & lt);
+      if (pos < capacity) out[pos] = value(j);
+    }
+    o += __popc(bal[j]);
+  }
+}
+
 template <class Pred>
 __global__ void __launch_bounds__(CMP_THREADS) k_count(Pred pred, long long n, int* counts) {
   __shared__ int sh[CMP_THREADS / 32];
-  const long long t0 = (long long)blockIdx.x * CMP_TILE + (long long)threadIdx.x * CMP_IPT;
+  const long long wb = warp_base() + (threadIdx.x & 31);
   int c = 0;
 #pragma unroll 4
   for (int j = 0; j < CMP_IPT; ++j) {
-    long long e = t0 + j;
+    const long long e = wb + 32 * j;
     if (e < n && pred(e)) ++c;
   }
   int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
@@ -110,21 +154,18 @@ template <class Pred>
 __global__ void __launch_bounds__(CMP_THREADS) k_write(Pred pred, long long n, const int* offsets,
                                                        int32_t* out, long long capacity) {
   __shared__ int sh[33];
-  const long long t0 = (long long)blockIdx.x * CMP_TILE + (long long)threadIdx.x * CMP_IPT;
-  unsigned int bits = 0;
-#pragma unroll 4
+  const long long wb = warp_base() + (threadIdx.x & 31);
+  unsigned int bal[CMP_IPT];
+  int wt = 0;
+#pragma unroll
   for (int j = 0; j < CMP_IPT; ++j) {
-    long long e = t0 + j;
-    if (e < n && pred(e)) bits |= 1u << j;
+    const long long e = wb + 32 * j;
+    bal[j] = __ballot_sync(0xffffffffu, e < n && pred(e));
+    wt += __popc(bal[j]);
   }
   int tot;
-  long long o = (long long)offsets[blockIdx.x] + block_exclusive_scan(__popc(bits), sh, &tot);
-  while (bits) {
-    int j = __ffs(bits) - 1;
-    bits &= bits - 1;
-    if (o < capacity) out[o] = (int32_t)(t0 + j);
-    ++o;
-  }
+  const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
+  write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)(wb + 32 * j); });
 }
 
 // Band write pass: indices + dense occupancy + margin / static-count data.
@@ -137,49 +178,50 @@ __global__ void __launch_bounds__(CMP_THREADS) k_band_write(const float* __restr
   __shared__ int shi[CMP_THREADS / 32];
   const long long n = (long long)nx * ny * nz;
   const long long syz = (long long)ny * nz;
-  const long long t0 = (long long)blockIdx.x * CMP_TILE + (long long)threadIdx.x * CMP_IPT;
-  unsigned int bits = 0;
+  const long long wb = warp_base() + (threadIdx.x & 31);
+  unsigned int bal[CMP_IPT];
+  int wt = 0;
   int inside_static = 0;
   int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
   int ilo[3] = {INT_MAX, INT_MAX, INT_MAX}, ihi[3] = {-1, -1, -1};
-  // coordinates of the first node, then advanced incrementally (no division per node)
-  int c[3];
-  if (t0 < n) {
-    const int e0 = (int)t0, yz = e0 % (int)syz;
+  // coordinates of the lane's first node, then advanced by 32 nodes per chunk
+  int c[3] = {0, 0, 0};
+  if (wb < n) {
+    const int e0 = (int)wb, yz = e0 % (int)syz;
     c[0] = e0 / (int)syz;
     c[1] = yz / nz;
     c[2] = yz - c[1] * nz;
   }
+#pragma unroll
   for (int j = 0; j < CMP_IPT; ++j) {
-    long long e = t0 + j;
-    if (e >= n) break;
-    float v = phi[e];
-    bool sel = fabsf(v) < thresh;
-    bool neg = v < 0.0f;
-    if (occ) occ[e] = neg ? 1.0f : 0.0f;
-    if (sel) {
-      bits |= 1u << j;
+    const long long e = wb + 32 * j;
+    bool sel = false;
+    if (e < n) {
+      const float v = phi[e];
+      sel = fabsf(v) < thresh;
+      const bool neg = v < 0.0f;
+      if (occ) occ[e] = neg ? 1.0f : 0.0f;
+      if (sel) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
-    }
-    if (neg) {
+        for (int a = 0; a < 3; ++a) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
+      }
+      if (neg) {
 #pragma unroll
-      for (int a = 0; a < 3; ++a) { ilo[a] = min(ilo[a], c[a]); ihi[a] = max(ihi[a], c[a]); }
-      if (!sel) ++inside_static;
+        for (int a = 0; a < 3; ++a) { ilo[a] = min(ilo[a], c[a]); ihi[a] = max(ihi[a], c[a]); }
+        if (!sel) ++inside_static;
+      }
     }
-    if (++c[2] == nz) {
-      c[2] = 0;
+    bal[j] = __ballot_sync(0xffffffffu, sel);
+    wt += __popc(bal[j]);
+    c[2] += 32;
+    while (c[2] >= nz) {
+      c[2] -= nz;
       if (++c[1] == ny) { c[1] = 0; ++c[0]; }
     }
   }
   int tot;
-  long long o = (long long)offsets[blockIdx.x] + block_exclusive_scan(__popc(bits), sh, &tot);
-  while (bits) {
-    int j = __ffs(bits) - 1;
-    bits &= bits - 1;
-    if (o < capacity) out[o] = (int32_t)(t0 + j);
-    ++o;
-  }
+  const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
+  write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)(wb + 32 * j); });
   long long st = block_reduce((long long)inside_static, shl, OpSumLL(), 0LL);
   if (threadIdx.x == 0 && st) atomicAdd((unsigned long long*)&info->static_inside, (unsigned long long)st);
 #pragma unroll
@@ -296,20 +338,18 @@ __global__ void __launch_bounds__(CMP_THREADS) k_select(const uint8_t* __restric
                                                         long long n, const int* offsets, int32_t* out,
                                                         long long capacity) {
   __shared__ int sh[33];
-  const long long t0 = (long long)blockIdx.x * CMP_TILE + (long long)threadIdx.x * CMP_IPT;
-  unsigned int bits = 0;
+  const long long wb = warp_base() + (threadIdx.x & 31);
+  unsigned int bal[CMP_IPT];
+  int wt = 0;
+#pragma unroll
   for (int j = 0; j < CMP_IPT; ++j) {
-    long long e = t0 + j;
-    if (e < n && mask[e]) bits |= 1u << j;
+    const long long e = wb + 32 * j;
+    bal[j] = __ballot_sync(0xffffffffu, e < n && mask[e]);
+    wt += __popc(bal[j]);
   }
   int tot;
-  long long o = (long long)offsets[blockIdx.x] + block_exclusive_scan(__popc(bits), sh, &tot);
-  while (bits) {
-    int j = __ffs(bits) - 1;
-    bits &= bits - 1;
-    if (o < capacity) out[o] = vals[t0 + j];
-    ++o;
-  }
+  const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
+  write_selected(bal, o, out, capacity, [&](int j) { return vals[wb + 32 * j]; });
 }
 }  // namespace svie
 
@@ -344,31 +384,46 @@ constexpr int BRICK = BRX * BRY * BRZ;  // 256 = CMP_TILE / CMP_IPT rows of 16
 
 struct BrickGeom {
   int nx, ny, nz, nbx, nby, nbz;
-  SVIE_DEV long long total() const { return (long long)nbx * nby * nbz * BRICK; }
-  // first flat index of the z-row handled by row id r (one row = CMP_IPT nodes),
-  // or -1 if the row is outside the grid; *zlen = nodes of the row inside it.
-  SVIE_DEV long long row(long long r, int* zlen) const {
-    const long long b = r >> 4;  // 16 rows per brick
-    const int lr = (int)(r & 15);
-    const int bz = (int)(b % nbz);
-    const long long bxy = b / nbz;
-    const int by = (int)(bxy % nby), bx = (int)(bxy / nby);
-    const int x = bx * BRX + (lr >> 2), y = by * BRY + (lr & 3), z0 = bz * BRZ;
-    if (x >= nx || y >= ny) return -1;
-    *zlen = min(BRZ, nz - z0);
-    return ((long long)x * ny + y) * nz + z0;
+  __host__ __device__ long long bricks() const { return (long long)nbx * nby * nbz; }
+};
+
+// A warp covers 32 rows of 16 nodes = two bricks; in chunk j its lanes hold
+// rows 2j and 2j + 1 of the pair (half-warp per row, z fastest), so the
+// ballot bits follow the list order.  Node of the lane in chunk j, or -1.
+struct BrickWalk {
+  int x0[2], y0[2], z0[2];
+  bool ok[2];
+  SVIE_DEV BrickWalk(const BrickGeom& G) {
+    const long long b0 = ((long long)blockIdx.x * CMP_THREADS + (threadIdx.x & ~31)) >> 4;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const long long b = b0 + h;
+      ok[h] = b < G.bricks();
+      const int bz = ok[h] ? (int)(b % G.nbz) : 0;
+      const long long bxy = ok[h] ? b / G.nbz : 0;
+      x0[h] = (int)(bxy / G.nby) * BRX;
+      y0[h] = (int)(bxy % G.nby) * BRY;
+      z0[h] = bz * BRZ;
+    }
+  }
+  SVIE_DEV long long node(const BrickGeom& G, int j) const {
+    const int lane = threadIdx.x & 31, h = j >> 3;
+    const int lr = ((2 * j) & 15) + (lane >> 4);
+    const int x = x0[h] + (lr >> 2), y = y0[h] + (lr & 3), z = z0[h] + (lane & 15);
+    if (!ok[h] || x >= G.nx || y >= G.ny || z >= G.nz) return -1;
+    return ((long long)x * G.ny + y) * G.nz + z;
   }
 };
 
 template <class Pred>
 __global__ void __launch_bounds__(CMP_THREADS) k_brick_count(Pred pred, BrickGeom G, int* counts) {
   __shared__ int sh[CMP_THREADS / 32];
-  const long long r = (long long)blockIdx.x * CMP_THREADS + threadIdx.x;
-  int c = 0, zlen = 0;
-  if (r * CMP_IPT < G.total()) {
-    const long long f0 = G.row(r, &zlen);
-    if (f0 >= 0)
-      for (int j = 0; j < zlen; ++j) c += pred(f0 + j) ? 1 : 0;
+  const BrickWalk W(G);
+  int c = 0;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = W.node(G, j);
+    if (e >= 0 && pred(e)) ++c;
   }
   int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
   if (threadIdx.x == 0) counts[blockIdx.x] = tot;
@@ -378,24 +433,18 @@ template <class Pred>
 __global__ void __launch_bounds__(CMP_THREADS) k_brick_write(Pred pred, BrickGeom G, const int* offsets, int32_t* out,
                                                              long long capacity) {
   __shared__ int sh[33];
-  const long long r = (long long)blockIdx.x * CMP_THREADS + threadIdx.x;
-  unsigned int bits = 0;
-  long long f0 = -1;
-  int zlen = 0;
-  if (r * CMP_IPT < G.total()) {
-    f0 = G.row(r, &zlen);
-    if (f0 >= 0)
-      for (int j = 0; j < zlen; ++j)
-        if (pred(f0 + j)) bits |= 1u << j;
+  const BrickWalk W(G);
+  unsigned int bal[CMP_IPT];
+  int wt = 0;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = W.node(G, j);
+    bal[j] = __ballot_sync(0xffffffffu, e >= 0 && pred(e));
+    wt += __popc(bal[j]);
   }
   int tot;
-  long long o = (long long)offsets[blockIdx.x] + block_exclusive_scan(__popc(bits), sh, &tot);
-  while (bits) {
-    int j = __ffs(bits) - 1;
-    bits &= bits - 1;
-    if (o < capacity) out[o] = (int32_t)(f0 + j);
-    ++o;
-  }
+  const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
+  write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)W.node(G, j); });
 }
 
 struct AbsLessPred {
@@ -409,7 +458,7 @@ static BrickGeom brick_geom(int nx, int ny, int nz) {
 }
 
 static long long brick_blocks(const BrickGeom& G) {
-  const long long rows = (long long)G.nbx * G.nby * G.nbz * (BRICK / CMP_IPT);
+  const long long rows = G.bricks() * (BRICK / CMP_IPT);
   return (rows + CMP_THREADS - 1) / CMP_THREADS;
 }
 

@@ -221,6 +221,98 @@ __global__ void k_dilate_axis(const uint8_t* __restrict__ src, uint8_t* __restri
   }
 }
 
+// Box dilation by r <= DB_RMAX in one pass (the three axis passes of
+// k_dilate_axis fused): a CTA owns a DB_X x DB_Y x DB_Z tile and reads its
+// neighbourhood widened by r, one row (x, y) at a time as bit masks (three
+// ballots of 32 z values, bit i <-> z = z0 - r + i); the box OR is then
+// separable bit arithmetic: shifts along z, ORs of row masks along y and x.
+// Nodes outside the grid count as 0; margin > 0 clears the outer layers.
+constexpr int DB_X = 16, DB_Y = 16, DB_Z = 64, DB_RMAX = 8;
+constexpr int DB_EMAX = DB_X + 2 * DB_RMAX;  // = DB_Y + 2 * DB_RMAX
+
+__global__ void __launch_bounds__(256) k_dilate_box(const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                                                    int nx, int ny, int nz, int r, int margin) {
+  __shared__ uint32_t inm[DB_EMAX * DB_EMAX][3];
+  __shared__ unsigned long long zm[DB_EMAX * DB_EMAX];
+  __shared__ unsigned long long ym[DB_EMAX * DB_Y];
+  __shared__ unsigned long long fm[DB_X * DB_Y];
+  const int x0 = blockIdx.z * DB_X, y0 = blockIdx.y * DB_Y, z0 = blockIdx.x * DB_Z;
+  const int EX = DB_X + 2 * r, EY = DB_Y + 2 * r, EZ = DB_Z + 2 * r;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int row = warp; row < EX * EY; row += 8) {
+    const int ix = row / EY, iy = row - ix * EY;
+    const int x = x0 - r + ix, y = y0 - r + iy;
+    const bool rowok = x >= 0 && x < nx && y >= 0 && y < ny;
+    const long long rb = rowok ? ((long long)x * ny + y) * nz : 0;
+#pragma unroll
+    for (int w = 0; w < 3; ++w) {
+      const int i = 32 * w + lane, z = z0 - r + i;
+      const bool v = rowok && i < EZ && z >= 0 && z < nz && __ldg(src + rb + z) != 0;
+      const unsigned int b = __ballot_sync(0xffffffffu, v);
+      if (lane == 0) inm[row][w] = b;
+    }
+  }
+  __syncthreads();
+  // z: output bit k (z = z0 + k) = OR of input bits k .. k + 2r
+  for (int row = threadIdx.x; row < EX * EY; row += blockDim.x) {
+    const unsigned long long lo = inm[row][0] | ((unsigned long long)inm[row][1] << 32);
+    const unsigned long long hi = inm[row][2];
+    unsigned long long acc = lo;
+    for (int d = 1; d <= 2 * r; ++d) acc |= (lo >> d) | (hi << (64 - d));
+    zm[row] = acc;
+  }
+  __syncthreads();
+  // y: rows (ix, y) = OR over iy = y .. y + 2r
+  for (int t = threadIdx.x; t < EX * DB_Y; t += blockDim.x) {
+    const int ix = t / DB_Y, y = t - ix * DB_Y;
+    unsigned long long acc = 0;
+    for (int d = 0; d <= 2 * r; ++d) acc |= zm[ix * EY + y + d];
+    ym[t] = acc;
+  }
+  __syncthreads();
+  // x: rows (x, y) = OR over ix = x .. x + 2r
+  for (int t = threadIdx.x; t < DB_X * DB_Y; t += blockDim.x) {
+    const int x = t / DB_Y, y = t - x * DB_Y;
+    unsigned long long acc = 0;
+    for (int d = 0; d <= 2 * r; ++d) acc |= ym[(x + d) * DB_Y + y];
+    fm[t] = acc;
+  }
+  __syncthreads();
+  for (int row = warp; row < DB_X * DB_Y; row += 8) {
+    const int x = x0 + row / DB_Y, y = y0 + row % DB_Y;
+    if (x >= nx || y >= ny) continue;
+    const bool rowclear = margin > 0 && (x < margin || y < margin || x >= nx - margin || y >= ny - margin);
+    const unsigned long long mk = fm[row];
+    uint8_t* drow = dst + ((long long)x * ny + y) * nz;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = 32 * h + lane, z = z0 + k;
+      if (z < nz) {
+        const bool zclear = margin > 0 && (z < margin || z >= nz - margin);
+        drow[z] = (!rowclear && !zclear && ((mk >> k) & 1ull)) ? 1 : 0;
+      }
+    }
+  }
+}
+
+// dst = src dilated by the (2r+1)^3 box; tmp is a same-size scratch used
+// only for r > DB_RMAX (three axis passes).
+static void dilate_box(const uint8_t* src, uint8_t* dst, uint8_t* tmp, int nx, int ny, int nz, int r, int margin,
+                       cudaStream_t s, int* launches) {
+  if (r <= DB_RMAX) {
+    const dim3 gd((nz + DB_Z - 1) / DB_Z, (ny + DB_Y - 1) / DB_Y, (nx + DB_X - 1) / DB_X);
+    k_dilate_box<<<gd, 256, 0, s>>>(src, dst, nx, ny, nz, r, margin);
+    *launches += 1;
+    return;
+  }
+  const dim3 gd((nz + 127) / 128, ny, nx);
+  k_dilate_axis<<<gd, 128, 0, s>>>(src, tmp, nx, ny, nz, 0, r, 0);
+  k_dilate_axis<<<gd, 128, 0, s>>>(tmp, dst, nx, ny, nz, 1, r, 0);
+  k_dilate_axis<<<gd, 128, 0, s>>>(dst, tmp, nx, ny, nz, 2, r, margin);
+  cudaMemcpyAsync(dst, tmp, (size_t)nx * ny * nz, cudaMemcpyDeviceToDevice, s);
+  *launches += 3;
+}
+
 inline size_t geo_bytes(long long m) { return (size_t)(m < 1 ? 1 : m) * 29 + 256; }
 
 }  // namespace svie
@@ -237,20 +329,27 @@ int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int
     return SVIE_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  if (cudaMemsetAsync(mask, 0, (size_t)n, s) != cudaSuccess) {
+  // the band marked into tmp, then dilated into mask
+  if (cudaMemsetAsync(tmp, 0, (size_t)n, s) != cudaSuccess) {
     set_error("svie_reinit_mask: memset failed");
     return SVIE_ERR_LAUNCH;
   }
-  if (m > 0) k_mark<<<blocks_for(m, 256), 256, 0, s>>>(band, m, mask);
-  const dim3 gd((nz + 127) / 128, ny, nx);
-  k_dilate_axis<<<gd, 128, 0, s>>>(mask, tmp, nx, ny, nz, 0, dilation, 0);
-  k_dilate_axis<<<gd, 128, 0, s>>>(tmp, mask, nx, ny, nz, 1, dilation, 0);
-  k_dilate_axis<<<gd, 128, 0, s>>>(mask, tmp, nx, ny, nz, 2, dilation, margin);
-  if (cudaMemcpyAsync(mask, tmp, (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
-    set_error("svie_reinit_mask: copy failed");
-    return SVIE_ERR_LAUNCH;
+  int launches = 0;
+  if (m > 0) {
+    k_mark<<<blocks_for(m, 256), 256, 0, s>>>(band, m, tmp);
+    ++launches;
   }
-  return launch_status("svie_reinit_mask", m > 0 ? 4 : 3);
+  if (dilation <= DB_RMAX) {
+    dilate_box(tmp, mask, nullptr, nx, ny, nz, dilation, margin, s, &launches);
+  } else {
+    // the three axis passes need a scratch distinct from source and target
+    if (cudaMemcpyAsync(mask, tmp, (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+      set_error("svie_reinit_mask: copy failed");
+      return SVIE_ERR_LAUNCH;
+    }
+    dilate_box(mask, mask, tmp, nx, ny, nz, dilation, margin, s, &launches);
+  }
+  return launch_status("svie_reinit_mask", launches);
 }
 
 size_t svie_reinit_geometry_bytes(int64_t m) { return geo_bytes(m); }
@@ -315,13 +414,14 @@ extern "C" int svie_dilate(const uint8_t* mask, int nx, int ny, int nz, int step
     return SVIE_ERR_ARG;
   }
   cudaStream_t s = (cudaStream_t)stream;
-  const dim3 gd((nz + 127) / 128, ny, nx);
-  svie::k_dilate_axis<<<gd, 128, 0, s>>>(mask, tmp, nx, ny, nz, 0, steps, 0);
-  svie::k_dilate_axis<<<gd, 128, 0, s>>>(tmp, out, nx, ny, nz, 1, steps, 0);
-  svie::k_dilate_axis<<<gd, 128, 0, s>>>(out, tmp, nx, ny, nz, 2, steps, 0);
-  if (cudaMemcpyAsync(out, tmp, (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
-    svie::set_error("svie_dilate: copy failed");
-    return SVIE_ERR_LAUNCH;
+  if (mask == out && steps <= svie::DB_RMAX) {
+    if (cudaMemcpyAsync(tmp, mask, (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+      svie::set_error("svie_dilate: copy failed");
+      return SVIE_ERR_LAUNCH;
+    }
+    mask = tmp;
   }
-  return svie::launch_status("svie_dilate", 3);
+  int launches = 0;
+  svie::dilate_box(mask, out, tmp, nx, ny, nz, steps, 0, s, &launches);
+  return svie::launch_status("svie_dilate", launches);
 }
