@@ -130,6 +130,17 @@ int svie_brick_scan(int kind, const void* src, int nx, int ny, int nz, float thr
                     size_t ws_bytes, int64_t* count, void* stream);
 int svie_brick_write(int kind, const void* src, int nx, int ny, int nz, float thresh,
                      const void* ws, size_t ws_bytes, int32_t* out, int64_t capacity, void* stream);
+/* LevelSet.rebuild_band (svierosion/levelset.py:70-86) with the band listed in
+ * brick order: svie_brick_band_scan clamps phi to [-cap, cap] in place and
+ * counts |phi| < thresh (info->count on the device); svie_brick_band_write
+ * lists those nodes in brick order and, like svie_band_write, writes occ (when
+ * non-NULL) and the rest of *info.  Two grid passes in place of four when the
+ * ascending list is not needed at once.  Workspace: svie_brick_workspace_bytes. */
+int svie_brick_band_scan(float* phi, int nx, int ny, int nz, float cap, float thresh, void* ws,
+                         size_t ws_bytes, svie_band_info* info, void* stream);
+int svie_brick_band_write(const float* phi, int nx, int ny, int nz, float thresh, const void* ws,
+                          size_t ws_bytes, int32_t* out, int64_t capacity, float* occ,
+                          svie_band_info* info, void* stream);
 
 /* ------------------------------------------------- stencil kernels (API) */
 /* svierosion/kernels.py:146 godunov_inward(flat, idx, sx, sy, sz, inv_h) */

@@ -86,6 +86,8 @@ _SIGS = {
     "svie_brick_workspace_bytes": (Z, [I, I, I]),
     "svie_brick_scan": (I, [I, V, I, I, I, F, V, Z, V, V]),
     "svie_brick_write": (I, [I, V, I, I, I, F, V, Z, V, I64, V]),
+    "svie_brick_band_scan": (I, [V, I, I, I, F, F, V, Z, V, V]),
+    "svie_brick_band_write": (I, [V, I, I, I, F, V, Z, V, I64, V, V, V]),
     "svie_godunov_inward": (I, [V, V, I64, I64, I64, I64, F, V, V]),
     "svie_cell_fractions": (I, [V, V, I64, I64, I64, I64, V, V]),
     "svie_closest_points": (I, [V, V, I64, I, I, F, F, F, F, V, V]),

@@ -54,21 +54,6 @@ SVIE_DEV int block_exclusive_scan(int v, int* sh, int* total) {
 }
 
 // ------------------------------------------------------------ predicates
-struct BandPred {
-  float* phi;
-  float cap, thresh;
-  bool clamp;
-  SVIE_DEV bool operator()(long long e) const {
-    float v = phi[e];
-    if (clamp) {
-      float c = fminf(fmaxf(v, -cap), cap);
-      if (c != v) phi[e] = c;  // torch clamp_ semantics (NaN stays NaN)
-      v = c;
-    }
-    return fabsf(v) < thresh;
-  }
-};
-
 struct MaskPred {
   const uint8_t* mask;
   SVIE_DEV bool operator()(long long e) const { return mask[e] != 0; }
@@ -125,6 +110,34 @@ __global__ void __launch_bounds__(CMP_THREADS) k_count(Pred pred, long long n, i
   for (int j = 0; j < CMP_IPT; ++j) {
     const long long e = wb + 32 * j;
     if (e < n && pred(e)) ++c;
+  }
+  int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
+  if (threadIdx.x == 0) counts[blockIdx.x] = tot;
+}
+
+// Band count pass: clamp phi to [-cap, cap] in place (torch clamp_: NaN
+// stays NaN) and count |phi| < thresh; all sixteen loads of a thread are
+// issued before the conditional stores.
+__global__ void __launch_bounds__(CMP_THREADS) k_band_count(float* __restrict__ phi, long long n, float cap,
+                                                            float thresh, int* counts) {
+  __shared__ int sh[CMP_THREADS / 32];
+  const long long wb = warp_base() + (threadIdx.x & 31);
+  float v[CMP_IPT];
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = wb + 32 * j;
+    v[j] = e < n ? phi[e] : 0.0f;
+  }
+  int c = 0;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = wb + 32 * j;
+    if (e < n) {
+      const float x = v[j];
+      const float cl = (x != x) ? x : fminf(fmaxf(x, -cap), cap);
+      if (cl != x && x == x) phi[e] = cl;
+      c += fabsf(cl) < thresh ? 1 : 0;
+    }
   }
   int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
   if (threadIdx.x == 0) counts[blockIdx.x] = tot;
@@ -192,12 +205,18 @@ __global__ void __launch_bounds__(CMP_THREADS) k_band_write(const float* __restr
     c[1] = yz / nz;
     c[2] = yz - c[1] * nz;
   }
+  float pv[CMP_IPT];
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = wb + 32 * j;
+    pv[j] = e < n ? phi[e] : 0.0f;
+  }
 #pragma unroll
   for (int j = 0; j < CMP_IPT; ++j) {
     const long long e = wb + 32 * j;
     bool sel = false;
     if (e < n) {
-      const float v = phi[e];
+      const float v = pv[j];
       sel = fabsf(v) < thresh;
       const bool neg = v < 0.0f;
       if (occ) occ[e] = neg ? 1.0f : 0.0f;
@@ -271,8 +290,7 @@ int svie_band_scan(float* phi, int64_t n, float cap, float thresh, void* ws, siz
   }
   cudaStream_t s = (cudaStream_t)stream;
   long long nb = cmp_blocks(n);
-  BandPred p{phi, cap, thresh, true};
-  k_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(p, n, (int*)ws);
+  k_band_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(phi, n, cap, thresh, (int*)ws);
   k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)&info->count);
   k_info_init<<<1, 1, 0, s>>>(info);
   return launch_status("svie_band_scan", 3);
@@ -406,14 +424,109 @@ struct BrickWalk {
       z0[h] = bz * BRZ;
     }
   }
-  SVIE_DEV long long node(const BrickGeom& G, int j) const {
+  SVIE_DEV long long at(const BrickGeom& G, int j, int* c) const {
     const int lane = threadIdx.x & 31, h = j >> 3;
     const int lr = ((2 * j) & 15) + (lane >> 4);
-    const int x = x0[h] + (lr >> 2), y = y0[h] + (lr & 3), z = z0[h] + (lane & 15);
-    if (!ok[h] || x >= G.nx || y >= G.ny || z >= G.nz) return -1;
-    return ((long long)x * G.ny + y) * G.nz + z;
+    c[0] = x0[h] + (lr >> 2);
+    c[1] = y0[h] + (lr & 3);
+    c[2] = z0[h] + (lane & 15);
+    if (!ok[h] || c[0] >= G.nx || c[1] >= G.ny || c[2] >= G.nz) return -1;
+    return ((long long)c[0] * G.ny + c[1]) * G.nz + c[2];
+  }
+  SVIE_DEV long long node(const BrickGeom& G, int j) const {
+    int c[3];
+    return at(G, j, c);
   }
 };
+
+// LevelSet.rebuild_band (levelset.py:70-77) in brick order, pass 1: clamp phi
+// to [-cap, cap] in place (NaN stays NaN) and count |phi| < thresh per CTA.
+__global__ void __launch_bounds__(CMP_THREADS) k_brick_band_count(float* __restrict__ phi, BrickGeom G, float cap,
+                                                                  float thresh, int* counts) {
+  __shared__ int sh[CMP_THREADS / 32];
+  const BrickWalk W(G);
+  float v[CMP_IPT];
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = W.node(G, j);
+    v[j] = e >= 0 ? phi[e] : 0.0f;
+  }
+  int c = 0;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = W.node(G, j);
+    if (e >= 0) {
+      const float x = v[j];
+      const float cl = (x != x) ? x : fminf(fmaxf(x, -cap), cap);
+      if (cl != x && x == x) phi[e] = cl;
+      c += fabsf(cl) < thresh ? 1 : 0;
+    }
+  }
+  int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
+  if (threadIdx.x == 0) counts[blockIdx.x] = tot;
+}
+
+// Pass 2: brick-ordered band indices, dense occupancy (phi < 0) and the band
+// info (static inside count, band and inside bounding boxes).
+__global__ void __launch_bounds__(CMP_THREADS) k_brick_band_write(const float* __restrict__ phi, BrickGeom G,
+                                                                  float thresh, const int* offsets, int32_t* out,
+                                                                  long long capacity, float* occ,
+                                                                  svie_band_info* info) {
+  __shared__ int sh[33];
+  __shared__ long long shl[CMP_THREADS / 32];
+  __shared__ int shi[CMP_THREADS / 32];
+  const BrickWalk W(G);
+  float pv[CMP_IPT];
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = W.node(G, j);
+    pv[j] = e >= 0 ? phi[e] : 0.0f;
+  }
+  unsigned int bal[CMP_IPT];
+  int wt = 0, inside_static = 0;
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
+  int ilo[3] = {INT_MAX, INT_MAX, INT_MAX}, ihi[3] = {-1, -1, -1};
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    int c[3];
+    const long long e = W.at(G, j, c);
+    bool sel = false;
+    if (e >= 0) {
+      const float v = pv[j];
+      sel = fabsf(v) < thresh;
+      const bool neg = v < 0.0f;
+      if (occ) occ[e] = neg ? 1.0f : 0.0f;
+      if (sel) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
+      }
+      if (neg) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { ilo[a] = min(ilo[a], c[a]); ihi[a] = max(ihi[a], c[a]); }
+        if (!sel) ++inside_static;
+      }
+    }
+    bal[j] = __ballot_sync(0xffffffffu, sel);
+    wt += __popc(bal[j]);
+  }
+  int tot;
+  const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
+  write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)W.node(G, j); });
+  long long st = block_reduce((long long)inside_static, shl, OpSumLL(), 0LL);
+  if (threadIdx.x == 0 && st) atomicAdd((unsigned long long*)&info->static_inside, (unsigned long long)st);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    int v;
+    v = block_reduce(lo[a], shi, OpMinI(), INT_MAX);
+    if (threadIdx.x == 0 && v != INT_MAX) atomicMin(&info->lo[a], v);
+    v = block_reduce(hi[a], shi, OpMaxI(), -1);
+    if (threadIdx.x == 0 && v >= 0) atomicMax(&info->hi[a], v);
+    v = block_reduce(ilo[a], shi, OpMinI(), INT_MAX);
+    if (threadIdx.x == 0 && v != INT_MAX) atomicMin(&info->ilo[a], v);
+    v = block_reduce(ihi[a], shi, OpMaxI(), -1);
+    if (threadIdx.x == 0 && v >= 0) atomicMax(&info->ihi[a], v);
+  }
+}
 
 template <class Pred>
 __global__ void __launch_bounds__(CMP_THREADS) k_brick_count(Pred pred, BrickGeom G, int* counts) {
@@ -512,6 +625,46 @@ int svie_brick_write(int kind, const void* src, int nx, int ny, int nz, float th
     k_brick_write<<<(unsigned)nb, CMP_THREADS, 0, s>>>(AbsLessPred{(const float*)src, thresh}, G, (const int*)ws, out,
                                                        capacity);
   return launch_status("svie_brick_write");
+}
+
+int svie_brick_band_scan(float* phi, int nx, int ny, int nz, float cap, float thresh, void* ws, size_t ws_bytes,
+                         svie_band_info* info, void* stream) {
+  using namespace svie;
+  const long long n = (long long)nx * ny * nz;
+  if (!phi || !info || n <= 0 || n >= (1LL << 31)) {
+    set_error("svie_brick_band_scan: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_brick_workspace_bytes(nx, ny, nz)) {
+    set_error("svie_brick_band_scan: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const BrickGeom G = brick_geom(nx, ny, nz);
+  const long long nb = brick_blocks(G);
+  k_brick_band_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(phi, G, cap, thresh, (int*)ws);
+  k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)&info->count);
+  k_info_init<<<1, 1, 0, s>>>(info);
+  return launch_status("svie_brick_band_scan", 3);
+}
+
+int svie_brick_band_write(const float* phi, int nx, int ny, int nz, float thresh, const void* ws, size_t ws_bytes,
+                          int32_t* out, int64_t capacity, float* occ, svie_band_info* info, void* stream) {
+  using namespace svie;
+  const long long n = (long long)nx * ny * nz;
+  if (!phi || !info || n <= 0 || n >= (1LL << 31) || (capacity > 0 && !out)) {
+    set_error("svie_brick_band_write: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_brick_workspace_bytes(nx, ny, nz)) {
+    set_error("svie_brick_band_write: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  const BrickGeom G = brick_geom(nx, ny, nz);
+  const long long nb = brick_blocks(G);
+  k_brick_band_write<<<(unsigned)nb, CMP_THREADS, 0, (cudaStream_t)stream>>>(phi, G, thresh, (const int*)ws, out,
+                                                                             capacity, occ, info);
+  return launch_status("svie_brick_band_write");
 }
 
 }  // extern "C"

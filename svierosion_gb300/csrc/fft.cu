@@ -373,7 +373,10 @@ struct KGeom {
 // Slab skipping: when `slabflag` is given, a CTA returns at once for an outer
 // slab whose flag lacks `need` (bit 0: the forward data of the slab is zero,
 // bit 1: no N value of the slab is read afterwards).
-__global__ void __launch_bounds__(FFT_T) k_fft_strided(float2* __restrict__ data, AxisPlan P, long long stride,
+// MINB: CTAs per SM the register budget is sized for (the y passes fit four
+// in shared memory, the x pass three).
+template <int MINB>
+__global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict__ data, AxisPlan P, long long stride,
                                                        int ninner, long long outer_stride, int mode, KGeom K,
                                                        const uint8_t* __restrict__ slabflag, int need) {
   if (slabflag && !(__ldg(slabflag + blockIdx.y) & need)) return;
@@ -637,7 +640,8 @@ static int ensure_smem_attr() {
   const int bytes = 227 * 1024;
   cudaError_t e1 = cudaFuncSetAttribute(k_fft_z_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaError_t e2 = cudaFuncSetAttribute(k_fft_z_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaError_t e3 = cudaFuncSetAttribute(k_fft_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e3 = cudaFuncSetAttribute(k_fft_strided<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e3 == cudaSuccess) e3 = cudaFuncSetAttribute(k_fft_strided<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
     set_error("fft: cudaFuncSetAttribute failed");
     return SVIE_ERR_LAUNCH;
@@ -685,7 +689,7 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const size_t smem = 2 * (size_t)smem_buffer(SW, ny) * sizeof(float2);
   dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)nx);
-  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, KGeom{nullptr, ny, nzh},
+  k_fft_strided<4><<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, KGeom{nullptr, ny, nzh},
                                        slabflag, mode == 1 ? 2 : 1);
 }
 
@@ -694,7 +698,7 @@ static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int m
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const size_t smem = 2 * (size_t)smem_buffer(SW, nx) * sizeof(float2);
   dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)ny);
-  k_fft_strided<<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, KGeom{P.kred, ny, nzh},
+  k_fft_strided<3><<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, KGeom{P.kred, ny, nzh},
                                        nullptr, 0);
 }
 

@@ -152,7 +152,7 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, co
   return -sgn * (sqrtf(g2) - 1.0f);
 }
 
-__global__ void __launch_bounds__(RI_THREADS) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
+__global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
                                                              const int32_t* __restrict__ idx, long long m, int sx,
                                                              int sy, int sz, float h, float rh, void* geo,
                                                              int second) {
@@ -239,17 +239,30 @@ __global__ void __launch_bounds__(256) k_dilate_box(const uint8_t* __restrict__ 
   const int x0 = blockIdx.z * DB_X, y0 = blockIdx.y * DB_Y, z0 = blockIdx.x * DB_Z;
   const int EX = DB_X + 2 * r, EY = DB_Y + 2 * r, EZ = DB_Z + 2 * r;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int row = warp; row < EX * EY; row += 8) {
-    const int ix = row / EY, iy = row - ix * EY;
-    const int x = x0 - r + ix, y = y0 - r + iy;
-    const bool rowok = x >= 0 && x < nx && y >= 0 && y < ny;
-    const long long rb = rowok ? ((long long)x * ny + y) * nz : 0;
+  // four rows per warp step: twelve loads in flight before the ballots
+  for (int row0 = warp; row0 < EX * EY; row0 += 32) {
+    uint8_t v[4][3];
 #pragma unroll
-    for (int w = 0; w < 3; ++w) {
-      const int i = 32 * w + lane, z = z0 - r + i;
-      const bool v = rowok && i < EZ && z >= 0 && z < nz && __ldg(src + rb + z) != 0;
-      const unsigned int b = __ballot_sync(0xffffffffu, v);
-      if (lane == 0) inm[row][w] = b;
+    for (int u = 0; u < 4; ++u) {
+      const int row = row0 + 8 * u;
+      const int ix = row / EY, iy = row - ix * EY;
+      const int x = x0 - r + ix, y = y0 - r + iy;
+      const bool rowok = row < EX * EY && x >= 0 && x < nx && y >= 0 && y < ny;
+      const long long rb = rowok ? ((long long)x * ny + y) * nz : 0;
+#pragma unroll
+      for (int w = 0; w < 3; ++w) {
+        const int i = 32 * w + lane, z = z0 - r + i;
+        v[u][w] = (rowok && i < EZ && z >= 0 && z < nz) ? __ldg(src + rb + z) : 0;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int row = row0 + 8 * u;
+#pragma unroll
+      for (int w = 0; w < 3; ++w) {
+        const unsigned int b = __ballot_sync(0xffffffffu, v[u][w] != 0);
+        if (lane == 0 && row < EX * EY) inm[row][w] = b;
+      }
     }
   }
   __syncthreads();

@@ -165,7 +165,7 @@ SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
   if (threadIdx.x == 0) partial[2 * blockIdx.x + 1] = d;
 }
 
-__global__ void __launch_bounds__(SG_THREADS) k_stage_svi(const float* __restrict__ phi,
+__global__ void __launch_bounds__(SG_THREADS, 6) k_stage_svi(const float* __restrict__ phi,
                                                           const int32_t* __restrict__ band, long long m, int nx,
                                                           int ny, int nz, const float* __restrict__ Nd,
                                                           svie_law L, StageConst C, float* __restrict__ Lout,

@@ -69,6 +69,7 @@ class LevelSet:
         self._info = torch.zeros(nat.BAND_INFO_BYTES, dtype=torch.uint8, device=self.device)
         self._vstats = torch.zeros(nat.STATS_BYTES, dtype=torch.uint8, device=self.device)
         self._band64 = None
+        self._band32 = None
         self.last_flags = (1, 1)
         self.rebuild_band()
 
@@ -76,6 +77,17 @@ class LevelSet:
     @property
     def flat(self) -> torch.Tensor:
         return self.phi.view(-1)
+
+    @property
+    def band32(self) -> torch.Tensor:
+        """The band in ascending flat order (int32), listed on first use after a rebuild."""
+        if self._band32 is None:
+            self._band32 = self._ascending_band()
+        return self._band32
+
+    @band32.setter
+    def band32(self, idx: torch.Tensor) -> None:
+        self._band32 = idx
 
     @property
     def band(self) -> torch.Tensor:
@@ -91,31 +103,28 @@ class LevelSet:
         self._band64 = None
         self.occ_current = False
 
-    def rebuild_band(self) -> None:
-        """Clamp phi to +-width*h and list |phi| < width*h (1 - 1e-5) (levelset.py:70-77)."""
+    def _thresh(self):
         cap = self.width * self.h
-        n = self.grid.size
+        return nat.f32(cap), nat.f32(cap * (1 - 1e-5))
+
+    def rebuild_band(self) -> None:
+        """Clamp phi to +-width*h and list |phi| < width*h (1 - 1e-5) (levelset.py:70-77).
+
+        The stencil kernels take the brick-ordered list ``work32``; the
+        ascending list of the API (``band32`` / ``band``) is made on demand."""
+        cap, thresh = self._thresh()
         nx, ny, nz = self.grid.shape
         sc = self.scratch
-        wsb = nat.lib().svie_band_workspace_bytes(n)
-        ws = sc.get("band", wsb)
-        thresh = nat.f32(cap * (1 - 1e-5))
-        nat.call("svie_band_scan", nat.ptr(self.flat), n, nat.f32(cap), thresh, nat.ptr(ws), ws.numel(),
+        bws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
+        nat.call("svie_brick_band_scan", nat.ptr(self.flat), nx, ny, nz, cap, thresh, nat.ptr(bws), bws.numel(),
                  nat.ptr(self._info), nat.stream())
         count = int(_read(self._info, nat.BAND_INFO_DTYPE)["count"])
-        band = torch.empty(count, dtype=torch.int32, device=self.device)
-        nat.call("svie_band_write", nat.ptr(self.flat), nx, ny, nz, thresh, nat.ptr(ws), ws.numel(), nat.ptr(band),
-                 count, nat.ptr(self.occ), nat.ptr(self._info), nat.stream())
-        bws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
-        bcnt = sc.get("brick_count", 8)
         work = torch.empty(count, dtype=torch.int32, device=self.device)
-        nat.call("svie_brick_scan", 1, nat.ptr(self.flat), nx, ny, nz, thresh, nat.ptr(bws), bws.numel(), nat.ptr(bcnt),
-                 nat.stream())
-        nat.call("svie_brick_write", 1, nat.ptr(self.flat), nx, ny, nz, thresh, nat.ptr(bws), bws.numel(),
-                 nat.ptr(work), count, nat.stream())
+        nat.call("svie_brick_band_write", nat.ptr(self.flat), nx, ny, nz, thresh, nat.ptr(bws), bws.numel(),
+                 nat.ptr(work), count, nat.ptr(self.occ), nat.ptr(self._info), nat.stream())
         info = _read(self._info, nat.BAND_INFO_DTYPE)
-        self.band32 = band
         self.work32 = work
+        self._band32 = None
         self._band64 = None
         self.static_inside = int(info["static_inside"])
         self.band_lo = tuple(int(v) for v in info["lo"])
@@ -128,6 +137,25 @@ class LevelSet:
             for ax in range(3):
                 if self.band_lo[ax] < MARGIN or self.band_hi[ax] > shape[ax] - 1 - MARGIN:
                     raise RuntimeError("narrow band reaches the grid boundary; enlarge the padding")
+
+    def _ascending_band(self) -> torch.Tensor:
+        """The nodes of ``work32`` (the band of the last rebuild) in ascending flat order."""
+        n = self.grid.size
+        nx, ny, nz = self.grid.shape
+        m = self.work32.numel()
+        if m == 0:
+            return torch.empty(0, dtype=torch.int32, device=self.device)
+        sc = self.scratch
+        mask = sc.get("reinit_mask", n)
+        tmp = sc.get("reinit_tmp", n)
+        nat.call("svie_reinit_mask", nat.ptr(self.work32), m, nx, ny, nz, 0, 0, nat.ptr(mask), nat.ptr(tmp),
+                 nat.stream())
+        ws = sc.get("band", nat.lib().svie_band_workspace_bytes(n))
+        cnt = sc.get("band_count", 8)
+        nat.call("svie_mask_scan", nat.ptr(mask), n, nat.ptr(ws), ws.numel(), nat.ptr(cnt), nat.stream())
+        band = torch.empty(m, dtype=torch.int32, device=self.device)
+        nat.call("svie_mask_write", nat.ptr(mask), n, nat.ptr(ws), ws.numel(), nat.ptr(band), m, nat.stream())
+        return band
 
     def _check_margin(self, idx: torch.Tensor) -> None:
         """levelset.py:79-86 for an arbitrary index list."""
@@ -199,7 +227,7 @@ class LevelSet:
         """Dense occupancy field (levelset.py:117-121), recomputed from phi."""
         f = torch.empty(self.grid.size, dtype=torch.float32, device=self.device)
         nat.call("svie_dense_occupancy", nat.ptr(self.flat), self.grid.size, nat.ptr(f), nat.stream())
-        nat.call("svie_scatter_fractions", nat.ptr(self.flat), nat.ptr(self.band32), self.band32.numel(),
+        nat.call("svie_scatter_fractions", nat.ptr(self.flat), nat.ptr(self.work32), self.work32.numel(),
                  *self.strides, nat.ptr(f), nat.stream())
         return f.view(self.grid.shape)
 
@@ -246,7 +274,7 @@ class LevelSet:
         sc = self.scratch
         mask = sc.get("reinit_mask", n)
         tmp = sc.get("reinit_tmp", n)
-        nat.call("svie_reinit_mask", nat.ptr(self.band32), self.band32.numel(), nx, ny, nz, int(dilation), MARGIN,
+        nat.call("svie_reinit_mask", nat.ptr(self.work32), self.work32.numel(), nx, ny, nz, int(dilation), MARGIN,
                  nat.ptr(mask), nat.ptr(tmp), nat.stream())
         ws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
         cnt = sc.get("reinit_count", 8)

@@ -150,3 +150,60 @@ def test_band_scan_write_and_info(shape):
     nat.call("svie_brick_write", 1, nat.ptr(t), nx, ny, nz, float(thresh), nat.ptr(bws), bws.numel(), nat.ptr(bout),
              k, nat.stream())
     assert np.array_equal(bout.cpu().numpy(), _brick_order(ref, shape))
+
+
+@pytest.mark.parametrize("shape", SHAPES[1:])
+def test_brick_band_scan_write(shape):
+    """The brick-ordered rebuild (clamp, list, occupancy, info) equals the ascending one reordered."""
+    rng = np.random.default_rng(5)
+    h = np.float32(0.05)
+    phi = (rng.standard_normal(shape) * 0.4).astype(np.float32)
+    phi.reshape(-1)[7] = np.nan  # NaN stays NaN and is not in the band
+    nx, ny, nz = shape
+    cap = np.float32(6.0 * h)
+    thresh = np.float32(6.0 * h * (1 - 1e-5))
+    clamped = np.where(np.isnan(phi), phi, np.clip(phi, -cap, cap))
+    with np.errstate(invalid="ignore"):
+        sel = np.abs(clamped) < thresh
+        neg = clamped < 0
+    ref = _brick_order(np.flatnonzero(sel.reshape(-1)), shape)
+    t = torch.from_numpy(phi).cuda().view(-1)
+    lib = nat.lib()
+    bws = torch.empty(lib.svie_brick_workspace_bytes(nx, ny, nz), dtype=torch.uint8, device="cuda")
+    info = torch.zeros(nat.BAND_INFO_BYTES, dtype=torch.uint8, device="cuda")
+    nat.call("svie_brick_band_scan", nat.ptr(t), nx, ny, nz, float(cap), float(thresh), nat.ptr(bws), bws.numel(),
+             nat.ptr(info), nat.stream())
+    k = int(np.frombuffer(info.cpu().numpy().tobytes(), dtype=nat.BAND_INFO_DTYPE)[0]["count"])
+    assert k == ref.size
+    got_phi = t.cpu().numpy().reshape(shape)
+    assert np.array_equal(got_phi, clamped, equal_nan=True)
+    out = torch.empty(k, dtype=torch.int32, device="cuda")
+    occ = torch.empty(phi.size, dtype=torch.float32, device="cuda")
+    nat.call("svie_brick_band_write", nat.ptr(t), nx, ny, nz, float(thresh), nat.ptr(bws), bws.numel(),
+             nat.ptr(out), k, nat.ptr(occ), nat.ptr(info), nat.stream())
+    assert np.array_equal(out.cpu().numpy(), ref)
+    assert np.array_equal(occ.cpu().numpy().reshape(shape), neg.astype(np.float32))
+    d = np.frombuffer(info.cpu().numpy().tobytes(), dtype=nat.BAND_INFO_DTYPE)[0]
+    coords, icoords = np.argwhere(sel), np.argwhere(neg)
+    assert int(d["static_inside"]) == int((neg & ~sel).sum())
+    assert list(d["lo"]) == list(coords.min(0)) and list(d["hi"]) == list(coords.max(0))
+    assert list(d["ilo"]) == list(icoords.min(0)) and list(d["ihi"]) == list(icoords.max(0))
+
+
+def test_levelset_band_views_agree():
+    """LevelSet keeps the brick-ordered work list; its ascending band is the same node set, sorted,
+    and stays the band of the last rebuild while phi changes."""
+    from svierosion_gb300.grid import Grid
+    from svierosion_gb300.levelset import LevelSet
+
+    n, h = 48, 0.05
+    ax = (np.arange(n) - 0.5 * (n - 1)) * h
+    X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
+    phi = (np.sqrt(X ** 2 + Y ** 2 + Z ** 2) - 0.6).astype(np.float32)
+    ls = LevelSet(torch.from_numpy(phi).cuda(), Grid((float(ax[0]),) * 3, h, (n, n, n)), width=6)
+    work = ls.work32.cpu().numpy()
+    ls.flat[ls.work32.long()] += 0.3 * h  # values move; the band set must not
+    band = ls.band32.cpu().numpy()
+    assert np.array_equal(band, np.sort(work))
+    ref = np.flatnonzero(np.abs(np.clip(phi, -6 * h, 6 * h)) < np.float32(6 * h * (1 - 1e-5)))
+    assert np.array_equal(band, ref)
