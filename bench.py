@@ -250,9 +250,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
                               reinit_iterations=params.reinit_iterations)
     torch.cuda.synchronize()
     t_setup = time.time() - t_setup
-    band0 = ls.band32.numel()
+    band0 = ls.work32.numel()
     sim.run(target_fraction=None, max_steps=args.warmup)
-    timer = KernelTimer(capacity=64 * args.steps + 64)
+    # timed region: events only around the convolution passes (the roofline
+    # kernel); the full per-kernel breakdown comes from a second pass below
+    timer = KernelTimer(capacity=32 * args.steps + 64, only={"fft"})
     sim.timer = timer
     lib = nat.lib()
     if world > 1:
@@ -275,7 +277,18 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     updates = sim.band_updates - u0
-    kt = timer.summary()
+    kt_timed = timer.summary()
+    # breakdown pass: the same number of steps with events around every kernel
+    timer2 = KernelTimer(capacity=64 * args.steps + 64)
+    sim.timer = timer2
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record()
+    sim.run(target_fraction=None, max_steps=args.steps)
+    e3.record()
+    torch.cuda.synchronize()
+    ms2 = e2.elapsed_time(e3)
+    kt = timer2.summary()
     sim.timer = None
     if world > 1:
         t = torch.tensor([ms], dtype=torch.float64, device=dev)
@@ -302,11 +315,12 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     for k, v in kt.items():
         b = abytes.get(k)
         kern[k] = {"launches": v["launches"], "mean_us": round(1000 * v["mean_ms"], 2),
-                   "share": round(v["total_ms"] / ms, 4),
+                   "share": round(v["total_ms"] / ms2, 4),
                    "gbs": round(b / (v["mean_ms"] * 1e6), 1) if b else None}
     roof = None
     if dom is not None:
-        ach = abytes[dom] / (kt[dom]["mean_ms"] * 1e6)
+        dur = kt_timed[dom] if dom in kt_timed else kt[dom]
+        ach = abytes[dom] / (dur["mean_ms"] * 1e6)
         traffic = None
         tfile = ROOT / "profiles" / "traffic.json"
         if tfile.exists():
@@ -316,7 +330,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
                 traffic = None
         roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_src,
-                "algorithmic_bytes_per_launch": abytes[dom]}
+                "algorithmic_bytes_per_launch": abytes[dom], "launches_timed": dur["launches"],
+                "duration_source": "timed region" if dom in kt_timed else "breakdown pass"}
     step_bytes = 3 * (12 * grid.size + 20 * band_mean) + 4 * grid.size
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -328,6 +343,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
                    "setup_s": round(t_setup, 3)},
         "roofline": roof,
         "kernels": kern,
+        "kernels_pass": {"steps": args.steps, "ms_per_step": round(ms2 / args.steps, 4),
+                         "note": "second pass of the same steps with events around every kernel"},
         "step_roofline": {"bytes_per_step": int(step_bytes),
                           "achieved_gbs": round(step_bytes / (ms / args.steps) / 1e6, 1),
                           "frac": round(step_bytes / (ms / args.steps) / 1e6 / peak, 4)},

@@ -15,13 +15,20 @@ import torch
 
 
 class KernelTimer:
-    def __init__(self, capacity: int = 8192):
+    """``only``: names of the sections to time (None = all); a section named
+    "fft" stands for the five convolution passes."""
+
+    def __init__(self, capacity: int = 8192, only=None):
+        self.only = None if only is None else set(only)
         self.events = [torch.cuda.Event(enable_timing=True) for _ in range(capacity)]
         for e in self.events:
             e.record()
         torch.cuda.synchronize()
         self.next = 0
         self.groups = []  # (names, events)
+
+    def wants(self, name: str) -> bool:
+        return self.only is None or name in self.only
 
     def take(self, k: int) -> list:
         if self.next + k > len(self.events):
