@@ -15,6 +15,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 F32 = np.float32
+C64 = np.complex64   # spectrum type (complex128 in the float64 variant, oracle/fp64.py)
 I64 = np.int64
 MARGIN = 4
 KEY_EMPTY = np.iinfo(np.int64).max
@@ -489,12 +490,12 @@ def kernel_hat(shape, radius, spacing, quad=32):
     r = np.arange(-m, m + 1)
     ii, jj, kk = r % shape[0], r % shape[1], r % shape[2]
     kern[ii[:, None, None], jj[None, :, None], kk[None, None, :]] = w.astype(F32)
-    return np.fft.rfftn(kern).astype(np.complex64), m
+    return np.fft.rfftn(kern).astype(C64), m
 
 
 def exterior_fraction(fractions3, khat, radius, spacing):
     """svi.py:84-93."""
-    fh = np.fft.rfftn(fractions3.astype(F32)).astype(np.complex64)
+    fh = np.fft.rfftn(fractions3.astype(F32)).astype(C64)
     fh *= khat
     g = np.fft.irfftn(fh, s=fractions3.shape, axes=(0, 1, 2)).astype(F32) * F32(spacing ** 3)
     ball_volume = 4.0 / 3.0 * math.pi * radius ** 3

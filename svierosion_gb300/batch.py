@@ -1,11 +1,12 @@
 """Batched and served erosion: many independent solids on one GPU.
 
 Every solid (an :class:`ErosionJob`) owns its level set, simulation,
-workspaces and CUDA stream.  The scheduler advances all active jobs in
-rounds: it enqueues one TVD-RK3 step of every job on that job's stream (no
-host synchronisation), then finishes the steps job by job (one 256-byte read
-back each, plus the reference's rare extra work: regula falsi on the last
-step, reinitialisation).  Kernels of different jobs overlap on the GPU, so
+workspaces and CUDA stream.  The scheduler keeps one TVD-RK3 step of
+every active job in flight on that job's stream and polls their completion
+events: a job whose step has finished is finished on the host (one 256-byte
+read back, plus the reference's rare extra work: regula falsi on the last
+step, reinitialisation) and relaunched at once, without waiting for the
+other jobs.  Kernels of different jobs overlap on the GPU, so
 small grids that cannot fill 152 SMs alone fill them together, and each job
 stops independently.  A job's arithmetic is exactly the plain path's, so its
 result is the same alone and in the mix.
@@ -133,6 +134,16 @@ class ErosionJob:
         with torch.cuda.stream(self.stream):
             self.sim.step_finish()
 
+    def ready(self) -> bool:
+        """The launched step has completed on the GPU (non-blocking)."""
+        return self.sim.step_ready()
+
+    def wait(self) -> None:
+        """Block until the launched step has completed."""
+        ev = self.sim._done_event
+        if ev is not None:
+            ev.synchronize()
+
     def _complete(self, res) -> None:
         self.done = True
         self.result = JobResult(self.name, res.stop_reason, res.fraction, self.sim.time, self.sim.steps,
@@ -154,21 +165,37 @@ class BatchedErosion:
     def run(self, release: bool = True) -> list[JobResult]:
         for j in self.jobs:
             j.setup()
-        active = list(self.jobs)
-        while active:
-            launched = [j for j in active if j.launch()]
-            for j in launched:
-                j.finish()
-            still = []
-            for j in active:
-                if j.done:
-                    if release:
-                        j.release()
-                else:
-                    still.append(j)
-            active = still
+        pending = [j for j in self.jobs if j.launch()]
+        for j in self.jobs:
+            if j.done and release:
+                j.release()
+        while pending:
+            pending = _advance(pending, release)
         torch.cuda.synchronize()
         return [j.result for j in self.jobs]
+
+
+def _advance(pending: list, release: bool, on_done=None) -> list:
+    """One polling sweep: every job whose step has completed is finished and
+    relaunched at once (its stream never waits for the other jobs); if none
+    has completed, block on the oldest launched step instead of spinning."""
+    still, progressed = [], False
+    for j in pending:
+        if j.ready():
+            progressed = True
+            j.finish()
+            if j.launch():
+                still.append(j)
+            else:
+                if on_done is not None:
+                    on_done(j)
+                if release:
+                    j.release()
+        else:
+            still.append(j)
+    if not progressed and still:
+        still[0].wait()
+    return still
 
 
 def run_plain(jobs: list[ErosionJob]) -> list[JobResult]:
@@ -222,13 +249,20 @@ class ErosionServer:
             job.setup()
             req.admitted = now
             self.in_use += need
-            self.active.append((req, job))
+            if job.launch():
+                self.active.append((req, job))
+            else:  # finished at set-up (e.g. already below its target)
+                req.completed = time.time() - self._t0
+                req.result = job.result
+                self.in_use -= need
+                job.release()
+                self.done.append(req)
 
     def run(self, requests: list[Request]) -> dict:
         """Open-loop: request i becomes visible at t0 + arrival_i."""
         for r in sorted(requests, key=lambda r: r.arrival):
             self.submit(r)
-        t0 = time.time()
+        t0 = self._t0 = time.time()
         updates = 0
         while self.queue or self.active:
             now = time.time() - t0
@@ -236,21 +270,23 @@ class ErosionServer:
             if not self.active:
                 time.sleep(max(0.0, min(self.queue[0].arrival - now, 0.01)))
                 continue
-            launched = [(r, j) for r, j in self.active if j.launch()]
-            for _, j in launched:
-                j.finish()
-            still = []
-            for r, j in self.active:
-                if j.done:
-                    r.completed = time.time() - t0
-                    r.result = j.result
-                    updates += j.result.band_updates
-                    self.in_use -= j.footprint()
-                    j.release()
-                    self.done.append(r)
-                else:
-                    still.append((r, j))
-            self.active = still
+            req_of = {id(j): r for r, j in self.active}
+            finished = []
+
+            def on_done(j):
+                r = req_of[id(j)]
+                r.completed = time.time() - t0
+                r.result = j.result
+                finished.append(j)
+
+            jobs = _advance([j for _, j in self.active], release=False, on_done=on_done)
+            for j in finished:
+                updates += j.result.band_updates
+                self.in_use -= j.footprint()
+                j.release()
+                self.done.append(req_of[id(j)])
+            alive = {id(j) for j in jobs}
+            self.active = [(r, j) for r, j in self.active if id(j) in alive]
         wall = time.time() - t0
         lat = np.array([r.completed - r.arrival for r in self.done])
         return {"requests": len(self.done), "wall_s": wall, "solves_per_s": len(self.done) / wall,
