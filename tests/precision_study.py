@@ -59,7 +59,9 @@ def run_gpu(path: str) -> None:
     for name, (kind, kw, target, params) in laws.items():
         grid = S.make_grid(mesh, params)
         phi0 = S.mesh_to_sdf(mesh, grid, band=params.band)
-        save[name + "/phi0"] = phi0.cpu().numpy()
+        key = "phi0_%dx%dx%d" % grid.shape
+        if key not in save:
+            save[key] = phi0.cpu().numpy()
         save[name + "/grid"] = np.array([*grid.origin, grid.spacing, *grid.shape], dtype=np.float64)
         ls = S.LevelSet(phi0.clone(), grid, width=params.band)
         sim = S.ErosionSimulation(ls, params.make_law(length_scale=length))
@@ -89,7 +91,7 @@ def compare(path: str) -> None:
         g = d[name + "/grid"]
         shape = tuple(int(v) for v in g[4:7])
         h = float(g[3])
-        phi0 = d[name + "/phi0"].astype(np.float64).reshape(shape)
+        phi0 = d["phi0_%dx%dx%d" % shape].astype(np.float64).reshape(shape)
         law = fp64.make_law(kind, length_scale=length, **kw)
         ref = fp64.Simulation(phi0, h, law)
         rep = {"law": name, "grid": list(shape)}
