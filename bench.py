@@ -363,7 +363,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
 
 
 def e2e_solve(args, mesh, params, dev) -> dict:
-    """The public erode() call: host mesh in, host history and band values out."""
+    """The public erode() call: host mesh in; the eroded meshes at the snapshot fractions and the
+    target, the history and the band values out."""
     import torch
     import svierosion_gb300 as S
     from svierosion_gb300 import _native as nat
@@ -379,7 +380,7 @@ def e2e_solve(args, mesh, params, dev) -> dict:
     torch.cuda.synchronize()
     nat.reset_transfer_counters()
     t0 = time.time()
-    res = S.erode(mesh, params, extract_meshes=False, keep_state=True)
+    res = S.erode(mesh, params, keep_state=True)
     ls = res.level_set
     band_vals = nat.d2h(ls.flat[ls.band32])
     hist = [(r.step, r.fraction) for r in res.history]
@@ -392,6 +393,8 @@ def e2e_solve(args, mesh, params, dev) -> dict:
             "d2h_bytes_per_step": int(d2h / steps), "solve_s": round(wall, 3), "steps": len(res.history),
             "stop_reason": res.stop_reason, "fraction": round(res.fraction, 7),
             "sdf_s": round(res.timings.get("sdf", 0.0), 3), "evolve_s": round(res.timings.get("evolve", 0.0), 3),
+            "mesh_s": round(res.timings.get("mesh", 0.0), 3),
+            "mesh_faces": int(len(res.mesh.faces)) if res.mesh is not None else 0,
             "solves_per_s": round(1.0 / wall, 4), "history_len": len(hist)}
 
 

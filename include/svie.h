@@ -303,6 +303,26 @@ int svie_rk_stage(float* phi, const int32_t* band, int64_t m, const float* u0, c
                   const double* dt, int stage, void* stream);
 int svie_set_f64(double* dst, double value, void* stream);
 
+/* ------------------------------------------------- surface extraction */
+/* extract_surface (svierosion/surface.py:16-56): marching cubes over the cells
+ * whose lower corner is one of the m band nodes (ascending), with a case table
+ * generated from the method's definition (svie_surface_table returns it:
+ * tri[256][16] cell-edge triples, -1 after the last; ntri[256] triangle
+ * counts).  svie_surface_scan counts vertices and faces (device int64
+ * totals[2]); svie_surface_write fills verts (nv, 3) in index coordinates and
+ * faces (nt, 3), using vinfo (int32, one per grid node) as scratch; ids follow
+ * the band order.  svie_surface_project moves every vertex by one Newton step
+ * on the tricubic interpolant, limited to max_shift cells (surface.py:44-51). */
+int svie_surface_table(int8_t* tri, uint8_t* ntri);
+size_t svie_surface_workspace_bytes(int64_t m);
+int svie_surface_scan(const float* phi, const int32_t* band, int64_t m, int nx, int ny, int nz,
+                      void* ws, size_t ws_bytes, int64_t* totals, void* stream);
+int svie_surface_write(const float* phi, const int32_t* band, int64_t m, int nx, int ny, int nz,
+                       const void* ws, size_t ws_bytes, int32_t* vinfo, float* verts, int64_t nv,
+                       int32_t* faces, int64_t nt, void* stream);
+int svie_surface_project(const float* phi, int ny, int nz, float* verts, int64_t nv, float max_shift,
+                         void* stream);
+
 /* ------------------------------------------------------ reinitialisation */
 /* LevelSet.reinitialize (svierosion/levelset.py:154-183): work mask = band
  * dilated by `dilation` cells with the `margin` outer layers cleared. */

@@ -133,6 +133,11 @@ _SIGS = {
     "svie_reinit_geometry": (I, [V, V, I64, I64, I64, I64, F, F, V, V]),
     "svie_reinit_iterate": (I, [V, V, I64, V, I64, I64, I64, I64, F, V, I, V]),
     "svie_reinit_rhs": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),
+    "svie_surface_table": (I, [V, V]),
+    "svie_surface_workspace_bytes": (Z, [I64]),
+    "svie_surface_scan": (I, [V, V, I64, I, I, I, V, Z, V, V]),
+    "svie_surface_write": (I, [V, V, I64, I, I, I, V, Z, V, V, I64, V, I64, V]),
+    "svie_surface_project": (I, [V, I, I, V, I64, F, V]),
     "svie_reinit_geometry_unpack": (I, [V, I64, V, V, V, V, V]),
     "svie_dilate": (I, [V, I, I, I, I, V, V, V]),
     "svie_mesh_tri_index": (I, [V, V, I64, D, D, D, D, V, V, V, V]),

@@ -166,6 +166,7 @@ struct OpMaxF { SVIE_DEV float operator()(float a, float b) const { return fmaxf
 struct OpMinF { SVIE_DEV float operator()(float a, float b) const { return fminf(a, b); } };
 struct OpSumD { SVIE_DEV double operator()(double a, double b) const { return a + b; } };
 struct OpSumU { SVIE_DEV unsigned int operator()(unsigned int a, unsigned int b) const { return a + b; } };
+struct OpSumI { SVIE_DEV int operator()(int a, int b) const { return a + b; } };
 struct OpSumLL { SVIE_DEV long long operator()(long long a, long long b) const { return a + b; } };
 struct OpMinI { SVIE_DEV int operator()(int a, int b) const { return min(a, b); } };
 struct OpMaxI { SVIE_DEV int operator()(int a, int b) const { return max(a, b); } };
@@ -306,6 +307,33 @@ SVIE_DEV void cubic_dw(float t, float w[4]) {
 }
 
 // Tricubic interpolation at index coordinates p (reference kernels.py:212-228).
+// tricubic_with_gradient (kernels.py:232-253): value and per-cell gradient at
+// index coordinates p, accumulated tap by tap in the reference's order.
+SVIE_DEV void tricubic_grad_at(const float* __restrict__ g, int ny, int nz, float3 p, float* val, float* gxo,
+                               float* gyo, float* gzo) {
+  const float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
+  const float tx = p.x - fx, ty = p.y - fy, tz = p.z - fz;
+  float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
+  cubic_w(tx, wx); cubic_w(ty, wy); cubic_w(tz, wz);
+  cubic_dw(tx, dx); cubic_dw(ty, dy); cubic_dw(tz, dz);
+  const long long syz = (long long)ny * nz;
+  const long long b0 = ((long long)fx - 1) * syz + ((long long)fy - 1) * nz + ((long long)fz - 1);
+  float v = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
+  for (int a = 0; a < 4; ++a)
+    for (int b = 0; b < 4; ++b)
+      for (int c = 0; c < 4; ++c) {
+        const float s = __ldg(g + b0 + a * syz + b * nz + c);
+        v = v + wx[a] * wy[b] * wz[c] * s;
+        gx = gx + dx[a] * wy[b] * wz[c] * s;
+        gy = gy + wx[a] * dy[b] * wz[c] * s;
+        gz = gz + wx[a] * wy[b] * dz[c] * s;
+      }
+  *val = v;
+  *gxo = gx;
+  *gyo = gy;
+  *gzo = gz;
+}
+
 SVIE_DEV float tricubic_at(const float* __restrict__ g, int ny, int nz, float3 p) {
   float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
   float wx[4], wy[4], wz[4];

@@ -48,24 +48,8 @@ __global__ void k_tricubic_grad(const float* __restrict__ g, int ny, int nz, con
                                 long long m, float* __restrict__ val, float* __restrict__ grad) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  float px = p[3 * t], py = p[3 * t + 1], pz = p[3 * t + 2];
-  float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
-  float tx = px - fx, ty = py - fy, tz = pz - fz;
-  float wx[4], wy[4], wz[4], dx[4], dy[4], dz[4];
-  cubic_w(tx, wx); cubic_w(ty, wy); cubic_w(tz, wz);
-  cubic_dw(tx, dx); cubic_dw(ty, dy); cubic_dw(tz, dz);
-  const long long syz = (long long)ny * nz;
-  const long long b0 = ((long long)fx - 1) * syz + ((long long)fy - 1) * nz + ((long long)fz - 1);
-  float v = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-  for (int a = 0; a < 4; ++a)
-    for (int b = 0; b < 4; ++b)
-      for (int c = 0; c < 4; ++c) {
-        float s = __ldg(g + b0 + a * syz + b * nz + c);
-        v = v + wx[a] * wy[b] * wz[c] * s;
-        gx = gx + dx[a] * wy[b] * wz[c] * s;
-        gy = gy + wx[a] * dy[b] * wz[c] * s;
-        gz = gz + wx[a] * wy[b] * dz[c] * s;
-      }
+  float v, gx, gy, gz;
+  tricubic_grad_at(g, ny, nz, make_float3(p[3 * t], p[3 * t + 1], p[3 * t + 2]), &v, &gx, &gy, &gz);
   val[t] = v;
   grad[3 * t] = gx;
   grad[3 * t + 1] = gy;
