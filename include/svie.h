@@ -303,6 +303,26 @@ int svie_rk_stage(float* phi, const int32_t* band, int64_t m, const float* u0, c
                   const double* dt, int stage, void* stream);
 int svie_set_f64(double* dst, double value, void* stream);
 
+/* ------------------------------------------------- point-to-mesh distance */
+/* point_mesh_distance (svierosion/api.py:104-168), exact: the T pieces (T x 9
+ * floats) are binned by centroid into a gx x gy x gz grid of cells of side cs
+ * from (ox, oy, oz) (svie_piece_grid_build, workspace svie_piece_grid_bytes);
+ * svie_point_mesh_distance walks Chebyshev shells of cells around each point
+ * until no unvisited piece can be closer (rho bounds centroid-to-piece
+ * distances) and writes the distance (float32, sqrt of the float32 squared
+ * distance of kernels.py:382-427). */
+/* The triangles of a device mesh relative to (sx, sy, sz) as float32 pieces (T x 9), the first-edge
+ * lengths (float32 [T]) and the largest edge and centroid-to-vertex distance (float bits in
+ * maxbits[0], maxbits[1]). */
+int svie_mesh_pieces(const double* vertices, const int32_t* faces, int64_t T, double sx, double sy, double sz,
+                     float* out, float* first_edge, uint32_t* maxbits, void* stream);
+size_t svie_piece_grid_bytes(int64_t T, int gx, int gy, int gz);
+int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float oz, float cs, int gx, int gy,
+                          int gz, void* ws, size_t ws_bytes, void* stream);
+int svie_point_mesh_distance(const float* pts, int64_t n, const float* tri, int64_t T, float ox, float oy,
+                             float oz, float cs, int gx, int gy, int gz, const void* ws, size_t ws_bytes,
+                             float rho, float* out, void* stream);
+
 /* ------------------------------------------------- surface extraction */
 /* extract_surface (svierosion/surface.py:16-56): marching cubes over the cells
  * whose lower corner is one of the m band nodes (ascending), with a case table
@@ -322,6 +342,10 @@ int svie_surface_write(const float* phi, const int32_t* band, int64_t m, int nx,
                        int32_t* faces, int64_t nt, void* stream);
 int svie_surface_project(const float* phi, int ny, int nz, float* verts, int64_t nv, float max_shift,
                          void* stream);
+/* Signed volume (float64) of the mesh (verts in index coordinates) about (cx, cy, cz), for the
+ * orientation test of surface.py:54-55. */
+int svie_surface_signed_volume(const float* verts, const int32_t* faces, int64_t nt, double cx, double cy,
+                               double cz, double* out, void* stream);
 
 /* ------------------------------------------------------ reinitialisation */
 /* LevelSet.reinitialize (svierosion/levelset.py:154-183): work mask = band

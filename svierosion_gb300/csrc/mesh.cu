@@ -187,6 +187,47 @@ __global__ void k_signed_volume(const double* __restrict__ v, const int32_t* __r
   if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(out, s);
 }
 
+// Triangles of a device mesh as float32 coordinates relative to `shift`
+// (T x 9), with the length of each first edge (v1 - v0, float32) and the
+// largest edge length and centroid-to-vertex distance as float bits
+// (maxbits[0], maxbits[1]; non-negative floats order like their bits).
+__global__ void k_mesh_pieces(const double* __restrict__ v, const int32_t* __restrict__ f, long long T, double sx,
+                              double sy, double sz, float* __restrict__ out, float* __restrict__ first,
+                              unsigned int* maxbits) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float edge = 0.0f, rad = 0.0f;
+  if (t < T) {
+    float q[3][3];
+    for (int a = 0; a < 3; ++a) {
+      const long long vi = f[3 * t + a];
+      q[a][0] = (float)(v[3 * vi] - sx);
+      q[a][1] = (float)(v[3 * vi + 1] - sy);
+      q[a][2] = (float)(v[3 * vi + 2] - sz);
+      for (int d = 0; d < 3; ++d) out[9 * t + 3 * a + d] = q[a][d];
+    }
+    float c[3];
+    for (int d = 0; d < 3; ++d) c[d] = (q[0][d] + q[1][d] + q[2][d]) * (1.0f / 3.0f);
+    for (int a = 0; a < 3; ++a) {
+      const int b = (a + 1) % 3;
+      float e2 = 0.0f, r2 = 0.0f;
+      for (int d = 0; d < 3; ++d) {
+        const float de = q[b][d] - q[a][d], dr = q[a][d] - c[d];
+        e2 += de * de;
+        r2 += dr * dr;
+      }
+      edge = fmaxf(edge, sqrtf(e2));
+      rad = fmaxf(rad, sqrtf(r2));
+      if (a == 0) first[t] = sqrtf(e2);
+    }
+  }
+  edge = warp_max(edge);
+  rad = warp_max(rad);
+  if ((threadIdx.x & 31) == 0 && t - (threadIdx.x & 31) < T) {
+    atomicMax(maxbits, __float_as_uint(edge));
+    atomicMax(maxbits + 1, __float_as_uint(rad));
+  }
+}
+
 }  // namespace svie
 
 using namespace svie;
@@ -299,6 +340,22 @@ int svie_mesh_signed_volume(const double* vertices, const int32_t* faces, int64_
   if (T == 0) return SVIE_OK;
   k_signed_volume<<<blocks_for(T, 256), 256, 0, s>>>(vertices, faces, T, cx, cy, cz, out);
   return launch_status("svie_mesh_signed_volume");
+}
+
+int svie_mesh_pieces(const double* vertices, const int32_t* faces, int64_t T, double sx, double sy, double sz,
+                     float* out, float* first_edge, uint32_t* maxbits, void* stream) {
+  if (T < 0 || !maxbits || (T > 0 && (!vertices || !faces || !out || !first_edge))) {
+    set_error("svie_mesh_pieces: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(maxbits, 0, 2 * sizeof(uint32_t), s) != cudaSuccess) {
+    set_error("svie_mesh_pieces: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  if (T == 0) return SVIE_OK;
+  k_mesh_pieces<<<blocks_for(T, 256), 256, 0, s>>>(vertices, faces, T, sx, sy, sz, out, first_edge, maxbits);
+  return launch_status("svie_mesh_pieces");
 }
 
 }  // extern "C"

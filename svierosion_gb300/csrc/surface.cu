@@ -358,6 +358,28 @@ __global__ void k_surf_project(const float* __restrict__ f, int ny, int nz, floa
   verts[3 * t + 2] = p.z - sz;
 }
 
+// Signed volume of the extracted mesh from its float32 index-coordinate
+// vertices about (cx, cy, cz), accumulated in float64: only its sign is used
+// (surface.py:54-55 flips the faces of a negative mesh).
+__global__ void k_surf_volume(const float* __restrict__ v, const int32_t* __restrict__ f, long long T, double cx,
+                              double cy, double cz, double* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double s = 0.0;
+  if (t < T) {
+    double p[3][3];
+    for (int a = 0; a < 3; ++a) {
+      const long long vi = f[3 * t + a];
+      p[a][0] = (double)v[3 * vi] - cx;
+      p[a][1] = (double)v[3 * vi + 1] - cy;
+      p[a][2] = (double)v[3 * vi + 2] - cz;
+    }
+    s = p[0][0] * (p[1][1] * p[2][2] - p[1][2] * p[2][1]) + p[0][1] * (p[1][2] * p[2][0] - p[1][0] * p[2][2]) +
+        p[0][2] * (p[1][0] * p[2][1] - p[1][1] * p[2][0]);
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(out, s / 6.0);
+}
+
 }  // namespace svie
 
 using namespace svie;
@@ -442,6 +464,19 @@ int svie_surface_project(const float* phi, int ny, int nz, float* verts, int64_t
   if (nv == 0) return SVIE_OK;
   k_surf_project<<<blocks_for(nv, 256), 256, 0, (cudaStream_t)stream>>>(phi, ny, nz, verts, nv, max_shift);
   return launch_status("svie_surface_project");
+}
+
+int svie_surface_signed_volume(const float* verts, const int32_t* faces, int64_t nt, double cx, double cy, double cz,
+                               double* out, void* stream) {
+  if (nt < 0 || !out || (nt > 0 && (!verts || !faces))) {
+    set_error("svie_surface_signed_volume: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(out, 0, sizeof(double), s) != cudaSuccess) return SVIE_ERR_LAUNCH;
+  if (nt == 0) return SVIE_OK;
+  k_surf_volume<<<blocks_for(nt, 256), 256, 0, s>>>(verts, faces, nt, cx, cy, cz, out);
+  return launch_status("svie_surface_signed_volume");
 }
 
 }  // extern "C"

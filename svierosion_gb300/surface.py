@@ -40,19 +40,17 @@ def extract_surface(ls: LevelSet, project: bool = True, max_shift: float = 0.5) 
     if project and nv:
         nat.call("svie_surface_project", nat.ptr(ls.flat), ny, nz, nat.ptr(verts), nv, float(max_shift),
                  nat.stream())
-    # world coordinates in float64 and the orientation test on the device
-    world_d = verts.double() * grid.spacing + torch.tensor(grid.origin, dtype=torch.float64, device=ls.device)
-    vol = torch.zeros(1, dtype=torch.float64, device=ls.device)
-    if nt:
-        c = [grid.origin[a] + 0.5 * (grid.shape[a] - 1) * grid.spacing for a in range(3)]
-        nat.call("svie_mesh_signed_volume", nat.ptr(world_d), nat.ptr(faces), nt, *c, nat.ptr(vol), nat.stream())
-    world = nat.d2h(world_d)
+    # orientation test on the device; world coordinates (float64) on the host
+    vol = torch.empty(1, dtype=torch.float64, device=ls.device)
+    centre = [0.5 * (n - 1) for n in grid.shape]
+    nat.call("svie_surface_signed_volume", nat.ptr(verts), nat.ptr(faces), nt, *centre, nat.ptr(vol), nat.stream())
+    v = nat.d2h(verts).astype(np.float64)
     f = nat.d2h(faces).astype(np.int64)
     if len(f) and f.min() < 0:
         raise RuntimeError("surface extraction met a crossing outside the band (phi is not distance-like)")
     if float(vol.item()) < 0:
         f = f[:, ::-1].copy()
-    return TriMesh(world, f)
+    return TriMesh(np.asarray(grid.origin) + grid.spacing * v, f)
 
 
 def sample_field(field: torch.Tensor, grid: Grid, points_world: np.ndarray) -> np.ndarray:

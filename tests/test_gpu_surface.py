@@ -82,3 +82,36 @@ def test_erode_returns_closed_mesh_at_target():
     assert len(res.snapshots) == 1 and res.snapshots[0][2] is not None
     assert res.snapshots[0][2].is_watertight()
     assert "mesh" in res.timings
+
+
+def test_point_mesh_distance_is_exact():
+    """GPU shell search against brute force over all pieces (float64 numpy)."""
+    from svierosion_gb300.api import point_mesh_distance
+    from svierosion_gb300.sdf import bisect_long_triangles
+
+    mesh = shapes.icosphere(3)
+    rng = np.random.default_rng(5)
+    pts = np.concatenate([rng.uniform(-1.3, 1.3, (400, 3)), rng.standard_normal((200, 3)) * 0.02,
+                          mesh.vertices[:50] * 0.97])
+    got = point_mesh_distance(pts, mesh, max_edge=0.05)
+    tri = bisect_long_triangles(mesh.triangles(), max(0.05, 2 * float(np.median(
+        np.linalg.norm(mesh.triangles()[:, 1] - mesh.triangles()[:, 0], axis=1)))))
+    a, b, c = tri[:, 0], tri[:, 1], tri[:, 2]
+    from oracle.reference_np import point_triangle_distance2
+    ref = np.array([np.sqrt(point_triangle_distance2(np.broadcast_to(p, a.shape).astype(np.float32),
+                                                     a.astype(np.float32), b.astype(np.float32),
+                                                     c.astype(np.float32)).min()) for p in pts])
+    assert np.allclose(got, ref, rtol=1e-5, atol=2e-6)
+
+
+def test_erode_meshes_carry_vertex_data():
+    m = shapes.cube(1.0)
+    res = S.erode(m, S.ErosionParams(law="svi", radius=0.2, k=1, s=1, t=0.9, resolution=48, target_fraction=0.95))
+    vd = res.mesh.vertex_data
+    for key in ("depth", "N", "speed"):
+        assert key in vd and len(vd[key]) == len(res.mesh.vertices)
+    assert float(vd["depth"].max()) > 0
+    assert np.all((vd["N"] > 0) & (vd["N"] < 1))
+    res2 = S.erode(m, S.ErosionParams(law="mean", alpha=1.0, resolution=40, target_fraction=0.99, max_steps=30))
+    for key in ("depth", "H", "K", "speed"):
+        assert key in res2.mesh.vertex_data
