@@ -34,6 +34,7 @@ struct AxisPlan {
   int nst;
   unsigned long long radices;  // radix of stage s in bits [4s, 4s+4) (no arrays: no local-memory copy)
   const float2* tw;            // tw[k] = exp(-2 pi i k / n), k < n
+  const float2* stw;           // per-stage twiddles: stage with span p at p - 1 + k (R - 1) + q - 1 (n - 1 entries)
 };
 
 static bool factor_axis(int n, AxisPlan* p) {
@@ -187,9 +188,8 @@ __host__ __device__ inline int padded_len(int a) { return a + (a >> 4) + 1; }
 // already applied.
 template <int R>
 SVIE_DEV void fft_stage(const float2* __restrict__ src, float2* __restrict__ dst, int LS, int n, int nlines, int p,
-                        unsigned int pmagic, const float2* __restrict__ tw) {
+                        unsigned int pmagic, const float2* __restrict__ stw) {
   const int m = n / R;
-  const int twstep = n / (p * R);
   const int total = nlines * m;
   const unsigned int mmagic = m > 1 ? 0xFFFFFFFFu / (unsigned)m + 1u : 0u;
   for (int j = threadIdx.x; j < total; j += FFT_T) {
@@ -201,9 +201,9 @@ SVIE_DEV void fft_stage(const float2* __restrict__ src, float2* __restrict__ dst
 #pragma unroll
     for (int q = 0; q < R; ++q) v[q] = src[px(base + i + q * m)];
     if (k) {
-      const int tq = k * twstep;
+      const float2* tk = stw + k * (R - 1);  // the stage's twiddles w^(q k n / (p R)), q = 1..R-1
 #pragma unroll
-      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], __ldg(tw + q * tq));
+      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tk[q - 1]);
     }
     dft<R>(v);
     const int o = base + (i - k) * R + k;
@@ -213,20 +213,23 @@ SVIE_DEV void fft_stage(const float2* __restrict__ src, float2* __restrict__ dst
   __syncthreads();
 }
 
-SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPlan& P) {
+// `stw` is the axis' stage-twiddle table staged in shared memory; the stage
+// with span p starts at entry p - 1 (the earlier stages hold p - 1 entries).
+SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPlan& P, const float2* stw) {
   int p = 1;
   for (int st = 0; st < P.nst; ++st) {
     const int R = (int)((P.radices >> (4 * st)) & 15ULL);
     // ceil(2^32 / p): exact i / p = umulhi(i, mg) for i * p < 2^32
     const unsigned int mg = p > 1 ? 0xFFFFFFFFu / (unsigned)p + 1u : 0u;
+    const float2* sw = stw + (p - 1);
     switch (R) {
-      case 8: fft_stage<8>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
-      case 7: fft_stage<7>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
-      case 6: fft_stage<6>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
-      case 5: fft_stage<5>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
-      case 4: fft_stage<4>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
-      case 3: fft_stage<3>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
-      default: fft_stage<2>(a, b, LS, P.n, nlines, p, mg, P.tw); break;
+      case 8: fft_stage<8>(a, b, LS, P.n, nlines, p, mg, sw); break;
+      case 7: fft_stage<7>(a, b, LS, P.n, nlines, p, mg, sw); break;
+      case 6: fft_stage<6>(a, b, LS, P.n, nlines, p, mg, sw); break;
+      case 5: fft_stage<5>(a, b, LS, P.n, nlines, p, mg, sw); break;
+      case 4: fft_stage<4>(a, b, LS, P.n, nlines, p, mg, sw); break;
+      case 3: fft_stage<3>(a, b, LS, P.n, nlines, p, mg, sw); break;
+      default: fft_stage<2>(a, b, LS, P.n, nlines, p, mg, sw); break;
     }
     float2* t = a; a = b; b = t;
     p *= R;
@@ -238,6 +241,17 @@ SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPla
 __host__ __device__ inline int line_stride(int n) { return (n & 1) ? n : n + 1; }
 __host__ __device__ inline int padded_nzh(int nz) { return ((nz / 2 + 1) + 7) & ~7; }  // 64-byte rows
 __host__ __device__ inline int smem_buffer(int W, int n) { return padded_len(W * line_stride(n)); }
+// shared memory of a tile: two line buffers and the stage-twiddle table
+__host__ __device__ inline size_t tile_smem(int W, int n) {
+  return (2 * (size_t)smem_buffer(W, n) + (size_t)n) * sizeof(float2);
+}
+
+// Copy the axis' stage twiddles (n - 1 entries) into shared memory after the buffers.
+SVIE_DEV float2* stage_twiddles_to_smem(float2* sm, int W, const AxisPlan& P) {
+  float2* stw = sm + 2 * smem_buffer(W, P.n);
+  for (int e = threadIdx.x; e < P.n - 1; e += blockDim.x) stw[e] = __ldg(P.stw + e);
+  return stw;
+}
 
 // ----------------------------------------------------------------- z passes
 // Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
@@ -265,6 +279,7 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ i
       return;
     }
   }
+  const float2* stw = stage_twiddles_to_smem(sm, W, P);
   for (int l = warp; l < 2 * np; l += FFT_T / 32) {
     const bool ok = l < nl && (!lineflag || (__ldg(lineflag + line0 + l) & 1));
     float* row = reinterpret_cast<float*>(sa);
@@ -281,7 +296,7 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ i
     for (; z < n; z += 32) row[2 * px((l >> 1) * LS + z) + (l & 1)] = ok ? __ldg(g + z) : 0.0f;
   }
   __syncthreads();
-  const float2* r = run_fft(sa, sb, LS, np, P);
+  const float2* r = run_fft(sa, sb, LS, np, P, stw);
   float2* dst = out + line0 * nzp;
   for (int l = warp; l < nl; l += FFT_T / 32) {
     const int w = l >> 1;
@@ -316,6 +331,7 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
   const float2* src = in + line0 * nzp;
   const bool even = (n & 1) == 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float2* stw = stage_twiddles_to_smem(sm, W, P);
   for (int w = warp; w < np; w += FFT_T / 32) {
     const bool has2 = 2 * w + 1 < nl;
     const float2* s1 = src + (long long)(2 * w) * nzp;
@@ -345,7 +361,7 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
     }
   }
   __syncthreads();
-  const float2* r = run_fft(sa, sb, LS, np, P);
+  const float2* r = run_fft(sa, sb, LS, np, P, stw);
   float* dst = out + line0 * n;
   for (int l = warp; l < nl; l += FFT_T / 32) {
     if (lineflag && !(__ldg(lineflag + line0 + l) & 2)) continue;
@@ -387,6 +403,7 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
   const int c0 = blockIdx.x * SW;
   const int nl = min(SW, ninner - c0);
   float2* base = data + (long long)blockIdx.y * outer_stride + c0;
+  const float2* stw = stage_twiddles_to_smem(sm, SW, P);
   // each thread owns column c = tid & 7 and rows k = tid >> 3, + 32, ...
   const int c = threadIdx.x & 7, k0 = threadIdx.x >> 3;
   const bool col = c < nl;
@@ -412,7 +429,7 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
     }
   }
   __syncthreads();
-  float2* r = run_fft(sa, sb, LS, nl, P);
+  float2* r = run_fft(sa, sb, LS, nl, P, stw);
   if (mode == 2) {
     const int nyh = K.ny / 2 + 1;
     const int y = blockIdx.y, yr = min(y, K.ny - y);
@@ -428,7 +445,7 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
     }
     __syncthreads();
     float2* other = (r == sa) ? sb : sa;
-    r = run_fft(r, other, LS, nl, P);
+    r = run_fft(r, other, LS, nl, P, stw);
   }
   if (col) {
     const bool conj_out = (mode != 0);
@@ -448,6 +465,23 @@ __global__ void k_twiddles(float2* tw, int n) {
   double s, c;
   sincospi(2.0 * (double)k / (double)n, &s, &c);
   tw[k] = make_float2((float)c, (float)(-s));
+}
+
+// Stage twiddle table from the axis table: entry p - 1 + k (R - 1) + (q - 1)
+// of the stage with span p and radix R is tw[q k n / (p R)] (k < p, 1 <= q < R).
+__global__ void k_stage_twiddles(AxisPlan P, float2* stw) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.n - 1) return;
+  int p = 1;
+  for (int st = 0; st < P.nst; ++st) {
+    const int R = (int)((P.radices >> (4 * st)) & 15ULL);
+    if (e < p * R - 1) {
+      const int r = e - (p - 1), k = r / (R - 1), q = r % (R - 1) + 1;
+      stw[e] = P.tw[q * k * (P.n / (p * R))];
+      return;
+    }
+    p *= R;
+  }
 }
 
 struct GL32 {
@@ -611,7 +645,7 @@ __global__ void k_khat_expand(const float* __restrict__ K, int nx, int ny, int n
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct PlanLayout {
-  size_t tw_x, tw_y, tw_z, kred, total;
+  size_t tw_x, tw_y, tw_z, stw_x, stw_y, stw_z, kred, total;
 };
 
 static PlanLayout plan_layout(int nx, int ny, int nz) {
@@ -620,16 +654,20 @@ static PlanLayout plan_layout(int nx, int ny, int nz) {
   L.tw_x = off; off += align256((size_t)nx * sizeof(float2));
   L.tw_y = off; off += align256((size_t)ny * sizeof(float2));
   L.tw_z = off; off += align256((size_t)nz * sizeof(float2));
+  L.stw_x = off; off += align256((size_t)nx * sizeof(float2));
+  L.stw_y = off; off += align256((size_t)ny * sizeof(float2));
+  L.stw_z = off; off += align256((size_t)nz * sizeof(float2));
   L.kred = off; off += align256((size_t)(nx / 2 + 1) * (ny / 2 + 1) * (nz / 2 + 1) * sizeof(float));
   L.total = off;
   return L;
 }
 
-// Complex lines per CTA of the z passes: two shared buffers of W lines stay
-// under ~56 KB, so four CTAs fit on an SM.
+// Complex lines per CTA of the z passes: the two shared buffers of W lines and
+// the twiddle table stay under 55 KB, so four CTAs fit on an SM.
 static int z_width(int n) {
-  int w = 3290 / line_stride(n);
-  return w > 16 ? 16 : (w < 1 ? 1 : w);
+  int w = 16;
+  while (w > 1 && tile_smem(w, n) > 55 * 1024) --w;
+  return w;
 }
 
 static int ensure_smem_attr() {
@@ -669,6 +707,9 @@ static int make_plans(const void* plan, int nx, int ny, int nz, Plans* P) {
   P->x.tw = (const float2*)(b + L.tw_x);
   P->y.tw = (const float2*)(b + L.tw_y);
   P->z.tw = (const float2*)(b + L.tw_z);
+  P->x.stw = (const float2*)(b + L.stw_x);
+  P->y.stw = (const float2*)(b + L.stw_y);
+  P->z.stw = (const float2*)(b + L.stw_z);
   P->kred = (const float*)(b + L.kred);
   return SVIE_OK;
 }
@@ -677,7 +718,7 @@ static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, flo
                      float alpha, float beta, cudaStream_t s, const uint8_t* lineflag = nullptr) {
   const long long nlines = (long long)nx * ny;
   const int W = z_width(nz), nzp = padded_nzh(nz);
-  const size_t smem = 2 * (size_t)smem_buffer(W, nz) * sizeof(float2);
+  const size_t smem = tile_smem(W, nz);
   const long long nb = (nlines + 2 * W - 1) / (2 * W);
   if (fwd) k_fft_z_r2c<<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, W, nzp, lineflag);
   else k_fft_z_c2r<<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, W, nzp, alpha, beta, lineflag);
@@ -687,7 +728,7 @@ static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, flo
 static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s,
                      const uint8_t* slabflag = nullptr) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
-  const size_t smem = 2 * (size_t)smem_buffer(SW, ny) * sizeof(float2);
+  const size_t smem = tile_smem(SW, ny);
   dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)nx);
   k_fft_strided<4><<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, KGeom{nullptr, ny, nzh},
                                        slabflag, mode == 1 ? 2 : 1);
@@ -696,7 +737,7 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
 // x lines: outer index y, line index kz, element stride ny * nzp.
 static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
-  const size_t smem = 2 * (size_t)smem_buffer(SW, nx) * sizeof(float2);
+  const size_t smem = tile_smem(SW, nx);
   dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)ny);
   k_fft_strided<3><<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, KGeom{P.kred, ny, nzh},
                                        nullptr, 0);
@@ -789,6 +830,9 @@ int svie_conv_plan_init(void* plan, int nx, int ny, int nz, const double* w, int
   k_twiddles<<<blocks_for(nx, 256), 256, 0, s>>>((float2*)(b + L.tw_x), nx);
   k_twiddles<<<blocks_for(ny, 256), 256, 0, s>>>((float2*)(b + L.tw_y), ny);
   k_twiddles<<<blocks_for(nz, 256), 256, 0, s>>>((float2*)(b + L.tw_z), nz);
+  k_stage_twiddles<<<blocks_for(nx, 256), 256, 0, s>>>(P.x, (float2*)(b + L.stw_x));
+  k_stage_twiddles<<<blocks_for(ny, 256), 256, 0, s>>>(P.y, (float2*)(b + L.stw_y));
+  k_stage_twiddles<<<blocks_for(nz, 256), 256, 0, s>>>(P.z, (float2*)(b + L.stw_z));
   const int side = 2 * m + 1, nzh = nz / 2 + 1, nyh = ny / 2 + 1, nxh = nx / 2 + 1;
   double* A = (double*)ws;
   double* Bq = (double*)((char*)ws + align256((size_t)side * side * nzh * sizeof(double)));
@@ -797,7 +841,7 @@ int svie_conv_plan_init(void* plan, int nx, int ny, int nz, const double* w, int
   k_khat_b<<<blocks_for((long long)side * nyh * nzh, TB, 4096), TB, ny * sizeof(double), s>>>(A, m, ny, nzh, Bq);
   k_khat_c<<<blocks_for((long long)nxh * nyh * nzh, TB, 8192), TB, nx * sizeof(double), s>>>(
       Bq, m, nx, ny, nzh, (float*)(b + L.kred));
-  return launch_status("svie_conv_plan_init", 6);
+  return launch_status("svie_conv_plan_init", 9);
 }
 
 int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, float* out, double alpha,
