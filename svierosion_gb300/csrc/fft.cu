@@ -37,19 +37,31 @@ struct AxisPlan {
   const float2* stw;           // per-stage twiddles: stage with span p at p - 1 + k (R - 1) + q - 1 (n - 1 entries)
 };
 
+// Radix order: the largest odd radix first, then the even radices
+// (descending), then the other odd ones.  With an odd first radix no stage of
+// the 8-line tiles writes at an even stride from p = 1 (see tile_stage).
 static bool factor_axis(int n, AxisPlan* p) {
   if (n < 1 || n > FFT_MAXN) return false;
   static const int rs[] = {8, 7, 6, 5, 4, 3, 2};
-  int m = n, st = 0;
-  unsigned long long packed = 0;
+  int m = n, cnt = 0, fac[FFT_MAXST + 1];
   for (int r : rs) {
     while (m % r == 0) {
-      if (st >= FFT_MAXST) return false;
-      packed |= (unsigned long long)r << (4 * st++);
+      if (cnt >= FFT_MAXST) return false;
+      fac[cnt++] = r;
       m /= r;
     }
   }
   if (m != 1) return false;
+  int order[FFT_MAXST], st = 0, first_odd = -1;
+  for (int i = 0; i < cnt; ++i)
+    if (fac[i] & 1) { first_odd = i; break; }
+  if (first_odd >= 0) order[st++] = fac[first_odd];
+  for (int i = 0; i < cnt; ++i)
+    if (!(fac[i] & 1)) order[st++] = fac[i];
+  for (int i = 0; i < cnt; ++i)
+    if ((fac[i] & 1) && i != first_odd) order[st++] = fac[i];
+  unsigned long long packed = 0;
+  for (int i = 0; i < st; ++i) packed |= (unsigned long long)order[i] << (4 * i);
   p->n = n;
   p->nst = st;
   p->radices = packed;
@@ -174,62 +186,65 @@ SVIE_DEV void dft<6>(float2* x) {
   x[5] = csub(e[2], o2);
 }
 
-// Shared-memory index with one pad slot every 16 complex values: the stride-R
-// writes of the early Stockham stages then fall on distinct banks.
-SVIE_DEV int px(int a) { return a + (a >> 4); }
-__host__ __device__ inline int padded_len(int a) { return a + (a >> 4) + 1; }
-
-// One Stockham radix-R stage over `nlines` lines of length n, reading
-// src[line*LS + k] and writing dst (ping-pong buffers).  The nlines * n / R
-// butterflies of the stage are spread over all threads of the CTA (thread j
-// takes butterflies j, j + FFT_T, ...), so lanes stay busy when n / R is not
-// a multiple of 32; line = j / m and k = i mod p use magic multipliers
-// (exact: j * m and i * p stay below 2^32).  p = product of the radices
-// already applied.
-template <int R>
-SVIE_DEV void fft_stage(const float2* __restrict__ src, float2* __restrict__ dst, int LS, int n, int nlines, int p,
-                        unsigned int pmagic, const float2* __restrict__ stw) {
+// ------------------------------------------------------------ tile layout
+// A tile holds LW lines of length n in shared memory, element (line l,
+// position x) at x * PS + l.  Butterfly j of a stage takes line j % LW and
+// column b = j / LW, so the 16 lanes of a half-warp (one wavefront of 8-byte
+// shared accesses) touch LW lines at 16 / LW consecutive columns:
+//  - LW = 16: every stage access is 16 consecutive slots, free of bank
+//    conflicts for any PS (the z passes use PS = 17 so that their loads and
+//    stores, lanes along a line, are conflict-free too);
+//  - LW = 8 (PS = 8): the two columns b, b + 1 (b even) land on different
+//    halves of the bank row whenever their positions differ in parity, which
+//    fails only where a run of k = b mod p wraps inside the pair (p odd, R
+//    even) and in a first stage of even radix; factor_axis puts one odd radix
+//    first so that only the wrap case remains (measured: about 1.5% extra
+//    wavefronts);
+//  - LW = 1 (PS = 1): one line per tile, for axes too long for the others.
+// Each stage is one Stockham radix-R pass from src to dst (ping-pong).
+template <int R, int LW, int PS>
+SVIE_DEV void tile_stage(const float2* __restrict__ src, float2* __restrict__ dst, int n, int p, unsigned int pmagic,
+                         const float2* __restrict__ stw) {
   const int m = n / R;
-  const int total = nlines * m;
-  const unsigned int mmagic = m > 1 ? 0xFFFFFFFFu / (unsigned)m + 1u : 0u;
+  const int total = LW * m;
   for (int j = threadIdx.x; j < total; j += FFT_T) {
-    const int line = m > 1 ? (int)__umulhi((unsigned)j, mmagic) : j;
-    const int i = j - line * m;
-    const int base = line * LS;
-    const int k = (p == 1) ? 0 : i - (int)__umulhi((unsigned)i, pmagic) * p;
+    const int l = j % LW, b = j / LW;
+    // k = b mod p; umulhi(b, ceil(2^32 / p)) = b / p exactly for b * p < 2^32
+    const int k = (p == 1) ? 0 : b - (int)__umulhi((unsigned)b, pmagic) * p;
+    const float2* s = src + b * PS + l;
     float2 v[R];
 #pragma unroll
-    for (int q = 0; q < R; ++q) v[q] = src[px(base + i + q * m)];
+    for (int q = 0; q < R; ++q) v[q] = s[q * m * PS];
     if (k) {
       const float2* tk = stw + k * (R - 1);  // the stage's twiddles w^(q k n / (p R)), q = 1..R-1
 #pragma unroll
       for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tk[q - 1]);
     }
     dft<R>(v);
-    const int o = base + (i - k) * R + k;
+    float2* d = dst + ((b - k) * R + k) * PS + l;
 #pragma unroll
-    for (int q = 0; q < R; ++q) dst[px(o + q * p)] = v[q];
+    for (int q = 0; q < R; ++q) d[q * p * PS] = v[q];
   }
   __syncthreads();
 }
 
 // `stw` is the axis' stage-twiddle table staged in shared memory; the stage
 // with span p starts at entry p - 1 (the earlier stages hold p - 1 entries).
-SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPlan& P, const float2* stw) {
+template <int LW, int PS>
+SVIE_DEV float2* run_tile_fft(float2* a, float2* b, const AxisPlan& P, const float2* stw) {
   int p = 1;
   for (int st = 0; st < P.nst; ++st) {
     const int R = (int)((P.radices >> (4 * st)) & 15ULL);
-    // ceil(2^32 / p): exact i / p = umulhi(i, mg) for i * p < 2^32
     const unsigned int mg = p > 1 ? 0xFFFFFFFFu / (unsigned)p + 1u : 0u;
     const float2* sw = stw + (p - 1);
     switch (R) {
-      case 8: fft_stage<8>(a, b, LS, P.n, nlines, p, mg, sw); break;
-      case 7: fft_stage<7>(a, b, LS, P.n, nlines, p, mg, sw); break;
-      case 6: fft_stage<6>(a, b, LS, P.n, nlines, p, mg, sw); break;
-      case 5: fft_stage<5>(a, b, LS, P.n, nlines, p, mg, sw); break;
-      case 4: fft_stage<4>(a, b, LS, P.n, nlines, p, mg, sw); break;
-      case 3: fft_stage<3>(a, b, LS, P.n, nlines, p, mg, sw); break;
-      default: fft_stage<2>(a, b, LS, P.n, nlines, p, mg, sw); break;
+      case 8: tile_stage<8, LW, PS>(a, b, P.n, p, mg, sw); break;
+      case 7: tile_stage<7, LW, PS>(a, b, P.n, p, mg, sw); break;
+      case 6: tile_stage<6, LW, PS>(a, b, P.n, p, mg, sw); break;
+      case 5: tile_stage<5, LW, PS>(a, b, P.n, p, mg, sw); break;
+      case 4: tile_stage<4, LW, PS>(a, b, P.n, p, mg, sw); break;
+      case 3: tile_stage<3, LW, PS>(a, b, P.n, p, mg, sw); break;
+      default: tile_stage<2, LW, PS>(a, b, P.n, p, mg, sw); break;
     }
     float2* t = a; a = b; b = t;
     p *= R;
@@ -237,76 +252,81 @@ SVIE_DEV float2* run_fft(float2* a, float2* b, int LS, int nlines, const AxisPla
   return a;
 }
 
-// line stride in shared memory: odd -> conflict-free columns
-__host__ __device__ inline int line_stride(int n) { return (n & 1) ? n : n + 1; }
 __host__ __device__ inline int padded_nzh(int nz) { return ((nz / 2 + 1) + 7) & ~7; }  // 64-byte rows
-__host__ __device__ inline int smem_buffer(int W, int n) { return padded_len(W * line_stride(n)); }
-// shared memory of a tile: two line buffers and the stage-twiddle table
-__host__ __device__ inline size_t tile_smem(int W, int n) {
-  return (2 * (size_t)smem_buffer(W, n) + (size_t)n) * sizeof(float2);
-}
+// shared memory of a tile: two buffers of n positions and the stage-twiddle table (n entries)
+__host__ __device__ inline size_t tile_smem(int PS, int n) { return (2 * (size_t)PS + 1) * (size_t)n * sizeof(float2); }
+constexpr size_t TILE_SMEM_MAX = 227 * 1024;
 
 // Copy the axis' stage twiddles (n - 1 entries) into shared memory after the buffers.
-SVIE_DEV float2* stage_twiddles_to_smem(float2* sm, int W, const AxisPlan& P) {
-  float2* stw = sm + 2 * smem_buffer(W, P.n);
+SVIE_DEV float2* stage_twiddles_to_smem(float2* sm, int PS, const AxisPlan& P) {
+  float2* stw = sm + 2 * PS * P.n;
   for (int e = threadIdx.x; e < P.n - 1; e += blockDim.x) stw[e] = __ldg(P.stw + e);
   return stw;
 }
 
 // ----------------------------------------------------------------- z passes
 // Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
-// W complex (paired) lines per CTA; the tile is one contiguous chunk.
+// A CTA takes 2 LW real lines, packed in pairs into LW complex lines (one
+// contiguous chunk of the input); a warp loads one pair, lanes along z.
 // `lineflag` (optional): lines whose flag lacks bit 0 hold no solid, so their
 // input is zero; a tile without any such line only writes zeros.
+template <int LW, int PS>
 __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ in, float2* __restrict__ out,
-                                                     AxisPlan P, long long nlines, int W, int nzp,
+                                                     AxisPlan P, long long nlines, int nzp,
                                                      const uint8_t* __restrict__ lineflag) {
   extern __shared__ float2 sm[];
-  const int n = P.n, LS = line_stride(n), nh = n / 2 + 1;
+  const int n = P.n, nh = n / 2 + 1;
   float2* sa = sm;
-  float2* sb = sm + smem_buffer(W, n);
-  const long long line0 = (long long)blockIdx.x * 2 * W;
-  const int nl = (int)min((long long)2 * W, nlines - line0);
-  const int np = (nl + 1) >> 1;
+  float2* sb = sm + PS * n;
+  const long long line0 = (long long)blockIdx.x * 2 * LW;
+  const int nl = (int)min((long long)2 * LW, nlines - line0);
   const float* src = in + line0 * n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = FFT_T / 32;
   if (lineflag) {
     const int any = __syncthreads_or(threadIdx.x < nl ? (__ldg(lineflag + line0 + threadIdx.x) & 1) : 0);
     if (!any) {
       float2* dst = out + line0 * nzp;
-      for (int l = warp; l < nl; l += FFT_T / 32)
+      for (int l = warp; l < nl; l += NW)
         for (int k = lane; k < nh; k += 32) dst[(long long)l * nzp + k] = make_float2(0.f, 0.f);
       return;
     }
   }
-  const float2* stw = stage_twiddles_to_smem(sm, W, P);
-  for (int l = warp; l < 2 * np; l += FFT_T / 32) {
-    const bool ok = l < nl && (!lineflag || (__ldg(lineflag + line0 + l) & 1));
-    float* row = reinterpret_cast<float*>(sa);
-    const float* g = src + l * n;
+  const float2* stw = stage_twiddles_to_smem(sm, PS, P);
+  for (int w = warp; w < LW; w += NW) {
+    const int l0 = 2 * w, l1 = 2 * w + 1;
+    const bool ok0 = l0 < nl && (!lineflag || (__ldg(lineflag + line0 + l0) & 1));
+    const bool ok1 = l1 < nl && (!lineflag || (__ldg(lineflag + line0 + l1) & 1));
+    const float* g0 = src + (long long)l0 * n;
+    const float* g1 = g0 + n;
     int z = lane;
-    // eight loads in flight per thread before the shared-memory stores
+    // eight positions of both lines in flight per thread before the stores
     for (; z + 7 * 32 < n; z += 8 * 32) {
-      float t[8];
+      float a[8], b[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) t[u] = ok ? __ldg(g + z + 32 * u) : 0.0f;
+      for (int u = 0; u < 8; ++u) {
+        a[u] = ok0 ? __ldg(g0 + z + 32 * u) : 0.0f;
+        b[u] = ok1 ? __ldg(g1 + z + 32 * u) : 0.0f;
+      }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) row[2 * px((l >> 1) * LS + z + 32 * u) + (l & 1)] = t[u];
+      for (int u = 0; u < 8; ++u) sa[(z + 32 * u) * PS + w] = make_float2(a[u], b[u]);
     }
-    for (; z < n; z += 32) row[2 * px((l >> 1) * LS + z) + (l & 1)] = ok ? __ldg(g + z) : 0.0f;
+    for (; z < n; z += 32)
+      sa[z * PS + w] = make_float2(ok0 ? __ldg(g0 + z) : 0.0f, ok1 ? __ldg(g1 + z) : 0.0f);
   }
   __syncthreads();
-  const float2* r = run_fft(sa, sb, LS, np, P, stw);
+  const float2* r = run_tile_fft<LW, PS>(sa, sb, P, stw);
+  // untangle the two real spectra of each pair: X1 = (C_k + conj C_{n-k}) / 2,
+  // X2 = (C_k - conj C_{n-k}) / (2 i)
   float2* dst = out + line0 * nzp;
-  for (int l = warp; l < nl; l += FFT_T / 32) {
-    const int w = l >> 1;
+  for (int w = warp; 2 * w < nl; w += NW) {
+    const bool has2 = 2 * w + 1 < nl;
+    float2* d0 = dst + (long long)(2 * w) * nzp;
     for (int k = lane; k < nh; k += 32) {
-      const float2 a = r[px(w * LS + k)];
-      const float2 b = r[px(w * LS + (k == 0 ? 0 : n - k))];
-      float2 v;
-      if ((l & 1) == 0) v = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
-      else v = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
-      dst[(long long)l * nzp + k] = v;
+      const float2 a = r[k * PS + w];
+      const float2 b = r[(k == 0 ? 0 : n - k) * PS + w];
+      d0[k] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+      if (has2) d0[nzp + k] = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
     }
   }
 }
@@ -314,16 +334,16 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ i
 // Inverse: half spectra -> real lines, out = beta + alpha * irfft_unnormalised.
 // `lineflag` (optional): only lines with bit 1 set are written (the others
 // are never read); a tile without such lines returns at once.
+template <int LW, int PS>
 __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ in, float* __restrict__ out,
-                                                     AxisPlan P, long long nlines, int W, int nzp, float alpha,
-                                                     float beta, const uint8_t* __restrict__ lineflag) {
+                                                     AxisPlan P, long long nlines, int nzp, float alpha, float beta,
+                                                     const uint8_t* __restrict__ lineflag) {
   extern __shared__ float2 sm[];
-  const int n = P.n, LS = line_stride(n);
+  const int n = P.n;
   float2* sa = sm;
-  float2* sb = sm + smem_buffer(W, n);
-  const long long line0 = (long long)blockIdx.x * 2 * W;
-  const int nl = (int)min((long long)2 * W, nlines - line0);
-  const int np = (nl + 1) >> 1;
+  float2* sb = sm + PS * n;
+  const long long line0 = (long long)blockIdx.x * 2 * LW;
+  const int nl = (int)min((long long)2 * LW, nlines - line0);
   if (lineflag) {
     const int any = __syncthreads_or(threadIdx.x < nl ? (__ldg(lineflag + line0 + threadIdx.x) & 2) : 0);
     if (!any) return;
@@ -331,19 +351,20 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
   const float2* src = in + line0 * nzp;
   const bool even = (n & 1) == 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const float2* stw = stage_twiddles_to_smem(sm, W, P);
-  for (int w = warp; w < np; w += FFT_T / 32) {
-    const bool has2 = 2 * w + 1 < nl;
+  constexpr int NW = FFT_T / 32;
+  const float2* stw = stage_twiddles_to_smem(sm, PS, P);
+  for (int w = warp; w < LW; w += NW) {
+    const bool has1 = 2 * w < nl, has2 = 2 * w + 1 < nl;
     const float2* s1 = src + (long long)(2 * w) * nzp;
     const float2* s2 = s1 + nzp;
-    // four (k, line pair) loads in flight per thread before the stores
+    // four positions of both half spectra in flight per thread before the stores
     for (int k0 = lane; k0 < n; k0 += 4 * 32) {
       float2 x1[4], x2[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int k = k0 + 32 * u;
         const int kk = k > n / 2 ? n - k : k;
-        x1[u] = k < n ? __ldg(s1 + kk) : make_float2(0.f, 0.f);
+        x1[u] = (has1 && k < n) ? __ldg(s1 + kk) : make_float2(0.f, 0.f);
         x2[u] = (has2 && k < n) ? __ldg(s2 + kk) : make_float2(0.f, 0.f);
       }
 #pragma unroll
@@ -356,31 +377,35 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
         if (kk == 0 || (even && kk == n / 2)) { a.y = 0.f; b.y = 0.f; }
         if (mirror) { a.y = -a.y; b.y = -b.y; }
         // C = X1 + i X2, stored conjugated for the inverse-by-forward transform
-        sa[px(w * LS + k)] = make_float2(a.x - b.y, -(a.y + b.x));
+        sa[k * PS + w] = make_float2(a.x - b.y, -(a.y + b.x));
       }
     }
   }
   __syncthreads();
-  const float2* r = run_fft(sa, sb, LS, np, P, stw);
+  const float2* r = run_tile_fft<LW, PS>(sa, sb, P, stw);
   float* dst = out + line0 * n;
-  for (int l = warp; l < nl; l += FFT_T / 32) {
-    if (lineflag && !(__ldg(lineflag + line0 + l) & 2)) continue;
-    const int w = l >> 1;
+  for (int w = warp; 2 * w < nl; w += NW) {
+    const int l0 = 2 * w, l1 = 2 * w + 1;
+    const bool w0 = !lineflag || (__ldg(lineflag + line0 + l0) & 2);
+    const bool w1 = l1 < nl && (!lineflag || (__ldg(lineflag + line0 + l1) & 2));
+    if (!w0 && !w1) continue;
+    float* d0 = dst + (long long)l0 * n;
     for (int z = lane; z < n; z += 32) {
-      const float2 v = r[px(w * LS + z)];
-      dst[l * n + z] = beta + alpha * ((l & 1) ? -v.y : v.x);
+      const float2 v = r[z * PS + w];
+      if (w0) d0[z] = beta + alpha * v.x;
+      if (w1) d0[n + z] = beta + alpha * (-v.y);
     }
   }
 }
 
 // ------------------------------------------------------------ strided passes
-// Lines along an axis with element stride `stride`; a CTA takes SW = 8
-// consecutive lines (one aligned 64-byte row segment of the padded spectrum)
-// of one outer slab: base = data + blockIdx.y * outer_stride + blockIdx.x * 8.
+// Lines along an axis with element stride `stride`; a CTA takes LW
+// consecutive lines (LW = 8: one aligned 64-byte row segment of the padded
+// spectrum) of one outer slab: base = data + blockIdx.y * outer_stride +
+// blockIdx.x * LW.  The tile is stored like the spectrum (position-major,
+// PS = LW), so thread t loads line t % LW of rows t / LW, + FFT_T / LW, ...
 // mode 0 = forward, 1 = inverse, 2 = forward * K^ then inverse (x axis only;
 // the outer index is y and the line index kz).
-constexpr int SW = 8;
-
 struct KGeom {
   const float* kred;  // [(nx/2+1)][(ny/2+1)][nzh]
   int ny, nzh;
@@ -391,67 +416,68 @@ struct KGeom {
 // bit 1: no N value of the slab is read afterwards).
 // MINB: CTAs per SM the register budget is sized for (the y passes fit four
 // in shared memory, the x pass three).
-template <int MINB>
+template <int LW, int MINB>
 __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict__ data, AxisPlan P, long long stride,
                                                        int ninner, long long outer_stride, int mode, KGeom K,
                                                        const uint8_t* __restrict__ slabflag, int need) {
   if (slabflag && !(__ldg(slabflag + blockIdx.y) & need)) return;
   extern __shared__ float2 sm[];
-  const int n = P.n, LS = line_stride(n);
+  constexpr int KS = FFT_T / LW;  // rows per sweep of the CTA
+  const int n = P.n;
   float2* sa = sm;
-  float2* sb = sm + smem_buffer(SW, n);
-  const int c0 = blockIdx.x * SW;
-  const int nl = min(SW, ninner - c0);
+  float2* sb = sm + LW * n;
+  const int c0 = blockIdx.x * LW;
+  const int nl = min(LW, ninner - c0);
   float2* base = data + (long long)blockIdx.y * outer_stride + c0;
-  const float2* stw = stage_twiddles_to_smem(sm, SW, P);
-  // each thread owns column c = tid & 7 and rows k = tid >> 3, + 32, ...
-  const int c = threadIdx.x & 7, k0 = threadIdx.x >> 3;
+  const float2* stw = stage_twiddles_to_smem(sm, LW, P);
+  const int c = threadIdx.x % LW, k0 = threadIdx.x / LW;
   const bool col = c < nl;
-  const long long rstep = 32 * stride;
-  if (col) {
+  const long long rstep = KS * stride;
+  {
     const float2* g = base + (long long)k0 * stride + c;
     int k = k0;
-    // eight loads in flight per thread before the shared-memory stores
-    for (; k + 7 * 32 < n; k += 8 * 32, g += 8 * rstep) {
+    // eight loads in flight per thread before the shared-memory stores; the
+    // lines past the slab's end are zero
+    for (; k + 7 * KS < n; k += 8 * KS, g += 8 * rstep) {
       float2 v[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = g[u * rstep];
+      for (int u = 0; u < 8; ++u) v[u] = col ? g[u * rstep] : make_float2(0.f, 0.f);
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         if (mode == 1) v[u].y = -v[u].y;
-        sa[px(c * LS + k + 32 * u)] = v[u];
+        sa[(k + KS * u) * LW + c] = v[u];
       }
     }
-    for (; k < n; k += 32, g += rstep) {
-      float2 v = *g;
+    for (; k < n; k += KS, g += rstep) {
+      float2 v = col ? *g : make_float2(0.f, 0.f);
       if (mode == 1) v.y = -v.y;
-      sa[px(c * LS + k)] = v;
+      sa[k * LW + c] = v;
     }
   }
   __syncthreads();
-  float2* r = run_fft(sa, sb, LS, nl, P, stw);
+  float2* r = run_tile_fft<LW, LW>(sa, sb, P, stw);
   if (mode == 2) {
     const int nyh = K.ny / 2 + 1;
     const int y = blockIdx.y, yr = min(y, K.ny - y);
     if (col) {
       const float* krow = K.kred + (long long)yr * K.nzh + c0 + c;
       const long long kst = (long long)nyh * K.nzh;
-      for (int k = k0; k < n; k += 32) {
+      for (int k = k0; k < n; k += KS) {
         const int kr = min(k, n - k);
         const float kv = __ldg(krow + kr * kst);
-        const float2 v = r[px(c * LS + k)];
-        r[px(c * LS + k)] = make_float2(v.x * kv, -(v.y * kv));  // conj for the inverse
+        const float2 v = r[k * LW + c];
+        r[k * LW + c] = make_float2(v.x * kv, -(v.y * kv));  // conj for the inverse
       }
     }
     __syncthreads();
     float2* other = (r == sa) ? sb : sa;
-    r = run_fft(r, other, LS, nl, P, stw);
+    r = run_tile_fft<LW, LW>(r, other, P, stw);
   }
   if (col) {
     const bool conj_out = (mode != 0);
     float2* g = base + (long long)k0 * stride + c;
-    for (int k = k0; k < n; k += 32, g += rstep) {
-      float2 v = r[px(c * LS + k)];
+    for (int k = k0; k < n; k += KS, g += rstep) {
+      float2 v = r[k * LW + c];
       if (conj_out) v.y = -v.y;
       *g = v;
     }
@@ -662,13 +688,11 @@ static PlanLayout plan_layout(int nx, int ny, int nz) {
   return L;
 }
 
-// Complex lines per CTA of the z passes: the two shared buffers of W lines and
-// the twiddle table stay under 55 KB, so four CTAs fit on an SM.
-static int z_width(int n) {
-  int w = 16;
-  while (w > 1 && tile_smem(w, n) > 55 * 1024) --w;
-  return w;
-}
+// Tile shapes: z passes 16 complex lines (PS = 17) and strided passes 8 lines
+// when the two buffers and the twiddles fit in shared memory, else one line
+// per tile (axes longer than about 830 for z and 1700 for x and y).
+static bool z_wide(int n) { return tile_smem(17, n) <= TILE_SMEM_MAX; }
+static bool strided_wide(int n) { return tile_smem(8, n) <= TILE_SMEM_MAX; }
 
 static int ensure_smem_attr() {
   static unsigned long long done = 0;
@@ -676,11 +700,14 @@ static int ensure_smem_attr() {
   if (cudaGetDevice(&dev) != cudaSuccess) return SVIE_ERR_LAUNCH;
   if (dev < 64 && (done >> dev) & 1ULL) return SVIE_OK;
   const int bytes = 227 * 1024;
-  cudaError_t e1 = cudaFuncSetAttribute(k_fft_z_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaError_t e2 = cudaFuncSetAttribute(k_fft_z_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaError_t e3 = cudaFuncSetAttribute(k_fft_strided<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e3 == cudaSuccess) e3 = cudaFuncSetAttribute(k_fft_strided<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+  const void* fns[] = {(const void*)k_fft_z_r2c<16, 17>, (const void*)k_fft_z_r2c<1, 1>,
+                       (const void*)k_fft_z_c2r<16, 17>, (const void*)k_fft_z_c2r<1, 1>,
+                       (const void*)k_fft_strided<8, 4>,  (const void*)k_fft_strided<8, 3>,
+                       (const void*)k_fft_strided<1, 1>};
+  cudaError_t e1 = cudaSuccess;
+  for (const void* f : fns)
+    if (e1 == cudaSuccess) e1 = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e1 != cudaSuccess) {
     set_error("fft: cudaFuncSetAttribute failed");
     return SVIE_ERR_LAUNCH;
   }
@@ -717,30 +744,50 @@ static int make_plans(const void* plan, int nx, int ny, int nz, Plans* P) {
 static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, float2* spec, float* out, bool fwd,
                      float alpha, float beta, cudaStream_t s, const uint8_t* lineflag = nullptr) {
   const long long nlines = (long long)nx * ny;
-  const int W = z_width(nz), nzp = padded_nzh(nz);
-  const size_t smem = tile_smem(W, nz);
-  const long long nb = (nlines + 2 * W - 1) / (2 * W);
-  if (fwd) k_fft_z_r2c<<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, W, nzp, lineflag);
-  else k_fft_z_c2r<<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, W, nzp, alpha, beta, lineflag);
+  const int nzp = padded_nzh(nz);
+  if (z_wide(nz)) {
+    const size_t smem = tile_smem(17, nz);
+    const long long nb = (nlines + 31) / 32;
+    if (fwd) k_fft_z_r2c<16, 17><<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, nzp, lineflag);
+    else k_fft_z_c2r<16, 17><<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, nzp, alpha, beta, lineflag);
+  } else {
+    const size_t smem = tile_smem(1, nz);
+    const long long nb = (nlines + 1) / 2;
+    if (fwd) k_fft_z_r2c<1, 1><<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, nzp, lineflag);
+    else k_fft_z_c2r<1, 1><<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, nzp, alpha, beta, lineflag);
+  }
 }
 
 // y lines: outer index x, line index kz, element stride nzp.
 static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s,
                      const uint8_t* slabflag = nullptr) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
-  const size_t smem = tile_smem(SW, ny);
-  dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)nx);
-  k_fft_strided<4><<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, KGeom{nullptr, ny, nzh},
-                                       slabflag, mode == 1 ? 2 : 1);
+  const KGeom K{nullptr, ny, nzh};
+  const int need = mode == 1 ? 2 : 1;
+  if (strided_wide(ny)) {
+    dim3 g((unsigned)((nzh + 7) / 8), (unsigned)nx);
+    k_fft_strided<8, 4><<<g, FFT_T, tile_smem(8, ny), s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, K,
+                                                          slabflag, need);
+  } else {
+    dim3 g((unsigned)nzh, (unsigned)nx);
+    k_fft_strided<1, 1><<<g, FFT_T, tile_smem(1, ny), s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, K,
+                                                          slabflag, need);
+  }
 }
 
 // x lines: outer index y, line index kz, element stride ny * nzp.
 static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
-  const size_t smem = tile_smem(SW, nx);
-  dim3 g((unsigned)((nzh + SW - 1) / SW), (unsigned)ny);
-  k_fft_strided<3><<<g, FFT_T, smem, s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, KGeom{P.kred, ny, nzh},
-                                       nullptr, 0);
+  const KGeom K{P.kred, ny, nzh};
+  if (strided_wide(nx)) {
+    dim3 g((unsigned)((nzh + 7) / 8), (unsigned)ny);
+    k_fft_strided<8, 3><<<g, FFT_T, tile_smem(8, nx), s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, K,
+                                                          nullptr, 0);
+  } else {
+    dim3 g((unsigned)nzh, (unsigned)ny);
+    k_fft_strided<1, 1><<<g, FFT_T, tile_smem(1, nx), s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, K,
+                                                          nullptr, 0);
+  }
 }
 
 static void gauss_legendre(int n, double* x, double* w) {

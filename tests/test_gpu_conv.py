@@ -108,7 +108,7 @@ def test_convolution_vs_oracle_float64():
     kern = np.zeros(g.shape)
     ii = np.arange(-m, m + 1)
     kern[(ii % g.shape[0])[:, None, None], (ii % g.shape[1])[None, :, None], (ii % g.shape[2])[None, None, :]] = w
-    g64 = np.fft.irfftn(np.fft.rfftn(f.astype(np.float64)) * np.fft.rfftn(kern), s=g.shape) * h ** 3
+    g64 = np.fft.irfftn(np.fft.rfftn(f.astype(np.float64)) * np.fft.rfftn(kern), s=g.shape, axes=(0, 1, 2)) * h ** 3
     N64 = 1 - g64 / (4 / 3 * np.pi * r ** 3)
     conv = S.BallConvolution(g, r)
     N = conv.exterior_fraction(torch.from_numpy(f).cuda()).cpu().numpy()
