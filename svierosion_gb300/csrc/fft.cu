@@ -35,6 +35,8 @@ struct AxisPlan {
   unsigned long long radices;  // radix of stage s in bits [4s, 4s+4) (no arrays: no local-memory copy)
   const float2* tw;            // tw[k] = exp(-2 pi i k / n), k < n
   const float2* stw;           // per-stage twiddles: stage with span p at p - 1 + k (R - 1) + q - 1 (n - 1 entries)
+  unsigned long long rradices; // the radices in reverse order (the inverse of the fused x pass)
+  const float2* rstw;          // stage twiddles of the reverse order (x axis only)
 };
 
 // Radix order: the largest odd radix first, then the even radices
@@ -60,11 +62,16 @@ static bool factor_axis(int n, AxisPlan* p) {
     if (!(fac[i] & 1)) order[st++] = fac[i];
   for (int i = 0; i < cnt; ++i)
     if ((fac[i] & 1) && i != first_odd) order[st++] = fac[i];
-  unsigned long long packed = 0;
-  for (int i = 0; i < st; ++i) packed |= (unsigned long long)order[i] << (4 * i);
+  unsigned long long packed = 0, rpacked = 0;
+  for (int i = 0; i < st; ++i) {
+    packed |= (unsigned long long)order[i] << (4 * i);
+    rpacked |= (unsigned long long)order[st - 1 - i] << (4 * i);
+  }
   p->n = n;
   p->nst = st;
   p->radices = packed;
+  p->rradices = rpacked;
+  p->rstw = nullptr;
   return true;
 }
 
@@ -202,12 +209,12 @@ SVIE_DEV void dft<6>(float2* x) {
 //    wavefronts);
 //  - LW = 1 (PS = 1): one line per tile, for axes too long for the others.
 // Each stage is one Stockham radix-R pass from src to dst (ping-pong).
-template <int R, int LW, int PS>
+template <int R, int LW, int PS, int NT = FFT_T>
 SVIE_DEV void tile_stage(const float2* __restrict__ src, float2* __restrict__ dst, int n, int p, unsigned int pmagic,
-                         const float2* __restrict__ stw) {
+                         const float2* __restrict__ stw, bool conj_in) {
   const int m = n / R;
   const int total = LW * m;
-  for (int j = threadIdx.x; j < total; j += FFT_T) {
+  for (int j = threadIdx.x; j < total; j += NT) {
     const int l = j % LW, b = j / LW;
     // k = b mod p; umulhi(b, ceil(2^32 / p)) = b / p exactly for b * p < 2^32
     const int k = (p == 1) ? 0 : b - (int)__umulhi((unsigned)b, pmagic) * p;
@@ -215,6 +222,10 @@ SVIE_DEV void tile_stage(const float2* __restrict__ src, float2* __restrict__ ds
     float2 v[R];
 #pragma unroll
     for (int q = 0; q < R; ++q) v[q] = s[q * m * PS];
+    if (conj_in) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[q].y = -v[q].y;
+    }
     if (k) {
       const float2* tk = stw + k * (R - 1);  // the stage's twiddles w^(q k n / (p R)), q = 1..R-1
 #pragma unroll
@@ -228,29 +239,131 @@ SVIE_DEV void tile_stage(const float2* __restrict__ src, float2* __restrict__ ds
   __syncthreads();
 }
 
-// `stw` is the axis' stage-twiddle table staged in shared memory; the stage
-// with span p starts at entry p - 1 (the earlier stages hold p - 1 entries).
-template <int LW, int PS>
-SVIE_DEV float2* run_tile_fft(float2* a, float2* b, const AxisPlan& P, const float2* stw) {
-  int p = 1;
-  for (int st = 0; st < P.nst; ++st) {
-    const int R = (int)((P.radices >> (4 * st)) & 15ULL);
+SVIE_DEV int radix_of(unsigned long long rad, int st) { return (int)((rad >> (4 * st)) & 15ULL); }
+
+// Stages [s0, s1) of the radix sequence `rad` (4 bits per stage) from a to b
+// and back; p is the span before stage s0 and is advanced past s1.  Returns
+// the buffer holding the result.  `stw` is the stage-twiddle table of that
+// sequence staged in shared memory; the stage with span p starts at entry
+// p - 1 (the earlier stages hold p - 1 entries).  conj_first: stage s0 reads
+// conj(a) (inverse transforms as conj(FFT(conj(x)))).
+template <int LW, int PS, int NT>
+SVIE_DEV float2* run_stages(float2* a, float2* b, int n, unsigned long long rad, int s0, int s1, const float2* stw,
+                            bool conj_first, int& p) {
+  for (int st = s0; st < s1; ++st) {
+    const int R = radix_of(rad, st);
     const unsigned int mg = p > 1 ? 0xFFFFFFFFu / (unsigned)p + 1u : 0u;
     const float2* sw = stw + (p - 1);
+    const bool cj = conj_first && st == s0;
     switch (R) {
-      case 8: tile_stage<8, LW, PS>(a, b, P.n, p, mg, sw); break;
-      case 7: tile_stage<7, LW, PS>(a, b, P.n, p, mg, sw); break;
-      case 6: tile_stage<6, LW, PS>(a, b, P.n, p, mg, sw); break;
-      case 5: tile_stage<5, LW, PS>(a, b, P.n, p, mg, sw); break;
-      case 4: tile_stage<4, LW, PS>(a, b, P.n, p, mg, sw); break;
-      case 3: tile_stage<3, LW, PS>(a, b, P.n, p, mg, sw); break;
-      default: tile_stage<2, LW, PS>(a, b, P.n, p, mg, sw); break;
+      case 8: tile_stage<8, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
+      case 7: tile_stage<7, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
+      case 6: tile_stage<6, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
+      case 5: tile_stage<5, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
+      case 4: tile_stage<4, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
+      case 3: tile_stage<3, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
+      default: tile_stage<2, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
     }
     float2* t = a; a = b; b = t;
     p *= R;
   }
   return a;
 }
+
+template <int LW, int PS, int NT = FFT_T>
+SVIE_DEV float2* run_tile_fft(float2* a, float2* b, const AxisPlan& P, const float2* stw, bool conj_first = false) {
+  int p = 1;
+  return run_stages<LW, PS, NT>(a, b, P.n, P.radices, 0, P.nst, stw, conj_first, p);
+}
+
+// The last stage of a transform (span p = m = n / R, so k = b): butterfly
+// (line l, column b) reads and writes the positions b + q m of line l, and its
+// outputs go to epi.apply(v, b, l, m) instead of back to shared memory.
+template <int R, int LW, int PS, int NT, class Epi>
+SVIE_DEV void last_stage(const float2* __restrict__ src, int n, const float2* __restrict__ stw, bool conj_in,
+                         const Epi& epi) {
+  const int m = n / R;
+  const int total = LW * m;
+  for (int j = threadIdx.x; j < total; j += NT) {
+    const int l = j % LW, b = j / LW;
+    const float2* s = src + b * PS + l;
+    float2 v[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = s[q * m * PS];
+    if (conj_in) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[q].y = -v[q].y;
+    }
+    if (b) {
+      const float2* tk = stw + (m - 1) + b * (R - 1);
+#pragma unroll
+      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tk[q - 1]);
+    }
+    dft<R>(v);
+    epi.template apply<R>(v, b, l, m);
+  }
+}
+
+template <int LW, int PS, int NT, class Epi>
+SVIE_DEV void run_last(const float2* src, int n, int R, const float2* stw, bool conj_in, const Epi& epi) {
+  const float2* sw = stw;
+  switch (R) {
+    case 8: last_stage<8, LW, PS, NT>(src, n, sw, conj_in, epi); break;
+    case 7: last_stage<7, LW, PS, NT>(src, n, sw, conj_in, epi); break;
+    case 6: last_stage<6, LW, PS, NT>(src, n, sw, conj_in, epi); break;
+    case 5: last_stage<5, LW, PS, NT>(src, n, sw, conj_in, epi); break;
+    case 4: last_stage<4, LW, PS, NT>(src, n, sw, conj_in, epi); break;
+    case 3: last_stage<3, LW, PS, NT>(src, n, sw, conj_in, epi); break;
+    default: last_stage<2, LW, PS, NT>(src, n, sw, conj_in, epi); break;
+  }
+}
+
+// Epilogue: store line l's outputs at base + l + position * stride (lines
+// l < nl only), conjugated for inverse transforms.
+struct StoreEpi {
+  float2* base;
+  long long stride;
+  int nl;
+  bool conj;
+  template <int R>
+  SVIE_DEV void apply(float2 (&v)[R], int b, int l, int m) const {
+    if (l >= nl) return;
+    float2* g = base + l + (long long)b * stride;
+    const long long ms = (long long)m * stride;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      float2 w = v[q];
+      if (conj) w.y = -w.y;
+      g[q * ms] = w;
+    }
+  }
+};
+
+// Epilogue of the x pass: multiply the forward outputs by K^ (real, even in
+// kx) and conjugate, then run the first stage of the inverse, whose radix
+// order is the forward's reversed: its first radix is this stage's R and it
+// reads exactly the positions b + q m this butterfly holds (span 1, no
+// twiddles); the results go to dst at positions b R + q.
+template <int PS>
+struct KEpi {
+  float2* dst;
+  const float* krow;  // K^ row of this slab and column block: + l + kr * kst
+  long long kst;
+  int n, nl;
+  template <int R>
+  SVIE_DEV void apply(float2 (&v)[R], int b, int l, int m) const {
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+      const int pos = b + q * m, kr = min(pos, n - pos);
+      const float kv = l < nl ? __ldg(krow + l + kr * kst) : 0.0f;
+      v[q] = make_float2(v[q].x * kv, -(v[q].y * kv));
+    }
+    dft<R>(v);
+    float2* d = dst + b * R * PS + l;
+#pragma unroll
+    for (int q = 0; q < R; ++q) d[q * PS] = v[q];
+  }
+};
 
 __host__ __device__ inline int padded_nzh(int nz) { return ((nz / 2 + 1) + 7) & ~7; }  // 64-byte rows
 // shared memory of a tile: two buffers of n positions and the stage-twiddle table (n entries)
@@ -430,6 +543,8 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
   const int nl = min(LW, ninner - c0);
   float2* base = data + (long long)blockIdx.y * outer_stride + c0;
   const float2* stw = stage_twiddles_to_smem(sm, LW, P);
+  if (mode == 2)
+    for (int e = threadIdx.x; e < n - 1; e += FFT_T) sm[2 * LW * n + n + e] = __ldg(P.rstw + e);
   const int c = threadIdx.x % LW, k0 = threadIdx.x / LW;
   const bool col = c < nl;
   const long long rstep = KS * stride;
@@ -455,33 +570,105 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
     }
   }
   __syncthreads();
-  float2* r = run_tile_fft<LW, LW>(sa, sb, P, stw);
-  if (mode == 2) {
-    const int nyh = K.ny / 2 + 1;
-    const int y = blockIdx.y, yr = min(y, K.ny - y);
+  const int nst = P.nst;
+  int p = 1;
+  float2* r = run_stages<LW, LW, FFT_T>(sa, sb, n, P.radices, 0, nst - 1, stw, false, p);
+  const int Rl = radix_of(P.radices, nst - 1);
+  if (mode != 2) {
+    run_last<LW, LW, FFT_T>(r, n, Rl, stw, false, StoreEpi{base, stride, nl, mode != 0});
+    return;
+  }
+  // forward, then K^ and the first inverse stage in one pass, then the rest
+  // of the inverse in reverse radix order (its twiddles follow the forward's)
+  const float2* rstw = stw + n;
+  const int nyh = K.ny / 2 + 1;
+  const int y = blockIdx.y, yr = min(y, K.ny - y);
+  float2* o = (r == sa) ? sb : sa;
+  run_last<LW, LW, FFT_T>(r, n, Rl, stw, false,
+                          KEpi<LW>{o, K.kred + (long long)yr * K.nzh + c0, (long long)nyh * K.nzh, n, nl});
+  __syncthreads();
+  if (nst == 1) {  // that stage was the whole transform both ways
     if (col) {
-      const float* krow = K.kred + (long long)yr * K.nzh + c0 + c;
-      const long long kst = (long long)nyh * K.nzh;
-      for (int k = k0; k < n; k += KS) {
-        const int kr = min(k, n - k);
-        const float kv = __ldg(krow + kr * kst);
-        const float2 v = r[k * LW + c];
-        r[k * LW + c] = make_float2(v.x * kv, -(v.y * kv));  // conj for the inverse
+      float2* g = base + (long long)k0 * stride + c;
+      for (int k = k0; k < n; k += KS, g += rstep) {
+        const float2 v = o[k * LW + c];
+        *g = make_float2(v.x, -v.y);
       }
     }
-    __syncthreads();
-    float2* other = (r == sa) ? sb : sa;
-    r = run_tile_fft<LW, LW>(r, other, P, stw);
+    return;
   }
-  if (col) {
-    const bool conj_out = (mode != 0);
-    float2* g = base + (long long)k0 * stride + c;
-    for (int k = k0; k < n; k += KS, g += rstep) {
-      float2 v = r[k * LW + c];
-      if (conj_out) v.y = -v.y;
-      *g = v;
+  int p2 = Rl;
+  float2* r2 = run_stages<LW, LW, FFT_T>(o, r, n, P.rradices, 1, nst - 1, rstw, false, p2);
+  run_last<LW, LW, FFT_T>(r2, n, radix_of(P.rradices, nst - 1), rstw, false, StoreEpi{base, stride, nl, true});
+}
+
+// 16-byte asynchronous global -> shared copies (L2 only), completed by groups.
+SVIE_DEV void cp_async16(void* smem, const void* gmem) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+SVIE_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+SVIE_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Persistent form of the 8-line strided pass: each CTA walks the tiles
+// t = blockIdx.x, + gridDim.x, ... (tile t: column block t % ncb of outer slab
+// t / ncb) and copies the next tile into a third shared buffer with cp.async
+// while it transforms the current one, so the loads of one tile overlap the
+// butterflies of the previous.  The copies take whole 64-byte row segments:
+// the spectrum rows are padded to multiples of 8 complex values (the columns
+// past ninner are copied and transformed but never stored).  Modes 0 and 1
+// and the slab skipping of k_fft_strided (the y passes).
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_fft_tiles(float2* __restrict__ data, AxisPlan P, long long stride,
+                                                     int ninner, long long outer_stride, int nouter, int mode,
+                                                     const uint8_t* __restrict__ slabflag, int need) {
+  constexpr int LW = 8;
+  extern __shared__ __align__(16) float2 sm[];
+  const int n = P.n, tile = LW * n;
+  const int ncb = (ninner + LW - 1) / LW;
+  const long long ntiles = (long long)ncb * nouter;
+  float2* stw = sm + 3 * tile;
+  for (int e = threadIdx.x; e < n - 1; e += NT) stw[e] = __ldg(P.stw + e);
+  auto next = [&](long long t) {
+    if (slabflag)
+      while (t < ntiles && !(__ldg(slabflag + t / ncb) & need)) t += gridDim.x;
+    return t;
+  };
+  auto issue = [&](long long t, float2* dst) {
+    const long long outer = t / ncb;
+    const float2* src = data + outer * outer_stride + (t - outer * ncb) * LW;
+    for (int e = threadIdx.x; e < 4 * n; e += NT) {
+      const int row = e >> 2, part = 2 * (e & 3);
+      cp_async16(dst + row * LW + part, src + row * stride + part);
     }
+  };
+  float2* bi = sm;         // the tile being transformed
+  float2* bq = sm + tile;  // its ping-pong partner
+  float2* bf = sm + 2 * tile;  // the next tile, in flight
+  long long t = next(blockIdx.x);
+  if (t < ntiles) issue(t, bi);
+  cp_async_commit();
+  while (t < ntiles) {
+    const long long tn = next(t + gridDim.x);
+    if (tn < ntiles) issue(tn, bf);
+    cp_async_commit();
+    cp_async_wait<1>();  // every group but the newest (the prefetch) has landed
+    __syncthreads();
+    int p = 1;
+    const float2* r = run_stages<LW, LW, NT>(bi, bq, n, P.radices, 0, P.nst - 1, stw, mode == 1, p);
+    const long long outer = t / ncb;
+    const int c0 = (int)(t - outer * ncb) * LW;
+    run_last<LW, LW, NT>(r, n, radix_of(P.radices, P.nst - 1), stw, mode == 1 && P.nst == 1,
+                         StoreEpi{data + outer * outer_stride + c0, stride, min(LW, ninner - c0), mode == 1});
+    __syncthreads();  // bi and bq are free: the next tile is bf, the one after goes to bq
+    float2* tmp = bi;
+    bi = bf;
+    bf = bq;
+    bq = tmp;
+    t = tn;
   }
+  cp_async_wait<0>();
 }
 
 // ------------------------------------------------------ plan construction
@@ -671,7 +858,7 @@ __global__ void k_khat_expand(const float* __restrict__ K, int nx, int ny, int n
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 struct PlanLayout {
-  size_t tw_x, tw_y, tw_z, stw_x, stw_y, stw_z, kred, total;
+  size_t tw_x, tw_y, tw_z, stw_x, stw_y, stw_z, rstw_x, kred, total;
 };
 
 static PlanLayout plan_layout(int nx, int ny, int nz) {
@@ -683,6 +870,7 @@ static PlanLayout plan_layout(int nx, int ny, int nz) {
   L.stw_x = off; off += align256((size_t)nx * sizeof(float2));
   L.stw_y = off; off += align256((size_t)ny * sizeof(float2));
   L.stw_z = off; off += align256((size_t)nz * sizeof(float2));
+  L.rstw_x = off; off += align256((size_t)nx * sizeof(float2));
   L.kred = off; off += align256((size_t)(nx / 2 + 1) * (ny / 2 + 1) * (nz / 2 + 1) * sizeof(float));
   L.total = off;
   return L;
@@ -692,7 +880,22 @@ static PlanLayout plan_layout(int nx, int ny, int nz) {
 // when the two buffers and the twiddles fit in shared memory, else one line
 // per tile (axes longer than about 830 for z and 1700 for x and y).
 static bool z_wide(int n) { return tile_smem(17, n) <= TILE_SMEM_MAX; }
-static bool strided_wide(int n) { return tile_smem(8, n) <= TILE_SMEM_MAX; }
+// the strided passes also hold the reverse-order twiddles of the fused x pass
+static size_t strided_smem(int lw, int n) { return tile_smem(lw, n) + (size_t)n * sizeof(float2); }
+static bool strided_wide(int n) { return strided_smem(8, n) <= TILE_SMEM_MAX; }
+// the persistent 8-line pass holds three tiles and the twiddles
+static size_t tiles_smem(int n) { return (3 * 8 + 1) * (size_t)n * sizeof(float2); }
+static bool strided_tiles(int n) { return tiles_smem(n) <= TILE_SMEM_MAX; }
+
+// Grid of a persistent kernel: as many CTAs as are resident at once, at most one per tile.
+static unsigned persistent_grid(const void* fn, int threads, size_t smem, long long ntiles) {
+  int dev = 0, nsm = 1, per = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem) != cudaSuccess || per < 1) per = 1;
+  const long long g = (long long)per * nsm;
+  return (unsigned)(ntiles < g ? ntiles : g);
+}
 
 static int ensure_smem_attr() {
   static unsigned long long done = 0;
@@ -703,7 +906,7 @@ static int ensure_smem_attr() {
   const void* fns[] = {(const void*)k_fft_z_r2c<16, 17>, (const void*)k_fft_z_r2c<1, 1>,
                        (const void*)k_fft_z_c2r<16, 17>, (const void*)k_fft_z_c2r<1, 1>,
                        (const void*)k_fft_strided<8, 4>,  (const void*)k_fft_strided<8, 3>,
-                       (const void*)k_fft_strided<1, 1>};
+                       (const void*)k_fft_strided<1, 1>,  (const void*)k_fft_tiles<256, 3>};
   cudaError_t e1 = cudaSuccess;
   for (const void* f : fns)
     if (e1 == cudaSuccess) e1 = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -737,6 +940,7 @@ static int make_plans(const void* plan, int nx, int ny, int nz, Plans* P) {
   P->x.stw = (const float2*)(b + L.stw_x);
   P->y.stw = (const float2*)(b + L.stw_y);
   P->z.stw = (const float2*)(b + L.stw_z);
+  P->x.rstw = (const float2*)(b + L.rstw_x);
   P->kred = (const float*)(b + L.kred);
   return SVIE_OK;
 }
@@ -764,14 +968,18 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const KGeom K{nullptr, ny, nzh};
   const int need = mode == 1 ? 2 : 1;
-  if (strided_wide(ny)) {
+  const long long ostr = (long long)ny * nzp;
+  if (strided_tiles(ny)) {
+    const size_t smem = tiles_smem(ny);
+    const long long ntiles = (long long)((nzh + 7) / 8) * nx;
+    k_fft_tiles<256, 3><<<persistent_grid((const void*)k_fft_tiles<256, 3>, 256, smem, ntiles), 256, smem, s>>>(
+        spec, P.y, nzp, nzh, ostr, nx, mode, slabflag, need);
+  } else if (strided_wide(ny)) {
     dim3 g((unsigned)((nzh + 7) / 8), (unsigned)nx);
-    k_fft_strided<8, 4><<<g, FFT_T, tile_smem(8, ny), s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, K,
-                                                          slabflag, need);
+    k_fft_strided<8, 4><<<g, FFT_T, strided_smem(8, ny), s>>>(spec, P.y, nzp, nzh, ostr, mode, K, slabflag, need);
   } else {
     dim3 g((unsigned)nzh, (unsigned)nx);
-    k_fft_strided<1, 1><<<g, FFT_T, tile_smem(1, ny), s>>>(spec, P.y, nzp, nzh, (long long)ny * nzp, mode, K,
-                                                          slabflag, need);
+    k_fft_strided<1, 1><<<g, FFT_T, strided_smem(1, ny), s>>>(spec, P.y, nzp, nzh, ostr, mode, K, slabflag, need);
   }
 }
 
@@ -779,14 +987,13 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
 static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const KGeom K{P.kred, ny, nzh};
+  const long long lstr = (long long)ny * nzp;
   if (strided_wide(nx)) {
     dim3 g((unsigned)((nzh + 7) / 8), (unsigned)ny);
-    k_fft_strided<8, 3><<<g, FFT_T, tile_smem(8, nx), s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, K,
-                                                          nullptr, 0);
+    k_fft_strided<8, 3><<<g, FFT_T, strided_smem(8, nx), s>>>(spec, P.x, lstr, nzh, nzp, mode, K, nullptr, 0);
   } else {
     dim3 g((unsigned)nzh, (unsigned)ny);
-    k_fft_strided<1, 1><<<g, FFT_T, tile_smem(1, nx), s>>>(spec, P.x, (long long)ny * nzp, nzh, nzp, mode, K,
-                                                          nullptr, 0);
+    k_fft_strided<1, 1><<<g, FFT_T, strided_smem(1, nx), s>>>(spec, P.x, lstr, nzh, nzp, mode, K, nullptr, 0);
   }
 }
 
@@ -880,6 +1087,9 @@ int svie_conv_plan_init(void* plan, int nx, int ny, int nz, const double* w, int
   k_stage_twiddles<<<blocks_for(nx, 256), 256, 0, s>>>(P.x, (float2*)(b + L.stw_x));
   k_stage_twiddles<<<blocks_for(ny, 256), 256, 0, s>>>(P.y, (float2*)(b + L.stw_y));
   k_stage_twiddles<<<blocks_for(nz, 256), 256, 0, s>>>(P.z, (float2*)(b + L.stw_z));
+  AxisPlan xr = P.x;  // the x axis in reverse radix order: the inverse half of the fused x pass
+  xr.radices = P.x.rradices;
+  k_stage_twiddles<<<blocks_for(nx, 256), 256, 0, s>>>(xr, (float2*)(b + L.rstw_x));
   const int side = 2 * m + 1, nzh = nz / 2 + 1, nyh = ny / 2 + 1, nxh = nx / 2 + 1;
   double* A = (double*)ws;
   double* Bq = (double*)((char*)ws + align256((size_t)side * side * nzh * sizeof(double)));
@@ -888,7 +1098,7 @@ int svie_conv_plan_init(void* plan, int nx, int ny, int nz, const double* w, int
   k_khat_b<<<blocks_for((long long)side * nyh * nzh, TB, 4096), TB, ny * sizeof(double), s>>>(A, m, ny, nzh, Bq);
   k_khat_c<<<blocks_for((long long)nxh * nyh * nzh, TB, 8192), TB, nx * sizeof(double), s>>>(
       Bq, m, nx, ny, nzh, (float*)(b + L.kred));
-  return launch_status("svie_conv_plan_init", 9);
+  return launch_status("svie_conv_plan_init", 10);
 }
 
 int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, float* out, double alpha,
@@ -900,8 +1110,8 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
     set_error("svie_conv_apply: null input/output");
     return SVIE_ERR_ARG;
   }
-  if (!ws || ws_bytes < svie_conv_workspace_bytes(nx, ny, nz)) {
-    set_error("svie_conv_apply: workspace too small");
+  if (!ws || ws_bytes < svie_conv_workspace_bytes(nx, ny, nz) || ((uintptr_t)ws & 15)) {
+    set_error("svie_conv_apply: workspace too small or not 16-byte aligned");
     return SVIE_ERR_WORKSPACE;
   }
   if ((st = ensure_smem_attr())) return st;
@@ -925,8 +1135,8 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
     set_error("svie_conv_apply_masked: null input/output, or only one of the two flag arrays");
     return SVIE_ERR_ARG;
   }
-  if (!ws || ws_bytes < svie_conv_workspace_bytes(nx, ny, nz)) {
-    set_error("svie_conv_apply_masked: workspace too small");
+  if (!ws || ws_bytes < svie_conv_workspace_bytes(nx, ny, nz) || ((uintptr_t)ws & 15)) {
+    set_error("svie_conv_apply_masked: workspace too small or not 16-byte aligned");
     return SVIE_ERR_WORKSPACE;
   }
   if ((st = ensure_smem_attr())) return st;
@@ -980,6 +1190,10 @@ int svie_rfft3(const void* plan, int nx, int ny, int nz, const float* f, void* s
   Plans P;
   int st = make_plans(plan, nx, ny, nz, &P);
   if (st) return st;
+  if (!f || !spec || ((uintptr_t)spec & 15)) {
+    set_error("svie_rfft3: null input, or spectrum not 16-byte aligned");
+    return SVIE_ERR_ARG;
+  }
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
   launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s);
@@ -993,6 +1207,10 @@ int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out
   Plans P;
   int st = make_plans(plan, nx, ny, nz, &P);
   if (st) return st;
+  if (!spec || !out || ((uintptr_t)spec & 15)) {
+    set_error("svie_irfft3: null input, or spectrum not 16-byte aligned");
+    return SVIE_ERR_ARG;
+  }
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
   launch_x(P, nx, ny, nz, (float2*)spec, 1, s);
