@@ -22,6 +22,11 @@ constexpr int SG_THREADS = 256;
 struct StageConst {
   float h, inv_h, hx, hy, hz;  // spacing, 1/h, clamp bounds n - 3.001
   float n_cap, eps, cut_b, cut_scale;
+  float t;  // the SVI law's t, rounded to float as the reference's float32 tensors see it
+  // curvature laws: alpha, alpha - 1, alpha - 2 and delta rounded once; amode
+  // 0: alpha = 1, 1: alpha < 1, 2: alpha > 1
+  float alpha, am1, am2, delta;
+  int amode;
 };
 
 static StageConst stage_const(const svie_law& L, int nx, int ny, int nz) {
@@ -35,6 +40,12 @@ static StageConst stage_const(const svie_law& L, int nx, int ny, int nz) {
   c.eps = (float)L.eps;
   c.cut_b = (float)L.cut_b;
   c.cut_scale = (float)(1.0 / (L.cut_b - L.cut_a));
+  c.t = (float)L.t;
+  c.alpha = (float)L.alpha;
+  c.am1 = (float)(L.alpha - 1.0);
+  c.am2 = (float)(L.alpha - 2.0);
+  c.delta = (float)L.delta;
+  c.amode = L.alpha == 1.0 ? 0 : (L.alpha < 1.0 ? 1 : 2);
   return c;
 }
 
@@ -46,15 +57,15 @@ SVIE_DEV float powk(float x, int k) {
   return powf(x, (float)k);
 }
 
-// SVIPowerLaw.speed (flows.py:89-96).  t - N is formed in float64 (exact for
-// float N) and rounded once: N approaches t at edges and corners, where the
-// float32 difference would lose relative accuracy.
+// SVIPowerLaw.speed (flows.py:89-96).  t - N in float32 with t rounded to
+// float, as the reference computes it on float32 tensors (N <= n_cap < t, so
+// the difference stays well away from zero).
 SVIE_DEV float svi_speed(float N, const svie_law& L, const StageConst& C) {
   N = fminf(fmaxf(N, 0.0f), 1.0f);
   float V;
   if (L.s) {
     N = fminf(N, C.n_cap);
-    V = powk(N, L.k) / (float)(L.t - (double)N);
+    V = powk(N, L.k) / (C.t - N);
   } else {
     V = L.k ? powk(N, L.k) : 1.0f;
   }
@@ -66,7 +77,7 @@ SVIE_DEV float svi_dspeed(float N, const svie_law& L, const StageConst& C) {
   N = fminf(fmaxf(N, 1e-12f), 1.0f);
   if (L.s) {
     N = fminf(N, C.n_cap);
-    const float d = (float)(L.t - (double)N);
+    const float d = C.t - N;
     const float V = powk(N, L.k) / d;
     return V * ((float)L.k / N + 1.0f / d);
   }
@@ -75,33 +86,32 @@ SVIE_DEV float svi_dspeed(float N, const svie_law& L, const StageConst& C) {
 }
 
 // _CurvatureLaw._power / _dpower (flows.py:139-158)
-SVIE_DEV float curv_power(float x, const svie_law& L) {
-  if (L.alpha == 1.0) return x;
-  if (L.alpha < 1.0) return x * powf(x + (float)L.delta, (float)(L.alpha - 1.0));
-  return powf(x, (float)L.alpha);
+SVIE_DEV float curv_power(float x, const StageConst& C) {
+  if (C.amode == 0) return x;
+  if (C.amode == 1) return x * powf(x + C.delta, C.am1);
+  return powf(x, C.alpha);
 }
-SVIE_DEV float curv_dpower(float x, const svie_law& L) {
-  const double a = L.alpha;
-  if (a == 1.0) return 1.0f;
-  if (a < 1.0) {
-    float y = x + (float)L.delta;
-    return powf(y, (float)(a - 2.0)) * ((float)a * x + (float)L.delta);
+SVIE_DEV float curv_dpower(float x, const StageConst& C) {
+  if (C.amode == 0) return 1.0f;
+  if (C.amode == 1) {
+    float y = x + C.delta;
+    return powf(y, C.am2) * (C.alpha * x + C.delta);
   }
-  return (float)a * powf(fmaxf(x, 0.0f), (float)(a - 1.0));
+  return C.alpha * powf(fmaxf(x, 0.0f), C.am1);
 }
 
 // Speed and diffusivity of the curvature laws (flows.py:170-206).
-SVIE_DEV void curv_speed(float k1, float k2, const svie_law& L, float* V, float* D) {
+SVIE_DEV void curv_speed(float k1, float k2, const svie_law& L, const StageConst& C, float* V, float* D) {
   if (L.kind == 1) {
     float H = 0.5f * (k1 + k2);
     float Hp = fmaxf(H, 0.0f);
-    *V = curv_power(Hp, L) + (float)L.eps;
-    *D = H > 0.0f ? curv_dpower(Hp, L) : 0.0f;
+    *V = curv_power(Hp, C) + C.eps;
+    *D = H > 0.0f ? curv_dpower(Hp, C) : 0.0f;
   } else {
     float a = fmaxf(k1, 0.0f), b = fmaxf(k2, 0.0f);
     float Kc = a * b;
-    *V = curv_power(Kc, L) + (float)L.eps;
-    float dF = curv_dpower(Kc, L);
+    *V = curv_power(Kc, C) + C.eps;
+    float dF = curv_dpower(Kc, C);
     *D = Kc > 0.0f ? dF * (a + b) : dF * 0.0f;
   }
 }
@@ -131,38 +141,73 @@ SVIE_DEV void stat_init(StatAcc& s) {
   s.vs_n = s.vs_a = 0.0f;
 }
 
-// Per-CTA reduction of the statistics and one atomic / partial write per CTA.
+// Per-CTA reduction of the statistics and one atomic / partial write per CTA:
+// every quantity is reduced across its warp first, then warp 0 combines the
+// warps after a single barrier.  Maxima, minima and counts are exact in any
+// order; the two float64 partials are added in warp order.
 SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
-  __shared__ float shf[SG_THREADS / 32];
-  __shared__ double shd[SG_THREADS / 32];
-  __shared__ unsigned int shu[SG_THREADS / 32];
-  float v;
-  v = block_reduce(a.vmax, shf, OpMaxF(), 0.0f);
-  if (threadIdx.x == 0 && v > 0.0f) atomicMax(&st->vmax, __float_as_uint(v));
-  v = block_reduce(a.qmin_n, shf, OpMinF(), INFINITY);
-  if (threadIdx.x == 0 && v < INFINITY) atomicMin(&st->qmin_near, float_to_ordered(v));
-  v = block_reduce(a.qmax_n, shf, OpMaxF(), -INFINITY);
-  if (threadIdx.x == 0 && v > -INFINITY) atomicMax(&st->qmax_near, float_to_ordered(v));
-  v = block_reduce(a.qmin_a, shf, OpMinF(), INFINITY);
-  if (threadIdx.x == 0 && v < INFINITY) atomicMin(&st->qmin_all, float_to_ordered(v));
-  v = block_reduce(a.qmax_a, shf, OpMaxF(), -INFINITY);
-  if (threadIdx.x == 0 && v > -INFINITY) atomicMax(&st->qmax_all, float_to_ordered(v));
-  v = block_reduce(a.dv_n, shf, OpMaxF(), 0.0f);
-  if (threadIdx.x == 0 && v > 0.0f) atomicMax(&st->dvmax_near, __float_as_uint(v));
-  v = block_reduce(a.dv_a, shf, OpMaxF(), 0.0f);
-  if (threadIdx.x == 0 && v > 0.0f) atomicMax(&st->dvmax_all, __float_as_uint(v));
-  unsigned int u;
-  u = block_reduce(a.cap_n, shu, OpSumU(), 0u);
-  if (threadIdx.x == 0 && u) atomicAdd(&st->capped_near, u);
-  u = block_reduce(a.cap_a, shu, OpSumU(), 0u);
-  if (threadIdx.x == 0 && u) atomicAdd(&st->capped_all, u);
-  u = block_reduce(a.n_near, shu, OpSumU(), 0u);
-  if (threadIdx.x == 0 && u) atomicAdd(&st->n_near, u);
-  double d;
-  d = block_sum_compensated(a.vs_n, shd);
-  if (threadIdx.x == 0) partial[2 * blockIdx.x] = d;
-  d = block_sum_compensated(a.vs_a, shd);
-  if (threadIdx.x == 0) partial[2 * blockIdx.x + 1] = d;
+  constexpr int NW = SG_THREADS / 32;
+  __shared__ float shf[7][NW];
+  __shared__ unsigned int shu[3][NW];
+  __shared__ double shd[2][NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float f[7] = {a.vmax, a.qmin_n, a.qmax_n, a.qmin_a, a.qmax_a, a.dv_n, a.dv_a};
+  unsigned int u[3] = {a.cap_n, a.cap_a, a.n_near};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      const float w = __shfl_xor_sync(0xffffffffu, f[k], o);
+      f[k] = (k == 1 || k == 3) ? fminf(f[k], w) : fmaxf(f[k], w);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) u[k] += __shfl_xor_sync(0xffffffffu, u[k], o);
+  }
+  const double d0 = warp_sum_compensated(a.vs_n), d1 = warp_sum_compensated(a.vs_a);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) shf[k][wid] = f[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) shu[k][wid] = u[k];
+    shd[0][wid] = d0;
+    shd[1][wid] = d1;
+  }
+  __syncthreads();
+  if (wid != 0) return;
+  const bool in = lane < NW;
+  const float fid[7] = {0.0f, INFINITY, -INFINITY, INFINITY, -INFINITY, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < 7; ++k) f[k] = in ? shf[k][lane] : fid[k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u[k] = in ? shu[k][lane] : 0u;
+#pragma unroll
+  for (int o = NW / 2; o > 0; o >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      const float w = __shfl_xor_sync(0xffffffffu, f[k], o);
+      f[k] = (k == 1 || k == 3) ? fminf(f[k], w) : fmaxf(f[k], w);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) u[k] += __shfl_xor_sync(0xffffffffu, u[k], o);
+  }
+  if (lane != 0) return;
+  if (f[0] > 0.0f) atomicMax(&st->vmax, __float_as_uint(f[0]));
+  if (f[1] < INFINITY) atomicMin(&st->qmin_near, float_to_ordered(f[1]));
+  if (f[2] > -INFINITY) atomicMax(&st->qmax_near, float_to_ordered(f[2]));
+  if (f[3] < INFINITY) atomicMin(&st->qmin_all, float_to_ordered(f[3]));
+  if (f[4] > -INFINITY) atomicMax(&st->qmax_all, float_to_ordered(f[4]));
+  if (f[5] > 0.0f) atomicMax(&st->dvmax_near, __float_as_uint(f[5]));
+  if (f[6] > 0.0f) atomicMax(&st->dvmax_all, __float_as_uint(f[6]));
+  if (u[0]) atomicAdd(&st->capped_near, u[0]);
+  if (u[1]) atomicAdd(&st->capped_all, u[1]);
+  if (u[2]) atomicAdd(&st->n_near, u[2]);
+  double r0 = 0.0, r1 = 0.0;
+  for (int i = 0; i < NW; ++i) {
+    r0 += shd[0][i];
+    r1 += shd[1][i];
+  }
+  partial[2 * blockIdx.x] = r0;
+  partial[2 * blockIdx.x + 1] = r1;
 }
 
 __global__ void __launch_bounds__(SG_THREADS, 6) k_stage_svi(const float* __restrict__ phi,
@@ -227,7 +272,7 @@ __global__ void __launch_bounds__(SG_THREADS) k_stage_curv(const float* __restri
     const float k1 = trilinear_at(kd, ny, nz, p, 2, 0);
     const float k2 = trilinear_at(kd, ny, nz, p, 2, 1);
     float V, D;
-    curv_speed(k1, k2, L, &V, &D);
+    curv_speed(k1, k2, L, C, &V, &D);
     if (st) {
       const bool near = fabsf(c) < C.h;
       const float H = 0.5f * (k1 + k2);
@@ -413,16 +458,15 @@ namespace svie {
 // Elementwise law evaluation: SVI: V = speed(x1), D = dspeed(x1); curvature
 // laws: V, D = speed_and_diffusivity(x1 = k1, x2 = k2).
 __global__ void k_law_eval(const float* __restrict__ x1, const float* __restrict__ x2, long long m, svie_law L,
-                           float* __restrict__ V, float* __restrict__ D) {
+                           StageConst C, float* __restrict__ V, float* __restrict__ D) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  const StageConst C = {0.f, 0.f, 0.f, 0.f, 0.f, (float)L.n_cap, (float)L.eps, 0.f, 0.f};
   if (L.kind == 0) {
     if (V) V[t] = svi_speed(x1[t], L, C);
     if (D) D[t] = svi_dspeed(x1[t], L, C);
   } else {
     float v, d;
-    curv_speed(x1[t], x2[t], L, &v, &d);
+    curv_speed(x1[t], x2[t], L, C, &v, &d);
     if (V) V[t] = v;
     if (D) D[t] = d;
   }
@@ -436,6 +480,8 @@ extern "C" int svie_law_eval(const float* x1, const float* x2, int64_t m, const 
     return SVIE_ERR_ARG;
   }
   if (m == 0) return SVIE_OK;
-  svie::k_law_eval<<<svie::blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(x1, x2, m, *law, V, D);
+  // the law's float constants (the grid-dependent ones are unused here)
+  const svie::StageConst C = svie::stage_const(*law, 4, 4, 4);
+  svie::k_law_eval<<<svie::blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(x1, x2, m, *law, C, V, D);
   return svie::launch_status("svie_law_eval");
 }
