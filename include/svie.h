@@ -352,10 +352,11 @@ int svie_surface_signed_volume(const float* verts, const int32_t* faces, int64_t
  * dilated by `dilation` cells with the `margin` outer layers cleared. */
 int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin,
                      uint8_t* mask, uint8_t* tmp, void* stream);
-/* reinit_geometry (kernels.py:335-359) packed structure-of-arrays over the
- * m work-set nodes: dtau float[m], dist float[6m] (xp_x xm_x xp_y xm_y xp_z
- * xm_z), meta uint8[m] (bits 0-5 crossing flags cp/cm per axis, bit 6
- * phi0 > 0, bit 7 phi0 < 0). */
+/* reinit_geometry (kernels.py:335-359) packed over the m work-set nodes for
+ * svie_reinit_iterate / svie_reinit_rhs: dtau float[m], meta uint8[m] (bits
+ * 0-5 crossing flags cp/cm per axis, bit 6 phi0 > 0, bit 7 phi0 < 0), per-warp
+ * offsets and the subcell distances of the flagged crossings only (compact,
+ * in work-set order).  geo: svie_reinit_geometry_bytes(m), 16-byte aligned. */
 size_t svie_reinit_geometry_bytes(int64_t m);
 int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
                          int64_t sz, float h, float cfl, void* geo, void* stream);
@@ -367,9 +368,17 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
 /* kernels.reinit_rhs (kernels.py:363-379) for API parity. */
 int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz,
                     float h, const void* geo, float* out, void* stream);
-/* Unpack geometry into the 14 arrays of kernels.reinit_geometry. */
-int svie_reinit_geometry_unpack(const void* geo, int64_t m, float* sgn, float* dtau, uint8_t* flags,
+/* The 14 arrays of kernels.reinit_geometry (kernels.py:335-359): sgn, dtau
+ * float[m]; flags uint8[6][m] and dist6 float[6][m] in the order cp_x cm_x
+ * cp_y cm_y cp_z cm_z / xp_x xm_x xp_y xm_y xp_z xm_z (distances of every
+ * node, clamped below to 1e-6 h). */
+int svie_reinit_geometry_arrays(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
+                                int64_t sz, float h, float cfl, float* sgn, float* dtau, uint8_t* flags,
                                 float* dist6, void* stream);
+/* Packed geometry from those arrays (kernels.reinit_rhs takes them from the
+ * caller); dtau may be NULL. */
+int svie_reinit_geometry_pack(const float* sgn, const float* dtau, const uint8_t* flags, const float* dist6,
+                              int64_t m, void* geo, void* stream);
 /* levelset.dilate (levelset.py:25-34); tmp is a same-size scratch grid. */
 int svie_dilate(const uint8_t* mask, int nx, int ny, int nz, int steps, uint8_t* out, uint8_t* tmp,
                 void* stream);

@@ -143,7 +143,8 @@ _SIGS = {
     "svie_surface_scan": (I, [V, V, I64, I, I, I, V, Z, V, V]),
     "svie_surface_write": (I, [V, V, I64, I, I, I, V, Z, V, V, I64, V, I64, V]),
     "svie_surface_project": (I, [V, I, I, V, I64, F, V]),
-    "svie_reinit_geometry_unpack": (I, [V, I64, V, V, V, V, V]),
+    "svie_reinit_geometry_arrays": (I, [V, V, I64, I64, I64, I64, F, F, V, V, V, V, V]),
+    "svie_reinit_geometry_pack": (I, [V, V, V, V, I64, V, V]),
     "svie_dilate": (I, [V, I, I, I, I, V, V, V]),
     "svie_mesh_tri_index": (I, [V, V, I64, D, D, D, D, V, V, V, V]),
     "svie_mesh_weld_table_bytes": (Z, [I64]),

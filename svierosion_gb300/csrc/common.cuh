@@ -19,6 +19,10 @@
 
 namespace svie {
 
+// In-place exclusive scan of n ints on the stream; sums: ceil(n / 1024) ints
+// of scratch.  Returns the number of kernels launched (distance.cu).
+int scan_exclusive_i32(int* v, long long n, int* sums, cudaStream_t s);
+
 // Records a message for svie_last_error(); defined in capi.cu.
 void set_error(const char* fmt, ...);
 

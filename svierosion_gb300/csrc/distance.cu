@@ -106,6 +106,17 @@ __global__ void k_scan_add(int* __restrict__ v, long long n, const int* __restri
   if (i < n) v[i] += sums[blockIdx.x];
 }
 
+// In-place exclusive scan of n ints; sums: ceil(n / 1024) ints of scratch.
+// Returns the number of kernels launched.
+int scan_exclusive_i32(int* v, long long n, int* sums, cudaStream_t s) {
+  if (n <= 0) return 0;
+  const long long nb = (n + 1023) / 1024;
+  k_scan_local<<<(unsigned)nb, 1024, 0, s>>>(v, n, sums);
+  k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
+  k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(v, n, sums);
+  return 3;
+}
+
 __global__ void k_piece_fill(const float* __restrict__ tri, long long T, CellGrid G, const int* __restrict__ start,
                              int* __restrict__ cursor, int* __restrict__ order) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -200,10 +211,7 @@ int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float
   }
   const CellGrid G{ox, oy, oz, cs, 1.0f / cs, gx, gy, gz};
   if (T > 0) k_piece_count<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, start);
-  const long long n = cells + 1, nb = (n + 1023) / 1024;
-  k_scan_local<<<(unsigned)nb, 1024, 0, s>>>(start, n, sums);
-  k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
-  k_scan_add<<<(unsigned)nb, 1024, 0, s>>>(start, n, sums);
+  scan_exclusive_i32(start, cells + 1, sums, s);
   if (T > 0) k_piece_fill<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, start, cursor, order);
   return launch_status("svie_piece_grid_build", T > 0 ? 5 : 3);
 }

@@ -34,44 +34,68 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
   return fminf(fmaxf(ok ? quad : lin, 0.0f), h);
 }
 
-// Geometry record, structure of arrays over the work set (m entries):
-//   dtau  float [m]
-//   meta  uint8 [m]   bits 0-5: crossing flags cp_x cm_x cp_y cm_y cp_z cm_z,
-//                     bit 6: phi0 > 0, bit 7: phi0 < 0
-//   dist  float [6m]  xp_x xm_x xp_y xm_y xp_z xm_z, read only where the flag is set
-//   cfl   float       at geo_cfl_offset(m)
-// A sweep streams 1 byte of geometry per node (the flags) and rebuilds dtau
-// from the distances it reads anyway; dtau is stored for
-// svie_reinit_geometry_unpack.
+// Geometry record over the m work-set nodes (byte offsets in GeoLayout):
+//   dtau  float [m]     local pseudo-time step (for the array form; the
+//                       sweeps rebuild it from the distances they read)
+//   meta  uint8 [m]     bits 0-5: crossing flags cp_x cm_x cp_y cm_y cp_z cm_z,
+//                       bit 6: phi0 > 0, bit 7: phi0 < 0
+//   wbase int32 [W + 1] per warp of 32 entries (W = ceil(m / 32)): index of
+//                       its first distance in `dist`; wbase[W] = the count
+//   dist  float [<= 6m] the subcell distances of the flagged crossings only,
+//                       in work-set order and flag-bit order within a node
+//   cfl   float
+//   sums  int32         scratch of the scan that makes wbase
+// A sweep streams 1 byte of geometry per node and reads distances only at
+// crossings, from an array a few per cent of the work set long: the sweep's
+// whole footprint (the band part of the two grids, the index list, flags and
+// distances) then stays in L2 across the 40 sweeps of a call.
+struct GeoLayout {
+  long long m, W, meta, wbase, dist, cfl, sums, nsums, total;
+};
+
+__host__ __device__ inline long long align16ll(long long b) { return (b + 15) & ~15LL; }
+
+__host__ __device__ inline GeoLayout geo_layout(long long m) {
+  GeoLayout L;
+  L.m = m;
+  L.W = (m + 31) / 32;
+  L.meta = 4 * m;
+  L.wbase = align16ll(5 * m);
+  L.dist = align16ll(L.wbase + 4 * (L.W + 1));
+  L.cfl = align16ll(L.dist + 24 * m);
+  L.sums = L.cfl + 16;
+  L.nsums = (L.W + 1 + 1023) / 1024;
+  L.total = L.sums + 4 * L.nsums + 256;
+  return L;
+}
+
 struct Geo {
   float* dtau;
   uint8_t* meta;
+  int* wbase;
   float* dist;
+  float* cfl;
   long long m;
 };
 
-// cfl of the geometry, stored after the arrays (16-byte aligned).
-__host__ __device__ inline long long geo_cfl_offset(long long m) { return (29 * m + 15) & ~15LL; }
-SVIE_DEV float geo_cfl(const void* base, long long m) {
-  return __ldg(reinterpret_cast<const float*>(static_cast<const char*>(base) + geo_cfl_offset(m)));
-}
-
 SVIE_DEV Geo geo_view(void* base, long long m) {
-  Geo g;
+  const GeoLayout L = geo_layout(m);
   char* b = (char*)base;
+  Geo g;
   g.dtau = (float*)b;
-  g.dist = (float*)(b + 4 * m);
-  g.meta = (uint8_t*)(b + 28 * m);
+  g.meta = (uint8_t*)(b + L.meta);
+  g.wbase = (int*)(b + L.wbase);
+  g.dist = (float*)(b + L.dist);
+  g.cfl = (float*)(b + L.cfl);
   g.m = m;
   return g;
 }
 
-__global__ void k_reinit_geometry(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
-                                  int sx, int sy, int sz, float h, float cfl, void* geo) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
-  Geo g = geo_view(geo, m);
-  const int i = idx[t];
+// Crossing geometry at node i (kernels.py:335-359): flag bits 2a (cp) and
+// 2a + 1 (cm), distances d[2a] = xp, d[2a + 1] = xm clamped below to 1e-6 h,
+// and dtau = cfl max(hmin, 1e-3 h) with hmin from the unclamped distances.
+SVIE_DEV uint32_t geometry_at(const float* __restrict__ f, int i, int sx, int sy, int sz, float h, float cfl,
+                              float d[6], float& dtau) {
   const float* qp = f + i;
   const float c = __ldg(qp);
   float hmin = h;
@@ -92,25 +116,135 @@ __global__ void k_reinit_geometry(const float* __restrict__ f, const int32_t* __
     hmin = fminf(hmin, cm ? xm : hmin);
     flags |= (cp ? 1u : 0u) << (2 * a);
     flags |= (cm ? 1u : 0u) << (2 * a + 1);
-    g.dist[(2 * a) * m + t] = fmaxf(xp, 1e-6f * h);
-    g.dist[(2 * a + 1) * m + t] = fmaxf(xm, 1e-6f * h);
+    d[2 * a] = fmaxf(xp, 1e-6f * h);
+    d[2 * a + 1] = fmaxf(xm, 1e-6f * h);
   }
   flags |= (c > 0.0f ? 1u : 0u) << 6;
   flags |= (c < 0.0f ? 1u : 0u) << 7;
-  g.dtau[t] = cfl * fmaxf(hmin, 1e-3f * h);
-  g.meta[t] = (uint8_t)flags;
-  if (t == 0) *reinterpret_cast<float*>(static_cast<char*>(geo) + geo_cfl_offset(m)) = cfl;
+  dtau = cfl * fmaxf(hmin, 1e-3f * h);
+  return flags;
+}
+
+// Exclusive prefix of v over the lanes of the warp (all lanes take part).
+SVIE_DEV int warp_exclusive(int v) {
+  const int lane = threadIdx.x & 31;
+  int s = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, s, o);
+    if (lane >= o) s += y;
+  }
+  return s - v;
+}
+
+// Pass 1: flags, sign bits, dtau; per-warp crossing counts into wbase.
+__global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
+                               int sy, int sz, float h, float cfl, void* geo) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  Geo g = geo_view(geo, m);
+  uint32_t flags = 0;
+  if (t < m) {
+    float d[6], dtau;
+    flags = geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
+    g.dtau[t] = dtau;
+    g.meta[t] = (uint8_t)flags;
+  }
+  const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags & 63u));
+  const long long w = t >> 5;
+  if ((threadIdx.x & 31) == 0 && w < (m + 31) / 32) g.wbase[w] = cnt;
+  if (t == 0) {
+    g.wbase[(m + 31) / 32] = 0;
+    *g.cfl = cfl;
+  }
+}
+
+// Pass 3 (after the exclusive scan of wbase): the flagged distances.  The
+// flags come from pass 1; only warps holding a crossing recompute geometry.
+__global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
+                              int sy, int sz, float h, float cfl, void* geo) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  Geo g = geo_view(geo, m);
+  const uint32_t flags = t < m ? g.meta[t] & 63u : 0u;
+  if (!__ballot_sync(0xffffffffu, flags != 0u)) return;
+  const int off = warp_exclusive(__popc(flags));
+  if (!flags) return;
+  float d[6], dtau;
+  geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
+  float* out = g.dist + g.wbase[t >> 5] + off;
+  int r = 0;
+#pragma unroll
+  for (int b = 0; b < 6; ++b)
+    if ((flags >> b) & 1u) out[r++] = d[b];
+}
+
+// Array form of the geometry for kernels.reinit_geometry: every node's
+// distances (also where no crossing is flagged), flags one byte per axis side.
+__global__ void k_reinit_geometry_full(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
+                                       int sx, int sy, int sz, float h, float cfl, float* sgn, float* dtau_out,
+                                       uint8_t* flags6, float* dist6) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  float d[6], dtau;
+  const uint32_t flags = geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
+  sgn[t] = (flags & 64u) ? 1.0f : ((flags & 128u) ? -1.0f : 0.0f);
+  dtau_out[t] = dtau;
+  for (int a = 0; a < 6; ++a) {
+    flags6[a * m + t] = (flags >> a) & 1u;
+    dist6[a * m + t] = d[a];
+  }
+}
+
+// Packed form from the 14 arrays (kernels.reinit_rhs takes them from the
+// caller): pass 1 counts, pass 2 (after the scan) writes the distances.
+__global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __restrict__ dtau,
+                              const uint8_t* __restrict__ flags6, const float* __restrict__ dist6, long long m,
+                              void* geo, int pass) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  Geo g = geo_view(geo, m);
+  uint32_t flags = 0;
+  if (t < m)
+    for (int a = 0; a < 6; ++a) flags |= (flags6[a * m + t] ? 1u : 0u) << a;
+  if (pass == 0) {
+    const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags));
+    const long long w = t >> 5;
+    if ((threadIdx.x & 31) == 0 && w < (m + 31) / 32) g.wbase[w] = cnt;
+    if (t == 0) {
+      g.wbase[(m + 31) / 32] = 0;
+      *g.cfl = 0.0f;
+    }
+    if (t < m) {
+      const float s = sgn[t];
+      g.meta[t] = (uint8_t)(flags | (s > 0.0f ? 64u : 0u) | (s < 0.0f ? 128u : 0u));
+      g.dtau[t] = dtau ? dtau[t] : 0.0f;
+    }
+    return;
+  }
+  const int off = warp_exclusive(__popc(flags));
+  if (t >= m || !flags) return;
+  float* out = g.dist + g.wbase[t >> 5] + off;
+  int r = 0;
+  for (int b = 0; b < 6; ++b)
+    if ((flags >> b) & 1u) out[r++] = dist6[b * m + t];
 }
 
 SVIE_DEV float meta_sgn(uint32_t meta) { return (meta & 64u) ? 1.0f : ((meta & 128u) ? -1.0f : 0.0f); }
 
+// Index of entry t's first distance in g.dist; every lane of the warp calls
+// it (lanes past m with flags 0).  Warps without any crossing skip the scan.
+SVIE_DEV int dist_offset(const Geo& g, long long t, uint32_t flags) {
+  const uint32_t f6 = flags & 63u;
+  if (!__ballot_sync(0xffffffffu, f6 != 0u)) return 0;
+  const int off = warp_exclusive(__popc(f6));
+  return f6 ? __ldg(g.wbase + (t >> 5)) + off : 0;
+}
+
 // reinit_rhs (kernels.py:363-379) at work-set entry t.  Divisions by h use
 // the correctly rounded reciprocal rh (div_by); hh = RN(h * h).  Also returns
 // hmin = min(h, stored distances of the flagged crossings), from which
-// dtau = cfl * max(hmin, 1e-3 h) is rebuilt exactly as k_reinit_geometry
-// computed it (a distance below 1e-6 h, stored clamped to 1e-6 h, gives the
-// same 1e-3 h either way).
-SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, const Geo& g, uint32_t flags, int sx,
+// dtau = cfl * max(hmin, 1e-3 h) is rebuilt exactly as geometry_at computed
+// it (a distance below 1e-6 h, stored clamped to 1e-6 h, gives the same
+// 1e-3 h either way).  `off`: the node's first distance (dist_offset).
+SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, int off, uint32_t flags, int sx,
                              int sy, int sz, float h, float rh, float hh, float& hmin) {
   const float* qp = f + i;
   const float c = __ldg(qp);
@@ -128,6 +262,7 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, co
     v3[a][2] = __ldg(qp + s);
     v3[a][3] = __ldg(qp + 2 * s);
   }
+  const float* dn = g.dist + off;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const float m2 = v3[a][0], m1 = v3[a][1], p1 = v3[a][2], p2 = v3[a][3];
@@ -136,12 +271,12 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, long long t, co
     float Dp = div_by(p1 - c - 0.5f * mm_p, h, rh);
     float Dm = div_by(c - m1 + 0.5f * mm_m, h, rh);
     if ((flags >> (2 * a)) & 1u) {
-      const float xp = g.dist[(2 * a) * g.m + t];
+      const float xp = __ldg(dn + __popc(flags & ((1u << (2 * a)) - 1u)));
       Dp = -c / xp - 0.5f * xp * mm_p / hh;
       hmin = fminf(hmin, xp);
     }
     if ((flags >> (2 * a + 1)) & 1u) {
-      const float xm = g.dist[(2 * a + 1) * g.m + t];
+      const float xm = __ldg(dn + __popc(flags & ((1u << (2 * a + 1)) - 1u)));
       Dm = c / xm + 0.5f * xm * mm_m / hh;
       hmin = fminf(hmin, xm);
     }
@@ -157,12 +292,15 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
                                                              int sy, int sz, float h, float rh, void* geo,
                                                              int second) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
   Geo g = geo_view(geo, m);
-  const float cfl = geo_cfl(geo, m);
-  const int i = idx[t];
+  const bool act = t < m;
+  const uint32_t flags = act ? __ldg(g.meta + t) : 0u;
+  const int off = dist_offset(g, t, flags);
+  if (!act) return;
+  const float cfl = __ldg(g.cfl);
+  const int i = __ldg(idx + t);
   float hmin;
-  const float r = reinit_rhs_at(src, i, t, g, g.meta[t], sx, sy, sz, h, rh, h * h, hmin);
+  const float r = reinit_rhs_at(src, i, g, off, flags, sx, sy, sz, h, rh, h * h, hmin);
   const float dtau = cfl * fmaxf(hmin, 1e-3f * h);
   if (!second) {
     dst[i] = src[i] + dtau * r;  // u0 + dtau rhs(A)
@@ -175,23 +313,13 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
 __global__ void k_reinit_rhs(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx, int sy,
                              int sz, float h, float rh, void* geo, float* out) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
   Geo g = geo_view(geo, m);
+  const bool act = t < m;
+  const uint32_t flags = act ? g.meta[t] : 0u;
+  const int off = dist_offset(g, t, flags);
+  if (!act) return;
   float hmin;
-  out[t] = reinit_rhs_at(f, idx[t], t, g, g.meta[t], sx, sy, sz, h, rh, h * h, hmin);
-}
-
-__global__ void k_geo_unpack(const void* geo, long long m, float* sgn, float* dtau, uint8_t* flags, float* dist6) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
-  Geo g = geo_view(const_cast<void*>(geo), m);
-  const uint32_t meta = g.meta[t];
-  sgn[t] = meta_sgn(meta);
-  dtau[t] = g.dtau[t];
-  for (int a = 0; a < 6; ++a) {
-    flags[a * m + t] = (meta >> a) & 1u;
-    dist6[a * m + t] = g.dist[a * m + t];
-  }
+  out[t] = reinit_rhs_at(f, idx[t], g, off, flags, sx, sy, sz, h, rh, h * h, hmin);
 }
 
 __global__ void k_mark(const int32_t* __restrict__ band, long long m, uint8_t* __restrict__ mask) {
@@ -326,7 +454,7 @@ static void dilate_box(const uint8_t* src, uint8_t* dst, uint8_t* tmp, int nx, i
   *launches += 3;
 }
 
-inline size_t geo_bytes(long long m) { return (size_t)(m < 1 ? 1 : m) * 29 + 256; }
+inline size_t geo_bytes(long long m) { return (size_t)geo_layout(m < 1 ? 1 : m).total; }
 
 }  // namespace svie
 
@@ -369,14 +497,19 @@ size_t svie_reinit_geometry_bytes(int64_t m) { return geo_bytes(m); }
 
 int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz,
                          float h, float cfl, void* geo, void* stream) {
-  if (m < 0 || (m > 0 && (!phi || !idx || !geo))) {
-    set_error("svie_reinit_geometry: bad arguments");
+  if (m < 0 || (m > 0 && (!phi || !idx || !geo)) || ((uintptr_t)geo & 15)) {
+    set_error("svie_reinit_geometry: bad arguments (geo must be 16-byte aligned)");
     return SVIE_ERR_ARG;
   }
   if (m == 0) return SVIE_OK;
-  k_reinit_geometry<<<blocks_for(m, RI_THREADS), RI_THREADS, 0, (cudaStream_t)stream>>>(phi, idx, m, sx, sy, sz, h,
-                                                                                        cfl, geo);
-  return launch_status("svie_reinit_geometry");
+  cudaStream_t s = (cudaStream_t)stream;
+  const GeoLayout L = geo_layout(m);
+  const int nb = blocks_for(m, RI_THREADS);
+  k_reinit_count<<<nb, RI_THREADS, 0, s>>>(phi, idx, m, sx, sy, sz, h, cfl, geo);
+  char* b = (char*)geo;
+  const int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
+  k_reinit_dist<<<nb, RI_THREADS, 0, s>>>(phi, idx, m, sx, sy, sz, h, cfl, geo);
+  return launch_status("svie_reinit_geometry", 2 + ns);
 }
 
 int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
@@ -408,11 +541,34 @@ int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx,
   return launch_status("svie_reinit_rhs");
 }
 
-int svie_reinit_geometry_unpack(const void* geo, int64_t m, float* sgn, float* dtau, uint8_t* flags, float* dist6,
+int svie_reinit_geometry_arrays(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz,
+                                float h, float cfl, float* sgn, float* dtau, uint8_t* flags, float* dist6,
                                 void* stream) {
-  if (m <= 0) return m < 0 ? SVIE_ERR_ARG : SVIE_OK;
-  k_geo_unpack<<<blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(geo, m, sgn, dtau, flags, dist6);
-  return launch_status("svie_reinit_geometry_unpack");
+  if (m < 0 || (m > 0 && (!phi || !idx || !sgn || !dtau || !flags || !dist6))) {
+    set_error("svie_reinit_geometry_arrays: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (m == 0) return SVIE_OK;
+  k_reinit_geometry_full<<<blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(phi, idx, m, sx, sy, sz, h, cfl,
+                                                                             sgn, dtau, flags, dist6);
+  return launch_status("svie_reinit_geometry_arrays");
+}
+
+int svie_reinit_geometry_pack(const float* sgn, const float* dtau, const uint8_t* flags, const float* dist6, int64_t m,
+                              void* geo, void* stream) {
+  if (m < 0 || (m > 0 && (!sgn || !flags || !dist6 || !geo)) || ((uintptr_t)geo & 15)) {
+    set_error("svie_reinit_geometry_pack: bad arguments (geo must be 16-byte aligned)");
+    return SVIE_ERR_ARG;
+  }
+  if (m == 0) return SVIE_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  const GeoLayout L = geo_layout(m);
+  const int nb = blocks_for(m, 256);
+  k_reinit_pack<<<nb, 256, 0, s>>>(sgn, dtau, flags, dist6, m, geo, 0);
+  char* b = (char*)geo;
+  const int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
+  k_reinit_pack<<<nb, 256, 0, s>>>(sgn, dtau, flags, dist6, m, geo, 1);
+  return launch_status("svie_reinit_geometry_pack", 2 + ns);
 }
 
 }  // extern "C"

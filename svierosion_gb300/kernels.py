@@ -125,18 +125,20 @@ def reinit_geometry(flat, idx, sx, sy, sz, h, cfl):
     """Per-axis crossings and subcell distances (kernels.py:335-359).
 
     Returns (sgn, dtau, cp_x, cm_x, xp_x, xm_x, cp_y, ..., xm_z) like the
-    reference; the fused reinitialisation uses the packed form directly."""
+    reference; the packed device form the fused reinitialisation uses rides
+    along as ``.packed``."""
     i = _i32(idx)
     m = i.numel()
+    f = _flat(flat)
     geo = torch.empty(nat.lib().svie_reinit_geometry_bytes(m), dtype=torch.uint8, device=flat.device)
-    nat.call("svie_reinit_geometry", nat.ptr(_flat(flat)), nat.ptr(i), m, int(sx), int(sy), int(sz), float(h),
+    nat.call("svie_reinit_geometry", nat.ptr(f), nat.ptr(i), m, int(sx), int(sy), int(sz), float(h),
              float(cfl), nat.ptr(geo), nat.stream())
     sgn = torch.empty(m, dtype=torch.float32, device=flat.device)
     dtau = torch.empty_like(sgn)
     flags = torch.empty((6, m), dtype=torch.uint8, device=flat.device)
     dist = torch.empty((6, m), dtype=torch.float32, device=flat.device)
-    nat.call("svie_reinit_geometry_unpack", nat.ptr(geo), m, nat.ptr(sgn), nat.ptr(dtau), nat.ptr(flags),
-             nat.ptr(dist), nat.stream())
+    nat.call("svie_reinit_geometry_arrays", nat.ptr(f), nat.ptr(i), m, int(sx), int(sy), int(sz), float(h),
+             float(cfl), nat.ptr(sgn), nat.ptr(dtau), nat.ptr(flags), nat.ptr(dist), nat.stream())
     fl = flags.view(torch.bool)
     out = [sgn, dtau]
     for a in range(3):
@@ -167,18 +169,13 @@ def reinit_rhs(flat, idx, sx, sy, sz, h, sgn, cpx, cmx, xpx, xmx, cpy, cmy, xpy,
 
 
 def _pack_geometry(sgn, flags6, dist6, m, device):
-    """Byte layout of svie_reinit_geometry: dtau float[m] (unused by reinit_rhs),
-    dist float[6m], meta uint8[m] (crossing flags, sign bits)."""
-    geo = torch.zeros(nat.lib().svie_reinit_geometry_bytes(m), dtype=torch.uint8, device=device)
-    dist = geo[4 * m:28 * m].view(torch.float32).view(6, m)
-    for a, d in enumerate(dist6):
-        dist[a] = d.to(torch.float32)
-    meta = torch.zeros(m, dtype=torch.int32, device=device)
-    for a, f in enumerate(flags6):
-        meta |= f.to(torch.int32) << a
-    meta |= (sgn > 0).to(torch.int32) << 6
-    meta |= (sgn < 0).to(torch.int32) << 7
-    geo[28 * m:29 * m] = meta.to(torch.uint8)
+    """The packed device form of svie_reinit_geometry from the reference's arrays."""
+    geo = torch.empty(nat.lib().svie_reinit_geometry_bytes(m), dtype=torch.uint8, device=device)
+    s = sgn.to(torch.float32).contiguous()
+    fl = torch.stack([f.to(torch.uint8) for f in flags6]).contiguous()
+    di = torch.stack([d.to(torch.float32) for d in dist6]).contiguous()
+    nat.call("svie_reinit_geometry_pack", nat.ptr(s), None, nat.ptr(fl), nat.ptr(di), m, nat.ptr(geo),
+             nat.stream())
     return geo
 
 
