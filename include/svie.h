@@ -122,7 +122,8 @@ int svie_mask_select(const uint8_t* mask, const int32_t* vals, int64_t n, const 
                      size_t ws_bytes, int32_t* out, int64_t capacity, void* stream);
 /* The same node sets in brick order (bricks of 4 x 4 x 16 nodes, x-major
  * brick order, z fastest inside a row): kind 0 selects mask[i] != 0 (uint8
- * src), kind 1 selects |phi[i]| < thresh (float src).  Same two-call
+ * src), kind 1 selects |phi[i]| < thresh (float src), kind 2 the set bits of
+ * a bit mask in the layout of svie_reinit_bits (uint32 src).  Same two-call
  * protocol; the brick-ordered lists drive the stencil kernels, the ascending
  * lists stay the API's node lists. */
 size_t svie_brick_workspace_bytes(int nx, int ny, int nz);
@@ -352,6 +353,12 @@ int svie_surface_signed_volume(const float* verts, const int32_t* faces, int64_t
  * dilated by `dilation` cells with the `margin` outer layers cleared. */
 int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin,
                      uint8_t* mask, uint8_t* tmp, void* stream);
+/* The same work mask as bits (rows (x, y) of ceil(nz / 32) words, bit z % 32
+ * of word z / 32; dilation <= 31), for svie_brick_scan / svie_brick_write
+ * kind 2.  bits and tmp: svie_reinit_bits_bytes(nx, ny, nz) each. */
+size_t svie_reinit_bits_bytes(int nx, int ny, int nz);
+int svie_reinit_bits(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin,
+                     uint32_t* bits, uint32_t* tmp, void* stream);
 /* reinit_geometry (kernels.py:335-359) packed over the m work-set nodes for
  * svie_reinit_iterate / svie_reinit_rhs: dtau float[m], meta uint8[m] (bits
  * 0-5 crossing flags cp/cm per axis, bit 6 phi0 > 0, bit 7 phi0 < 0), per-warp

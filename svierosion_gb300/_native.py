@@ -130,6 +130,8 @@ _SIGS = {
     "svie_rk_stage": (I, [V, V, I64, V, V, V, I, V]),
     "svie_reinit_mask": (I, [V, I64, I, I, I, I, I, V, V, V]),
     "svie_reinit_geometry_bytes": (Z, [I64]),
+    "svie_reinit_bits_bytes": (Z, [I, I, I]),
+    "svie_reinit_bits": (I, [V, I64, I, I, I, I, I, V, V, V]),
     "svie_reinit_geometry": (I, [V, V, I64, I64, I64, I64, F, F, V, V]),
     "svie_reinit_iterate": (I, [V, V, I64, V, I64, I64, I64, I64, F, V, I, V]),
     "svie_reinit_rhs": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),

@@ -410,7 +410,8 @@ struct BrickGeom {
 // ballot bits follow the list order.  Node of the lane in chunk j, or -1.
 struct BrickWalk {
   int x0[2], y0[2], z0[2];
-  bool ok[2];
+  long long base[2];  // node of row 0 of each brick for this lane (z0 + lane % 16)
+  bool ok[2], full[2];
   SVIE_DEV BrickWalk(const BrickGeom& G) {
     const long long b0 = ((long long)blockIdx.x * CMP_THREADS + (threadIdx.x & ~31)) >> 4;
 #pragma unroll
@@ -422,6 +423,8 @@ struct BrickWalk {
       x0[h] = (int)(bxy / G.nby) * BRX;
       y0[h] = (int)(bxy % G.nby) * BRY;
       z0[h] = bz * BRZ;
+      full[h] = ok[h] && x0[h] + BRX <= G.nx && y0[h] + BRY <= G.ny && z0[h] + BRZ <= G.nz;
+      base[h] = ((long long)x0[h] * G.ny + y0[h]) * G.nz + z0[h] + (threadIdx.x & 15);
     }
   }
   SVIE_DEV long long at(const BrickGeom& G, int j, int* c) const {
@@ -433,7 +436,21 @@ struct BrickWalk {
     if (!ok[h] || c[0] >= G.nx || c[1] >= G.ny || c[2] >= G.nz) return -1;
     return ((long long)c[0] * G.ny + c[1]) * G.nz + c[2];
   }
+  // Coordinates of chunk j (valid where node() >= 0).
+  SVIE_DEV void coords(int j, int& x, int& y, int& z) const {
+    const int h = j >> 3, lr = ((2 * j) & 15) + ((threadIdx.x >> 4) & 1);
+    x = x0[h] + (lr >> 2);
+    y = y0[h] + (lr & 3);
+    z = z0[h] + (threadIdx.x & 15);
+  }
+  // Node of chunk j; bricks inside the grid (all but the last of each axis)
+  // take it from the brick's base without bounds checks.
   SVIE_DEV long long node(const BrickGeom& G, int j) const {
+    const int h = j >> 3;
+    if (full[h]) {
+      const int lr = ((2 * j) & 15) + ((threadIdx.x >> 4) & 1);
+      return base[h] + (long long)((lr >> 2) * (G.ny * G.nz) + (lr & 3) * G.nz);
+    }
     int c[3];
     return at(G, j, c);
   }
@@ -473,8 +490,6 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_band_write(const float* _
                                                                   long long capacity, float* occ,
                                                                   svie_band_info* info) {
   __shared__ int sh[33];
-  __shared__ long long shl[CMP_THREADS / 32];
-  __shared__ int shi[CMP_THREADS / 32];
   const BrickWalk W(G);
   float pv[CMP_IPT];
 #pragma unroll
@@ -486,45 +501,78 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_band_write(const float* _
   int wt = 0, inside_static = 0;
   int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
   int ilo[3] = {INT_MAX, INT_MAX, INT_MAX}, ihi[3] = {-1, -1, -1};
+  // the bounding boxes and the static-inside count are kept by the first lane
+  // of each half-warp, one row of 16 nodes per chunk, from the ballot bits
+  const int lane = threadIdx.x & 31, hs = lane & 16;
+  const bool leader = (lane & 15) == 0;
 #pragma unroll
   for (int j = 0; j < CMP_IPT; ++j) {
-    int c[3];
-    const long long e = W.at(G, j, c);
-    bool sel = false;
-    if (e >= 0) {
-      const float v = pv[j];
-      sel = fabsf(v) < thresh;
-      const bool neg = v < 0.0f;
-      if (occ) occ[e] = neg ? 1.0f : 0.0f;
-      if (sel) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
-      }
-      if (neg) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) { ilo[a] = min(ilo[a], c[a]); ihi[a] = max(ihi[a], c[a]); }
-        if (!sel) ++inside_static;
+    const long long e = W.node(G, j);
+    const float v = pv[j];
+    const bool valid = e >= 0;
+    const bool sel = valid && fabsf(v) < thresh;
+    const bool neg = valid && v < 0.0f;
+    if (valid && occ) occ[e] = neg ? 1.0f : 0.0f;
+    const unsigned int bs = __ballot_sync(0xffffffffu, sel), bn = __ballot_sync(0xffffffffu, neg);
+    bal[j] = bs;
+    wt += __popc(bs);
+    if (leader) {
+      const unsigned int ms = (bs >> hs) & 0xffffu, mn = (bn >> hs) & 0xffffu;
+      if (ms | mn) {
+        int x, y, z;
+        W.coords(j, x, y, z);  // the row's first z
+        if (ms) {
+          lo[0] = min(lo[0], x); hi[0] = max(hi[0], x);
+          lo[1] = min(lo[1], y); hi[1] = max(hi[1], y);
+          lo[2] = min(lo[2], z + __ffs(ms) - 1); hi[2] = max(hi[2], z + 31 - __clz(ms));
+        }
+        if (mn) {
+          ilo[0] = min(ilo[0], x); ihi[0] = max(ihi[0], x);
+          ilo[1] = min(ilo[1], y); ihi[1] = max(ihi[1], y);
+          ilo[2] = min(ilo[2], z + __ffs(mn) - 1); ihi[2] = max(ihi[2], z + 31 - __clz(mn));
+          inside_static += __popc(mn & ~ms);
+        }
       }
     }
-    bal[j] = __ballot_sync(0xffffffffu, sel);
-    wt += __popc(bal[j]);
   }
   int tot;
   const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
   write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)W.node(G, j); });
-  long long st = block_reduce((long long)inside_static, shl, OpSumLL(), 0LL);
-  if (threadIdx.x == 0 && st) atomicAdd((unsigned long long*)&info->static_inside, (unsigned long long)st);
+  // the static-inside count and the two bounding boxes: warp reductions,
+  // then one barrier and warp 0 across the warps
+  constexpr int NW = CMP_THREADS / 32;
+  int r[13] = {inside_static, lo[0], lo[1], lo[2], -hi[0], -hi[1], -hi[2],
+               ilo[0], ilo[1], ilo[2], -ihi[0], -ihi[1], -ihi[2]};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    r[0] += __shfl_xor_sync(0xffffffffu, r[0], o);
+#pragma unroll
+    for (int k = 1; k < 13; ++k) r[k] = min(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+  }
+  __shared__ int shr[13][NW];
+  const int wid = threadIdx.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 13; ++k) shr[k][wid] = r[k];
+  }
+  __syncthreads();
+  if (wid != 0) return;
+#pragma unroll
+  for (int k = 0; k < 13; ++k) r[k] = lane < NW ? shr[k][lane] : (k == 0 ? 0 : INT_MAX);
+#pragma unroll
+  for (int o = NW / 2; o > 0; o >>= 1) {
+    r[0] += __shfl_xor_sync(0xffffffffu, r[0], o);
+#pragma unroll
+    for (int k = 1; k < 13; ++k) r[k] = min(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+  }
+  if (lane != 0) return;
+  if (r[0]) atomicAdd((unsigned long long*)&info->static_inside, (unsigned long long)r[0]);
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    int v;
-    v = block_reduce(lo[a], shi, OpMinI(), INT_MAX);
-    if (threadIdx.x == 0 && v != INT_MAX) atomicMin(&info->lo[a], v);
-    v = block_reduce(hi[a], shi, OpMaxI(), -1);
-    if (threadIdx.x == 0 && v >= 0) atomicMax(&info->hi[a], v);
-    v = block_reduce(ilo[a], shi, OpMinI(), INT_MAX);
-    if (threadIdx.x == 0 && v != INT_MAX) atomicMin(&info->ilo[a], v);
-    v = block_reduce(ihi[a], shi, OpMaxI(), -1);
-    if (threadIdx.x == 0 && v >= 0) atomicMax(&info->ihi[a], v);
+    if (r[1 + a] != INT_MAX) atomicMin(&info->lo[a], r[1 + a]);
+    if (-r[4 + a] >= 0) atomicMax(&info->hi[a], -r[4 + a]);
+    if (r[7 + a] != INT_MAX) atomicMin(&info->ilo[a], r[7 + a]);
+    if (-r[10 + a] >= 0) atomicMax(&info->ihi[a], -r[10 + a]);
   }
 }
 
@@ -560,6 +608,44 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_write(Pred pred, BrickGeo
   write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)W.node(G, j); });
 }
 
+// The reinitialisation work mask as bits (svie_reinit_bits: rows (x, y) of
+// nzw words, bit z % 32 of word z / 32, nothing set past nz): the lane's bit
+// in chunk j; one word per half-warp row, no node index needed for the test.
+SVIE_DEV bool brick_bit(const uint32_t* __restrict__ bits, int nzw, const BrickWalk& W, const BrickGeom& G, int j) {
+  int x, y, z;
+  W.coords(j, x, y, z);
+  if (!W.ok[j >> 3] || x >= G.nx || y >= G.ny) return false;
+  return (__ldg(bits + ((long long)x * G.ny + y) * nzw + (z >> 5)) >> (z & 31)) & 1u;
+}
+
+__global__ void __launch_bounds__(CMP_THREADS) k_brick_bits_count(const uint32_t* __restrict__ bits, int nzw,
+                                                                  BrickGeom G, int* counts) {
+  __shared__ int sh[CMP_THREADS / 32];
+  const BrickWalk W(G);
+  int c = 0;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) c += brick_bit(bits, nzw, W, G, j) ? 1 : 0;
+  int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
+  if (threadIdx.x == 0) counts[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(CMP_THREADS) k_brick_bits_write(const uint32_t* __restrict__ bits, int nzw,
+                                                                  BrickGeom G, const int* offsets, int32_t* out,
+                                                                  long long capacity) {
+  __shared__ int sh[33];
+  const BrickWalk W(G);
+  unsigned int bal[CMP_IPT];
+  int wt = 0;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    bal[j] = __ballot_sync(0xffffffffu, brick_bit(bits, nzw, W, G, j));
+    wt += __popc(bal[j]);
+  }
+  int tot;
+  const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
+  write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)W.node(G, j); });
+}
+
 struct AbsLessPred {
   const float* phi;
   float thresh;
@@ -587,7 +673,7 @@ int svie_brick_scan(int kind, const void* src, int nx, int ny, int nz, float thr
                     int64_t* count, void* stream) {
   using namespace svie;
   const long long n = (long long)nx * ny * nz;
-  if (!src || !count || n <= 0 || n >= (1LL << 31) || (kind != 0 && kind != 1)) {
+  if (!src || !count || n <= 0 || n >= (1LL << 31) || kind < 0 || kind > 2) {
     set_error("svie_brick_scan: bad arguments");
     return SVIE_ERR_ARG;
   }
@@ -599,7 +685,8 @@ int svie_brick_scan(int kind, const void* src, int nx, int ny, int nz, float thr
   const BrickGeom G = brick_geom(nx, ny, nz);
   const long long nb = brick_blocks(G);
   if (kind == 0) k_brick_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(MaskPred{(const uint8_t*)src}, G, (int*)ws);
-  else k_brick_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(AbsLessPred{(const float*)src, thresh}, G, (int*)ws);
+  else if (kind == 1) k_brick_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(AbsLessPred{(const float*)src, thresh}, G, (int*)ws);
+  else k_brick_bits_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>((const uint32_t*)src, (nz + 31) / 32, G, (int*)ws);
   k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)count);
   return launch_status("svie_brick_scan", 2);
 }
@@ -608,7 +695,7 @@ int svie_brick_write(int kind, const void* src, int nx, int ny, int nz, float th
                      int32_t* out, int64_t capacity, void* stream) {
   using namespace svie;
   const long long n = (long long)nx * ny * nz;
-  if (!src || n <= 0 || n >= (1LL << 31) || (kind != 0 && kind != 1) || (capacity > 0 && !out)) {
+  if (!src || n <= 0 || n >= (1LL << 31) || kind < 0 || kind > 2 || (capacity > 0 && !out)) {
     set_error("svie_brick_write: bad arguments");
     return SVIE_ERR_ARG;
   }
@@ -621,9 +708,12 @@ int svie_brick_write(int kind, const void* src, int nx, int ny, int nz, float th
   const long long nb = brick_blocks(G);
   if (kind == 0)
     k_brick_write<<<(unsigned)nb, CMP_THREADS, 0, s>>>(MaskPred{(const uint8_t*)src}, G, (const int*)ws, out, capacity);
-  else
+  else if (kind == 1)
     k_brick_write<<<(unsigned)nb, CMP_THREADS, 0, s>>>(AbsLessPred{(const float*)src, thresh}, G, (const int*)ws, out,
                                                        capacity);
+  else
+    k_brick_bits_write<<<(unsigned)nb, CMP_THREADS, 0, s>>>((const uint32_t*)src, (nz + 31) / 32, G, (const int*)ws,
+                                                            out, capacity);
   return launch_status("svie_brick_write");
 }
 

@@ -454,6 +454,59 @@ static void dilate_box(const uint8_t* src, uint8_t* dst, uint8_t* tmp, int nx, i
   *launches += 3;
 }
 
+// ------------------------------------------------- bit-packed work mask
+// The reinitialisation work mask as bits: rows (x, y) of nzw = ceil(nz / 32)
+// words, bit z % 32 of word z / 32 (4.6 MB on the 448 x 336 x 245 grid
+// instead of 37 MB of bytes).  The band is marked with atomicOr, then the
+// box dilation runs as three separable word passes (z by shifts across the
+// neighbouring words, then y and x as ORs of neighbouring rows), the last of
+// which also clears the margin layers and the bits past nz.
+__global__ void k_mark_bits(const int32_t* __restrict__ band, long long m, int nz, int nzw, uint32_t* bits) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const int i = band[t];
+  const int row = i / nz, z = i - row * nz;
+  atomicOr(bits + (long long)row * nzw + (z >> 5), 1u << (z & 31));
+}
+
+__global__ void k_dilate_bits_z(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, long long nwords,
+                                int nzw, int r) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nwords) return;
+  const int w = (int)(t % nzw);
+  const uint32_t cur = in[t];
+  const uint32_t prev = w > 0 ? in[t - 1] : 0u, next = w + 1 < nzw ? in[t + 1] : 0u;
+  uint32_t acc = cur;
+  for (int d = 1; d <= r; ++d) acc |= (cur << d) | (prev >> (32 - d)) | (cur >> d) | (next << (32 - d));
+  out[t] = acc;
+}
+
+// axis 1: OR over rows y - r .. y + r; axis 0: over x - r .. x + r, then the
+// margin and the bits past nz are cleared.
+__global__ void k_dilate_bits_rows(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int nx, int ny,
+                                   int nz, int nzw, int axis, int r, int margin) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nwords = (long long)nx * ny * nzw;
+  if (t >= nwords) return;
+  const int w = (int)(t % nzw);
+  const long long row = t / nzw;
+  const int x = (int)(row / ny), y = (int)(row - (long long)x * ny);
+  const int c = axis == 0 ? x : y, len = axis == 0 ? nx : ny;
+  const long long step = axis == 0 ? (long long)ny * nzw : nzw;
+  uint32_t acc = 0;
+  const int lo = max(c - r, 0), hi = min(c + r, len - 1);
+  for (int d = lo; d <= hi; ++d) acc |= in[t + (long long)(d - c) * step];
+  if (axis == 0) {
+    // valid z: margin <= z < nz - margin (margin 0: z < nz)
+    if (x < margin || y < margin || x >= nx - margin || y >= ny - margin) acc = 0;
+    const int zlo = margin - 32 * w, zhi = nz - margin - 32 * w;  // bit range [zlo, zhi)
+    const uint32_t below = zlo <= 0 ? 0u : (zlo >= 32 ? 0xffffffffu : ((1u << zlo) - 1u));
+    const uint32_t upto = zhi >= 32 ? 0xffffffffu : (zhi <= 0 ? 0u : ((1u << zhi) - 1u));
+    acc &= upto & ~below;
+  }
+  out[t] = acc;
+}
+
 inline size_t geo_bytes(long long m) { return (size_t)geo_layout(m < 1 ? 1 : m).total; }
 
 }  // namespace svie
@@ -491,6 +544,36 @@ int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int
     dilate_box(mask, mask, tmp, nx, ny, nz, dilation, margin, s, &launches);
   }
   return launch_status("svie_reinit_mask", launches);
+}
+
+size_t svie_reinit_bits_bytes(int nx, int ny, int nz) {
+  return (size_t)nx * ny * ((nz + 31) / 32) * sizeof(uint32_t);
+}
+
+int svie_reinit_bits(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin, uint32_t* bits,
+                     uint32_t* tmp, void* stream) {
+  if (!bits || !tmp || nx <= 0 || ny <= 0 || nz <= 0 || (long long)nx * ny * nz >= (1LL << 31) || dilation < 0 ||
+      dilation > 31 || margin < 0 || m < 0 || (m > 0 && !band)) {
+    set_error("svie_reinit_bits: bad arguments (dilation <= 31)");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nzw = (nz + 31) / 32;
+  const long long nwords = (long long)nx * ny * nzw;
+  if (cudaMemsetAsync(tmp, 0, (size_t)nwords * sizeof(uint32_t), s) != cudaSuccess) {
+    set_error("svie_reinit_bits: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  int launches = 3;
+  if (m > 0) {
+    k_mark_bits<<<blocks_for(m, 256), 256, 0, s>>>(band, m, nz, nzw, tmp);
+    ++launches;
+  }
+  const int nb = blocks_for(nwords, 256);
+  k_dilate_bits_z<<<nb, 256, 0, s>>>(tmp, bits, nwords, nzw, dilation);
+  k_dilate_bits_rows<<<nb, 256, 0, s>>>(bits, tmp, nx, ny, nz, nzw, 1, dilation, 0);
+  k_dilate_bits_rows<<<nb, 256, 0, s>>>(tmp, bits, nx, ny, nz, nzw, 0, dilation, margin);
+  return launch_status("svie_reinit_bits", launches);
 }
 
 size_t svie_reinit_geometry_bytes(int64_t m) { return geo_bytes(m); }

@@ -272,17 +272,22 @@ class LevelSet:
         n = self.grid.size
         nx, ny, nz = self.grid.shape
         sc = self.scratch
-        mask = sc.get("reinit_mask", n)
-        tmp = sc.get("reinit_tmp", n)
-        nat.call("svie_reinit_mask", nat.ptr(self.work32), self.work32.numel(), nx, ny, nz, int(dilation), MARGIN,
+        # the work mask (band dilated, margin cleared) as bits, listed in brick order
+        if dilation <= 31:
+            kind, nbytes, call = 2, nat.lib().svie_reinit_bits_bytes(nx, ny, nz), "svie_reinit_bits"
+        else:
+            kind, nbytes, call = 0, n, "svie_reinit_mask"
+        mask = sc.get("reinit_mask", nbytes)
+        tmp = sc.get("reinit_tmp", nbytes)
+        nat.call(call, nat.ptr(self.work32), self.work32.numel(), nx, ny, nz, int(dilation), MARGIN,
                  nat.ptr(mask), nat.ptr(tmp), nat.stream())
         ws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
         cnt = sc.get("reinit_count", 8)
-        nat.call("svie_brick_scan", 0, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
+        nat.call("svie_brick_scan", kind, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
                  nat.stream())
         m = int(cnt[:8].cpu().view(torch.int64)[0])
         idx = sc.get("reinit_idx", 4 * max(m, 1))[:4 * m].view(torch.int32)
-        nat.call("svie_brick_write", 0, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
+        nat.call("svie_brick_write", kind, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
                  nat.stream())
         geo = sc.get("reinit_geo", nat.lib().svie_reinit_geometry_bytes(m))
         nat.call("svie_reinit_geometry", nat.ptr(self.flat), nat.ptr(idx), m, *self.strides, self.h, cfl,

@@ -97,33 +97,37 @@ def main(argv=None) -> int:
         nx, ny, nz = shape
         sc = ls.scratch
         for _ in range(a.reinit):
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+            # the steps of LevelSet.reinitialize, with events between them
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
             ev[0].record()
-            mask, tmp = sc.get("reinit_mask", n), sc.get("reinit_tmp", n)
-            nat.call("svie_reinit_mask", nat.ptr(ls.band32), ls.band32.numel(), nx, ny, nz, 3, 4, nat.ptr(mask),
+            nbits = nat.lib().svie_reinit_bits_bytes(nx, ny, nz)
+            mask, tmp = sc.get("reinit_mask", nbits), sc.get("reinit_tmp", nbits)
+            nat.call("svie_reinit_bits", nat.ptr(ls.work32), ls.work32.numel(), nx, ny, nz, 3, 4, nat.ptr(mask),
                      nat.ptr(tmp), nat.stream())
             ev[1].record()
             ws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
             cnt = sc.get("reinit_count", 8)
-            nat.call("svie_brick_scan", 0, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
+            nat.call("svie_brick_scan", 2, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
                      nat.stream())
             m = int(cnt[:8].cpu().view(torch.int64)[0])
             idx = sc.get("reinit_idx", 4 * m)[:4 * m].view(torch.int32)
-            nat.call("svie_brick_write", 0, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
+            nat.call("svie_brick_write", 2, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
                      nat.stream())
+            ev[2].record()
             geo = sc.get("reinit_geo", nat.lib().svie_reinit_geometry_bytes(m))
             nat.call("svie_reinit_geometry", nat.ptr(ls.flat), nat.ptr(idx), m, *ls.strides, ls.h, 0.45, nat.ptr(geo),
                      nat.stream())
-            ev[2].record()
+            ev[3].record()
             pt = sc.get("reinit_phi", 4 * n)
             nat.call("svie_reinit_iterate", nat.ptr(ls.flat), nat.ptr(pt), n, nat.ptr(idx), m, *ls.strides, ls.h,
                      nat.ptr(geo), 20, nat.stream())
-            ev[3].record()
-            ls.rebuild_band()
             ev[4].record()
+            ls.rebuild_band()
+            ev[5].record()
             torch.cuda.synchronize()
-            t = [ev[i].elapsed_time(ev[i + 1]) for i in range(4)]
-            print("work set %d mask %.3f compact+geometry %.3f 40 sweeps %.3f rebuild %.3f ms" % (m, *t), flush=True)
+            t = [ev[i].elapsed_time(ev[i + 1]) for i in range(5)]
+            print("work set %d mask %.3f compact %.3f geometry %.3f copy+40 sweeps %.3f rebuild %.3f ms" % (m, *t),
+                  flush=True)
         return 0
     law = S.SVIPowerLaw(0.05 * 2.078, 1, 1, 0.93)
     sim = S.ErosionSimulation(ls, law)

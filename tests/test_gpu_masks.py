@@ -65,6 +65,48 @@ def test_reinit_work_mask(shape, dilation, margin):
     assert np.array_equal(out.cpu().numpy().reshape(shape).astype(bool), ref)
 
 
+@pytest.mark.parametrize("shape", SHAPES[1:])
+@pytest.mark.parametrize("dilation,margin", [(3, 4), (1, 0), (9, 4), (0, 0)])
+def test_reinit_bits_match_byte_mask(shape, dilation, margin):
+    """The bit-packed work mask lists the same nodes, in the same brick order, as the byte mask."""
+    n = int(np.prod(shape))
+    nx, ny, nz = shape
+    rng = np.random.default_rng(4)
+    band = torch.from_numpy(np.sort(rng.choice(n, size=n // 40, replace=False)).astype(np.int32)).cuda()
+    lib = nat.lib()
+    mask = torch.empty(n, dtype=torch.uint8, device="cuda")
+    tmp = torch.empty(n, dtype=torch.uint8, device="cuda")
+    nat.call("svie_reinit_mask", nat.ptr(band), band.numel(), nx, ny, nz, dilation, margin, nat.ptr(mask),
+             nat.ptr(tmp), nat.stream())
+    nb = lib.svie_reinit_bits_bytes(nx, ny, nz)
+    bits = torch.empty(nb // 4, dtype=torch.int32, device="cuda")
+    btmp = torch.empty_like(bits)
+    nat.call("svie_reinit_bits", nat.ptr(band), band.numel(), nx, ny, nz, dilation, margin, nat.ptr(bits),
+             nat.ptr(btmp), nat.stream())
+    # unpack: bit z % 32 of word z // 32 of row (x, y)
+    w = bits.cpu().numpy().view(np.uint32).reshape(nx, ny, -1)
+    z = np.arange(nz)
+    unpacked = (w[:, :, z // 32] >> (z % 32).astype(np.uint32)) & 1
+    assert np.array_equal(unpacked.astype(bool), mask.cpu().numpy().reshape(shape).astype(bool))
+    # no bits past nz
+    if nz % 32:
+        assert not (w[:, :, -1] >> np.uint32(nz % 32)).any()
+    bws = torch.empty(lib.svie_brick_workspace_bytes(nx, ny, nz), dtype=torch.uint8, device="cuda")
+    lists = []
+    for kind, src in ((0, mask), (2, bits)):
+        cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+        nat.call("svie_brick_scan", kind, nat.ptr(src), nx, ny, nz, 0.0, nat.ptr(bws), bws.numel(), nat.ptr(cnt),
+                 nat.stream())
+        k = int(cnt.item())
+        out = torch.full((max(k, 1),), -1, dtype=torch.int32, device="cuda")
+        nat.call("svie_brick_write", kind, nat.ptr(src), nx, ny, nz, 0.0, nat.ptr(bws), bws.numel(), nat.ptr(out), k,
+                 nat.stream())
+        lists.append(out[:k].cpu().numpy())
+    assert np.array_equal(lists[0], lists[1])
+    ref = np.flatnonzero(mask.cpu().numpy())
+    assert np.array_equal(lists[1], _brick_order(ref, shape))
+
+
 def _brick_order(idx, shape):
     nx, ny, nz = shape
     x, r = np.divmod(idx, ny * nz)
