@@ -377,6 +377,24 @@ SVIE_DEV float2* stage_twiddles_to_smem(float2* sm, int PS, const AxisPlan& P) {
   return stw;
 }
 
+// 16-byte asynchronous global -> shared copies (L2 only), completed by groups.
+SVIE_DEV void cp_async16(void* smem, const void* gmem) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+// 8- and 4-byte forms (cached in L1 as well: the only forms for these sizes).
+SVIE_DEV void cp_async8(void* smem, const void* gmem) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+SVIE_DEV void cp_async4(void* smem, const void* gmem) {
+  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+SVIE_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+SVIE_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // ----------------------------------------------------------------- z passes
 // Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
 // A CTA takes 2 LW real lines, packed in pairs into LW complex lines (one
@@ -405,28 +423,23 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ i
       return;
     }
   }
-  const float2* stw = stage_twiddles_to_smem(sm, PS, P);
+  // the whole tile in flight at once: 4-byte asynchronous copies straight into
+  // the paired layout, lanes along (z, line of the pair) so that both the
+  // global reads (two 64-byte runs) and the shared writes are contiguous
+  float* sf = reinterpret_cast<float*>(sa);
   for (int w = warp; w < LW; w += NW) {
-    const int l0 = 2 * w, l1 = 2 * w + 1;
-    const bool ok0 = l0 < nl && (!lineflag || (__ldg(lineflag + line0 + l0) & 1));
-    const bool ok1 = l1 < nl && (!lineflag || (__ldg(lineflag + line0 + l1) & 1));
-    const float* g0 = src + (long long)l0 * n;
-    const float* g1 = g0 + n;
-    int z = lane;
-    // eight positions of both lines in flight per thread before the stores
-    for (; z + 7 * 32 < n; z += 8 * 32) {
-      float a[8], b[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        a[u] = ok0 ? __ldg(g0 + z + 32 * u) : 0.0f;
-        b[u] = ok1 ? __ldg(g1 + z + 32 * u) : 0.0f;
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) sa[(z + 32 * u) * PS + w] = make_float2(a[u], b[u]);
+    const int par = lane & 1, l = 2 * w + par;
+    const bool ok = l < nl && (!lineflag || (__ldg(lineflag + line0 + l) & 1));
+    const float* g = src + (long long)l * n;
+    for (int z = lane >> 1; z < n; z += 16) {
+      float* d = sf + 2 * (z * PS + w) + par;
+      if (ok) cp_async4(d, g + z);
+      else *d = 0.0f;
     }
-    for (; z < n; z += 32)
-      sa[z * PS + w] = make_float2(ok0 ? __ldg(g0 + z) : 0.0f, ok1 ? __ldg(g1 + z) : 0.0f);
   }
+  cp_async_commit();
+  const float2* stw = stage_twiddles_to_smem(sm, PS, P);
+  cp_async_wait<0>();
   __syncthreads();
   const float2* r = run_tile_fft<LW, PS>(sa, sb, P, stw);
   // untangle the two real spectra of each pair: X1 = (C_k + conj C_{n-k}) / 2,
@@ -534,7 +547,7 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
                                                        int ninner, long long outer_stride, int mode, KGeom K,
                                                        const uint8_t* __restrict__ slabflag, int need) {
   if (slabflag && !(__ldg(slabflag + blockIdx.y) & need)) return;
-  extern __shared__ float2 sm[];
+  extern __shared__ __align__(16) float2 sm[];
   constexpr int KS = FFT_T / LW;  // rows per sweep of the CTA
   const int n = P.n;
   float2* sa = sm;
@@ -542,40 +555,32 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
   const int c0 = blockIdx.x * LW;
   const int nl = min(LW, ninner - c0);
   float2* base = data + (long long)blockIdx.y * outer_stride + c0;
+  // the whole tile in flight at once: asynchronous copies of the row segments
+  // (LW = 8: whole 64-byte segments of the padded rows, the columns past
+  // ninner included and never stored; LW = 1: one value per row)
+  if (LW == 8) {
+    for (int e = threadIdx.x; e < 4 * n; e += FFT_T) {
+      const int row = e >> 2, part = 2 * (e & 3);
+      cp_async16(sa + row * LW + part, base + row * stride + part);
+    }
+  } else {
+    for (int row = threadIdx.x; row < n; row += FFT_T) cp_async8(sa + row, base + row * stride);
+  }
+  cp_async_commit();
   const float2* stw = stage_twiddles_to_smem(sm, LW, P);
   if (mode == 2)
     for (int e = threadIdx.x; e < n - 1; e += FFT_T) sm[2 * LW * n + n + e] = __ldg(P.rstw + e);
   const int c = threadIdx.x % LW, k0 = threadIdx.x / LW;
   const bool col = c < nl;
   const long long rstep = KS * stride;
-  {
-    const float2* g = base + (long long)k0 * stride + c;
-    int k = k0;
-    // eight loads in flight per thread before the shared-memory stores; the
-    // lines past the slab's end are zero
-    for (; k + 7 * KS < n; k += 8 * KS, g += 8 * rstep) {
-      float2 v[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = col ? g[u * rstep] : make_float2(0.f, 0.f);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        if (mode == 1) v[u].y = -v[u].y;
-        sa[(k + KS * u) * LW + c] = v[u];
-      }
-    }
-    for (; k < n; k += KS, g += rstep) {
-      float2 v = col ? *g : make_float2(0.f, 0.f);
-      if (mode == 1) v.y = -v.y;
-      sa[k * LW + c] = v;
-    }
-  }
+  cp_async_wait<0>();
   __syncthreads();
   const int nst = P.nst;
   int p = 1;
-  float2* r = run_stages<LW, LW, FFT_T>(sa, sb, n, P.radices, 0, nst - 1, stw, false, p);
+  float2* r = run_stages<LW, LW, FFT_T>(sa, sb, n, P.radices, 0, nst - 1, stw, mode == 1, p);
   const int Rl = radix_of(P.radices, nst - 1);
   if (mode != 2) {
-    run_last<LW, LW, FFT_T>(r, n, Rl, stw, false, StoreEpi{base, stride, nl, mode != 0});
+    run_last<LW, LW, FFT_T>(r, n, Rl, stw, mode == 1 && nst == 1, StoreEpi{base, stride, nl, mode != 0});
     return;
   }
   // forward, then K^ and the first inverse stage in one pass, then the rest
@@ -601,15 +606,6 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
   float2* r2 = run_stages<LW, LW, FFT_T>(o, r, n, P.rradices, 1, nst - 1, rstw, false, p2);
   run_last<LW, LW, FFT_T>(r2, n, radix_of(P.rradices, nst - 1), rstw, false, StoreEpi{base, stride, nl, true});
 }
-
-// 16-byte asynchronous global -> shared copies (L2 only), completed by groups.
-SVIE_DEV void cp_async16(void* smem, const void* gmem) {
-  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-SVIE_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-SVIE_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // Persistent form of the 8-line strided pass: each CTA walks the tiles
 // t = blockIdx.x, + gridDim.x, ... (tile t: column block t % ncb of outer slab
