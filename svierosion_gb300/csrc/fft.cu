@@ -457,6 +457,28 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ i
   }
 }
 
+// Real lines 2w (real parts) and 2w + 1 (imaginary parts, negated: the
+// inverse-by-forward transform) of the tile to dst = out + line0 * n,
+// out = beta + alpha * value; with `lineflag`, only lines with bit 1.
+template <int LW, int PS>
+SVIE_DEV void c2r_store(const float2* __restrict__ r, float* __restrict__ dst, int n, int nl, long long line0,
+                        float alpha, float beta, const uint8_t* __restrict__ lineflag) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = FFT_T / 32;
+  for (int w = warp; 2 * w < nl; w += NW) {
+    const int l0 = 2 * w, l1 = 2 * w + 1;
+    const bool w0 = !lineflag || (__ldg(lineflag + line0 + l0) & 2);
+    const bool w1 = l1 < nl && (!lineflag || (__ldg(lineflag + line0 + l1) & 2));
+    if (!w0 && !w1) continue;
+    float* d0 = dst + (long long)l0 * n;
+    for (int z = lane; z < n; z += 32) {
+      const float2 v = r[z * PS + w];
+      if (w0) d0[z] = beta + alpha * v.x;
+      if (w1) d0[n + z] = beta + alpha * (-v.y);
+    }
+  }
+}
+
 // Inverse: half spectra -> real lines, out = beta + alpha * irfft_unnormalised.
 // `lineflag` (optional): only lines with bit 1 set are written (the others
 // are never read); a tile without such lines returns at once.
@@ -476,8 +498,43 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
   }
   const float2* src = in + line0 * nzp;
   const bool even = (n & 1) == 0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nzh = n / 2 + 1;
   constexpr int NW = FFT_T / 32;
+  // C_k = X1_k + i X2_k over k = 0..n-1 (X_{n-k} = conj X_k), stored
+  // conjugated for the inverse-by-forward transform
+  auto combine = [&](float2 a, float2 b, int k, int kk) {
+    if (kk == 0 || (even && kk == n / 2)) { a.y = 0.f; b.y = 0.f; }
+    if (k > n / 2) { a.y = -a.y; b.y = -b.y; }
+    return make_float2(a.x - b.y, -(a.y + b.x));
+  };
+  if (2 * LW * nzh <= PS * n) {
+    // the 2 LW half spectra land in the idle second buffer with 8-byte
+    // asynchronous copies (all in flight at once), then C is built from there
+    for (int l = warp; l < 2 * LW; l += NW) {
+      float2* d = sb + l * nzh;
+      const float2* g = src + (long long)l * nzp;
+      for (int k = lane; k < nzh; k += 32) {
+        if (l < nl) cp_async8(d + k, g + k);
+        else d[k] = make_float2(0.f, 0.f);
+      }
+    }
+    cp_async_commit();
+    const float2* stw = stage_twiddles_to_smem(sm, PS, P);
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int w = warp; w < LW; w += NW) {
+      const float2* x1 = sb + (2 * w) * nzh;
+      const float2* x2 = x1 + nzh;
+      for (int k = lane; k < n; k += 32) {
+        const int kk = k > n / 2 ? n - k : k;
+        sa[k * PS + w] = combine(x1[kk], x2[kk], k, kk);
+      }
+    }
+    __syncthreads();
+    const float2* r = run_tile_fft<LW, PS>(sa, sb, P, stw);
+    c2r_store<LW, PS>(r, out + line0 * n, n, nl, line0, alpha, beta, lineflag);
+    return;
+  }
   const float2* stw = stage_twiddles_to_smem(sm, PS, P);
   for (int w = warp; w < LW; w += NW) {
     const bool has1 = 2 * w < nl, has2 = 2 * w + 1 < nl;
@@ -497,31 +554,14 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
       for (int u = 0; u < 4; ++u) {
         const int k = k0 + 32 * u;
         if (k >= n) break;
-        const bool mirror = k > n / 2;
-        const int kk = mirror ? n - k : k;
-        float2 a = x1[u], b = x2[u];
-        if (kk == 0 || (even && kk == n / 2)) { a.y = 0.f; b.y = 0.f; }
-        if (mirror) { a.y = -a.y; b.y = -b.y; }
-        // C = X1 + i X2, stored conjugated for the inverse-by-forward transform
-        sa[k * PS + w] = make_float2(a.x - b.y, -(a.y + b.x));
+        const int kk = k > n / 2 ? n - k : k;
+        sa[k * PS + w] = combine(x1[u], x2[u], k, kk);
       }
     }
   }
   __syncthreads();
   const float2* r = run_tile_fft<LW, PS>(sa, sb, P, stw);
-  float* dst = out + line0 * n;
-  for (int w = warp; 2 * w < nl; w += NW) {
-    const int l0 = 2 * w, l1 = 2 * w + 1;
-    const bool w0 = !lineflag || (__ldg(lineflag + line0 + l0) & 2);
-    const bool w1 = l1 < nl && (!lineflag || (__ldg(lineflag + line0 + l1) & 2));
-    if (!w0 && !w1) continue;
-    float* d0 = dst + (long long)l0 * n;
-    for (int z = lane; z < n; z += 32) {
-      const float2 v = r[z * PS + w];
-      if (w0) d0[z] = beta + alpha * v.x;
-      if (w1) d0[n + z] = beta + alpha * (-v.y);
-    }
-  }
+  c2r_store<LW, PS>(r, out + line0 * n, n, nl, line0, alpha, beta, lineflag);
 }
 
 // ------------------------------------------------------------ strided passes
