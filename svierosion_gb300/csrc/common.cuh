@@ -268,11 +268,50 @@ SVIE_DEV float cell_fraction_at(const float* __restrict__ f, int i, int sx, int 
   return cube_plane_fraction(c * rg, hi, mid, lo);
 }
 
+// Exact n / d for 0 <= n < 2^31 and 1 <= d < 2^31 by one multiply and a
+// shift (T. Granlund and P. L. Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994): with l = ceil(log2 d) and
+// m = ceil(2^(31 + l) / d) < 2^32, n / d = (n m) >> (31 + l).
+struct DivMagic {
+  unsigned int m;
+  int s;
+};
+inline DivMagic div_magic(int d) {
+  int l = 0;
+  while ((1LL << l) < d) ++l;
+  const unsigned long long m = ((1ULL << (31 + l)) + (unsigned long long)d - 1) / (unsigned long long)d;
+  return DivMagic{(unsigned int)m, 31 + l};
+}
+SVIE_DEV int div_exact(int n, DivMagic g) { return (int)(((unsigned long long)(unsigned int)n * g.m) >> g.s); }
+
+// Grid constants of the closest-point projection: strides with their
+// division constants, clamp bounds hi = (n - 3.001) rounded to float, the
+// spacing and its correctly rounded reciprocal.
+struct CpGeom {
+  int sx, sy;
+  DivMagic dsx, dsy;
+  float hx, hy, hz, h, rh;
+};
+inline CpGeom cp_geom(int ny, int nz, float hx, float hy, float hz, float h) {
+  CpGeom g;
+  g.sx = ny * nz;
+  g.sy = nz;
+  g.dsx = div_magic(g.sx);
+  g.dsy = div_magic(g.sy);
+  g.hx = hx;
+  g.hy = hy;
+  g.hz = hz;
+  g.h = h;
+  g.rh = rn_reciprocal(h);
+  return g;
+}
+
 // First Newton projection to the zero set (reference kernels.py:185-208).
-// hi = (nx-3.001, ny-3.001, nz-3.001) rounded to float.
-SVIE_DEV float3 closest_point_at(const float* __restrict__ f, int i, int ny, int nz, float hx, float hy,
-                                 float hz, float h) {
-  const int sx = ny * nz, sy = nz;
+// The division by h uses the correctly rounded reciprocal (div_by), the node
+// coordinates the exact multiply-shift division: same results as the plain
+// operations.
+SVIE_DEV float3 closest_point_at(const float* __restrict__ f, int i, const CpGeom& G) {
+  const int sx = G.sx, sy = G.sy;
   const float* q = f + i;
   float c = __ldg(q);
   float gx = 0.5f * (__ldg(q + sx) - __ldg(q - sx));
@@ -281,16 +320,16 @@ SVIE_DEV float3 closest_point_at(const float* __restrict__ f, int i, int ny, int
   float g2 = fmaxf(gx * gx + gy * gy + gz * gz, 1e-30f);
   float ac = fabsf(c);
   float length = ac / sqrtf(g2);
-  float cap = 1.25f * ac / h + 0.25f;
+  float cap = div_by(1.25f * ac, G.h, G.rh) + 0.25f;
   float scale = (c / g2) * fminf(cap / fmaxf(length, 1e-30f), 1.0f);
-  const int ii = i / sx, rem = i - ii * sx, jj = rem / sy;
+  const int ii = div_exact(i, G.dsx), rem = i - ii * sx, jj = div_exact(rem, G.dsy);
   float fi = (float)ii;
   float fj = (float)jj;
   float fk = (float)(rem - jj * sy);
   float3 p;
-  p.x = fminf(fmaxf(fi - scale * gx, 1.0f), hx);
-  p.y = fminf(fmaxf(fj - scale * gy, 1.0f), hy);
-  p.z = fminf(fmaxf(fk - scale * gz, 1.0f), hz);
+  p.x = fminf(fmaxf(fi - scale * gx, 1.0f), G.hx);
+  p.y = fminf(fmaxf(fj - scale * gy, 1.0f), G.hy);
+  p.z = fminf(fmaxf(fk - scale * gz, 1.0f), G.hz);
   return p;
 }
 

@@ -27,6 +27,7 @@ struct StageConst {
   // 0: alpha = 1, 1: alpha < 1, 2: alpha > 1
   float alpha, am1, am2, delta;
   int amode;
+  CpGeom cp;  // the closest-point projection's grid constants
 };
 
 static StageConst stage_const(const svie_law& L, int nx, int ny, int nz) {
@@ -46,6 +47,7 @@ static StageConst stage_const(const svie_law& L, int nx, int ny, int nz) {
   c.am2 = (float)(L.alpha - 2.0);
   c.delta = (float)L.delta;
   c.amode = L.alpha == 1.0 ? 0 : (L.alpha < 1.0 ? 1 : 2);
+  c.cp = cp_geom(ny, nz, c.hx, c.hy, c.hz, c.h);
   return c;
 }
 
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(SG_THREADS, 6) k_stage_svi(const float* __rest
   if (t < m) {
     const int i = band[t];
     const float c = __ldg(phi + i);
-    const float3 p = closest_point_at(phi, i, ny, nz, C.hx, C.hy, C.hz, C.h);
+    const float3 p = closest_point_at(phi, i, C.cp);
     const float N = tricubic_at(Nd, ny, nz, p);
     float V = svi_speed(N, L, C);
     if (st) {
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(SG_THREADS) k_stage_curv(const float* __restri
   if (t < m) {
     const int i = band[t];
     const float c = __ldg(phi + i);
-    const float3 p = closest_point_at(phi, i, ny, nz, C.hx, C.hy, C.hz, C.h);
+    const float3 p = closest_point_at(phi, i, C.cp);
     const float k1 = trilinear_at(kd, ny, nz, p, 2, 0);
     const float k2 = trilinear_at(kd, ny, nz, p, 2, 1);
     float V, D;

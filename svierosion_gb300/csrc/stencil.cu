@@ -27,11 +27,11 @@ __global__ void k_fractions(const float* __restrict__ f, const int32_t* __restri
   if (scatter) out[i] = v; else out[t] = v;
 }
 
-__global__ void k_closest(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int ny,
-                          int nz, float hx, float hy, float hz, float h, float* __restrict__ out) {
+__global__ void k_closest(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, CpGeom G,
+                          float* __restrict__ out) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  float3 p = closest_point_at(f, idx[t], ny, nz, hx, hy, hz, h);
+  float3 p = closest_point_at(f, idx[t], G);
   out[3 * t] = p.x;
   out[3 * t + 1] = p.y;
   out[3 * t + 2] = p.z;
@@ -182,8 +182,8 @@ int svie_scatter_fractions(const float* phi, const int32_t* band, int64_t m, int
 int svie_closest_points(const float* flat, const int32_t* idx, int64_t m, int ny, int nz, float hi_x,
                         float hi_y, float hi_z, float h, float* out, void* stream) {
   SVIE_CHECK_M("svie_closest_points", m);
-  k_closest<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(flat, idx, m, ny, nz, hi_x,
-                                                                                 hi_y, hi_z, h, out);
+  k_closest<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(
+      flat, idx, m, cp_geom(ny, nz, hi_x, hi_y, hi_z, h), out);
   return launch_status("svie_closest_points");
 }
 
@@ -274,10 +274,11 @@ __global__ void k_central_gradient(const float* __restrict__ f, const int32_t* _
 // first projection from the central gradient, then Newton steps on the
 // tricubic interpolant with the same step cap, clamped to [1, n - 3.001].
 __global__ void k_closest_newton(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int ny,
-                                 int nz, float hx, float hy, float hz, float h, int steps, float* __restrict__ out) {
+                                 int nz, CpGeom G, int steps, float* __restrict__ out) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  float3 p = closest_point_at(f, idx[t], ny, nz, hx, hy, hz, h);
+  float3 p = closest_point_at(f, idx[t], G);
+  const float hx = G.hx, hy = G.hy, hz = G.hz, h = G.h;
   const long long syz = (long long)ny * nz;
   for (int s = 1; s < steps; ++s) {
     float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
@@ -335,7 +336,7 @@ int svie_closest_points_newton(const float* flat, const int32_t* idx, int64_t m,
     return SVIE_ERR_ARG;
   }
   k_closest_newton<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(
-      flat, idx, m, ny, nz, hi_x, hi_y, hi_z, h, newton_steps, out);
+      flat, idx, m, ny, nz, cp_geom(ny, nz, hi_x, hi_y, hi_z, h), newton_steps, out);
   return launch_status("svie_closest_points_newton");
 }
 
