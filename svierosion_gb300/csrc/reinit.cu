@@ -238,14 +238,14 @@ SVIE_DEV int dist_offset(const Geo& g, long long t, uint32_t flags) {
   return f6 ? __ldg(g.wbase + (t >> 5)) + off : 0;
 }
 
-// reinit_rhs (kernels.py:363-379) at work-set entry t.  Divisions by h use
-// the correctly rounded reciprocal rh (div_by); hh = RN(h * h).  Also returns
+// reinit_rhs (kernels.py:363-379) at work-set entry t.  Divisions by h and by
+// hh = RN(h * h) use the correctly rounded reciprocals rh and rhh (div_by).  Also returns
 // hmin = min(h, stored distances of the flagged crossings), from which
 // dtau = cfl * max(hmin, 1e-3 h) is rebuilt exactly as geometry_at computed
 // it (a distance below 1e-6 h, stored clamped to 1e-6 h, gives the same
 // 1e-3 h either way).  `off`: the node's first distance (dist_offset).
 SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, int off, uint32_t flags, int sx,
-                             int sy, int sz, float h, float rh, float hh, float& hmin) {
+                             int sy, int sz, float h, float rh, float hh, float rhh, float& hmin) {
   const float* qp = f + i;
   const float c = __ldg(qp);
   const float sgn = meta_sgn(flags);
@@ -272,12 +272,12 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, i
     float Dm = div_by(c - m1 + 0.5f * mm_m, h, rh);
     if ((flags >> (2 * a)) & 1u) {
       const float xp = __ldg(dn + __popc(flags & ((1u << (2 * a)) - 1u)));
-      Dp = -c / xp - 0.5f * xp * mm_p / hh;
+      Dp = -c / xp - div_by(0.5f * xp * mm_p, hh, rhh);
       hmin = fminf(hmin, xp);
     }
     if ((flags >> (2 * a + 1)) & 1u) {
       const float xm = __ldg(dn + __popc(flags & ((1u << (2 * a + 1)) - 1u)));
-      Dm = c / xm + 0.5f * xm * mm_m / hh;
+      Dm = c / xm + div_by(0.5f * xm * mm_m, hh, rhh);
       hmin = fminf(hmin, xm);
     }
     const float a1 = outside ? fmaxf(Dm, 0.0f) : fminf(Dm, 0.0f);
@@ -289,7 +289,7 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, i
 
 __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
                                                              const int32_t* __restrict__ idx, long long m, int sx,
-                                                             int sy, int sz, float h, float rh, void* geo,
+                                                             int sy, int sz, float h, float rh, float rhh, void* geo,
                                                              int second) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   Geo g = geo_view(geo, m);
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
   const float cfl = __ldg(g.cfl);
   const int i = __ldg(idx + t);
   float hmin;
-  const float r = reinit_rhs_at(src, i, g, off, flags, sx, sy, sz, h, rh, h * h, hmin);
+  const float r = reinit_rhs_at(src, i, g, off, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
   const float dtau = cfl * fmaxf(hmin, 1e-3f * h);
   if (!second) {
     dst[i] = src[i] + dtau * r;  // u0 + dtau rhs(A)
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
 }
 
 __global__ void k_reinit_rhs(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx, int sy,
-                             int sz, float h, float rh, void* geo, float* out) {
+                             int sz, float h, float rh, float rhh, void* geo, float* out) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   Geo g = geo_view(geo, m);
   const bool act = t < m;
@@ -319,7 +319,7 @@ __global__ void k_reinit_rhs(const float* __restrict__ f, const int32_t* __restr
   const int off = dist_offset(g, t, flags);
   if (!act) return;
   float hmin;
-  out[t] = reinit_rhs_at(f, idx[t], g, off, flags, sx, sy, sz, h, rh, h * h, hmin);
+  out[t] = reinit_rhs_at(f, idx[t], g, off, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
 }
 
 __global__ void k_mark(const int32_t* __restrict__ band, long long m, uint8_t* __restrict__ mask) {
@@ -608,10 +608,10 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
     return SVIE_ERR_LAUNCH;
   }
   const int nb = blocks_for(m, RI_THREADS);
-  const float rh = rn_reciprocal(h);
+  const float rh = rn_reciprocal(h), rhh = rn_reciprocal(h * h);
   for (int it = 0; it < iterations; ++it) {
-    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, const_cast<void*>(geo), 0);
-    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, const_cast<void*>(geo), 1);
+    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, const_cast<void*>(geo), 0);
+    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, rhh, const_cast<void*>(geo), 1);
   }
   return launch_status("svie_reinit_iterate", 2 * iterations);
 }
@@ -620,7 +620,7 @@ int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx,
                     const void* geo, float* out, void* stream) {
   if (m <= 0) return m < 0 ? SVIE_ERR_ARG : SVIE_OK;
   k_reinit_rhs<<<blocks_for(m, RI_THREADS), RI_THREADS, 0, (cudaStream_t)stream>>>(
-      phi, idx, m, sx, sy, sz, h, rn_reciprocal(h), const_cast<void*>(geo), out);
+      phi, idx, m, sx, sy, sz, h, rn_reciprocal(h), rn_reciprocal(h * h), const_cast<void*>(geo), out);
   return launch_status("svie_reinit_rhs");
 }
 
