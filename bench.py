@@ -214,8 +214,9 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- our arm
-def algorithmic_bytes(shape, band: int) -> dict:
-    """Compulsory bytes per launch of each kernel (one-pass counting)."""
+def algorithmic_bytes(shape, band: int, work: int = 0) -> dict:
+    """Compulsory bytes per launch of each kernel (one-pass counting); work: the
+    mean reinitialisation work set (band dilated by 3)."""
     nx, ny, nz = shape
     G = nx * ny * nz
     S = nx * ny * (nz // 2 + 1)
@@ -231,6 +232,8 @@ def algorithmic_bytes(shape, band: int) -> dict:
         "scatter_fractions": 8 * band,
         "rk_stage": 16 * band,       # idx, u0, L read, phi written
         "volume": 8 * band,          # idx + phi (fractions recomputed)
+        # one pseudo-time sweep: read and write phi at every work node (8 B per node)
+        "reinit_sweep": 8 * work,
     }
 
 
@@ -256,9 +259,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     t_setup = time.time() - t_setup
     band0 = ls.work32.numel()
     sim.run(target_fraction=None, max_steps=args.warmup)
-    # timed region: events only around the convolution passes (the roofline
-    # kernel); the full per-kernel breakdown comes from a second pass below
-    timer = KernelTimer(capacity=32 * args.steps + 64, only={"fft"})
+    # timed region: events only around the convolution passes and the
+    # reinitialisation sweeps (the roofline candidates); the full per-kernel
+    # breakdown comes from a second pass below
+    timer = KernelTimer(capacity=32 * args.steps + 64, only={"fft", "reinit_sweep"})
     sim.timer = timer
     lib = nat.lib()
     if world > 1:
@@ -312,7 +316,16 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     except (OSError, KeyError, ValueError):
         peak, peak_src = 6800.0, "fallback"
     band_mean = updates / max(args.steps, 1)
-    abytes = algorithmic_bytes(grid.shape, int(band_mean))
+    def _work_mean(t):
+        w = t.notes.get("reinit_work", [])
+        return int(sum(w) / len(w)) if w else 0
+
+    # bytes per launch for the breakdown pass's kernels; the roofline below
+    # pairs each duration with the work sizes of the pass it was timed in
+    abytes = algorithmic_bytes(grid.shape, int(band_mean), _work_mean(timer2))
+    abytes_timed = algorithmic_bytes(grid.shape, int(band_mean), _work_mean(timer))
+    if not _work_mean(timer2):
+        abytes.pop("reinit_sweep")
     single = {k: v for k, v in kt.items() if k in abytes}
     dom = max(single.items(), key=lambda kv: kv[1]["total_ms"])[0] if single else None
     kern = {}
@@ -323,8 +336,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
                    "gbs": round(b / (v["mean_ms"] * 1e6), 1) if b else None}
     roof = None
     if dom is not None:
-        dur = kt_timed[dom] if dom in kt_timed else kt[dom]
-        ach = abytes[dom] / (dur["mean_ms"] * 1e6)
+        timed = dom in kt_timed
+        dur = kt_timed[dom] if timed else kt[dom]
+        dbytes = abytes_timed[dom] if timed else abytes[dom]
+        ach = dbytes / (dur["mean_ms"] * 1e6)
         traffic = None
         tfile = ROOT / "profiles" / "traffic.json"
         if tfile.exists():
@@ -334,7 +349,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
                 traffic = None
         roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(ach / peak, 4), "traffic": traffic, "peak_source": peak_src,
-                "algorithmic_bytes_per_launch": abytes[dom], "launches_timed": dur["launches"],
+                "algorithmic_bytes_per_launch": dbytes, "launches_timed": dur["launches"],
                 "duration_source": "timed region" if dom in kt_timed else "breakdown pass"}
     step_bytes = 3 * (12 * grid.size + 20 * band_mean) + 4 * grid.size
     out = {

@@ -267,8 +267,11 @@ class LevelSet:
         return torch.minimum(p.clamp_min(1.0), hi)
 
     # --------------------------------------------------- reinitialisation
-    def reinitialize(self, iterations: int = 12, cfl: float = 0.45, dilation: int = 3) -> None:
-        """Subcell-fixed PDE reinitialisation (Min 2010) on the dilated band (levelset.py:154-183)."""
+    def reinitialize(self, iterations: int = 12, cfl: float = 0.45, dilation: int = 3, timer=None) -> None:
+        """Subcell-fixed PDE reinitialisation (Min 2010) on the dilated band (levelset.py:154-183).
+
+        ``timer`` (optional profiling.KernelTimer): events around the sweeps
+        ("reinit_sweep", 2 iterations launches) and the work-set size."""
         n = self.grid.size
         nx, ny, nz = self.grid.shape
         sc = self.scratch
@@ -293,8 +296,16 @@ class LevelSet:
         nat.call("svie_reinit_geometry", nat.ptr(self.flat), nat.ptr(idx), m, *self.strides, self.h, cfl,
                  nat.ptr(geo), nat.stream())
         phi_tmp = sc.get("reinit_phi", 4 * n)
+        timed = timer is not None and timer.wants("reinit_sweep") and m > 0 and iterations > 0
+        if timed:
+            ev = timer.take(2)
+            ev[0].record()
         nat.call("svie_reinit_iterate", nat.ptr(self.flat), nat.ptr(phi_tmp), n, nat.ptr(idx), m, *self.strides,
                  self.h, nat.ptr(geo), int(iterations), nat.stream())
+        if timed:
+            ev[1].record()
+            timer.add(["reinit_sweep"], ev, [2 * int(iterations)])
+            timer.note("reinit_work", m)
         self.rebuild_band()
 
 

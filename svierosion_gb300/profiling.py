@@ -25,7 +25,8 @@ class KernelTimer:
             e.record()
         torch.cuda.synchronize()
         self.next = 0
-        self.groups = []  # (names, events)
+        self.groups = []  # (names, events, launches)
+        self.notes = {}
 
     def wants(self, name: str) -> bool:
         return self.only is None or name in self.only
@@ -41,22 +42,31 @@ class KernelTimer:
     def handles(evs) -> ctypes.Array:
         return (ctypes.c_void_p * len(evs))(*[ctypes.c_void_p(e.cuda_event) for e in evs])
 
-    def add(self, names, evs) -> None:
-        self.groups.append((list(names), evs))
+    def add(self, names, evs, launches=None) -> None:
+        """Event pairs (evs[i], evs[i + 1]) for names[i]; ``launches[i]``: the
+        kernel launches the pair brackets (default 1)."""
+        self.groups.append((list(names), evs, list(launches) if launches is not None else [1] * len(names)))
+
+    def note(self, key: str, value) -> None:
+        """A value recorded beside the timings (e.g. the work-set size of a call)."""
+        self.notes.setdefault(key, []).append(value)
 
     def reset(self) -> None:
         self.next = 0
         self.groups = []
+        self.notes = {}
 
     def summary(self) -> dict:
         """name -> {"launches": n, "total_ms": t, "mean_ms": t / n}."""
         torch.cuda.synchronize()
-        acc = defaultdict(list)
-        for names, evs in self.groups:
+        tot = defaultdict(float)
+        cnt = defaultdict(int)
+        for names, evs, launches in self.groups:
             for i, nm in enumerate(names):
-                acc[nm].append(evs[i].elapsed_time(evs[i + 1]))
-        return {k: {"launches": len(v), "total_ms": float(sum(v)), "mean_ms": float(sum(v) / len(v))}
-                for k, v in acc.items()}
+                tot[nm] += evs[i].elapsed_time(evs[i + 1])
+                cnt[nm] += launches[i]
+        return {k: {"launches": cnt[k], "total_ms": float(tot[k]), "mean_ms": float(tot[k] / max(cnt[k], 1))}
+                for k in tot}
 
 
 def _synthetic_levelset(shape, h):
