@@ -78,6 +78,21 @@ struct Geo {
   long long m;
 };
 
+// The same view built on the host (the sweeps take it as a kernel argument
+// instead of deriving the offsets from m in every thread).
+inline Geo geo_view_host(void* base, long long m) {
+  const GeoLayout L = geo_layout(m);
+  char* b = (char*)base;
+  Geo g;
+  g.dtau = (float*)b;
+  g.meta = (uint8_t*)(b + L.meta);
+  g.wbase = (int*)(b + L.wbase);
+  g.dist = (float*)(b + L.dist);
+  g.cfl = (float*)(b + L.cfl);
+  g.m = m;
+  return g;
+}
+
 SVIE_DEV Geo geo_view(void* base, long long m) {
   const GeoLayout L = geo_layout(m);
   char* b = (char*)base;
@@ -289,10 +304,9 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, i
 
 __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
                                                              const int32_t* __restrict__ idx, long long m, int sx,
-                                                             int sy, int sz, float h, float rh, float rhh, void* geo,
+                                                             int sy, int sz, float h, float rh, float rhh, Geo g,
                                                              int second) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  Geo g = geo_view(geo, m);
   const bool act = t < m;
   const uint32_t flags = act ? __ldg(g.meta + t) : 0u;
   const int off = dist_offset(g, t, flags);
@@ -311,9 +325,8 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
 }
 
 __global__ void k_reinit_rhs(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx, int sy,
-                             int sz, float h, float rh, float rhh, void* geo, float* out) {
+                             int sz, float h, float rh, float rhh, Geo g, float* out) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  Geo g = geo_view(geo, m);
   const bool act = t < m;
   const uint32_t flags = act ? g.meta[t] : 0u;
   const int off = dist_offset(g, t, flags);
@@ -609,9 +622,10 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
   }
   const int nb = blocks_for(m, RI_THREADS);
   const float rh = rn_reciprocal(h), rhh = rn_reciprocal(h * h);
+  const Geo g = geo_view_host(const_cast<void*>(geo), m);
   for (int it = 0; it < iterations; ++it) {
-    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, const_cast<void*>(geo), 0);
-    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, rhh, const_cast<void*>(geo), 1);
+    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, g, 0);
+    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, rhh, g, 1);
   }
   return launch_status("svie_reinit_iterate", 2 * iterations);
 }
@@ -620,7 +634,8 @@ int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx,
                     const void* geo, float* out, void* stream) {
   if (m <= 0) return m < 0 ? SVIE_ERR_ARG : SVIE_OK;
   k_reinit_rhs<<<blocks_for(m, RI_THREADS), RI_THREADS, 0, (cudaStream_t)stream>>>(
-      phi, idx, m, sx, sy, sz, h, rn_reciprocal(h), rn_reciprocal(h * h), const_cast<void*>(geo), out);
+      phi, idx, m, sx, sy, sz, h, rn_reciprocal(h), rn_reciprocal(h * h), geo_view_host(const_cast<void*>(geo), m),
+      out);
   return launch_status("svie_reinit_rhs");
 }
 
