@@ -8,6 +8,8 @@
 // Each TVD-RK2 iteration is two Jacobi sweeps between the level-set grid A and
 // a second dense grid B that mirrors A off the work set:
 //   B[idx] = u0 + dtau rhs(A);   A[idx] = (u0 + B[idx] + dtau rhs(B)) / 2.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace svie {
@@ -43,6 +45,9 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
 //                       its first distance in `dist`; wbase[W] = the count
 //   dist  float [<= 6m] the subcell distances of the flagged crossings only,
 //                       in work-set order and flag-bit order within a node
+//   wx    int32 [W + 1] per warp: index of its first crossing node in xlist
+//   xlist int32 [<= m]  the entries with a flagged crossing (work-set order)
+//   xoff  int32 [<= m]  the index of each one's first distance in dist
 //   cfl   float
 //   sums  int32         scratch of the scan that makes wbase
 // A sweep streams 1 byte of geometry per node and reads distances only at
@@ -50,7 +55,7 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
 // whole footprint (the band part of the two grids, the index list, flags and
 // distances) then stays in L2 across the 40 sweeps of a call.
 struct GeoLayout {
-  long long m, W, meta, wbase, dist, cfl, sums, nsums, total;
+  long long m, W, meta, wbase, dist, wx, xlist, xoff, cfl, sums, nsums, total;
 };
 
 __host__ __device__ inline long long align16ll(long long b) { return (b + 15) & ~15LL; }
@@ -62,7 +67,10 @@ __host__ __device__ inline GeoLayout geo_layout(long long m) {
   L.meta = 4 * m;
   L.wbase = align16ll(5 * m);
   L.dist = align16ll(L.wbase + 4 * (L.W + 1));
-  L.cfl = align16ll(L.dist + 24 * m);
+  L.wx = align16ll(L.dist + 24 * m);
+  L.xlist = align16ll(L.wx + 4 * (L.W + 1));
+  L.xoff = align16ll(L.xlist + 4 * m);
+  L.cfl = align16ll(L.xoff + 4 * m);
   L.sums = L.cfl + 16;
   L.nsums = (L.W + 1 + 1023) / 1024;
   L.total = L.sums + 4 * L.nsums + 256;
@@ -74,8 +82,11 @@ struct Geo {
   uint8_t* meta;
   int* wbase;
   float* dist;
+  int* wx;     // per warp: index of its first crossing node in xlist; wx[W] = the count
+  int* xlist;  // the work-set entries with a flagged crossing, in work-set order
+  int* xoff;   // for each of them, the index of its first distance in dist
   float* cfl;
-  long long m;
+  long long m, W;
 };
 
 // The same view built on the host (the sweeps take it as a kernel argument
@@ -88,8 +99,12 @@ inline Geo geo_view_host(void* base, long long m) {
   g.meta = (uint8_t*)(b + L.meta);
   g.wbase = (int*)(b + L.wbase);
   g.dist = (float*)(b + L.dist);
+  g.wx = (int*)(b + L.wx);
+  g.xlist = (int*)(b + L.xlist);
+  g.xoff = (int*)(b + L.xoff);
   g.cfl = (float*)(b + L.cfl);
   g.m = m;
+  g.W = L.W;
   return g;
 }
 
@@ -101,8 +116,12 @@ SVIE_DEV Geo geo_view(void* base, long long m) {
   g.meta = (uint8_t*)(b + L.meta);
   g.wbase = (int*)(b + L.wbase);
   g.dist = (float*)(b + L.dist);
+  g.wx = (int*)(b + L.wx);
+  g.xlist = (int*)(b + L.xlist);
+  g.xoff = (int*)(b + L.xoff);
   g.cfl = (float*)(b + L.cfl);
   g.m = m;
+  g.W = L.W;
   return g;
 }
 
@@ -165,10 +184,15 @@ __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __res
     g.meta[t] = (uint8_t)flags;
   }
   const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags & 63u));
+  const int cx = __reduce_add_sync(0xffffffffu, (flags & 63u) ? 1 : 0);
   const long long w = t >> 5;
-  if ((threadIdx.x & 31) == 0 && w < (m + 31) / 32) g.wbase[w] = cnt;
+  if ((threadIdx.x & 31) == 0 && w < g.W) {
+    g.wbase[w] = cnt;
+    g.wx[w] = cx;
+  }
   if (t == 0) {
-    g.wbase[(m + 31) / 32] = 0;
+    g.wbase[g.W] = 0;
+    g.wx[g.W] = 0;
     *g.cfl = cfl;
   }
 }
@@ -182,14 +206,19 @@ __global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __rest
   const uint32_t flags = t < m ? g.meta[t] & 63u : 0u;
   if (!__ballot_sync(0xffffffffu, flags != 0u)) return;
   const int off = warp_exclusive(__popc(flags));
+  const int xo = warp_exclusive(flags ? 1 : 0);
   if (!flags) return;
   float d[6], dtau;
   geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
-  float* out = g.dist + g.wbase[t >> 5] + off;
+  const int doff = g.wbase[t >> 5] + off;
+  float* out = g.dist + doff;
   int r = 0;
 #pragma unroll
   for (int b = 0; b < 6; ++b)
     if ((flags >> b) & 1u) out[r++] = d[b];
+  const int k = g.wx[t >> 5] + xo;
+  g.xlist[k] = (int)t;
+  g.xoff[k] = doff;
 }
 
 // Array form of the geometry for kernels.reinit_geometry: every node's
@@ -221,10 +250,15 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
     for (int a = 0; a < 6; ++a) flags |= (flags6[a * m + t] ? 1u : 0u) << a;
   if (pass == 0) {
     const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags));
+    const int cx = __reduce_add_sync(0xffffffffu, flags ? 1 : 0);
     const long long w = t >> 5;
-    if ((threadIdx.x & 31) == 0 && w < (m + 31) / 32) g.wbase[w] = cnt;
+    if ((threadIdx.x & 31) == 0 && w < g.W) {
+      g.wbase[w] = cnt;
+      g.wx[w] = cx;
+    }
     if (t == 0) {
-      g.wbase[(m + 31) / 32] = 0;
+      g.wbase[g.W] = 0;
+      g.wx[g.W] = 0;
       *g.cfl = 0.0f;
     }
     if (t < m) {
@@ -235,11 +269,16 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
     return;
   }
   const int off = warp_exclusive(__popc(flags));
+  const int xo = warp_exclusive(flags ? 1 : 0);
   if (t >= m || !flags) return;
-  float* out = g.dist + g.wbase[t >> 5] + off;
+  const int doff = g.wbase[t >> 5] + off;
+  float* out = g.dist + doff;
   int r = 0;
   for (int b = 0; b < 6; ++b)
     if ((flags >> b) & 1u) out[r++] = dist6[b * m + t];
+  const int k = g.wx[t >> 5] + xo;
+  g.xlist[k] = (int)t;
+  g.xoff[k] = doff;
 }
 
 SVIE_DEV float meta_sgn(uint32_t meta) { return (meta & 64u) ? 1.0f : ((meta & 128u) ? -1.0f : 0.0f); }
@@ -259,6 +298,9 @@ SVIE_DEV int dist_offset(const Geo& g, long long t, uint32_t flags) {
 // dtau = cfl * max(hmin, 1e-3 h) is rebuilt exactly as geometry_at computed
 // it (a distance below 1e-6 h, stored clamped to 1e-6 h, gives the same
 // 1e-3 h either way).  `off`: the node's first distance (dist_offset).
+// CROSS = false: a node without flagged crossings (the subcell branches
+// compiled out, hmin = h).
+template <bool CROSS = true>
 SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, int off, uint32_t flags, int sx,
                              int sy, int sz, float h, float rh, float hh, float rhh, float& hmin) {
   const float* qp = f + i;
@@ -285,12 +327,12 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, i
     const float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
     float Dp = div_by(p1 - c - 0.5f * mm_p, h, rh);
     float Dm = div_by(c - m1 + 0.5f * mm_m, h, rh);
-    if ((flags >> (2 * a)) & 1u) {
+    if (CROSS && ((flags >> (2 * a)) & 1u)) {
       const float xp = __ldg(dn + __popc(flags & ((1u << (2 * a)) - 1u)));
       Dp = -c / xp - div_by(0.5f * xp * mm_p, hh, rhh);
       hmin = fminf(hmin, xp);
     }
-    if ((flags >> (2 * a + 1)) & 1u) {
+    if (CROSS && ((flags >> (2 * a + 1)) & 1u)) {
       const float xm = __ldg(dn + __popc(flags & ((1u << (2 * a + 1)) - 1u)));
       Dm = c / xm + div_by(0.5f * xm * mm_m, hh, rhh);
       hmin = fminf(hmin, xm);
@@ -302,25 +344,53 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, i
   return -sgn * (sqrtf(g2) - 1.0f);
 }
 
+// One Jacobi half-step of the TVD-RK2 pseudo-time iteration at work-set
+// entry t: first = u0 + dtau rhs(A) into B, second = (u0 + B + dtau rhs(B)) / 2
+// into A (u0 is A's value, still in dst).
+SVIE_DEV void sweep_update(const float* __restrict__ src, float* __restrict__ dst, int i, float r, float dtau,
+                           int second) {
+  if (!second) {
+    dst[i] = src[i] + dtau * r;
+  } else {
+    const float u0 = dst[i], u1 = src[i];
+    dst[i] = 0.5f * (u0 + u1 + dtau * r);
+  }
+}
+
+// The entries without a flagged crossing (about nine in ten): no subcell
+// branch, no distance reads, dtau = cfl max(h, 1e-3 h).  The others are left
+// to k_reinit_sweep_cross, so no warp runs the subcell branch for a few lanes.
 __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
                                                              const int32_t* __restrict__ idx, long long m, int sx,
                                                              int sy, int sz, float h, float rh, float rhh, Geo g,
                                                              int second) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool act = t < m;
-  const uint32_t flags = act ? __ldg(g.meta + t) : 0u;
-  const int off = dist_offset(g, t, flags);
-  if (!act) return;
+  if (t >= m) return;
+  const uint32_t flags = __ldg(g.meta + t);
+  if (flags & 63u) return;
   const float cfl = __ldg(g.cfl);
   const int i = __ldg(idx + t);
   float hmin;
-  const float r = reinit_rhs_at(src, i, g, off, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
-  const float dtau = cfl * fmaxf(hmin, 1e-3f * h);
-  if (!second) {
-    dst[i] = src[i] + dtau * r;  // u0 + dtau rhs(A)
-  } else {
-    const float u0 = dst[i], u1 = src[i];
-    dst[i] = 0.5f * (u0 + u1 + dtau * r);
+  const float r = reinit_rhs_at<false>(src, i, g, 0, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
+  sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
+}
+
+// The entries with a flagged crossing, from the compact list (count wx[W]),
+// grid-stride over a grid of about the resident CTAs.
+__global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep_cross(const float* __restrict__ src,
+                                                                   float* __restrict__ dst,
+                                                                   const int32_t* __restrict__ idx, int sx, int sy,
+                                                                   int sz, float h, float rh, float rhh, Geo g,
+                                                                   int second) {
+  const int X = __ldg(g.wx + g.W);
+  const float cfl = __ldg(g.cfl);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < X; k += gridDim.x * blockDim.x) {
+    const int t = __ldg(g.xlist + k);
+    const uint32_t flags = __ldg(g.meta + t);
+    const int i = __ldg(idx + t);
+    float hmin;
+    const float r = reinit_rhs_at<true>(src, i, g, __ldg(g.xoff + k), flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
+    sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
   }
 }
 
@@ -603,7 +673,8 @@ int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_
   const int nb = blocks_for(m, RI_THREADS);
   k_reinit_count<<<nb, RI_THREADS, 0, s>>>(phi, idx, m, sx, sy, sz, h, cfl, geo);
   char* b = (char*)geo;
-  const int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
+  int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
+  ns += scan_exclusive_i32((int*)(b + L.wx), L.W + 1, (int*)(b + L.sums), s);
   k_reinit_dist<<<nb, RI_THREADS, 0, s>>>(phi, idx, m, sx, sy, sz, h, cfl, geo);
   return launch_status("svie_reinit_geometry", 2 + ns);
 }
@@ -623,11 +694,17 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
   const int nb = blocks_for(m, RI_THREADS);
   const float rh = rn_reciprocal(h), rhh = rn_reciprocal(h * h);
   const Geo g = geo_view_host(const_cast<void*>(geo), m);
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nbx = (int)std::min<long long>((long long)blocks_for(m, RI_THREADS), 8LL * nsm);
   for (int it = 0; it < iterations; ++it) {
     k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, g, 0);
+    k_reinit_sweep_cross<<<nbx, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, sx, sy, sz, h, rh, rhh, g, 0);
     k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, rhh, g, 1);
+    k_reinit_sweep_cross<<<nbx, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, sx, sy, sz, h, rh, rhh, g, 1);
   }
-  return launch_status("svie_reinit_iterate", 2 * iterations);
+  return launch_status("svie_reinit_iterate", 4 * iterations);
 }
 
 int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz, float h,
@@ -664,7 +741,8 @@ int svie_reinit_geometry_pack(const float* sgn, const float* dtau, const uint8_t
   const int nb = blocks_for(m, 256);
   k_reinit_pack<<<nb, 256, 0, s>>>(sgn, dtau, flags, dist6, m, geo, 0);
   char* b = (char*)geo;
-  const int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
+  int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
+  ns += scan_exclusive_i32((int*)(b + L.wx), L.W + 1, (int*)(b + L.sums), s);
   k_reinit_pack<<<nb, 256, 0, s>>>(sgn, dtau, flags, dist6, m, geo, 1);
   return launch_status("svie_reinit_geometry_pack", 2 + ns);
 }
