@@ -125,6 +125,23 @@ SVIE_DEV Geo geo_view(void* base, long long m) {
   return g;
 }
 
+// Crossing flags and sign bits of node i alone (the flags of geometry_at).
+SVIE_DEV uint32_t crossing_flags(const float* __restrict__ f, int i, int sx, int sy, int sz) {
+  const float* qp = f + i;
+  const float c = __ldg(qp);
+  uint32_t flags = 0;
+  const int st[3] = {sx, sy, sz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float m1 = __ldg(qp - st[a]), p1 = __ldg(qp + st[a]);
+    flags |= ((c * p1) < 0.0f ? 1u : 0u) << (2 * a);
+    flags |= ((c * m1) < 0.0f ? 1u : 0u) << (2 * a + 1);
+  }
+  flags |= (c > 0.0f ? 1u : 0u) << 6;
+  flags |= (c < 0.0f ? 1u : 0u) << 7;
+  return flags;
+}
+
 // Crossing geometry at node i (kernels.py:335-359): flag bits 2a (cp) and
 // 2a + 1 (cm), distances d[2a] = xp, d[2a + 1] = xm clamped below to 1e-6 h,
 // and dtau = cfl max(hmin, 1e-3 h) with hmin from the unclamped distances.
@@ -171,16 +188,17 @@ SVIE_DEV int warp_exclusive(int v) {
   return s - v;
 }
 
-// Pass 1: flags, sign bits, dtau; per-warp crossing counts into wbase.
+// Pass 1: flags and sign bits from the 7-point stencil, dtau of a node
+// without crossings (pass 3 writes the others); per-warp counts of the
+// flagged distances (wbase) and of the crossing nodes (wx).
 __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
                                int sy, int sz, float h, float cfl, void* geo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   Geo g = geo_view(geo, m);
   uint32_t flags = 0;
   if (t < m) {
-    float d[6], dtau;
-    flags = geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
-    g.dtau[t] = dtau;
+    flags = crossing_flags(f, idx[t], sx, sy, sz);
+    g.dtau[t] = cfl * fmaxf(h, 1e-3f * h);
     g.meta[t] = (uint8_t)flags;
   }
   const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags & 63u));
@@ -197,8 +215,9 @@ __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __res
   }
 }
 
-// Pass 3 (after the exclusive scan of wbase): the flagged distances.  The
-// flags come from pass 1; only warps holding a crossing recompute geometry.
+// Pass 3 (after the exclusive scans of wbase and wx): the flagged distances,
+// dtau, and the crossing list.  The flags come from pass 1; only warps
+// holding a crossing compute the geometry.
 __global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
                               int sy, int sz, float h, float cfl, void* geo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -210,6 +229,7 @@ __global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __rest
   if (!flags) return;
   float d[6], dtau;
   geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
+  g.dtau[t] = dtau;
   const int doff = g.wbase[t >> 5] + off;
   float* out = g.dist + doff;
   int r = 0;
