@@ -609,22 +609,29 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_write(Pred pred, BrickGeo
 }
 
 // The reinitialisation work mask as bits (svie_reinit_bits: rows (x, y) of
-// nzw words, bit z % 32 of word z / 32, nothing set past nz): the lane's bit
-// in chunk j; one word per half-warp row, no node index needed for the test.
-SVIE_DEV bool brick_bit(const uint32_t* __restrict__ bits, int nzw, const BrickWalk& W, const BrickGeom& G, int j) {
-  int x, y, z;
-  W.coords(j, x, y, z);
-  if (!W.ok[j >> 3] || x >= G.nx || y >= G.ny) return false;
-  return (__ldg(bits + ((long long)x * G.ny + y) * nzw + (z >> 5)) >> (z & 31)) & 1u;
+// nzw words, bit z % 32 of word z / 32, nothing set past nz).  One lane per
+// brick row of 16 nodes: thread t of CTA k takes row t % 16 of brick
+// 16 k + t / 16, i.e. the same 4096 nodes per CTA and the same order (brick,
+// row, z) as the node-per-lane brick kernels.  Returns the row's 16 bits.
+SVIE_DEV unsigned int brick_row_bits(const uint32_t* __restrict__ bits, int nzw, const BrickGeom& G, long long* e0) {
+  const long long r = (long long)blockIdx.x * CMP_THREADS + threadIdx.x;
+  const long long b = r >> 4;
+  *e0 = -1;
+  if (b >= G.bricks()) return 0u;
+  const int bz = (int)(b % G.nbz);
+  const long long bxy = b / G.nbz;
+  const int lr = (int)(r & 15);
+  const int x = (int)(bxy / G.nby) * BRX + (lr >> 2), y = (int)(bxy % G.nby) * BRY + (lr & 3), z0 = bz * BRZ;
+  if (x >= G.nx || y >= G.ny) return 0u;
+  *e0 = ((long long)x * G.ny + y) * G.nz + z0;
+  return (__ldg(bits + ((long long)x * G.ny + y) * nzw + (z0 >> 5)) >> (z0 & 31)) & 0xffffu;
 }
 
 __global__ void __launch_bounds__(CMP_THREADS) k_brick_bits_count(const uint32_t* __restrict__ bits, int nzw,
                                                                   BrickGeom G, int* counts) {
   __shared__ int sh[CMP_THREADS / 32];
-  const BrickWalk W(G);
-  int c = 0;
-#pragma unroll
-  for (int j = 0; j < CMP_IPT; ++j) c += brick_bit(bits, nzw, W, G, j) ? 1 : 0;
+  long long e0;
+  const int c = __popc(brick_row_bits(bits, nzw, G, &e0));
   int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
   if (threadIdx.x == 0) counts[blockIdx.x] = tot;
 }
@@ -632,18 +639,29 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_bits_count(const uint32_t
 __global__ void __launch_bounds__(CMP_THREADS) k_brick_bits_write(const uint32_t* __restrict__ bits, int nzw,
                                                                   BrickGeom G, const int* offsets, int32_t* out,
                                                                   long long capacity) {
-  __shared__ int sh[33];
-  const BrickWalk W(G);
-  unsigned int bal[CMP_IPT];
-  int wt = 0;
+  __shared__ int sh[CMP_THREADS / 32];
+  long long e0;
+  unsigned int rb = brick_row_bits(bits, nzw, G, &e0);
+  const int c = __popc(rb);
+  // exclusive prefix of the row counts over the CTA (lane order = list order)
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int s = c;
 #pragma unroll
-  for (int j = 0; j < CMP_IPT; ++j) {
-    bal[j] = __ballot_sync(0xffffffffu, brick_bit(bits, nzw, W, G, j));
-    wt += __popc(bal[j]);
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, s, o);
+    if (lane >= o) s += y;
   }
-  int tot;
-  const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
-  write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)W.node(G, j); });
+  if (lane == 31) sh[wid] = s;
+  __syncthreads();
+  int before = 0;
+  for (int w = 0; w < wid; ++w) before += sh[w];
+  long long o = (long long)offsets[blockIdx.x] + before + s - c;
+  while (rb) {
+    const int k = __ffs(rb) - 1;
+    rb &= rb - 1u;
+    if (o < capacity) out[o] = (int32_t)(e0 + k);
+    ++o;
+  }
 }
 
 struct AbsLessPred {
