@@ -409,51 +409,42 @@ struct BrickGeom {
 // rows 2j and 2j + 1 of the pair (half-warp per row, z fastest), so the
 // ballot bits follow the list order.  Node of the lane in chunk j, or -1.
 struct BrickWalk {
+  long long base[2];  // node (x0, y0, z0 + lane % 16) of each brick
   int x0[2], y0[2], z0[2];
-  long long base[2];  // node of row 0 of each brick for this lane (z0 + lane % 16)
-  bool ok[2], full[2];
+  int xm[2], ym[2];   // rows of each brick inside the grid along x and y (0 where this lane's z is outside)
+  int syz, nz, hl;    // strides; hl = lane / 16, the half-warp
   SVIE_DEV BrickWalk(const BrickGeom& G) {
     const long long b0 = ((long long)blockIdx.x * CMP_THREADS + (threadIdx.x & ~31)) >> 4;
+    const int zl = threadIdx.x & 15;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const long long b = b0 + h;
-      ok[h] = b < G.bricks();
-      const int bz = ok[h] ? (int)(b % G.nbz) : 0;
-      const long long bxy = ok[h] ? b / G.nbz : 0;
+      const bool ok = b < G.bricks();
+      const int bz = ok ? (int)(b % G.nbz) : 0;
+      const long long bxy = ok ? b / G.nbz : 0;
       x0[h] = (int)(bxy / G.nby) * BRX;
       y0[h] = (int)(bxy % G.nby) * BRY;
       z0[h] = bz * BRZ;
-      full[h] = ok[h] && x0[h] + BRX <= G.nx && y0[h] + BRY <= G.ny && z0[h] + BRZ <= G.nz;
-      base[h] = ((long long)x0[h] * G.ny + y0[h]) * G.nz + z0[h] + (threadIdx.x & 15);
+      const bool zin = ok && z0[h] + zl < G.nz;
+      xm[h] = zin ? min(BRX, G.nx - x0[h]) : 0;
+      ym[h] = zin ? min(BRY, G.ny - y0[h]) : 0;
+      base[h] = ((long long)x0[h] * G.ny + y0[h]) * G.nz + z0[h] + zl;
     }
+    syz = G.ny * G.nz;
+    nz = G.nz;
+    hl = (threadIdx.x >> 4) & 1;
   }
-  SVIE_DEV long long at(const BrickGeom& G, int j, int* c) const {
-    const int lane = threadIdx.x & 31, h = j >> 3;
-    const int lr = ((2 * j) & 15) + (lane >> 4);
-    c[0] = x0[h] + (lr >> 2);
-    c[1] = y0[h] + (lr & 3);
-    c[2] = z0[h] + (lane & 15);
-    if (!ok[h] || c[0] >= G.nx || c[1] >= G.ny || c[2] >= G.nz) return -1;
-    return ((long long)c[0] * G.ny + c[1]) * G.nz + c[2];
-  }
-  // Coordinates of chunk j (valid where node() >= 0).
-  SVIE_DEV void coords(int j, int& x, int& y, int& z) const {
-    const int h = j >> 3, lr = ((2 * j) & 15) + ((threadIdx.x >> 4) & 1);
-    x = x0[h] + (lr >> 2);
-    y = y0[h] + (lr & 3);
-    z = z0[h] + (threadIdx.x & 15);
-  }
-  // Node of chunk j; bricks inside the grid (all but the last of each axis)
-  // take it from the brick's base without bounds checks.
-  SVIE_DEV long long node(const BrickGeom& G, int j) const {
+  // Chunk j: brick j / 8, row (2j % 16) + hl of it, i.e. x offset (2j % 16) / 4
+  // (the same for both half-warps: 2j % 16 is even) and y offset 2j % 4 + hl.
+  SVIE_DEV bool valid(int j) const {
     const int h = j >> 3;
-    if (full[h]) {
-      const int lr = ((2 * j) & 15) + ((threadIdx.x >> 4) & 1);
-      return base[h] + (long long)((lr >> 2) * (G.ny * G.nz) + (lr & 3) * G.nz);
-    }
-    int c[3];
-    return at(G, j, c);
+    return ((2 * j) & 15) / 4 < xm[h] && ((2 * j) & 3) + hl < ym[h];
   }
+  SVIE_DEV long long offset(int j) const {
+    return base[j >> 3] + (long long)(((2 * j) & 15) / 4 * syz + (((2 * j) & 3) + hl) * nz);
+  }
+  // Node of chunk j, or -1 outside the grid.
+  SVIE_DEV long long node(const BrickGeom&, int j) const { return valid(j) ? offset(j) : -1; }
 };
 
 // LevelSet.rebuild_band (levelset.py:70-77) in brick order, pass 1: clamp phi
@@ -464,18 +455,14 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_band_count(float* __restr
   const BrickWalk W(G);
   float v[CMP_IPT];
 #pragma unroll
-  for (int j = 0; j < CMP_IPT; ++j) {
-    const long long e = W.node(G, j);
-    v[j] = e >= 0 ? phi[e] : 0.0f;
-  }
+  for (int j = 0; j < CMP_IPT; ++j) v[j] = W.valid(j) ? phi[W.offset(j)] : 0.0f;
   int c = 0;
 #pragma unroll
   for (int j = 0; j < CMP_IPT; ++j) {
-    const long long e = W.node(G, j);
-    if (e >= 0) {
+    if (W.valid(j)) {
       const float x = v[j];
       const float cl = (x != x) ? x : fminf(fmaxf(x, -cap), cap);
-      if (cl != x && x == x) phi[e] = cl;
+      if (cl != x && x == x) phi[W.offset(j)] = cl;
       c += fabsf(cl) < thresh ? 1 : 0;
     }
   }
@@ -493,47 +480,41 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_band_write(const float* _
   const BrickWalk W(G);
   float pv[CMP_IPT];
 #pragma unroll
-  for (int j = 0; j < CMP_IPT; ++j) {
-    const long long e = W.node(G, j);
-    pv[j] = e >= 0 ? phi[e] : 0.0f;
-  }
+  for (int j = 0; j < CMP_IPT; ++j) pv[j] = W.valid(j) ? phi[W.offset(j)] : 0.0f;
   unsigned int bal[CMP_IPT];
   int wt = 0, inside_static = 0;
-  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
-  int ilo[3] = {INT_MAX, INT_MAX, INT_MAX}, ihi[3] = {-1, -1, -1};
-  // the bounding boxes and the static-inside count are kept by the first lane
-  // of each half-warp, one row of 16 nodes per chunk, from the ballot bits
-  const int lane = threadIdx.x & 31, hs = lane & 16;
-  const bool leader = (lane & 15) == 0;
+  unsigned int selm = 0, negm = 0;  // chunks where this lane holds a band / an inside node
 #pragma unroll
   for (int j = 0; j < CMP_IPT; ++j) {
-    const long long e = W.node(G, j);
+    const bool valid = W.valid(j);
     const float v = pv[j];
-    const bool valid = e >= 0;
     const bool sel = valid && fabsf(v) < thresh;
     const bool neg = valid && v < 0.0f;
-    if (valid && occ) occ[e] = neg ? 1.0f : 0.0f;
-    const unsigned int bs = __ballot_sync(0xffffffffu, sel), bn = __ballot_sync(0xffffffffu, neg);
-    bal[j] = bs;
-    wt += __popc(bs);
-    if (leader) {
-      const unsigned int ms = (bs >> hs) & 0xffffu, mn = (bn >> hs) & 0xffffu;
-      if (ms | mn) {
-        int x, y, z;
-        W.coords(j, x, y, z);  // the row's first z
-        if (ms) {
-          lo[0] = min(lo[0], x); hi[0] = max(hi[0], x);
-          lo[1] = min(lo[1], y); hi[1] = max(hi[1], y);
-          lo[2] = min(lo[2], z + __ffs(ms) - 1); hi[2] = max(hi[2], z + 31 - __clz(ms));
-        }
-        if (mn) {
-          ilo[0] = min(ilo[0], x); ihi[0] = max(ihi[0], x);
-          ilo[1] = min(ilo[1], y); ihi[1] = max(ihi[1], y);
-          ilo[2] = min(ilo[2], z + __ffs(mn) - 1); ihi[2] = max(ihi[2], z + 31 - __clz(mn));
-          inside_static += __popc(mn & ~ms);
-        }
-      }
-    }
+    if (valid && occ) occ[W.offset(j)] = neg ? 1.0f : 0.0f;
+    bal[j] = __ballot_sync(0xffffffffu, sel);
+    wt += __popc(bal[j]);
+    selm |= (sel ? 1u : 0u) << j;
+    negm |= (neg ? 1u : 0u) << j;
+    inside_static += (neg && !sel) ? 1 : 0;
+  }
+  // bounding boxes of this lane's nodes: chunk k of brick h sits at x offset
+  // k / 2, y offset 2 (k % 2) + hl and the lane's z
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
+  int ilo[3] = {INT_MAX, INT_MAX, INT_MAX}, ihi[3] = {-1, -1, -1};
+  auto box = [&](unsigned int M, int h, int* l, int* u) {
+    if (!M) return;
+    const int z = W.z0[h] + (threadIdx.x & 15);
+    l[0] = min(l[0], W.x0[h] + ((__ffs(M) - 1) >> 1));
+    u[0] = max(u[0], W.x0[h] + ((31 - __clz(M)) >> 1));
+    l[1] = min(l[1], W.y0[h] + ((M & 0x55u) ? W.hl : 2 + W.hl));
+    u[1] = max(u[1], W.y0[h] + ((M & 0xAAu) ? 2 + W.hl : W.hl));
+    l[2] = min(l[2], z);
+    u[2] = max(u[2], z);
+  };
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    box((selm >> (8 * h)) & 0xffu, h, lo, hi);
+    box((negm >> (8 * h)) & 0xffu, h, ilo, ihi);
   }
   int tot;
   const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
@@ -550,7 +531,7 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_band_write(const float* _
     for (int k = 1; k < 13; ++k) r[k] = min(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
   }
   __shared__ int shr[13][NW];
-  const int wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) {
 #pragma unroll
     for (int k = 0; k < 13; ++k) shr[k][wid] = r[k];
