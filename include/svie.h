@@ -179,6 +179,9 @@ int svie_central_gradient(const float* flat, const int32_t* idx, int64_t m, int6
 int svie_closest_points_newton(const float* flat, const int32_t* idx, int64_t m, int ny, int nz,
                                float hi_x, float hi_y, float hi_z, float h, int newton_steps,
                                float* out, void* stream);
+/* phi[band] (the reference's `flat[band]`, e.g. levelset.py:123-126 and the
+ * band values a caller reads back): out[k] = src[idx[k]]. */
+int svie_gather(const float* src, const int32_t* idx, int64_t m, float* out, void* stream);
 /* levelset.cube_plane_fraction (levelset.py:37-48, kernels.py:104-122) */
 int svie_cube_plane_fraction(const float* s, const float* a, const float* b, const float* c,
                              int64_t m, float* out, void* stream);

@@ -100,6 +100,7 @@ _SIGS = {
     "svie_point_triangle_distance2": (I, [V, V, V, V, I64, V, V]),
     "svie_central_gradient": (I, [V, V, I64, I64, I64, I64, V, V]),
     "svie_cube_plane_fraction": (I, [V, V, V, V, I64, V, V]),
+    "svie_gather": (I, [V, V, I64, V, V]),
     "svie_law_eval": (I, [V, V, I64, POINTER(Law), V, V, V]),
     "svie_scatter_fractions": (I, [V, V, I64, I64, I64, I64, V, V]),
     "svie_dense_occupancy": (I, [V, I64, V, V]),

@@ -121,7 +121,7 @@ class ErosionJob:
                 res = self.sim.end_run()
                 snap_phi = None
                 if self.keep_snapshot_phi:
-                    snap_phi = nat.d2h(self.ls.flat[self.ls.band32])
+                    snap_phi = nat.d2h(self.ls.band_values())
                 self.snapshots.append((res.fraction, self.sim.time, snap_phi))
                 self.targets.pop(0)
                 if res.stop_reason != "target_volume" or not self.targets:

@@ -309,6 +309,12 @@ __global__ void k_closest_newton(const float* __restrict__ f, const int32_t* __r
   out[3 * t + 2] = p.z;
 }
 
+__global__ void k_gather(const float* __restrict__ src, const int32_t* __restrict__ idx, long long m,
+                         float* __restrict__ out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m) out[t] = __ldg(src + __ldg(idx + t));
+}
+
 __global__ void k_cube_plane(const float* __restrict__ s, const float* __restrict__ a, const float* __restrict__ b,
                              const float* __restrict__ c, long long m, float* __restrict__ out) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -338,6 +344,16 @@ int svie_closest_points_newton(const float* flat, const int32_t* idx, int64_t m,
   k_closest_newton<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(
       flat, idx, m, ny, nz, cp_geom(ny, nz, hi_x, hi_y, hi_z, h), newton_steps, out);
   return launch_status("svie_closest_points_newton");
+}
+
+int svie_gather(const float* src, const int32_t* idx, int64_t m, float* out, void* stream) {
+  SVIE_CHECK_M("svie_gather", m);
+  if (m > 0 && (!src || !idx || !out)) {
+    set_error("svie_gather: null pointer");
+    return SVIE_ERR_ARG;
+  }
+  k_gather<<<blocks_for(m, ST_THREADS), ST_THREADS, 0, (cudaStream_t)stream>>>(src, idx, m, out);
+  return launch_status("svie_gather");
 }
 
 int svie_cube_plane_fraction(const float* s, const float* a, const float* b, const float* c, int64_t m, float* out,

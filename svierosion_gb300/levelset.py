@@ -245,6 +245,13 @@ class LevelSet:
     def volume_from_stats(self, st) -> float:
         return (self.static_inside + float(st["fsum"])) * self.h ** 3
 
+    def band_values(self) -> torch.Tensor:
+        """phi at the band nodes in ascending order (the reference's ``flat[band]``)."""
+        b = self.band32
+        out = torch.empty(b.numel(), dtype=torch.float32, device=self.device)
+        nat.call("svie_gather", nat.ptr(self.flat), nat.ptr(b), b.numel(), nat.ptr(out), nat.stream())
+        return out
+
     def volume(self) -> float:
         """Solid volume (levelset.py:123-126): off-band inside count + float64 sum of band fractions."""
         self._volume_kernel(True)

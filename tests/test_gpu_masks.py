@@ -249,3 +249,5 @@ def test_levelset_band_views_agree():
     assert np.array_equal(band, np.sort(work))
     ref = np.flatnonzero(np.abs(np.clip(phi, -6 * h, 6 * h)) < np.float32(6 * h * (1 - 1e-5)))
     assert np.array_equal(band, ref)
+    # band values through the library's gather equal phi at the band
+    assert np.array_equal(ls.band_values().cpu().numpy(), ls.flat.cpu().numpy()[band])
