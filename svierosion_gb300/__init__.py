@@ -8,17 +8,19 @@ path: on a machine without the built library or a CUDA device every call
 raises.
 """
 
-from .api import ErosionParams, ErosionResult, erode, make_grid
+from .api import ErosionParams, ErosionResult, erode, make_grid, point_mesh_distance, write_result
 from .evolve import ErosionSimulation, RunResult, StepRecord
 from .flows import GaussCurvatureLaw, MeanCurvatureLaw, SVIPowerLaw, make_law
 from .grid import Grid, get_device
 from .levelset import LevelSet
-from .meshio import TriMesh
+from .meshio import TriMesh, read_ply, write_ply
 from .sdf import mesh_to_sdf
+from .surface import extract_surface
 from .svi import BallConvolution
 
 __version__ = "0.1.0"
 
-__all__ = ["ErosionParams", "ErosionResult", "erode", "make_grid", "ErosionSimulation", "RunResult", "StepRecord",
-           "GaussCurvatureLaw", "MeanCurvatureLaw", "SVIPowerLaw", "make_law", "Grid", "get_device", "LevelSet",
-           "TriMesh", "mesh_to_sdf", "BallConvolution"]
+__all__ = ["ErosionParams", "ErosionResult", "erode", "make_grid", "point_mesh_distance", "write_result",
+           "ErosionSimulation", "RunResult", "StepRecord", "GaussCurvatureLaw", "MeanCurvatureLaw", "SVIPowerLaw",
+           "make_law", "Grid", "get_device", "LevelSet", "TriMesh", "read_ply", "write_ply", "mesh_to_sdf",
+           "extract_surface", "BallConvolution"]

@@ -115,3 +115,24 @@ def test_erode_meshes_carry_vertex_data():
     res2 = S.erode(m, S.ErosionParams(law="mean", alpha=1.0, resolution=40, target_fraction=0.99, max_steps=30))
     for key in ("depth", "H", "K", "speed"):
         assert key in res2.mesh.vertex_data
+
+
+def test_result_files_of_an_erosion(tmp_path):
+    """An erode() result with a snapshot goes to disk in the reference's result format
+    (cli.py:101-126) and reads back: meshes with their vertex fields, history, summary."""
+    import csv
+    import json
+
+    res = S.erode(shapes.cube(1.0), S.ErosionParams(law="svi", radius=0.2, k=1, s=1, t=0.9, resolution=48,
+                                                    target_fraction=0.95, snapshots=(0.97,)))
+    written = S.write_result(res, tmp_path / "cube.ply")
+    assert [p.name for p in written] == ["cube_v0.970.ply", "cube.ply"]
+    m = S.read_ply(tmp_path / "cube.ply")
+    assert np.array_equal(m.faces, res.mesh.faces)
+    assert np.allclose(m.vertices, res.mesh.vertices, atol=1e-6)
+    assert np.allclose(m.vertex_data["quality"], res.mesh.vertex_data["depth"], atol=1e-6)
+    assert m.is_watertight()
+    rows = list(csv.DictReader(open(tmp_path / "cube_history.csv")))
+    assert len(rows) == len(res.history) and float(rows[-1]["fraction"]) == pytest.approx(res.fraction)
+    meta = json.loads((tmp_path / "cube.json").read_text())
+    assert meta["stop_reason"] == res.stop_reason and meta["snapshots"][0]["fraction"] == 0.97

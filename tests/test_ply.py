@@ -118,3 +118,24 @@ def test_mesh_cleanup():
     assert np.array_equal(c.faces, [[0, 1, 2]])
     assert np.array_equal(c.vertices, m.vertices[[0, 2, 3]])
     assert np.array_equal(c.vertex_data["q"], [0.0, 2.0, 3.0])
+
+
+def test_result_files_match_reference(tmp_path):
+    """write_result writes the files of the reference's result writer (cli.py:101-126), byte for
+    byte, for the same synthetic result."""
+    import importlib.util
+
+    from svierosion_gb300.api import ErosionResult, write_result
+    from svierosion_gb300.evolve import StepRecord
+    from svierosion_gb300.grid import Grid
+
+    spec = importlib.util.spec_from_file_location("make_ply_golden", GOLD.parent / "make_ply_golden.py")
+    gold = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gold)
+    res = gold.synthetic_result(ErosionResult, StepRecord, Grid, TriMesh, shapes.cube(1.0))
+    written = write_result(res, tmp_path / "result.ply", "depth")
+    assert [p.name for p in written] == ["result_v0.950.ply", "result.ply"]
+    for name in ("result_v0.950.ply", "result.ply", "result_history.csv", "result.json"):
+        assert (tmp_path / name).read_bytes() == (GOLD / name).read_bytes(), name
+    m = read_ply(tmp_path / "result.ply")
+    assert np.array_equal(m.vertex_data["quality"], m.vertex_data["depth"])
