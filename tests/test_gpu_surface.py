@@ -135,4 +135,6 @@ def test_result_files_of_an_erosion(tmp_path):
     rows = list(csv.DictReader(open(tmp_path / "cube_history.csv")))
     assert len(rows) == len(res.history) and float(rows[-1]["fraction"]) == pytest.approx(res.fraction)
     meta = json.loads((tmp_path / "cube.json").read_text())
-    assert meta["stop_reason"] == res.stop_reason and meta["snapshots"][0]["fraction"] == 0.97
+    assert meta["stop_reason"] == res.stop_reason
+    # the snapshot records the fraction reached, within the tolerance of the request
+    assert meta["snapshots"][0]["fraction"] == pytest.approx(0.97, abs=1e-3)
