@@ -131,6 +131,22 @@ int svie_brick_scan(int kind, const void* src, int nx, int ny, int nz, float thr
                     size_t ws_bytes, int64_t* count, void* stream);
 int svie_brick_write(int kind, const void* src, int nx, int ny, int nz, float thresh,
                      const void* ws, size_t ws_bytes, int32_t* out, int64_t capacity, void* stream);
+/* LevelSet.rebuild_band (levelset.py:70-86) restricted to a node list idx of m
+ * nodes (the reinitialisation work set, brick order), for a phi that changed
+ * only on the list since the last full rebuild: clamp and count (scan), then
+ * the band entries in list order, occupancy of the listed nodes and info
+ * (count, band box; static_inside and the inside box cover the listed nodes
+ * only).  ws: svie_list_workspace_bytes(m). */
+size_t svie_list_workspace_bytes(int64_t m);
+int svie_list_band_scan(float* phi, const int32_t* idx, int64_t m, float cap, float thresh, void* ws,
+                        size_t ws_bytes, svie_band_info* info, void* stream);
+int svie_list_band_write(const float* phi, const int32_t* idx, int64_t m, int nx, int ny, int nz, float thresh,
+                         const void* ws, size_t ws_bytes, int32_t* out, int64_t capacity, float* occ,
+                         svie_band_info* info, void* stream);
+/* *count = the listed nodes with phi < 0 whose bit in `marked` (layout of
+ * svie_reinit_bits) is clear. */
+int svie_list_inside_off_mask(const float* phi, const int32_t* idx, int64_t m, const uint32_t* marked, int nx,
+                              int ny, int nz, uint64_t* count, void* stream);
 /* LevelSet.rebuild_band (svierosion/levelset.py:70-86) with the band listed in
  * brick order: svie_brick_band_scan clamps phi to [-cap, cap] in place and
  * counts |phi| < thresh (info->count on the device); svie_brick_band_write
@@ -358,10 +374,11 @@ int svie_reinit_mask(const int32_t* band, int64_t m, int nx, int ny, int nz, int
                      uint8_t* mask, uint8_t* tmp, void* stream);
 /* The same work mask as bits (rows (x, y) of ceil(nz / 32) words, bit z % 32
  * of word z / 32; dilation <= 31), for svie_brick_scan / svie_brick_write
- * kind 2.  bits and tmp: svie_reinit_bits_bytes(nx, ny, nz) each. */
+ * kind 2.  bits, tmp and marked: svie_reinit_bits_bytes(nx, ny, nz) each;
+ * marked (may be NULL) receives the undilated band's bits. */
 size_t svie_reinit_bits_bytes(int nx, int ny, int nz);
 int svie_reinit_bits(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin,
-                     uint32_t* bits, uint32_t* tmp, void* stream);
+                     uint32_t* bits, uint32_t* tmp, uint32_t* marked, void* stream);
 /* reinit_geometry (kernels.py:335-359) packed over the m work-set nodes for
  * svie_reinit_iterate / svie_reinit_rhs: dtau float[m], meta uint8[m] (bits
  * 0-5 crossing flags cp/cm per axis, bit 6 phi0 > 0, bit 7 phi0 < 0), per-warp

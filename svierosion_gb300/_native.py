@@ -132,7 +132,11 @@ _SIGS = {
     "svie_reinit_mask": (I, [V, I64, I, I, I, I, I, V, V, V]),
     "svie_reinit_geometry_bytes": (Z, [I64]),
     "svie_reinit_bits_bytes": (Z, [I, I, I]),
-    "svie_reinit_bits": (I, [V, I64, I, I, I, I, I, V, V, V]),
+    "svie_reinit_bits": (I, [V, I64, I, I, I, I, I, V, V, V, V]),
+    "svie_list_workspace_bytes": (Z, [I64]),
+    "svie_list_band_scan": (I, [V, V, I64, F, F, V, Z, V, V]),
+    "svie_list_band_write": (I, [V, V, I64, I, I, I, F, V, Z, V, I64, V, V, V]),
+    "svie_list_inside_off_mask": (I, [V, V, I64, V, I, I, I, V, V]),
     "svie_reinit_geometry": (I, [V, V, I64, I64, I64, I64, F, F, V, V]),
     "svie_reinit_iterate": (I, [V, V, I64, V, I64, I64, I64, I64, F, V, I, V]),
     "svie_reinit_rhs": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),

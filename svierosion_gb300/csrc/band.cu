@@ -447,6 +447,47 @@ struct BrickWalk {
   SVIE_DEV long long node(const BrickGeom&, int j) const { return valid(j) ? offset(j) : -1; }
 };
 
+// The CTA's static-inside count and band / inside bounding boxes into the
+// band info: warp reductions, then one barrier and warp 0 across the warps,
+// one atomic per quantity (exact and order independent).  Ends the caller.
+SVIE_DEV void band_info_commit(int inside_static, const int* lo, const int* hi, const int* ilo, const int* ihi,
+                               svie_band_info* info) {
+  constexpr int NW = CMP_THREADS / 32;
+  int r[13] = {inside_static, lo[0], lo[1], lo[2], -hi[0], -hi[1], -hi[2],
+               ilo[0], ilo[1], ilo[2], -ihi[0], -ihi[1], -ihi[2]};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    r[0] += __shfl_xor_sync(0xffffffffu, r[0], o);
+#pragma unroll
+    for (int k = 1; k < 13; ++k) r[k] = min(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+  }
+  __shared__ int shr[13][NW];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 13; ++k) shr[k][wid] = r[k];
+  }
+  __syncthreads();
+  if (wid != 0) return;
+#pragma unroll
+  for (int k = 0; k < 13; ++k) r[k] = lane < NW ? shr[k][lane] : (k == 0 ? 0 : INT_MAX);
+#pragma unroll
+  for (int o = NW / 2; o > 0; o >>= 1) {
+    r[0] += __shfl_xor_sync(0xffffffffu, r[0], o);
+#pragma unroll
+    for (int k = 1; k < 13; ++k) r[k] = min(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+  }
+  if (lane != 0) return;
+  if (r[0]) atomicAdd((unsigned long long*)&info->static_inside, (unsigned long long)r[0]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (r[1 + a] != INT_MAX) atomicMin(&info->lo[a], r[1 + a]);
+    if (-r[4 + a] >= 0) atomicMax(&info->hi[a], -r[4 + a]);
+    if (r[7 + a] != INT_MAX) atomicMin(&info->ilo[a], r[7 + a]);
+    if (-r[10 + a] >= 0) atomicMax(&info->ihi[a], -r[10 + a]);
+  }
+}
+
 // LevelSet.rebuild_band (levelset.py:70-77) in brick order, pass 1: clamp phi
 // to [-cap, cap] in place (NaN stays NaN) and count |phi| < thresh per CTA.
 __global__ void __launch_bounds__(CMP_THREADS) k_brick_band_count(float* __restrict__ phi, BrickGeom G, float cap,
@@ -519,42 +560,109 @@ __global__ void __launch_bounds__(CMP_THREADS) k_brick_band_write(const float* _
   int tot;
   const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
   write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)W.node(G, j); });
-  // the static-inside count and the two bounding boxes: warp reductions,
-  // then one barrier and warp 0 across the warps
-  constexpr int NW = CMP_THREADS / 32;
-  int r[13] = {inside_static, lo[0], lo[1], lo[2], -hi[0], -hi[1], -hi[2],
-               ilo[0], ilo[1], ilo[2], -ihi[0], -ihi[1], -ihi[2]};
+  band_info_commit(inside_static, lo, hi, ilo, ihi, info);
+}
+
+// ---------------------------------------------- rebuild over a node list
+// LevelSet.rebuild_band restricted to a node list: the reinitialisation work
+// set (the band dilated, in brick order).  Off the list phi has not changed
+// since the last rebuild, where it was clamped to +-cap, so the new band
+// (|phi| < thresh < cap) lies in the list and comes out in brick order, the
+// same list a full rebuild makes.  The list entries of a warp's chunks are
+// the warp's 32 x CMP_IPT consecutive entries (coalesced index loads).
+__global__ void __launch_bounds__(CMP_THREADS) k_list_band_count(float* __restrict__ phi,
+                                                                 const int32_t* __restrict__ idx, long long m,
+                                                                 float cap, float thresh, int* counts) {
+  __shared__ int sh[CMP_THREADS / 32];
+  const long long wb = warp_base() + (threadIdx.x & 31);
+  int iv[CMP_IPT];
+  float v[CMP_IPT];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    r[0] += __shfl_xor_sync(0xffffffffu, r[0], o);
+  for (int j = 0; j < CMP_IPT; ++j) iv[j] = wb + 32 * j < m ? __ldg(idx + wb + 32 * j) : -1;
 #pragma unroll
-    for (int k = 1; k < 13; ++k) r[k] = min(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+  for (int j = 0; j < CMP_IPT; ++j) v[j] = iv[j] >= 0 ? phi[iv[j]] : 0.0f;
+  int c = 0;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    if (iv[j] >= 0) {
+      const float x = v[j];
+      const float cl = (x != x) ? x : fminf(fmaxf(x, -cap), cap);
+      if (cl != x && x == x) phi[iv[j]] = cl;
+      c += fabsf(cl) < thresh ? 1 : 0;
+    }
   }
-  __shared__ int shr[13][NW];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) {
+  int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
+  if (threadIdx.x == 0) counts[blockIdx.x] = tot;
+}
+
+// Pass 2: the band entries in list order, occupancy (phi < 0) of every listed
+// node, the band and inside boxes of the listed nodes, and the number of
+// listed inside nodes off the band (info->static_inside).
+__global__ void __launch_bounds__(CMP_THREADS) k_list_band_write(const float* __restrict__ phi,
+                                                                 const int32_t* __restrict__ idx, long long m,
+                                                                 float thresh, const int* offsets, int32_t* out,
+                                                                 long long capacity, float* occ, int syz, int nz,
+                                                                 DivMagic dsyz, DivMagic dnz, svie_band_info* info) {
+  __shared__ int sh[33];
+  const long long wb = warp_base() + (threadIdx.x & 31);
+  int iv[CMP_IPT];
+  float v[CMP_IPT];
 #pragma unroll
-    for (int k = 0; k < 13; ++k) shr[k][wid] = r[k];
+  for (int j = 0; j < CMP_IPT; ++j) iv[j] = wb + 32 * j < m ? __ldg(idx + wb + 32 * j) : -1;
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) v[j] = iv[j] >= 0 ? phi[iv[j]] : 0.0f;
+  unsigned int bal[CMP_IPT];
+  int wt = 0, inside_static = 0;
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {-1, -1, -1};
+  int ilo[3] = {INT_MAX, INT_MAX, INT_MAX}, ihi[3] = {-1, -1, -1};
+#pragma unroll
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const bool valid = iv[j] >= 0;
+    const bool sel = valid && fabsf(v[j]) < thresh;
+    const bool neg = valid && v[j] < 0.0f;
+    if (valid && occ) occ[iv[j]] = neg ? 1.0f : 0.0f;
+    bal[j] = __ballot_sync(0xffffffffu, sel);
+    wt += __popc(bal[j]);
+    if (sel || neg) {
+      const int i = iv[j], x = div_exact(i, dsyz), r = i - x * syz, y = div_exact(r, dnz), z = r - y * nz;
+      const int c[3] = {x, y, z};
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        if (sel) { lo[a] = min(lo[a], c[a]); hi[a] = max(hi[a], c[a]); }
+        if (neg) { ilo[a] = min(ilo[a], c[a]); ihi[a] = max(ihi[a], c[a]); }
+      }
+      inside_static += (neg && !sel) ? 1 : 0;
+    }
   }
-  __syncthreads();
-  if (wid != 0) return;
-#pragma unroll
-  for (int k = 0; k < 13; ++k) r[k] = lane < NW ? shr[k][lane] : (k == 0 ? 0 : INT_MAX);
-#pragma unroll
-  for (int o = NW / 2; o > 0; o >>= 1) {
-    r[0] += __shfl_xor_sync(0xffffffffu, r[0], o);
-#pragma unroll
-    for (int k = 1; k < 13; ++k) r[k] = min(r[k], __shfl_xor_sync(0xffffffffu, r[k], o));
+  int tot;
+  const long long o = (long long)offsets[blockIdx.x] + warp_offsets(wt, sh, &tot);
+  write_selected(bal, o, out, capacity, [&](int j) { return (int32_t)iv[j]; });
+  band_info_commit(inside_static, lo, hi, ilo, ihi, info);
+}
+
+// Listed nodes with phi < 0 whose bit in `marked` (the bit layout of
+// svie_reinit_bits) is clear, added to *count.
+__global__ void __launch_bounds__(CMP_THREADS) k_list_inside_off_mask(const float* __restrict__ phi,
+                                                                      const int32_t* __restrict__ idx, long long m,
+                                                                      const uint32_t* __restrict__ marked, int nz,
+                                                                      int nzw, DivMagic dnz,
+                                                                      unsigned long long* count) {
+  __shared__ int sh[CMP_THREADS / 32];
+  const long long wb = warp_base() + (threadIdx.x & 31);
+  int c = 0;
+#pragma unroll 4
+  for (int j = 0; j < CMP_IPT; ++j) {
+    const long long e = wb + 32 * j;
+    if (e < m) {
+      const int i = __ldg(idx + e);
+      if (__ldg(phi + i) < 0.0f) {
+        const int row = div_exact(i, dnz), z = i - row * nz;
+        c += ((__ldg(marked + (long long)row * nzw + (z >> 5)) >> (z & 31)) & 1u) ? 0 : 1;
+      }
+    }
   }
-  if (lane != 0) return;
-  if (r[0]) atomicAdd((unsigned long long*)&info->static_inside, (unsigned long long)r[0]);
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    if (r[1 + a] != INT_MAX) atomicMin(&info->lo[a], r[1 + a]);
-    if (-r[4 + a] >= 0) atomicMax(&info->hi[a], -r[4 + a]);
-    if (r[7 + a] != INT_MAX) atomicMin(&info->ilo[a], r[7 + a]);
-    if (-r[10 + a] >= 0) atomicMax(&info->ihi[a], -r[10 + a]);
-  }
+  const int tot = block_reduce(c, sh, [](int a, int b) { return a + b; }, 0);
+  if (threadIdx.x == 0 && tot) atomicAdd(count, (unsigned long long)tot);
 }
 
 template <class Pred>
@@ -754,6 +862,69 @@ int svie_brick_band_write(const float* phi, int nx, int ny, int nz, float thresh
   k_brick_band_write<<<(unsigned)nb, CMP_THREADS, 0, (cudaStream_t)stream>>>(phi, G, thresh, (const int*)ws, out,
                                                                              capacity, occ, info);
   return launch_status("svie_brick_band_write");
+}
+
+size_t svie_list_workspace_bytes(int64_t m) {
+  return (size_t)((m + svie::CMP_TILE - 1) / svie::CMP_TILE + 1) * sizeof(int) + 256;
+}
+
+int svie_list_band_scan(float* phi, const int32_t* idx, int64_t m, float cap, float thresh, void* ws, size_t ws_bytes,
+                        svie_band_info* info, void* stream) {
+  using namespace svie;
+  if (!phi || !info || m < 0 || (m > 0 && !idx)) {
+    set_error("svie_list_band_scan: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_list_workspace_bytes(m)) {
+    set_error("svie_list_band_scan: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long nb = (m + CMP_TILE - 1) / CMP_TILE;
+  if (nb > 0) k_list_band_count<<<(unsigned)nb, CMP_THREADS, 0, s>>>(phi, idx, m, cap, thresh, (int*)ws);
+  k_scan_counts<<<1, 1024, 0, s>>>((int*)ws, nb, (long long*)&info->count);
+  k_info_init<<<1, 1, 0, s>>>(info);
+  return launch_status("svie_list_band_scan", nb > 0 ? 3 : 2);
+}
+
+int svie_list_band_write(const float* phi, const int32_t* idx, int64_t m, int nx, int ny, int nz, float thresh,
+                         const void* ws, size_t ws_bytes, int32_t* out, int64_t capacity, float* occ,
+                         svie_band_info* info, void* stream) {
+  using namespace svie;
+  if (!phi || !info || m < 0 || (m > 0 && !idx) || (capacity > 0 && !out) || nx <= 0 || ny <= 0 || nz <= 0 ||
+      (long long)nx * ny * nz >= (1LL << 31)) {
+    set_error("svie_list_band_write: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_list_workspace_bytes(m)) {
+    set_error("svie_list_band_write: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  const long long nb = (m + CMP_TILE - 1) / CMP_TILE;
+  if (nb == 0) return SVIE_OK;
+  const int syz = ny * nz;
+  k_list_band_write<<<(unsigned)nb, CMP_THREADS, 0, (cudaStream_t)stream>>>(
+      phi, idx, m, thresh, (const int*)ws, out, capacity, occ, syz, nz, div_magic(syz), div_magic(nz), info);
+  return launch_status("svie_list_band_write");
+}
+
+int svie_list_inside_off_mask(const float* phi, const int32_t* idx, int64_t m, const uint32_t* marked, int nx, int ny,
+                              int nz, uint64_t* count, void* stream) {
+  using namespace svie;
+  if (!phi || !marked || !count || m < 0 || (m > 0 && !idx) || nz <= 0) {
+    set_error("svie_list_inside_off_mask: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(count, 0, sizeof(uint64_t), s) != cudaSuccess) {
+    set_error("svie_list_inside_off_mask: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  const long long nb = (m + CMP_TILE - 1) / CMP_TILE;
+  if (nb == 0) return SVIE_OK;
+  k_list_inside_off_mask<<<(unsigned)nb, CMP_THREADS, 0, s>>>(phi, idx, m, marked, nz, (nz + 31) / 32, div_magic(nz),
+                                                               (unsigned long long*)count);
+  return launch_status("svie_list_inside_off_mask");
 }
 
 }  // extern "C"

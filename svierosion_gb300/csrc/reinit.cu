@@ -654,7 +654,7 @@ size_t svie_reinit_bits_bytes(int nx, int ny, int nz) {
 }
 
 int svie_reinit_bits(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin, uint32_t* bits,
-                     uint32_t* tmp, void* stream) {
+                     uint32_t* tmp, uint32_t* marked, void* stream) {
   if (!bits || !tmp || nx <= 0 || ny <= 0 || nz <= 0 || (long long)nx * ny * nz >= (1LL << 31) || dilation < 0 ||
       dilation > 31 || margin < 0 || m < 0 || (m > 0 && !band)) {
     set_error("svie_reinit_bits: bad arguments (dilation <= 31)");
@@ -663,17 +663,19 @@ int svie_reinit_bits(const int32_t* band, int64_t m, int nx, int ny, int nz, int
   cudaStream_t s = (cudaStream_t)stream;
   const int nzw = (nz + 31) / 32;
   const long long nwords = (long long)nx * ny * nzw;
-  if (cudaMemsetAsync(tmp, 0, (size_t)nwords * sizeof(uint32_t), s) != cudaSuccess) {
+  // the band's own bits go to `marked` when given (kept for the caller), else to tmp
+  uint32_t* mk = marked ? marked : tmp;
+  if (cudaMemsetAsync(mk, 0, (size_t)nwords * sizeof(uint32_t), s) != cudaSuccess) {
     set_error("svie_reinit_bits: memset failed");
     return SVIE_ERR_LAUNCH;
   }
   int launches = 3;
   if (m > 0) {
-    k_mark_bits<<<blocks_for(m, 256), 256, 0, s>>>(band, m, nz, nzw, tmp);
+    k_mark_bits<<<blocks_for(m, 256), 256, 0, s>>>(band, m, nz, nzw, mk);
     ++launches;
   }
   const int nb = blocks_for(nwords, 256);
-  k_dilate_bits_z<<<nb, 256, 0, s>>>(tmp, bits, nwords, nzw, dilation);
+  k_dilate_bits_z<<<nb, 256, 0, s>>>(mk, bits, nwords, nzw, dilation);
   k_dilate_bits_rows<<<nb, 256, 0, s>>>(bits, tmp, nx, ny, nz, nzw, 1, dilation, 0);
   k_dilate_bits_rows<<<nb, 256, 0, s>>>(tmp, bits, nx, ny, nz, nzw, 0, dilation, margin);
   return launch_status("svie_reinit_bits", launches);

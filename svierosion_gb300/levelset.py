@@ -274,24 +274,39 @@ class LevelSet:
         return torch.minimum(p.clamp_min(1.0), hi)
 
     # --------------------------------------------------- reinitialisation
-    def reinitialize(self, iterations: int = 12, cfl: float = 0.45, dilation: int = 3, timer=None) -> None:
+    def reinitialize(self, iterations: int = 12, cfl: float = 0.45, dilation: int = 3, timer=None,
+                     work_set_rebuild: bool = False) -> None:
         """Subcell-fixed PDE reinitialisation (Min 2010) on the dilated band (levelset.py:154-183).
 
         ``timer`` (optional profiling.KernelTimer): events around the sweeps
-        ("reinit_sweep", 2 iterations launches) and the work-set size."""
+        ("reinit_sweep", 2 iterations launches) and the work-set size.
+
+        ``work_set_rebuild``: rebuild the band over the work set only, for a phi
+        that changed only on the band since the last rebuild (the evolution
+        loop's case).  Off the work set phi is then unchanged and clamped, so
+        the band, its order, phi, the occupancy and ``static_inside`` equal the
+        full rebuild's; the inside box becomes the old box joined with the work
+        set's inside nodes (a box that contains the exact one)."""
         n = self.grid.size
         nx, ny, nz = self.grid.shape
         sc = self.scratch
+        lib = nat.lib()
+        fast = work_set_rebuild and dilation <= 31
         # the work mask (band dilated, margin cleared) as bits, listed in brick order
+        marked = None
         if dilation <= 31:
-            kind, nbytes, call = 2, nat.lib().svie_reinit_bits_bytes(nx, ny, nz), "svie_reinit_bits"
+            kind, nbytes = 2, lib.svie_reinit_bits_bytes(nx, ny, nz)
+            mask, tmp = sc.get("reinit_mask", nbytes), sc.get("reinit_tmp", nbytes)
+            if fast:
+                marked = sc.get("reinit_marked", nbytes)  # the band's own bits, kept
+            nat.call("svie_reinit_bits", nat.ptr(self.work32), self.work32.numel(), nx, ny, nz, int(dilation), MARGIN,
+                     nat.ptr(mask), nat.ptr(tmp), nat.ptr(marked), nat.stream())
         else:
-            kind, nbytes, call = 0, n, "svie_reinit_mask"
-        mask = sc.get("reinit_mask", nbytes)
-        tmp = sc.get("reinit_tmp", nbytes)
-        nat.call(call, nat.ptr(self.work32), self.work32.numel(), nx, ny, nz, int(dilation), MARGIN,
-                 nat.ptr(mask), nat.ptr(tmp), nat.stream())
-        ws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
+            kind = 0
+            mask, tmp = sc.get("reinit_mask", n), sc.get("reinit_tmp", n)
+            nat.call("svie_reinit_mask", nat.ptr(self.work32), self.work32.numel(), nx, ny, nz, int(dilation), MARGIN,
+                     nat.ptr(mask), nat.ptr(tmp), nat.stream())
+        ws = sc.get("brick", lib.svie_brick_workspace_bytes(nx, ny, nz))
         cnt = sc.get("reinit_count", 8)
         nat.call("svie_brick_scan", kind, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
                  nat.stream())
@@ -299,9 +314,15 @@ class LevelSet:
         idx = sc.get("reinit_idx", 4 * max(m, 1))[:4 * m].view(torch.int32)
         nat.call("svie_brick_write", kind, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
                  nat.stream())
-        geo = sc.get("reinit_geo", nat.lib().svie_reinit_geometry_bytes(m))
+        geo = sc.get("reinit_geo", lib.svie_reinit_geometry_bytes(m))
         nat.call("svie_reinit_geometry", nat.ptr(self.flat), nat.ptr(idx), m, *self.strides, self.h, cfl,
                  nat.ptr(geo), nat.stream())
+        off_inside = None
+        if fast:
+            # inside work-set nodes off the old band, before the sweeps
+            off_inside = sc.get("reinit_off_inside", 8)
+            nat.call("svie_list_inside_off_mask", nat.ptr(self.flat), nat.ptr(idx), m, nat.ptr(marked), nx, ny, nz,
+                     nat.ptr(off_inside), nat.stream())
         phi_tmp = sc.get("reinit_phi", 4 * n)
         timed = timer is not None and timer.wants("reinit_sweep") and m > 0 and iterations > 0
         if timed:
@@ -313,7 +334,46 @@ class LevelSet:
             ev[1].record()
             timer.add(["reinit_sweep"], ev, [2 * int(iterations)])
             timer.note("reinit_work", m)
-        self.rebuild_band()
+        if fast:
+            self.rebuild_band_on(idx, off_inside)
+        else:
+            self.rebuild_band()
+
+    def rebuild_band_on(self, idx: torch.Tensor, off_inside: torch.Tensor) -> None:
+        """rebuild_band over the node list ``idx`` (the work set), valid when phi
+        changed only on it since the last rebuild; ``off_inside`` (device int64)
+        holds the listed nodes that were inside and off the old band before phi
+        changed, so that ``static_inside`` stays exact."""
+        cap, thresh = self._thresh()
+        nx, ny, nz = self.grid.shape
+        m = idx.numel()
+        lib = nat.lib()
+        ws = self.scratch.get("list", lib.svie_list_workspace_bytes(m))
+        nat.call("svie_list_band_scan", nat.ptr(self.flat), nat.ptr(idx), m, cap, thresh, nat.ptr(ws), ws.numel(),
+                 nat.ptr(self._info), nat.stream())
+        count = int(_read(self._info, nat.BAND_INFO_DTYPE)["count"])
+        work = torch.empty(count, dtype=torch.int32, device=self.device)
+        nat.call("svie_list_band_write", nat.ptr(self.flat), nat.ptr(idx), m, nx, ny, nz, thresh, nat.ptr(ws),
+                 ws.numel(), nat.ptr(work), count, nat.ptr(self.occ), nat.ptr(self._info), nat.stream())
+        info = _read(self._info, nat.BAND_INFO_DTYPE)
+        before = int(off_inside[:8].cpu().view(torch.int64)[0])
+        self.static_inside = self.static_inside - before + int(info["static_inside"])
+        self.work32 = work
+        self._band32 = None
+        self._band64 = None
+        self.band_lo = tuple(int(v) for v in info["lo"])
+        self.band_hi = tuple(int(v) for v in info["hi"])
+        ilo, ihi = [int(v) for v in info["ilo"]], [int(v) for v in info["ihi"]]
+        if self.inside_hi[0] >= 0:
+            ilo = [min(a, b) for a, b in zip(ilo, self.inside_lo)]
+            ihi = [max(a, b) for a, b in zip(ihi, self.inside_hi)]
+        self.inside_lo, self.inside_hi = tuple(ilo), tuple(ihi)
+        self.occ_current = False
+        if count:
+            shape = self.grid.shape
+            for ax in range(3):
+                if self.band_lo[ax] < MARGIN or self.band_hi[ax] > shape[ax] - 1 - MARGIN:
+                    raise RuntimeError("narrow band reaches the grid boundary; enlarge the padding")
 
 
 # ------------------------------------------------------------- interpolation

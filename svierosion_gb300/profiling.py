@@ -112,8 +112,9 @@ def main(argv=None) -> int:
             ev[0].record()
             nbits = nat.lib().svie_reinit_bits_bytes(nx, ny, nz)
             mask, tmp = sc.get("reinit_mask", nbits), sc.get("reinit_tmp", nbits)
+            marked = sc.get("reinit_marked", nbits)
             nat.call("svie_reinit_bits", nat.ptr(ls.work32), ls.work32.numel(), nx, ny, nz, 3, 4, nat.ptr(mask),
-                     nat.ptr(tmp), nat.stream())
+                     nat.ptr(tmp), nat.ptr(marked), nat.stream())
             ev[1].record()
             ws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
             cnt = sc.get("reinit_count", 8)
@@ -127,12 +128,15 @@ def main(argv=None) -> int:
             geo = sc.get("reinit_geo", nat.lib().svie_reinit_geometry_bytes(m))
             nat.call("svie_reinit_geometry", nat.ptr(ls.flat), nat.ptr(idx), m, *ls.strides, ls.h, 0.45, nat.ptr(geo),
                      nat.stream())
+            off = sc.get("reinit_off_inside", 8)
+            nat.call("svie_list_inside_off_mask", nat.ptr(ls.flat), nat.ptr(idx), m, nat.ptr(marked), nx, ny, nz,
+                     nat.ptr(off), nat.stream())
             ev[3].record()
             pt = sc.get("reinit_phi", 4 * n)
             nat.call("svie_reinit_iterate", nat.ptr(ls.flat), nat.ptr(pt), n, nat.ptr(idx), m, *ls.strides, ls.h,
                      nat.ptr(geo), 20, nat.stream())
             ev[4].record()
-            ls.rebuild_band()
+            ls.rebuild_band_on(idx, off)
             ev[5].record()
             torch.cuda.synchronize()
             t = [ev[i].elapsed_time(ev[i + 1]) for i in range(5)]

@@ -103,3 +103,26 @@ def test_erode_stops_at_target():
                                                     target_fraction=0.93), extract_meshes=False, keep_state=True)
     assert res.stop_reason == "target_volume"
     assert abs(res.fraction - 0.93) < 1e-5
+
+
+def test_work_set_rebuild_equals_full_rebuild():
+    """After evolution steps (phi changed on the band only), reinitialisation with the band rebuilt
+    over the work set gives exactly the state of a full-grid rebuild: phi, band list and order,
+    occupancy, static inside count and band box; the inside box contains the exact one."""
+    mesh = shapes.fragment(3, seed=1)
+    params = S.ErosionParams(law="svi", radius=0.2, k=1, s=1, t=0.93, resolution=56)
+    L = float((mesh.bounds[1] - mesh.bounds[0]).max())
+    states = []
+    for fast in (False, True):
+        g = S.make_grid(mesh, params)
+        ls = S.LevelSet(S.mesh_to_sdf(mesh, g, band=6), g, width=6)
+        sim = S.ErosionSimulation(ls, params.make_law(length_scale=L), reinit_distance=1e9)  # no reinit in run
+        sim.run(target_fraction=None, max_steps=4)
+        ls.reinitialize(20, work_set_rebuild=fast)
+        states.append((ls.flat.cpu().numpy(), ls.work32.cpu().numpy(), ls.occ.cpu().numpy(), ls.static_inside,
+                       ls.band_lo, ls.band_hi, ls.inside_lo, ls.inside_hi, ls.volume()))
+    full, fast = states
+    for k in range(6):
+        assert np.array_equal(np.asarray(full[k]), np.asarray(fast[k])), k
+    assert all(a <= b for a, b in zip(fast[6], full[6])) and all(a >= b for a, b in zip(fast[7], full[7]))
+    assert fast[8] == full[8]

@@ -81,8 +81,14 @@ def test_reinit_bits_match_byte_mask(shape, dilation, margin):
     nb = lib.svie_reinit_bits_bytes(nx, ny, nz)
     bits = torch.empty(nb // 4, dtype=torch.int32, device="cuda")
     btmp = torch.empty_like(bits)
+    marked = torch.empty_like(bits)
     nat.call("svie_reinit_bits", nat.ptr(band), band.numel(), nx, ny, nz, dilation, margin, nat.ptr(bits),
-             nat.ptr(btmp), nat.stream())
+             nat.ptr(btmp), nat.ptr(marked), nat.stream())
+    # the band's own bits, kept in `marked`
+    mw = marked.cpu().numpy().view(np.uint32).reshape(nx, ny, -1)
+    zz = np.arange(nz)
+    own = ((mw[:, :, zz // 32] >> (zz % 32).astype(np.uint32)) & 1).astype(bool).reshape(-1)
+    assert np.array_equal(np.flatnonzero(own), np.sort(band.cpu().numpy()))
     # unpack: bit z % 32 of word z // 32 of row (x, y)
     w = bits.cpu().numpy().view(np.uint32).reshape(nx, ny, -1)
     z = np.arange(nz)
