@@ -377,34 +377,31 @@ SVIE_DEV void sweep_update(const float* __restrict__ src, float* __restrict__ ds
   }
 }
 
-// The entries without a flagged crossing (about nine in ten): no subcell
-// branch, no distance reads, dtau = cfl max(h, 1e-3 h).  The others are left
-// to k_reinit_sweep_cross, so no warp runs the subcell branch for a few lanes.
+// One launch per half-step.  Blocks [0, nbm) take the entries without a
+// flagged crossing (about nine in ten): no subcell branch, no distance reads,
+// dtau = cfl max(h, 1e-3 h).  The blocks after them take the entries with a
+// crossing from the compact list (count wx[W]), grid-stride, so that no warp
+// runs the subcell branch for a few lanes; they are scheduled last and fill
+// the tail of the first part.
 __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
                                                              const int32_t* __restrict__ idx, long long m, int sx,
                                                              int sy, int sz, float h, float rh, float rhh, Geo g,
-                                                             int second) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
-  const uint32_t flags = __ldg(g.meta + t);
-  if (flags & 63u) return;
+                                                             int second, int nbm) {
   const float cfl = __ldg(g.cfl);
-  const int i = __ldg(idx + t);
-  float hmin;
-  const float r = reinit_rhs_at<false>(src, i, g, 0, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
-  sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
-}
-
-// The entries with a flagged crossing, from the compact list (count wx[W]),
-// grid-stride over a grid of about the resident CTAs.
-__global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep_cross(const float* __restrict__ src,
-                                                                   float* __restrict__ dst,
-                                                                   const int32_t* __restrict__ idx, int sx, int sy,
-                                                                   int sz, float h, float rh, float rhh, Geo g,
-                                                                   int second) {
+  if ((int)blockIdx.x < nbm) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    const uint32_t flags = __ldg(g.meta + t);
+    if (flags & 63u) return;
+    const int i = __ldg(idx + t);
+    float hmin;
+    const float r = reinit_rhs_at<false>(src, i, g, 0, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
+    sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
+    return;
+  }
   const int X = __ldg(g.wx + g.W);
-  const float cfl = __ldg(g.cfl);
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < X; k += gridDim.x * blockDim.x) {
+  const int stride = (gridDim.x - nbm) * blockDim.x;
+  for (int k = (blockIdx.x - nbm) * blockDim.x + threadIdx.x; k < X; k += stride) {
     const int t = __ldg(g.xlist + k);
     const uint32_t flags = __ldg(g.meta + t);
     const int i = __ldg(idx + t);
@@ -721,12 +718,10 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int nbx = (int)std::min<long long>((long long)blocks_for(m, RI_THREADS), 8LL * nsm);
   for (int it = 0; it < iterations; ++it) {
-    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, g, 0);
-    k_reinit_sweep_cross<<<nbx, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, sx, sy, sz, h, rh, rhh, g, 0);
-    k_reinit_sweep<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, rhh, g, 1);
-    k_reinit_sweep_cross<<<nbx, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, sx, sy, sz, h, rh, rhh, g, 1);
+    k_reinit_sweep<<<nb + nbx, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, g, 0, nb);
+    k_reinit_sweep<<<nb + nbx, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, rhh, g, 1, nb);
   }
-  return launch_status("svie_reinit_iterate", 4 * iterations);
+  return launch_status("svie_reinit_iterate", 2 * iterations);
 }
 
 int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz, float h,

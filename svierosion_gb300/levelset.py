@@ -351,11 +351,14 @@ class LevelSet:
         ws = self.scratch.get("list", lib.svie_list_workspace_bytes(m))
         nat.call("svie_list_band_scan", nat.ptr(self.flat), nat.ptr(idx), m, cap, thresh, nat.ptr(ws), ws.numel(),
                  nat.ptr(self._info), nat.stream())
-        count = int(_read(self._info, nat.BAND_INFO_DTYPE)["count"])
-        work = torch.empty(count, dtype=torch.int32, device=self.device)
+        # the band is part of the list: a list-sized buffer takes it without
+        # reading the count first (one host sync for count and info together)
+        buf = torch.empty(max(m, 1), dtype=torch.int32, device=self.device)
         nat.call("svie_list_band_write", nat.ptr(self.flat), nat.ptr(idx), m, nx, ny, nz, thresh, nat.ptr(ws),
-                 ws.numel(), nat.ptr(work), count, nat.ptr(self.occ), nat.ptr(self._info), nat.stream())
+                 ws.numel(), nat.ptr(buf), m, nat.ptr(self.occ), nat.ptr(self._info), nat.stream())
         info = _read(self._info, nat.BAND_INFO_DTYPE)
+        count = int(info["count"])
+        work = buf[:count]
         before = int(off_inside[:8].cpu().view(torch.int64)[0])
         self.static_inside = self.static_inside - before + int(info["static_inside"])
         self.work32 = work
