@@ -27,6 +27,25 @@ def compile_enabled() -> bool:
     return _COMPILE
 
 
+class Kernel:
+    """The reference's compile wrapper (kernels.py:35-66), kept for callers that
+    decorate their own torch functions with ``kernel``: here the function runs
+    as written, because nothing in this package is compiled at run time."""
+
+    def __init__(self, fn):
+        self.fn = fn
+        self.__doc__ = fn.__doc__
+        self.__name__ = fn.__name__
+
+    def __call__(self, *args):
+        return self.fn(*args)
+
+
+def kernel(fn) -> Kernel:
+    """Decorator form of Kernel (kernels.py:77-78)."""
+    return Kernel(fn)
+
+
 def _flat(flat: torch.Tensor) -> torch.Tensor:
     if flat.dtype != torch.float32 or not flat.is_contiguous():
         raise ValueError("flat must be a contiguous float32 tensor")
