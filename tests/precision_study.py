@@ -9,8 +9,10 @@ does not hold a GPU:
     python tests/precision_study.py compare gpurun_out/precision.npz  # anywhere: float64 runs, report
 
 The report (one JSON line per law) gives max |N_r(fp32) - N_r(fp64)| on the initial grid, the largest
-volume-fraction difference along the trajectory, both stopping steps, and max |phi(fp32) - phi(fp64)|
-over the final band in cells (an upper bound of the zero-level-set distance where |grad phi| ~ 1).
+volume-fraction difference along the trajectory, both stopping steps, max |phi(fp32) - phi(fp64)|
+over the final band in cells, and the symmetric Hausdorff distance in cells between the two final
+zero level sets, each extracted by the CPU marching cubes of oracle/marching.py (vertex-to-surface
+distances, exact over the triangles with the 16 nearest centroids).
 """
 
 from __future__ import annotations
@@ -82,6 +84,31 @@ def run_gpu(path: str) -> None:
     print("saved", path)
 
 
+def _to_surface(pts, verts, faces, k=16):
+    """Distance from each point to the mesh, exact over the k triangles with the nearest centroids."""
+    from scipy.spatial import cKDTree
+
+    from oracle.reference_np import point_triangle_distance2
+
+    tri = verts[faces].astype(np.float64)
+    _, cand = cKDTree(tri.mean(1)).query(pts, k=k)
+    best = np.full(len(pts), np.inf)
+    for j in range(k):
+        t = tri[cand[:, j]]
+        best = np.minimum(best, point_triangle_distance2(pts, t[:, 0], t[:, 1], t[:, 2]))
+    return np.sqrt(best)
+
+
+def _hausdorff_cells(phi32, band32, phi64, band64) -> float:
+    """Symmetric Hausdorff distance (grid cells) between the zero sets of two fields."""
+    from oracle import marching as M
+
+    va, fa = M.extract(phi32, band32)
+    vb, fb = M.extract(phi64, band64)
+    va, vb = va.astype(np.float64), vb.astype(np.float64)
+    return float(max(_to_surface(va, vb, fb).max(), _to_surface(vb, va, fa).max()))
+
+
 def compare(path: str) -> None:
     from oracle.fp64 import fp64
 
@@ -110,6 +137,14 @@ def compare(path: str) -> None:
             common = np.intersect1d(band32, ref.band)
             pos = np.searchsorted(band32, common)
             rep["max_abs_dphi_cells"] = float(np.abs(d[name + "/phi_band"][pos] - ref.flat[common]).max() / h)
+            # the float32 field: band values on the band, the clamped value (sign of the float64 field,
+            # the same far from the interface) elsewhere
+            cap = np.float32(params.band * h)
+            f64 = ref.flat.reshape(shape)
+            phi32 = np.where(f64 < 0, -cap, cap).astype(np.float32).reshape(-1)
+            phi32[band32] = d[name + "/phi_band"]
+            rep["hausdorff_cells"] = _hausdorff_cells(phi32.reshape(shape), band32.astype(np.int64),
+                                                      f64.astype(np.float32), np.asarray(ref.band, dtype=np.int64))
         print(json.dumps(rep), flush=True)
 
 
