@@ -336,6 +336,15 @@ int svie_set_f64(double* dst, double value, void* stream);
  * maxbits[0], maxbits[1]). */
 int svie_mesh_pieces(const double* vertices, const int32_t* faces, int64_t T, double sx, double sy, double sz,
                      float* out, float* first_edge, uint32_t* maxbits, void* stream);
+/* Exact bounding box of V float64 vertices (V, 3): out = (min x, min y, min z, max x, max y, max z),
+ * numpy's per-column min / max (TriMesh.bounds, meshio.py:35-37); ws holds 48 bytes. */
+int svie_mesh_bounds(const double* vertices, int64_t V, void* ws, size_t ws_bytes, double* out, void* stream);
+/* out[0], out[1] = the k0-th and k1-th smallest of n floats (0-based; np.partition's kth values) by
+ * an exact radix select over order-preserving keys: the middle values of np.median over the
+ * first-edge lengths of api.py:122-126.  Workspace svie_order_stats_bytes(). */
+size_t svie_order_stats_bytes(void);
+int svie_order_stats_f32(const float* x, int64_t n, int64_t k0, int64_t k1, void* ws, size_t ws_bytes, float* out,
+                         void* stream);
 size_t svie_piece_grid_bytes(int64_t T, int gx, int gy, int gz);
 int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float oz, float cs, int gx, int gy,
                           int gz, void* ws, size_t ws_bytes, void* stream);
@@ -366,6 +375,17 @@ int svie_surface_project(const float* phi, int ny, int nz, float* verts, int64_t
  * orientation test of surface.py:54-55. */
 int svie_surface_signed_volume(const float* verts, const int32_t* faces, int64_t nt, double cx, double cy,
                                double cz, double* out, void* stream);
+/* The host mesh of surface.py:52-56 written on the device: world = origin + h * verts (float64,
+ * rounded as numpy rounds it), faces64 (int64) reversed when *vol < 0, and *bad = the number of
+ * faces with a negative vertex index (a crossing outside the band, an error). */
+int svie_surface_finish(const float* verts, int64_t nv, const int32_t* faces, int64_t nt, const double* vol,
+                        double ox, double oy, double oz, double h, double* world, int64_t* faces64, int* bad,
+                        void* stream);
+/* out = float32((points - (sx, sy, sz)) / scale) for n float64 points (n, 3): the query points of
+ * api.py:147-153 (scale 1, shifted by the pieces' centre) and Grid.to_index before the float32
+ * cast of surface.py:59-67 (shift = origin, scale = h), computed as numpy computes them. */
+int svie_points_f32(const double* points, int64_t n, double sx, double sy, double sz, double scale, float* out,
+                    void* stream);
 
 /* ------------------------------------------------------ reinitialisation */
 /* LevelSet.reinitialize (svierosion/levelset.py:154-183): work mask = band

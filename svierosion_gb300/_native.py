@@ -141,7 +141,12 @@ _SIGS = {
     "svie_reinit_iterate": (I, [V, V, I64, V, I64, I64, I64, I64, F, V, I, V]),
     "svie_reinit_rhs": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),
     "svie_mesh_pieces": (I, [V, V, I64, D, D, D, V, V, V, V]),
+    "svie_mesh_bounds": (I, [V, I64, V, Z, V, V]),
+    "svie_order_stats_bytes": (Z, []),
+    "svie_order_stats_f32": (I, [V, I64, I64, I64, V, Z, V, V]),
     "svie_surface_signed_volume": (I, [V, V, I64, D, D, D, V, V]),
+    "svie_surface_finish": (I, [V, I64, V, I64, V, D, D, D, D, V, V, V, V]),
+    "svie_points_f32": (I, [V, I64, D, D, D, D, V, V]),
     "svie_piece_grid_bytes": (Z, [I64, I, I, I]),
     "svie_piece_grid_build": (I, [V, I64, F, F, F, F, I, I, I, V, Z, V]),
     "svie_point_mesh_distance": (I, [V, I64, V, I64, F, F, F, F, I, I, I, V, Z, F, V, V]),

@@ -12,6 +12,8 @@
 //  * the signed volume of the mesh in float64.
 // Hash tables live in caller workspaces; every probe loop is bounded and
 // reports SVIE_ERR_CAPACITY through a device flag instead of spinning.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace svie {
@@ -228,6 +230,132 @@ __global__ void k_mesh_pieces(const double* __restrict__ v, const int32_t* __res
   }
 }
 
+// ------------------------------------------------------------ bounding box
+// Order-preserving unsigned keys of IEEE values: the sign bit set for
+// non-negative values, all bits flipped for negative ones.  min / max of keys
+// are the min / max of the values (min and max are exact, so the box equals
+// numpy's per-column min / max; -0.0 orders below +0.0, which compare equal).
+SVIE_DEV unsigned long long order_key64(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+SVIE_DEV double order_value64(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+SVIE_DEV unsigned int order_key32(float x) {
+  const unsigned int b = __float_as_uint(x);
+  return (b >> 31) ? ~b : (b | 0x80000000u);
+}
+
+SVIE_DEV float order_value32(unsigned int k) { return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k); }
+
+// keys[0..2] = min key per axis, keys[3..5] = max key per axis
+__global__ void k_mesh_bounds(const double* __restrict__ v, long long n, unsigned long long* keys) {
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    for (int a = 0; a < 3; ++a) {
+      const unsigned long long k = order_key64(v[3 * i + a]);
+      lo[a] = k < lo[a] ? k : lo[a];
+      hi[a] = k > hi[a] ? k : hi[a];
+    }
+  for (int a = 0; a < 3; ++a)
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long l = __shfl_xor_sync(0xffffffffu, lo[a], o), h = __shfl_xor_sync(0xffffffffu, hi[a], o);
+      lo[a] = l < lo[a] ? l : lo[a];
+      hi[a] = h > hi[a] ? h : hi[a];
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(keys + a, lo[a]);
+      atomicMax(keys + 3 + a, hi[a]);
+    }
+}
+
+__global__ void k_mesh_bounds_values(const unsigned long long* keys, double* out) {
+  if (threadIdx.x < 6) out[threadIdx.x] = order_value64(keys[threadIdx.x]);
+}
+
+// ------------------------------------------------------ order statistics
+// Exact k-th smallest values of a float array by a three-pass radix select
+// over the order-preserving keys (digits of 11, 11 and 10 bits from the top).
+// Two ranks are selected together (the two middle values of a median).  Each
+// pass histograms the digit of the keys that match the selected prefix; one
+// warp per rank then finds the digit that holds the rank.
+constexpr int OS_BINS = 2048;
+constexpr int OS_PASSES = 3;
+__constant__ int c_os_shift[OS_PASSES] = {21, 10, 0};
+__constant__ int c_os_width[OS_PASSES] = {11, 11, 10};
+
+struct OrderState {
+  unsigned int prefix[2];     // selected high bits of each rank's key
+  long long rank[2];          // rank among the keys with that prefix
+};
+
+__global__ void __launch_bounds__(512) k_os_hist(const float* __restrict__ x, long long n, int pass,
+                                                 const OrderState* __restrict__ st, unsigned int* __restrict__ hist) {
+  __shared__ unsigned int h[2 * OS_BINS];
+  for (int i = threadIdx.x; i < 2 * OS_BINS; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const int shift = c_os_shift[pass], width = c_os_width[pass], top = shift + width;
+  const unsigned int p0 = st->prefix[0], p1 = st->prefix[1], dmask = (1u << width) - 1u;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long rounds = (n + stride - 1) / stride;  // the same for every lane: full-warp matches
+  for (long long r = 0; r < rounds; ++r) {
+    const long long i = r * stride + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned int k = i < n ? order_key32(x[i]) : 0u;
+    const unsigned int hi = top >= 32 ? 0u : (k >> top);
+    const unsigned int d = (k >> shift) & dmask;
+    for (int s = 0; s < 2; ++s) {
+      const bool take = i < n && hi == (s ? p1 : p0);
+      const unsigned int voters = __ballot_sync(0xffffffffu, take);
+      if (take) {
+        // lanes with the same digit add once, by their lowest lane
+        const unsigned int peers = __match_any_sync(voters, d);
+        if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&h[s * OS_BINS + d], __popc(peers));
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * OS_BINS; i += blockDim.x)
+    if (h[i]) atomicAdd(hist + i, h[i]);
+}
+
+__global__ void k_os_init(OrderState* st, long long k0, long long k1) {
+  st->prefix[0] = st->prefix[1] = 0u;
+  st->rank[0] = k0;
+  st->rank[1] = k1;
+}
+
+// one warp per rank: the digit whose cumulative count passes the rank
+__global__ void k_os_find(const unsigned int* __restrict__ hist, int pass, OrderState* st, float* out) {
+  const int s = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int width = c_os_width[pass], bins = 1 << width, per = bins / 32;
+  const unsigned int* hs = hist + s * OS_BINS;
+  const long long rank = st->rank[s];
+  long long local = 0;
+  for (int j = 0; j < per; ++j) local += hs[lane * per + j];
+  long long incl = local;
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const long long excl = incl - local;
+  const bool mine = excl <= rank && rank < incl;
+  const unsigned int owner = __ballot_sync(0xffffffffu, mine);
+  if (owner == 0) return;  // rank out of range: prevented by the host checks
+  if (lane == __ffs(owner) - 1) {
+    long long c = excl;
+    int d = lane * per;
+    while (c + hs[d] <= rank) c += hs[d++];
+    const unsigned int prefix = (st->prefix[s] << width) | (unsigned int)d;
+    st->prefix[s] = prefix;
+    st->rank[s] = rank - c;
+    if (pass == OS_PASSES - 1) out[s] = order_value32(prefix);
+  }
+}
+
 }  // namespace svie
 
 using namespace svie;
@@ -286,9 +414,19 @@ int svie_mesh_stars(const int32_t* faces, const int32_t* weld, int64_t T, int64_
   const long long n3 = 3 * T;
   k_gather_ids<<<blocks_for(n3, 256), 256, 0, s>>>(faces, weld, n3, vid);
   k_degree<<<blocks_for(n3, 256), 256, 0, s>>>(vid, n3, deg);
-  k_scan_deg<<<1, 1024, 0, s>>>(deg, nv, first);
+  int scans = 1;
+  if ((nv + 1023) / 1024 <= n3) {
+    // multi-block scan, its block sums in `star` (written in full by k_fill_star afterwards)
+    if (cudaMemcpyAsync(first, deg, (size_t)nv * sizeof(int), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+      set_error("svie_mesh_stars: copy failed");
+      return SVIE_ERR_LAUNCH;
+    }
+    scans = scan_exclusive_i32(first, nv, star, s);
+  } else {
+    k_scan_deg<<<1, 1024, 0, s>>>(deg, nv, first);
+  }
   k_fill_star<<<blocks_for(n3, 256), 256, 0, s>>>(vid, n3, first, cursor, star);
-  return launch_status("svie_mesh_stars", 4);
+  return launch_status("svie_mesh_stars", 3 + scans);
 }
 
 size_t svie_mesh_edge_table_bytes(int64_t T) {
@@ -356,6 +494,62 @@ int svie_mesh_pieces(const double* vertices, const int32_t* faces, int64_t T, do
   if (T == 0) return SVIE_OK;
   k_mesh_pieces<<<blocks_for(T, 256), 256, 0, s>>>(vertices, faces, T, sx, sy, sz, out, first_edge, maxbits);
   return launch_status("svie_mesh_pieces");
+}
+
+int svie_mesh_bounds(const double* vertices, int64_t V, void* ws, size_t ws_bytes, double* out, void* stream) {
+  if (V < 1 || !vertices || !out || !ws) {
+    set_error("svie_mesh_bounds: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (ws_bytes < 6 * sizeof(unsigned long long)) {
+    set_error("svie_mesh_bounds: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned long long* keys = (unsigned long long*)ws;
+  if (cudaMemsetAsync(keys, 0xff, 3 * sizeof(unsigned long long), s) != cudaSuccess ||
+      cudaMemsetAsync(keys + 3, 0, 3 * sizeof(unsigned long long), s) != cudaSuccess) {
+    set_error("svie_mesh_bounds: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = (int)std::min<long long>(blocks_for(V, 256), 2LL * nsm);
+  k_mesh_bounds<<<blocks, 256, 0, s>>>(vertices, V, keys);
+  k_mesh_bounds_values<<<1, 32, 0, s>>>(keys, out);
+  return launch_status("svie_mesh_bounds", 2);
+}
+
+size_t svie_order_stats_bytes(void) { return (size_t)OS_PASSES * 2 * OS_BINS * sizeof(unsigned int) + 64; }
+
+int svie_order_stats_f32(const float* x, int64_t n, int64_t k0, int64_t k1, void* ws, size_t ws_bytes, float* out,
+                         void* stream) {
+  if (n < 1 || !x || !out || !ws || k0 < 0 || k1 < 0 || k0 >= n || k1 >= n) {
+    set_error("svie_order_stats_f32: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (ws_bytes < svie_order_stats_bytes()) {
+    set_error("svie_order_stats_f32: workspace too small");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int* hist = (unsigned int*)ws;
+  OrderState* st = (OrderState*)(hist + OS_PASSES * 2 * OS_BINS);
+  if (cudaMemsetAsync(ws, 0, svie_order_stats_bytes(), s) != cudaSuccess) {
+    set_error("svie_order_stats_f32: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  k_os_init<<<1, 1, 0, s>>>(st, k0, k1);
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = (int)std::min<long long>(blocks_for(n, 512), 2LL * nsm);
+  for (int p = 0; p < OS_PASSES; ++p) {
+    k_os_hist<<<blocks, 512, 0, s>>>(x, n, p, st, hist + p * 2 * OS_BINS);
+    k_os_find<<<1, 64, 0, s>>>(hist + p * 2 * OS_BINS, p, st, out);
+  }
+  return launch_status("svie_order_stats_f32", 1 + 2 * OS_PASSES);
 }
 
 }  // extern "C"

@@ -380,6 +380,45 @@ __global__ void k_surf_volume(const float* __restrict__ v, const int32_t* __rest
   if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(out, s / 6.0);
 }
 
+// World coordinates origin + h * v in float64, rounded after the product and
+// after the sum as numpy rounds them (surface.py:56, grid.py:to_world).
+__global__ void k_surf_world(const float* __restrict__ v, long long n3, double ox, double oy, double oz, double h,
+                             double* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  const int a = (int)(i % 3);
+  const double o = a == 0 ? ox : (a == 1 ? oy : oz);
+  out[i] = __dadd_rn(o, __dmul_rn(h, (double)v[i]));
+}
+
+// Faces as int64, reversed (f2, f1, f0) when the signed volume is negative
+// (surface.py:54-55); any negative index (a crossing met outside the band) is
+// counted into *bad.
+__global__ void k_surf_faces64(const int32_t* __restrict__ f, long long T, const double* __restrict__ vol,
+                               int64_t* __restrict__ out, int* __restrict__ bad) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int a = f[3 * t], b = f[3 * t + 1], c = f[3 * t + 2];
+  if ((a | b | c) < 0) atomicAdd(bad, 1);
+  const bool flip = *vol < 0.0;
+  out[3 * t] = flip ? c : a;
+  out[3 * t + 1] = b;
+  out[3 * t + 2] = flip ? a : c;
+}
+
+// float32((p - shift) / scale) of float64 points, as numpy's float64
+// subtraction and division followed by the cast to float32; scale 1 is the
+// plain shifted copy.
+__global__ void k_points_f32(const double* __restrict__ p, long long n3, double sx, double sy, double sz,
+                             double scale, float* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  const int a = (int)(i % 3);
+  const double s = a == 0 ? sx : (a == 1 ? sy : sz);
+  const double d = __dsub_rn(p[i], s);
+  out[i] = __double2float_rn(scale == 1.0 ? d : __ddiv_rn(d, scale));
+}
+
 }  // namespace svie
 
 using namespace svie;
@@ -477,6 +516,38 @@ int svie_surface_signed_volume(const float* verts, const int32_t* faces, int64_t
   if (nt == 0) return SVIE_OK;
   k_surf_volume<<<blocks_for(nt, 256), 256, 0, s>>>(verts, faces, nt, cx, cy, cz, out);
   return launch_status("svie_surface_signed_volume");
+}
+
+int svie_surface_finish(const float* verts, int64_t nv, const int32_t* faces, int64_t nt, const double* vol,
+                        double ox, double oy, double oz, double h, double* world, int64_t* faces64, int* bad,
+                        void* stream) {
+  if (nv < 0 || nt < 0 || !vol || !bad || (nv > 0 && (!verts || !world)) || (nt > 0 && (!faces || !faces64))) {
+    set_error("svie_surface_finish: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(bad, 0, sizeof(int), s) != cudaSuccess) return SVIE_ERR_LAUNCH;
+  int launches = 0;
+  if (nv > 0) {
+    k_surf_world<<<blocks_for(3 * nv, 256), 256, 0, s>>>(verts, 3 * nv, ox, oy, oz, h, world);
+    ++launches;
+  }
+  if (nt > 0) {
+    k_surf_faces64<<<blocks_for(nt, 256), 256, 0, s>>>(faces, nt, vol, faces64, bad);
+    ++launches;
+  }
+  return launch_status("svie_surface_finish", launches);
+}
+
+int svie_points_f32(const double* points, int64_t n, double sx, double sy, double sz, double scale, float* out,
+                    void* stream) {
+  if (n < 0 || (n > 0 && (!points || !out)) || !(scale > 0.0)) {
+    set_error("svie_points_f32: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (n == 0) return SVIE_OK;
+  k_points_f32<<<blocks_for(3 * n, 256), 256, 0, (cudaStream_t)stream>>>(points, 3 * n, sx, sy, sz, scale, out);
+  return launch_status("svie_points_f32");
 }
 
 }  // extern "C"

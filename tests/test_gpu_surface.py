@@ -138,3 +138,96 @@ def test_result_files_of_an_erosion(tmp_path):
     assert meta["stop_reason"] == res.stop_reason
     # the snapshot records the fraction reached, within the tolerance of the request
     assert meta["snapshots"][0]["fraction"] == pytest.approx(0.97, abs=1e-3)
+
+
+def test_device_assembled_mesh_equals_host_assembly():
+    """extract_surface assembles the host mesh on the device: the same arrays as origin + h * v
+    in float64 and int64 faces on the host (surface.py:52-56), reversed for a negative volume."""
+    from svierosion_gb300.meshio import TriMesh
+    from svierosion_gb300.surface import extract_surface_device
+
+    phi, grid = _levelset()
+    for sign in (1.0, -1.0):   # outward and inward orientation of the raw triangles
+        ls = S.LevelSet(torch.from_numpy((sign * phi).astype(np.float32)).cuda(), grid, width=6)
+        verts, faces = _raw_mesh(ls)
+        nx, ny, nz = grid.shape
+        nat.call("svie_surface_project", nat.ptr(ls.flat), ny, nz, nat.ptr(verts), verts.shape[0], 0.5,
+                 nat.stream())
+        world = np.asarray(grid.origin) + grid.spacing * verts.cpu().numpy().astype(np.float64)
+        f = faces.cpu().numpy().astype(np.int64)
+        if TriMesh(world, f).signed_volume() < 0:
+            f = f[:, ::-1]
+        mesh, dev_world = extract_surface_device(ls)
+        assert np.array_equal(mesh.vertices, world)
+        assert np.array_equal(mesh.faces, f)
+        assert np.array_equal(dev_world.cpu().numpy(), world)
+        assert mesh.signed_volume() > 0
+
+
+def test_device_point_conversions_round_like_numpy():
+    """svie_points_f32: float32((p - shift) / h) as numpy computes it (no contraction)."""
+    rng = np.random.default_rng(11)
+    pts = rng.uniform(-3.0, 3.0, (20000, 3)) * 1.2345
+    grid = Grid((-1.1, -2.3, 0.7), 0.0123, (10, 10, 10))
+    p = torch.from_numpy(pts).cuda()
+    out = torch.empty((len(pts), 3), dtype=torch.float32, device="cuda")
+    nat.call("svie_points_f32", nat.ptr(p), len(pts), *grid.origin, grid.spacing, nat.ptr(out), nat.stream())
+    assert np.array_equal(out.cpu().numpy(), grid.to_index(pts).astype(np.float32))
+    shift = np.array([0.3, -0.2, 0.1])
+    nat.call("svie_points_f32", nat.ptr(p), len(pts), *shift, 1.0, nat.ptr(out), nat.stream())
+    assert np.array_equal(out.cpu().numpy(), (pts - shift).astype(np.float32))
+
+
+def test_annotation_from_device_points_equals_host_points():
+    """erode() annotates from the device copy of the vertices: the same depth, N and speed as
+    from the host vertices."""
+    from svierosion_gb300.api import _annotate, _PieceGrid
+    from svierosion_gb300.meshio import TriMesh
+    from svierosion_gb300.sdf import device_mesh
+    from svierosion_gb300.surface import extract_surface_device
+
+    m = shapes.cube(1.0)
+    p = S.ErosionParams(law="svi", radius=0.2, k=1, s=1, t=0.9, resolution=48, target_fraction=0.95)
+    res = S.erode(m, p, keep_state=True, extract_meshes=False)
+    surf, world = extract_surface_device(res.level_set)
+    dev = res.level_set.device
+    pieces = _PieceGrid(m, 4 * res.grid.spacing, dev, device_mesh(m, dev))
+    law = p.make_law(length_scale=1.0)
+    a = TriMesh(surf.vertices, surf.faces)
+    b = TriMesh(surf.vertices, surf.faces)
+    _annotate(res.simulation, a, pieces, law)
+    _annotate(res.simulation, b, pieces, law, world)
+    assert set(a.vertex_data) == {"depth", "N", "speed"}
+    for key in a.vertex_data:
+        assert np.array_equal(a.vertex_data[key], b.vertex_data[key]), key
+
+
+def test_order_statistics_and_bounds_are_exact():
+    """svie_order_stats_f32 against np.partition, svie_mesh_bounds against TriMesh.bounds."""
+    rng = np.random.default_rng(3)
+    cases = [rng.random(1), rng.random(2), rng.random(1001), np.round(rng.standard_normal(100000) * 10, 1),
+             np.concatenate([np.zeros(40), -np.zeros(3), np.full(7, np.inf), -rng.random(20)]),
+             rng.random(1 << 20) * 1e-3 + 0.5]
+    ws = torch.empty(nat.lib().svie_order_stats_bytes(), dtype=torch.uint8, device="cuda")
+    out = torch.empty(2, dtype=torch.float32, device="cuda")
+    for x in cases:
+        x = x.astype(np.float32)
+        n = len(x)
+        xd = torch.from_numpy(x).cuda()
+        for k0, k1 in {(0, n - 1), (max(n // 2 - 1, 0), n // 2), (n - 1, n - 1), (n // 3, 0)}:
+            nat.call("svie_order_stats_f32", nat.ptr(xd), n, k0, k1, nat.ptr(ws), ws.numel(), nat.ptr(out),
+                     nat.stream())
+            got = out.cpu().numpy()
+            ref = np.partition(x, sorted({k0, k1}))
+            assert got[0] == ref[k0] and got[1] == ref[k1], (n, k0, k1)
+    with pytest.raises(nat.SvieError):
+        nat.call("svie_order_stats_f32", nat.ptr(xd), n, n, 0, nat.ptr(ws), ws.numel(), nat.ptr(out), nat.stream())
+
+    from svierosion_gb300.meshio import TriMesh
+    bws = torch.empty(64, dtype=torch.uint8, device="cuda")
+    bout = torch.empty(6, dtype=torch.float64, device="cuda")
+    for v in (rng.standard_normal((1, 3)), rng.standard_normal((70001, 3)) * 1e3 - 5.0,
+              np.abs(rng.standard_normal((999, 3))) + 1.0):
+        vd = torch.from_numpy(v).cuda()
+        nat.call("svie_mesh_bounds", nat.ptr(vd), len(v), nat.ptr(bws), bws.numel(), nat.ptr(bout), nat.stream())
+        assert np.array_equal(bout.cpu().numpy().reshape(2, 3), TriMesh(v, np.zeros((0, 3))).bounds)
