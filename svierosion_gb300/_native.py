@@ -274,11 +274,26 @@ def h2d(array, dtype: torch.dtype, device) -> torch.Tensor:
     return t.to(device, non_blocking=False).contiguous()
 
 
+_NP_DTYPES = {torch.float32: np.float32, torch.float64: np.float64, torch.int32: np.int32, torch.int64: np.int64,
+              torch.uint8: np.uint8, torch.int8: np.int8, torch.int16: np.int16, torch.bool: np.bool_,
+              torch.float16: np.float16}
+
+
 def d2h(t: torch.Tensor) -> np.ndarray:
-    """Copy a device tensor to a host numpy array (counted)."""
+    """Copy a device tensor to a host numpy array (counted).
+
+    Large destinations are faulted in by the CPU (one write per 4 KiB) before the copy: a
+    device-to-host copy into freshly mapped, untouched pages measured up to 10 ms for 18 MB
+    on the GB300's host, against 0.1 ms into resident pages."""
     global _d2h_bytes
     _d2h_bytes += t.numel() * t.element_size()
-    return t.cpu().numpy()
+    dt = _NP_DTYPES.get(t.dtype)
+    if dt is None or t.numel() * t.element_size() < (1 << 20):
+        return t.cpu().numpy()
+    out = np.empty(tuple(t.shape), dtype=dt)
+    out.reshape(-1).view(np.uint8)[::4096] = 0
+    torch.from_numpy(out).copy_(t)
+    return out
 
 
 def f32(x) -> float:

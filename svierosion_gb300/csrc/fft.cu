@@ -737,43 +737,61 @@ struct GL32 {
   double x[64], w[64];
 };
 
-// Ball/cell overlap fractions (reference svi.py:24-55) in float64.
-__global__ void k_ball_weights(double R, int m, int quad, GL32 gl, double* __restrict__ w) {
+// Ball/cell overlap fractions (reference svi.py:24-55) in float64, one block
+// per (x, y) column of cells.  Cells entirely inside the ball weigh 1, cells
+// outside 0; for a cut cell the z-extent of the ball is integrated exactly and
+// the (x, y) integral by quad x quad Gauss-Legendre points.  The half-height
+// zr(X, Y) of the ball at a quadrature point is the same for every cell of the
+// column, so the block computes the quad^2 square roots once (shared memory)
+// and reuses them for each cut cell; the cell's sum is a block reduction.
+__global__ void __launch_bounds__(256) k_ball_weights(double R, int m, int quad, GL32 gl, double* __restrict__ w) {
+  extern __shared__ double zr[];  // quad * quad
+  __shared__ double gx[64], gw[64], red[8];
   const int side = 2 * m + 1;
-  const long long tot = (long long)side * side * side;
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= tot) return;
-  const int i = (int)(t / ((long long)side * side)) - m;
-  const int j = (int)((t / side) % side) - m;
-  const int k = (int)(t % side) - m;
-  const double ci = i, cj = j, ck = k;
-  auto nr = [](double c) { double v = fabs(c) - 0.5; return v > 0 ? v : 0.0; };
-  double a0 = nr(ci), a1 = nr(cj), a2 = nr(ck);
-  double near = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
-  double b0 = fabs(ci) + 0.5, b1 = fabs(cj) + 0.5, b2 = fabs(ck) + 0.5;
-  double far = sqrt(b0 * b0 + b1 * b1 + b2 * b2);
-  double v = 0.0;
-  if (far <= R) {
-    v = 1.0;
-  } else if (near < R && far > R) {
+  const int i = (int)(blockIdx.x / side) - m, j = (int)(blockIdx.x % side) - m;
+  const double ci = i, cj = j;
+  if (threadIdx.x < quad) {
+    gx[threadIdx.x] = gl.x[threadIdx.x];
+    gw[threadIdx.x] = gl.w[threadIdx.x];
+  }
+  __syncthreads();
+  const int q2 = quad * quad;
+  for (int p = threadIdx.x; p < q2; p += blockDim.x) {
+    const double X = ci + gx[p / quad], Y = cj + gx[p % quad];
+    const double r2 = R * R - X * X - Y * Y;
+    zr[p] = sqrt(r2 > 0 ? r2 : 0.0);
+  }
+  __syncthreads();
+  auto nr = [](double c) { const double v = fabs(c) - 0.5; return v > 0 ? v : 0.0; };
+  const double a0 = nr(ci), a1 = nr(cj), b0 = fabs(ci) + 0.5, b1 = fabs(cj) + 0.5;
+  double* col = w + ((long long)(i + m) * side + (j + m)) * side;
+  for (int kk = 0; kk < side; ++kk) {
+    const double ck = kk - m;
+    const double a2 = nr(ck), b2 = fabs(ck) + 0.5;
+    const double near = sqrt(a0 * a0 + a1 * a1 + a2 * a2);   // squares of half-integers: exact sums
+    const double far = sqrt(b0 * b0 + b1 * b1 + b2 * b2);
+    if (!(near < R && far > R)) {
+      if (threadIdx.x == 0) col[kk] = far <= R ? 1.0 : 0.0;
+      continue;
+    }
     const double lo = ck - 0.5, hi = ck + 0.5;
     double acc = 0.0;
-    for (int a = 0; a < quad; ++a) {
-      const double X = ci + gl.x[a];
-      double row = 0.0;
-      for (int b = 0; b < quad; ++b) {
-        const double Y = cj + gl.x[b];
-        double r2 = R * R - X * X - Y * Y;
-        double zr = sqrt(r2 > 0 ? r2 : 0.0);
-        double L = fmin(hi, zr) - fmax(lo, -zr);
-        if (L < 0) L = 0;
-        row += L * gl.w[b];
-      }
-      acc += row * gl.w[a];
+    for (int p = threadIdx.x; p < q2; p += blockDim.x) {
+      const double z = zr[p];
+      double L = fmin(hi, z) - fmax(lo, -z);
+      if (L < 0) L = 0;
+      acc += L * gw[p / quad] * gw[p % quad];
     }
-    v = acc;
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+      col[kk] = t;
+    }
+    __syncthreads();
   }
-  w[t] = v;
 }
 
 // K^ step A: A[(i,j)][kz] = sum_k w[i][j][k] cos(2 pi kz k / nz), i, j in [-m, m].
@@ -1077,8 +1095,9 @@ int svie_ball_weights(double radius, double spacing, int quad, double* w, void* 
   GL32 gl;
   memset(&gl, 0, sizeof(gl));
   gauss_legendre(quad, gl.x, gl.w);
-  const long long side = 2 * m + 1, tot = side * side * side;
-  k_ball_weights<<<blocks_for(tot, 128), 128, 0, (cudaStream_t)stream>>>(radius / spacing, m, quad, gl, w);
+  const long long side = 2 * m + 1;
+  k_ball_weights<<<(unsigned)(side * side), 256, (size_t)quad * quad * sizeof(double), (cudaStream_t)stream>>>(
+      radius / spacing, m, quad, gl, w);
   return launch_status("svie_ball_weights");
 }
 
