@@ -326,11 +326,13 @@ int svie_set_f64(double* dst, double value, void* stream);
 /* ------------------------------------------------- point-to-mesh distance */
 /* point_mesh_distance (svierosion/api.py:104-168), exact: the T pieces (T x 9
  * floats) are binned by centroid into a gx x gy x gz grid of cells of side cs
- * from (ox, oy, oz) (svie_piece_grid_build, workspace svie_piece_grid_bytes);
+ * from (ox, oy, oz), with the bounding box of each cell's pieces
+ * (svie_piece_grid_build, workspace svie_piece_grid_bytes);
  * svie_point_mesh_distance walks Chebyshev shells of cells around each point
- * until no unvisited piece can be closer (rho bounds centroid-to-piece
- * distances) and writes the distance (float32, sqrt of the float32 squared
- * distance of kernels.py:382-427). */
+ * (one warp per point), visiting the cells whose piece box is not farther than
+ * the best distance so far, until no unvisited piece can be closer (rho bounds
+ * centroid-to-piece distances), and writes the distance (float32, sqrt of the
+ * float32 squared distance of kernels.py:382-427). */
 /* The triangles of a device mesh relative to (sx, sy, sz) as float32 pieces (T x 9), the first-edge
  * lengths (float32 [T]) and the largest edge and centroid-to-vertex distance (float bits in
  * maxbits[0], maxbits[1]). */

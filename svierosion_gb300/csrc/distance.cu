@@ -125,55 +125,179 @@ __global__ void k_piece_fill(const float* __restrict__ tri, long long T, CellGri
   order[start[c] + atomicAdd(cursor + c, 1)] = (int)t;
 }
 
-// distance from v to the interval [lo, lo + cs]
-SVIE_DEV float box_gap(float v, float lo, float cs) { return fmaxf(fmaxf(lo - v, v - (lo + cs)), 0.0f); }
+// Order-preserving unsigned keys of floats (sign bit set for non-negative
+// values, all bits flipped for negative ones).
+SVIE_DEV unsigned int fkey(float x) {
+  const unsigned int b = __float_as_uint(x);
+  return (b >> 31) ? ~b : (b | 0x80000000u);
+}
 
-SVIE_DEV void visit_cell(const float* __restrict__ tri, const int* __restrict__ start, const int* __restrict__ order,
-                         int c, float3 p, float* best) {
-  const int e = start[c + 1];
-  for (int k = start[c]; k < e; ++k) {
-    const int t = order[k];
-    const float d2 = point_triangle_d2(p, piece_vertex(tri, t, 0), piece_vertex(tri, t, 1), piece_vertex(tri, t, 2));
-    *best = fminf(*best, d2);
+SVIE_DEV float fkey_value(unsigned int k) { return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k); }
+
+// Bounding box of the pieces of every cell, as keys: box[6 c + a] = min, box[6 c + 3 + a] = max.
+__global__ void k_piece_box(const float* __restrict__ tri, long long T, CellGrid G, unsigned int* __restrict__ box) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int c = piece_cell(tri, t, G);
+  for (int a = 0; a < 3; ++a) {
+    const float v0 = tri[9 * t + a], v1 = tri[9 * t + 3 + a], v2 = tri[9 * t + 6 + a];
+    atomicMin(box + 6LL * c + a, fkey(fminf(fminf(v0, v1), v2)));
+    atomicMax(box + 6LL * c + 3 + a, fkey(fmaxf(fmaxf(v0, v1), v2)));
   }
 }
 
-__global__ void k_point_distance(const float* __restrict__ pts, long long n, const float* __restrict__ tri,
-                                 const int* __restrict__ start, const int* __restrict__ order, CellGrid G, float rho,
-                                 float* __restrict__ out) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+// min keys start at the largest key, max keys at the smallest
+__global__ void k_piece_box_init(unsigned int* __restrict__ box, long long n6) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n6) box[e] = (e % 6) < 3 ? 0xffffffffu : 0u;
+}
+
+// keys -> floats; an empty cell gets the box [+inf, -inf], at infinite distance from every point
+__global__ void k_piece_box_finish(const int* __restrict__ start, long long cells, unsigned int* __restrict__ box) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cells) return;
+  float* f = reinterpret_cast<float*>(box + 6 * c);
+  const bool empty = start[c] == start[c + 1];
+  for (int a = 0; a < 3; ++a) {
+    const unsigned int lo = box[6 * c + a], hi = box[6 * c + 3 + a];
+    f[a] = empty ? INFINITY : fkey_value(lo);
+    f[3 + a] = empty ? -INFINITY : fkey_value(hi);
+  }
+}
+
+// distance from v to the interval [lo, hi] (infinite for an empty interval)
+SVIE_DEV float span_gap(float v, float lo, float hi) { return fmaxf(fmaxf(lo - v, v - hi), 0.0f); }
+
+// Cell (dx, dy, dz) number q of the Chebyshev shell of radius r: the two z
+// faces ((2r+1)^2 cells each), the two y faces ((2r+1)(2r-1)), the two x faces
+// ((2r-1)^2); 24 r^2 + 2 cells for r > 0, one for r = 0.
+SVIE_DEV void shell_cell(int r, int q, int& dx, int& dy, int& dz) {
+  if (r == 0) {
+    dx = dy = dz = 0;
+    return;
+  }
+  // u / w for 0 <= u < w * w and w < 2048 by a float reciprocal: (u + 0.5) / w is at
+  // least 0.5 / w away from an integer, far more than the float rounding error
+  auto divmod = [](int u, int w, float inv_w, int& quo, int& rem) {
+    quo = w < 2000 ? (int)(((float)u + 0.5f) * inv_w) : u / w;
+    rem = u - quo * w;
+  };
+  const int s = 2 * r + 1, t = 2 * r - 1;
+  const float inv_s = 1.0f / (float)s, inv_t = 1.0f / (float)t;
+  const int zf = s * s, yf = s * t;
+  int a, b;
+  if (q < 2 * zf) {
+    dz = q < zf ? -r : r;
+    divmod(q < zf ? q : q - zf, s, inv_s, a, b);
+    dx = a - r;
+    dy = b - r;
+    return;
+  }
+  q -= 2 * zf;
+  if (q < 2 * yf) {
+    dy = q < yf ? -r : r;
+    divmod(q < yf ? q : q - yf, t, inv_t, a, b);
+    dx = a - r;
+    dz = b - (r - 1);
+    return;
+  }
+  q -= 2 * yf;
+  const int xf = t * t;
+  dx = q < xf ? -r : r;
+  divmod(q < xf ? q : q - xf, t, inv_t, a, b);
+  dy = a - (r - 1);
+  dz = b - (r - 1);
+}
+
+// One warp per query point.  The lanes split the cells of each Chebyshev
+// shell around the point's cell; a cell is a candidate while the bounding box
+// of its pieces is not farther than the best distance so far (empty cells have
+// an empty box, never a candidate).  Each shell takes two passes: the first
+// tests one piece of every candidate cell, which gives the warp a near-final
+// bound; the second tests the other pieces of the cells that are still
+// candidates, spread over all 32 lanes (a warp scan of the per-cell counts and
+// a search for each piece's cell) so that a cell with many pieces does not
+// leave the other lanes idle.  After each shell the warp takes the minimum and
+// stops once no unvisited piece can be closer (pieces are binned by centroid,
+// so an unvisited one is farther than r cs - rho).  The result is the exact
+// minimum over the pieces.
+__global__ void __launch_bounds__(128) k_point_distance(const float* __restrict__ pts, long long n,
+                                                        const float* __restrict__ tri, const int* __restrict__ start,
+                                                        const int* __restrict__ order, const float* __restrict__ box,
+                                                        CellGrid G, float rho, float* __restrict__ out) {
+  const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;  // whole warps
   const float3 p = make_float3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
   const int cx = cell_of(p.x, G.ox, G.inv_cs, G.gx), cy = cell_of(p.y, G.oy, G.inv_cs, G.gy),
             cz = cell_of(p.z, G.oz, G.inv_cs, G.gz);
   const int rmax = max(max(G.gx, G.gy), G.gz);
+  // cell number q of shell r if it lies in the grid and is a candidate for `bound`, else -1;
+  // the squared box distance is shrunk by 1e-5 so that rounding never drops a cell
+  auto candidate = [&](int r, int q, float bound) -> int {
+    int dx, dy, dz;
+    shell_cell(r, q, dx, dy, dz);
+    const int x = cx + dx, y = cy + dy, z = cz + dz;
+    if (x < 0 || y < 0 || z < 0 || x >= G.gx || y >= G.gy || z >= G.gz) return -1;
+    const int c = (x * G.gy + y) * G.gz + z;
+    const float* b = box + 6LL * c;
+    const float bx = span_gap(p.x, b[0], b[3]), by = span_gap(p.y, b[1], b[4]), bz = span_gap(p.z, b[2], b[5]);
+    const float g2 = (bx * bx + by * by + bz * bz) * 0.99999f;
+    return (g2 <= bound && g2 < INFINITY) ? c : -1;
+  };
+  auto piece_d2 = [&](int k) {
+    const int t = order[k];
+    return point_triangle_d2(p, piece_vertex(tri, t, 0), piece_vertex(tri, t, 1), piece_vertex(tri, t, 2));
+  };
   float best = INFINITY;
   for (int r = 0; r <= rmax; ++r) {
-    const int x0 = cx - r, x1 = cx + r, y0 = cy - r, y1 = cy + r, z0 = cz - r, z1 = cz + r;
-    for (int x = max(x0, 0); x <= min(x1, G.gx - 1); ++x) {
-      const float bx = box_gap(p.x, G.ox + x * G.cs, G.cs);
-      for (int y = max(y0, 0); y <= min(y1, G.gy - 1); ++y) {
-        const float by = box_gap(p.y, G.oy + y * G.cs, G.cs);
-        const bool face = (x == x0 || x == x1 || y == y0 || y == y1);
-        const int base = (x * G.gy + y) * G.gz;
-        // on an x or y face of the shell every z; inside it only the two z faces
-        const int zs = face ? max(z0, 0) : (z0 >= 0 ? z0 : z1);
-        const int ze = min(z1, G.gz - 1);
-        const int step = face ? 1 : (z1 - z0 > 0 ? z1 - z0 : 1);
-        for (int z = zs; z <= ze; z += step) {
-          // a cell whose box is farther than the best distance + rho holds no closer piece
-          const float bz = box_gap(p.z, G.oz + z * G.cs, G.cs);
-          const float gap = sqrtf(bx * bx + by * by + bz * bz) - rho;
-          if (gap <= 0.0f || gap * gap <= best) visit_cell(tri, start, order, base + z, p, &best);
-        }
+    const int ncell = r ? 24 * r * r + 2 : 1;
+    // pass 1: the first piece of every candidate cell
+    for (int q = lane; q < ncell; q += 32) {
+      const int c = candidate(r, q, best);
+      if (c >= 0) {
+        const int k0 = start[c];
+        if (k0 < start[c + 1]) best = fminf(best, piece_d2(k0));
       }
     }
+    best = warp_min(best);
+    // pass 2: the remaining pieces of the cells that are still candidates
+    for (int q0 = 0; q0 < ncell; q0 += 32) {
+      const int q = q0 + lane;
+      int k1 = 0, cnt = 0;
+      if (q < ncell) {
+        const int c = candidate(r, q, best);
+        if (c >= 0) {
+          k1 = start[c] + 1;
+          cnt = max(start[c + 1] - k1, 0);
+        }
+      }
+      int incl = cnt;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      const int excl = incl - cnt;
+      for (int base = 0; base < total; base += 32) {
+        const int j = base + lane;
+        // owner: the first lane whose inclusive count passes j (counts are non-decreasing)
+        int lo = 0;
+        for (int step = 16; step; step >>= 1) {
+          const int v = __shfl_sync(0xffffffffu, incl, lo + step - 1);
+          if (v <= j) lo += step;
+        }
+        const int ok1 = __shfl_sync(0xffffffffu, k1, lo), oex = __shfl_sync(0xffffffffu, excl, lo);
+        if (j < total) best = fminf(best, piece_d2(ok1 + (j - oex)));
+      }
+    }
+    best = warp_min(best);
     // unvisited centroids are farther than r cs (also for p outside the grid box,
     // whose cell is clamped: the bound only gets looser), unvisited pieces than r cs - rho
     const float reach = (float)r * G.cs - rho;
     if (reach > 0.0f && best <= reach * reach) break;
   }
-  out[i] = sqrtf(best);
+  if (lane == 0) out[i] = sqrtf(best);
 }
 
 }  // namespace svie
@@ -182,10 +306,16 @@ using namespace svie;
 
 extern "C" {
 
+// Piece grid workspace: start (cells + 1), cursor (cells + 1), order (T), scan
+// sums, then the per-cell piece boxes (6 floats per cell, 16-byte aligned).
+static long long piece_box_offset(long long T, long long cells) {
+  const long long nb = (cells + 1 + 1023) / 1024;
+  return ((2 * (cells + 1) + T + nb) + 3) / 4 * 4;  // in ints
+}
+
 size_t svie_piece_grid_bytes(int64_t T, int gx, int gy, int gz) {
   const long long cells = (long long)gx * gy * gz;
-  const long long nb = (cells + 1 + 1023) / 1024;
-  return (size_t)(2 * (cells + 1) + T + nb) * sizeof(int) + 256;
+  return (size_t)(piece_box_offset(T, cells) + 6 * cells) * sizeof(int) + 256;
 }
 
 int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float oz, float cs, int gx, int gy, int gz,
@@ -210,16 +340,22 @@ int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float
     return SVIE_ERR_LAUNCH;
   }
   const CellGrid G{ox, oy, oz, cs, 1.0f / cs, gx, gy, gz};
+  unsigned int* box = (unsigned int*)ws + piece_box_offset(T, cells);
+  k_piece_box_init<<<blocks_for(6 * cells, 256), 256, 0, s>>>(box, 6 * cells);
   if (T > 0) k_piece_count<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, start);
   scan_exclusive_i32(start, cells + 1, sums, s);
-  if (T > 0) k_piece_fill<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, start, cursor, order);
-  return launch_status("svie_piece_grid_build", T > 0 ? 5 : 3);
+  if (T > 0) {
+    k_piece_fill<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, start, cursor, order);
+    k_piece_box<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, box);
+  }
+  k_piece_box_finish<<<blocks_for(cells, 256), 256, 0, s>>>(start, cells, box);
+  return launch_status("svie_piece_grid_build", T > 0 ? 8 : 5);
 }
 
 int svie_point_mesh_distance(const float* pts, int64_t n, const float* tri, int64_t T, float ox, float oy, float oz,
                              float cs, int gx, int gy, int gz, const void* ws, size_t ws_bytes, float rho, float* out,
                              void* stream) {
-  if (n < 0 || (n > 0 && (!pts || !out)) || (T > 0 && !tri) || !ws) {
+  if (n < 0 || n >= (1LL << 31) || (n > 0 && (!pts || !out)) || (T > 0 && !tri) || !ws) {
     set_error("svie_point_mesh_distance: bad arguments");
     return SVIE_ERR_ARG;
   }
@@ -231,8 +367,10 @@ int svie_point_mesh_distance(const float* pts, int64_t n, const float* tri, int6
   const long long cells = (long long)gx * gy * gz;
   const int* start = (const int*)ws;
   const int* order = start + 2 * (cells + 1);
+  const float* box = (const float*)ws + piece_box_offset(T, cells);
   const CellGrid G{ox, oy, oz, cs, 1.0f / cs, gx, gy, gz};
-  k_point_distance<<<blocks_for(n, 128), 128, 0, (cudaStream_t)stream>>>(pts, n, tri, start, order, G, rho, out);
+  k_point_distance<<<blocks_for(32 * n, 128), 128, 0, (cudaStream_t)stream>>>(pts, n, tri, start, order, box, G,
+                                                                               rho, out);
   return launch_status("svie_point_mesh_distance");
 }
 
