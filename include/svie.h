@@ -450,6 +450,11 @@ int svie_sdf_unpack(const int64_t* keys, int64_t n, float* dist, int32_t* tid, u
  * triangles (new values into new_dist/new_tid); scatter writes them back and
  * marks the nodes known. */
 int svie_sdf_ring_mask(const uint8_t* known, int nx, int ny, int nz, uint8_t* ring, void* stream);
+/* The same ring from the previous ring's node list `last` (m nodes): ring = 1 at the unknown
+ * interior neighbours of those nodes, 0 elsewhere.  For every ring after the first this is
+ * svie_sdf_ring_mask's set (an unknown node next to an older known node is in an older ring). */
+int svie_sdf_ring_mark(const int32_t* last, int64_t m, const uint8_t* known, int nx, int ny, int nz, uint8_t* ring,
+                       void* stream);
 int svie_sdf_ring_update(const int32_t* upd, int64_t m, int nx, int ny, int nz, const float* tri,
                          const float* dist, const int32_t* tid, float* new_dist, int32_t* new_tid,
                          void* stream);

@@ -169,6 +169,7 @@ _SIGS = {
     "svie_sdf_near_field": (I, [V, V, I64, I, I, I, D, F, V, V]),
     "svie_sdf_unpack": (I, [V, I64, V, V, V, V]),
     "svie_sdf_ring_mask": (I, [V, I, I, I, V, V]),
+    "svie_sdf_ring_mark": (I, [V, I64, V, I, I, I, V, V]),
     "svie_sdf_ring_update": (I, [V, I64, I, I, I, V, V, V, V, V, V]),
     "svie_sdf_scatter": (I, [V, I64, V, V, V, V, V, V]),
     "svie_sdf_outer_mask": (I, [V, I64, F, F, V, V]),

@@ -29,37 +29,53 @@ __global__ void k_keys_init(long long* keys, long long n) {
     keys[e] = 0x7fffffffffffffffLL;
 }
 
-// sdf.py:100-145; bbox from the float64 vertices, distances in float32.
+// sdf.py:100-145; bbox from the float64 vertices, distances in float32.  A
+// warp takes 32 triangles: each lane computes one triangle's node box in
+// float64 (FP64 is slow on this part, so it runs once per triangle, not once
+// per lane of a warp), then the warp walks the boxes one triangle after the
+// other, a node per lane.
 __global__ void k_near_field(const float* __restrict__ tri, const double* __restrict__ tri64, long long ntri, int nx,
                              int ny, int nz, double eb_cells, float eb_keep, unsigned long long* keys) {
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long t0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) << 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= ntri) return;
-  const double* q = tri64 + 9 * warp;
-  int lo[3], dim[3];
-  const int shape[3] = {nx, ny, nz};
+  if (t0 >= ntri) return;  // whole warps
+  const long long tl = t0 + lane;
+  int lo[3] = {0, 0, 0}, dim[3] = {0, 0, 0};
+  if (tl < ntri) {
+    const double* q = tri64 + 9 * tl;
+    const int shape[3] = {nx, ny, nz};
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    double mn = fmin(fmin(q[a], q[3 + a]), q[6 + a]);
-    double mx = fmax(fmax(q[a], q[3 + a]), q[6 + a]);
-    long long l = (long long)ceil(mn - eb_cells), h = (long long)floor(mx + eb_cells);
-    l = l < 0 ? 0 : (l > shape[a] - 1 ? shape[a] - 1 : l);
-    h = h < 0 ? 0 : (h > shape[a] - 1 ? shape[a] - 1 : h);
-    lo[a] = (int)l;
-    dim[a] = (int)(h - l + 1 > 0 ? h - l + 1 : 0);
+    for (int a = 0; a < 3; ++a) {
+      double mn = fmin(fmin(q[a], q[3 + a]), q[6 + a]);
+      double mx = fmax(fmax(q[a], q[3 + a]), q[6 + a]);
+      long long l = (long long)ceil(mn - eb_cells), h = (long long)floor(mx + eb_cells);
+      l = l < 0 ? 0 : (l > shape[a] - 1 ? shape[a] - 1 : l);
+      h = h < 0 ? 0 : (h > shape[a] - 1 ? shape[a] - 1 : h);
+      lo[a] = (int)l;
+      dim[a] = (int)(h - l + 1 > 0 ? h - l + 1 : 0);
+    }
   }
-  const long long cnt = (long long)dim[0] * dim[1] * dim[2];
-  const float3 A = tri_v(tri, warp, 0), B = tri_v(tri, warp, 1), C = tri_v(tri, warp, 2);
   const long long syz = (long long)ny * nz;
-  for (long long e = lane; e < cnt; e += 32) {
-    const int ii = lo[0] + (int)(e / ((long long)dim[1] * dim[2]));
-    const long long rem = e % ((long long)dim[1] * dim[2]);
-    const int jj = lo[1] + (int)(rem / dim[2]);
-    const int kk = lo[2] + (int)(rem % dim[2]);
-    const float d = sqrtf(point_triangle_d2(make_float3((float)ii, (float)jj, (float)kk), A, B, C));
-    if (d <= eb_keep) {
-      const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)warp;
-      atomicMin(keys + (ii * syz + (long long)jj * nz + kk), key);
+  const int nt = (int)min(32LL, ntri - t0);
+  for (int k = 0; k < nt; ++k) {
+    const int l0 = __shfl_sync(0xffffffffu, lo[0], k), l1 = __shfl_sync(0xffffffffu, lo[1], k),
+              l2 = __shfl_sync(0xffffffffu, lo[2], k);
+    const int d0 = __shfl_sync(0xffffffffu, dim[0], k), d1 = __shfl_sync(0xffffffffu, dim[1], k),
+              d2 = __shfl_sync(0xffffffffu, dim[2], k);
+    const long long t = t0 + k;
+    const int d12 = d1 * d2, cnt = d0 * d12;  // below the grid size, < 2^31
+    if (cnt == 0) continue;
+    const float3 A = tri_v(tri, t, 0), B = tri_v(tri, t, 1), C = tri_v(tri, t, 2);
+    for (int e = lane; e < cnt; e += 32) {
+      const int ii = l0 + e / d12;
+      const int rem = e - (e / d12) * d12;
+      const int jj = l1 + rem / d2;
+      const int kk = l2 + (rem - (rem / d2) * d2);
+      const float d = sqrtf(point_triangle_d2(make_float3((float)ii, (float)jj, (float)kk), A, B, C));
+      if (d <= eb_keep) {
+        const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)t;
+        atomicMin(keys + (ii * syz + (long long)jj * nz + kk), key);
+      }
     }
   }
 }
@@ -89,6 +105,26 @@ __global__ void k_ring_mask(const uint8_t* __restrict__ known, int nx, int ny, i
     }
     ring[e] = r;
   }
+}
+
+// The next ring from the last one: the unknown interior neighbours of the
+// last ring's nodes.  Equal to k_ring_mask's set after the first ring: an
+// unknown node next to an older known node would already be in a ring.
+__global__ void k_ring_mark(const int32_t* __restrict__ last, long long m, const uint8_t* __restrict__ known, int nx,
+                            int ny, int nz, uint8_t* ring) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const long long syz = (long long)ny * nz;
+  const long long u = last[t];
+  const int x = (int)(u / syz), y = (int)((u / nz) % ny), z = (int)(u % nz);
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dz = -1; dz <= 1; ++dz) {
+        const int a = x + dx, b = y + dy, c = z + dz;
+        if (a <= 0 || b <= 0 || c <= 0 || a >= nx - 1 || b >= ny - 1 || c >= nz - 1) continue;
+        const long long e = (long long)a * syz + (long long)b * nz + c;
+        if (!known[e]) ring[e] = 1;
+      }
 }
 
 // sdf.py:183-200: best over the closest triangles of the 26 neighbours, in the
@@ -186,29 +222,67 @@ SVIE_DEV int orient_sos(double x1, double y1, double x2, double y2, double* area
 }
 
 // sdf.py:285-333 for one axis: a = axis, b = (a+1)%3, c = (a+2)%3; acc has
-// (na+1) x nb x nc int32 counters.
+// (na+1) x nb x nc int32 counters.  A warp takes 32 triangles: each lane
+// computes one triangle's range of grid lines (float64, once per triangle),
+// then the warp walks the (triangle, line) pairs of all 32 triangles together,
+// one pair per lane (a warp scan of the counts and a search for each pair's
+// triangle), so the float64 crossing tests run with all lanes busy however
+// few lines a triangle covers.
 __global__ void k_crossings(const double* __restrict__ tri64, long long ntri, int na, int nb, int nc, int axis,
                             int signed_rule, int* acc) {
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long t0 = (((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5) << 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= ntri) return;
+  if (t0 >= ntri) return;  // whole warps
+  const long long tl = t0 + lane;
   const int a = axis, b = (axis + 1) % 3, c = (axis + 2) % 3;
-  const double* q = tri64 + 9 * warp;
-  const double U0 = q[b], U1 = q[3 + b], U2 = q[6 + b];
-  const double W0 = q[c], W1 = q[3 + c], W2 = q[6 + c];
-  const double Z0 = q[a], Z1 = q[3 + a], Z2 = q[6 + a];
-  double j0d = ceil(fmin(fmin(U0, U1), U2)), j1d = floor(fmax(fmax(U0, U1), U2));
-  double k0d = ceil(fmin(fmin(W0, W1), W2)), k1d = floor(fmax(fmax(W0, W1), W2));
-  long long j0 = (long long)fmin(fmax(j0d, 0.0), (double)nb), j1 = (long long)fmin(fmax(j1d, -1.0), (double)(nb - 1));
-  long long k0 = (long long)fmin(fmax(k0d, 0.0), (double)nc), k1 = (long long)fmin(fmax(k1d, -1.0), (double)(nc - 1));
-  const long long dj = j1 - j0 + 1 > 0 ? j1 - j0 + 1 : 0;
-  const long long dk = k1 - k0 + 1 > 0 ? k1 - k0 + 1 : 0;
-  const long long cnt = dj * dk;
-  for (long long e = lane; e < cnt; e += 32) {
-    const long long jj = j0 + e / dk, kk = k0 + e % dk;
+  double U0 = 0, U1 = 0, U2 = 0, W0 = 0, W1 = 0, W2 = 0, Z0 = 0, Z1 = 0, Z2 = 0;
+  int j0 = 0, k0 = 0, dk = 1, cnt = 0;
+  if (tl < ntri) {
+    const double* q = tri64 + 9 * tl;
+    U0 = q[b]; U1 = q[3 + b]; U2 = q[6 + b];
+    W0 = q[c]; W1 = q[3 + c]; W2 = q[6 + c];
+    Z0 = q[a]; Z1 = q[3 + a]; Z2 = q[6 + a];
+    const double j0d = ceil(fmin(fmin(U0, U1), U2)), j1d = floor(fmax(fmax(U0, U1), U2));
+    const double k0d = ceil(fmin(fmin(W0, W1), W2)), k1d = floor(fmax(fmax(W0, W1), W2));
+    const long long jl = (long long)fmin(fmax(j0d, 0.0), (double)nb), jh = (long long)fmin(fmax(j1d, -1.0), (double)(nb - 1));
+    const long long kl = (long long)fmin(fmax(k0d, 0.0), (double)nc), kh = (long long)fmin(fmax(k1d, -1.0), (double)(nc - 1));
+    const long long dj = jh - jl + 1 > 0 ? jh - jl + 1 : 0;
+    const long long dkk = kh - kl + 1 > 0 ? kh - kl + 1 : 0;
+    j0 = (int)jl;
+    k0 = (int)kl;
+    dk = dkk > 0 ? (int)dkk : 1;
+    cnt = (int)(dj * dkk);  // lines of one triangle: below nb * nc < 2^31
+  }
+  long long incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const long long total = __shfl_sync(0xffffffffu, incl, 31);
+  const long long excl = incl - cnt;
+  for (long long base = 0; base < total; base += 32) {
+    const long long j = base + lane;
+    // owner: the first lane whose inclusive count passes j (counts are non-decreasing)
+    int own = 0;
+    for (int step = 16; step; step >>= 1) {
+      const long long v = __shfl_sync(0xffffffffu, incl, own + step - 1);
+      if (v <= j) own += step;
+    }
+    const double u0 = __shfl_sync(0xffffffffu, U0, own), u1 = __shfl_sync(0xffffffffu, U1, own),
+                 u2 = __shfl_sync(0xffffffffu, U2, own);
+    const double w0 = __shfl_sync(0xffffffffu, W0, own), w1 = __shfl_sync(0xffffffffu, W1, own),
+                 w2 = __shfl_sync(0xffffffffu, W2, own);
+    const double z0 = __shfl_sync(0xffffffffu, Z0, own), z1 = __shfl_sync(0xffffffffu, Z1, own),
+                 z2 = __shfl_sync(0xffffffffu, Z2, own);
+    const int oj0 = __shfl_sync(0xffffffffu, j0, own), ok0 = __shfl_sync(0xffffffffu, k0, own),
+              odk = __shfl_sync(0xffffffffu, dk, own);
+    const long long oex = __shfl_sync(0xffffffffu, excl, own);
+    if (j >= total) continue;
+    const int e = (int)(j - oex);
+    const int jj = oj0 + e / odk, kk = ok0 + (e - (e / odk) * odk);
     const double fj = (double)jj, fk = (double)kk;
-    const double x1 = __dsub_rn(U0, fj), x2 = __dsub_rn(U1, fj), x3 = __dsub_rn(U2, fj);
-    const double y1 = __dsub_rn(W0, fk), y2 = __dsub_rn(W1, fk), y3 = __dsub_rn(W2, fk);
+    const double x1 = __dsub_rn(u0, fj), x2 = __dsub_rn(u1, fj), x3 = __dsub_rn(u2, fj);
+    const double y1 = __dsub_rn(w0, fk), y2 = __dsub_rn(w1, fk), y3 = __dsub_rn(w2, fk);
     double A, B, C;
     const int sa = orient_sos(x2, y2, x3, y3, &A);
     const int sb = orient_sos(x3, y3, x1, y1, &B);
@@ -216,11 +290,11 @@ __global__ void k_crossings(const double* __restrict__ tri64, long long ntri, in
     if (!(sa != 0 && sb == sa && sc == sa)) continue;
     const double S = __dadd_rn(__dadd_rn(A, B), C);
     if (S == 0.0) continue;
-    const double num = __dadd_rn(__dadd_rn(__dmul_rn(A, Z0), __dmul_rn(B, Z1)), __dmul_rn(C, Z2));
+    const double num = __dadd_rn(__dadd_rn(__dmul_rn(A, z0), __dmul_rn(B, z1)), __dmul_rn(C, z2));
     const double z = __ddiv_rn(num, S);
     long long i0 = (long long)floor(z) + 1;
     i0 = i0 < 0 ? 0 : (i0 > na ? na : i0);
-    atomicAdd(acc + (i0 * nb + jj) * nc + kk, signed_rule ? -sa : 1);
+    atomicAdd(acc + ((long long)i0 * nb + jj) * nc + kk, signed_rule ? -sa : 1);
   }
 }
 
@@ -274,9 +348,9 @@ int svie_sdf_near_field(const float* tri, const double* tri64, int64_t ntri, int
     return SVIE_ERR_ARG;
   }
   if (ntri == 0) return SVIE_OK;
-  const long long threads = ntri * 32;
-  k_near_field<<<blocks_for(threads, 256), 256, 0, (cudaStream_t)stream>>>(tri, tri64, ntri, nx, ny, nz, exact_band,
-                                                                           eb_keep, (unsigned long long*)keys);
+  // one warp per 32 triangles
+  k_near_field<<<blocks_for(ntri, 256), 256, 0, (cudaStream_t)stream>>>(tri, tri64, ntri, nx, ny, nz, exact_band,
+                                                                        eb_keep, (unsigned long long*)keys);
   return launch_status("svie_sdf_near_field");
 }
 
@@ -298,6 +372,22 @@ int svie_sdf_ring_mask(const uint8_t* known, int nx, int ny, int nz, uint8_t* ri
   const dim3 gd((nz + 127) / 128, ny, nx);
   k_ring_mask<<<gd, 128, 0, (cudaStream_t)stream>>>(known, nx, ny, nz, ring);
   return launch_status("svie_sdf_ring_mask");
+}
+
+int svie_sdf_ring_mark(const int32_t* last, int64_t m, const uint8_t* known, int nx, int ny, int nz, uint8_t* ring,
+                       void* stream) {
+  if (m < 0 || !known || !ring || (m > 0 && !last) || nx < 1 || ny < 1 || nz < 1) {
+    set_error("svie_sdf_ring_mark: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(ring, 0, (size_t)nx * ny * nz, s) != cudaSuccess) {
+    set_error("svie_sdf_ring_mark: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  if (m == 0) return SVIE_OK;
+  k_ring_mark<<<blocks_for(m, 256), 256, 0, s>>>(last, m, known, nx, ny, nz, ring);
+  return launch_status("svie_sdf_ring_mark");
 }
 
 int svie_sdf_ring_update(const int32_t* upd, int64_t m, int nx, int ny, int nz, const float* tri, const float* dist,
@@ -343,8 +433,9 @@ int svie_sdf_crossings(const double* tri64, int64_t ntri, int nx, int ny, int nz
   if (ntri == 0) return SVIE_OK;
   const int shape[3] = {nx, ny, nz};
   const int na = shape[axis], nb = shape[(axis + 1) % 3], nc = shape[(axis + 2) % 3];
-  k_crossings<<<blocks_for(ntri * 32, 256), 256, 0, (cudaStream_t)stream>>>(tri64, ntri, na, nb, nc, axis, signed_rule,
-                                                                           acc);
+  // one warp per 32 triangles
+  k_crossings<<<blocks_for(ntri, 256), 256, 0, (cudaStream_t)stream>>>(tri64, ntri, na, nb, nc, axis, signed_rule,
+                                                                        acc);
   return launch_status("svie_sdf_crossings");
 }
 
