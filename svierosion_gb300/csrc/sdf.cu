@@ -127,6 +127,31 @@ __global__ void k_ring_mark(const int32_t* __restrict__ last, long long m, const
       }
 }
 
+// The last K distinct triangle ids met by one thread, in registers (constant
+// indices only).  A repeated candidate gives the same distance as its first
+// visit, which can no longer be strictly smaller than the best (the best only
+// decreases) nor change a minimum key, so it is skipped.
+template <int K>
+struct SeenTriangles {
+  int v[K];
+  int next = 0;
+  SVIE_DEV SeenTriangles() {
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = -1;
+  }
+  // true if t (>= 0) is among the last K; otherwise records it in place of the oldest
+  SVIE_DEV bool seen(int t) {
+    bool hit = false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) hit |= v[k] == t;
+    if (hit) return true;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = k == next ? t : v[k];
+    next = next + 1 == K ? 0 : next + 1;
+    return false;
+  }
+};
+
 // sdf.py:183-200: best over the closest triangles of the 26 neighbours, in the
 // reference's neighbour order (first strictly smaller distance wins).
 __global__ void k_ring_update(const int32_t* __restrict__ upd, long long m, int nx, int ny, int nz,
@@ -140,6 +165,7 @@ __global__ void k_ring_update(const int32_t* __restrict__ upd, long long m, int 
   const float px = (float)(u / syz), py = (float)((u / nz) % ny), pz = (float)(u % nz);
   float best = dist[u];
   int32_t bt = tid[u];
+  SeenTriangles<8> cache;
   for (int ox = -1; ox <= 1; ++ox)
     for (int oy = -1; oy <= 1; ++oy)
       for (int oz = -1; oz <= 1; ++oz) {
@@ -147,7 +173,7 @@ __global__ void k_ring_update(const int32_t* __restrict__ upd, long long m, int 
         long long nb = u + ox * syz + oy * nz + oz;
         nb = nb < 0 ? 0 : (nb > n - 1 ? n - 1 : nb);
         const int32_t tt = tid[nb];
-        if (tt < 0) continue;
+        if (tt < 0 || cache.seen(tt)) continue;
         const float d = node_tri_dist(tri, tt, px, py, pz);
         if (d < best) { best = d; bt = tt; }
       }
@@ -186,11 +212,13 @@ __global__ void k_star_pass(const int32_t* __restrict__ nodes, long long m, int 
       const long long syz = (long long)ny * nz;
       const float px = (float)(u / syz), py = (float)((u / nz) % ny), pz = (float)(u % nz);
       unsigned long long best = 0x7fffffffffffffffULL;
+      SeenTriangles<8> cache;
       for (int v = 0; v < 3; ++v) {
         const int32_t vv = vid[3 * (long long)t0 + v];
         const int32_t f0 = first[vv], dg = deg[vv];
         for (int q = 0; q < dg; ++q) {
           const int32_t cand = star[f0 + q];
+          if (cache.seen(cand)) continue;
           const float d = node_tri_dist(tri, cand, px, py, pz);
           const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned int)cand;
           best = key < best ? key : best;
