@@ -439,9 +439,10 @@ int svie_dilate(const uint8_t* mask, int nx, int ny, int nz, int steps, uint8_t*
  * initialised to INT64_MAX by svie_sdf_keys_init. */
 int svie_sdf_keys_init(int64_t* keys, int64_t n, void* stream);
 /* _exact_near_field (sdf.py:100-145): nodes within exact_band cells of a
- * triangle's bounding box, kept when dist <= eb_keep. */
+ * triangle's bounding box, kept when dist <= eb_keep.  A warp takes 32
+ * triangles; `slices` (1-32) warps share them (more for larger triangles). */
 int svie_sdf_near_field(const float* tri, const double* tri64, int64_t ntri, int nx, int ny, int nz,
-                        double exact_band, float eb_keep, int64_t* keys, void* stream);
+                        double exact_band, float eb_keep, int slices, int64_t* keys, void* stream);
 /* keys -> dist (inf where empty), tid (-1 where empty), known mask */
 int svie_sdf_unpack(const int64_t* keys, int64_t n, float* dist, int32_t* tid, uint8_t* known,
                     void* stream);
@@ -472,9 +473,11 @@ int svie_sdf_star_pass(const int32_t* nodes, int64_t m, int nx, int ny, int nz, 
 /* _crossings_along_axis (sdf.py:285-340): acc int32 (n_axis+1) x n_b x n_c,
  * zeroed by the caller, accumulates the crossings of the grid lines parallel
  * to `axis`; svie_sdf_inside adds 1 to votes[x,y,z] where the prefix sum says
- * inside (signed_rule = winding number, else parity). */
+ * inside (signed_rule = winding number, else parity).  A warp takes 32
+ * triangles and their (triangle, line) pairs; `slices` (1-1024) warps share the
+ * pairs of one group (more for triangles that cover many lines). */
 int svie_sdf_crossings(const double* tri64, int64_t ntri, int nx, int ny, int nz, int axis,
-                       int signed_rule, int32_t* acc, void* stream);
+                       int signed_rule, int slices, int32_t* acc, void* stream);
 int svie_sdf_inside(const int32_t* acc, int nx, int ny, int nz, int axis, int signed_rule,
                     uint8_t* votes, void* stream);
 /* Mesh preprocessing (the host numpy work of sdf.py:205-208,385,398-402

@@ -166,7 +166,7 @@ _SIGS = {
     "svie_mesh_edge_topology": (I, [V, I64, V, Z, V, V, V]),
     "svie_mesh_signed_volume": (I, [V, V, I64, D, D, D, V, V]),
     "svie_sdf_keys_init": (I, [V, I64, V]),
-    "svie_sdf_near_field": (I, [V, V, I64, I, I, I, D, F, V, V]),
+    "svie_sdf_near_field": (I, [V, V, I64, I, I, I, D, F, I, V, V]),
     "svie_sdf_unpack": (I, [V, I64, V, V, V, V]),
     "svie_sdf_ring_mask": (I, [V, I, I, I, V, V]),
     "svie_sdf_ring_mark": (I, [V, I64, V, I, I, I, V, V]),
@@ -174,7 +174,7 @@ _SIGS = {
     "svie_sdf_scatter": (I, [V, I64, V, V, V, V, V, V]),
     "svie_sdf_outer_mask": (I, [V, I64, F, F, V, V]),
     "svie_sdf_star_pass": (I, [V, I64, I, I, I, V, V, V, V, V, V, V, V, V]),
-    "svie_sdf_crossings": (I, [V, I64, I, I, I, I, I, V, V]),
+    "svie_sdf_crossings": (I, [V, I64, I, I, I, I, I, I, V, V]),
     "svie_sdf_inside": (I, [V, I, I, I, I, I, V, V]),
     "svie_sdf_finalize": (I, [V, V, I64, I, F, F, V, V]),
 }

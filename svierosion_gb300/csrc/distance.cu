@@ -146,6 +146,14 @@ __global__ void k_piece_box(const float* __restrict__ tri, long long T, CellGrid
   }
 }
 
+// Occupancy of the cells, one bit per cell (32 cells per word, a warp per word).
+__global__ void k_piece_occupancy(const int* __restrict__ start, long long cells, unsigned int* __restrict__ bits) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool full = c < cells && start[c] < start[c + 1];
+  const unsigned int w = __ballot_sync(0xffffffffu, full);
+  if ((threadIdx.x & 31) == 0 && c < cells) bits[c >> 5] = w;
+}
+
 // min keys start at the largest key, max keys at the smallest
 __global__ void k_piece_box_init(unsigned int* __restrict__ box, long long n6) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -167,6 +175,9 @@ __global__ void k_piece_box_finish(const int* __restrict__ start, long long cell
 
 // distance from v to the interval [lo, hi] (infinite for an empty interval)
 SVIE_DEV float span_gap(float v, float lo, float hi) { return fmaxf(fmaxf(lo - v, v - hi), 0.0f); }
+
+// distance from v to the interval [lo, lo + cs]
+SVIE_DEV float box_gap(float v, float lo, float cs) { return fmaxf(fmaxf(lo - v, v - (lo + cs)), 0.0f); }
 
 // Cell (dx, dy, dz) number q of the Chebyshev shell of radius r: the two z
 // faces ((2r+1)^2 cells each), the two y faces ((2r+1)(2r-1)), the two x faces
@@ -224,7 +235,8 @@ SVIE_DEV void shell_cell(int r, int q, int& dx, int& dy, int& dz) {
 __global__ void __launch_bounds__(128) k_point_distance(const float* __restrict__ pts, long long n,
                                                         const float* __restrict__ tri, const int* __restrict__ start,
                                                         const int* __restrict__ order, const float* __restrict__ box,
-                                                        CellGrid G, float rho, float* __restrict__ out) {
+                                                        const unsigned int* __restrict__ occ, CellGrid G, float rho,
+                                                        float* __restrict__ out) {
   const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= n) return;  // whole warps
@@ -239,7 +251,13 @@ __global__ void __launch_bounds__(128) k_point_distance(const float* __restrict_
     shell_cell(r, q, dx, dy, dz);
     const int x = cx + dx, y = cy + dy, z = cz + dz;
     if (x < 0 || y < 0 || z < 0 || x >= G.gx || y >= G.gy || z >= G.gz) return -1;
+    // the cell's own box, widened by rho, first (no memory access), then its occupancy bit
+    const float ex = box_gap(p.x, G.ox + x * G.cs, G.cs), ey = box_gap(p.y, G.oy + y * G.cs, G.cs),
+                ez = box_gap(p.z, G.oz + z * G.cs, G.cs);
+    const float cgap = sqrtf(ex * ex + ey * ey + ez * ez) - rho;
+    if (cgap > 0.0f && cgap * cgap * 0.99999f > bound) return -1;
     const int c = (x * G.gy + y) * G.gz + z;
+    if (!((occ[c >> 5] >> (c & 31)) & 1u)) return -1;
     const float* b = box + 6LL * c;
     const float bx = span_gap(p.x, b[0], b[3]), by = span_gap(p.y, b[1], b[4]), bz = span_gap(p.z, b[2], b[5]);
     const float g2 = (bx * bx + by * by + bz * bz) * 0.99999f;
@@ -315,7 +333,7 @@ static long long piece_box_offset(long long T, long long cells) {
 
 size_t svie_piece_grid_bytes(int64_t T, int gx, int gy, int gz) {
   const long long cells = (long long)gx * gy * gz;
-  return (size_t)(piece_box_offset(T, cells) + 6 * cells) * sizeof(int) + 256;
+  return (size_t)(piece_box_offset(T, cells) + 6 * cells + (cells + 31) / 32) * sizeof(int) + 256;
 }
 
 int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float oz, float cs, int gx, int gy, int gz,
@@ -349,7 +367,8 @@ int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float
     k_piece_box<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, box);
   }
   k_piece_box_finish<<<blocks_for(cells, 256), 256, 0, s>>>(start, cells, box);
-  return launch_status("svie_piece_grid_build", T > 0 ? 8 : 5);
+  k_piece_occupancy<<<blocks_for(cells, 256), 256, 0, s>>>(start, cells, box + 6 * cells);
+  return launch_status("svie_piece_grid_build", T > 0 ? 9 : 6);
 }
 
 int svie_point_mesh_distance(const float* pts, int64_t n, const float* tri, int64_t T, float ox, float oy, float oz,
@@ -368,9 +387,10 @@ int svie_point_mesh_distance(const float* pts, int64_t n, const float* tri, int6
   const int* start = (const int*)ws;
   const int* order = start + 2 * (cells + 1);
   const float* box = (const float*)ws + piece_box_offset(T, cells);
+  const unsigned int* occ = (const unsigned int*)(box + 6 * cells);
   const CellGrid G{ox, oy, oz, cs, 1.0f / cs, gx, gy, gz};
-  k_point_distance<<<blocks_for(32 * n, 128), 128, 0, (cudaStream_t)stream>>>(pts, n, tri, start, order, box, G,
-                                                                               rho, out);
+  k_point_distance<<<blocks_for(32 * n, 128), 128, 0, (cudaStream_t)stream>>>(pts, n, tri, start, order, box, occ,
+                                                                               G, rho, out);
   return launch_status("svie_point_mesh_distance");
 }
 

@@ -57,7 +57,8 @@ __global__ void k_near_field(const float* __restrict__ tri, const double* __rest
   }
   const long long syz = (long long)ny * nz;
   const int nt = (int)min(32LL, ntri - t0);
-  for (int k = 0; k < nt; ++k) {
+  // gridDim.y slices share the 32 triangles (big triangles: more warps per group)
+  for (int k = blockIdx.y; k < nt; k += gridDim.y) {
     const int l0 = __shfl_sync(0xffffffffu, lo[0], k), l1 = __shfl_sync(0xffffffffu, lo[1], k),
               l2 = __shfl_sync(0xffffffffu, lo[2], k);
     const int d0 = __shfl_sync(0xffffffffu, dim[0], k), d1 = __shfl_sync(0xffffffffu, dim[1], k),
@@ -288,7 +289,8 @@ __global__ void k_crossings(const double* __restrict__ tri64, long long ntri, in
   }
   const long long total = __shfl_sync(0xffffffffu, incl, 31);
   const long long excl = incl - cnt;
-  for (long long base = 0; base < total; base += 32) {
+  // gridDim.y slices share the pairs (big triangles: more warps per group)
+  for (long long base = 32LL * blockIdx.y; base < total; base += 32LL * gridDim.y) {
     const long long j = base + lane;
     // owner: the first lane whose inclusive count passes j (counts are non-decreasing)
     int own = 0;
@@ -370,15 +372,16 @@ int svie_sdf_keys_init(int64_t* keys, int64_t n, void* stream) {
 }
 
 int svie_sdf_near_field(const float* tri, const double* tri64, int64_t ntri, int nx, int ny, int nz,
-                        double exact_band, float eb_keep, int64_t* keys, void* stream) {
-  if (ntri < 0 || !keys || (ntri > 0 && (!tri || !tri64)) || ntri >= (1LL << 31)) {
+                        double exact_band, float eb_keep, int slices, int64_t* keys, void* stream) {
+  if (ntri < 0 || !keys || (ntri > 0 && (!tri || !tri64)) || ntri >= (1LL << 31) || slices < 1 || slices > 32) {
     set_error("svie_sdf_near_field: bad arguments");
     return SVIE_ERR_ARG;
   }
   if (ntri == 0) return SVIE_OK;
-  // one warp per 32 triangles
-  k_near_field<<<blocks_for(ntri, 256), 256, 0, (cudaStream_t)stream>>>(tri, tri64, ntri, nx, ny, nz, exact_band,
-                                                                        eb_keep, (unsigned long long*)keys);
+  // one warp per 32 triangles, times `slices`
+  const dim3 grid(blocks_for(ntri, 256), slices);
+  k_near_field<<<grid, 256, 0, (cudaStream_t)stream>>>(tri, tri64, ntri, nx, ny, nz, exact_band, eb_keep,
+                                                        (unsigned long long*)keys);
   return launch_status("svie_sdf_near_field");
 }
 
@@ -453,17 +456,17 @@ int svie_sdf_star_pass(const int32_t* nodes, int64_t m, int nx, int ny, int nz, 
 }
 
 int svie_sdf_crossings(const double* tri64, int64_t ntri, int nx, int ny, int nz, int axis, int signed_rule,
-                       int32_t* acc, void* stream) {
-  if (ntri < 0 || axis < 0 || axis > 2 || !acc || ntri >= (1LL << 31)) {
+                       int slices, int32_t* acc, void* stream) {
+  if (ntri < 0 || axis < 0 || axis > 2 || !acc || ntri >= (1LL << 31) || slices < 1 || slices > 1024) {
     set_error("svie_sdf_crossings: bad arguments");
     return SVIE_ERR_ARG;
   }
   if (ntri == 0) return SVIE_OK;
   const int shape[3] = {nx, ny, nz};
   const int na = shape[axis], nb = shape[(axis + 1) % 3], nc = shape[(axis + 2) % 3];
-  // one warp per 32 triangles
-  k_crossings<<<blocks_for(ntri, 256), 256, 0, (cudaStream_t)stream>>>(tri64, ntri, na, nb, nc, axis, signed_rule,
-                                                                        acc);
+  // one warp per 32 triangles, times `slices`
+  const dim3 grid(blocks_for(ntri, 256), slices);
+  k_crossings<<<grid, 256, 0, (cudaStream_t)stream>>>(tri64, ntri, na, nb, nc, axis, signed_rule, acc);
   return launch_status("svie_sdf_crossings");
 }
 
