@@ -338,6 +338,9 @@ int svie_set_f64(double* dst, double value, void* stream);
  * maxbits[0], maxbits[1]). */
 int svie_mesh_pieces(const double* vertices, const int32_t* faces, int64_t T, double sx, double sy, double sz,
                      float* out, float* first_edge, uint32_t* maxbits, void* stream);
+/* The (T, 3) int64 faces of a host mesh as int32 on the device (the upload of meshio.TriMesh's faces);
+ * *bad = the number of indices outside [0, V), which are written as 0. */
+int svie_mesh_faces_i32(const int64_t* faces64, int64_t T, int64_t V, int32_t* faces, int* bad, void* stream);
 /* Exact bounding box of V float64 vertices (V, 3): out = (min x, min y, min z, max x, max y, max z),
  * numpy's per-column min / max (TriMesh.bounds, meshio.py:35-37); ws holds 48 bytes. */
 int svie_mesh_bounds(const double* vertices, int64_t V, void* ws, size_t ws_bytes, double* out, void* stream);

@@ -142,6 +142,7 @@ _SIGS = {
     "svie_reinit_rhs": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),
     "svie_mesh_pieces": (I, [V, V, I64, D, D, D, V, V, V, V]),
     "svie_mesh_bounds": (I, [V, I64, V, Z, V, V]),
+    "svie_mesh_faces_i32": (I, [V, I64, I64, V, V, V]),
     "svie_order_stats_bytes": (Z, []),
     "svie_order_stats_f32": (I, [V, I64, I64, I64, V, Z, V, V]),
     "svie_surface_signed_volume": (I, [V, V, I64, D, D, D, V, V]),

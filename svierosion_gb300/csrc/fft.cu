@@ -745,35 +745,42 @@ struct GL32 {
 // column, so the block computes the quad^2 square roots once (shared memory)
 // and reuses them for each cut cell; the cell's sum is a block reduction.
 __global__ void __launch_bounds__(256) k_ball_weights(double R, int m, int quad, GL32 gl, double* __restrict__ w) {
-  extern __shared__ double zr[];  // quad * quad
+  extern __shared__ double zr[];  // quad * quad square roots, then one class byte per cell of the column
   __shared__ double gx[64], gw[64], red[8];
   const int side = 2 * m + 1;
+  const int q2 = quad * quad;
+  unsigned char* cls = reinterpret_cast<unsigned char*>(zr + q2);
   const int i = (int)(blockIdx.x / side) - m, j = (int)(blockIdx.x % side) - m;
   const double ci = i, cj = j;
+  double* col = w + ((long long)(i + m) * side + (j + m)) * side;
   if (threadIdx.x < quad) {
     gx[threadIdx.x] = gl.x[threadIdx.x];
     gw[threadIdx.x] = gl.w[threadIdx.x];
   }
-  __syncthreads();
-  const int q2 = quad * quad;
+  // each cell of the column classified once: 1 inside, 0 outside, 2 cut
+  auto nr = [](double c) { const double v = fabs(c) - 0.5; return v > 0 ? v : 0.0; };
+  const double a0 = nr(ci), a1 = nr(cj), b0 = fabs(ci) + 0.5, b1 = fabs(cj) + 0.5;
+  bool any_cut = false;
+  for (int kk = threadIdx.x; kk < side; kk += blockDim.x) {
+    const double ck = kk - m;
+    const double a2 = nr(ck), b2 = fabs(ck) + 0.5;
+    const double near = sqrt(a0 * a0 + a1 * a1 + a2 * a2);  // squares of half-integers: exact sums
+    const double far = sqrt(b0 * b0 + b1 * b1 + b2 * b2);
+    const unsigned char c = far <= R ? 1 : ((near < R && far > R) ? 2 : 0);
+    cls[kk] = c;
+    if (c != 2) col[kk] = c == 1 ? 1.0 : 0.0;
+    any_cut |= c == 2;
+  }
+  if (!__syncthreads_or(any_cut)) return;
   for (int p = threadIdx.x; p < q2; p += blockDim.x) {
     const double X = ci + gx[p / quad], Y = cj + gx[p % quad];
     const double r2 = R * R - X * X - Y * Y;
     zr[p] = sqrt(r2 > 0 ? r2 : 0.0);
   }
   __syncthreads();
-  auto nr = [](double c) { const double v = fabs(c) - 0.5; return v > 0 ? v : 0.0; };
-  const double a0 = nr(ci), a1 = nr(cj), b0 = fabs(ci) + 0.5, b1 = fabs(cj) + 0.5;
-  double* col = w + ((long long)(i + m) * side + (j + m)) * side;
   for (int kk = 0; kk < side; ++kk) {
+    if (cls[kk] != 2) continue;
     const double ck = kk - m;
-    const double a2 = nr(ck), b2 = fabs(ck) + 0.5;
-    const double near = sqrt(a0 * a0 + a1 * a1 + a2 * a2);   // squares of half-integers: exact sums
-    const double far = sqrt(b0 * b0 + b1 * b1 + b2 * b2);
-    if (!(near < R && far > R)) {
-      if (threadIdx.x == 0) col[kk] = far <= R ? 1.0 : 0.0;
-      continue;
-    }
     const double lo = ck - 0.5, hi = ck + 0.5;
     double acc = 0.0;
     for (int p = threadIdx.x; p < q2; p += blockDim.x) {
@@ -806,10 +813,12 @@ __global__ void k_khat_a(const double* __restrict__ w, int m, int nz, int nzh, d
     const int kz = (int)(t - ij * nzh);
     const double* row = w + ij * side;
     double acc = 0.0;
+    // phase (kz k) mod nz, stepped by kz from k = -m (no division in the loop)
+    int ph = (int)(((long long)kz * (nz - m % nz)) % nz);
     for (int k = -m; k <= m; ++k) {
-      long long ph = ((long long)kz * k) % nz;
-      if (ph < 0) ph += nz;
       acc += row[k + m] * ctab[ph];
+      ph += kz;
+      if (ph >= nz) ph -= nz;
     }
     A[t] = acc;
   }
@@ -827,10 +836,11 @@ __global__ void k_khat_b(const double* __restrict__ A, int m, int ny, int nzh, d
     const int ky = (int)((t / nzh) % nyh);
     const int i = (int)(t / ((long long)nzh * nyh));
     double acc = 0.0;
+    int ph = (int)(((long long)ky * (ny - m % ny)) % ny);
     for (int j = -m; j <= m; ++j) {
-      long long ph = ((long long)ky * j) % ny;
-      if (ph < 0) ph += ny;
       acc += A[((long long)i * side + (j + m)) * nzh + kz] * ctab[ph];
+      ph += ky;
+      if (ph >= ny) ph -= ny;
     }
     Bq[t] = acc;
   }
@@ -848,10 +858,11 @@ __global__ void k_khat_c(const double* __restrict__ Bq, int m, int nx, int ny, i
     const int kx = (int)(t / plane);
     const long long r = t - (long long)kx * plane;
     double acc = 0.0;
+    int ph = (int)(((long long)kx * (nx - m % nx)) % nx);
     for (int i = -m; i <= m; ++i) {
-      long long ph = ((long long)kx * i) % nx;
-      if (ph < 0) ph += nx;
       acc += Bq[(long long)(i + m) * plane + r] * ctab[ph];
+      ph += kx;
+      if (ph >= nx) ph -= nx;
     }
     K[t] = (float)acc;
   }
@@ -1096,8 +1107,12 @@ int svie_ball_weights(double radius, double spacing, int quad, double* w, void* 
   memset(&gl, 0, sizeof(gl));
   gauss_legendre(quad, gl.x, gl.w);
   const long long side = 2 * m + 1;
-  k_ball_weights<<<(unsigned)(side * side), 256, (size_t)quad * quad * sizeof(double), (cudaStream_t)stream>>>(
-      radius / spacing, m, quad, gl, w);
+  const size_t smem = (size_t)quad * quad * sizeof(double) + (size_t)side;
+  if (smem > 48 * 1024) {
+    set_error("svie_ball_weights: ball too large for one column per block (radius/spacing %g)", radius / spacing);
+    return SVIE_ERR_UNSUPPORTED;
+  }
+  k_ball_weights<<<(unsigned)(side * side), 256, smem, (cudaStream_t)stream>>>(radius / spacing, m, quad, gl, w);
   return launch_status("svie_ball_weights");
 }
 

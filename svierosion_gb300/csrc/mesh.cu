@@ -230,6 +230,17 @@ __global__ void k_mesh_pieces(const double* __restrict__ v, const int32_t* __res
   }
 }
 
+// int64 faces -> int32, counting indices outside [0, V) into *bad
+__global__ void k_faces_i32(const int64_t* __restrict__ src, long long n3, long long V, int32_t* __restrict__ dst,
+                            int* bad) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n3) return;
+  const long long v = src[e];
+  const bool ok = v >= 0 && v < V;
+  dst[e] = ok ? (int32_t)v : 0;
+  if (!ok) atomicAdd(bad, 1);
+}
+
 // ------------------------------------------------------------ bounding box
 // Order-preserving unsigned keys of IEEE values: the sign bit set for
 // non-negative values, all bits flipped for negative ones.  min / max of keys
@@ -462,6 +473,21 @@ int svie_mesh_edge_topology(const int32_t* faces, int64_t T, void* table, size_t
   k_edges<<<blocks_for(3 * T, 256), 256, 0, s>>>(faces, T, keys, count, dsum, cap, overflow);
   k_edge_stats<<<blocks_for(cap, 256), 256, 0, s>>>(keys, count, dsum, cap, (unsigned long long*)out4);
   return launch_status("svie_mesh_edge_topology", 2);
+}
+
+int svie_mesh_faces_i32(const int64_t* faces64, int64_t T, int64_t V, int32_t* faces, int* bad, void* stream) {
+  if (T < 0 || V < 0 || V >= (1LL << 31) || !bad || (T > 0 && (!faces64 || !faces))) {
+    set_error("svie_mesh_faces_i32: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemsetAsync(bad, 0, sizeof(int), s) != cudaSuccess) {
+    set_error("svie_mesh_faces_i32: memset failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  if (T == 0) return SVIE_OK;
+  k_faces_i32<<<blocks_for(3 * T, 256), 256, 0, s>>>(faces64, 3 * T, V, faces, bad);
+  return launch_status("svie_mesh_faces_i32");
 }
 
 int svie_mesh_signed_volume(const double* vertices, const int32_t* faces, int64_t T, double cx, double cy, double cz,
