@@ -176,3 +176,32 @@ def test_laws_elementwise():
         Vr, Dr = ref.speed_and_diffusivity(k1.cpu().numpy(), k2.cpu().numpy())
         _close(V, Vr, 1e-5, 1e-5)
         _close(D, Dr, 1e-5, 1e-4)
+
+
+def test_sdf_slices_do_not_change_results():
+    """svie_sdf_near_field and svie_sdf_crossings split a group of 32 triangles over `slices`
+    warps; the node keys and crossing counters are the same for any split (coarse cube
+    triangles, which cover many lines and nodes, and a fine fragment)."""
+    from svierosion_gb300 import shapes
+    from svierosion_gb300.sdf import device_mesh
+
+    for mesh, res in ((shapes.cube(1.0), 40), (shapes.fragment(3, seed=1), 48)):
+        params = S.ErosionParams(law="svi", radius=0.1, k=1, s=1, t=0.93, resolution=res)
+        g = S.make_grid(mesh, params)
+        nx, ny, nz = g.shape
+        tri64, tri32, _ = device_mesh(mesh).tri_index(g)
+        T = tri64.shape[0]
+        keys, accs = [], []
+        for slices in (1, 7, 32):
+            k = torch.empty(g.size, dtype=torch.int64, device="cuda")
+            nat.call("svie_sdf_keys_init", nat.ptr(k), g.size, nat.stream())
+            nat.call("svie_sdf_near_field", nat.ptr(tri32), nat.ptr(tri64), T, nx, ny, nz, 2.0,
+                     nat.f32(2.0 * (1 + 1e-6)), slices, nat.ptr(k), nat.stream())
+            keys.append(k.cpu().numpy())
+            acc = torch.zeros((nx + 1) * ny * nz, dtype=torch.int32, device="cuda")
+            nat.call("svie_sdf_crossings", nat.ptr(tri64), T, nx, ny, nz, 0, 1, slices * 3, nat.ptr(acc),
+                     nat.stream())
+            accs.append(acc.cpu().numpy())
+        assert (keys[0] != np.iinfo(np.int64).max).any() and accs[0].any()
+        for k, a in zip(keys[1:], accs[1:]):
+            assert np.array_equal(k, keys[0]) and np.array_equal(a, accs[0])
