@@ -389,14 +389,18 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
                                                              int second, int nbm) {
   const float cfl = __ldg(g.cfl);
   if ((int)blockIdx.x < nbm) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= m) return;
-    const uint32_t flags = __ldg(g.meta + t);
-    if (flags & 63u) return;
-    const int i = __ldg(idx + t);
-    float hmin;
-    const float r = reinit_rhs_at<false>(src, i, g, 0, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
-    sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
+    // a contiguous run of the brick-ordered list per block: the bricks that follow one
+    // another along z are swept by the same SM, whose L1 still holds their shared rows
+    const long long per = ((m + nbm - 1) / nbm + blockDim.x - 1) / blockDim.x * blockDim.x;
+    const long long t0 = (long long)blockIdx.x * per, t1 = min(t0 + per, m);
+    for (long long t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+      const uint32_t flags = __ldg(g.meta + t);
+      if (flags & 63u) continue;
+      const int i = __ldg(idx + t);
+      float hmin;
+      const float r = reinit_rhs_at<false>(src, i, g, 0, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
+      sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
+    }
     return;
   }
   const int X = __ldg(g.wx + g.W);
@@ -710,12 +714,13 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
     set_error("svie_reinit_iterate: copy failed");
     return SVIE_ERR_LAUNCH;
   }
-  const int nb = blocks_for(m, RI_THREADS);
   const float rh = rn_reciprocal(h), rhh = rn_reciprocal(h * h);
   const Geo g = geo_view_host(const_cast<void*>(geo), m);
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // main blocks: one resident wave (8 per SM), each over a contiguous run of the list
+  const int nb = (int)std::min<long long>((long long)blocks_for(m, RI_THREADS), 8LL * nsm);
   const int nbx = (int)std::min<long long>((long long)blocks_for(m, RI_THREADS), 8LL * nsm);
   for (int it = 0; it < iterations; ++it) {
     k_reinit_sweep<<<nb + nbx, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, g, 0, nb);
