@@ -5,8 +5,8 @@ r = 0.08 L, four laws: svi k0 s0, svi k1 s1 t0.93, svi k2 s1 t0.95 (to 90% of th
 curvature alpha 1 (capped at 40 steps).  Two phases, so that the float64 oracle (CPU, minutes per law)
 does not hold a GPU:
 
-    python tests/precision_study.py gpu gpurun_out/precision.npz      # on a GPU machine: GPU runs + inputs
-    python tests/precision_study.py compare gpurun_out/precision.npz  # anywhere: float64 runs, report
+    python tests/precision_study.py gpu precision.npz      # with a GPU: the GPU runs and their inputs
+    python tests/precision_study.py compare precision.npz  # anywhere: the float64 runs and the report
 
 The report (one JSON line per law) gives max |N_r(fp32) - N_r(fp64)| on the initial grid, the largest
 volume-fraction difference along the trajectory, both stopping steps, max |phi(fp32) - phi(fp64)|
