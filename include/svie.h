@@ -326,11 +326,13 @@ int svie_set_f64(double* dst, double value, void* stream);
 /* ------------------------------------------------- point-to-mesh distance */
 /* point_mesh_distance (svierosion/api.py:104-168), exact: the T pieces (T x 9
  * floats) are binned by centroid into a gx x gy x gz grid of cells of side cs
- * from (ox, oy, oz), with the bounding box of each cell's pieces
- * (svie_piece_grid_build, workspace svie_piece_grid_bytes);
+ * from (ox, oy, oz), with the bounding box of each cell's pieces, an occupancy
+ * bit per cell and each piece's bounding sphere (svie_piece_grid_build,
+ * workspace svie_piece_grid_bytes);
  * svie_point_mesh_distance walks Chebyshev shells of cells around each point
  * (one warp per point), visiting the cells whose piece box is not farther than
- * the best distance so far, until no unvisited piece can be closer (rho bounds
+ * the best distance so far and testing their pieces against their bounding
+ * spheres first, until no unvisited piece can be closer (rho bounds
  * centroid-to-piece distances), and writes the distance (float32, sqrt of the
  * float32 squared distance of kernels.py:382-427). */
 /* The triangles of a device mesh relative to (sx, sy, sz) as float32 pieces (T x 9), the first-edge

@@ -154,6 +154,22 @@ __global__ void k_piece_occupancy(const int* __restrict__ start, long long cells
   if ((threadIdx.x & 31) == 0 && c < cells) bits[c >> 5] = w;
 }
 
+// Bounding sphere of every piece, in the order of the cell lists: sph[k] = (centroid,
+// radius) of piece order[k]; the radius is widened by 1e-5 relative so that it bounds
+// the float32 vertices despite rounding.
+__global__ void k_piece_spheres(const float* __restrict__ tri, const int* __restrict__ order, long long T,
+                                float4* __restrict__ sph) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= T) return;
+  const int t = order[k];
+  const float3 a = piece_vertex(tri, t, 0), b = piece_vertex(tri, t, 1), c = piece_vertex(tri, t, 2);
+  const float3 m = make_float3((a.x + b.x + c.x) * (1.0f / 3.0f), (a.y + b.y + c.y) * (1.0f / 3.0f),
+                               (a.z + b.z + c.z) * (1.0f / 3.0f));
+  auto d2 = [&](float3 v) { return (v.x - m.x) * (v.x - m.x) + (v.y - m.y) * (v.y - m.y) + (v.z - m.z) * (v.z - m.z); };
+  const float r = sqrtf(fmaxf(fmaxf(d2(a), d2(b)), d2(c)));
+  sph[k] = make_float4(m.x, m.y, m.z, r * 1.00001f + 1e-30f);
+}
+
 // min keys start at the largest key, max keys at the smallest
 __global__ void k_piece_box_init(unsigned int* __restrict__ box, long long n6) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -235,7 +251,8 @@ SVIE_DEV void shell_cell(int r, int q, int& dx, int& dy, int& dz) {
 __global__ void __launch_bounds__(128) k_point_distance(const float* __restrict__ pts, long long n,
                                                         const float* __restrict__ tri, const int* __restrict__ start,
                                                         const int* __restrict__ order, const float* __restrict__ box,
-                                                        const unsigned int* __restrict__ occ, CellGrid G, float rho,
+                                                        const unsigned int* __restrict__ occ,
+                                                        const float4* __restrict__ sph, CellGrid G, float rho,
                                                         float* __restrict__ out) {
   const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -306,7 +323,14 @@ __global__ void __launch_bounds__(128) k_point_distance(const float* __restrict_
           if (v <= j) lo += step;
         }
         const int ok1 = __shfl_sync(0xffffffffu, k1, lo), oex = __shfl_sync(0xffffffffu, excl, lo);
-        if (j < total) best = fminf(best, piece_d2(ok1 + (j - oex)));
+        if (j < total) {
+          // the piece's bounding sphere first: skip it when even the sphere is farther than the best
+          const int k = ok1 + (j - oex);
+          const float4 b = __ldg(sph + k);
+          const float ex = p.x - b.x, ey = p.y - b.y, ez = p.z - b.z;
+          const float lb = sqrtf(ex * ex + ey * ey + ez * ez) - b.w;
+          if (lb <= 0.0f || lb * lb * 0.99999f <= best) best = fminf(best, piece_d2(k));
+        }
       }
     }
     best = warp_min(best);
@@ -331,9 +355,14 @@ static long long piece_box_offset(long long T, long long cells) {
   return ((2 * (cells + 1) + T + nb) + 3) / 4 * 4;  // in ints
 }
 
+// then the occupancy bits (one per cell), then the piece spheres (float4 per piece, 16-byte aligned)
+static long long piece_sphere_offset(long long T, long long cells) {
+  return (piece_box_offset(T, cells) + 6 * cells + (cells + 31) / 32 + 3) / 4 * 4;  // in ints
+}
+
 size_t svie_piece_grid_bytes(int64_t T, int gx, int gy, int gz) {
   const long long cells = (long long)gx * gy * gz;
-  return (size_t)(piece_box_offset(T, cells) + 6 * cells + (cells + 31) / 32) * sizeof(int) + 256;
+  return (size_t)(piece_sphere_offset(T, cells) + 4 * T) * sizeof(int) + 256;
 }
 
 int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float oz, float cs, int gx, int gy, int gz,
@@ -365,10 +394,12 @@ int svie_piece_grid_build(const float* tri, int64_t T, float ox, float oy, float
   if (T > 0) {
     k_piece_fill<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, start, cursor, order);
     k_piece_box<<<blocks_for(T, 256), 256, 0, s>>>(tri, T, G, box);
+    k_piece_spheres<<<blocks_for(T, 256), 256, 0, s>>>(tri, order, T,
+                                                      (float4*)((int*)ws + piece_sphere_offset(T, cells)));
   }
   k_piece_box_finish<<<blocks_for(cells, 256), 256, 0, s>>>(start, cells, box);
   k_piece_occupancy<<<blocks_for(cells, 256), 256, 0, s>>>(start, cells, box + 6 * cells);
-  return launch_status("svie_piece_grid_build", T > 0 ? 9 : 6);
+  return launch_status("svie_piece_grid_build", T > 0 ? 10 : 6);
 }
 
 int svie_point_mesh_distance(const float* pts, int64_t n, const float* tri, int64_t T, float ox, float oy, float oz,
@@ -388,9 +419,10 @@ int svie_point_mesh_distance(const float* pts, int64_t n, const float* tri, int6
   const int* order = start + 2 * (cells + 1);
   const float* box = (const float*)ws + piece_box_offset(T, cells);
   const unsigned int* occ = (const unsigned int*)(box + 6 * cells);
+  const float4* sph = (const float4*)((const int*)ws + piece_sphere_offset(T, cells));
   const CellGrid G{ox, oy, oz, cs, 1.0f / cs, gx, gy, gz};
   k_point_distance<<<blocks_for(32 * n, 128), 128, 0, (cudaStream_t)stream>>>(pts, n, tri, start, order, box, occ,
-                                                                               G, rho, out);
+                                                                               sph, G, rho, out);
   return launch_status("svie_point_mesh_distance");
 }
 
