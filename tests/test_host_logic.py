@@ -62,3 +62,28 @@ def test_params_make_law_auto_delta():
     assert law.delta == 0.25
     p = ErosionParams(law="mean", alpha=0.5)
     assert p.make_law(length_scale=2.0).delta == 0.5
+
+
+def test_warp_slices_for_triangle_groups():
+    """The number of warps that share a group of 32 triangles grows with the square of the
+    longest edge (lines or nodes a triangle covers) and stays within [1, cap]."""
+    from svierosion_gb300.sdf import _slices
+
+    assert _slices(1.1, 64.0, 1024) == 1          # scan-size triangles: one warp per group
+    assert _slices(1.1, 2.0, 32) == 1
+    assert _slices(8.0, 2.0, 32) == 32            # split soup: edges up to 8 cells
+    assert _slices(45.0, 64.0, 1024) == 32        # a coarse cube at resolution 32
+    assert _slices(1e6, 64.0, 1024) == 1024
+    assert _slices(0.0, 64.0, 1024) == 1
+
+
+def test_mesh_bounds_without_a_device_copy():
+    """mesh_bounds falls back to TriMesh.bounds when the mesh has no device copy."""
+    from svierosion_gb300.sdf import mesh_bounds
+
+    m = shapes.fragment(2, seed=4)
+    assert np.array_equal(mesh_bounds(m), m.bounds)
+    g = make_grid(m, ErosionParams(law="mean", resolution=48))
+    lo, hi = m.bounds
+    top = np.asarray(g.origin) + g.spacing * (np.asarray(g.shape) - 1)
+    assert np.all(np.asarray(g.origin) < lo) and np.all(top > hi)
