@@ -237,14 +237,15 @@ SVIE_DEV void shell_cell(int r, int q, int& dx, int& dy, int& dz) {
 }
 
 // One warp per query point.  The lanes split the cells of each Chebyshev
-// shell around the point's cell; a cell is a candidate while the bounding box
-// of its pieces is not farther than the best distance so far (empty cells have
-// an empty box, never a candidate).  Each shell takes two passes: the first
-// tests one piece of every candidate cell, which gives the warp a near-final
-// bound; the second tests the other pieces of the cells that are still
-// candidates, spread over all 32 lanes (a warp scan of the per-cell counts and
-// a search for each piece's cell) so that a cell with many pieces does not
-// leave the other lanes idle.  After each shell the warp takes the minimum and
+// shell around the point's cell; a cell is a candidate while it is not farther
+// than the best distance so far: first by its own box widened by rho (no memory
+// access), then by its occupancy bit, then by the bounding box of its pieces.
+// Each shell takes two passes: the first tests one piece of every candidate
+// cell, which gives the warp a near-final bound; the second tests the other
+// pieces of the cells that are still candidates, spread over all 32 lanes (a
+// warp scan of the per-cell counts and a search for each piece's cell) so that
+// a cell with many pieces does not leave the other lanes idle, each piece first
+// against its bounding sphere.  After each shell the warp takes the minimum and
 // stops once no unvisited piece can be closer (pieces are binned by centroid,
 // so an unvisited one is farther than r cs - rho).  The result is the exact
 // minimum over the pieces.
