@@ -228,9 +228,12 @@ int svie_band_volume(const float* phi, const int32_t* band, int64_t m, int64_t s
  * scratch is a static 512 KiB device array held by every GPU that loads the
  * library, so m is limited to svie_band_volume_noalloc_max() band nodes
  * (16,777,216); larger m returns SVIE_ERR_CAPACITY.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress), so make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race and must be ordered by the caller. */
+ * device (and in each further CUDA context made current on it) looks up the
+ * array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  Do not reset the device between calls: a
+ * recreated context may reuse its old handle, and the cached address would
+ * then be stale.  All calls share the array: calls that overlap on the GPU
+ * race and must be ordered by the caller. */
 int64_t svie_band_volume_noalloc_max(void);
 int svie_band_volume_noalloc(const float* phi, const int32_t* band, int64_t m, int64_t sx,
                              int64_t sy, int64_t sz, float* occ, svie_stats* stats, void* stream);

@@ -400,27 +400,70 @@ constexpr long long VOLUME_NOALLOC_MAX_CTAS = 65536;  // 512 KiB of float64 part
 static __device__ __align__(256) double g_volume_partials[VOLUME_NOALLOC_MAX_CTAS];
 
 static std::mutex g_volume_symbol_mutex;
-static double* g_volume_symbol[64] = {};
 
-// Device address of g_volume_partials on the current device, looked up once per
-// device (the array's name in host code is only a stand-in for the symbol).
+// One resolved address per (device, context).  A driver-API context made
+// current by a host framework loads this library's module anew, so the array
+// has another address there; the context handle tells the cases apart.  A
+// context destroyed and created again (cudaDeviceReset) may reuse its old
+// handle value, which this cache cannot tell from the old context: callers
+// must not reset the device between calls.
+struct VolumeSymbol {
+  int dev;
+  void* ctx;
+  double* addr;
+};
+static VolumeSymbol g_volume_symbol[64];
+static int g_volume_symbol_n = 0;
+
+typedef int (*CtxGetCurrentFn)(void**);
+
+// The current context's handle through the driver entry point (no link to
+// libcuda); nullptr when it cannot be had, and then the device alone keys the
+// cache.  Called with g_volume_symbol_mutex held.
+static void* current_context() {
+  static CtxGetCurrentFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (CtxGetCurrentFn)f;
+    tried = true;
+  }
+  void* ctx = nullptr;
+  if (fn && fn(&ctx) != 0) ctx = nullptr;
+  return ctx;
+}
+
+// Device address of g_volume_partials in the current device's context, looked
+// up once per device and context (the array's name in host code is only a
+// stand-in for the symbol).
 static int volume_partials_address(double** out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
     set_error("svie_band_volume_noalloc: no usable current CUDA device");
     return SVIE_ERR_LAUNCH;
   }
   std::lock_guard<std::mutex> lock(g_volume_symbol_mutex);
-  if (!g_volume_symbol[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_volume_partials);
-    if (e != cudaSuccess || !p) {
-      set_error("svie_band_volume_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
-      return SVIE_ERR_LAUNCH;
+  // nullptr while no context is current: the runtime then works in the
+  // device's primary context, which that key stands for
+  void* ctx = current_context();
+  for (int i = 0; i < g_volume_symbol_n; ++i) {
+    if (g_volume_symbol[i].dev == dev && g_volume_symbol[i].ctx == ctx) {
+      *out = g_volume_symbol[i].addr;
+      return SVIE_OK;
     }
-    g_volume_symbol[dev] = (double*)p;
   }
-  *out = g_volume_symbol[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_volume_partials);
+  if (e != cudaSuccess || !p) {
+    set_error("svie_band_volume_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+    return SVIE_ERR_LAUNCH;
+  }
+  // a full table (more than 64 device/context pairs) keeps working uncached
+  if (g_volume_symbol_n < 64) g_volume_symbol[g_volume_symbol_n++] = VolumeSymbol{dev, ctx, (double*)p};
+  *out = (double*)p;
   return SVIE_OK;
 }
 
@@ -433,14 +476,15 @@ int64_t svie_band_volume_noalloc_max(void) { return (int64_t)svie::VOLUME_NOALLO
 int svie_band_volume_noalloc(const float* phi, const int32_t* band, int64_t m, int64_t sx, int64_t sy, int64_t sz,
                              float* occ, svie_stats* stats, void* stream) {
   using namespace svie;
-  if (m < 0 || !stats || (m > 0 && (!phi || !band))) {
-    set_error("svie_band_volume_noalloc: bad arguments");
-    return SVIE_ERR_ARG;
-  }
+  // the size limit is checked first, before any pointer is looked at
   if (m > svie_band_volume_noalloc_max()) {
     set_error("svie_band_volume_noalloc: %lld band nodes exceed the static scratch limit of %lld; use "
               "svie_band_volume with a workspace", (long long)m, (long long)svie_band_volume_noalloc_max());
     return SVIE_ERR_CAPACITY;
+  }
+  if (m < 0 || !stats || (m > 0 && (!phi || !band))) {
+    set_error("svie_band_volume_noalloc: bad arguments");
+    return SVIE_ERR_ARG;
   }
   double* partials = nullptr;
   int st = volume_partials_address(&partials);

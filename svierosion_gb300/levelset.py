@@ -157,16 +157,6 @@ class LevelSet:
         nat.call("svie_mask_write", nat.ptr(mask), n, nat.ptr(ws), ws.numel(), nat.ptr(band), m, nat.stream())
         return band
 
-    def _check_margin(self, idx: torch.Tensor) -> None:
-        """levelset.py:79-86 for an arbitrary index list."""
-        if idx.numel() == 0:
-            return
-        shape = self.grid.shape
-        for ax, s in enumerate(self.strides):
-            coord = (idx // s) % shape[ax]
-            if int(coord.min()) < MARGIN or int(coord.max()) > shape[ax] - 1 - MARGIN:
-                raise RuntimeError("narrow band reaches the grid boundary; enlarge the padding")
-
     def interface_nodes(self, idx: torch.Tensor | None = None) -> torch.Tensor:
         """Band nodes having a 6-neighbour of the opposite sign (levelset.py:88-91)."""
         from .kernels import interface_mask
@@ -268,10 +258,6 @@ class LevelSet:
         nat.call("svie_closest_points_newton", nat.ptr(self.flat), nat.ptr(i), i.numel(), ny, nz, nx - 3.001,
                  ny - 3.001, nz - 3.001, self.h, int(newton_steps), nat.ptr(out), nat.stream())
         return out
-
-    def clamp_to_interior(self, p: torch.Tensor) -> torch.Tensor:
-        hi = torch.tensor([n - 3.001 for n in self.grid.shape], device=p.device, dtype=p.dtype)
-        return torch.minimum(p.clamp_min(1.0), hi)
 
     # --------------------------------------------------- reinitialisation
     def reinitialize(self, iterations: int = 12, cfl: float = 0.45, dilation: int = 3, timer=None,

@@ -70,10 +70,10 @@ def test_noalloc_volume_matches_workspace_version():
 def test_noalloc_rejects_sizes_beyond_the_static_scratch():
     from svierosion_gb300 import _native as nat
     lib = nat.load()
-    ls = _level_set(h=0.08)
     stats = _stats_tensor()
     too_many = lib.svie_band_volume_noalloc_max() + 1
-    rc = lib.svie_band_volume_noalloc(nat.ptr(ls.flat), nat.ptr(ls.band32), too_many, *ls.strides, None,
-                                      nat.ptr(stats), nat.stream())
+    # no field or band is passed: the size check comes before any pointer is
+    # used, so the call cannot reach device memory even if the check broke
+    rc = lib.svie_band_volume_noalloc(None, None, too_many, 1 << 20, 1 << 10, 1, None, nat.ptr(stats), nat.stream())
     assert rc == 6  # SVIE_ERR_CAPACITY, before anything is launched
     assert b"static scratch limit" in lib.svie_last_error()
