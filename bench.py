@@ -17,9 +17,10 @@ Lines printed (one JSON line on rank 0):
              from a host mesh to host results), roofline of the dominant
              kernel (CUDA-event duration, algorithmic bytes), cpu_baseline
              (the numpy oracle on a bounded sample), clocks, gpu_launches.
-  reference: the reference algorithm's CPU restatement (numpy oracle, on all
-             host cores) on the same workload, one RK stage per step (bounded
-             sample).
+  reference: the reference algorithm's CPU restatement (the numpy oracle
+             port on all host cores) on the same workload: whole steps of the
+             reference's step loop, reinitialisations included (bounded to
+             --ref-budget seconds).
 Multi-GPU: every rank erodes its own replica (no collective in the path):
 ``value`` sums the band updates of all ranks over the slowest rank's time.
 """
@@ -122,25 +123,89 @@ def run_batched(args) -> dict:
             "stop_reasons": {k: sum(r.stop_reason == k for r in res_b) for k in {r.stop_reason for r in res_b}}}
 
 
-def run_served(args) -> dict:
-    """Open-loop Poisson stream through the continuous-batching server."""
-    import torch
+def _served_stream(specs, arrivals, hbm_gb: float, max_active: int):
     from svierosion_gb300.batch import ErosionServer, Request
 
-    torch.cuda.set_device(0)
-    specs = batch_specs(args.requests, seed=args.seed, served=True, max_steps=args.max_steps)
-    rng = np.random.default_rng(7 + args.seed)
-    gaps = rng.exponential(1.0 / args.rate, len(specs))
-    arrivals = np.cumsum(gaps) - gaps[0]
     reqs = [Request(i, float(a), m, p) for i, (a, (m, p)) in enumerate(zip(arrivals, specs))]
-    srv = ErosionServer(hbm_budget_bytes=int(args.hbm_gb * (1 << 30)), max_active=args.max_active)
-    stats = srv.run(reqs)
-    return {"metric": METRIC, "value": round(stats["band_updates_per_s"], 1), "unit": UNIT, "n_gpus": 1,
+    srv = ErosionServer(hbm_budget_bytes=int(hbm_gb * (1 << 30)), max_active=max_active)
+    return srv.run(reqs), reqs
+
+
+def served_vs_plain(n_requests: int, seed: int = 0, max_steps: int = 400, hbm_gb: float = 150.0,
+                    max_active: int = 64, load: float = 0.8) -> dict:
+    """The served form against the plain one on the same requests (the served configuration's mix).
+
+    1. capacity: every request queued at t = 0 through the continuous-batching server;
+    2. stream: the same requests as an open-loop Poisson stream at `load` x that capacity;
+    3. plain: the same requests solved one at a time in arrival order on the plain path, each solve
+       timed; its latencies are those of a FIFO queue fed the stream's arrival times with the measured
+       solve times.
+    Results of the served stream and of the plain solves are compared request by request."""
+    import torch
+    from svierosion_gb300.batch import ErosionJob, run_plain
+
+    torch.cuda.set_device(0)
+    t_in = time.time()
+    specs = batch_specs(n_requests, seed=seed, served=True, max_steps=max_steps)
+    t_in = time.time() - t_in
+    cap, _ = _served_stream(specs, np.zeros(len(specs)), hbm_gb, max_active)
+    rate = load * cap["solves_per_s"]
+    rng = np.random.default_rng(7 + seed)
+    gaps = rng.exponential(1.0 / rate, len(specs))
+    arrivals = np.cumsum(gaps) - gaps[0]
+    srv, reqs = _served_stream(specs, arrivals, hbm_gb, max_active)
+    torch.cuda.synchronize()
+    service, plain = [], []
+    for i, (m, p) in enumerate(specs):
+        job = ErosionJob(m, p, name=str(i))
+        t0 = time.time()
+        plain += run_plain([job])
+        service.append(time.time() - t0)
+    t_plain = float(sum(service))
+    done, lat = 0.0, []
+    for a, sv in zip(arrivals, service):
+        done = max(float(a), done) + sv
+        lat.append(done - float(a))
+    lat = np.array(lat)
+    upd_plain = sum(r.band_updates for r in plain)
+    served_res = {r.rid: r.result for r in reqs}
+    dfrac, dhist, same = 0.0, 0.0, 0
+    for i, rp in enumerate(plain):
+        rs = served_res[i]
+        dfrac = max(dfrac, abs(rs.fraction - rp.fraction))
+        fs, fp = [h.fraction for h in rs.history], [h.fraction for h in rp.history]
+        if len(fs) == len(fp):
+            dhist = max([dhist] + [abs(x - y) for x, y in zip(fs, fp)])
+        else:
+            dhist = float("inf")
+        same += fs == fp and rs.stop_reason == rp.stop_reason
+    pl = {"solves_per_s": round(len(plain) / t_plain, 3), "band_updates_per_s": round(upd_plain / t_plain, 1),
+          "wall_s": round(t_plain, 2),
+          "latency_s_fifo_at_stream_arrivals": {q: round(float(np.percentile(lat, v)), 4)
+                                                for q, v in (("p50", 50), ("p95", 95), ("p99", 99))}}
+    return {"requests": len(specs),
+            "mix": "served configuration: sub 4-8 (40/30/15/10/5), res lognormal median 160 in [64,400], target "
+                   f"U[0.85,0.95], 0-2 snapshots, laws 50/25/15/10, curvature laws capped at {max_steps} steps",
+            "capacity": {k: cap[k] for k in ("solves_per_s", "band_updates_per_s", "wall_s")},
+            "stream": {"rate_per_s": round(rate, 3), "load": load, **srv},
+            "plain": pl,
+            "ratio_capacity_vs_plain": {"solves_per_s": round(cap["solves_per_s"] / pl["solves_per_s"], 3),
+                                        "band_updates_per_s": round(cap["band_updates_per_s"]
+                                                                    / max(pl["band_updates_per_s"], 1e-9), 3)},
+            "deviation_vs_plain": {"max_abs_final_fraction": dfrac, "max_abs_history_fraction": dhist,
+                                   "identical_histories": int(same)},
+            "inputs_s": round(t_in, 2)}
+
+
+def run_served(args) -> dict:
+    """Open-loop Poisson stream through the continuous-batching server, against the plain path."""
+    out = served_vs_plain(args.requests, seed=args.seed, max_steps=args.max_steps, hbm_gb=args.hbm_gb,
+                          max_active=args.max_active, load=args.load)
+    return {"metric": METRIC, "value": out["stream"]["band_updates_per_s"], "unit": UNIT, "n_gpus": 1,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"served: {args.requests} Poisson requests at {args.rate}/s, sub 4-8 "
-                                   f"(40/30/15/10/5), res lognormal median 160 in [64,400], target U[0.85,0.95], "
-                                   f"0-2 snapshots, law mix 50/25/15/10, HBM budget {args.hbm_gb} GB"},
-            "served": stats}
+            "config": {"workload": f"served: {args.requests} Poisson requests at {args.load} x the measured "
+                                   f"capacity, HBM budget {args.hbm_gb} GB; " + out["mix"]},
+            "served": out}
 
 
 def workload(name: str, seed: int = 0):
@@ -374,6 +439,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         out["e2e"] = e2e_solve(args, mesh, params, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(ls, sim, grid, law)
+    if rank == 0 and world == 1 and args.served_requests > 0:
+        del sim, ls, phi
+        torch.cuda.empty_cache()
+        out["served"] = served_vs_plain(args.served_requests, seed=args.seed, max_steps=args.max_steps,
+                                        hbm_gb=args.hbm_gb, max_active=args.max_active, load=args.load)
     return out
 
 
@@ -433,56 +503,51 @@ def _host_cores() -> int:
         return os.cpu_count() or 1
 
 
-def _oracle_sample(phi_host, h, shape, law_kw, band_host=None, steps=1, warmup=0):
-    """Times the oracle's RK stage RHS and volume on all host cores (threaded oracle).
-
-    Returns (band nodes, [per-step seconds]); a step is timed as one RHS stage
-    and one volume, and counted as three stages plus the volume."""
+def _port_simulation(phi_host, h, law_kw, workers):
+    """The reference's step loop as the threaded oracle port (oracle/threaded_np.py): whole steps of
+    svierosion/evolve.py:182-250 on ``workers`` host threads."""
     import oracle as O
-    from oracle.threaded_np import ThreadedStage
+    from oracle.threaded_np import ThreadedSimulation
 
-    sim = O.Simulation.__new__(O.Simulation)
-    sim.phi = phi_host
-    sim.shape = tuple(shape)
-    sim.h, sim.width = float(h), 6.0
-    sim.law = O.make_law("svi", **law_kw)
-    sim.cfl, sim.feedback_cfl, sim.parabolic_cfl = 0.5, 1.0, 0.25
-    sim.reinit_distance, sim.reinit_iterations, sim.cutoff = 1.5, 20, (4.0, 5.5)
-    sim.st = O.strides_of(sim.shape)
-    sim.band = O.rebuild_band(sim.flat, 6.0, sim.h) if band_host is None else band_host
-    sim.khat, sim.m = O.kernel_hat(sim.shape, sim.law.radius, sim.h)
-    ts = ThreadedStage(sim, _host_cores())
-    times = []
+    law = O.make_law("svi", **law_kw)
+    return ThreadedSimulation(np.ascontiguousarray(phi_host, dtype=np.float32), float(h), law, workers=workers)
+
+
+def _port_steps(sim, steps: int, budget_s: float | None = None):
+    """Run up to `steps` whole steps; with a budget, stop after the step that crosses it.
+    Returns (steps run, band-cell updates, seconds, reinitialisations)."""
+    u0, n0, r0 = sim.band_updates, sim.steps, sum(r.reinit for r in sim.history)
+    t0 = time.time()
+    while sim.steps - n0 < steps:
+        sim.run(target_fraction=None, max_steps=1)
+        if budget_s is not None and time.time() - t0 >= budget_s:
+            break
+    dt = time.time() - t0
+    return sim.steps - n0, sim.band_updates - u0, dt, sum(r.reinit for r in sim.history) - r0
+
+
+def cpu_baseline(ls, sim, grid, law, budget_s: float = 25.0) -> dict:
+    """Whole steps of the reference algorithm (the oracle port on all host cores) from the level set
+    the GPU run reached, for about `budget_s` seconds after one untimed warm-up step."""
+    cores = _host_cores()
+    port = _port_simulation(ls.phi.cpu().numpy(), grid.spacing,
+                            dict(radius=law.radius, k=law.k, s=law.s, t=law.t), cores)
     try:
-        for i in range(warmup + steps):
-            t0 = time.time()
-            ts.rhs()
-            t_stage = time.time() - t0
-            t0 = time.time()
-            ts.volume()
-            t_vol = time.time() - t0
-            if i >= warmup:
-                times.append((t_stage, t_vol))
+        _port_steps(port, 1)
+        n, upd, secs, reinits = _port_steps(port, 10 ** 6, budget_s)
     finally:
-        ts.close()
-    return sim.band.size, times
-
-
-def cpu_baseline(ls, sim, grid, law) -> dict:
-    phi = ls.phi.cpu().numpy().copy()
-    B, times = _oracle_sample(phi, grid.spacing, grid.shape, dict(radius=law.radius, k=law.k, s=law.s, t=law.t),
-                              steps=2, warmup=1)
-    t_stage = float(np.mean([t[0] for t in times]))
-    t_vol = float(np.mean([t[1] for t in times]))
-    step = 3 * t_stage + t_vol
-    return {"value": round(B / step, 1), "unit": UNIT, "cores": _host_cores(), "kind": "port",
-            "sample": f"numpy oracle on {_host_cores()} threads (band chunks, multi-threaded pocketfft): one RK "
-                      f"stage RHS ({t_stage:.2f}s) + one volume ({t_vol:.2f}s) of the same level set ({B} band "
-                      f"nodes), mean of 2 after 1 warm-up; step = 3 stages + volume"}
+        port.close()
+    return {"value": round(upd / secs, 1), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"numpy oracle port of the reference's step loop on {cores} threads: {n} whole steps "
+                      f"(3 RHS stages, RK combinations, volume, {reinits} reinitialisations at the reference's "
+                      f"trigger) in {secs:.1f} s from the GPU run's level set, after 1 untimed step"}
 
 
 # --------------------------------------------------------- reference arm
 def run_reference(args, rank: int, world: int, local_rank: int) -> dict | None:
+    """The reference algorithm's CPU implementation (the oracle port of svierosion/evolve.py:182-250
+    on all host cores) timed on whole steps of the same workload: W untimed warm-up steps, then K
+    timed steps, or fewer when K would not end within the time budget (``steps`` says how many ran)."""
     if rank != 0:
         return None
     import torch
@@ -491,24 +556,36 @@ def run_reference(args, rank: int, world: int, local_rank: int) -> dict | None:
     mesh, params, desc = workload(args.workload, seed=args.seed)
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
+    t_setup = time.time()
     grid = S.make_grid(mesh, params)
-    # input preparation only: the level set's initial SDF comes from the GPU SDF
+    # input preparation only (untimed): the initial SDF comes from the GPU SDF, which equals the
+    # reference's mesh_to_sdf on these inputs (tests/test_gpu_configs.py)
     phi = S.mesh_to_sdf(mesh, grid, band=params.band, device=dev).cpu().numpy()
     law = params.make_law(length_scale=float((mesh.bounds[1] - mesh.bounds[0]).max()))
-    import oracle as O
-    band = O.rebuild_band(phi.reshape(-1), params.band, grid.spacing)
-    kw = dict(radius=law.radius, k=law.k, s=law.s, t=law.t)
-    B, times = _oracle_sample(phi, grid.spacing, grid.shape, kw, band, steps=args.steps, warmup=args.warmup)
-    step = float(np.mean([3 * ts + tv for ts, tv in times]))
-    value = B / step
     cores = _host_cores()
+    port = _port_simulation(phi, grid.spacing, dict(radius=law.radius, k=law.k, s=law.s, t=law.t), cores)
+    band0 = int(port.band.size)
+    t_setup = time.time() - t_setup
+    try:
+        _, _, warm_s, _ = _port_steps(port, args.warmup, args.ref_budget / 3)
+        per_step = warm_s / max(args.warmup, 1)
+        k = max(1, min(args.steps, int(args.ref_budget / max(per_step, 1e-3))))
+        n, upd, secs, reinits = _port_steps(port, k)
+    finally:
+        port.close()
+    value = upd / secs
+    sample = (f"numpy oracle port of the reference's step loop (svierosion/evolve.py:182-250) on {cores} host "
+              f"threads: {n} whole timed steps ({reinits} with reinitialisation) after {args.warmup} warm-up "
+              f"steps; {k} of the {args.steps} requested steps fit the {args.ref_budget:.0f} s budget")
     return {"impl": "reference", "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * step, 1),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": desc, "grid": list(grid.shape), "band_nodes": int(B)},
+            "steps": n, "steps_requested": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1000 * secs / n, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "grid": list(grid.shape), "grid_nodes": grid.size, "band_nodes": band0,
+                       "band_nodes_mean_timed": int(upd / n), "parallelism": f"host threads x{cores}",
+                       "l2": "host memory (CPU)", "setup_s": round(t_setup, 3)},
             "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"numpy restatement of the reference path on {cores} threads; per step one "
-                                       "RK stage RHS + one volume timed, step = 3 stages + volume"},
+                             "sample": sample},
             "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -521,13 +598,18 @@ def main() -> int:
     ap.add_argument("--workload", choices=["scan", "precision", "cube64", "batched", "served"], default="scan")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--requests", type=int, default=200)
-    ap.add_argument("--rate", type=float, default=4.0)
+    ap.add_argument("--load", type=float, default=0.8, help="served stream rate as a fraction of the capacity")
+    ap.add_argument("--served-requests", type=int, default=200,
+                    help="requests of the served-vs-plain comparison in the default line (0: none)")
     ap.add_argument("--hbm-gb", type=float, default=150.0)
     ap.add_argument("--max-active", type=int, default=64)
     ap.add_argument("--max-steps", type=int, default=400)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-budget", type=float, default=120.0,
+                    help="seconds of timed whole steps the reference arm may take (it runs fewer than --steps "
+                         "steps when they would not fit)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -654,6 +654,7 @@ class Simulation:
             self.khat, self.m = kernel_hat(self.shape, law.radius, self.h)
         self.initial_volume = self.volume()
         self.time, self.steps, self.history, self._displacement = 0.0, 0, [], 0.0
+        self.band_updates = 0   # band nodes x accepted steps (the benchmark's work unit)
 
     @property
     def flat(self):
@@ -711,6 +712,10 @@ class Simulation:
             info["vmean"] = float(V[near].astype(np.float64).mean()) if near.any() else float(V.mean())
         V = V * self._cutoff_factor(phi_b)
         return V.astype(F32), info
+
+    def _reinitialize(self):
+        """levelset.py:154-183 on this level set; returns the rebuilt band."""
+        return reinitialize(self.phi, self.band, self.h, self.reinit_iterations, width=self.width)
 
     def _rhs(self, stats=False):
         V, info = self._velocity(stats)
@@ -784,11 +789,12 @@ class Simulation:
             vmax = float(Vb.max())
             self.time += dt
             self.steps += 1
+            self.band_updates += idx.size
             self._displacement += dt * vmax
             did_reinit = False
             reached = target is not None and vnew <= target * (1 + tol)
             if self._displacement >= self.reinit_distance * self.h and not reached:
-                self.band = reinitialize(self.phi, self.band, self.h, self.reinit_iterations, width=self.width)
+                self.band = self._reinitialize()
                 self._displacement = 0.0
                 did_reinit = True
                 vnew = self.volume()

@@ -1,4 +1,4 @@
-"""Multi-threaded evaluation of the oracle's RK stage and volume (test infrastructure only).
+"""Multi-threaded evaluation of the oracle's steps (test infrastructure only).
 
 The CPU baseline of the benchmark times the reference algorithm on all host
 cores, as the reference itself runs on the CPU (torch with one intra-op
@@ -8,7 +8,12 @@ thread per core).  This module evaluates the same arithmetic as
 split into contiguous chunks on a thread pool (numpy releases the GIL inside
 its gather and ufunc loops) and the FFTs of svierosion/svi.py:84-93 on
 scipy's multi-threaded pocketfft.  ``tests/test_oracle_golden.py`` checks it
-against the serial oracle.
+against the serial oracle.  ``ThreadedSimulation`` runs the reference's whole
+step loop (svierosion/evolve.py:182-250: three stages, the RK combinations,
+the volume, regula falsi and the reinitialisation of levelset.py:154-183 at the
+reference's trigger) with these threaded pieces; every piece is elementwise
+over the band or the work set, so its results equal the serial oracle's bit
+for bit.
 """
 
 from __future__ import annotations
@@ -19,8 +24,8 @@ from concurrent.futures import ThreadPoolExecutor
 import numpy as np
 import scipy.fft
 
-from .reference_np import (F32, Simulation, cell_fractions, closest_points, godunov_inward, strides_of,
-                           tricubic)
+from .reference_np import (F32, MARGIN, Simulation, cell_fractions, check_margin, closest_points, dilate,
+                           godunov_inward, reinit_geometry, reinit_rhs, strides_of, tricubic)
 
 
 def _spans(n: int, parts: int):
@@ -130,3 +135,98 @@ class ThreadedStage:
         band_inside = sum(p[0] for p in parts)
         fsum = sum(p[1] for p in parts)
         return (inside - band_inside + fsum) * sim.h ** 3
+
+
+def threaded_reinitialize(pool, workers: int, phi3, band, h, iterations=12, cfl=0.45, dilation=3, width=6.0):
+    """reference_np.reinitialize (levelset.py:154-183) with the geometry, the pseudo-time sweeps and the
+    band rebuild split over ``pool``; returns the rebuilt band.  Each sweep evaluates the right-hand
+    side of every work node from the same field before any node is written, as the serial form does."""
+    shape = phi3.shape
+    mask = np.zeros(shape, dtype=bool)
+    mask.reshape(-1)[band] = True
+    mask = dilate(mask, dilation)
+    for ax in range(3):
+        sl = [slice(None)] * 3
+        sl[ax] = slice(0, MARGIN)
+        mask[tuple(sl)] = False
+        sl[ax] = slice(shape[ax] - MARGIN, shape[ax])
+        mask[tuple(sl)] = False
+    idx = np.nonzero(mask.reshape(-1))[0].astype(np.int64)
+    f = phi3.reshape(-1)
+    st = strides_of(shape)
+    spans = _spans(idx.size, 4 * workers)
+
+    def each(fn):
+        """fn(k, a, b) for every span k = [a, b) of the work list, on the pool."""
+        list(pool.map(lambda k: fn(k, *spans[k]), range(len(spans))))
+
+    geo = [None] * len(spans)
+
+    def geometry(k, a, b):
+        geo[k] = reinit_geometry(f, idx[a:b], *st, h, cfl)
+
+    each(geometry)
+    r = np.empty(idx.size, dtype=F32)
+    u0 = np.empty(idx.size, dtype=F32)
+    u1 = np.empty(idx.size, dtype=F32)
+
+    def keep_u0(k, a, b):
+        u0[a:b] = f[idx[a:b]]
+
+    def keep_u1(k, a, b):
+        u1[a:b] = f[idx[a:b]]
+
+    def rhs(k, a, b):
+        g = geo[k]
+        r[a:b] = reinit_rhs(f, idx[a:b], *st, h, g[0], *g[2:])
+
+    def first_half(k, a, b):
+        f[idx[a:b]] = u0[a:b] + geo[k][1] * r[a:b]
+
+    def second_half(k, a, b):
+        f[idx[a:b]] = 0.5 * (u0[a:b] + u1[a:b] + geo[k][1] * r[a:b])
+
+    # TVD-RK2 in pseudo time: every right-hand side of a half-step is evaluated before any node is written
+    for _ in range(iterations):
+        each(keep_u0)
+        each(rhs)
+        each(first_half)
+        each(keep_u1)
+        each(rhs)
+        each(second_half)
+    # levelset.py:70-77: clamp, then list |phi| < cap (1 - 1e-5), chunk by chunk of the grid
+    cap = width * h
+    gspans = _spans(f.size, workers)
+
+    def rebuild(a, b):
+        np.clip(f[a:b], F32(-cap), F32(cap), out=f[a:b])
+        return np.nonzero(np.abs(f[a:b]) < F32(cap * (1 - 1e-5)))[0].astype(np.int64) + a
+
+    out = np.concatenate(list(pool.map(lambda ab: rebuild(*ab), gspans)))
+    check_margin(out, shape)
+    return out
+
+
+class ThreadedSimulation(Simulation):
+    """reference_np.Simulation (evolve.py:67-250) whose stages, volume and reinitialisation run on
+    ``workers`` threads (SVI laws)."""
+
+    def __init__(self, phi3, h, law, workers: int, **kw):
+        super().__init__(phi3, h, law, **kw)
+        self.workers = int(workers)
+        self.stage = ThreadedStage(self, self.workers)
+
+    def close(self) -> None:
+        self.stage.close()
+
+    def _rhs(self, stats=False):
+        return self.stage.rhs()
+
+    def volume(self):
+        if not hasattr(self, "stage"):   # the initial volume, taken in Simulation.__init__
+            return super().volume()
+        return self.stage.volume()
+
+    def _reinitialize(self):
+        return threaded_reinitialize(self.stage.pool, self.workers, self.phi, self.band, self.h,
+                                     self.reinit_iterations, width=self.width)

@@ -23,10 +23,84 @@ import numpy as np
 OUT = Path(__file__).resolve().parent
 
 
-def main(ref_root: str) -> None:
+def history_arrays(hist) -> dict:
+    keys = ["step", "time", "dt", "volume", "fraction", "vmax", "vmean", "qmin", "qmax", "capped", "reinit"]
+    return {"hist_" + k: np.array([getattr(r, k) for r in hist], dtype=np.float64) for k in keys}
+
+
+def run_case(name, mesh, params, phi_store=True) -> None:
+    """One full run of the reference's ErosionSimulation.run, stored as run_<name>.npz."""
+    from svierosion.api import make_grid
+    from svierosion.evolve import ErosionSimulation
+    from svierosion.levelset import LevelSet
+    from svierosion.sdf import mesh_to_sdf
+
+    grid = make_grid(mesh, params)
+    lo, hi = mesh.bounds
+    law = params.make_law(length_scale=float((hi - lo).max()))
+    phi = mesh_to_sdf(mesh, grid, band=params.band, device="cpu")
+    phi_init = phi.clone()
+    ls = LevelSet(phi, grid, width=params.band)
+    band_init = ls.band.clone()
+    sim = ErosionSimulation(ls, law, cfl=params.cfl, feedback_cfl=params.feedback_cfl,
+                            parabolic_cfl=params.parabolic_cfl, reinit_distance=params.reinit_distance,
+                            reinit_iterations=params.reinit_iterations)
+    res = sim.run(target_fraction=params.target_fraction, max_steps=params.max_steps)
+    fb = ls.flat[ls.band].numpy()
+    rng = np.random.default_rng(0)
+    probe = np.sort(rng.choice(ls.band.numel(), size=min(4000, ls.band.numel()), replace=False))
+    extra = {"phi_init": phi_init.numpy()} if phi_store else {}
+    np.savez_compressed(
+        OUT / f"run_{name}.npz", vertices=mesh.vertices, faces=mesh.faces, origin=np.array(grid.origin),
+        shape=np.array(grid.shape), h=grid.spacing, band_init=band_init.numpy(),
+        initial_volume=sim.initial_volume, stop_reason=res.stop_reason, steps=res.steps, time=res.time,
+        fraction=res.fraction, band_final_count=ls.band.numel(),
+        band_final_head=ls.band[:2000].numpy(), band_final_tail=ls.band[-2000:].numpy(),
+        phi_band_sum=float(fb.astype(np.float64).sum()), phi_band_abs_sum=float(np.abs(fb).astype(np.float64).sum()),
+        probe_idx=ls.band[probe].numpy(), probe_phi=ls.flat[ls.band[probe]].numpy(),
+        params=np.array([params.radius or 0.0, params.k, params.s, params.t or 0.0, params.alpha,
+                         params.resolution, params.target_fraction]),
+        law=params.law, max_steps=params.max_steps, **extra, **history_arrays(sim.history))
+    print(name, grid.shape, res.stop_reason, res.steps, res.fraction)
+
+
+def full_runs(only=None) -> None:
+    """The full-run fixtures: cube-64 svi k1 s1, cube-32 svi k0 s0, and cube-32 mean and Gauss curvature."""
+    from svierosion import shapes
+    from svierosion.api import ErosionParams
+
+    cube = shapes.cube(1.0)
+    cases = {
+        "cube64": ErosionParams(law="svi", radius=0.1, k=1, s=1, t=0.93, resolution=64, target_fraction=0.9,
+                                device="cpu"),
+        "cube32_k0s0": ErosionParams(law="svi", radius=0.15, k=0, s=0, resolution=32, target_fraction=0.95,
+                                     device="cpu"),
+        "cube32_mean": ErosionParams(law="mean", alpha=1.0, resolution=32, target_fraction=0.97, device="cpu",
+                                     max_steps=40),
+        # GaussCurvatureLaw (flows.py:186-213) with the automatic delta = L^-2 (api.py:62-64)
+        "cube32_gauss": ErosionParams(law="gauss", alpha=0.25, resolution=32, target_fraction=0.97,
+                                      device="cpu", max_steps=40),
+    }
+    for name, params in cases.items():
+        if only is None or name in only:
+            run_case(name, cube, params)
+
+
+def setup_reference(ref_root: str) -> None:
     os.environ.setdefault("SVIEROSION_COMPILE", "0")
     sys.dont_write_bytecode = True
     sys.path.insert(0, ref_root)
+    import torch
+    from svierosion import kernels as K
+    torch.set_num_threads(os.cpu_count() or 1)
+    K.set_compile(False)
+
+
+def main(ref_root: str, only=None) -> None:
+    setup_reference(ref_root)
+    if only is not None:      # just the named full runs
+        full_runs(only)
+        return
     import torch
     from svierosion import kernels as K, shapes
     from svierosion.evolve import ErosionSimulation
@@ -37,8 +111,6 @@ def main(ref_root: str) -> None:
     from svierosion.svi import BallConvolution, ball_cell_weights
     from svierosion.api import ErosionParams, make_grid
 
-    torch.set_num_threads(os.cpu_count() or 1)
-    K.set_compile(False)
     ctr = np.array([0.0123, -0.0311, 0.0217])
 
     def sphere_phi(R, h, pad, distort):
@@ -120,49 +192,10 @@ def main(ref_root: str) -> None:
                         torus_v=t.vertices, torus_f=t.faces, torus_origin=np.array(gt.origin),
                         torus_shape=np.array(gt.shape), torus_h=gt.spacing, torus_phi=phi_t.numpy())
 
-    # ---- 6. full runs (the reference's ErosionSimulation.run)
-    def history_arrays(hist):
-        keys = ["step", "time", "dt", "volume", "fraction", "vmax", "vmean", "qmin", "qmax", "capped", "reinit"]
-        return {"hist_" + k: np.array([getattr(r, k) for r in hist], dtype=np.float64) for k in keys}
-
-    def run_case(name, mesh, params, phi_store=True):
-        grid = make_grid(mesh, params)
-        lo, hi = mesh.bounds
-        law = params.make_law(length_scale=float((hi - lo).max()))
-        phi = mesh_to_sdf(mesh, grid, band=params.band, device="cpu")
-        phi_init = phi.clone()
-        ls = LevelSet(phi, grid, width=params.band)
-        band_init = ls.band.clone()
-        sim = ErosionSimulation(ls, law, cfl=params.cfl, feedback_cfl=params.feedback_cfl,
-                                parabolic_cfl=params.parabolic_cfl, reinit_distance=params.reinit_distance,
-                                reinit_iterations=params.reinit_iterations)
-        res = sim.run(target_fraction=params.target_fraction, max_steps=params.max_steps)
-        fb = ls.flat[ls.band].numpy()
-        rng = np.random.default_rng(0)
-        probe = np.sort(rng.choice(ls.band.numel(), size=min(4000, ls.band.numel()), replace=False))
-        extra = {"phi_init": phi_init.numpy()} if phi_store else {}
-        np.savez_compressed(
-            OUT / f"run_{name}.npz", vertices=mesh.vertices, faces=mesh.faces, origin=np.array(grid.origin),
-            shape=np.array(grid.shape), h=grid.spacing, band_init=band_init.numpy(),
-            initial_volume=sim.initial_volume, stop_reason=res.stop_reason, steps=res.steps, time=res.time,
-            fraction=res.fraction, band_final_count=ls.band.numel(),
-            band_final_head=ls.band[:2000].numpy(), band_final_tail=ls.band[-2000:].numpy(),
-            phi_band_sum=float(fb.astype(np.float64).sum()), phi_band_abs_sum=float(np.abs(fb).astype(np.float64).sum()),
-            probe_idx=ls.band[probe].numpy(), probe_phi=ls.flat[ls.band[probe]].numpy(),
-            params=np.array([params.radius or 0.0, params.k, params.s, params.t or 0.0, params.alpha,
-                             params.resolution, params.target_fraction]),
-            law=params.law, **extra, **history_arrays(sim.history))
-        print(name, grid.shape, res.stop_reason, res.steps, res.fraction)
-
-    cube = shapes.cube(1.0)
-    run_case("cube64", cube, ErosionParams(law="svi", radius=0.1, k=1, s=1, t=0.93, resolution=64,
-                                           target_fraction=0.9, device="cpu"))
-    run_case("cube32_k0s0", cube, ErosionParams(law="svi", radius=0.15, k=0, s=0, resolution=32,
-                                                target_fraction=0.95, device="cpu"))
-    run_case("cube32_mean", cube, ErosionParams(law="mean", alpha=1.0, resolution=32,
-                                                target_fraction=0.97, device="cpu", max_steps=40))
+    full_runs()
     print("fixtures written to", OUT)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # make_golden.py [reference root] [run name ...]: with names, only those full runs are redone
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", sys.argv[2:] or None)

@@ -68,11 +68,11 @@ def _run(golden, name):
     law = params.make_law(length_scale=float((hi - lo).max()))
     sim = S.ErosionSimulation(ls, law)
     assert abs(sim.initial_volume - float(d["initial_volume"])) < 1e-9
-    res = sim.run(float(P[6]))
+    res = sim.run(float(P[6]), max_steps=int(d.get("max_steps", 100000)))
     return d, res, ls
 
 
-@pytest.mark.parametrize("name", ["cube64", "cube32_k0s0", "cube32_mean"])
+@pytest.mark.parametrize("name", ["cube64", "cube32_k0s0", "cube32_mean", "cube32_gauss"])
 def test_full_run_matches_reference(golden, name):
     d, res, ls = _run(golden, name)
     assert res.stop_reason == str(d["stop_reason"])

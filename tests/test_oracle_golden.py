@@ -84,7 +84,7 @@ def test_sdf_cube_and_torus(golden):
     _close(pt, sd["torus_phi"], 1e-6)
 
 
-@pytest.mark.parametrize("name", ["cube32_k0s0", "cube32_mean"])
+@pytest.mark.parametrize("name", ["cube32_k0s0", "cube32_mean", "cube32_gauss"])
 def test_full_run_small(golden, name):
     d = golden(f"run_{name}")
     P = d["params"]
@@ -94,7 +94,7 @@ def test_full_run_small(golden, name):
                      length_scale=float((hi - lo).max()))
     sim = O.Simulation(phi, float(d["h"]), law)
     assert np.array_equal(sim.band, d["band_init"])
-    reason, steps, _, frac = sim.run(float(P[6]))
+    reason, steps, _, frac = sim.run(float(P[6]), max_steps=int(d.get("max_steps", 100000)))
     assert reason == str(d["stop_reason"]) and steps == int(d["steps"])
     assert abs(frac - float(d["fraction"])) < 1e-6
     fr = np.array([r.fraction for r in sim.history])

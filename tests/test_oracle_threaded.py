@@ -31,3 +31,27 @@ def test_threaded_stage_matches_serial(workers):
         assert info1[k] == pytest.approx(info0[k], rel=1e-5)
     assert abs(info1["capped"] - info0["capped"]) <= 1
     assert vol1 == pytest.approx(sim.volume(), rel=1e-12)
+
+
+def test_threaded_simulation_matches_serial():
+    """Whole steps (three stages, RK combinations, volume, regula falsi at the target and
+    reinitialisation at the reference's trigger) on threads give the serial oracle's results."""
+    from oracle.threaded_np import ThreadedSimulation
+
+    base = _ellipsoid_sim()
+    phi0, law, h = base.phi.copy(), base.law, base.h
+    # a short trigger distance, so that the steps include reinitialisations
+    serial = O.Simulation(phi0, h, law, reinit_distance=0.3)
+    out_s = serial.run(target_fraction=0.93, max_steps=12)
+    threaded = ThreadedSimulation(phi0, h, law, workers=3, reinit_distance=0.3)
+    try:
+        out_t = threaded.run(target_fraction=0.93, max_steps=12)
+    finally:
+        threaded.close()
+    assert out_t[0] == out_s[0] and out_t[1] == out_s[1]
+    assert any(r.reinit for r in serial.history)
+    np.testing.assert_allclose([r.fraction for r in threaded.history], [r.fraction for r in serial.history],
+                               atol=1e-6)
+    assert [r.reinit for r in threaded.history] == [r.reinit for r in serial.history]
+    assert np.array_equal(threaded.band, serial.band)
+    np.testing.assert_allclose(threaded.flat[serial.band], serial.flat[serial.band], atol=1e-5 * serial.h)
