@@ -379,45 +379,50 @@ SVIE_DEV void tricubic_grad_at(const float* __restrict__ g, int ny, int nz, floa
 
 // Squared point-triangle distance with Ericson's region classification in the
 // priority order of the reference (kernels.py:382-427).
+// Every operation of the point-triangle distance is rounded on its own, in
+// the reference's order (products first, then left-to-right sums, as its
+// float32 tensor arithmetic evaluates them): no multiply-add is fused, so the
+// distances, and the nearest-triangle ties they decide, are bit-identical.
+SVIE_DEV float rmul(float x, float y) { return __fmul_rn(x, y); }
+SVIE_DEV float radd(float x, float y) { return __fadd_rn(x, y); }
+SVIE_DEV float rsub(float x, float y) { return __fsub_rn(x, y); }
+SVIE_DEV float rdot3(float3 u, float3 v) { return radd(radd(rmul(u.x, v.x), rmul(u.y, v.y)), rmul(u.z, v.z)); }
+SVIE_DEV float3 rsub3(float3 u, float3 v) { return make_float3(rsub(u.x, v.x), rsub(u.y, v.y), rsub(u.z, v.z)); }
+
 SVIE_DEV float point_triangle_d2(float3 p, float3 a, float3 b, float3 c) {
-  float3 ab = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
-  float3 ac = make_float3(c.x - a.x, c.y - a.y, c.z - a.z);
-  float3 ap = make_float3(p.x - a.x, p.y - a.y, p.z - a.z);
-  float3 bp = make_float3(p.x - b.x, p.y - b.y, p.z - b.z);
-  float3 cp = make_float3(p.x - c.x, p.y - c.y, p.z - c.z);
-  float d1 = ab.x * ap.x + ab.y * ap.y + ab.z * ap.z;
-  float d2 = ac.x * ap.x + ac.y * ap.y + ac.z * ap.z;
-  float d3 = ab.x * bp.x + ab.y * bp.y + ab.z * bp.z;
-  float d4 = ac.x * bp.x + ac.y * bp.y + ac.z * bp.z;
-  float d5 = ab.x * cp.x + ab.y * cp.y + ab.z * cp.z;
-  float d6 = ac.x * cp.x + ac.y * cp.y + ac.z * cp.z;
-  float va = d3 * d6 - d5 * d4;
-  float vb = d5 * d2 - d1 * d6;
-  float vc = d1 * d4 - d3 * d2;
+  const float3 ab = rsub3(b, a), ac = rsub3(c, a);
+  const float3 ap = rsub3(p, a), bp = rsub3(p, b), cp = rsub3(p, c);
+  const float d1 = rdot3(ab, ap), d2 = rdot3(ac, ap);
+  const float d3 = rdot3(ab, bp), d4 = rdot3(ac, bp);
+  const float d5 = rdot3(ab, cp), d6 = rdot3(ac, cp);
+  const float va = rsub(rmul(d3, d6), rmul(d5, d4));
+  const float vb = rsub(rmul(d5, d2), rmul(d1, d6));
+  const float vc = rsub(rmul(d1, d4), rmul(d3, d2));
   const float tiny = 1e-30f;
-  float denom = va + vb + vc;
+  float denom = radd(radd(va, vb), vc);
   denom = fabsf(denom) > tiny ? denom : tiny;
   float v = vb / denom, w = vc / denom;
-  float e1 = d4 - d3, e2 = d5 - d6;
+  const float e1 = rsub(d4, d3), e2 = rsub(d5, d6);
   if (d1 <= 0.f && d2 <= 0.f) {                 // vertex a
     v = 0.f; w = 0.f;
   } else if (d3 >= 0.f && d4 <= d3) {           // vertex b
     v = 1.f; w = 0.f;
   } else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {  // edge ab
-    v = d1 / fmaxf(d1 - d3, tiny); w = 0.f;
+    v = d1 / fmaxf(rsub(d1, d3), tiny); w = 0.f;
   } else if (d6 >= 0.f && d5 <= d6) {           // vertex c
     v = 0.f; w = 1.f;
   } else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {  // edge ac
-    v = 0.f; w = d2 / fmaxf(d2 - d6, tiny);
+    v = 0.f; w = d2 / fmaxf(rsub(d2, d6), tiny);
   } else if (va <= 0.f && e1 >= 0.f && e2 >= 0.f) {  // edge bc
-    float wbc = e1 / fmaxf(e1 + e2, tiny);
-    v = 1.f - wbc; w = wbc;
+    const float wbc = e1 / fmaxf(radd(e1, e2), tiny);
+    v = rsub(1.f, wbc); w = wbc;
   }
-  float qx = a.x + v * ab.x + w * ac.x;
-  float qy = a.y + v * ab.y + w * ac.y;
-  float qz = a.z + v * ab.z + w * ac.z;
-  float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
-  return dx * dx + dy * dy + dz * dz;
+  // q = (a + v ab) + w ac, then |p - q|^2 as ((dx^2 + dy^2) + dz^2)
+  const float3 q = make_float3(radd(radd(a.x, rmul(v, ab.x)), rmul(w, ac.x)),
+                               radd(radd(a.y, rmul(v, ab.y)), rmul(w, ac.y)),
+                               radd(radd(a.z, rmul(v, ab.z)), rmul(w, ac.z)));
+  const float3 d = rsub3(p, q);
+  return rdot3(d, d);
 }
 
 SVIE_DEV float tricubic_at(const float* __restrict__ g, int ny, int nz, float3 p) {
