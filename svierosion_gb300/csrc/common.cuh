@@ -17,6 +17,9 @@
 
 #define SVIE_DEV __device__ __forceinline__
 
+// threads of the one-CTA kernels that sum per-CTA partials
+constexpr int SUM_THREADS = 256;
+
 namespace svie {
 
 // In-place exclusive scan of n ints on the stream; sums: ceil(n / 1024) ints
@@ -138,8 +141,61 @@ SVIE_DEV double warp_sum_compensated(float v) {
   return (double)hi + (double)lo;
 }
 
+// Double-float partial sums: a value hi + lo kept as two floats and added with
+// TwoSum, about 2^-46 relative, in FP32 arithmetic throughout.  Per-CTA
+// partials are stored in this form (8 bytes, the size of a double) and summed
+// across CTAs without the FP64 pipe, whose rate on GB300 is 1/64 of FP32.
+struct DF {
+  float hi, lo;
+};
+SVIE_DEV DF df_add(DF a, DF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  const float hi = s + e;
+  return DF{hi, e - (hi - s)};
+}
+SVIE_DEV DF warp_sum_df(DF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v = df_add(v, DF{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)});
+  return v;
+}
+SVIE_DEV double df_value(DF v) { return (double)v.hi + (double)v.lo; }
+
+// Sum of the n double-float partials p[0..n) by one CTA, in a fixed order
+// (strided per thread, then a warp tree, then warp 0 over the warps); the
+// result is valid in thread 0.  `scratch` holds blockDim.x / 32 entries.
+SVIE_DEV DF block_sum_partials_df(const float2* __restrict__ p, long long n, DF* scratch) {
+  DF v{0.0f, 0.0f};
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const float2 q = p[i];
+    v = df_add(v, DF{q.x, q.y});
+  }
+  v = warp_sum_df(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < nw ? scratch[lane] : DF{0.0f, 0.0f};
+    v = warp_sum_df(v);
+  }
+  return v;
+}
+
 // Block sum of one float per thread as a double (compensated warp sums, FP64
 // across the warps); the result is valid in thread 0.
+SVIE_DEV DF block_sum_df(float v, DF* scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  DF w = warp_sum_df(DF{v, 0.0f});
+  __syncthreads();
+  if (lane == 0) scratch[wid] = w;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 1; i < nw; ++i) w = df_add(w, scratch[i]);
+  return w;
+}
+
 SVIE_DEV double block_sum_compensated(float v, double* scratch) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const double w = warp_sum_compensated(v);

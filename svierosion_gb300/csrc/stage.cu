@@ -151,7 +151,7 @@ SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
   constexpr int NW = SG_THREADS / 32;
   __shared__ float shf[7][NW];
   __shared__ unsigned int shu[3][NW];
-  __shared__ double shd[2][NW];
+  __shared__ DF shd[2][NW];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   float f[7] = {a.vmax, a.qmin_n, a.qmax_n, a.qmin_a, a.qmax_a, a.dv_n, a.dv_a};
   unsigned int u[3] = {a.cap_n, a.cap_a, a.n_near};
@@ -165,7 +165,7 @@ SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) u[k] += __shfl_xor_sync(0xffffffffu, u[k], o);
   }
-  const double d0 = warp_sum_compensated(a.vs_n), d1 = warp_sum_compensated(a.vs_a);
+  const DF d0 = warp_sum_df(DF{a.vs_n, 0.0f}), d1 = warp_sum_df(DF{a.vs_a, 0.0f});
   if (lane == 0) {
 #pragma unroll
     for (int k = 0; k < 7; ++k) shf[k][wid] = f[k];
@@ -203,13 +203,15 @@ SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
   if (u[0]) atomicAdd(&st->capped_near, u[0]);
   if (u[1]) atomicAdd(&st->capped_all, u[1]);
   if (u[2]) atomicAdd(&st->n_near, u[2]);
-  double r0 = 0.0, r1 = 0.0;
-  for (int i = 0; i < NW; ++i) {
-    r0 += shd[0][i];
-    r1 += shd[1][i];
+  DF r0 = shd[0][0], r1 = shd[1][0];
+  for (int i = 1; i < NW; ++i) {
+    r0 = df_add(r0, shd[0][i]);
+    r1 = df_add(r1, shd[1][i]);
   }
-  partial[2 * blockIdx.x] = r0;
-  partial[2 * blockIdx.x + 1] = r1;
+  // double-float partials, two per CTA (near, all), in the 16 bytes of two doubles
+  float2* pp = reinterpret_cast<float2*>(partial);
+  pp[2 * blockIdx.x] = make_float2(r0.hi, r0.lo);
+  pp[2 * blockIdx.x + 1] = make_float2(r1.hi, r1.lo);
 }
 
 __global__ void __launch_bounds__(SG_THREADS, 6) k_stage_svi(const float* __restrict__ phi,
@@ -305,19 +307,30 @@ __global__ void k_stats_reset(svie_stats* st, double dt_cap) {
 }
 
 // stable_dt (evolve.py:162-170) plus the float64 sums of V.
-__global__ void __launch_bounds__(1024) k_stats_finalize(svie_stats* st, svie_law L, const double* partial,
-                                                         long long nb, long long m) {
-  __shared__ double sh[32];
-  double a = 0.0, b = 0.0;
+__global__ void __launch_bounds__(SUM_THREADS) k_stats_finalize(svie_stats* st, svie_law L, const double* partial,
+                                                                long long nb, long long m) {
+  __shared__ DF sh[SUM_THREADS / 32];
+  // the (near, all) double-float partials interleaved per CTA: sum each stream in a fixed order
+  const float2* pp = reinterpret_cast<const float2*>(partial);
+  DF a{0.0f, 0.0f}, b{0.0f, 0.0f};
   for (long long i = threadIdx.x; i < nb; i += blockDim.x) {
-    a += partial[2 * i];
-    b += partial[2 * i + 1];
+    const float2 x = pp[2 * i], y = pp[2 * i + 1];
+    a = df_add(a, DF{x.x, x.y});
+    b = df_add(b, DF{y.x, y.y});
   }
-  a = block_reduce(a, sh, OpSumD(), 0.0);
-  b = block_reduce(b, sh, OpSumD(), 0.0);
+  a = warp_sum_df(a);
+  b = warp_sum_df(b);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = a;
+  __syncthreads();
+  if (wid == 0) a = warp_sum_df(lane < SUM_THREADS / 32 ? sh[lane] : DF{0.0f, 0.0f});
+  __syncthreads();
+  if (lane == 0) sh[wid] = b;
+  __syncthreads();
+  if (wid == 0) b = warp_sum_df(lane < SUM_THREADS / 32 ? sh[lane] : DF{0.0f, 0.0f});
   if (threadIdx.x != 0) return;
-  st->vsum_near = a;
-  st->vsum_all = b;
+  st->vsum_near = df_value(a);
+  st->vsum_all = df_value(b);
   const bool any_near = st->n_near > 0;
   const double vmax = m > 0 ? (double)__uint_as_float(st->vmax) : 0.0;
   const double h = L.h;
@@ -439,7 +452,7 @@ int svie_stats_finalize(svie_stats* stats, const svie_law* law, const void* ws, 
     return SVIE_ERR_WORKSPACE;
   }
   const long long nb = (m + SG_THREADS - 1) / SG_THREADS;
-  k_stats_finalize<<<1, 1024, 0, (cudaStream_t)stream>>>(stats, *law, (const double*)ws, nb, m);
+  k_stats_finalize<<<1, SUM_THREADS, 0, (cudaStream_t)stream>>>(stats, *law, (const double*)ws, nb, m);
   return launch_status("svie_stats_finalize");
 }
 

@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(ST_THREADS) k_volume_partial(const float* __re
                                                                long long sx, long long sy, long long sz,
                                                                float* __restrict__ occ, double* partial,
                                                                svie_stats* stats) {
-  __shared__ double shd[ST_THREADS / 32];
+  __shared__ DF shd[ST_THREADS / 32];
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   float v = 0.0f;
   int neg = 0, pos = 0;
@@ -118,22 +118,21 @@ __global__ void __launch_bounds__(ST_THREADS) k_volume_partial(const float* __re
     neg = c < 0.0f;
     pos = c > 0.0f;
   }
-  const double s = block_sum_compensated(v, shd);
+  const DF s = block_sum_df(v, shd);
   const int an = __syncthreads_or(neg), ap = __syncthreads_or(pos);
   if (threadIdx.x == 0) {
-    partial[blockIdx.x] = s;
+    reinterpret_cast<float2*>(partial)[blockIdx.x] = make_float2(s.hi, s.lo);
     if (an) atomicOr(&stats->any_neg, 1u);
     if (ap) atomicOr(&stats->any_pos, 1u);
   }
 }
 
-__global__ void __launch_bounds__(1024) k_sum_partials(const double* partial, long long nb, double* out) {
-  __shared__ double sh[32];
-  double v = 0.0;
-  // fixed assignment of partials to threads -> deterministic result
-  for (long long i = threadIdx.x; i < nb; i += blockDim.x) v += partial[i];
-  double s = block_reduce(v, sh, OpSumD(), 0.0);
-  if (threadIdx.x == 0) *out = s;
+// The per-CTA double-float partials (stored in the 8 bytes of a double each)
+// summed in a fixed order: deterministic run to run.
+__global__ void __launch_bounds__(SUM_THREADS) k_sum_partials(const double* partial, long long nb, double* out) {
+  __shared__ DF sh[SUM_THREADS / 32];
+  const DF s = block_sum_partials_df(reinterpret_cast<const float2*>(partial), nb, sh);
+  if (threadIdx.x == 0) *out = df_value(s);
 }
 
 __global__ void k_clear_flags(svie_stats* stats, unsigned int n_band) {
@@ -251,7 +250,7 @@ int svie_band_volume(const float* phi, const int32_t* band, int64_t m, int64_t s
   k_clear_flags<<<1, 1, 0, s>>>(stats, (unsigned)m);
   if (nb > 0)
     k_volume_partial<<<(unsigned)nb, ST_THREADS, 0, s>>>(phi, band, m, sx, sy, sz, occ, (double*)ws, stats);
-  k_sum_partials<<<1, 1024, 0, s>>>((const double*)ws, nb, &stats->fsum);
+  k_sum_partials<<<1, SUM_THREADS, 0, s>>>((const double*)ws, nb, &stats->fsum);
   return launch_status("svie_band_volume", nb > 0 ? 3 : 2);
 }
 
@@ -496,7 +495,7 @@ int svie_band_volume_noalloc(const float* phi, const int32_t* band, int64_t m, i
   // entries, so nothing left from an earlier call is read
   if (nb > 0)
     k_volume_partial<<<(unsigned)nb, ST_THREADS, 0, s>>>(phi, band, m, sx, sy, sz, occ, partials, stats);
-  k_sum_partials<<<1, 1024, 0, s>>>(partials, nb, &stats->fsum);
+  k_sum_partials<<<1, SUM_THREADS, 0, s>>>(partials, nb, &stats->fsum);
   return launch_status("svie_band_volume_noalloc", nb > 0 ? 3 : 2);
 }
 
