@@ -326,6 +326,72 @@ int svie_rk_stage(float* phi, const int32_t* band, int64_t m, const float* u0, c
                   const double* dt, int stage, void* stream);
 int svie_set_f64(double* dst, double value, void* stream);
 
+/* ------------------------------------------- many level sets in one launch */
+/* The per-step band work of svierosion/evolve.py:118-179 (stage right-hand
+ * sides, statistics and time step, RK combinations, occupancy refresh, the
+ * float64 volume of levelset.py:123-126) for a group of independent level
+ * sets -- the batched form of ErosionSimulation.run (evolve.py:182-250), which
+ * the reference runs one solid at a time.  Every member's band is cut into
+ * tiles of 256 entries, the CTAs of the one-level-set kernels, and each launch
+ * takes the packed (member, tile) list of all members: one launch per pass
+ * instead of one per member.  A member's arithmetic is the one-level-set
+ * kernels' own, so its results equal svie_stage_* / svie_rk_stage /
+ * svie_band_volume bit for bit.  Members keep their own arrays; time steps
+ * (stats->dt) are per member and never leave the device.  No time cap: a
+ * member's stats->dt_cap is +inf. */
+typedef struct svie_group_member {
+  float* phi;               /* the member's dense level set                  */
+  const int32_t* band;      /* its band (work order), m entries              */
+  int64_t m;
+  int32_t nx, ny, nz;
+  int32_t kind;             /* 0: SVI law, field = N; 1: curvature law,
+                               field = interleaved (k1, k2) (zero off band)  */
+  float* field;
+  float* occ;               /* the maintained occupancy                      */
+  float* u0;                /* phi at the band at the start of the step      */
+  float* L[3];              /* stage right-hand sides                        */
+  svie_stats* stats;        /* stage statistics and dt                       */
+  svie_stats* vstats;       /* volume statistics                             */
+  void* stage_ws;           /* >= svie_stage_workspace_bytes(m)              */
+  size_t stage_ws_bytes;
+  void* volume_ws;          /* >= svie_volume_workspace_bytes(m)             */
+  size_t volume_ws_bytes;
+  svie_law law;
+} svie_group_member;
+
+typedef struct svie_group {  /* a built group (filled by svie_group_build)  */
+  void* table;              /* device table of member records and tiles      */
+  int32_t n;                /* members                                       */
+  int32_t pad;
+  int64_t tiles;            /* tiles of all members                          */
+  int64_t tiles_svi;        /* of which the first tiles_svi are SVI members' */
+} svie_group;
+
+int64_t svie_group_tiles(const svie_group_member* members, int32_t n);
+size_t svie_group_table_bytes(int32_t n, int64_t tiles);
+/* Packs the table into host_staging (table_bytes, caller-owned; pinned memory
+ * for an asynchronous copy, which must stay untouched until the copy has run)
+ * and copies it to the device table on `stream`. */
+int svie_group_build(const svie_group_member* members, int32_t n, void* table, size_t table_bytes,
+                     void* host_staging, svie_group* out, void* stream);
+int svie_group_stats_reset(const svie_group* g, void* stream);
+/* occupancy refresh of the SVI members (svie_scatter_fractions) */
+int svie_group_scatter_fractions(const svie_group* g, void* stream);
+/* principal curvatures of the curvature members (svie_curvature_scatter) */
+int svie_group_curvature_scatter(const svie_group* g, void* stream);
+/* stage right-hand side into L[stage] (0..2); stage 0 also writes u0 and the
+ * statistics (svie_stage_svi / svie_stage_curvature) */
+int svie_group_stage(const svie_group* g, int stage, void* stream);
+/* every member's dt from its statistics (svie_stats_finalize) */
+int svie_group_stats_finalize(const svie_group* g, void* stream);
+/* RK combination `stage` (1..3; 0 restores u0) with L[stage - 1] and the
+ * member's own dt (svie_rk_stage) */
+int svie_group_rk(const svie_group* g, int stage, void* stream);
+/* float64 band volume, interface flags and occupancy (svie_band_volume) */
+int svie_group_volume(const svie_group* g, void* stream);
+/* copies member k's stats and vstats to dst[2k] and dst[2k + 1] */
+int svie_group_gather_stats(const svie_group* g, svie_stats* dst, void* stream);
+
 /* ------------------------------------------------- point-to-mesh distance */
 /* point_mesh_distance (svierosion/api.py:104-168), exact: the T pieces (T x 9
  * floats) are binned by centroid into a gx x gy x gz grid of cells of side cs

@@ -43,6 +43,20 @@ class Law(ctypes.Structure):
                 ("parabolic_cfl", c_double), ("h", c_double), ("cut_a", c_double), ("cut_b", c_double)]
 
 
+class GroupMember(ctypes.Structure):
+    """svie_group_member (include/svie.h)."""
+    _fields_ = [("phi", c_void_p), ("band", c_void_p), ("m", c_int64), ("nx", c_int32), ("ny", c_int32),
+                ("nz", c_int32), ("kind", c_int32), ("field", c_void_p), ("occ", c_void_p), ("u0", c_void_p),
+                ("L", c_void_p * 3), ("stats", c_void_p), ("vstats", c_void_p), ("stage_ws", c_void_p),
+                ("stage_ws_bytes", c_size_t), ("volume_ws", c_void_p), ("volume_ws_bytes", c_size_t),
+                ("law", Law)]
+
+
+class Group(ctypes.Structure):
+    """svie_group (include/svie.h)."""
+    _fields_ = [("table", c_void_p), ("n", c_int32), ("pad", c_int32), ("tiles", c_int64), ("tiles_svi", c_int64)]
+
+
 STATS_DTYPE = np.dtype([
     ("vsum_near", "<f8"), ("vsum_all", "<f8"), ("fsum", "<f8"), ("dt", "<f8"), ("dt_cap", "<f8"),
     ("reserved_d", "<f8", (3,)), ("vmax", "<u4"), ("qmin_near", "<u4"), ("qmax_near", "<u4"),
@@ -129,6 +143,17 @@ _SIGS = {
     "svie_stage_curvature": (I, [V, V, I64, I, I, I, V, POINTER(Law), V, V, V, V, V, Z, V]),
     "svie_stats_finalize": (I, [V, POINTER(Law), V, Z, I64, V]),
     "svie_rk_stage": (I, [V, V, I64, V, V, V, I, V]),
+    "svie_group_tiles": (I64, [POINTER(GroupMember), c_int32]),
+    "svie_group_table_bytes": (Z, [c_int32, I64]),
+    "svie_group_build": (I, [POINTER(GroupMember), c_int32, V, Z, V, POINTER(Group), V]),
+    "svie_group_stats_reset": (I, [POINTER(Group), V]),
+    "svie_group_scatter_fractions": (I, [POINTER(Group), V]),
+    "svie_group_curvature_scatter": (I, [POINTER(Group), V]),
+    "svie_group_stage": (I, [POINTER(Group), I, V]),
+    "svie_group_stats_finalize": (I, [POINTER(Group), V]),
+    "svie_group_rk": (I, [POINTER(Group), I, V]),
+    "svie_group_volume": (I, [POINTER(Group), V]),
+    "svie_group_gather_stats": (I, [POINTER(Group), V, V]),
     "svie_reinit_mask": (I, [V, I64, I, I, I, I, I, V, V, V]),
     "svie_reinit_geometry_bytes": (Z, [I64]),
     "svie_reinit_bits_bytes": (Z, [I, I, I]),

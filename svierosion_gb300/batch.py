@@ -1,19 +1,20 @@
 """Batched and served erosion: many independent solids on one GPU.
 
-Every solid (an :class:`ErosionJob`) owns its level set, simulation,
-workspaces and CUDA stream.  The scheduler keeps one TVD-RK3 step of
-every active job in flight on that job's stream and polls their completion
-events: a job whose step has finished is finished on the host (one 256-byte
-read back, plus the reference's rare extra work: regula falsi on the last
-step, reinitialisation) and relaunched at once, without waiting for the
-other jobs.  Kernels of different jobs overlap on the GPU, so
-small grids that cannot fill 152 SMs alone fill them together, and each job
-stops independently.  A job's arithmetic is exactly the plain path's, so its
-result is the same alone and in the mix.
+Every solid (an :class:`ErosionJob`) owns its level set, simulation and
+workspaces.  The scheduler opens the next step of every active job on the
+host (the stop tests; snapshot fractions and the next target when a run
+stops) and hands the due steps to :class:`GroupedStepper`: the curvature-law
+jobs advance in one group and the SVI-law jobs in another
+(:class:`~svierosion_gb300.group.GroupStep`), each a single launch per pass
+over the packed band tiles of all its members, on two streams that overlap.
+Each job's time step and stop test are its own; a job finishes its step on
+the host exactly as alone (regula falsi on the last step, reinitialisation),
+and its arithmetic is the plain path's, so its result is the same alone and
+in the mix.
 
 :class:`ErosionServer` runs an open-loop request stream on top: requests are
 admitted as slots and HBM (estimated footprint) free up, folded into the
-running batch at step boundaries, and their latency (arrival to result) is
+running groups at step boundaries, and their latency (arrival to result) is
 recorded.
 """
 
@@ -31,6 +32,7 @@ from . import _native as nat
 from .api import ErosionParams, make_grid
 from .evolve import ErosionSimulation
 from .grid import get_device
+from .group import GroupStep
 from .levelset import LevelSet, tricubic
 from .meshio import TriMesh
 from .sdf import mesh_to_sdf
@@ -118,16 +120,34 @@ class ErosionJob:
             return False
         with torch.cuda.stream(self.stream):
             while not self.sim.step_launch():
-                res = self.sim.end_run()
-                snap_phi = None
-                if self.keep_snapshot_phi:
-                    snap_phi = nat.d2h(self.ls.band_values())
-                self.snapshots.append((res.fraction, self.sim.time, snap_phi))
-                self.targets.pop(0)
-                if res.stop_reason != "target_volume" or not self.targets:
-                    self._complete(res)
+                if not self._next_target():
                     return False
-                self.sim.begin_run(self.targets[0], max_steps=self.params.max_steps)
+        return True
+
+    def begin_step(self) -> bool:
+        """Open the job's next step (stop tests; at a stop, the snapshot and the next target);
+        False once the job has finished.  The step itself is run by a :class:`GroupedStepper`."""
+        if self.done:
+            return False
+        with torch.cuda.stream(self.stream):
+            while not self.sim.step_begin():
+                if not self._next_target():
+                    return False
+        return True
+
+    def _next_target(self) -> bool:
+        """The run stopped: keep the snapshot, then start the run to the next target fraction;
+        False when the job is complete."""
+        res = self.sim.end_run()
+        snap_phi = None
+        if self.keep_snapshot_phi:
+            snap_phi = nat.d2h(self.ls.band_values())
+        self.snapshots.append((res.fraction, self.sim.time, snap_phi))
+        self.targets.pop(0)
+        if res.stop_reason != "target_volume" or not self.targets:
+            self._complete(res)
+            return False
+        self.sim.begin_run(self.targets[0], max_steps=self.params.max_steps)
         return True
 
     def finish(self) -> None:
@@ -156,6 +176,39 @@ class ErosionJob:
         self.ls = None
 
 
+class GroupedStepper:
+    """Runs the due steps of many jobs: the curvature-law jobs as one graph-captured group, the
+    SVI-law jobs (whose bands change at every reinitialisation) as an eager group, on two streams."""
+
+    def __init__(self, device):
+        self.groups = [(torch.cuda.Stream(device=device), GroupStep(device, use_graphs=False), True),
+                       (torch.cuda.Stream(device=device), GroupStep(device, use_graphs=True), False)]
+
+    def step(self, jobs: list[ErosionJob]) -> None:
+        """One step of every job in ``jobs`` (each one's ``begin_step`` returned True)."""
+        cur = torch.cuda.current_stream()
+        busy = []
+        for stream, group, svi in self.groups:
+            sims = [j.sim for j in jobs if j.sim.law.requires_svi == svi]
+            if not sims:
+                continue
+            stream.wait_stream(cur)
+            with torch.cuda.stream(stream):
+                group.launch(sims)
+            busy.append((stream, group))
+        while busy:
+            k = next((i for i, (_, g) in enumerate(busy) if g.ready()), 0)
+            stream, group = busy.pop(k)
+            with torch.cuda.stream(stream):
+                group.finish()
+        for stream, _, _ in self.groups:
+            cur.wait_stream(stream)
+
+    @property
+    def kernel_launches(self) -> int:
+        return sum(g.kernel_launches for _, g, _ in self.groups)
+
+
 class BatchedErosion:
     """Advance many solids together; each stops independently (spec batched form)."""
 
@@ -165,37 +218,19 @@ class BatchedErosion:
     def run(self, release: bool = True) -> list[JobResult]:
         for j in self.jobs:
             j.setup()
-        pending = [j for j in self.jobs if j.launch()]
-        for j in self.jobs:
-            if j.done and release:
-                j.release()
-        while pending:
-            pending = _advance(pending, release)
+        stepper = self.stepper = GroupedStepper(self.jobs[0].device if self.jobs else get_device(None))
+        active = list(self.jobs)
+        while active:
+            due = [j for j in active if j.begin_step()]
+            if release:
+                for j in active:
+                    if j.done:
+                        j.release()
+            active = due
+            if due:
+                stepper.step(due)
         torch.cuda.synchronize()
         return [j.result for j in self.jobs]
-
-
-def _advance(pending: list, release: bool, on_done=None) -> list:
-    """One polling sweep: every job whose step has completed is finished and
-    relaunched at once (its stream never waits for the other jobs); if none
-    has completed, block on the oldest launched step instead of spinning."""
-    still, progressed = [], False
-    for j in pending:
-        if j.ready():
-            progressed = True
-            j.finish()
-            if j.launch():
-                still.append(j)
-            else:
-                if on_done is not None:
-                    on_done(j)
-                if release:
-                    j.release()
-        else:
-            still.append(j)
-    if not progressed and still:
-        still[0].wait()
-    return still
 
 
 def run_plain(jobs: list[ErosionJob]) -> list[JobResult]:
@@ -249,19 +284,14 @@ class ErosionServer:
             job.setup()
             req.admitted = now
             self.in_use += need
-            if job.launch():
-                self.active.append((req, job))
-            else:  # finished at set-up (e.g. already below its target)
-                req.completed = time.time() - self._t0
-                req.result = job.result
-                self.in_use -= need
-                job.release()
-                self.done.append(req)
+            self.active.append((req, job))
 
     def run(self, requests: list[Request]) -> dict:
-        """Open-loop: request i becomes visible at t0 + arrival_i."""
+        """Open-loop: request i becomes visible at t0 + arrival_i; admitted requests join the
+        running groups at the next step boundary."""
         for r in sorted(requests, key=lambda r: r.arrival):
             self.submit(r)
+        stepper = GroupedStepper(self.device)
         t0 = self._t0 = time.time()
         updates = 0
         while self.queue or self.active:
@@ -270,23 +300,21 @@ class ErosionServer:
             if not self.active:
                 time.sleep(max(0.0, min(self.queue[0].arrival - now, 0.01)))
                 continue
-            req_of = {id(j): r for r, j in self.active}
-            finished = []
-
-            def on_done(j):
-                r = req_of[id(j)]
-                r.completed = time.time() - t0
-                r.result = j.result
-                finished.append(j)
-
-            jobs = _advance([j for _, j in self.active], release=False, on_done=on_done)
-            for j in finished:
-                updates += j.result.band_updates
-                self.in_use -= j.footprint()
-                j.release()
-                self.done.append(req_of[id(j)])
-            alive = {id(j) for j in jobs}
-            self.active = [(r, j) for r, j in self.active if id(j) in alive]
+            due, still = [], []
+            for r, j in self.active:
+                if j.begin_step():
+                    due.append(j)
+                    still.append((r, j))
+                else:   # finished: result, latency, memory back
+                    r.completed = time.time() - t0
+                    r.result = j.result
+                    updates += j.result.band_updates
+                    self.in_use -= j.footprint()
+                    j.release()
+                    self.done.append(r)
+            self.active = still
+            if due:
+                stepper.step(due)
         wall = time.time() - t0
         lat = np.array([r.completed - r.arrival for r in self.done])
         return {"requests": len(self.done), "wall_s": wall, "solves_per_s": len(self.done) / wall,

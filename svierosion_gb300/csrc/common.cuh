@@ -362,6 +362,56 @@ inline CpGeom cp_geom(int ny, int nz, float hx, float hy, float hz, float h) {
   return g;
 }
 
+// Float constants of a stage, rounded once on the host: the kernels then do no
+// float64 work per node except the t - N difference of the SVI law.
+struct StageConst {
+  float h, inv_h, hx, hy, hz;  // spacing, 1/h, clamp bounds n - 3.001
+  float n_cap, eps, cut_b, cut_scale;
+  float t;  // the SVI law's t, rounded to float as the reference's float32 tensors see it
+  // curvature laws: alpha, alpha - 1, alpha - 2 and delta rounded once; amode
+  // 0: alpha = 1, 1: alpha < 1, 2: alpha > 1
+  float alpha, am1, am2, delta;
+  int amode;
+  CpGeom cp;  // the closest-point projection's grid constants
+};
+
+// Band work of many level sets in one launch (svie_group_*): every member's
+// band is cut into tiles of GROUP_TILE consecutive entries -- the CTAs of the
+// one-level-set kernels -- and a launch takes a packed list of (member, tile)
+// pairs.  A member's record holds its arrays, sizes and law; the tile bodies
+// are the one-level-set kernels' own, so a member's results are bit-identical
+// to solving it alone.
+constexpr int GROUP_TILE = 256;
+
+struct GroupInst {
+  float* phi;
+  const int32_t* band;
+  float* field;       // SVI: the dense N field; curvature laws: interleaved (k1, k2)
+  float* occ;
+  float* u0;
+  float* L[3];
+  svie_stats* stats;  // stage statistics and the member's time step
+  svie_stats* vstats; // volume statistics
+  double* stage_part; // per-tile statistics partials
+  double* vol_part;   // per-tile volume partials
+  long long m;
+  int nx, ny, nz, kind;  // kind 0: SVI law, 1: curvature law
+  svie_law law;
+  StageConst C;
+};
+
+// Group table layout: the member records, then the (member, tile) pairs, SVI
+// members' tiles first.
+__host__ __device__ inline size_t group_tiles_offset(int n) { return ((size_t)n * sizeof(GroupInst) + 15) & ~(size_t)15; }
+
+// The CTA copies member k's record into shared memory (and waits for the copy).
+SVIE_DEV void load_group_inst(GroupInst& dst, const GroupInst* src) {
+  const int words = (int)(sizeof(GroupInst) / 4);
+  for (int k = threadIdx.x; k < words; k += blockDim.x)
+    reinterpret_cast<int*>(&dst)[k] = reinterpret_cast<const int*>(src)[k];
+  __syncthreads();
+}
+
 // First Newton projection to the zero set (reference kernels.py:185-208).
 // The division by h uses the correctly rounded reciprocal (div_by), the node
 // coordinates the exact multiply-shift division: same results as the plain

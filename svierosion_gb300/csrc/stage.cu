@@ -17,19 +17,6 @@ namespace svie {
 
 constexpr int SG_THREADS = 256;
 
-// Float constants of a stage, rounded once on the host: the kernels then do no
-// float64 work per node except the t - N difference of the SVI law.
-struct StageConst {
-  float h, inv_h, hx, hy, hz;  // spacing, 1/h, clamp bounds n - 3.001
-  float n_cap, eps, cut_b, cut_scale;
-  float t;  // the SVI law's t, rounded to float as the reference's float32 tensors see it
-  // curvature laws: alpha, alpha - 1, alpha - 2 and delta rounded once; amode
-  // 0: alpha = 1, 1: alpha < 1, 2: alpha > 1
-  float alpha, am1, am2, delta;
-  int amode;
-  CpGeom cp;  // the closest-point projection's grid constants
-};
-
 static StageConst stage_const(const svie_law& L, int nx, int ny, int nz) {
   StageConst c;
   c.h = (float)L.h;
@@ -147,7 +134,7 @@ SVIE_DEV void stat_init(StatAcc& s) {
 // every quantity is reduced across its warp first, then warp 0 combines the
 // warps after a single barrier.  Maxima, minima and counts are exact in any
 // order; the two float64 partials are added in warp order.
-SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
+SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial, long long tile) {
   constexpr int NW = SG_THREADS / 32;
   __shared__ float shf[7][NW];
   __shared__ unsigned int shu[3][NW];
@@ -210,17 +197,17 @@ SVIE_DEV void stat_commit(StatAcc& a, svie_stats* st, double* partial) {
   }
   // double-float partials, two per CTA (near, all), in the 16 bytes of two doubles
   float2* pp = reinterpret_cast<float2*>(partial);
-  pp[2 * blockIdx.x] = make_float2(r0.hi, r0.lo);
-  pp[2 * blockIdx.x + 1] = make_float2(r1.hi, r1.lo);
+  pp[2 * tile] = make_float2(r0.hi, r0.lo);
+  pp[2 * tile + 1] = make_float2(r1.hi, r1.lo);
 }
 
-__global__ void __launch_bounds__(SG_THREADS, 6) k_stage_svi(const float* __restrict__ phi,
-                                                          const int32_t* __restrict__ band, long long m, int nx,
-                                                          int ny, int nz, const float* __restrict__ Nd,
-                                                          svie_law L, StageConst C, float* __restrict__ Lout,
-                                                          float* __restrict__ u0, float* __restrict__ Vout,
-                                                          svie_stats* st, double* partial) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// One tile (SG_THREADS consecutive band entries, the tile-th) of the SVI stage;
+// the statistics partial of the tile goes to slot `tile` of `partial`.
+SVIE_DEV void stage_svi_tile(long long tile, const float* __restrict__ phi, const int32_t* __restrict__ band,
+                             long long m, int ny, int nz, const float* __restrict__ Nd, const svie_law& L,
+                             const StageConst& C, float* __restrict__ Lout, float* __restrict__ u0,
+                             float* __restrict__ Vout, svie_stats* st, double* partial) {
+  const long long t = tile * SG_THREADS + threadIdx.x;
   const int syz = ny * nz;
   StatAcc acc;
   if (st) stat_init(acc);
@@ -246,12 +233,21 @@ __global__ void __launch_bounds__(SG_THREADS, 6) k_stage_svi(const float* __rest
     if (Vout) Vout[t] = V;
     if (st) acc.vmax = V;
   }
-  if (st) stat_commit(acc, st, partial);
+  if (st) stat_commit(acc, st, partial, tile);
 }
 
-__global__ void k_curv_scatter(const float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
-                               int ny, int nz, float h, float* __restrict__ kd) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(SG_THREADS, 6) k_stage_svi(const float* __restrict__ phi,
+                                                          const int32_t* __restrict__ band, long long m, int nx,
+                                                          int ny, int nz, const float* __restrict__ Nd,
+                                                          svie_law L, StageConst C, float* __restrict__ Lout,
+                                                          float* __restrict__ u0, float* __restrict__ Vout,
+                                                          svie_stats* st, double* partial) {
+  stage_svi_tile(blockIdx.x, phi, band, m, ny, nz, Nd, L, C, Lout, u0, Vout, st, partial);
+}
+
+SVIE_DEV void curv_scatter_tile(long long tile, const float* __restrict__ phi, const int32_t* __restrict__ band,
+                                long long m, int ny, int nz, float h, float* __restrict__ kd) {
+  const long long t = tile * SG_THREADS + threadIdx.x;
   if (t >= m) return;
   const int i = band[t];
   const float2 k = principal_curvatures_at(phi, i, ny * nz, nz, 1, h);
@@ -259,13 +255,16 @@ __global__ void k_curv_scatter(const float* __restrict__ phi, const int32_t* __r
   kd[2 * i + 1] = k.y;
 }
 
-__global__ void __launch_bounds__(SG_THREADS) k_stage_curv(const float* __restrict__ phi,
-                                                           const int32_t* __restrict__ band, long long m, int nx,
-                                                           int ny, int nz, const float* __restrict__ kd,
-                                                           svie_law L, StageConst C, float* __restrict__ Lout,
-                                                           float* __restrict__ u0, float* __restrict__ Vout,
-                                                           svie_stats* st, double* partial) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_curv_scatter(const float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
+                               int ny, int nz, float h, float* __restrict__ kd) {
+  curv_scatter_tile(blockIdx.x, phi, band, m, ny, nz, h, kd);
+}
+
+SVIE_DEV void stage_curv_tile(long long tile, const float* __restrict__ phi, const int32_t* __restrict__ band,
+                              long long m, int ny, int nz, const float* __restrict__ kd, const svie_law& L,
+                              const StageConst& C, float* __restrict__ Lout, float* __restrict__ u0,
+                              float* __restrict__ Vout, svie_stats* st, double* partial) {
+  const long long t = tile * SG_THREADS + threadIdx.x;
   const int syz = ny * nz;
   StatAcc acc;
   if (st) stat_init(acc);
@@ -290,10 +289,19 @@ __global__ void __launch_bounds__(SG_THREADS) k_stage_curv(const float* __restri
     if (Vout) Vout[t] = V;
     if (st) acc.vmax = V;
   }
-  if (st) stat_commit(acc, st, partial);
+  if (st) stat_commit(acc, st, partial, tile);
 }
 
-__global__ void k_stats_reset(svie_stats* st, double dt_cap) {
+__global__ void __launch_bounds__(SG_THREADS) k_stage_curv(const float* __restrict__ phi,
+                                                           const int32_t* __restrict__ band, long long m, int nx,
+                                                           int ny, int nz, const float* __restrict__ kd,
+                                                           svie_law L, StageConst C, float* __restrict__ Lout,
+                                                           float* __restrict__ u0, float* __restrict__ Vout,
+                                                           svie_stats* st, double* partial) {
+  stage_curv_tile(blockIdx.x, phi, band, m, ny, nz, kd, L, C, Lout, u0, Vout, st, partial);
+}
+
+SVIE_DEV void stats_reset_at(svie_stats* st, double dt_cap) {
   st->vsum_near = st->vsum_all = 0.0;
   st->dt = 0.0;
   st->dt_cap = dt_cap;
@@ -306,9 +314,11 @@ __global__ void k_stats_reset(svie_stats* st, double dt_cap) {
   st->n_near = 0u;
 }
 
+__global__ void k_stats_reset(svie_stats* st, double dt_cap) { stats_reset_at(st, dt_cap); }
+
 // stable_dt (evolve.py:162-170) plus the float64 sums of V.
-__global__ void __launch_bounds__(SUM_THREADS) k_stats_finalize(svie_stats* st, svie_law L, const double* partial,
-                                                                long long nb, long long m) {
+SVIE_DEV void stats_finalize_block(svie_stats* st, const svie_law& L, const double* partial, long long nb,
+                                   long long m) {
   __shared__ DF sh[SUM_THREADS / 32];
   // the (near, all) double-float partials interleaved per CTA: sum each stream in a fixed order
   const float2* pp = reinterpret_cast<const float2*>(partial);
@@ -348,11 +358,15 @@ __global__ void __launch_bounds__(SUM_THREADS) k_stats_finalize(svie_stats* st, 
   st->dt = dt;
 }
 
+__global__ void __launch_bounds__(SUM_THREADS) k_stats_finalize(svie_stats* st, svie_law L, const double* partial,
+                                                                long long nb, long long m) {
+  stats_finalize_block(st, L, partial, nb, m);
+}
+
 // TVD-RK3 stage combinations (evolve.py:175-179) with the reference's float32
 // operation order; dt read from the device.
-__global__ void k_rk(float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
-                     const float* __restrict__ u0, const float* __restrict__ L, const double* dtp, int stage) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+SVIE_DEV void rk_at(long long t, float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
+                    const float* __restrict__ u0, const float* __restrict__ L, const double* dtp, int stage) {
   if (t >= m) return;
   const long long i = band[t];
   if (stage == 0) {
@@ -370,6 +384,11 @@ __global__ void k_rk(float* __restrict__ phi, const int32_t* __restrict__ band, 
   } else {
     phi[i] = a / 3.0f + (float)(2.0 / 3.0) * (phi[i] + dl);
   }
+}
+
+__global__ void k_rk(float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
+                     const float* __restrict__ u0, const float* __restrict__ L, const double* dtp, int stage) {
+  rk_at((long long)blockIdx.x * blockDim.x + threadIdx.x, phi, band, m, u0, L, dtp, stage);
 }
 
 }  // namespace svie
@@ -500,3 +519,219 @@ extern "C" int svie_law_eval(const float* x1, const float* x2, int64_t m, const 
   svie::k_law_eval<<<svie::blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(x1, x2, m, *law, C, V, D);
   return svie::launch_status("svie_law_eval");
 }
+
+// ------------------------------------------------ many level sets in one launch
+namespace svie {
+
+static_assert(SG_THREADS == GROUP_TILE, "group tiles are the stage kernels' CTAs");
+
+SVIE_DEV const GroupInst* group_members(const void* table) { return (const GroupInst*)table; }
+SVIE_DEV const int2* group_tile_list(const void* table, int n) {
+  return (const int2*)((const char*)table + group_tiles_offset(n));
+}
+
+__global__ void k_group_stats_reset(const void* table, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) stats_reset_at(group_members(table)[k].stats, INFINITY);
+}
+
+__global__ void __launch_bounds__(SG_THREADS) k_group_curv_scatter(const void* table, int n, long long first) {
+  __shared__ GroupInst I;
+  const int2 tl = group_tile_list(table, n)[first + blockIdx.x];
+  load_group_inst(I, group_members(table) + tl.x);
+  curv_scatter_tile(tl.y, I.phi, I.band, I.m, I.ny, I.nz, (float)I.law.h, I.field);
+}
+
+__global__ void __launch_bounds__(SG_THREADS, 6) k_group_stage_svi(const void* table, int n, int stage) {
+  __shared__ GroupInst I;
+  const int2 tl = group_tile_list(table, n)[blockIdx.x];
+  load_group_inst(I, group_members(table) + tl.x);
+  const bool first = stage == 0;
+  stage_svi_tile(tl.y, I.phi, I.band, I.m, I.ny, I.nz, I.field, I.law, I.C, I.L[stage], first ? I.u0 : nullptr,
+                 nullptr, first ? I.stats : nullptr, I.stage_part);
+}
+
+__global__ void __launch_bounds__(SG_THREADS) k_group_stage_curv(const void* table, int n, long long first_tile,
+                                                                 int stage) {
+  __shared__ GroupInst I;
+  const int2 tl = group_tile_list(table, n)[first_tile + blockIdx.x];
+  load_group_inst(I, group_members(table) + tl.x);
+  const bool first = stage == 0;
+  stage_curv_tile(tl.y, I.phi, I.band, I.m, I.ny, I.nz, I.field, I.law, I.C, I.L[stage], first ? I.u0 : nullptr,
+                  nullptr, first ? I.stats : nullptr, I.stage_part);
+}
+
+// one CTA per member
+__global__ void __launch_bounds__(SUM_THREADS) k_group_stats_finalize(const void* table) {
+  const GroupInst* I = group_members(table) + blockIdx.x;
+  const long long m = I->m;
+  stats_finalize_block(I->stats, I->law, I->stage_part, (m + SG_THREADS - 1) / SG_THREADS, m);
+}
+
+__global__ void __launch_bounds__(GROUP_TILE) k_group_rk(const void* table, int n, int stage) {
+  const int2 tl = group_tile_list(table, n)[blockIdx.x];
+  const GroupInst* I = group_members(table) + tl.x;
+  rk_at((long long)tl.y * GROUP_TILE + threadIdx.x, I->phi, I->band, I->m, I->u0,
+        stage > 0 ? I->L[stage - 1] : nullptr, &I->stats->dt, stage);
+}
+
+__global__ void k_group_gather_stats(const void* table, svie_stats* dst) {
+  const GroupInst* I = group_members(table) + blockIdx.x;
+  constexpr int W = (int)(sizeof(svie_stats) / 4);
+  const int* a = (const int*)I->stats;
+  const int* b = (const int*)I->vstats;
+  int* o = (int*)(dst + 2 * blockIdx.x);
+  for (int k = threadIdx.x; k < 2 * W; k += blockDim.x) o[k] = k < W ? a[k] : b[k - W];
+}
+
+static bool group_ok(const char* name, const svie_group* g) {
+  if (!g || (g->n > 0 && !g->table) || g->n < 0 || g->tiles < 0 || g->tiles_svi < 0 || g->tiles_svi > g->tiles) {
+    set_error("%s: bad group", name);
+    return false;
+  }
+  return true;
+}
+
+}  // namespace svie
+
+extern "C" {
+
+int64_t svie_group_tiles(const svie_group_member* members, int32_t n) {
+  if (!members || n < 0) return -1;
+  int64_t t = 0;
+  for (int k = 0; k < n; ++k) t += (members[k].m + GROUP_TILE - 1) / GROUP_TILE;
+  return t;
+}
+
+size_t svie_group_table_bytes(int32_t n, int64_t tiles) {
+  if (n < 0 || tiles < 0) return 0;
+  return group_tiles_offset(n) + (size_t)tiles * sizeof(int2) + 16;
+}
+
+int svie_group_build(const svie_group_member* members, int32_t n, void* table, size_t table_bytes,
+                     void* host_staging, svie_group* out, void* stream) {
+  if (!out || n < 0 || (n > 0 && (!members || !table || !host_staging)) || ((uintptr_t)table & 15) ||
+      ((uintptr_t)host_staging & 15)) {
+    set_error("svie_group_build: bad arguments (table and staging 16-byte aligned)");
+    return SVIE_ERR_ARG;
+  }
+  const int64_t tiles = svie_group_tiles(members, n);
+  if (table_bytes < svie_group_table_bytes(n, tiles)) {
+    set_error("svie_group_build: table of %zu bytes, %zu needed", table_bytes, svie_group_table_bytes(n, tiles));
+    return SVIE_ERR_WORKSPACE;
+  }
+  GroupInst* rec = (GroupInst*)host_staging;
+  int2* tl = (int2*)((char*)host_staging + group_tiles_offset(n));
+  int64_t w = 0;
+  for (int pass = 0; pass < 2; ++pass) {  // SVI members' tiles first
+    for (int k = 0; k < n; ++k) {
+      const svie_group_member& M = members[k];
+      if (M.kind != pass) continue;
+      if (M.m < 0 || M.m >= (1LL << 31) || M.nx < 8 || M.ny < 8 || M.nz < 8 || (M.kind != 0 && M.kind != 1) ||
+          (M.m > 0 && (!M.phi || !M.band || !M.field || !M.occ || !M.u0 || !M.L[0] || !M.L[1] || !M.L[2])) ||
+          !M.stats || !M.vstats || (long long)M.nx * M.ny * M.nz >= (1LL << 31)) {
+        set_error("svie_group_build: member %d: bad arguments", k);
+        return SVIE_ERR_ARG;
+      }
+      if (!M.stage_ws || M.stage_ws_bytes < svie_stage_workspace_bytes(M.m) || !M.volume_ws ||
+          M.volume_ws_bytes < svie_volume_workspace_bytes(M.m)) {
+        set_error("svie_group_build: member %d: workspace too small", k);
+        return SVIE_ERR_WORKSPACE;
+      }
+      GroupInst& r = rec[k];
+      r.phi = M.phi;
+      r.band = M.band;
+      r.field = M.field;
+      r.occ = M.occ;
+      r.u0 = M.u0;
+      for (int j = 0; j < 3; ++j) r.L[j] = M.L[j];
+      r.stats = M.stats;
+      r.vstats = M.vstats;
+      r.stage_part = (double*)M.stage_ws;
+      r.vol_part = (double*)M.volume_ws;
+      r.m = M.m;
+      r.nx = M.nx;
+      r.ny = M.ny;
+      r.nz = M.nz;
+      r.kind = M.kind;
+      r.law = M.law;
+      r.C = stage_const(M.law, M.nx, M.ny, M.nz);
+      const long long nt = (M.m + GROUP_TILE - 1) / GROUP_TILE;
+      for (long long j = 0; j < nt; ++j) tl[w++] = make_int2(k, (int)j);
+    }
+    if (pass == 0) out->tiles_svi = w;
+  }
+  out->table = table;
+  out->n = n;
+  out->pad = 0;
+  out->tiles = w;
+  if (n > 0 && cudaMemcpyAsync(table, host_staging, svie_group_table_bytes(n, tiles), cudaMemcpyHostToDevice,
+                               (cudaStream_t)stream) != cudaSuccess) {
+    set_error("svie_group_build: table copy failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  return SVIE_OK;
+}
+
+int svie_group_stats_reset(const svie_group* g, void* stream) {
+  if (!group_ok("svie_group_stats_reset", g)) return SVIE_ERR_ARG;
+  if (g->n == 0) return SVIE_OK;
+  k_group_stats_reset<<<(g->n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(g->table, g->n);
+  return launch_status("svie_group_stats_reset");
+}
+
+int svie_group_curvature_scatter(const svie_group* g, void* stream) {
+  if (!group_ok("svie_group_curvature_scatter", g)) return SVIE_ERR_ARG;
+  const long long nt = g->tiles - g->tiles_svi;
+  if (nt == 0) return SVIE_OK;
+  k_group_curv_scatter<<<(unsigned)nt, SG_THREADS, 0, (cudaStream_t)stream>>>(g->table, g->n, g->tiles_svi);
+  return launch_status("svie_group_curvature_scatter");
+}
+
+int svie_group_stage(const svie_group* g, int stage, void* stream) {
+  if (!group_ok("svie_group_stage", g) || stage < 0 || stage > 2) {
+    set_error("svie_group_stage: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int launches = 0;
+  if (g->tiles_svi > 0) {
+    k_group_stage_svi<<<(unsigned)g->tiles_svi, SG_THREADS, 0, s>>>(g->table, g->n, stage);
+    ++launches;
+  }
+  const long long nc = g->tiles - g->tiles_svi;
+  if (nc > 0) {
+    k_group_stage_curv<<<(unsigned)nc, SG_THREADS, 0, s>>>(g->table, g->n, g->tiles_svi, stage);
+    ++launches;
+  }
+  return launch_status("svie_group_stage", launches);
+}
+
+int svie_group_stats_finalize(const svie_group* g, void* stream) {
+  if (!group_ok("svie_group_stats_finalize", g)) return SVIE_ERR_ARG;
+  if (g->n == 0) return SVIE_OK;
+  k_group_stats_finalize<<<g->n, SUM_THREADS, 0, (cudaStream_t)stream>>>(g->table);
+  return launch_status("svie_group_stats_finalize");
+}
+
+int svie_group_rk(const svie_group* g, int stage, void* stream) {
+  if (!group_ok("svie_group_rk", g) || stage < 0 || stage > 3) {
+    set_error("svie_group_rk: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (g->tiles == 0) return SVIE_OK;
+  k_group_rk<<<(unsigned)g->tiles, GROUP_TILE, 0, (cudaStream_t)stream>>>(g->table, g->n, stage);
+  return launch_status("svie_group_rk");
+}
+
+int svie_group_gather_stats(const svie_group* g, svie_stats* dst, void* stream) {
+  if (!group_ok("svie_group_gather_stats", g) || (g->n > 0 && !dst)) {
+    set_error("svie_group_gather_stats: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  if (g->n == 0) return SVIE_OK;
+  k_group_gather_stats<<<g->n, 64, 0, (cudaStream_t)stream>>>(g->table, dst);
+  return launch_status("svie_group_gather_stats");
+}
+
+}  // extern "C"

@@ -100,13 +100,14 @@ __global__ void k_pt_tri(const float* __restrict__ p, const float* __restrict__ 
 // Band volume: per-CTA float64 partial sums of the cell fractions, reduced in a
 // fixed order by a second one-CTA kernel (deterministic); also the
 // has_interface flags and (optionally) the occupancy scatter.
-__global__ void __launch_bounds__(ST_THREADS) k_volume_partial(const float* __restrict__ f,
-                                                               const int32_t* __restrict__ idx, long long m,
-                                                               long long sx, long long sy, long long sz,
-                                                               float* __restrict__ occ, double* partial,
-                                                               svie_stats* stats) {
+// One tile (ST_THREADS consecutive band entries, the tile-th) of the band
+// volume: its double-float partial into slot `tile`, the interface flags by
+// atomics, the cell fractions into occ when given.
+SVIE_DEV void volume_tile(long long tile, const float* __restrict__ f, const int32_t* __restrict__ idx, long long m,
+                          long long sx, long long sy, long long sz, float* __restrict__ occ, double* partial,
+                          svie_stats* stats) {
   __shared__ DF shd[ST_THREADS / 32];
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long t = tile * ST_THREADS + threadIdx.x;
   float v = 0.0f;
   int neg = 0, pos = 0;
   if (t < m) {
@@ -121,10 +122,18 @@ __global__ void __launch_bounds__(ST_THREADS) k_volume_partial(const float* __re
   const DF s = block_sum_df(v, shd);
   const int an = __syncthreads_or(neg), ap = __syncthreads_or(pos);
   if (threadIdx.x == 0) {
-    reinterpret_cast<float2*>(partial)[blockIdx.x] = make_float2(s.hi, s.lo);
+    reinterpret_cast<float2*>(partial)[tile] = make_float2(s.hi, s.lo);
     if (an) atomicOr(&stats->any_neg, 1u);
     if (ap) atomicOr(&stats->any_pos, 1u);
   }
+}
+
+__global__ void __launch_bounds__(ST_THREADS) k_volume_partial(const float* __restrict__ f,
+                                                               const int32_t* __restrict__ idx, long long m,
+                                                               long long sx, long long sy, long long sz,
+                                                               float* __restrict__ occ, double* partial,
+                                                               svie_stats* stats) {
+  volume_tile(blockIdx.x, f, idx, m, sx, sy, sz, occ, partial, stats);
 }
 
 // The per-CTA double-float partials (stored in the 8 bytes of a double each)
@@ -497,6 +506,75 @@ int svie_band_volume_noalloc(const float* phi, const int32_t* band, int64_t m, i
     k_volume_partial<<<(unsigned)nb, ST_THREADS, 0, s>>>(phi, band, m, sx, sy, sz, occ, partials, stats);
   k_sum_partials<<<1, SUM_THREADS, 0, s>>>(partials, nb, &stats->fsum);
   return launch_status("svie_band_volume_noalloc", nb > 0 ? 3 : 2);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------ many level sets in one launch
+namespace svie {
+
+static_assert(ST_THREADS == GROUP_TILE, "group tiles are the volume kernel's CTAs");
+
+__global__ void __launch_bounds__(GROUP_TILE) k_group_fractions(const void* table, int n) {
+  const int2 tl = ((const int2*)((const char*)table + group_tiles_offset(n)))[blockIdx.x];
+  const GroupInst* I = (const GroupInst*)table + tl.x;
+  const long long t = (long long)tl.y * GROUP_TILE + threadIdx.x;
+  if (t >= I->m) return;
+  const long long syz = (long long)I->ny * I->nz;
+  const int i = I->band[t];
+  I->occ[i] = cell_fraction_at(I->phi, i, syz, I->nz, 1);
+}
+
+__global__ void k_group_clear_flags(const void* table, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const GroupInst* I = (const GroupInst*)table + k;
+  I->vstats->any_neg = 0;
+  I->vstats->any_pos = 0;
+  I->vstats->n_band = (unsigned)I->m;
+}
+
+__global__ void __launch_bounds__(GROUP_TILE) k_group_volume_partial(const void* table, int n) {
+  __shared__ GroupInst I;
+  const int2 tl = ((const int2*)((const char*)table + group_tiles_offset(n)))[blockIdx.x];
+  load_group_inst(I, (const GroupInst*)table + tl.x);
+  volume_tile(tl.y, I.phi, I.band, I.m, (long long)I.ny * I.nz, I.nz, 1, I.occ, I.vol_part, I.vstats);
+}
+
+// one CTA per member
+__global__ void __launch_bounds__(SUM_THREADS) k_group_sum_partials(const void* table) {
+  __shared__ DF sh[SUM_THREADS / 32];
+  const GroupInst* I = (const GroupInst*)table + blockIdx.x;
+  const long long nb = (I->m + GROUP_TILE - 1) / GROUP_TILE;
+  const DF s = block_sum_partials_df(reinterpret_cast<const float2*>(I->vol_part), nb, sh);
+  if (threadIdx.x == 0) I->vstats->fsum = df_value(s);
+}
+
+}  // namespace svie
+
+extern "C" {
+
+int svie_group_scatter_fractions(const svie_group* g, void* stream) {
+  if (!g || g->n < 0 || (g->n > 0 && !g->table) || g->tiles_svi < 0) {
+    set_error("svie_group_scatter_fractions: bad group");
+    return SVIE_ERR_ARG;
+  }
+  if (g->tiles_svi == 0) return SVIE_OK;
+  k_group_fractions<<<(unsigned)g->tiles_svi, GROUP_TILE, 0, (cudaStream_t)stream>>>(g->table, g->n);
+  return launch_status("svie_group_scatter_fractions");
+}
+
+int svie_group_volume(const svie_group* g, void* stream) {
+  if (!g || g->n < 0 || (g->n > 0 && !g->table) || g->tiles < 0) {
+    set_error("svie_group_volume: bad group");
+    return SVIE_ERR_ARG;
+  }
+  if (g->n == 0) return SVIE_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_group_clear_flags<<<(g->n + 127) / 128, 128, 0, s>>>(g->table, g->n);
+  if (g->tiles > 0) k_group_volume_partial<<<(unsigned)g->tiles, GROUP_TILE, 0, s>>>(g->table, g->n);
+  k_group_sum_partials<<<g->n, SUM_THREADS, 0, s>>>(g->table);
+  return launch_status("svie_group_volume", g->tiles > 0 ? 3 : 2);
 }
 
 }  // extern "C"
