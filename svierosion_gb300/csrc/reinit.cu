@@ -320,6 +320,32 @@ SVIE_DEV int dist_offset(const Geo& g, long long t, uint32_t flags) {
 // 1e-3 h either way).  `off`: the node's first distance (dist_offset).
 // CROSS = false: a node without flagged crossings (the subcell branches
 // compiled out, hmin = h).
+// The term of axis a (0: x, 1: y, 2: z) in the right-hand side at a node with
+// value c, its neighbours m2, m1, p1, p2 along the axis, flag byte `flags` and
+// first subcell distance at dn; hmin takes the flagged crossings' distances.
+template <bool CROSS = true>
+SVIE_DEV float axis_term(int a, float c, float m2, float m1, float p1, float p2, bool outside,
+                         const float* __restrict__ dn, uint32_t flags, float h, float rh, float hh, float rhh,
+                         float& hmin) {
+  const float mm_p = minmod(p1 - 2.0f * c + m1, p2 - 2.0f * p1 + c);
+  const float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
+  float Dp = div_by(p1 - c - 0.5f * mm_p, h, rh);
+  float Dm = div_by(c - m1 + 0.5f * mm_m, h, rh);
+  if (CROSS && ((flags >> (2 * a)) & 1u)) {
+    const float xp = __ldg(dn + __popc(flags & ((1u << (2 * a)) - 1u)));
+    Dp = -c / xp - div_by(0.5f * xp * mm_p, hh, rhh);
+    hmin = fminf(hmin, xp);
+  }
+  if (CROSS && ((flags >> (2 * a + 1)) & 1u)) {
+    const float xm = __ldg(dn + __popc(flags & ((1u << (2 * a + 1)) - 1u)));
+    Dm = c / xm + div_by(0.5f * xm * mm_m, hh, rhh);
+    hmin = fminf(hmin, xm);
+  }
+  const float a1 = outside ? fmaxf(Dm, 0.0f) : fminf(Dm, 0.0f);
+  const float b1 = outside ? fminf(Dp, 0.0f) : fmaxf(Dp, 0.0f);
+  return fmaxf(a1 * a1, b1 * b1);
+}
+
 template <bool CROSS = true>
 SVIE_DEV float rhs_values(float c, const float (&v3)[3][4], const float* __restrict__ dn, uint32_t flags, float h,
                           float rh, float hh, float rhh, float& hmin) {
@@ -328,26 +354,9 @@ SVIE_DEV float rhs_values(float c, const float (&v3)[3][4], const float* __restr
   float g2 = 0.0f;
   hmin = h;
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float m2 = v3[a][0], m1 = v3[a][1], p1 = v3[a][2], p2 = v3[a][3];
-    const float mm_p = minmod(p1 - 2.0f * c + m1, p2 - 2.0f * p1 + c);
-    const float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
-    float Dp = div_by(p1 - c - 0.5f * mm_p, h, rh);
-    float Dm = div_by(c - m1 + 0.5f * mm_m, h, rh);
-    if (CROSS && ((flags >> (2 * a)) & 1u)) {
-      const float xp = __ldg(dn + __popc(flags & ((1u << (2 * a)) - 1u)));
-      Dp = -c / xp - div_by(0.5f * xp * mm_p, hh, rhh);
-      hmin = fminf(hmin, xp);
-    }
-    if (CROSS && ((flags >> (2 * a + 1)) & 1u)) {
-      const float xm = __ldg(dn + __popc(flags & ((1u << (2 * a + 1)) - 1u)));
-      Dm = c / xm + div_by(0.5f * xm * mm_m, hh, rhh);
-      hmin = fminf(hmin, xm);
-    }
-    const float a1 = outside ? fmaxf(Dm, 0.0f) : fminf(Dm, 0.0f);
-    const float b1 = outside ? fminf(Dp, 0.0f) : fmaxf(Dp, 0.0f);
-    g2 = g2 + fmaxf(a1 * a1, b1 * b1);
-  }
+  for (int a = 0; a < 3; ++a)
+    g2 = g2 + axis_term<CROSS>(a, c, v3[a][0], v3[a][1], v3[a][2], v3[a][3], outside, dn, flags, h, rh, hh, rhh,
+                               hmin);
   return -sgn * (sqrtf(g2) - 1.0f);
 }
 
@@ -784,11 +793,32 @@ struct RowShift {  // (d * stride) mod 4 for d = -2, -1, 1, 2 and stride mod 4 =
 // One Jacobi half-step over the quads (first: B = u0 + dtau rhs(A) with src = A,
 // dst = B; second: A = (u0 + B + dtau rhs(B)) / 2 with src = B, dst = A).
 // Blocks take contiguous runs of the quad list (one resident wave).
+// The x and y terms of the four nodes of a quad (rows at -2, -1, +1, +2 strides).
+template <int SM2, int SM1, int SP1, int SP2>
+SVIE_DEV void quad_axis(int a, const float* __restrict__ src, long long i0, long long stride, const float c[4],
+                        const uint32_t fl[4], const float* const dn[4], float h, float rh, float hh, float rhh,
+                        float g2[4], float hm[4]) {
+  float m2[4], m1[4], p1[4], p2[4];
+  load4<SM2>(src, i0 - 2 * stride, m2);
+  load4<SM1>(src, i0 - stride, m1);
+  load4<SP1>(src, i0 + stride, p1);
+  load4<SP2>(src, i0 + 2 * stride, p2);
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (fl[k]) g2[k] = g2[k] + axis_term<true>(a, c[k], m2[k], m1[k], p1[k], p2[k], (fl[k] & 64u) != 0u, dn[k],
+                                                fl[k], h, rh, hh, rhh, hm[k]);
+}
+
+// One Jacobi half-step over the quads (first: B = u0 + dtau rhs(A) with src = A,
+// dst = B; second: A = (u0 + B + dtau rhs(B)) / 2 with src = B, dst = A).
+// The axes are taken one after the other (x, y, z, the order of rhs_values),
+// so only one axis's neighbour rows are live at a time.  Blocks take
+// contiguous runs of the quad list (one resident wave).
 template <int OY, int OX>
-__global__ void __launch_bounds__(RI_THREADS, 3) k_quad_sweep(const float* __restrict__ src, float* __restrict__ dst,
-                                                            const int2* __restrict__ quad, const int* __restrict__ dbase,
-                                                            const float* __restrict__ dist, long long nq, int sx, int sy,
-                                                            float h, float rh, float rhh, float cfl, int second) {
+__global__ void __launch_bounds__(RI_THREADS) k_quad_sweep(const float* __restrict__ src, float* __restrict__ dst,
+                                                        const int2* __restrict__ quad, const int* __restrict__ dbase,
+                                                        const float* __restrict__ dist, long long nq, int sx, int sy,
+                                                        float h, float rh, float rhh, float cfl, int second) {
   using Y = RowShift<OY>;
   using X = RowShift<OX>;
   const long long per = ((nq + gridDim.x - 1) / gridDim.x + blockDim.x - 1) / blockDim.x * blockDim.x;
@@ -802,38 +832,39 @@ __global__ void __launch_bounds__(RI_THREADS, 3) k_quad_sweep(const float* __res
     const float4* zp = reinterpret_cast<const float4*>(src + i0) - 1;
     const float4 za = __ldg(zp), zb = __ldg(zp + 1), zc = __ldg(zp + 2);
     const float z[12] = {za.x, za.y, za.z, za.w, zb.x, zb.y, zb.z, zb.w, zc.x, zc.y, zc.z, zc.w};
-    float ym2[4], ym1[4], yp1[4], yp2[4], xm2[4], xm1[4], xp1[4], xp2[4];
-    load4<Y::m2>(src, i0 - 2LL * sy, ym2);
-    load4<Y::m1>(src, i0 - sy, ym1);
-    load4<Y::p1>(src, i0 + sy, yp1);
-    load4<Y::p2>(src, i0 + 2LL * sy, yp2);
-    load4<X::m2>(src, i0 - 2LL * sx, xm2);
-    load4<X::m1>(src, i0 - sx, xm1);
-    load4<X::p1>(src, i0 + sx, xp1);
-    load4<X::p2>(src, i0 + 2LL * sx, xp2);
+    const float c[4] = {zb.x, zb.y, zb.z, zb.w};
+    const float* dq = (meta & 0x3f3f3f3fu) ? dist + __ldg(dbase + q) : dist;
+    uint32_t fl[4];
+    const float* dn[4];
+    float g2[4], hm[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      fl[k] = (meta >> (8 * k)) & 255u;
+      dn[k] = dq + __popc(meta & 0x3f3f3f3fu & ((1u << (8 * k)) - 1u));
+      g2[k] = 0.0f;
+      hm[k] = h;
+    }
+    quad_axis<X::m2, X::m1, X::p1, X::p2>(0, src, i0, sx, c, fl, dn, h, rh, hh, rhh, g2, hm);
+    quad_axis<Y::m2, Y::m1, Y::p1, Y::p2>(1, src, i0, sy, c, fl, dn, h, rh, hh, rhh, g2, hm);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (fl[k]) g2[k] = g2[k] + axis_term<true>(2, c[k], z[k + 2], z[k + 3], z[k + 5], z[k + 6], (fl[k] & 64u) != 0u,
+                                                  dn[k], fl[k], h, rh, hh, rhh, hm[k]);
     float u0[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     if (second) {
       const float4 d4 = *reinterpret_cast<const float4*>(dst + i0);
       u0[0] = d4.x; u0[1] = d4.y; u0[2] = d4.z; u0[3] = d4.w;
     }
-    const float* dn = (meta & 0x3f3f3f3fu) ? dist + __ldg(dbase + q) : dist;
     float out[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const uint32_t fl = (meta >> (8 * k)) & 255u;
-      const float c = z[k + 4];
-      if (fl == 0u) {
-        out[k] = second ? u0[k] : c;   // a node that does not change: dst already holds it
+      if (fl[k] == 0u) {
+        out[k] = second ? u0[k] : c[k];   // a node that does not change: dst already holds it
         continue;
       }
-      const float v3[3][4] = {{xm2[k], xm1[k], xp1[k], xp2[k]},
-                              {ym2[k], ym1[k], yp1[k], yp2[k]},
-                              {z[k + 2], z[k + 3], z[k + 5], z[k + 6]}};
-      float hmin;
-      const float r = rhs_values<true>(c, v3, dn + __popc(meta & 0x3f3f3f3fu & ((1u << (8 * k)) - 1u)), fl, h, rh, hh,
-                                       rhh, hmin);
-      const float dtau = cfl * fmaxf(hmin, dfl);
-      out[k] = second ? 0.5f * (u0[k] + c + dtau * r) : c + dtau * r;
+      const float r = -meta_sgn(fl[k]) * (sqrtf(g2[k]) - 1.0f);
+      const float dtau = cfl * fmaxf(hm[k], dfl);
+      out[k] = second ? 0.5f * (u0[k] + c[k] + dtau * r) : c[k] + dtau * r;
     }
     *reinterpret_cast<float4*>(dst + i0) = make_float4(out[0], out[1], out[2], out[3]);
   }

@@ -85,7 +85,7 @@ def main(argv=None) -> int:
     """Profiling driver for ncu captures of the step kernels on a synthetic level set.
 
         python -m svierosion_gb300.profiling --grid 448x336x245 --steps 2     # RK3 steps (FFT + stages)
-        python -m svierosion_gb300.profiling --grid 448x336x245 --reinit 3    # reinitialisation sub-steps
+        python -m svierosion_gb300.profiling --grid 448x336x245 --reinit 3 [--sweep quad|list|both]
     """
     import argparse
     import time
@@ -97,51 +97,28 @@ def main(argv=None) -> int:
     ap.add_argument("--grid", default="448x336x245")
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--reinit", type=int, default=0)
+    ap.add_argument("--sweep", choices=["quad", "list", "both"], default="quad")
     a = ap.parse_args(argv)
     shape = tuple(int(v) for v in a.grid.split("x"))
     h = 2.078 / 400
     ls = _synthetic_levelset(shape, h)
     print("grid", shape, "band", ls.band32.numel(), flush=True)
     if a.reinit:
-        n = ls.grid.size
-        nx, ny, nz = shape
-        sc = ls.scratch
+        # reinitialisation calls as the evolution loop makes them (work-set band rebuild), alternating
+        # the quad and the list sweeps: per call the total and the 40 sweeps, by CUDA events
+        sweeps = ["quad", "list"] if a.sweep == "both" else [a.sweep]
         for _ in range(a.reinit):
-            # the steps of LevelSet.reinitialize, with events between them
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
-            ev[0].record()
-            nbits = nat.lib().svie_reinit_bits_bytes(nx, ny, nz)
-            mask, tmp = sc.get("reinit_mask", nbits), sc.get("reinit_tmp", nbits)
-            marked = sc.get("reinit_marked", nbits)
-            nat.call("svie_reinit_bits", nat.ptr(ls.work32), ls.work32.numel(), nx, ny, nz, 3, 4, nat.ptr(mask),
-                     nat.ptr(tmp), nat.ptr(marked), nat.stream())
-            ev[1].record()
-            ws = sc.get("brick", nat.lib().svie_brick_workspace_bytes(nx, ny, nz))
-            cnt = sc.get("reinit_count", 8)
-            nat.call("svie_brick_scan", 2, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
-                     nat.stream())
-            m = int(cnt[:8].cpu().view(torch.int64)[0])
-            idx = sc.get("reinit_idx", 4 * m)[:4 * m].view(torch.int32)
-            nat.call("svie_brick_write", 2, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
-                     nat.stream())
-            ev[2].record()
-            geo = sc.get("reinit_geo", nat.lib().svie_reinit_geometry_bytes(m))
-            nat.call("svie_reinit_geometry", nat.ptr(ls.flat), nat.ptr(idx), m, *ls.strides, ls.h, 0.45, nat.ptr(geo),
-                     nat.stream())
-            off = sc.get("reinit_off_inside", 8)
-            nat.call("svie_list_inside_off_mask", nat.ptr(ls.flat), nat.ptr(idx), m, nat.ptr(marked), nx, ny, nz,
-                     nat.ptr(off), nat.stream())
-            ev[3].record()
-            pt = sc.get("reinit_phi", 4 * n)
-            nat.call("svie_reinit_iterate", nat.ptr(ls.flat), nat.ptr(pt), n, nat.ptr(idx), m, *ls.strides, ls.h,
-                     nat.ptr(geo), 20, nat.stream())
-            ev[4].record()
-            ls.rebuild_band_on(idx, off)
-            ev[5].record()
-            torch.cuda.synchronize()
-            t = [ev[i].elapsed_time(ev[i + 1]) for i in range(5)]
-            print("work set %d mask %.3f compact %.3f geometry %.3f copy+40 sweeps %.3f rebuild %.3f ms" % (m, *t),
-                  flush=True)
+            for sweep in sweeps:
+                timer = KernelTimer(capacity=16)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                ls.reinitialize(20, timer=timer, work_set_rebuild=True, sweep=sweep)
+                e1.record()
+                torch.cuda.synchronize()
+                sw = timer.summary()["reinit_sweep"]
+                print("%s sweep: work set %d, reinitialize %.3f ms, 40 sweeps %.3f ms (%.2f us each)"
+                      % (sweep, timer.notes["reinit_work"][0], e0.elapsed_time(e1), sw["total_ms"],
+                         1000 * sw["mean_ms"]), flush=True)
         return 0
     law = S.SVIPowerLaw(0.05 * 2.078, 1, 1, 0.93)
     sim = S.ErosionSimulation(ls, law)
