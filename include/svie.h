@@ -488,24 +488,6 @@ int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_
 int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* idx, int64_t m,
                         int64_t sx, int64_t sy, int64_t sz, float h, const void* geo, int iterations,
                         void* stream);
-/* The sweeps of levelset.py:174-180 over quads: four consecutive nodes
- * i0 .. i0 + 3 of the flat grid (i0 % 4 == 0) holding a work node, each swept
- * by one thread with 16-byte loads of the z column and of the neighbour rows.
- * The work set is the bit mask of svie_reinit_bits.  _scan counts the quads
- * (rows in tiles of 4 x 4) into *count (device int64); _geometry lists them
- * with their crossing flags and the subcell distances of the flagged
- * crossings (m: the work-set size, which bounds the distances); _iterate runs
- * `iterations` TVD-RK2 iterations (phi_tmp: a grid-sized scratch).  The
- * results equal svie_reinit_geometry + svie_reinit_iterate bit for bit. */
-size_t svie_reinit_quad_workspace_bytes(int nx, int ny);
-int svie_reinit_quad_scan(const uint32_t* bits, int nx, int ny, int nz, void* ws, size_t ws_bytes,
-                          int64_t* count, void* stream);
-size_t svie_reinit_quad_geometry_bytes(int64_t nq, int64_t m);
-int svie_reinit_quad_geometry(const uint32_t* bits, const float* phi, int nx, int ny, int nz, float h,
-                              float cfl, const void* ws, size_t ws_bytes, int64_t nq, int64_t m, void* geo,
-                              size_t geo_bytes, void* stream);
-int svie_reinit_quad_iterate(float* phi, float* phi_tmp, int64_t n, int nx, int ny, int nz, float h,
-                             float cfl, const void* geo, int64_t nq, int64_t m, int iterations, void* stream);
 /* kernels.reinit_rhs (kernels.py:363-379) for API parity. */
 int svie_reinit_rhs(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy, int64_t sz,
                     float h, const void* geo, float* out, void* stream);

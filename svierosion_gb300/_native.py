@@ -165,11 +165,6 @@ _SIGS = {
     "svie_reinit_geometry": (I, [V, V, I64, I64, I64, I64, F, F, V, V]),
     "svie_reinit_iterate": (I, [V, V, I64, V, I64, I64, I64, I64, F, V, I, V]),
     "svie_reinit_rhs": (I, [V, V, I64, I64, I64, I64, F, V, V, V]),
-    "svie_reinit_quad_workspace_bytes": (Z, [I, I]),
-    "svie_reinit_quad_scan": (I, [V, I, I, I, V, Z, V, V]),
-    "svie_reinit_quad_geometry_bytes": (Z, [I64, I64]),
-    "svie_reinit_quad_geometry": (I, [V, V, I, I, I, F, F, V, Z, I64, I64, V, Z, V]),
-    "svie_reinit_quad_iterate": (I, [V, V, I64, I, I, I, F, F, V, I64, I64, I, V]),
     "svie_mesh_pieces": (I, [V, V, I64, D, D, D, V, V, V, V]),
     "svie_mesh_bounds": (I, [V, I64, V, Z, V, V]),
     "svie_mesh_faces_i32": (I, [V, I64, I64, V, V, V]),

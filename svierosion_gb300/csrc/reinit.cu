@@ -320,53 +320,15 @@ SVIE_DEV int dist_offset(const Geo& g, long long t, uint32_t flags) {
 // 1e-3 h either way).  `off`: the node's first distance (dist_offset).
 // CROSS = false: a node without flagged crossings (the subcell branches
 // compiled out, hmin = h).
-// The term of axis a (0: x, 1: y, 2: z) in the right-hand side at a node with
-// value c, its neighbours m2, m1, p1, p2 along the axis, flag byte `flags` and
-// first subcell distance at dn; hmin takes the flagged crossings' distances.
-template <bool CROSS = true>
-SVIE_DEV float axis_term(int a, float c, float m2, float m1, float p1, float p2, bool outside,
-                         const float* __restrict__ dn, uint32_t flags, float h, float rh, float hh, float rhh,
-                         float& hmin) {
-  const float mm_p = minmod(p1 - 2.0f * c + m1, p2 - 2.0f * p1 + c);
-  const float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
-  float Dp = div_by(p1 - c - 0.5f * mm_p, h, rh);
-  float Dm = div_by(c - m1 + 0.5f * mm_m, h, rh);
-  if (CROSS && ((flags >> (2 * a)) & 1u)) {
-    const float xp = __ldg(dn + __popc(flags & ((1u << (2 * a)) - 1u)));
-    Dp = -c / xp - div_by(0.5f * xp * mm_p, hh, rhh);
-    hmin = fminf(hmin, xp);
-  }
-  if (CROSS && ((flags >> (2 * a + 1)) & 1u)) {
-    const float xm = __ldg(dn + __popc(flags & ((1u << (2 * a + 1)) - 1u)));
-    Dm = c / xm + div_by(0.5f * xm * mm_m, hh, rhh);
-    hmin = fminf(hmin, xm);
-  }
-  const float a1 = outside ? fmaxf(Dm, 0.0f) : fminf(Dm, 0.0f);
-  const float b1 = outside ? fminf(Dp, 0.0f) : fmaxf(Dp, 0.0f);
-  return fmaxf(a1 * a1, b1 * b1);
-}
-
-template <bool CROSS = true>
-SVIE_DEV float rhs_values(float c, const float (&v3)[3][4], const float* __restrict__ dn, uint32_t flags, float h,
-                          float rh, float hh, float rhh, float& hmin) {
-  const float sgn = meta_sgn(flags);
-  const bool outside = sgn > 0.0f;
-  float g2 = 0.0f;
-  hmin = h;
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-    g2 = g2 + axis_term<CROSS>(a, c, v3[a][0], v3[a][1], v3[a][2], v3[a][3], outside, dn, flags, h, rh, hh, rhh,
-                               hmin);
-  return -sgn * (sqrtf(g2) - 1.0f);
-}
-
-// The same right-hand side read from the grid: the arithmetic of rhs_values on
-// the 13-point stencil loaded around node i.
 template <bool CROSS = true>
 SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, int off, uint32_t flags, int sx,
                              int sy, int sz, float h, float rh, float hh, float rhh, float& hmin) {
   const float* qp = f + i;
   const float c = __ldg(qp);
+  const float sgn = meta_sgn(flags);
+  const bool outside = sgn > 0.0f;
+  float g2 = 0.0f;
+  hmin = h;
   const int st[3] = {sx, sy, sz};
   float v3[3][4];
 #pragma unroll
@@ -377,7 +339,29 @@ SVIE_DEV float reinit_rhs_at(const float* __restrict__ f, int i, const Geo& g, i
     v3[a][2] = __ldg(qp + s);
     v3[a][3] = __ldg(qp + 2 * s);
   }
-  return rhs_values<CROSS>(c, v3, g.dist + off, flags, h, rh, hh, rhh, hmin);
+  const float* dn = g.dist + off;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float m2 = v3[a][0], m1 = v3[a][1], p1 = v3[a][2], p2 = v3[a][3];
+    const float mm_p = minmod(p1 - 2.0f * c + m1, p2 - 2.0f * p1 + c);
+    const float mm_m = minmod(p1 - 2.0f * c + m1, c - 2.0f * m1 + m2);
+    float Dp = div_by(p1 - c - 0.5f * mm_p, h, rh);
+    float Dm = div_by(c - m1 + 0.5f * mm_m, h, rh);
+    if (CROSS && ((flags >> (2 * a)) & 1u)) {
+      const float xp = __ldg(dn + __popc(flags & ((1u << (2 * a)) - 1u)));
+      Dp = -c / xp - div_by(0.5f * xp * mm_p, hh, rhh);
+      hmin = fminf(hmin, xp);
+    }
+    if (CROSS && ((flags >> (2 * a + 1)) & 1u)) {
+      const float xm = __ldg(dn + __popc(flags & ((1u << (2 * a + 1)) - 1u)));
+      Dm = c / xm + div_by(0.5f * xm * mm_m, hh, rhh);
+      hmin = fminf(hmin, xm);
+    }
+    const float a1 = outside ? fmaxf(Dm, 0.0f) : fminf(Dm, 0.0f);
+    const float b1 = outside ? fminf(Dp, 0.0f) : fmaxf(Dp, 0.0f);
+    g2 = g2 + fmaxf(a1 * a1, b1 * b1);
+  }
+  return -sgn * (sqrtf(g2) - 1.0f);
 }
 
 // One Jacobi half-step of the TVD-RK2 pseudo-time iteration at work-set
@@ -627,271 +611,6 @@ __global__ void k_dilate_bits_rows(const uint32_t* __restrict__ in, uint32_t* __
   out[t] = acc;
 }
 
-
-// ------------------------------------------------------ quad sweep
-// The sweeps of the evolution loop run over quads: four consecutive nodes
-// i0 .. i0 + 3 of the flat grid with i0 % 4 == 0, holding at least one work
-// node.  A thread takes one quad: the z column i0 - 4 .. i0 + 7 arrives as
-// three aligned 16-byte loads, and each of the four neighbour rows along y
-// and along x (offsets -2, -1, 1, 2 strides) as one 16-byte load, or two when
-// the stride is not a multiple of 4 (the template arguments are the strides
-// mod 4, so the selection of the four values is resolved at compile time).
-// That replaces 13 scalar gathers and their address arithmetic per node by
-// about 3 to 5 vector loads, in a kernel whose time is set by issued
-// instructions.  A work node lies at least MARGIN = 4 nodes from every face,
-// so a quad holding one never straddles a row and every load stays inside the
-// grid.  Per quad the sweep reads 8 bytes (i0 and the four nodes' flag
-// bytes; flags 0 = the node does not change) and, for quads with crossings,
-// the index of their first subcell distance.  The node arithmetic is
-// rhs_values, as in the one-node kernels, so the results are bit-identical.
-//
-// Quad order: rows (x, y) in tiles of 4 x 4 rows, the quads of a row in
-// ascending z, so that the rows a warp reads overlap.
-struct QuadGeo {
-  int2* quad;     // (i0, flag bytes of nodes i0 .. i0 + 3)
-  int* dbase;     // [nq + 1]: index of each quad's first distance; dbase[nq] = the count
-  float* dist;    // subcell distances of the flagged crossings, quad / node / flag-bit order
-  int* sums;      // scan scratch
-};
-
-__host__ __device__ inline long long qgeo_dbase_off(long long nq) { return align16ll(8 * nq); }
-__host__ __device__ inline long long qgeo_dist_off(long long nq) { return align16ll(qgeo_dbase_off(nq) + 4 * (nq + 1)); }
-__host__ __device__ inline long long qgeo_sums_off(long long nq, long long m) {
-  return align16ll(qgeo_dist_off(nq) + 24 * m);
-}
-__host__ __device__ inline long long qgeo_bytes(long long nq, long long m) {
-  return qgeo_sums_off(nq, m) + 4 * ((nq + 1 + 1023) / 1024 + 1) + 256;
-}
-inline QuadGeo qgeo_view(void* base, long long nq, long long m) {
-  char* b = (char*)base;
-  QuadGeo g;
-  g.quad = (int2*)b;
-  g.dbase = (int*)(b + qgeo_dbase_off(nq));
-  g.dist = (float*)(b + qgeo_dist_off(nq));
-  g.sums = (int*)(b + qgeo_sums_off(nq, m));
-  return g;
-}
-
-// Row of the t-th thread in tile order; false past the grid.
-SVIE_DEV bool quad_row(long long t, int nx, int ny, long long& row) {
-  const int TY = (ny + 3) >> 2;
-  const long long T = t >> 4;
-  const int w = (int)(t & 15);
-  const int x = (int)((T / TY) << 2) + (w >> 2), y = (int)((T % TY) << 2) + (w & 3);
-  row = (long long)x * ny + y;
-  return x < nx && y < ny;
-}
-
-// fn(q, mask) for every quad q of the row with a work node, in ascending q;
-// mask: bit k set when node 4q + k is in the work set.
-template <typename Fn>
-SVIE_DEV void for_row_quads(const uint32_t* __restrict__ bits, long long row, int nz, int nzw, Fn fn) {
-  const long long base = row * nz;
-  long long last = -1;
-  uint32_t qmask = 0;
-  for (int w = 0; w < nzw; ++w) {
-    uint32_t word = bits[row * nzw + w];
-    while (word) {
-      const int b = __ffs(word) - 1;
-      word &= word - 1;
-      const long long i = base + 32LL * w + b;
-      const long long q = i >> 2;
-      if (q != last) {
-        if (last >= 0) fn(last, qmask);
-        last = q;
-        qmask = 0;
-      }
-      qmask |= 1u << (int)(i & 3);
-    }
-  }
-  if (last >= 0) fn(last, qmask);
-}
-
-__global__ void k_quad_count(const uint32_t* __restrict__ bits, int nx, int ny, int nz, long long nthreads,
-                             int* __restrict__ counts) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nthreads) return;
-  long long row;
-  int c = 0;
-  if (quad_row(t, nx, ny, row)) for_row_quads(bits, row, nz, (nz + 31) / 32, [&](long long, uint32_t) { ++c; });
-  counts[t] = c;
-}
-
-__global__ void k_quad_total(const int* __restrict__ offsets, long long nthreads, long long* count) {
-  *count = offsets[nthreads];
-}
-
-// The quads with their flag bytes (crossing_flags of the initial phi at the
-// work nodes, 0 elsewhere) and each quad's number of flagged crossings.
-__global__ void k_quad_write(const uint32_t* __restrict__ bits, const float* __restrict__ f, int nx, int ny, int nz,
-                             long long nthreads, const int* __restrict__ offsets, int2* __restrict__ quad,
-                             int* __restrict__ ndist) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nthreads) return;
-  long long row;
-  if (!quad_row(t, nx, ny, row)) return;
-  const int sy = nz, sx = ny * nz;
-  long long o = offsets[t];
-  for_row_quads(bits, row, nz, (nz + 31) / 32, [&](long long q, uint32_t mask) {
-    uint32_t meta = 0;
-    int nd = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if ((mask >> k) & 1u) {
-        const uint32_t fl = crossing_flags(f, (int)(4 * q + k), sx, sy, 1);
-        meta |= fl << (8 * k);
-        nd += __popc(fl & 63u);
-      }
-    }
-    quad[o] = make_int2((int)(4 * q), (int)meta);
-    ndist[o] = nd;
-    ++o;
-  });
-}
-
-// Subcell distances of the flagged crossings (geometry_at), at dbase[q] on.
-__global__ void k_quad_dist(const float* __restrict__ f, const int2* __restrict__ quad, const int* __restrict__ dbase,
-                            long long nq, int sx, int sy, float h, float cfl, float* __restrict__ dist) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq) return;
-  const int2 qd = quad[q];
-  const uint32_t meta = (uint32_t)qd.y;
-  if (!(meta & 0x3f3f3f3fu)) return;
-  int o = dbase[q];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const uint32_t fl = (meta >> (8 * k)) & 255u;
-    if (!(fl & 63u)) continue;
-    float d[6], dtau;
-    geometry_at(f, qd.x + k, sx, sy, 1, h, cfl, d, dtau);
-#pragma unroll
-    for (int b = 0; b < 6; ++b)
-      if ((fl >> b) & 1u) dist[o++] = d[b];
-  }
-}
-
-// Four values f[start .. start + 3] where start = (aligned base) + S, S = start % 4.
-template <int S>
-SVIE_DEV void load4(const float* __restrict__ f, long long start, float out[4]) {
-  const float4* p = reinterpret_cast<const float4*>(f + (start - S));
-  const float4 a = __ldg(p);
-  if (S == 0) {
-    out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
-  } else {
-    const float4 b = __ldg(p + 1);
-    const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) out[j] = v[j + S];
-  }
-}
-
-template <int O>
-struct RowShift {  // (d * stride) mod 4 for d = -2, -1, 1, 2 and stride mod 4 = O
-  static constexpr int m2 = ((-2 * O) % 4 + 4) % 4, m1 = ((-O) % 4 + 4) % 4, p1 = O % 4, p2 = (2 * O) % 4;
-};
-
-// One Jacobi half-step over the quads (first: B = u0 + dtau rhs(A) with src = A,
-// dst = B; second: A = (u0 + B + dtau rhs(B)) / 2 with src = B, dst = A).
-// Blocks take contiguous runs of the quad list (one resident wave).
-// The x and y terms of the four nodes of a quad (rows at -2, -1, +1, +2 strides).
-template <int SM2, int SM1, int SP1, int SP2>
-SVIE_DEV void quad_axis(int a, const float* __restrict__ src, long long i0, long long stride, const float c[4],
-                        const uint32_t fl[4], const float* const dn[4], float h, float rh, float hh, float rhh,
-                        float g2[4], float hm[4]) {
-  float m2[4], m1[4], p1[4], p2[4];
-  load4<SM2>(src, i0 - 2 * stride, m2);
-  load4<SM1>(src, i0 - stride, m1);
-  load4<SP1>(src, i0 + stride, p1);
-  load4<SP2>(src, i0 + 2 * stride, p2);
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    if (fl[k]) g2[k] = g2[k] + axis_term<true>(a, c[k], m2[k], m1[k], p1[k], p2[k], (fl[k] & 64u) != 0u, dn[k],
-                                                fl[k], h, rh, hh, rhh, hm[k]);
-}
-
-// One Jacobi half-step over the quads (first: B = u0 + dtau rhs(A) with src = A,
-// dst = B; second: A = (u0 + B + dtau rhs(B)) / 2 with src = B, dst = A).
-// The axes are taken one after the other (x, y, z, the order of rhs_values),
-// so only one axis's neighbour rows are live at a time.  Blocks take
-// contiguous runs of the quad list (one resident wave).
-template <int OY, int OX>
-__global__ void __launch_bounds__(RI_THREADS) k_quad_sweep(const float* __restrict__ src, float* __restrict__ dst,
-                                                        const int2* __restrict__ quad, const int* __restrict__ dbase,
-                                                        const float* __restrict__ dist, long long nq, int sx, int sy,
-                                                        float h, float rh, float rhh, float cfl, int second) {
-  using Y = RowShift<OY>;
-  using X = RowShift<OX>;
-  const long long per = ((nq + gridDim.x - 1) / gridDim.x + blockDim.x - 1) / blockDim.x * blockDim.x;
-  const long long q0 = (long long)blockIdx.x * per, q1 = min(q0 + per, nq);
-  const float hh = h * h;
-  const float dfl = 1e-3f * h;
-  for (long long q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-    const int2 qd = __ldg(quad + q);
-    const long long i0 = qd.x;
-    const uint32_t meta = (uint32_t)qd.y;
-    const float4* zp = reinterpret_cast<const float4*>(src + i0) - 1;
-    const float4 za = __ldg(zp), zb = __ldg(zp + 1), zc = __ldg(zp + 2);
-    const float z[12] = {za.x, za.y, za.z, za.w, zb.x, zb.y, zb.z, zb.w, zc.x, zc.y, zc.z, zc.w};
-    const float c[4] = {zb.x, zb.y, zb.z, zb.w};
-    const float* dq = (meta & 0x3f3f3f3fu) ? dist + __ldg(dbase + q) : dist;
-    uint32_t fl[4];
-    const float* dn[4];
-    float g2[4], hm[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      fl[k] = (meta >> (8 * k)) & 255u;
-      dn[k] = dq + __popc(meta & 0x3f3f3f3fu & ((1u << (8 * k)) - 1u));
-      g2[k] = 0.0f;
-      hm[k] = h;
-    }
-    quad_axis<X::m2, X::m1, X::p1, X::p2>(0, src, i0, sx, c, fl, dn, h, rh, hh, rhh, g2, hm);
-    quad_axis<Y::m2, Y::m1, Y::p1, Y::p2>(1, src, i0, sy, c, fl, dn, h, rh, hh, rhh, g2, hm);
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (fl[k]) g2[k] = g2[k] + axis_term<true>(2, c[k], z[k + 2], z[k + 3], z[k + 5], z[k + 6], (fl[k] & 64u) != 0u,
-                                                  dn[k], fl[k], h, rh, hh, rhh, hm[k]);
-    float u0[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    if (second) {
-      const float4 d4 = *reinterpret_cast<const float4*>(dst + i0);
-      u0[0] = d4.x; u0[1] = d4.y; u0[2] = d4.z; u0[3] = d4.w;
-    }
-    float out[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if (fl[k] == 0u) {
-        out[k] = second ? u0[k] : c[k];   // a node that does not change: dst already holds it
-        continue;
-      }
-      const float r = -meta_sgn(fl[k]) * (sqrtf(g2[k]) - 1.0f);
-      const float dtau = cfl * fmaxf(hm[k], dfl);
-      out[k] = second ? 0.5f * (u0[k] + c[k] + dtau * r) : c[k] + dtau * r;
-    }
-    *reinterpret_cast<float4*>(dst + i0) = make_float4(out[0], out[1], out[2], out[3]);
-  }
-}
-
-typedef void (*QuadSweepFn)(const float*, float*, const int2*, const int*, const float*, long long, int, int, float,
-                            float, float, float, int);
-
-template <int OY>
-static QuadSweepFn quad_sweep_for_x(int ox) {
-  switch (ox) {
-    case 0: return k_quad_sweep<OY, 0>;
-    case 1: return k_quad_sweep<OY, 1>;
-    case 2: return k_quad_sweep<OY, 2>;
-    default: return k_quad_sweep<OY, 3>;
-  }
-}
-
-static QuadSweepFn quad_sweep_for(int oy, int ox) {
-  switch (oy) {
-    case 0: return quad_sweep_for_x<0>(ox);
-    case 1: return quad_sweep_for_x<1>(ox);
-    case 2: return quad_sweep_for_x<2>(ox);
-    default: return quad_sweep_for_x<3>(ox);
-  }
-}
-
 inline size_t geo_bytes(long long m) { return (size_t)geo_layout(m < 1 ? 1 : m).total; }
 
 }  // namespace svie
@@ -1073,88 +792,3 @@ extern "C" int svie_dilate(const uint8_t* mask, int nx, int ny, int nz, int step
   svie::dilate_box(mask, out, tmp, nx, ny, nz, steps, 0, s, &launches);
   return svie::launch_status("svie_dilate", launches);
 }
-
-extern "C" {
-
-size_t svie_reinit_quad_workspace_bytes(int nx, int ny) {
-  const long long nt = (long long)((nx + 3) / 4) * ((ny + 3) / 4) * 16;
-  return (size_t)(4 * (nt + 1) + 4 * ((nt + 1 + 1023) / 1024 + 1) + 256);
-}
-
-int svie_reinit_quad_scan(const uint32_t* bits, int nx, int ny, int nz, void* ws, size_t ws_bytes, int64_t* count,
-                          void* stream) {
-  if (!bits || !ws || !count || nx <= 0 || ny <= 0 || nz <= 0 || (long long)nx * ny * nz >= (1LL << 31) ||
-      ws_bytes < svie_reinit_quad_workspace_bytes(nx, ny)) {
-    set_error("svie_reinit_quad_scan: bad arguments");
-    return SVIE_ERR_ARG;
-  }
-  cudaStream_t s = (cudaStream_t)stream;
-  const long long nt = (long long)((nx + 3) / 4) * ((ny + 3) / 4) * 16;
-  int* counts = (int*)ws;
-  int* sums = (int*)((char*)ws + 4 * (nt + 1));
-  if (cudaMemsetAsync(counts + nt, 0, sizeof(int), s) != cudaSuccess) {
-    set_error("svie_reinit_quad_scan: memset failed");
-    return SVIE_ERR_LAUNCH;
-  }
-  k_quad_count<<<blocks_for(nt, 256), 256, 0, s>>>(bits, nx, ny, nz, nt, counts);
-  const int ns = scan_exclusive_i32(counts, nt + 1, sums, s);
-  k_quad_total<<<1, 1, 0, s>>>(counts, nt, (long long*)count);
-  return launch_status("svie_reinit_quad_scan", 2 + ns);
-}
-
-size_t svie_reinit_quad_geometry_bytes(int64_t nq, int64_t m) {
-  return nq < 0 || m < 0 ? 0 : (size_t)qgeo_bytes(nq, m);
-}
-
-int svie_reinit_quad_geometry(const uint32_t* bits, const float* phi, int nx, int ny, int nz, float h, float cfl,
-                              const void* ws, size_t ws_bytes, int64_t nq, int64_t m, void* geo, size_t geo_bytes,
-                              void* stream) {
-  if (!bits || !phi || !ws || !geo || nq < 0 || m < 0 || ((uintptr_t)geo & 15) ||
-      ws_bytes < svie_reinit_quad_workspace_bytes(nx, ny) || geo_bytes < svie_reinit_quad_geometry_bytes(nq, m)) {
-    set_error("svie_reinit_quad_geometry: bad arguments");
-    return SVIE_ERR_ARG;
-  }
-  if (nq == 0) return SVIE_OK;
-  cudaStream_t s = (cudaStream_t)stream;
-  const long long nt = (long long)((nx + 3) / 4) * ((ny + 3) / 4) * 16;
-  const QuadGeo g = qgeo_view(geo, nq, m);
-  k_quad_write<<<blocks_for(nt, 256), 256, 0, s>>>(bits, phi, nx, ny, nz, nt, (const int*)ws, g.quad, g.dbase);
-  if (cudaMemsetAsync(g.dbase + nq, 0, sizeof(int), s) != cudaSuccess) {
-    set_error("svie_reinit_quad_geometry: memset failed");
-    return SVIE_ERR_LAUNCH;
-  }
-  const int ns = scan_exclusive_i32(g.dbase, nq + 1, g.sums, s);
-  k_quad_dist<<<blocks_for(nq, 256), 256, 0, s>>>(phi, g.quad, g.dbase, nq, ny * nz, nz, h, cfl, g.dist);
-  return launch_status("svie_reinit_quad_geometry", 2 + ns);
-}
-
-int svie_reinit_quad_iterate(float* phi, float* phi_tmp, int64_t n, int nx, int ny, int nz, float h, float cfl,
-                             const void* geo, int64_t nq, int64_t m, int iterations, void* stream) {
-  if (!phi || !phi_tmp || !geo || n != (int64_t)nx * ny * nz || nq < 0 || m < 0 || iterations < 0 ||
-      ((uintptr_t)phi & 15) || ((uintptr_t)phi_tmp & 15)) {
-    set_error("svie_reinit_quad_iterate: bad arguments (grids 16-byte aligned)");
-    return SVIE_ERR_ARG;
-  }
-  if (nq == 0 || iterations == 0) return SVIE_OK;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (cudaMemcpyAsync(phi_tmp, phi, (size_t)n * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
-    set_error("svie_reinit_quad_iterate: copy failed");
-    return SVIE_ERR_LAUNCH;
-  }
-  const QuadGeo g = qgeo_view(const_cast<void*>(geo), nq, m);
-  const int sy = nz, sx = ny * nz;
-  const QuadSweepFn fn = quad_sweep_for(sy & 3, sx & 3);
-  int dev = 0, nsm = 1, per_sm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, RI_THREADS, 0);
-  const int nb = (int)std::min<long long>((long long)blocks_for(nq, RI_THREADS), (long long)std::max(per_sm, 1) * nsm);
-  const float rh = rn_reciprocal(h), rhh = rn_reciprocal(h * h);
-  for (int it = 0; it < iterations; ++it) {
-    fn<<<nb, RI_THREADS, 0, s>>>(phi, phi_tmp, g.quad, g.dbase, g.dist, nq, sx, sy, h, rh, rhh, cfl, 0);
-    fn<<<nb, RI_THREADS, 0, s>>>(phi_tmp, phi, g.quad, g.dbase, g.dist, nq, sx, sy, h, rh, rhh, cfl, 1);
-  }
-  return launch_status("svie_reinit_quad_iterate", 2 * iterations);
-}
-
-}  // extern "C"

@@ -42,11 +42,6 @@ def cube_plane_fraction(s, a, b, c):
     return f(s, a, b, c)
 
 
-def ctypes_addr(t: torch.Tensor, offset: int):
-    import ctypes
-    return ctypes.c_void_p(t.data_ptr() + int(offset))
-
-
 def _read(t: torch.Tensor, dtype: np.dtype):
     return np.frombuffer(t.cpu().numpy().tobytes(), dtype=dtype)[0]
 
@@ -266,7 +261,7 @@ class LevelSet:
 
     # --------------------------------------------------- reinitialisation
     def reinitialize(self, iterations: int = 12, cfl: float = 0.45, dilation: int = 3, timer=None,
-                     work_set_rebuild: bool = False, sweep: str = "quad") -> None:
+                     work_set_rebuild: bool = False) -> None:
         """Subcell-fixed PDE reinitialisation (Min 2010) on the dilated band (levelset.py:154-183).
 
         ``timer`` (optional profiling.KernelTimer): events around the sweeps
@@ -277,11 +272,7 @@ class LevelSet:
         loop's case).  Off the work set phi is then unchanged and clamped, so
         the band, its order, phi, the occupancy and ``static_inside`` equal the
         full rebuild's; the inside box becomes the old box joined with the work
-        set's inside nodes (a box that contains the exact one).
-
-        ``sweep``: "quad" (default) sweeps the work set as quads of four consecutive nodes with vector
-        loads; "list" sweeps the brick-ordered node list one node per thread.  Both give the same
-        bits."""
+        set's inside nodes (a box that contains the exact one)."""
         n = self.grid.size
         nx, ny, nz = self.grid.shape
         sc = self.scratch
@@ -301,31 +292,17 @@ class LevelSet:
             mask, tmp = sc.get("reinit_mask", n), sc.get("reinit_tmp", n)
             nat.call("svie_reinit_mask", nat.ptr(self.work32), self.work32.numel(), nx, ny, nz, int(dilation), MARGIN,
                      nat.ptr(mask), nat.ptr(tmp), nat.stream())
-        quads = sweep == "quad" and kind == 2
-        if sweep not in ("quad", "list"):
-            raise ValueError("sweep must be 'quad' or 'list'")
         ws = sc.get("brick", lib.svie_brick_workspace_bytes(nx, ny, nz))
-        cnt = sc.get("reinit_count", 16)
+        cnt = sc.get("reinit_count", 8)
         nat.call("svie_brick_scan", kind, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(cnt),
                  nat.stream())
-        if quads:
-            qws = sc.get("reinit_quad_ws", lib.svie_reinit_quad_workspace_bytes(nx, ny))
-            nat.call("svie_reinit_quad_scan", nat.ptr(mask), nx, ny, nz, nat.ptr(qws), qws.numel(),
-                     ctypes_addr(cnt, 8), nat.stream())
-        counts = cnt[:16].cpu().view(torch.int64)   # one read for both counts
-        m = int(counts[0])
-        nq = int(counts[1]) if quads else 0
+        m = int(cnt[:8].cpu().view(torch.int64)[0])
         idx = sc.get("reinit_idx", 4 * max(m, 1))[:4 * m].view(torch.int32)
         nat.call("svie_brick_write", kind, nat.ptr(mask), nx, ny, nz, 0.0, nat.ptr(ws), ws.numel(), nat.ptr(idx), m,
                  nat.stream())
-        if quads:
-            geo = sc.get("reinit_qgeo", lib.svie_reinit_quad_geometry_bytes(nq, m))
-            nat.call("svie_reinit_quad_geometry", nat.ptr(mask), nat.ptr(self.flat), nx, ny, nz, self.h, cfl,
-                     nat.ptr(qws), qws.numel(), nq, m, nat.ptr(geo), geo.numel(), nat.stream())
-        else:
-            geo = sc.get("reinit_geo", lib.svie_reinit_geometry_bytes(m))
-            nat.call("svie_reinit_geometry", nat.ptr(self.flat), nat.ptr(idx), m, *self.strides, self.h, cfl,
-                     nat.ptr(geo), nat.stream())
+        geo = sc.get("reinit_geo", lib.svie_reinit_geometry_bytes(m))
+        nat.call("svie_reinit_geometry", nat.ptr(self.flat), nat.ptr(idx), m, *self.strides, self.h, cfl,
+                 nat.ptr(geo), nat.stream())
         off_inside = None
         if fast:
             # inside work-set nodes off the old band, before the sweeps
@@ -337,12 +314,8 @@ class LevelSet:
         if timed:
             ev = timer.take(2)
             ev[0].record()
-        if quads:
-            nat.call("svie_reinit_quad_iterate", nat.ptr(self.flat), nat.ptr(phi_tmp), n, nx, ny, nz, self.h, cfl,
-                     nat.ptr(geo), nq, m, int(iterations), nat.stream())
-        else:
-            nat.call("svie_reinit_iterate", nat.ptr(self.flat), nat.ptr(phi_tmp), n, nat.ptr(idx), m, *self.strides,
-                     self.h, nat.ptr(geo), int(iterations), nat.stream())
+        nat.call("svie_reinit_iterate", nat.ptr(self.flat), nat.ptr(phi_tmp), n, nat.ptr(idx), m, *self.strides,
+                 self.h, nat.ptr(geo), int(iterations), nat.stream())
         if timed:
             ev[1].record()
             timer.add(["reinit_sweep"], ev, [2 * int(iterations)])

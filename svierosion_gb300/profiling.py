@@ -85,7 +85,7 @@ def main(argv=None) -> int:
     """Profiling driver for ncu captures of the step kernels on a synthetic level set.
 
         python -m svierosion_gb300.profiling --grid 448x336x245 --steps 2     # RK3 steps (FFT + stages)
-        python -m svierosion_gb300.profiling --grid 448x336x245 --reinit 3 [--sweep quad|list|both]
+        python -m svierosion_gb300.profiling --grid 448x336x245 --reinit 3    # reinitialisation calls
     """
     import argparse
     import time
@@ -97,28 +97,25 @@ def main(argv=None) -> int:
     ap.add_argument("--grid", default="448x336x245")
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--reinit", type=int, default=0)
-    ap.add_argument("--sweep", choices=["quad", "list", "both"], default="quad")
     a = ap.parse_args(argv)
     shape = tuple(int(v) for v in a.grid.split("x"))
     h = 2.078 / 400
     ls = _synthetic_levelset(shape, h)
     print("grid", shape, "band", ls.band32.numel(), flush=True)
     if a.reinit:
-        # reinitialisation calls as the evolution loop makes them (work-set band rebuild), alternating
-        # the quad and the list sweeps: per call the total and the 40 sweeps, by CUDA events
-        sweeps = ["quad", "list"] if a.sweep == "both" else [a.sweep]
+        # reinitialisation calls as the evolution loop makes them (work-set band rebuild): per call
+        # the total and the 40 sweeps, by CUDA events
         for _ in range(a.reinit):
-            for sweep in sweeps:
-                timer = KernelTimer(capacity=16)
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                ls.reinitialize(20, timer=timer, work_set_rebuild=True, sweep=sweep)
-                e1.record()
-                torch.cuda.synchronize()
-                sw = timer.summary()["reinit_sweep"]
-                print("%s sweep: work set %d, reinitialize %.3f ms, 40 sweeps %.3f ms (%.2f us each)"
-                      % (sweep, timer.notes["reinit_work"][0], e0.elapsed_time(e1), sw["total_ms"],
-                         1000 * sw["mean_ms"]), flush=True)
+            timer = KernelTimer(capacity=16)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            ls.reinitialize(20, timer=timer, work_set_rebuild=True)
+            e1.record()
+            torch.cuda.synchronize()
+            sw = timer.summary()["reinit_sweep"]
+            print("work set %d, reinitialize %.3f ms, 40 sweeps %.3f ms (%.2f us each)"
+                  % (timer.notes["reinit_work"][0], e0.elapsed_time(e1), sw["total_ms"], 1000 * sw["mean_ms"]),
+                  flush=True)
         return 0
     law = S.SVIPowerLaw(0.05 * 2.078, 1, 1, 0.93)
     sim = S.ErosionSimulation(ls, law)

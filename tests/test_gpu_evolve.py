@@ -130,25 +130,3 @@ def test_work_set_rebuild_equals_full_rebuild():
         assert np.array_equal(np.asarray(full[k]), np.asarray(fast[k])), k
     assert all(a <= b for a, b in zip(fast[6], full[6])) and all(a >= b for a, b in zip(fast[7], full[7]))
     assert fast[8] == full[8]
-
-
-@pytest.mark.parametrize("res", [40, 45, 47, 51, 68, 73])
-def test_quad_sweep_equals_list_sweep(res):
-    """The reinitialisation sweeps over quads (four nodes per thread, vector loads of the neighbour
-    rows, the loads' alignment set by the strides mod 4: these resolutions give the residues
-    (nz mod 4, ny nz mod 4) = (0, 0), (1, 0), (2, 2), (2, 0), (3, 0), (3, 3)) give the one-node
-    list sweep's field, band and order bit for bit, after evolution steps."""
-    mesh = shapes.fragment(3, seed=2)
-    params = S.ErosionParams(law="svi", radius=0.2, k=1, s=1, t=0.93, resolution=res)
-    L = float((mesh.bounds[1] - mesh.bounds[0]).max())
-    out = []
-    for sweep in ("list", "quad"):
-        g = S.make_grid(mesh, params)
-        ls = S.LevelSet(S.mesh_to_sdf(mesh, g, band=6), g, width=6)
-        sim = S.ErosionSimulation(ls, params.make_law(length_scale=L), reinit_distance=1e9)
-        sim.run(target_fraction=None, max_steps=3)
-        ls.reinitialize(20, work_set_rebuild=True, sweep=sweep)
-        out.append((ls.flat.cpu().numpy(), ls.work32.cpu().numpy(), ls.volume()))
-    assert np.array_equal(out[0][0], out[1][0])
-    assert np.array_equal(out[0][1], out[1][1])
-    assert out[0][2] == out[1][2]
