@@ -11,6 +11,7 @@ from __future__ import annotations
 import ctypes
 import math
 import os
+import struct
 from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_size_t, c_void_p
 from pathlib import Path
 
@@ -73,15 +74,19 @@ BAND_INFO_BYTES = BAND_INFO_DTYPE.itemsize  # 64
 assert STATS_BYTES == 128 and BAND_INFO_BYTES == 64
 
 
+_U32 = struct.Struct("<I")
+_F32 = struct.Struct("<f")
+
+
 def bits_to_float(u) -> float:
-    return float(np.array([u], dtype=np.uint32).view(np.float32)[0])
+    return _F32.unpack(_U32.pack(int(u) & 0xFFFFFFFF))[0]
 
 
 def ordered_to_float(u) -> float:
     """Inverse of the device's order-preserving float -> uint32 map."""
     u = int(u) & 0xFFFFFFFF
     b = (u & 0x7FFFFFFF) if (u & 0x80000000) else (~u & 0xFFFFFFFF)
-    return float(np.array([b], dtype=np.uint32).view(np.float32)[0])
+    return _F32.unpack(_U32.pack(b))[0]
 
 
 # name -> (restype, argtypes)

@@ -577,19 +577,49 @@ SVIE_DEV float trilinear_at(const float* __restrict__ g, int ny, int nz, float3 
   return out;
 }
 
+// trilinear_at of both components of an interleaved (k1, k2) field, one 8-byte
+// load per corner; each component is accumulated in trilinear_at's order.
+SVIE_DEV float2 trilinear2_at(const float2* __restrict__ g, int ny, int nz, float3 p) {
+  float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
+  float tx = p.x - fx, ty = p.y - fy, tz = p.z - fz;
+  const long long syz = (long long)ny * nz;
+  const long long b0 = (long long)fx * syz + (long long)fy * nz + (long long)fz;
+  float2 out = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    float wa = a ? tx : 1.0f - tx;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      float wb = wa * (b ? ty : 1.0f - ty);
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const float2 v = __ldg(g + (b0 + a * syz + b * nz + c));
+        const float w = wb * (c ? tz : 1.0f - tz);
+        out.x = out.x + w * v.x;
+        out.y = out.y + w * v.y;
+      }
+    }
+  }
+  return out;
+}
+
 // Principal curvatures k1 >= k2 of the level sets at node i (reference kernels.py:274-299).
 SVIE_DEV float2 principal_curvatures_at(const float* __restrict__ f, int i, int sx, int sy, int sz, float h) {
   float c = __ldg(f + i);
   float xp = __ldg(f + i + sx), xm = __ldg(f + i - sx);
   float yp = __ldg(f + i + sy), ym = __ldg(f + i - sy);
   float zp = __ldg(f + i + sz), zm = __ldg(f + i - sz);
+  // the divisions by the constants 2h, h^2 and 4h^2 through their correctly rounded reciprocals
+  // (div_by): the same quotients as IEEE division, in three operations each
   float h2 = 2.0f * h, hh = h * h, h4 = 4.0f * h * h;
-  float px = (xp - xm) / h2, py = (yp - ym) / h2, pz = (zp - zm) / h2;
-  float pxx = (xp - 2.0f * c + xm) / hh;
-  float pyy = (yp - 2.0f * c + ym) / hh;
-  float pzz = (zp - 2.0f * c + zm) / hh;
+  const float r2 = __frcp_rn(h2), rhh = __frcp_rn(hh), r4 = __frcp_rn(h4);
+  float px = div_by(xp - xm, h2, r2), py = div_by(yp - ym, h2, r2), pz = div_by(zp - zm, h2, r2);
+  float pxx = div_by(xp - 2.0f * c + xm, hh, rhh);
+  float pyy = div_by(yp - 2.0f * c + ym, hh, rhh);
+  float pzz = div_by(zp - 2.0f * c + zm, hh, rhh);
   auto mixed = [&](int a, int b) {
-    return (__ldg(f + i + a + b) - __ldg(f + i + a - b) - __ldg(f + i - a + b) + __ldg(f + i - a - b)) / h4;
+    return div_by(__ldg(f + i + a + b) - __ldg(f + i + a - b) - __ldg(f + i - a + b) + __ldg(f + i - a - b), h4,
+                  r4);
   };
   float pxy = mixed(sx, sy), pxz = mixed(sx, sz), pyz = mixed(sy, sz);
   float g2 = fmaxf(px * px + py * py + pz * pz, 1e-30f);

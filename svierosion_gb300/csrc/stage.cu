@@ -250,9 +250,7 @@ SVIE_DEV void curv_scatter_tile(long long tile, const float* __restrict__ phi, c
   const long long t = tile * SG_THREADS + threadIdx.x;
   if (t >= m) return;
   const int i = band[t];
-  const float2 k = principal_curvatures_at(phi, i, ny * nz, nz, 1, h);
-  kd[2 * i] = k.x;
-  kd[2 * i + 1] = k.y;
+  reinterpret_cast<float2*>(kd)[i] = principal_curvatures_at(phi, i, ny * nz, nz, 1, h);
 }
 
 __global__ void k_curv_scatter(const float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
@@ -272,8 +270,8 @@ SVIE_DEV void stage_curv_tile(long long tile, const float* __restrict__ phi, con
     const int i = band[t];
     const float c = __ldg(phi + i);
     const float3 p = closest_point_at(phi, i, C.cp);
-    const float k1 = trilinear_at(kd, ny, nz, p, 2, 0);
-    const float k2 = trilinear_at(kd, ny, nz, p, 2, 1);
+    const float2 kk = trilinear2_at(reinterpret_cast<const float2*>(kd), ny, nz, p);
+    const float k1 = kk.x, k2 = kk.y;
     float V, D;
     curv_speed(k1, k2, L, C, &V, &D);
     if (st) {

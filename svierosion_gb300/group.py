@@ -98,16 +98,9 @@ class GroupStep:
 
     @staticmethod
     def _key_of(sims):
-        """What the table depends on: the members, their bands and workspaces (sized here)."""
-        lib = nat.lib()
-        out = []
-        for sim in sims:
-            ls = sim.ls
-            m = ls.work32.numel()
-            sws = ls.scratch.get("stage", lib.svie_stage_workspace_bytes(m))
-            vws = ls.scratch.get("volume", lib.svie_volume_workspace_bytes(m))
-            out.append((id(sim), sim._band_key, sim._field.data_ptr(), sws.data_ptr(), vws.data_ptr()))
-        return tuple(out)
+        """What the table depends on: the members and their bands (a member's buffers and
+        workspaces are sized by its band, so they change only with it)."""
+        return tuple((id(sim), sim._band_key) for sim in sims)
 
     # ------------------------------------------------------------ launch
     def _body(self, sims) -> None:

@@ -79,6 +79,18 @@ class LevelSet:
         return self.phi.view(-1)
 
     @property
+    def work32(self) -> torch.Tensor:
+        """The band in brick order (int32), the list the stencil kernels visit."""
+        return self._work32
+
+    @work32.setter
+    def work32(self, idx: torch.Tensor) -> None:
+        self._work32 = idx
+        # counts the band's replacements: a rebuilt list may reuse the old one's memory and
+        # size, so users key cached per-band data on this instead of the pointer alone
+        self.band_generation = getattr(self, "band_generation", 0) + 1
+
+    @property
     def band32(self) -> torch.Tensor:
         """The band in ascending flat order (int32), listed on first use after a rebuild."""
         if self._band32 is None:
