@@ -1,16 +1,16 @@
 """Batched and served erosion: many independent solids on one GPU.
 
 Every solid (an :class:`ErosionJob`) owns its level set, simulation and
-workspaces.  The scheduler opens the next step of every active job on the
-host (the stop tests; snapshot fractions and the next target when a run
-stops) and hands the due steps to :class:`GroupedStepper`: the curvature-law
-jobs advance in one group and the SVI-law jobs in another
-(:class:`~svierosion_gb300.group.GroupStep`), each a single launch per pass
-over the packed band tiles of all its members, on two streams that overlap.
-Each job's time step and stop test are its own; a job finishes its step on
-the host exactly as alone (regula falsi on the last step, reinitialisation),
-and its arithmetic is the plain path's, so its result is the same alone and
-in the mix.
+workspaces.  :class:`LaneScheduler` runs the jobs in a few lanes, each a
+group of jobs of one law kind that advances a step at a time with a single
+launch per pass over the packed band tiles of all its members
+(:class:`~svierosion_gb300.group.GroupStep`), on its own stream.  The lanes
+are not in lockstep: the host opens a lane's next steps (stop tests;
+snapshot fractions and the next target when a run stops), finishes its
+completed step (statistics, regula falsi on the last step,
+reinitialisation) and relaunches it while the other lanes run on the GPU.
+Each job's time step and stop test are its own and its arithmetic is the
+plain path's, so its result is the same alone and in the mix.
 
 :class:`ErosionServer` runs an open-loop request stream on top: requests are
 admitted as slots and HBM (estimated footprint) free up, folded into the
@@ -126,7 +126,7 @@ class ErosionJob:
 
     def begin_step(self) -> bool:
         """Open the job's next step (stop tests; at a stop, the snapshot and the next target);
-        False once the job has finished.  The step itself is run by a :class:`GroupedStepper`."""
+        False once the job has finished.  The step itself is run by a :class:`LaneScheduler`."""
         if self.done:
             return False
         with torch.cuda.stream(self.stream):
@@ -176,37 +176,87 @@ class ErosionJob:
         self.ls = None
 
 
-class GroupedStepper:
-    """Runs the due steps of many jobs: the curvature-law jobs as one graph-captured group, the
-    SVI-law jobs (whose bands change at every reinitialisation) as an eager group, on two streams."""
+class _Lane:
+    """Jobs of one law kind advanced together by a :class:`GroupStep` on their own stream."""
 
-    def __init__(self, device):
-        self.groups = [(torch.cuda.Stream(device=device), GroupStep(device, use_graphs=False), True),
-                       (torch.cuda.Stream(device=device), GroupStep(device, use_graphs=True), False)]
+    def __init__(self, device, svi: bool):
+        self.svi = svi
+        self.stream = torch.cuda.Stream(device=device)
+        # an SVI job's band changes at every reinitialisation (every few steps), before a graph
+        # capture pays off; curvature-law jobs keep theirs for hundreds of steps
+        self.group = GroupStep(device, use_graphs=not svi)
+        self.jobs: list[ErosionJob] = []
+        self.busy = False
 
-    def step(self, jobs: list[ErosionJob]) -> None:
-        """One step of every job in ``jobs`` (each one's ``begin_step`` returned True)."""
-        cur = torch.cuda.current_stream()
-        busy = []
-        for stream, group, svi in self.groups:
-            sims = [j.sim for j in jobs if j.sim.law.requires_svi == svi]
-            if not sims:
-                continue
-            stream.wait_stream(cur)
-            with torch.cuda.stream(stream):
-                group.launch(sims)
-            busy.append((stream, group))
-        while busy:
-            k = next((i for i, (_, g) in enumerate(busy) if g.ready()), 0)
-            stream, group = busy.pop(k)
-            with torch.cuda.stream(stream):
-                group.finish()
-        for stream, _, _ in self.groups:
-            cur.wait_stream(stream)
+
+class LaneScheduler:
+    """Runs many jobs as a few lanes: each lane a group of jobs of one law kind advanced a step
+    at a time with one launch per pass (:class:`~svierosion_gb300.group.GroupStep`) on its own
+    stream.  The lanes are not in lockstep: while the GPU runs one lane's step, the host finishes
+    another's (statistics, stop tests, regula falsi, reinitialisation) and relaunches it at once,
+    so host work and GPU work overlap.  A job's arithmetic is its own throughout."""
+
+    def __init__(self, device, lanes_svi: int = 1, lanes_curvature: int = 2):
+        self.lanes = [_Lane(device, True) for _ in range(lanes_svi)] + \
+                     [_Lane(device, False) for _ in range(lanes_curvature)]
+
+    def add(self, job: ErosionJob) -> None:
+        """A set-up job joins the least loaded lane of its law kind (at that lane's next step)."""
+        svi = job.sim.law.requires_svi
+        lane = min((ln for ln in self.lanes if ln.svi == svi), key=lambda ln: len(ln.jobs))
+        lane.jobs.append(job)
+
+    @property
+    def active(self) -> bool:
+        return any(ln.jobs for ln in self.lanes)
+
+    def _relaunch(self, lane: _Lane, on_done) -> None:
+        """Open the next step of the lane's jobs (completed jobs leave it) and launch it."""
+        with torch.cuda.stream(lane.stream):
+            due = []
+            for j in lane.jobs:
+                if j.begin_step():
+                    due.append(j)
+                elif on_done is not None:
+                    on_done(j)
+            lane.jobs = due
+            if due:
+                lane.group.launch([j.sim for j in due])
+        lane.busy = bool(due)
+
+    def _finish(self, lane: _Lane) -> None:
+        with torch.cuda.stream(lane.stream):
+            lane.group.finish()
+        lane.busy = False
+
+    def poll(self, on_done=None) -> None:
+        """Advance: launch the idle lanes, finish (and relaunch) every lane whose step has completed;
+        if none has, wait for one.  ``on_done(job)`` is called for every job that completes."""
+        progressed = False
+        for lane in self.lanes:
+            if not lane.busy and lane.jobs:
+                self._relaunch(lane, on_done)
+                progressed = True
+        for lane in self.lanes:
+            if lane.busy and lane.group.ready():
+                self._finish(lane)
+                self._relaunch(lane, on_done)
+                progressed = True
+        if not progressed:
+            busy = [ln for ln in self.lanes if ln.busy]
+            if busy:
+                self._finish(busy[0])
+                self._relaunch(busy[0], on_done)
+
+    def drain(self, on_done=None) -> None:
+        while self.active:
+            self.poll(on_done)
+        torch.cuda.synchronize()
 
     @property
     def kernel_launches(self) -> int:
-        return sum(g.kernel_launches for _, g, _ in self.groups)
+        """Kernels run by graph replays (direct launches are counted by the library)."""
+        return sum(ln.group.kernel_launches for ln in self.lanes)
 
 
 class BatchedErosion:
@@ -218,18 +268,11 @@ class BatchedErosion:
     def run(self, release: bool = True) -> list[JobResult]:
         for j in self.jobs:
             j.setup()
-        stepper = self.stepper = GroupedStepper(self.jobs[0].device if self.jobs else get_device(None))
-        active = list(self.jobs)
-        while active:
-            due = [j for j in active if j.begin_step()]
-            if release:
-                for j in active:
-                    if j.done:
-                        j.release()
-            active = due
-            if due:
-                stepper.step(due)
-        torch.cuda.synchronize()
+        sched = self.stepper = LaneScheduler(self.jobs[0].device if self.jobs else get_device(None))
+        for j in self.jobs:
+            if not j.done:
+                sched.add(j)
+        sched.drain(on_done=(lambda j: j.release()) if release else None)
         return [j.result for j in self.jobs]
 
 
@@ -288,33 +331,37 @@ class ErosionServer:
 
     def run(self, requests: list[Request]) -> dict:
         """Open-loop: request i becomes visible at t0 + arrival_i; admitted requests join the
-        running groups at the next step boundary."""
+        running lanes at their next step boundary."""
         for r in sorted(requests, key=lambda r: r.arrival):
             self.submit(r)
-        stepper = GroupedStepper(self.device)
+        sched = LaneScheduler(self.device)
         t0 = self._t0 = time.time()
-        updates = 0
+        req_of = {}
+        total = [0]
+
+        def done(j):   # result, latency, memory back
+            r = req_of.pop(id(j))
+            r.completed = time.time() - t0
+            r.result = j.result
+            total[0] += j.result.band_updates
+            self.in_use -= j.footprint()
+            j.release()
+            self.done.append(r)
+            self.active = [(q, k) for q, k in self.active if k is not j]
+
         while self.queue or self.active:
             now = time.time() - t0
+            n0 = len(self.active)
             self._admit(now)
+            for r, j in self.active[n0:]:
+                req_of[id(j)] = r
+                sched.add(j)
             if not self.active:
                 time.sleep(max(0.0, min(self.queue[0].arrival - now, 0.01)))
                 continue
-            due, still = [], []
-            for r, j in self.active:
-                if j.begin_step():
-                    due.append(j)
-                    still.append((r, j))
-                else:   # finished: result, latency, memory back
-                    r.completed = time.time() - t0
-                    r.result = j.result
-                    updates += j.result.band_updates
-                    self.in_use -= j.footprint()
-                    j.release()
-                    self.done.append(r)
-            self.active = still
-            if due:
-                stepper.step(due)
+            sched.poll(on_done=done)
+        torch.cuda.synchronize()
+        updates = total[0]
         wall = time.time() - t0
         lat = np.array([r.completed - r.arrival for r in self.done])
         return {"requests": len(self.done), "wall_s": wall, "solves_per_s": len(self.done) / wall,
