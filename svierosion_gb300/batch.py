@@ -196,7 +196,7 @@ class LaneScheduler:
     another's (statistics, stop tests, regula falsi, reinitialisation) and relaunches it at once,
     so host work and GPU work overlap.  A job's arithmetic is its own throughout."""
 
-    def __init__(self, device, lanes_svi: int = 1, lanes_curvature: int = 2):
+    def __init__(self, device, lanes_svi: int = 2, lanes_curvature: int = 4):
         self.lanes = [_Lane(device, True) for _ in range(lanes_svi)] + \
                      [_Lane(device, False) for _ in range(lanes_curvature)]
 
@@ -229,9 +229,10 @@ class LaneScheduler:
             lane.group.finish()
         lane.busy = False
 
-    def poll(self, on_done=None) -> None:
+    def poll(self, on_done=None, block: bool = True) -> None:
         """Advance: launch the idle lanes, finish (and relaunch) every lane whose step has completed;
-        if none has, wait for one.  ``on_done(job)`` is called for every job that completes."""
+        if none has and ``block``, wait for one.  ``on_done(job)`` is called for every job that
+        completes."""
         progressed = False
         for lane in self.lanes:
             if not lane.busy and lane.jobs:
@@ -242,7 +243,7 @@ class LaneScheduler:
                 self._finish(lane)
                 self._relaunch(lane, on_done)
                 progressed = True
-        if not progressed:
+        if not progressed and block:
             busy = [ln for ln in self.lanes if ln.busy]
             if busy:
                 self._finish(busy[0])
@@ -262,17 +263,18 @@ class LaneScheduler:
 class BatchedErosion:
     """Advance many solids together; each stops independently (spec batched form)."""
 
-    def __init__(self, jobs: list[ErosionJob]):
+    def __init__(self, jobs: list[ErosionJob], lanes_svi: int = 2, lanes_curvature: int = 4):
         self.jobs = list(jobs)
+        self.lanes = (lanes_svi, lanes_curvature)
 
     def run(self, release: bool = True) -> list[JobResult]:
-        for j in self.jobs:
+        sched = self.stepper = LaneScheduler(self.jobs[0].device if self.jobs else get_device(None), *self.lanes)
+        on_done = (lambda j: j.release()) if release else None
+        for j in self.jobs:   # each job starts stepping as soon as it is set up
             j.setup()
-        sched = self.stepper = LaneScheduler(self.jobs[0].device if self.jobs else get_device(None))
-        for j in self.jobs:
-            if not j.done:
-                sched.add(j)
-        sched.drain(on_done=(lambda j: j.release()) if release else None)
+            sched.add(j)
+            sched.poll(on_done, block=False)
+        sched.drain(on_done)
         return [j.result for j in self.jobs]
 
 
@@ -304,7 +306,9 @@ class Request:
 class ErosionServer:
     """Continuous batching of erosion requests under an HBM budget."""
 
-    def __init__(self, hbm_budget_bytes: int = 150 << 30, max_active: int = 64, device=None):
+    def __init__(self, hbm_budget_bytes: int = 150 << 30, max_active: int = 64, device=None, lanes_svi: int = 2,
+                 lanes_curvature: int = 4):
+        self.lanes = (lanes_svi, lanes_curvature)
         self.budget = int(hbm_budget_bytes)
         self.max_active = int(max_active)
         self.device = get_device(device)
@@ -334,7 +338,7 @@ class ErosionServer:
         running lanes at their next step boundary."""
         for r in sorted(requests, key=lambda r: r.arrival):
             self.submit(r)
-        sched = LaneScheduler(self.device)
+        sched = LaneScheduler(self.device, *self.lanes)
         t0 = self._t0 = time.time()
         req_of = {}
         total = [0]
