@@ -398,7 +398,8 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
       if (flags & 63u) continue;
       const int i = __ldg(idx + t);
       float hmin;
-      const float r = reinit_rhs_at<false>(src, i, g, 0, flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
+      // z stride 1 (C order) as a constant: the z neighbours become immediate offsets
+      const float r = reinit_rhs_at<false>(src, i, g, 0, flags, sx, sy, 1, h, rh, h * h, rhh, hmin);
       sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
     }
     return;
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
     const uint32_t flags = __ldg(g.meta + t);
     const int i = __ldg(idx + t);
     float hmin;
-    const float r = reinit_rhs_at<true>(src, i, g, __ldg(g.xoff + k), flags, sx, sy, sz, h, rh, h * h, rhh, hmin);
+    const float r = reinit_rhs_at<true>(src, i, g, __ldg(g.xoff + k), flags, sx, sy, 1, h, rh, h * h, rhh, hmin);
     sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
   }
 }
@@ -704,8 +705,8 @@ int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_
 
 int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
                         int64_t sz, float h, const void* geo, int iterations, void* stream) {
-  if (!phi || !phi_tmp || n <= 0 || m < 0 || iterations < 0) {
-    set_error("svie_reinit_iterate: bad arguments");
+  if (!phi || !phi_tmp || n <= 0 || m < 0 || iterations < 0 || sz != 1) {
+    set_error("svie_reinit_iterate: bad arguments (C-order grid: sz == 1)");
     return SVIE_ERR_ARG;
   }
   if (m == 0 || iterations == 0) return SVIE_OK;
