@@ -86,6 +86,7 @@ def main(argv=None) -> int:
 
         python -m svierosion_gb300.profiling --grid 448x336x245 --steps 2     # RK3 steps (FFT + stages)
         python -m svierosion_gb300.profiling --grid 448x336x245 --reinit 3    # reinitialisation calls
+        python -m svierosion_gb300.profiling --job mean --resolution 160 --steps 30   # one served-mix job
     """
     import argparse
     import time
@@ -97,7 +98,25 @@ def main(argv=None) -> int:
     ap.add_argument("--grid", default="448x336x245")
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--reinit", type=int, default=0)
+    ap.add_argument("--job", choices=["svi", "mean", "gauss"], default=None,
+                    help="erode one seeded fragment (subdivided 5x) with this law on the plain path, twice")
+    ap.add_argument("--resolution", type=int, default=160)
     a = ap.parse_args(argv)
+    if a.job:
+        # one request of the served mix's kind, solved alone (a mid-size curvature or SVI job)
+        from svierosion_gb300 import shapes
+        mesh = shapes.fragment(5, seed=3)
+        L = float((mesh.bounds[1] - mesh.bounds[0]).max())
+        kw = dict(radius=0.08 * L, k=1, s=1, t=0.93) if a.job == "svi" else dict(alpha=1.0 if a.job == "mean" else 0.25)
+        params = S.ErosionParams(law=a.job, resolution=a.resolution, target_fraction=0.9, max_steps=a.steps, **kw)
+        for _ in range(2):
+            t0 = time.time()
+            res = S.erode(mesh, params, extract_meshes=False, keep_state=True)
+            torch.cuda.synchronize()
+            print(a.job, res.grid.shape, "band", res.level_set.work32.numel(), len(res.history), "steps",
+                  res.stop_reason, "%.1f us per step" % (1e6 * res.timings["evolve"] / max(len(res.history), 1)),
+                  flush=True)
+        return 0
     shape = tuple(int(v) for v in a.grid.split("x"))
     h = 2.078 / 400
     ls = _synthetic_levelset(shape, h)
