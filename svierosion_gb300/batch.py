@@ -32,7 +32,7 @@ from . import _native as nat
 from .api import ErosionParams, make_grid
 from .evolve import ErosionSimulation
 from .grid import get_device
-from .group import GroupStep
+from .group import GroupStep, SerialStep
 from .levelset import LevelSet, tricubic
 from .meshio import TriMesh
 from .sdf import mesh_to_sdf
@@ -177,14 +177,15 @@ class ErosionJob:
 
 
 class _Lane:
-    """Jobs of one law kind advanced together by a :class:`GroupStep` on their own stream."""
+    """Jobs of one law kind advanced together on their own stream, by a :class:`GroupStep` (packed
+    launches) or a :class:`SerialStep` (each job's own launch sequence, back to back)."""
 
-    def __init__(self, device, svi: bool):
+    def __init__(self, device, svi: bool, serial: bool = False):
         self.svi = svi
         self.stream = torch.cuda.Stream(device=device)
         # an SVI job's band changes at every reinitialisation (every few steps), before a graph
         # capture pays off; curvature-law jobs keep theirs for hundreds of steps
-        self.group = GroupStep(device, use_graphs=not svi)
+        self.group = SerialStep(device) if serial else GroupStep(device, use_graphs=not svi)
         self.jobs: list[ErosionJob] = []
         self.busy = False
 
@@ -196,9 +197,9 @@ class LaneScheduler:
     another's (statistics, stop tests, regula falsi, reinitialisation) and relaunches it at once,
     so host work and GPU work overlap.  A job's arithmetic is its own throughout."""
 
-    def __init__(self, device, lanes_svi: int = 2, lanes_curvature: int = 4):
+    def __init__(self, device, lanes_svi: int = 2, lanes_curvature: int = 4, serial_curvature: bool = False):
         self.lanes = [_Lane(device, True) for _ in range(lanes_svi)] + \
-                     [_Lane(device, False) for _ in range(lanes_curvature)]
+                     [_Lane(device, False, serial_curvature) for _ in range(lanes_curvature)]
 
     def add(self, job: ErosionJob) -> None:
         """A set-up job joins the least loaded lane of its law kind (at that lane's next step)."""
@@ -263,9 +264,10 @@ class LaneScheduler:
 class BatchedErosion:
     """Advance many solids together; each stops independently (spec batched form)."""
 
-    def __init__(self, jobs: list[ErosionJob], lanes_svi: int = 2, lanes_curvature: int = 4):
+    def __init__(self, jobs: list[ErosionJob], lanes_svi: int = 2, lanes_curvature: int = 4,
+                 serial_curvature: bool = False):
         self.jobs = list(jobs)
-        self.lanes = (lanes_svi, lanes_curvature)
+        self.lanes = (lanes_svi, lanes_curvature, serial_curvature)
 
     def run(self, release: bool = True) -> list[JobResult]:
         sched = self.stepper = LaneScheduler(self.jobs[0].device if self.jobs else get_device(None), *self.lanes)

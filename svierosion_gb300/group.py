@@ -100,7 +100,7 @@ class GroupStep:
     def _key_of(sims):
         """What the table depends on: the members and their bands (a member's buffers and
         workspaces are sized by its band, so they change only with it)."""
-        return tuple((id(sim), sim._band_key) for sim in sims)
+        return tuple((sim.serial, sim._band_key) for sim in sims)
 
     # ------------------------------------------------------------ launch
     def _body(self, sims) -> None:
@@ -193,3 +193,41 @@ class GroupStep:
 
 def band_ptr(t: torch.Tensor):
     return nat.ptr(t).value
+
+
+class SerialStep:
+    """The GroupStep interface over each member's own step: the members' launch sequences (the
+    curvature laws' own CUDA graphs) go back to back on one stream, each with its statistics copy,
+    and one event closes the step.  A member's kernels then run while its level set is the one in
+    L2, where packed launches interleave all members' data."""
+
+    def __init__(self, device):
+        self.device = device
+        self._sims = []
+        self._event = None
+        self.steps = 0
+
+    def launch(self, sims) -> None:
+        self._sims = list(sims)
+        for sim in sims:
+            sim._launch_step()
+        if self._event is None:
+            self._event = torch.cuda.Event()
+        self._event.record()
+        self.steps += 1
+
+    def ready(self) -> bool:
+        return self._event is None or self._event.query()
+
+    def finish(self) -> None:
+        sims = self._sims
+        self._sims = []
+        if not sims:
+            return
+        self._event.synchronize()
+        for sim in sims:
+            sim.step_finish()
+
+    @property
+    def kernel_launches(self) -> int:
+        return sum(sim.kernel_launches for sim in self._sims)

@@ -93,3 +93,29 @@ def test_cuda_graph_replay_matches_eager_launches():
     a, b = res[False], res[True]
     assert a.stop_reason == b.stop_reason and a.steps == b.steps
     np.testing.assert_array_equal([r.fraction for r in a.history], [r.fraction for r in b.history])
+
+
+def _many_jobs():
+    """Twelve small jobs of uneven length, so that jobs finish while others are still being set up
+    and lanes change members from step to step."""
+    out = []
+    for i in range(12):
+        frag = shapes.fragment(2 + i % 2, seed=20 + i)
+        L = float((frag.bounds[1] - frag.bounds[0]).max())
+        if i % 3 == 0:
+            p = S.ErosionParams(law="mean", alpha=1.0, resolution=20 + 2 * i, target_fraction=0.98, max_steps=6 + i)
+        else:
+            p = S.ErosionParams(law="svi", radius=0.1 * L, k=i % 2, s=0, resolution=20 + 2 * i,
+                                target_fraction=0.97 - 0.005 * i)
+        out.append(ErosionJob(frag, p, name=str(i)))
+    return out
+
+
+@pytest.mark.parametrize("serial", [False, True], ids=["packed", "serial"])
+def test_lanes_with_turnover_equal_plain(serial):
+    """Jobs set up while others step, lanes losing and gaining members: every job's history equals
+    its plain solve bit for bit (a lane's cached launch table must never outlive its members)."""
+    plain = run_plain(_many_jobs())
+    batched = BatchedErosion(_many_jobs(), lanes_svi=2, lanes_curvature=2, serial_curvature=serial).run()
+    for a, b in zip(plain, batched):
+        _same(a, b)
