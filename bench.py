@@ -105,7 +105,7 @@ def run_batched(args) -> dict:
     jobs = [ErosionJob(m, p, name=str(i)) for i, (m, p) in enumerate(specs)]
     torch.cuda.synchronize()
     t0 = time.time()
-    res_b = BatchedErosion(jobs, args.lanes_svi, args.lanes_curvature).run()
+    res_b = BatchedErosion(jobs, args.lanes_svi, args.lanes_curvature, not args.packed_curvature).run()
     tb = time.time() - t0
     ub = sum(r.band_updates for r in res_b)
     same = all([x.fraction for x in a.history] == [x.fraction for x in b.history] for a, b in zip(res_b, res_p))
@@ -123,17 +123,17 @@ def run_batched(args) -> dict:
             "stop_reasons": {k: sum(r.stop_reason == k for r in res_b) for k in {r.stop_reason for r in res_b}}}
 
 
-def _served_stream(specs, arrivals, hbm_gb: float, max_active: int, lanes=(2, 4)):
+def _served_stream(specs, arrivals, hbm_gb: float, max_active: int, lanes=(2, 8, True)):
     from svierosion_gb300.batch import ErosionServer, Request
 
     reqs = [Request(i, float(a), m, p) for i, (a, (m, p)) in enumerate(zip(arrivals, specs))]
     srv = ErosionServer(hbm_budget_bytes=int(hbm_gb * (1 << 30)), max_active=max_active, lanes_svi=lanes[0],
-                        lanes_curvature=lanes[1])
+                        lanes_curvature=lanes[1], serial_curvature=lanes[2])
     return srv.run(reqs), reqs
 
 
 def served_vs_plain(n_requests: int, seed: int = 0, max_steps: int = 400, hbm_gb: float = 150.0,
-                    max_active: int = 64, load: float = 0.8, lanes=(2, 4)) -> dict:
+                    max_active: int = 64, load: float = 0.8, lanes=(2, 8, True)) -> dict:
     """The served form against the plain one on the same requests (the served configuration's mix).
 
     1. capacity: every request queued at t = 0 through the continuous-batching server;
@@ -201,7 +201,8 @@ def served_vs_plain(n_requests: int, seed: int = 0, max_steps: int = 400, hbm_gb
 def run_served(args) -> dict:
     """Open-loop Poisson stream through the continuous-batching server, against the plain path."""
     out = served_vs_plain(args.requests, seed=args.seed, max_steps=args.max_steps, hbm_gb=args.hbm_gb,
-                          max_active=args.max_active, load=args.load, lanes=(args.lanes_svi, args.lanes_curvature))
+                          max_active=args.max_active, load=args.load,
+                          lanes=(args.lanes_svi, args.lanes_curvature, not args.packed_curvature))
     return {"metric": METRIC, "value": out["stream"]["band_updates_per_s"], "unit": UNIT, "n_gpus": 1,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"served: {args.requests} Poisson requests at {args.load} x the measured "
@@ -445,7 +446,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         torch.cuda.empty_cache()
         out["served"] = served_vs_plain(args.served_requests, seed=args.seed, max_steps=args.max_steps,
                                         hbm_gb=args.hbm_gb, max_active=args.max_active, load=args.load,
-                                        lanes=(args.lanes_svi, args.lanes_curvature))
+                                        lanes=(args.lanes_svi, args.lanes_curvature, not args.packed_curvature))
     return out
 
 
@@ -607,7 +608,9 @@ def main() -> int:
     ap.add_argument("--max-active", type=int, default=64)
     ap.add_argument("--max-steps", type=int, default=400)
     ap.add_argument("--lanes-svi", type=int, default=2, help="batched/served: lanes of SVI-law jobs")
-    ap.add_argument("--lanes-curvature", type=int, default=4, help="batched/served: lanes of curvature-law jobs")
+    ap.add_argument("--lanes-curvature", type=int, default=8, help="batched/served: lanes of curvature-law jobs")
+    ap.add_argument("--packed-curvature", action="store_true",
+                    help="batched/served: curvature lanes with packed launches instead of each job's own graph")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -192,12 +192,14 @@ class _Lane:
 
 class LaneScheduler:
     """Runs many jobs as a few lanes: each lane a group of jobs of one law kind advanced a step
-    at a time with one launch per pass (:class:`~svierosion_gb300.group.GroupStep`) on its own
-    stream.  The lanes are not in lockstep: while the GPU runs one lane's step, the host finishes
+    at a time on its own stream.  SVI lanes use one launch per pass over all their jobs' band
+    tiles (:class:`~svierosion_gb300.group.GroupStep`); curvature lanes by default replay each
+    job's own step graph back to back (:class:`~svierosion_gb300.group.SerialStep`), which keeps
+    one job's data in L2 while its kernels run (``serial_curvature=False``: packed launches).  The lanes are not in lockstep: while the GPU runs one lane's step, the host finishes
     another's (statistics, stop tests, regula falsi, reinitialisation) and relaunches it at once,
     so host work and GPU work overlap.  A job's arithmetic is its own throughout."""
 
-    def __init__(self, device, lanes_svi: int = 2, lanes_curvature: int = 4, serial_curvature: bool = False):
+    def __init__(self, device, lanes_svi: int = 2, lanes_curvature: int = 8, serial_curvature: bool = True):
         self.lanes = [_Lane(device, True) for _ in range(lanes_svi)] + \
                      [_Lane(device, False, serial_curvature) for _ in range(lanes_curvature)]
 
@@ -264,8 +266,8 @@ class LaneScheduler:
 class BatchedErosion:
     """Advance many solids together; each stops independently (spec batched form)."""
 
-    def __init__(self, jobs: list[ErosionJob], lanes_svi: int = 2, lanes_curvature: int = 4,
-                 serial_curvature: bool = False):
+    def __init__(self, jobs: list[ErosionJob], lanes_svi: int = 2, lanes_curvature: int = 8,
+                 serial_curvature: bool = True):
         self.jobs = list(jobs)
         self.lanes = (lanes_svi, lanes_curvature, serial_curvature)
 
@@ -309,8 +311,8 @@ class ErosionServer:
     """Continuous batching of erosion requests under an HBM budget."""
 
     def __init__(self, hbm_budget_bytes: int = 150 << 30, max_active: int = 64, device=None, lanes_svi: int = 2,
-                 lanes_curvature: int = 4):
-        self.lanes = (lanes_svi, lanes_curvature)
+                 lanes_curvature: int = 8, serial_curvature: bool = True):
+        self.lanes = (lanes_svi, lanes_curvature, serial_curvature)
         self.budget = int(hbm_budget_bytes)
         self.max_active = int(max_active)
         self.device = get_device(device)
