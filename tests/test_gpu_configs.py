@@ -113,6 +113,12 @@ def test_precision_config_matches_reference_and_fp64(golden, name):
     assert float(np.abs(fr[:k] - f64[:k]).max()) <= 2e-5
     hd64 = hausdorff_cells(final, shell_decode(d64, "", shape, h, far))
     assert hd64 <= 0.5, hd64
+    dn64 = float(np.abs(n_gpu.astype(np.float64) - d64["n_sample"]).max()) if n_gpu is not None else float("nan")
+    # the measured figures (shown with pytest -s)
+    print(f"\n[{name}] grid {shape}: steps {res.steps} (reference {int(d['steps'])}, fp64 {int(d64['steps'])}); "
+          f"max |dN_r| vs fp64 {dn64:.2e}; max |d fraction| vs reference "
+          f"{float(np.abs(fr - d['hist_fraction']).max()):.1e}, vs fp64 {float(np.abs(fr[:k] - f64[:k]).max()):.1e}; "
+          f"Hausdorff vs reference {hd:.4f} cells, vs fp64 {hd64:.4f} cells")
 
 
 def test_scan_config_first_stage_matches_reference(golden):
