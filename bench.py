@@ -304,6 +304,13 @@ def algorithmic_bytes(shape, band: int, work: int = 0) -> dict:
     }
 
 
+def svi_forms(shape) -> dict:
+    """The convolution passes' launch forms on this grid (tuned at the first convolution or the
+    fixed rule; every form gives the same bits)."""
+    from svierosion_gb300 import svi
+    return svi.fft_choice(shape)
+
+
 def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     import torch
     import svierosion_gb300 as S
@@ -426,7 +433,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         "config": {"workload": desc, "grid": list(grid.shape), "grid_nodes": grid.size, "band_nodes": band0,
                    "band_nodes_mean_timed": int(band_mean), "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (each dense grid 148 MB; every stage streams > 0.6 GB)",
-                   "setup_s": round(t_setup, 3)},
+                   "setup_s": round(t_setup, 3),
+                   "fft_forms": svi_forms(grid.shape)},
         "roofline": roof,
         "kernels": kern,
         "kernels_pass": {"steps": args.steps, "ms_per_step": round(ms2 / args.steps, 4),

@@ -139,6 +139,9 @@ _SIGS = {
     "svie_conv_apply_masked": (I, [V, I, I, I, V, V, D, D, V, Z, V, V, V, V]),
     "svie_conv_line_flags": (I, [V, I64, I, I, I, I, V, V, V, V]),
     "svie_conv_kernel_hat": (I, [V, I, I, I, V, V]),
+    "svie_conv_tune": (I, [V, I, I, I, V, V, V, Z, I, V]),
+    "svie_conv_get_choice": (I, [I, I, I, V, V, V]),
+    "svie_conv_set_choice": (I, [I, I, I, I, I, I]),
     "svie_rfft3": (I, [V, I, I, I, V, V, V]),
     "svie_irfft3": (I, [V, I, I, I, V, V, D, D, V]),
     "svie_stage_workspace_bytes": (Z, [I64]),

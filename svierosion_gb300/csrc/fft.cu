@@ -21,13 +21,16 @@
 #include <math.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
+
 #include "common.cuh"
 
 namespace svie {
 
 constexpr int FFT_T = 256;      // threads per CTA
 constexpr int FFT_MAXST = 14;   // radix stages per axis
-constexpr int FFT_MAXN = 8192;  // longest supported axis
+constexpr int FFT_MAXN = 7168;  // longest supported axis (its one-line pass fits shared memory)
 
 struct AxisPlan {
   int n;
@@ -654,18 +657,24 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
 // butterflies of the previous.  The copies take whole 64-byte row segments:
 // the spectrum rows are padded to multiples of 8 complex values (the columns
 // past ninner are copied and transformed but never stored).  Modes 0 and 1
-// and the slab skipping of k_fft_strided (the y passes).
-template <int NT, int MINB>
+// and the slab skipping of k_fft_strided (the y passes); with KX also mode 2,
+// the x pass with the K^ product fused (the reverse-order stage twiddles
+// follow the forward ones in shared memory).  Every line goes through the
+// same stage functions as in k_fft_strided, so both forms give the same bits.
+template <int NT, int MINB, bool KX>
 __global__ void __launch_bounds__(NT, MINB) k_fft_tiles(float2* __restrict__ data, AxisPlan P, long long stride,
                                                      int ninner, long long outer_stride, int nouter, int mode,
-                                                     const uint8_t* __restrict__ slabflag, int need) {
+                                                     KGeom K, const uint8_t* __restrict__ slabflag, int need) {
   constexpr int LW = 8;
   extern __shared__ __align__(16) float2 sm[];
-  const int n = P.n, tile = LW * n;
+  const int n = P.n, tile = LW * n, nst = P.nst;
   const int ncb = (ninner + LW - 1) / LW;
   const long long ntiles = (long long)ncb * nouter;
   float2* stw = sm + 3 * tile;
   for (int e = threadIdx.x; e < n - 1; e += NT) stw[e] = __ldg(P.stw + e);
+  const float2* rstw = stw + n;
+  if (KX && mode == 2)
+    for (int e = threadIdx.x; e < n - 1; e += NT) stw[n + e] = __ldg(P.rstw + e);
   auto next = [&](long long t) {
     if (slabflag)
       while (t < ntiles && !(__ldg(slabflag + t / ncb) & need)) t += gridDim.x;
@@ -685,18 +694,43 @@ __global__ void __launch_bounds__(NT, MINB) k_fft_tiles(float2* __restrict__ dat
   long long t = next(blockIdx.x);
   if (t < ntiles) issue(t, bi);
   cp_async_commit();
+  const int Rl = radix_of(P.radices, nst - 1);
   while (t < ntiles) {
     const long long tn = next(t + gridDim.x);
     if (tn < ntiles) issue(tn, bf);
     cp_async_commit();
     cp_async_wait<1>();  // every group but the newest (the prefetch) has landed
     __syncthreads();
-    int p = 1;
-    const float2* r = run_stages<LW, LW, NT>(bi, bq, n, P.radices, 0, P.nst - 1, stw, mode == 1, p);
     const long long outer = t / ncb;
     const int c0 = (int)(t - outer * ncb) * LW;
-    run_last<LW, LW, NT>(r, n, radix_of(P.radices, P.nst - 1), stw, mode == 1 && P.nst == 1,
-                         StoreEpi{data + outer * outer_stride + c0, stride, min(LW, ninner - c0), mode == 1});
+    const int nl = min(LW, ninner - c0);
+    float2* base = data + outer * outer_stride + c0;
+    int p = 1;
+    float2* r = run_stages<LW, LW, NT>(bi, bq, n, P.radices, 0, nst - 1, stw, mode == 1, p);
+    if (!KX || mode != 2) {
+      run_last<LW, LW, NT>(r, n, Rl, stw, mode == 1 && nst == 1, StoreEpi{base, stride, nl, mode == 1});
+    } else {
+      // forward, K^ and the first inverse stage, then the rest of the inverse (as k_fft_strided)
+      const int y = (int)outer, yr = min(y, K.ny - y);
+      float2* o = (r == bi) ? bq : bi;
+      run_last<LW, LW, NT>(r, n, Rl, stw, false,
+                           KEpi<LW>{o, K.kred + (long long)yr * K.nzh + c0, (long long)(K.ny / 2 + 1) * K.nzh, n,
+                                    nl});
+      __syncthreads();
+      if (nst == 1) {
+        for (int e = threadIdx.x; e < tile; e += NT) {
+          const int k = e / LW, c = e % LW;
+          if (c < nl) {
+            const float2 v = o[e];
+            base[(long long)k * stride + c] = make_float2(v.x, -v.y);
+          }
+        }
+      } else {
+        int p2 = Rl;
+        float2* r2 = run_stages<LW, LW, NT>(o, r, n, P.rradices, 1, nst - 1, rstw, false, p2);
+        run_last<LW, LW, NT>(r2, n, radix_of(P.rradices, nst - 1), rstw, false, StoreEpi{base, stride, nl, true});
+      }
+    }
     __syncthreads();  // bi and bq are free: the next tile is bf, the one after goes to bq
     float2* tmp = bi;
     bi = bf;
@@ -944,13 +978,76 @@ static PlanLayout plan_layout(int nx, int ny, int nz) {
 // Tile shapes: z passes 16 complex lines (PS = 17) and strided passes 8 lines
 // when the two buffers and the twiddles fit in shared memory, else one line
 // per tile (axes longer than about 830 for z and 1700 for x and y).
-static bool z_wide(int n) { return tile_smem(17, n) <= TILE_SMEM_MAX; }
+// ------------------------------------------------- pass variants and choice
+// Each axis pass has a few launch forms that differ only in how lines are
+// grouped into CTAs (lines per tile, CTAs per SM, persistent or one tile per
+// CTA).  Every line goes through the same radix stages with the same twiddles,
+// so all forms give the same bits and the choice is free to depend on timing:
+//   z: 0 = 16 line pairs per CTA (3 CTAs/SM at nz ~ 250), 1 = 8 pairs,
+//      2 = one pair (axes too long for the others);
+//   y: 0 = persistent 8-line tiles with the next tile prefetched, 1 = one
+//      8-line tile per CTA, 2 = one line per CTA;
+//   x: 0 = one 8-line tile per CTA, 1 = persistent 8-line tiles, 2 = one line.
+// The fixed rule takes z 0, y 1 and x 0 where they fit: the fastest forms on
+// every grid from 100 x 75 x 60 to 448 x 336 x 245 that was timed on a GB300
+// (the persistent forms lose there: y by 3-10%, x by 3-12%).  The radix order
+// is not a choice: it changes the rounding, and results must not depend on a
+// timing.
+constexpr int FFT_NCHOICE = 3;
+
+static size_t z_smem(int c, int n) { return tile_smem(c == 0 ? 17 : (c == 1 ? 9 : 1), n); }
 // the strided passes also hold the reverse-order twiddles of the fused x pass
 static size_t strided_smem(int lw, int n) { return tile_smem(lw, n) + (size_t)n * sizeof(float2); }
-static bool strided_wide(int n) { return strided_smem(8, n) <= TILE_SMEM_MAX; }
-// the persistent 8-line pass holds three tiles and the twiddles
-static size_t tiles_smem(int n) { return (3 * 8 + 1) * (size_t)n * sizeof(float2); }
-static bool strided_tiles(int n) { return tiles_smem(n) <= TILE_SMEM_MAX; }
+// the persistent passes hold three tiles and the twiddles (the x pass both orders)
+static size_t tiles_smem(int n, bool kx) { return (3 * 8 + (kx ? 2 : 1)) * (size_t)n * sizeof(float2); }
+static size_t y_smem(int c, int n) { return c == 0 ? tiles_smem(n, false) : strided_smem(c == 1 ? 8 : 1, n); }
+static size_t x_smem(int c, int n) { return c == 1 ? tiles_smem(n, true) : strided_smem(c == 0 ? 8 : 1, n); }
+static bool fits(size_t b) { return b <= TILE_SMEM_MAX; }
+
+struct FftChoice {
+  int z, y, x;
+};
+
+// the fixed rule (above)
+static FftChoice default_choice(int nx, int ny, int nz) {
+  FftChoice c;
+  c.z = fits(z_smem(0, nz)) ? 0 : 2;
+  c.y = fits(y_smem(1, ny)) ? 1 : 2;
+  c.x = fits(x_smem(0, nx)) ? 0 : 2;
+  return c;
+}
+
+static bool choice_fits(const FftChoice& c, int nx, int ny, int nz) {
+  return c.z >= 0 && c.z < FFT_NCHOICE && c.y >= 0 && c.y < FFT_NCHOICE && c.x >= 0 && c.x < FFT_NCHOICE &&
+         fits(z_smem(c.z, nz)) && fits(y_smem(c.y, ny)) && fits(x_smem(c.x, nx));
+}
+
+// Chosen forms per (device, grid shape): set by svie_conv_tune or svie_conv_set_choice.
+struct GridKey {
+  int dev, nx, ny, nz;
+  bool operator<(const GridKey& o) const {
+    if (dev != o.dev) return dev < o.dev;
+    if (nx != o.nx) return nx < o.nx;
+    if (ny != o.ny) return ny < o.ny;
+    return nz < o.nz;
+  }
+};
+static std::mutex g_choice_mu;
+static std::map<GridKey, FftChoice> g_choice;
+
+static GridKey grid_key(int nx, int ny, int nz) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return GridKey{dev, nx, ny, nz};
+}
+
+static FftChoice choice_for(int nx, int ny, int nz, bool* tuned = nullptr) {
+  const GridKey k = grid_key(nx, ny, nz);
+  std::lock_guard<std::mutex> lock(g_choice_mu);
+  auto it = g_choice.find(k);
+  if (tuned) *tuned = it != g_choice.end();
+  return it != g_choice.end() ? it->second : default_choice(nx, ny, nz);
+}
 
 // Grid of a persistent kernel: as many CTAs as are resident at once, at most one per tile.
 static unsigned persistent_grid(const void* fn, int threads, size_t smem, long long ntiles) {
@@ -968,10 +1065,12 @@ static int ensure_smem_attr() {
   if (cudaGetDevice(&dev) != cudaSuccess) return SVIE_ERR_LAUNCH;
   if (dev < 64 && (done >> dev) & 1ULL) return SVIE_OK;
   const int bytes = 227 * 1024;
-  const void* fns[] = {(const void*)k_fft_z_r2c<16, 17>, (const void*)k_fft_z_r2c<1, 1>,
-                       (const void*)k_fft_z_c2r<16, 17>, (const void*)k_fft_z_c2r<1, 1>,
-                       (const void*)k_fft_strided<8, 4>,  (const void*)k_fft_strided<8, 3>,
-                       (const void*)k_fft_strided<1, 1>,  (const void*)k_fft_tiles<256, 3>};
+  const void* fns[] = {(const void*)k_fft_z_r2c<16, 17>, (const void*)k_fft_z_r2c<8, 9>,
+                       (const void*)k_fft_z_r2c<1, 1>,   (const void*)k_fft_z_c2r<16, 17>,
+                       (const void*)k_fft_z_c2r<8, 9>,   (const void*)k_fft_z_c2r<1, 1>,
+                       (const void*)k_fft_strided<8, 4>, (const void*)k_fft_strided<8, 3>,
+                       (const void*)k_fft_strided<1, 1>, (const void*)k_fft_tiles<256, 3, false>,
+                       (const void*)k_fft_tiles<256, 2, true>};
   cudaError_t e1 = cudaSuccess;
   for (const void* f : fns)
     if (e1 == cudaSuccess) e1 = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -1010,56 +1109,82 @@ static int make_plans(const void* plan, int nx, int ny, int nz, Plans* P) {
   return SVIE_OK;
 }
 
+template <int LW, int PS>
+static void launch_z_as(const Plans& P, long long nlines, int nzp, const float* f, float2* spec, float* out,
+                        bool fwd, float alpha, float beta, cudaStream_t s, const uint8_t* lineflag) {
+  const size_t smem = tile_smem(PS, P.z.n);
+  const long long nb = (nlines + 2 * LW - 1) / (2 * LW);
+  if (fwd) k_fft_z_r2c<LW, PS><<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, nzp, lineflag);
+  else k_fft_z_c2r<LW, PS><<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, nzp, alpha, beta, lineflag);
+}
+
 static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, float2* spec, float* out, bool fwd,
-                     float alpha, float beta, cudaStream_t s, const uint8_t* lineflag = nullptr) {
+                     float alpha, float beta, cudaStream_t s, const uint8_t* lineflag, int c) {
   const long long nlines = (long long)nx * ny;
   const int nzp = padded_nzh(nz);
-  if (z_wide(nz)) {
-    const size_t smem = tile_smem(17, nz);
-    const long long nb = (nlines + 31) / 32;
-    if (fwd) k_fft_z_r2c<16, 17><<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, nzp, lineflag);
-    else k_fft_z_c2r<16, 17><<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, nzp, alpha, beta, lineflag);
-  } else {
-    const size_t smem = tile_smem(1, nz);
-    const long long nb = (nlines + 1) / 2;
-    if (fwd) k_fft_z_r2c<1, 1><<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, nzp, lineflag);
-    else k_fft_z_c2r<1, 1><<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, nzp, alpha, beta, lineflag);
-  }
+  if (c == 0) launch_z_as<16, 17>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag);
+  else if (c == 1) launch_z_as<8, 9>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag);
+  else launch_z_as<1, 1>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag);
 }
 
 // y lines: outer index x, line index kz, element stride nzp.
 static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s,
-                     const uint8_t* slabflag = nullptr) {
+                     const uint8_t* slabflag, int c) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const KGeom K{nullptr, ny, nzh};
   const int need = mode == 1 ? 2 : 1;
   const long long ostr = (long long)ny * nzp;
-  if (strided_tiles(ny)) {
-    const size_t smem = tiles_smem(ny);
+  const size_t smem = y_smem(c, ny);
+  if (c == 0) {
     const long long ntiles = (long long)((nzh + 7) / 8) * nx;
-    k_fft_tiles<256, 3><<<persistent_grid((const void*)k_fft_tiles<256, 3>, 256, smem, ntiles), 256, smem, s>>>(
-        spec, P.y, nzp, nzh, ostr, nx, mode, slabflag, need);
-  } else if (strided_wide(ny)) {
+    const void* fn = (const void*)k_fft_tiles<256, 3, false>;
+    k_fft_tiles<256, 3, false><<<persistent_grid(fn, 256, smem, ntiles), 256, smem, s>>>(
+        spec, P.y, nzp, nzh, ostr, nx, mode, K, slabflag, need);
+  } else if (c == 1) {
     dim3 g((unsigned)((nzh + 7) / 8), (unsigned)nx);
-    k_fft_strided<8, 4><<<g, FFT_T, strided_smem(8, ny), s>>>(spec, P.y, nzp, nzh, ostr, mode, K, slabflag, need);
+    k_fft_strided<8, 4><<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, ostr, mode, K, slabflag, need);
   } else {
     dim3 g((unsigned)nzh, (unsigned)nx);
-    k_fft_strided<1, 1><<<g, FFT_T, strided_smem(1, ny), s>>>(spec, P.y, nzp, nzh, ostr, mode, K, slabflag, need);
+    k_fft_strided<1, 1><<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, ostr, mode, K, slabflag, need);
   }
 }
 
 // x lines: outer index y, line index kz, element stride ny * nzp.
-static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s) {
+static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s, int c) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const KGeom K{P.kred, ny, nzh};
   const long long lstr = (long long)ny * nzp;
-  if (strided_wide(nx)) {
+  const size_t smem = x_smem(c, nx);
+  if (c == 1) {
+    const long long ntiles = (long long)((nzh + 7) / 8) * ny;
+    const void* fn = (const void*)k_fft_tiles<256, 2, true>;
+    k_fft_tiles<256, 2, true><<<persistent_grid(fn, 256, smem, ntiles), 256, smem, s>>>(
+        spec, P.x, lstr, nzh, nzp, ny, mode, K, nullptr, 0);
+  } else if (c == 0) {
     dim3 g((unsigned)((nzh + 7) / 8), (unsigned)ny);
-    k_fft_strided<8, 3><<<g, FFT_T, strided_smem(8, nx), s>>>(spec, P.x, lstr, nzh, nzp, mode, K, nullptr, 0);
+    k_fft_strided<8, 3><<<g, FFT_T, smem, s>>>(spec, P.x, lstr, nzh, nzp, mode, K, nullptr, 0);
   } else {
     dim3 g((unsigned)nzh, (unsigned)ny);
-    k_fft_strided<1, 1><<<g, FFT_T, strided_smem(1, nx), s>>>(spec, P.x, lstr, nzh, nzp, mode, K, nullptr, 0);
+    k_fft_strided<1, 1><<<g, FFT_T, smem, s>>>(spec, P.x, lstr, nzh, nzp, mode, K, nullptr, 0);
   }
+}
+
+// Times one pass form: `reps` launches of `fn` after one untimed launch, the
+// shortest kept (ms; a negative value when a launch failed).
+template <class F>
+static float time_form(F fn, int reps, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1) {
+  fn();
+  float best = -1.0f;
+  for (int r = 0; r < reps; ++r) {
+    cudaEventRecord(e0, s);
+    fn();
+    cudaEventRecord(e1, s);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return -1.0f;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (best < 0.0f || ms < best) best = ms;
+  }
+  return cudaGetLastError() == cudaSuccess ? best : -1.0f;
 }
 
 static void gauss_legendre(int n, double* x, double* w) {
@@ -1187,11 +1312,12 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
   float2* spec = (float2*)ws;
-  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s);
-  launch_y(P, nx, ny, nz, spec, 0, s);
-  launch_x(P, nx, ny, nz, spec, 2, s);
-  launch_y(P, nx, ny, nz, spec, 1, s);
-  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s);
+  const FftChoice c = choice_for(nx, ny, nz);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z);
+  launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c.y);
+  launch_x(P, nx, ny, nz, spec, 2, s, c.x);
+  launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c.y);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z);
   return launch_status("svie_conv_apply", 5);
 }
 
@@ -1213,18 +1339,118 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
   cudaStream_t s = (cudaStream_t)stream;
   float2* spec = (float2*)ws;
   cudaEvent_t* ev = (cudaEvent_t*)events;
+  const FftChoice c = choice_for(nx, ny, nz);
   if (ev) cudaEventRecord(ev[0], s);
-  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, lineflag);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, lineflag, c.z);
   if (ev) cudaEventRecord(ev[1], s);
-  launch_y(P, nx, ny, nz, spec, 0, s, slabflag);
+  launch_y(P, nx, ny, nz, spec, 0, s, slabflag, c.y);
   if (ev) cudaEventRecord(ev[2], s);
-  launch_x(P, nx, ny, nz, spec, 2, s);
+  launch_x(P, nx, ny, nz, spec, 2, s, c.x);
   if (ev) cudaEventRecord(ev[3], s);
-  launch_y(P, nx, ny, nz, spec, 1, s, slabflag);
+  launch_y(P, nx, ny, nz, spec, 1, s, slabflag, c.y);
   if (ev) cudaEventRecord(ev[4], s);
-  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag, c.z);
   if (ev) cudaEventRecord(ev[5], s);
   return launch_status("svie_conv_apply_masked", 5);
+}
+
+int svie_conv_get_choice(int nx, int ny, int nz, int* z, int* y, int* x) {
+  bool tuned = false;
+  const FftChoice c = choice_for(nx, ny, nz, &tuned);
+  if (z) *z = c.z;
+  if (y) *y = c.y;
+  if (x) *x = c.x;
+  return tuned ? 1 : 0;
+}
+
+int svie_conv_set_choice(int nx, int ny, int nz, int z, int y, int x) {
+  const GridKey k = grid_key(nx, ny, nz);
+  if (z < 0 || y < 0 || x < 0) {
+    std::lock_guard<std::mutex> lock(g_choice_mu);
+    g_choice.erase(k);
+    return SVIE_OK;
+  }
+  const FftChoice c{z, y, x};
+  if (!choice_fits(c, nx, ny, nz)) {
+    set_error("svie_conv_set_choice: forms (%d, %d, %d) do not exist or do not fit shared memory for %d x %d x %d",
+              z, y, x, nx, ny, nz);
+    return SVIE_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lock(g_choice_mu);
+  g_choice[k] = c;
+  return SVIE_OK;
+}
+
+int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, float* out, void* ws, size_t ws_bytes,
+                   int reps, void* stream) {
+  Plans P;
+  int st = make_plans(plan, nx, ny, nz, &P);
+  if (st) return st;
+  if (!f || !out || reps < 1 || reps > 100) {
+    set_error("svie_conv_tune: null input/output or reps outside 1..100");
+    return SVIE_ERR_ARG;
+  }
+  if (!ws || ws_bytes < svie_conv_workspace_bytes(nx, ny, nz) || ((uintptr_t)ws & 15)) {
+    set_error("svie_conv_tune: workspace too small or not 16-byte aligned");
+    return SVIE_ERR_WORKSPACE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    set_error("svie_conv_tune: the stream is being captured (tuning synchronises it)");
+    return SVIE_ERR_ARG;
+  }
+  if ((st = ensure_smem_attr())) return st;
+  float2* spec = (float2*)ws;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    set_error("svie_conv_tune: cudaEventCreate failed");
+    return SVIE_ERR_LAUNCH;
+  }
+  FftChoice best = default_choice(nx, ny, nz);
+  float tz = -1.f, ty = -1.f, tx = -1.f;
+  bool failed = false;
+  int launched = 1;
+  // the spectrum of f in the workspace first, so that every form transforms real data
+  const FftChoice d = best;
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, d.z);
+  for (int c = 0; c < FFT_NCHOICE && !failed; ++c) {
+    if (fits(z_smem(c, nz))) {  // forward and inverse z
+      const float t = time_form([&] {
+        launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c);
+        launch_z(P, nx, ny, nz, nullptr, spec, out, false, 1.f, 0.f, s, nullptr, c);
+        launched += 2;
+      }, reps, s, e0, e1);
+      if (t < 0.f) failed = true;
+      else if (tz < 0.f || t < tz) { tz = t; best.z = c; }
+    }
+    if (!failed && fits(y_smem(c, ny))) {  // forward and inverse y
+      const float t = time_form([&] {
+        launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c);
+        launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c);
+        launched += 2;
+      }, reps, s, e0, e1);
+      if (t < 0.f) failed = true;
+      else if (ty < 0.f || t < ty) { ty = t; best.y = c; }
+    }
+    if (!failed && fits(x_smem(c, nx))) {  // the fused x pass
+      const float t = time_form([&] {
+        launch_x(P, nx, ny, nz, spec, 2, s, c);
+        launched += 1;
+      }, reps, s, e0, e1);
+      if (t < 0.f) failed = true;
+      else if (tx < 0.f || t < tx) { tx = t; best.x = c; }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (failed) return launch_status("svie_conv_tune", launched);
+  {
+    std::lock_guard<std::mutex> lock(g_choice_mu);
+    g_choice[grid_key(nx, ny, nz)] = best;
+  }
+  return launch_status("svie_conv_tune", launched);
 }
 
 int svie_conv_line_flags(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, uint8_t* lineflag,
@@ -1266,9 +1492,10 @@ int svie_rfft3(const void* plan, int nx, int ny, int nz, const float* f, void* s
   }
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s);
-  launch_y(P, nx, ny, nz, (float2*)spec, 0, s);
-  launch_x(P, nx, ny, nz, (float2*)spec, 0, s);
+  const FftChoice c = choice_for(nx, ny, nz);
+  launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z);
+  launch_y(P, nx, ny, nz, (float2*)spec, 0, s, nullptr, c.y);
+  launch_x(P, nx, ny, nz, (float2*)spec, 0, s, c.x);
   return launch_status("svie_rfft3", 3);
 }
 
@@ -1283,9 +1510,10 @@ int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out
   }
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
-  launch_x(P, nx, ny, nz, (float2*)spec, 1, s);
-  launch_y(P, nx, ny, nz, (float2*)spec, 1, s);
-  launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s);
+  const FftChoice c = choice_for(nx, ny, nz);
+  launch_x(P, nx, ny, nz, (float2*)spec, 1, s, c.x);
+  launch_y(P, nx, ny, nz, (float2*)spec, 1, s, nullptr, c.y);
+  launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z);
   return launch_status("svie_irfft3", 3);
 }
 

@@ -9,6 +9,7 @@ spectrum multiply fused into the x pass (csrc/fft.cu).
 from __future__ import annotations
 
 import math
+import os
 from collections import OrderedDict
 
 import numpy as np
@@ -55,6 +56,43 @@ def _ball_weights_device(radius, spacing, quad, device) -> torch.Tensor:
     return w
 
 
+# grid shapes whose pass forms were timed in this process, per device (svie_conv_tune)
+_TUNED: set = set()
+TUNE_REPS = 2
+# Tuning costs a few milliseconds once per shape (8.6 ms at 448 x 336 x 245, about 1 ms at
+# 160 x 120 x 90): by default only grids of at least this many nodes are tuned, where that is
+# a small part of one solve; smaller ones keep the fixed rule.
+TUNE_MIN_NODES = 1 << 23
+
+
+def autotune_enabled(nodes: int | None = None) -> bool:
+    """Whether a grid of `nodes` nodes is tuned at its first convolution: SVIE_FFT_TUNE=0 never,
+    =all always, otherwise (default) from TUNE_MIN_NODES nodes up."""
+    mode = os.environ.get("SVIE_FFT_TUNE", "1")
+    if mode == "0":
+        return False
+    return mode == "all" or nodes is None or nodes >= TUNE_MIN_NODES
+
+
+def fft_choice(shape) -> dict:
+    """The launch forms the convolution passes use on `shape` (indices as in svie_conv_get_choice)
+    and whether they were tuned or set."""
+    z, y, x = (nat.ctypes.c_int() for _ in range(3))
+    tuned = nat.lib().svie_conv_get_choice(*(int(n) for n in shape), nat.ctypes.byref(z), nat.ctypes.byref(y),
+                                           nat.ctypes.byref(x))
+    return {"z": z.value, "y": y.value, "x": x.value, "tuned": bool(tuned)}
+
+
+def set_fft_choice(shape, z: int, y: int, x: int, device=None) -> None:
+    """Force the pass forms on `shape` (negative values return to tuning at the next first use)."""
+    nat.call("svie_conv_set_choice", *(int(n) for n in shape), int(z), int(y), int(x))
+    key = (torch.device(get_device(device)).index, tuple(int(n) for n in shape))
+    if z < 0 or y < 0 or x < 0:
+        _TUNED.discard(key)
+    else:
+        _TUNED.add(key)
+
+
 class BallConvolution:
     """Cached kernel spectrum on a grid; evaluates interior ball volumes (svi.py:58-93)."""
 
@@ -70,7 +108,7 @@ class BallConvolution:
             raise ValueError("ball kernel larger than the grid")
         L = nat.lib()
         if not all(L.svie_conv_supported(int(n)) for n in grid.shape):
-            raise ValueError(f"grid {grid.shape}: every dimension must be 2^a 3^b 5^c 7^d and <= 8192 "
+            raise ValueError(f"grid {grid.shape}: every dimension must be 2^a 3^b 5^c 7^d and <= 7168 "
                              "(use Grid.around(..., fast=True))")
         nx, ny, nz = grid.shape
         self.plan = torch.empty(L.svie_conv_plan_bytes(nx, ny, nz), dtype=torch.uint8, device=self.device)
@@ -105,6 +143,7 @@ class BallConvolution:
         if f.dtype != torch.float32 or not f.is_contiguous():
             f = f.to(torch.float32).contiguous()
         ws = self.scratch.get("conv", self.workspace_bytes)
+        self._tune(f, out, ws)
         if events is None and flags is None:
             nat.call("svie_conv_apply", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)),
                      float(alpha), float(beta), nat.ptr(ws), ws.numel(), nat.stream())
@@ -115,6 +154,16 @@ class BallConvolution:
             nat.call("svie_conv_apply_masked", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)),
                      float(alpha), float(beta), nat.ptr(ws), ws.numel(), nat.ptr(lf), nat.ptr(sf), ev, nat.stream())
         return out
+
+    def _tune(self, f, out, ws) -> None:
+        """Time the pass forms on this grid shape once per process (not while a graph is captured)."""
+        key = (self.device.index, tuple(self.grid.shape))
+        if key in _TUNED or not autotune_enabled(self.grid.size) or torch.cuda.is_current_stream_capturing():
+            return
+        nx, ny, nz = self.grid.shape
+        nat.call("svie_conv_tune", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)), nat.ptr(ws),
+                 ws.numel(), TUNE_REPS, nat.stream())
+        _TUNED.add(key)
 
     def interior_volume(self, fractions: torch.Tensor) -> torch.Tensor:
         """Dense |B_r(x) cap Omega| (svi.py:84-88)."""

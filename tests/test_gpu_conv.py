@@ -146,3 +146,52 @@ def test_masked_convolution_matches_on_needed_lines():
     for dx in range(4):
         for dy in range(4):
             assert bool(need[base[:, 0] + dx, base[:, 1] + dy].all())
+
+
+@pytest.mark.parametrize("shape", [(40, 42, 36), (64, 48, 35), (45, 60, 49)])
+def test_every_pass_form_gives_the_same_bits(shape):
+    """The launch forms of each pass (lines per CTA, persistent or not) run the same radix stages,
+    so the convolution, the masked convolution and rfftn / irfftn are bit-identical under every
+    combination; the tuner then keeps one of them."""
+    import itertools
+    from svierosion_gb300 import _native as nat
+    rng = np.random.default_rng(sum(shape))
+    g = Grid((0.0, 0.0, 0.0), 1.0, shape)
+    f = torch.from_numpy(rng.random(shape, dtype=np.float32)).cuda()
+    conv = S.BallConvolution(g, 3.0)
+    nx, ny, nz = shape
+    lf = torch.from_numpy((rng.random(nx * ny) < 0.5).astype(np.uint8) * 3).cuda()
+    sf = torch.from_numpy(np.full(nx, 3, dtype=np.uint8)).cuda()
+
+    def run():
+        full = conv.exterior_fraction(f)
+        masked = torch.zeros(shape, device="cuda")
+        conv.exterior_fraction_into(f, masked, flags=(lf, sf))
+        spec = svi.rfftn(f, conv)
+        return full, masked, spec.clone(), svi.irfftn(spec, conv)
+
+    try:
+        ref = None
+        for z, y, x in itertools.product(range(3), repeat=3):
+            svi.set_fft_choice(shape, z, y, x)
+            assert svi.fft_choice(shape) == {"z": z, "y": y, "x": x, "tuned": True}
+            got = run()
+            if ref is None:
+                ref = got
+                continue
+            for a, b in zip(ref, got):
+                assert torch.equal(torch.view_as_real(a) if a.is_complex() else a,
+                                   torch.view_as_real(b) if b.is_complex() else b), (z, y, x)
+        # a form that does not exist is refused; clearing returns to the tuner
+        with pytest.raises(RuntimeError):
+            nat.call("svie_conv_set_choice", nx, ny, nz, 3, 0, 0)
+        svi.set_fft_choice(shape, -1, -1, -1)
+        assert not svi.fft_choice(shape)["tuned"]
+        run()
+        c = svi.fft_choice(shape)
+        assert c["tuned"] == svi.autotune_enabled(nx * ny * nz) and all(0 <= c[k] < 3 for k in "zyx")
+        for a, b in zip(ref, run()):
+            assert torch.equal(torch.view_as_real(a) if a.is_complex() else a,
+                               torch.view_as_real(b) if b.is_complex() else b)
+    finally:
+        svi.set_fft_choice(shape, -1, -1, -1)

@@ -50,6 +50,24 @@ def test_size_queries_without_gpu(lib):
     assert lib.svie_ball_half_width(0.1, 1 / 64) == 7
     assert lib.svie_conv_workspace_bytes(448, 336, 245) >= 448 * 336 * 123 * 8
     assert lib.svie_band_workspace_bytes(1 << 20) > 0
+    assert lib.svie_conv_supported(7168) == 1 and lib.svie_conv_supported(7200) == 0
+
+
+def test_fft_form_table_without_gpu(lib):
+    """The per-shape table of pass forms (host only, no launch): the fixed rule, set, refuse, clear."""
+    import ctypes
+    z, y, x = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    get = lambda *s: (lib.svie_conv_get_choice(*s, ctypes.byref(z), ctypes.byref(y), ctypes.byref(x)),
+                      z.value, y.value, x.value)
+    assert get(448, 336, 245) == (0, 0, 1, 0)
+    # an x axis too long for 8-line tiles and a z axis too long for 16 line pairs: one-line forms
+    assert get(7168, 336, 7168) == (0, 2, 1, 2)
+    assert lib.svie_conv_set_choice(448, 336, 245, 1, 2, 1) == 0
+    assert get(448, 336, 245) == (1, 1, 2, 1)
+    assert lib.svie_conv_set_choice(448, 336, 245, 0, 3, 0) != 0
+    assert lib.svie_conv_set_choice(7168, 336, 245, 0, 0, 0) != 0   # 8-line x tiles do not fit
+    assert lib.svie_conv_set_choice(448, 336, 245, -1, 0, 0) == 0
+    assert get(448, 336, 245) == (0, 0, 1, 0)
 
 
 def test_no_cpu_fallback():
