@@ -1,6 +1,7 @@
 // Error reporting and small utilities of the C ABI.
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 
 #include <atomic>
 
@@ -18,6 +19,14 @@ void set_error(const char* fmt, ...) {
   va_start(ap, fmt);
   vsnprintf(g_err, sizeof(g_err), fmt, ap);
   va_end(ap);
+}
+
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* v = getenv("SVIE_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
 }
 
 __global__ void k_set_f64(double* dst, double v) { *dst = v; }

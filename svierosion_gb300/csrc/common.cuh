@@ -13,6 +13,8 @@
 #include <stdint.h>
 #include <math.h>
 
+#include <utility>
+
 #include "../../include/svie.h"
 
 #define SVIE_DEV __device__ __forceinline__
@@ -42,6 +44,36 @@ inline int launch_status(const char* what, int n = 1) {
     return SVIE_ERR_LAUNCH;
   }
   return SVIE_OK;
+}
+
+// ------------------------------------------- programmatic dependent launch
+// A kernel launched by launch_dependent may be scheduled while the previous
+// kernel of its stream is still running (its blocks become resident as the
+// previous grid's blocks retire); it must call pdl_wait() before it reads
+// anything an earlier kernel wrote.  pdl_wait() returns once every
+// prerequisite grid has completed and its writes are visible; in a kernel
+// launched the ordinary way it returns at once.  pdl_release() lets the next
+// dependent launch be scheduled (otherwise that happens when this grid ends).
+SVIE_DEV void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+SVIE_DEV void pdl_release() { asm volatile("griddepcontrol.launch_dependents;\n" :::); }
+
+// Whether launch_dependent uses the programmatic launch (SVIE_PDL=0 turns it off).
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                   Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 inline int blocks_for(long long n, int threads, long long cap = 1LL << 30) {

@@ -387,6 +387,8 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
                                                              const int32_t* __restrict__ idx, long long m, int sx,
                                                              int sy, int sz, float h, float rh, float rhh, Geo g,
                                                              int second, int nbm) {
+  pdl_wait();  // the previous half-step's writes (and the geometry) are visible from here on
+  pdl_release();
   const float cfl = __ldg(g.cfl);
   if ((int)blockIdx.x < nbm) {
     // a contiguous run of the brick-ordered list per block: the bricks that follow one
@@ -723,9 +725,23 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
   // main blocks: one resident wave (8 per SM), each over a contiguous run of the list
   const int nb = (int)std::min<long long>((long long)blocks_for(m, RI_THREADS), 8LL * nsm);
   const int nbx = (int)std::min<long long>((long long)blocks_for(m, RI_THREADS), 8LL * nsm);
-  for (int it = 0; it < iterations; ++it) {
-    k_reinit_sweep<<<nb + nbx, RI_THREADS, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, g, 0, nb);
-    k_reinit_sweep<<<nb + nbx, RI_THREADS, 0, s>>>(phi_tmp, phi, idx, m, sx, sy, sz, h, rh, rhh, g, 1, nb);
+  // every half-step after the first is a dependent launch: its blocks are scheduled while the
+  // previous half-step drains and wait in the kernel for its completion
+  const dim3 grid(nb + nbx), block(RI_THREADS);
+  cudaError_t e = cudaSuccess;
+  for (int it = 0; it < iterations && e == cudaSuccess; ++it) {
+    if (it == 0)
+      k_reinit_sweep<<<grid, block, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, g, 0, nb);
+    else
+      e = launch_dependent(k_reinit_sweep, grid, block, 0, s, (const float*)phi, phi_tmp, idx, (long long)m, (int)sx,
+                           (int)sy, (int)sz, h, rh, rhh, g, 0, nb);
+    if (e == cudaSuccess)
+      e = launch_dependent(k_reinit_sweep, grid, block, 0, s, (const float*)phi_tmp, phi, idx, (long long)m, (int)sx,
+                           (int)sy, (int)sz, h, rh, rhh, g, 1, nb);
+  }
+  if (e != cudaSuccess) {
+    set_error("svie_reinit_iterate: launch failed: %s", cudaGetErrorString(e));
+    return SVIE_ERR_LAUNCH;
   }
   return launch_status("svie_reinit_iterate", 2 * iterations);
 }

@@ -68,13 +68,14 @@ def extract_surface_device(ls: LevelSet, project: bool = True, max_shift: float 
     return TriMesh(v, f), world
 
 
-def sample_field(field: torch.Tensor, grid: Grid, points_world) -> np.ndarray:
-    """Tricubic interpolation of a dense grid field at world coordinates (surface.py:59-67).
+def sample_field_device(field: torch.Tensor, grid: Grid, points_world) -> torch.Tensor:
+    """Tricubic interpolation of a dense grid field at world coordinates (surface.py:59-67), as a
+    float32 tensor on the field's device.
 
     `points_world` is a host array or a float64 device tensor (n, 3); either way the index
     coordinates are (p - origin) / h in float64, rounded to float32."""
     if len(points_world) == 0:
-        return np.zeros(0)
+        return torch.zeros(0, dtype=torch.float32, device=field.device)
     if isinstance(points_world, torch.Tensor):
         n = points_world.shape[0]
         p = torch.empty((n, 3), dtype=torch.float32, device=field.device)
@@ -82,4 +83,11 @@ def sample_field(field: torch.Tensor, grid: Grid, points_world) -> np.ndarray:
                  nat.stream())
     else:
         p = torch.as_tensor(grid.to_index(points_world), dtype=torch.float32, device=field.device)
-    return nat.d2h(tricubic(field.reshape(-1), grid.shape, p)).astype(np.float64)
+    return tricubic(field.reshape(-1), grid.shape, p)
+
+
+def sample_field(field: torch.Tensor, grid: Grid, points_world) -> np.ndarray:
+    """sample_field_device read back as a float64 host array."""
+    if len(points_world) == 0:
+        return np.zeros(0)
+    return nat.d2h(sample_field_device(field, grid, points_world)).astype(np.float64)
