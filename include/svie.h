@@ -291,18 +291,22 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
 /* Launch forms of the passes.  Each pass has up to three forms that group the
  * lines into CTAs differently (z: 16, 8 or 1 line pairs per CTA; y: persistent
  * 8-line tiles, one 8-line tile or one line per CTA; x: one 8-line tile,
- * persistent 8-line tiles or one line per CTA).  All forms of a pass run the
- * same radix stages and give the same bits, so the choice only moves time.
- * svie_conv_tune times every form that fits shared memory on this grid shape
- * (`reps` timed launches after one untimed one, shortest kept; f is
- * transformed, out and ws are overwritten; the stream is synchronised, so not
- * while it is being captured) and keeps the fastest per (device, nx, ny, nz)
- * for every later call on that shape.  svie_conv_get_choice returns 1 and the
- * kept forms when the shape was tuned or set, else 0 and the fixed rule's
- * forms (z 16 line pairs, y one 8-line tile, x one 8-line tile, where they fit); svie_conv_set_choice sets them (SVIE_ERR_ARG
- * for a form that does not exist or fit), a negative value clears the entry.
- * Replaces nothing in the reference, whose transforms are torch.fft calls
- * (svi.py:84-93). */
+ * persistent 8-line tiles or one line per CTA).  All forms run the same radix
+ * stages; the z forms give the same bits, and so do the 8-line forms of y and
+ * x, while the one-line y and x forms (2) may differ from those in the last
+ * bit.
+ * svie_conv_tune times the forms that fit shared memory on this grid shape,
+ * the one-line y and x forms only where no 8-line form fits, so that a tuned
+ * shape gives the fixed rule's bits (`reps` timed launches after one untimed
+ * one, shortest kept; f is transformed, out and ws are overwritten; the
+ * stream is synchronised, so not while it is being captured).  It keeps the
+ * fastest forms per (device, nx, ny, nz) for every later call on that shape.
+ * svie_conv_get_choice returns 1 and the kept forms when the shape was tuned
+ * or set, else 0 and the fixed rule's forms (z 16 line pairs, y and x one
+ * 8-line tile per CTA, where they fit).  svie_conv_set_choice sets them
+ * (SVIE_ERR_ARG for a form that does not exist or fit); a negative value
+ * clears the entry.  Replaces nothing in the reference, whose transforms are
+ * torch.fft calls (svi.py:84-93). */
 int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, float* out, void* ws,
                    size_t ws_bytes, int reps, void* stream);
 int svie_conv_get_choice(int nx, int ny, int nz, int* z, int* y, int* x);

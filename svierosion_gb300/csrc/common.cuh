@@ -47,22 +47,28 @@ inline int launch_status(const char* what, int n = 1) {
 }
 
 // ------------------------------------------- programmatic dependent launch
-// A kernel launched by launch_dependent may be scheduled while the previous
-// kernel of its stream is still running (its blocks become resident as the
-// previous grid's blocks retire); it must call pdl_wait() before it reads
-// anything an earlier kernel wrote.  pdl_wait() returns once every
-// prerequisite grid has completed and its writes are visible; in a kernel
-// launched the ordinary way it returns at once.  pdl_release() lets the next
-// dependent launch be scheduled (otherwise that happens when this grid ends).
+// Within one entry point's chain of kernels (the convolution passes, the
+// reinitialisation half-steps, the volume sum), every kernel after the first
+// is launched by launch_dependent: it may be scheduled while the previous
+// kernel of the chain is still running (its blocks become resident as the
+// previous grid's blocks retire) and it calls pdl_wait() before it touches
+// memory.  pdl_wait() returns once the previous grid has completed and its
+// writes are visible; in a kernel launched the ordinary way it returns at
+// once.  pdl_release() lets the next dependent launch be scheduled (otherwise
+// that happens when this grid ends).  The first kernel of a chain is launched
+// the ordinary way, so whatever the caller queued before the call (kernels,
+// copies, event waits, other libraries' work) completes before it starts.
 SVIE_DEV void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 SVIE_DEV void pdl_release() { asm volatile("griddepcontrol.launch_dependents;\n" :::); }
 
 // Whether launch_dependent uses the programmatic launch (SVIE_PDL=0 turns it off).
 bool pdl_enabled();
 
+// `chained`: the previous operation on the stream is the previous kernel of
+// this entry point's own chain (false: an ordinary launch).
 template <typename... KArgs, typename... Args>
-inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                                   Args&&... args) {
+inline cudaError_t launch_dependent(bool chained, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                   cudaStream_t s, Args&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -72,8 +78,19 @@ inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 bl
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cfg.numAttrs = chained && pdl_enabled() ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// launch_status for entry points whose launches went through launch_dependent
+// (their first failure in `e`).
+inline int dependent_status(cudaError_t e, const char* what, int n = 1) {
+  if (e != cudaSuccess) {
+    note_launches(n);
+    set_error("%s: launch failed: %s", what, cudaGetErrorString(e));
+    return SVIE_ERR_LAUNCH;
+  }
+  return launch_status(what, n);
 }
 
 inline int blocks_for(long long n, int threads, long long cap = 1LL << 30) {

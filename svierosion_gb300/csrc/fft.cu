@@ -408,6 +408,8 @@ template <int LW, int PS>
 __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ in, float2* __restrict__ out,
                                                      AxisPlan P, long long nlines, int nzp,
                                                      const uint8_t* __restrict__ lineflag) {
+  pdl_wait();
+  pdl_release();
   extern __shared__ float2 sm[];
   const int n = P.n, nh = n / 2 + 1;
   float2* sa = sm;
@@ -489,6 +491,8 @@ template <int LW, int PS>
 __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ in, float* __restrict__ out,
                                                      AxisPlan P, long long nlines, int nzp, float alpha, float beta,
                                                      const uint8_t* __restrict__ lineflag) {
+  pdl_wait();
+  pdl_release();
   extern __shared__ float2 sm[];
   const int n = P.n;
   float2* sa = sm;
@@ -589,6 +593,8 @@ template <int LW, int MINB>
 __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict__ data, AxisPlan P, long long stride,
                                                        int ninner, long long outer_stride, int mode, KGeom K,
                                                        const uint8_t* __restrict__ slabflag, int need) {
+  pdl_wait();
+  pdl_release();
   if (slabflag && !(__ldg(slabflag + blockIdx.y) & need)) return;
   extern __shared__ __align__(16) float2 sm[];
   constexpr int KS = FFT_T / LW;  // rows per sweep of the CTA
@@ -665,6 +671,8 @@ template <int NT, int MINB, bool KX>
 __global__ void __launch_bounds__(NT, MINB) k_fft_tiles(float2* __restrict__ data, AxisPlan P, long long stride,
                                                      int ninner, long long outer_stride, int nouter, int mode,
                                                      KGeom K, const uint8_t* __restrict__ slabflag, int need) {
+  pdl_wait();
+  pdl_release();
   constexpr int LW = 8;
   extern __shared__ __align__(16) float2 sm[];
   const int n = P.n, tile = LW * n, nst = P.nst;
@@ -979,10 +987,15 @@ static PlanLayout plan_layout(int nx, int ny, int nz) {
 // when the two buffers and the twiddles fit in shared memory, else one line
 // per tile (axes longer than about 830 for z and 1700 for x and y).
 // ------------------------------------------------- pass variants and choice
-// Each axis pass has a few launch forms that differ only in how lines are
-// grouped into CTAs (lines per tile, CTAs per SM, persistent or one tile per
-// CTA).  Every line goes through the same radix stages with the same twiddles,
-// so all forms give the same bits and the choice is free to depend on timing:
+// Each axis pass has a few launch forms that differ in how lines are grouped
+// into CTAs (lines per tile, CTAs per SM, persistent or one tile per CTA).
+// Every line goes through the same radix stages with the same twiddles.  The
+// forms of one code family give the same bits: the z forms; the 8-line forms
+// of y and x (0 and 1); the one-line forms of y and x (2), which are compiled
+// apart from the 8-line ones and so may differ from them in the last bit
+// wherever the compiler fuses a multiply and an add differently.  The tuner
+// only chooses within the family the fixed rule picks for the shape, so that
+// results never depend on a timing:
 //   z: 0 = 16 line pairs per CTA (3 CTAs/SM at nz ~ 250), 1 = 8 pairs,
 //      2 = one pair (axes too long for the others);
 //   y: 0 = persistent 8-line tiles with the next tile prefetched, 1 = one
@@ -1016,6 +1029,12 @@ static FftChoice default_choice(int nx, int ny, int nz) {
   c.x = fits(x_smem(0, nx)) ? 0 : 2;
   return c;
 }
+
+// Forms the tuner may choose for an axis: those that fit and share the fixed
+// rule's code family (the one-line y and x forms only where no 8-line form fits).
+static bool tunable_z(int c, int nz) { return fits(z_smem(c, nz)); }
+static bool tunable_y(int c, int ny) { return fits(y_smem(c, ny)) && (c < 2) == fits(y_smem(1, ny)); }
+static bool tunable_x(int c, int nx) { return fits(x_smem(c, nx)) && (c < 2) == fits(x_smem(0, nx)); }
 
 static bool choice_fits(const FftChoice& c, int nx, int ny, int nz) {
   return c.z >= 0 && c.z < FFT_NCHOICE && c.y >= 0 && c.y < FFT_NCHOICE && c.x >= 0 && c.x < FFT_NCHOICE &&
@@ -1111,25 +1130,27 @@ static int make_plans(const void* plan, int nx, int ny, int nz, Plans* P) {
 
 template <int LW, int PS>
 static void launch_z_as(const Plans& P, long long nlines, int nzp, const float* f, float2* spec, float* out,
-                        bool fwd, float alpha, float beta, cudaStream_t s, const uint8_t* lineflag) {
+                        bool fwd, float alpha, float beta, cudaStream_t s, const uint8_t* lineflag, bool chained) {
   const size_t smem = tile_smem(PS, P.z.n);
-  const long long nb = (nlines + 2 * LW - 1) / (2 * LW);
-  if (fwd) k_fft_z_r2c<LW, PS><<<(unsigned)nb, FFT_T, smem, s>>>(f, spec, P.z, nlines, nzp, lineflag);
-  else k_fft_z_c2r<LW, PS><<<(unsigned)nb, FFT_T, smem, s>>>(spec, out, P.z, nlines, nzp, alpha, beta, lineflag);
+  const dim3 grid((unsigned)((nlines + 2 * LW - 1) / (2 * LW))), block(FFT_T);
+  // a failed launch is reported by the caller's launch_status (cudaGetLastError)
+  if (fwd) launch_dependent(chained, k_fft_z_r2c<LW, PS>, grid, block, smem, s, f, spec, P.z, nlines, nzp, lineflag);
+  else launch_dependent(chained, k_fft_z_c2r<LW, PS>, grid, block, smem, s, (const float2*)spec, out, P.z, nlines, nzp,
+                        alpha, beta, lineflag);
 }
 
 static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, float2* spec, float* out, bool fwd,
-                     float alpha, float beta, cudaStream_t s, const uint8_t* lineflag, int c) {
+                     float alpha, float beta, cudaStream_t s, const uint8_t* lineflag, int c, bool chained) {
   const long long nlines = (long long)nx * ny;
   const int nzp = padded_nzh(nz);
-  if (c == 0) launch_z_as<16, 17>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag);
-  else if (c == 1) launch_z_as<8, 9>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag);
-  else launch_z_as<1, 1>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag);
+  if (c == 0) launch_z_as<16, 17>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag, chained);
+  else if (c == 1) launch_z_as<8, 9>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag, chained);
+  else launch_z_as<1, 1>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag, chained);
 }
 
 // y lines: outer index x, line index kz, element stride nzp.
 static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s,
-                     const uint8_t* slabflag, int c) {
+                     const uint8_t* slabflag, int c, bool chained) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const KGeom K{nullptr, ny, nzh};
   const int need = mode == 1 ? 2 : 1;
@@ -1138,34 +1159,40 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
   if (c == 0) {
     const long long ntiles = (long long)((nzh + 7) / 8) * nx;
     const void* fn = (const void*)k_fft_tiles<256, 3, false>;
-    k_fft_tiles<256, 3, false><<<persistent_grid(fn, 256, smem, ntiles), 256, smem, s>>>(
-        spec, P.y, nzp, nzh, ostr, nx, mode, K, slabflag, need);
+    launch_dependent(chained, k_fft_tiles<256, 3, false>, dim3(persistent_grid(fn, 256, smem, ntiles)), dim3(256), smem, s,
+                     spec, P.y, (long long)nzp, nzh, ostr, nx, mode, K, slabflag, need);
   } else if (c == 1) {
-    dim3 g((unsigned)((nzh + 7) / 8), (unsigned)nx);
-    k_fft_strided<8, 4><<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, ostr, mode, K, slabflag, need);
+    const dim3 g((unsigned)((nzh + 7) / 8), (unsigned)nx);
+    launch_dependent(chained, k_fft_strided<8, 4>, g, dim3(FFT_T), smem, s, spec, P.y, (long long)nzp, nzh, ostr, mode, K,
+                     slabflag, need);
   } else {
-    dim3 g((unsigned)nzh, (unsigned)nx);
-    k_fft_strided<1, 1><<<g, FFT_T, smem, s>>>(spec, P.y, nzp, nzh, ostr, mode, K, slabflag, need);
+    const dim3 g((unsigned)nzh, (unsigned)nx);
+    launch_dependent(chained, k_fft_strided<1, 1>, g, dim3(FFT_T), smem, s, spec, P.y, (long long)nzp, nzh, ostr, mode, K,
+                     slabflag, need);
   }
 }
 
 // x lines: outer index y, line index kz, element stride ny * nzp.
-static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s, int c) {
+static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s, int c,
+                     bool chained) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const KGeom K{P.kred, ny, nzh};
   const long long lstr = (long long)ny * nzp;
   const size_t smem = x_smem(c, nx);
+  const uint8_t* none = nullptr;
   if (c == 1) {
     const long long ntiles = (long long)((nzh + 7) / 8) * ny;
     const void* fn = (const void*)k_fft_tiles<256, 2, true>;
-    k_fft_tiles<256, 2, true><<<persistent_grid(fn, 256, smem, ntiles), 256, smem, s>>>(
-        spec, P.x, lstr, nzh, nzp, ny, mode, K, nullptr, 0);
+    launch_dependent(chained, k_fft_tiles<256, 2, true>, dim3(persistent_grid(fn, 256, smem, ntiles)), dim3(256), smem, s,
+                     spec, P.x, lstr, nzh, (long long)nzp, ny, mode, K, none, 0);
   } else if (c == 0) {
-    dim3 g((unsigned)((nzh + 7) / 8), (unsigned)ny);
-    k_fft_strided<8, 3><<<g, FFT_T, smem, s>>>(spec, P.x, lstr, nzh, nzp, mode, K, nullptr, 0);
+    const dim3 g((unsigned)((nzh + 7) / 8), (unsigned)ny);
+    launch_dependent(chained, k_fft_strided<8, 3>, g, dim3(FFT_T), smem, s, spec, P.x, lstr, nzh, (long long)nzp, mode, K, none,
+                     0);
   } else {
-    dim3 g((unsigned)nzh, (unsigned)ny);
-    k_fft_strided<1, 1><<<g, FFT_T, smem, s>>>(spec, P.x, lstr, nzh, nzp, mode, K, nullptr, 0);
+    const dim3 g((unsigned)nzh, (unsigned)ny);
+    launch_dependent(chained, k_fft_strided<1, 1>, g, dim3(FFT_T), smem, s, spec, P.x, lstr, nzh, (long long)nzp, mode, K, none,
+                     0);
   }
 }
 
@@ -1313,11 +1340,11 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
   cudaStream_t s = (cudaStream_t)stream;
   float2* spec = (float2*)ws;
   const FftChoice c = choice_for(nx, ny, nz);
-  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z);
-  launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c.y);
-  launch_x(P, nx, ny, nz, spec, 2, s, c.x);
-  launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c.y);
-  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z, false);
+  launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c.y, true);
+  launch_x(P, nx, ny, nz, spec, 2, s, c.x, true);
+  launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c.y, true);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z, true);
   return launch_status("svie_conv_apply", 5);
 }
 
@@ -1340,16 +1367,18 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
   float2* spec = (float2*)ws;
   cudaEvent_t* ev = (cudaEvent_t*)events;
   const FftChoice c = choice_for(nx, ny, nz);
+  // with timing events between the passes every pass is an ordinary launch
+  const bool ch = ev == nullptr;
   if (ev) cudaEventRecord(ev[0], s);
-  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, lineflag, c.z);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, lineflag, c.z, false);
   if (ev) cudaEventRecord(ev[1], s);
-  launch_y(P, nx, ny, nz, spec, 0, s, slabflag, c.y);
+  launch_y(P, nx, ny, nz, spec, 0, s, slabflag, c.y, ch);
   if (ev) cudaEventRecord(ev[2], s);
-  launch_x(P, nx, ny, nz, spec, 2, s, c.x);
+  launch_x(P, nx, ny, nz, spec, 2, s, c.x, ch);
   if (ev) cudaEventRecord(ev[3], s);
-  launch_y(P, nx, ny, nz, spec, 1, s, slabflag, c.y);
+  launch_y(P, nx, ny, nz, spec, 1, s, slabflag, c.y, ch);
   if (ev) cudaEventRecord(ev[4], s);
-  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag, c.z);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag, c.z, ch);
   if (ev) cudaEventRecord(ev[5], s);
   return launch_status("svie_conv_apply_masked", 5);
 }
@@ -1414,29 +1443,29 @@ int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, flo
   int launched = 1;
   // the spectrum of f in the workspace first, so that every form transforms real data
   const FftChoice d = best;
-  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, d.z);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, d.z, false);
   for (int c = 0; c < FFT_NCHOICE && !failed; ++c) {
-    if (fits(z_smem(c, nz))) {  // forward and inverse z
+    if (tunable_z(c, nz)) {  // forward and inverse z
       const float t = time_form([&] {
-        launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c);
-        launch_z(P, nx, ny, nz, nullptr, spec, out, false, 1.f, 0.f, s, nullptr, c);
+        launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c, false);
+        launch_z(P, nx, ny, nz, nullptr, spec, out, false, 1.f, 0.f, s, nullptr, c, false);
         launched += 2;
       }, reps, s, e0, e1);
       if (t < 0.f) failed = true;
       else if (tz < 0.f || t < tz) { tz = t; best.z = c; }
     }
-    if (!failed && fits(y_smem(c, ny))) {  // forward and inverse y
+    if (!failed && tunable_y(c, ny)) {  // forward and inverse y
       const float t = time_form([&] {
-        launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c);
-        launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c);
+        launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c, false);
+        launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c, false);
         launched += 2;
       }, reps, s, e0, e1);
       if (t < 0.f) failed = true;
       else if (ty < 0.f || t < ty) { ty = t; best.y = c; }
     }
-    if (!failed && fits(x_smem(c, nx))) {  // the fused x pass
+    if (!failed && tunable_x(c, nx)) {  // the fused x pass
       const float t = time_form([&] {
-        launch_x(P, nx, ny, nz, spec, 2, s, c);
+        launch_x(P, nx, ny, nz, spec, 2, s, c, false);
         launched += 1;
       }, reps, s, e0, e1);
       if (t < 0.f) failed = true;
@@ -1493,9 +1522,9 @@ int svie_rfft3(const void* plan, int nx, int ny, int nz, const float* f, void* s
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const FftChoice c = choice_for(nx, ny, nz);
-  launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z);
-  launch_y(P, nx, ny, nz, (float2*)spec, 0, s, nullptr, c.y);
-  launch_x(P, nx, ny, nz, (float2*)spec, 0, s, c.x);
+  launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z, false);
+  launch_y(P, nx, ny, nz, (float2*)spec, 0, s, nullptr, c.y, true);
+  launch_x(P, nx, ny, nz, (float2*)spec, 0, s, c.x, true);
   return launch_status("svie_rfft3", 3);
 }
 
@@ -1511,9 +1540,9 @@ int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const FftChoice c = choice_for(nx, ny, nz);
-  launch_x(P, nx, ny, nz, (float2*)spec, 1, s, c.x);
-  launch_y(P, nx, ny, nz, (float2*)spec, 1, s, nullptr, c.y);
-  launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z);
+  launch_x(P, nx, ny, nz, (float2*)spec, 1, s, c.x, false);
+  launch_y(P, nx, ny, nz, (float2*)spec, 1, s, nullptr, c.y, true);
+  launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z, true);
   return launch_status("svie_irfft3", 3);
 }
 

@@ -730,14 +730,11 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
   const dim3 grid(nb + nbx), block(RI_THREADS);
   cudaError_t e = cudaSuccess;
   for (int it = 0; it < iterations && e == cudaSuccess; ++it) {
-    if (it == 0)
-      k_reinit_sweep<<<grid, block, 0, s>>>(phi, phi_tmp, idx, m, sx, sy, sz, h, rh, rhh, g, 0, nb);
-    else
-      e = launch_dependent(k_reinit_sweep, grid, block, 0, s, (const float*)phi, phi_tmp, idx, (long long)m, (int)sx,
-                           (int)sy, (int)sz, h, rh, rhh, g, 0, nb);
+    e = launch_dependent(it > 0, k_reinit_sweep, grid, block, 0, s, (const float*)phi, phi_tmp, idx, (long long)m,
+                         (int)sx, (int)sy, (int)sz, h, rh, rhh, g, 0, nb);
     if (e == cudaSuccess)
-      e = launch_dependent(k_reinit_sweep, grid, block, 0, s, (const float*)phi_tmp, phi, idx, (long long)m, (int)sx,
-                           (int)sy, (int)sz, h, rh, rhh, g, 1, nb);
+      e = launch_dependent(true, k_reinit_sweep, grid, block, 0, s, (const float*)phi_tmp, phi, idx, (long long)m,
+                           (int)sx, (int)sy, (int)sz, h, rh, rhh, g, 1, nb);
   }
   if (e != cudaSuccess) {
     set_error("svie_reinit_iterate: launch failed: %s", cudaGetErrorString(e));

@@ -133,18 +133,24 @@ __global__ void __launch_bounds__(ST_THREADS) k_volume_partial(const float* __re
                                                                long long sx, long long sy, long long sz,
                                                                float* __restrict__ occ, double* partial,
                                                                svie_stats* stats) {
+  pdl_wait();
+  pdl_release();
   volume_tile(blockIdx.x, f, idx, m, sx, sy, sz, occ, partial, stats);
 }
 
 // The per-CTA double-float partials (stored in the 8 bytes of a double each)
 // summed in a fixed order: deterministic run to run.
 __global__ void __launch_bounds__(SUM_THREADS) k_sum_partials(const double* partial, long long nb, double* out) {
+  pdl_wait();
+  pdl_release();
   __shared__ DF sh[SUM_THREADS / 32];
   const DF s = block_sum_partials_df(reinterpret_cast<const float2*>(partial), nb, sh);
   if (threadIdx.x == 0) *out = df_value(s);
 }
 
 __global__ void k_clear_flags(svie_stats* stats, unsigned int n_band) {
+  pdl_wait();
+  pdl_release();
   stats->any_neg = 0;
   stats->any_pos = 0;
   stats->n_band = n_band;
@@ -256,11 +262,14 @@ int svie_band_volume(const float* phi, const int32_t* band, int64_t m, int64_t s
   }
   cudaStream_t s = (cudaStream_t)stream;
   long long nb = (m + ST_THREADS - 1) / ST_THREADS;
-  k_clear_flags<<<1, 1, 0, s>>>(stats, (unsigned)m);
-  if (nb > 0)
-    k_volume_partial<<<(unsigned)nb, ST_THREADS, 0, s>>>(phi, band, m, sx, sy, sz, occ, (double*)ws, stats);
-  k_sum_partials<<<1, SUM_THREADS, 0, s>>>((const double*)ws, nb, &stats->fsum);
-  return launch_status("svie_band_volume", nb > 0 ? 3 : 2);
+  cudaError_t e = launch_dependent(false, k_clear_flags, dim3(1), dim3(1), 0, s, stats, (unsigned)m);
+  if (nb > 0 && e == cudaSuccess)
+    e = launch_dependent(true, k_volume_partial, dim3((unsigned)nb), dim3(ST_THREADS), 0, s, phi, band,
+                         (long long)m, (long long)sx, (long long)sy, (long long)sz, occ, (double*)ws, stats);
+  if (e == cudaSuccess)
+    e = launch_dependent(true, k_sum_partials, dim3(1), dim3(SUM_THREADS), 0, s, (const double*)ws, nb,
+                         &stats->fsum);
+  return dependent_status(e, "svie_band_volume", nb > 0 ? 3 : 2);
 }
 
 }  // extern "C"

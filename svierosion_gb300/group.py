@@ -206,11 +206,14 @@ class SerialStep:
         self._sims = []
         self._event = None
         self.steps = 0
+        self._replayed = 0   # kernels run by the members' graph replays so far
 
     def launch(self, sims) -> None:
         self._sims = list(sims)
         for sim in sims:
+            before = sim.kernel_launches
             sim._launch_step()
+            self._replayed += sim.kernel_launches - before
         if self._event is None:
             self._event = torch.cuda.Event()
         self._event.record()
@@ -230,4 +233,5 @@ class SerialStep:
 
     @property
     def kernel_launches(self) -> int:
-        return sum(sim.kernel_launches for sim in self._sims)
+        """Kernels run by the members' graph replays (direct launches are counted by the library)."""
+        return self._replayed

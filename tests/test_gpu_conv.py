@@ -150,9 +150,10 @@ def test_masked_convolution_matches_on_needed_lines():
 
 @pytest.mark.parametrize("shape", [(40, 42, 36), (64, 48, 35), (45, 60, 49)])
 def test_every_pass_form_gives_the_same_bits(shape):
-    """The launch forms of each pass (lines per CTA, persistent or not) run the same radix stages,
-    so the convolution, the masked convolution and rfftn / irfftn are bit-identical under every
-    combination; the tuner then keeps one of them."""
+    """The launch forms of each pass (lines per CTA, persistent or not) run the same radix stages.
+    Within a code family (every z form; the 8-line y and x forms) the convolution, the masked
+    convolution and rfftn / irfftn are bit-identical under every combination, and a tuned shape
+    keeps the fixed rule's family.  The one-line y and x forms agree to rounding."""
     import itertools
     from svierosion_gb300 import _native as nat
     rng = np.random.default_rng(sum(shape))
@@ -170,28 +171,39 @@ def test_every_pass_form_gives_the_same_bits(shape):
         spec = svi.rfftn(f, conv)
         return full, masked, spec.clone(), svi.irfftn(spec, conv)
 
+    def same(a, b):
+        return torch.equal(torch.view_as_real(a) if a.is_complex() else a,
+                           torch.view_as_real(b) if b.is_complex() else b)
+
     try:
-        ref = None
-        for z, y, x in itertools.product(range(3), repeat=3):
-            svi.set_fft_choice(shape, z, y, x)
-            assert svi.fft_choice(shape) == {"z": z, "y": y, "x": x, "tuned": True}
-            got = run()
-            if ref is None:
-                ref = got
-                continue
-            for a, b in zip(ref, got):
-                assert torch.equal(torch.view_as_real(a) if a.is_complex() else a,
-                                   torch.view_as_real(b) if b.is_complex() else b), (z, y, x)
-        # a form that does not exist is refused; clearing returns to the tuner
+        for family in ((0, 1), (2,)):
+            ref = None
+            for z, y, x in itertools.product(range(3), family, family):
+                svi.set_fft_choice(shape, z, y, x)
+                assert svi.fft_choice(shape) == {"z": z, "y": y, "x": x, "tuned": True}
+                got = run()
+                if ref is None:
+                    ref = got
+                    continue
+                assert all(same(a, b) for a, b in zip(ref, got)), (z, y, x)
+            if family == (0, 1):
+                ref8 = ref
+        # the one-line family agrees with the 8-line one to float32 rounding
+        for a, b in zip(ref8, ref):
+            a, b = (torch.view_as_real(t) if t.is_complex() else t for t in (a, b))
+            assert float((a - b).abs().max()) <= 1e-5 * max(float(a.abs().max()), 1.0)
+        # a form that does not exist is refused
         with pytest.raises(RuntimeError):
             nat.call("svie_conv_set_choice", nx, ny, nz, 3, 0, 0)
+        # the tuner keeps the fixed rule's family: the same bits
         svi.set_fft_choice(shape, -1, -1, -1)
         assert not svi.fft_choice(shape)["tuned"]
-        run()
+        ws = conv.scratch.get("conv", conv.workspace_bytes)
+        scratch_out = torch.empty(shape, device="cuda")
+        nat.call("svie_conv_tune", nat.ptr(conv.plan), nx, ny, nz, nat.ptr(f.reshape(-1)), nat.ptr(scratch_out),
+                 nat.ptr(ws), ws.numel(), 2, nat.stream())
         c = svi.fft_choice(shape)
-        assert c["tuned"] == svi.autotune_enabled(nx * ny * nz) and all(0 <= c[k] < 3 for k in "zyx")
-        for a, b in zip(ref, run()):
-            assert torch.equal(torch.view_as_real(a) if a.is_complex() else a,
-                               torch.view_as_real(b) if b.is_complex() else b)
+        assert c["tuned"] and c["y"] in (0, 1) and c["x"] in (0, 1) and 0 <= c["z"] < 3
+        assert all(same(a, b) for a, b in zip(ref8, run()))
     finally:
         svi.set_fft_choice(shape, -1, -1, -1)
