@@ -8,9 +8,11 @@ spectrum multiply fused into the x pass (csrc/fft.cu).
 
 from __future__ import annotations
 
+import json
 import math
 import os
 from collections import OrderedDict
+from pathlib import Path
 
 import numpy as np
 import torch
@@ -72,6 +74,50 @@ def autotune_enabled(nodes: int | None = None) -> bool:
     if mode == "0":
         return False
     return mode == "all" or nodes is None or nodes >= TUNE_MIN_NODES
+
+
+def _cache_path():
+    """SVIE_FFT_TUNE_CACHE: a JSON file of tuned pass forms kept across processes (unset: none)."""
+    p = os.environ.get("SVIE_FFT_TUNE_CACHE")
+    return Path(p) if p else None
+
+
+def _cache_key(device, shape) -> str:
+    return f"{torch.cuda.get_device_name(device)}|{'x'.join(str(int(n)) for n in shape)}"
+
+
+def load_tuned_forms(device, shape) -> bool:
+    """Set the forms of `shape` from the tuning cache file when it holds them for this GPU model."""
+    path = _cache_path()
+    if path is None or not path.exists():
+        return False
+    try:
+        forms = json.loads(path.read_text()).get(_cache_key(device, shape))
+    except (OSError, ValueError):
+        return False
+    if not forms:
+        return False
+    try:
+        set_fft_choice(shape, forms["z"], forms["y"], forms["x"], device)
+    except (nat.SvieError, KeyError, TypeError):
+        return False
+    return True
+
+
+def save_tuned_forms(device, shape) -> None:
+    """Record the forms the tuner kept for `shape` in the tuning cache file (when one is set)."""
+    path = _cache_path()
+    if path is None:
+        return
+    try:
+        table = json.loads(path.read_text()) if path.exists() else {}
+    except (OSError, ValueError):
+        table = {}
+    c = fft_choice(shape)
+    table[_cache_key(device, shape)] = {"z": c["z"], "y": c["y"], "x": c["x"]}
+    tmp = path.with_name(path.name + ".tmp")
+    tmp.write_text(json.dumps(table, indent=1, sort_keys=True) + "\n")
+    tmp.replace(path)
 
 
 def fft_choice(shape) -> dict:
@@ -156,14 +202,19 @@ class BallConvolution:
         return out
 
     def _tune(self, f, out, ws) -> None:
-        """Time the pass forms on this grid shape once per process (not while a graph is captured)."""
+        """Time the pass forms on this grid shape once per process (not while a graph is captured), or
+        take them from the tuning cache file (SVIE_FFT_TUNE_CACHE) when it holds this GPU model and
+        shape; newly tuned forms are added to that file."""
         key = (self.device.index, tuple(self.grid.shape))
         if key in _TUNED or not autotune_enabled(self.grid.size) or torch.cuda.is_current_stream_capturing():
+            return
+        if load_tuned_forms(self.device, self.grid.shape):
             return
         nx, ny, nz = self.grid.shape
         nat.call("svie_conv_tune", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)), nat.ptr(ws),
                  ws.numel(), TUNE_REPS, nat.stream())
         _TUNED.add(key)
+        save_tuned_forms(self.device, self.grid.shape)
 
     def interior_volume(self, fractions: torch.Tensor) -> torch.Tensor:
         """Dense |B_r(x) cap Omega| (svi.py:84-88)."""

@@ -1,5 +1,6 @@
 """Ball weights, the hand-written 3-D FFT and the N_r convolution."""
 
+import json
 import math
 
 import numpy as np
@@ -205,5 +206,32 @@ def test_every_pass_form_gives_the_same_bits(shape):
         c = svi.fft_choice(shape)
         assert c["tuned"] and c["y"] in (0, 1) and c["x"] in (0, 1) and 0 <= c["z"] < 3
         assert all(same(a, b) for a, b in zip(ref8, run()))
+    finally:
+        svi.set_fft_choice(shape, -1, -1, -1)
+
+
+def test_tuned_forms_are_kept_in_the_cache_file(tmp_path, monkeypatch):
+    """With SVIE_FFT_TUNE_CACHE set, a tuned shape's forms go to the file, and a later first use of
+    the shape takes them from there instead of timing the forms again."""
+    from svierosion_gb300 import _native as nat
+    shape = (48, 40, 36)
+    cache = tmp_path / "forms.json"
+    monkeypatch.setenv("SVIE_FFT_TUNE", "all")
+    monkeypatch.setenv("SVIE_FFT_TUNE_CACHE", str(cache))
+    g = Grid((0.0, 0.0, 0.0), 1.0, shape)
+    f = torch.rand(shape, device="cuda")
+    conv = S.BallConvolution(g, 3.0)
+    try:
+        svi.set_fft_choice(shape, -1, -1, -1)
+        conv.exterior_fraction(f)
+        tuned = svi.fft_choice(shape)
+        assert tuned["tuned"] and cache.exists()
+        table = json.loads(cache.read_text())
+        assert list(table.values()) == [{k: tuned[k] for k in "zyx"}]
+        svi.set_fft_choice(shape, -1, -1, -1)
+        n0 = nat.lib().svie_launch_count()
+        conv.exterior_fraction(f)
+        assert nat.lib().svie_launch_count() - n0 == 5     # the five passes only: no timing
+        assert svi.fft_choice(shape) == tuned
     finally:
         svi.set_fft_choice(shape, -1, -1, -1)

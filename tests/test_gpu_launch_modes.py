@@ -1,0 +1,48 @@
+"""Launch modes change timing only: the same solve with dependent launches off (SVIE_PDL=0) and with
+every grid shape's convolution forms tuned (SVIE_FFT_TUNE=all) gives the default run's results bit for
+bit.  Each mode runs in its own process, because both switches are read once per process."""
+
+import json
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+
+SCRIPT = r"""
+import hashlib, json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import svierosion_gb300 as S
+from svierosion_gb300 import shapes
+frag = shapes.fragment(3, seed=5)
+L = float((frag.bounds[1] - frag.bounds[0]).max())
+out = {}
+for law, kw in (("svi", dict(radius=0.08 * L, k=1, s=0, max_steps=12)), ("mean", dict(alpha=1.0, max_steps=30))):
+    res = S.erode(frag, S.ErosionParams(law=law, resolution=40, target_fraction=0.1, **kw), extract_meshes=False,
+                  keep_state=True)
+    phi = res.level_set.phi.cpu().numpy()
+    out[law] = {"fractions": [r.fraction for r in res.history], "dt": [r.dt for r in res.history],
+                "phi": hashlib.sha256(phi.tobytes()).hexdigest()}
+print(json.dumps(out))
+"""
+
+
+def _run(env_extra):
+    env = dict(os.environ, **env_extra)
+    r = subprocess.run([sys.executable, "-c", SCRIPT, str(ROOT)], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def test_dependent_launches_and_tuning_change_no_bits():
+    base = _run({"SVIE_PDL": "1", "SVIE_FFT_TUNE": "1"})
+    assert len(base["svi"]["fractions"]) == 12 and len(base["mean"]["fractions"]) == 30
+    for extra in ({"SVIE_PDL": "0"}, {"SVIE_FFT_TUNE": "all"}):
+        assert _run(extra) == base, extra
