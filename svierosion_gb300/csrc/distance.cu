@@ -249,7 +249,7 @@ SVIE_DEV void shell_cell(int r, int q, int& dx, int& dy, int& dz) {
 // stops once no unvisited piece can be closer (pieces are binned by centroid,
 // so an unvisited one is farther than r cs - rho).  The result is the exact
 // minimum over the pieces.
-__global__ void __launch_bounds__(128) k_point_distance(const float* __restrict__ pts, long long n,
+__global__ void __launch_bounds__(128, 8) k_point_distance(const float* __restrict__ pts, long long n,
                                                         const float* __restrict__ tri, const int* __restrict__ start,
                                                         const int* __restrict__ order, const float* __restrict__ box,
                                                         const unsigned int* __restrict__ occ,
@@ -288,20 +288,24 @@ __global__ void __launch_bounds__(128) k_point_distance(const float* __restrict_
   float best = INFINITY;
   for (int r = 0; r <= rmax; ++r) {
     const int ncell = r ? 24 * r * r + 2 : 1;
-    // pass 1: the first piece of every candidate cell
-    for (int q = lane; q < ncell; q += 32) {
+    // pass 1: the first piece of every candidate cell.  Bit k of `was` records whether the
+    // lane's k-th cell (q = lane + 32 k, k < 32) was a candidate: the bound only shrinks, so
+    // pass 2 need not test the others again.
+    unsigned int was = 0;
+    for (int q = lane, k = 0; q < ncell; q += 32, ++k) {
       const int c = candidate(r, q, best);
       if (c >= 0) {
+        if (k < 32) was |= 1u << k;
         const int k0 = start[c];
         if (k0 < start[c + 1]) best = fminf(best, piece_d2(k0));
       }
     }
     best = warp_min(best);
     // pass 2: the remaining pieces of the cells that are still candidates
-    for (int q0 = 0; q0 < ncell; q0 += 32) {
+    for (int q0 = 0, k = 0; q0 < ncell; q0 += 32, ++k) {
       const int q = q0 + lane;
       int k1 = 0, cnt = 0;
-      if (q < ncell) {
+      if (q < ncell && (k >= 32 || ((was >> k) & 1u))) {
         const int c = candidate(r, q, best);
         if (c >= 0) {
           k1 = start[c] + 1;
