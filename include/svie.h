@@ -309,6 +309,13 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
  * torch.fft calls (svi.py:84-93). */
 int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, float* out, void* ws,
                    size_t ws_bytes, int reps, void* stream);
+/* The 8-line y and x passes load their tiles with TMA boxes of a tensor map
+ * over the spectrum (cp.async when the axis length is odd or SVIE_TMA=0) and
+ * wait for them on an mbarrier with a bounded poll; this returns how many
+ * tiles ran out of that bound since the library was loaded (0 in a healthy
+ * run; such a tile is skipped), synchronising the device.  0xFFFFFFFF when the
+ * count could not be read. */
+unsigned int svie_conv_tma_timeouts(void);
 int svie_conv_get_choice(int nx, int ny, int nz, int* z, int* y, int* x);
 int svie_conv_set_choice(int nx, int ny, int nz, int z, int y, int x);
 /* Full complex64 half spectrum K^ (rfftn of the wrapped kernel, svi.py:76-81). */

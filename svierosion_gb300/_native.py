@@ -141,6 +141,7 @@ _SIGS = {
     "svie_conv_kernel_hat": (I, [V, I, I, I, V, V]),
     "svie_conv_tune": (I, [V, I, I, I, V, V, V, Z, I, V]),
     "svie_conv_get_choice": (I, [I, I, I, V, V, V]),
+    "svie_conv_tma_timeouts": (ctypes.c_uint, []),
     "svie_conv_set_choice": (I, [I, I, I, I, I, I]),
     "svie_rfft3": (I, [V, I, I, I, V, V, V]),
     "svie_irfft3": (I, [V, I, I, I, V, V, D, D, V]),

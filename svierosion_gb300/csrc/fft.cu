@@ -21,6 +21,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <cuda.h>  // CUtensorMap (the tensor-map encoder is reached through the runtime's driver entry point)
+
 #include <map>
 #include <mutex>
 
@@ -398,6 +400,49 @@ SVIE_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "m
 template <int N>
 SVIE_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// ------------------------------------------------ TMA tile loads (mbarrier)
+// A tile of the 8-line passes is one box or a few boxes of a 3-D tensor map
+// over the padded half spectrum (floats: 2 nzp x ny x nx), copied by the
+// tensor memory accelerator into shared memory; one thread issues the copies
+// and the CTA waits on an mbarrier for their bytes.  The wait is bounded:
+// after TMA_WAIT_LIMIT polls the CTA records a timeout in g_tma_timeouts,
+// polls once more as long for the copies in flight, and skips its tile.
+__device__ unsigned int g_tma_timeouts = 0;
+constexpr long long TMA_WAIT_LIMIT = 1LL << 22;
+
+SVIE_DEV unsigned int smem_u32(const void* p) { return (unsigned int)__cvta_generic_to_shared(p); }
+SVIE_DEV void mbar_init(uint64_t* bar, unsigned int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// the initialised barrier visible to the asynchronous proxy (the TMA unit)
+SVIE_DEV void fence_barrier_init() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+SVIE_DEV void mbar_expect_tx(uint64_t* bar, unsigned int bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+SVIE_DEV void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];\n" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+SVIE_DEV bool mbar_try_wait(uint64_t* bar, unsigned int phase) {
+  unsigned int ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+// true when the phase completed within the limit
+SVIE_DEV bool mbar_wait_bounded(uint64_t* bar, unsigned int phase) {
+  for (long long i = 0; i < TMA_WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, phase)) return true;
+  return false;
+}
+
 // ----------------------------------------------------------------- z passes
 // Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
 // A CTA takes 2 LW real lines, packed in pairs into LW complex lines (one
@@ -592,11 +637,13 @@ struct KGeom {
 template <int LW, int MINB>
 __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict__ data, AxisPlan P, long long stride,
                                                        int ninner, long long outer_stride, int mode, KGeom K,
-                                                       const uint8_t* __restrict__ slabflag, int need) {
+                                                       const uint8_t* __restrict__ slabflag, int need,
+                                                       const __grid_constant__ CUtensorMap tmap, int tma_rows,
+                                                       int tma_axis) {
   pdl_wait();
   pdl_release();
   if (slabflag && !(__ldg(slabflag + blockIdx.y) & need)) return;
-  extern __shared__ __align__(16) float2 sm[];
+  extern __shared__ __align__(128) float2 sm[];
   constexpr int KS = FFT_T / LW;  // rows per sweep of the CTA
   const int n = P.n;
   float2* sa = sm;
@@ -604,10 +651,25 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
   const int c0 = blockIdx.x * LW;
   const int nl = min(LW, ninner - c0);
   float2* base = data + (long long)blockIdx.y * outer_stride + c0;
-  // the whole tile in flight at once: asynchronous copies of the row segments
-  // (LW = 8: whole 64-byte segments of the padded rows, the columns past
-  // ninner included and never stored; LW = 1: one value per row)
-  if (LW == 8) {
+  // the whole tile in flight at once (LW = 8: whole 64-byte segments of the
+  // padded rows, the columns past ninner included and never stored; LW = 1: one
+  // value per row).  With a tensor map (tma_rows > 0, LW = 8) thread 0 issues
+  // n / tma_rows TMA boxes of tma_rows rows into the tile (rows along tensor
+  // dimension 1 for tma_axis 0, dimension 2 for tma_axis 1); otherwise every
+  // thread issues cp.async copies.
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + (2 * LW + 2) * n);
+  const bool tma = LW == 8 && tma_rows > 0;
+  if (tma) {
+    if (threadIdx.x == 0) {
+      mbar_init(bar, 1);
+      fence_barrier_init();
+      mbar_expect_tx(bar, (unsigned int)n * LW * (unsigned int)sizeof(float2));
+      for (int r0 = 0; r0 < n; r0 += tma_rows) {
+        if (tma_axis == 0) tma_load_3d(sa + r0 * LW, &tmap, 2 * c0, r0, (int)blockIdx.y, bar);
+        else tma_load_3d(sa + r0 * LW, &tmap, 2 * c0, (int)blockIdx.y, r0, bar);
+      }
+    }
+  } else if (LW == 8) {
     for (int e = threadIdx.x; e < 4 * n; e += FFT_T) {
       const int row = e >> 2, part = 2 * (e & 3);
       cp_async16(sa + row * LW + part, base + row * stride + part);
@@ -623,6 +685,15 @@ __global__ void __launch_bounds__(FFT_T, MINB) k_fft_strided(float2* __restrict_
   const bool col = c < nl;
   const long long rstep = KS * stride;
   cp_async_wait<0>();
+  if (tma) {
+    __syncthreads();  // the barrier was initialised by thread 0 before any thread polls it
+    // every thread observes the copies' completion itself; the CTA decides together
+    if (!__syncthreads_and(mbar_wait_bounded(bar, 0))) {
+      if (threadIdx.x == 0) atomicAdd(&g_tma_timeouts, 1u);
+      mbar_wait_bounded(bar, 0);  // the copies in flight, once more within the limit
+      return;
+    }
+  }
   __syncthreads();
   const int nst = P.nst;
   int p = 1;
@@ -1010,7 +1081,8 @@ constexpr int FFT_NCHOICE = 3;
 
 static size_t z_smem(int c, int n) { return tile_smem(c == 0 ? 17 : (c == 1 ? 9 : 1), n); }
 // the strided passes also hold the reverse-order twiddles of the fused x pass
-static size_t strided_smem(int lw, int n) { return tile_smem(lw, n) + (size_t)n * sizeof(float2); }
+// (and the mbarrier of the TMA tile load)
+static size_t strided_smem(int lw, int n) { return tile_smem(lw, n) + (size_t)n * sizeof(float2) + 16; }
 // the persistent passes hold three tiles and the twiddles (the x pass both orders)
 static size_t tiles_smem(int n, bool kx) { return (3 * 8 + (kx ? 2 : 1)) * (size_t)n * sizeof(float2); }
 static size_t y_smem(int c, int n) { return c == 0 ? tiles_smem(n, false) : strided_smem(c == 1 ? 8 : 1, n); }
@@ -1128,6 +1200,55 @@ static int make_plans(const void* plan, int nx, int ny, int nz, Plans* P) {
   return SVIE_OK;
 }
 
+// ------------------------------------------------------ TMA tensor maps
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static std::once_flag once;
+  static EncodeTiledFn fn = nullptr;
+  std::call_once(once, [] {
+    const char* v = getenv("SVIE_TMA");
+    if (v && v[0] == '0') return;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)f;
+  });
+  return fn;
+}
+
+// Rows per TMA box for an axis of n positions: the largest even divisor of n
+// up to 256 (a box dimension is at most 256, and an even row count keeps every
+// box's shared-memory address a multiple of 128 bytes); 0 when n is odd.
+static int tma_box_rows(int n) {
+  if (n & 1) return 0;
+  for (int r = 256; r >= 2; r -= 2)
+    if (n % r == 0) return r;
+  return 0;
+}
+
+// Tensor map over the padded half spectrum as floats (2 nzp, ny, nx), boxes of
+// 16 floats (8 complex columns) by `rows` positions along y (axis 0) or x
+// (axis 1).  Returns the rows per box, or 0 when no map could be made (then
+// the pass loads its tiles with cp.async).
+static int spectrum_map(CUtensorMap* map, float2* spec, int nx, int ny, int nzp, int n, int axis) {
+  memset(map, 0, sizeof(*map));
+  const int rows = tma_box_rows(n);
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || rows == 0 || ((uintptr_t)spec & 15)) return 0;
+  const cuuint64_t dims[3] = {(cuuint64_t)2 * nzp, (cuuint64_t)ny, (cuuint64_t)nx};
+  const cuuint64_t strides[2] = {(cuuint64_t)nzp * sizeof(float2), (cuuint64_t)ny * nzp * sizeof(float2)};
+  const cuuint32_t box[3] = {16, axis == 0 ? (cuuint32_t)rows : 1u, axis == 0 ? 1u : (cuuint32_t)rows};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, spec, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? rows : 0;
+}
+
 template <int LW, int PS>
 static void launch_z_as(const Plans& P, long long nlines, int nzp, const float* f, float2* spec, float* out,
                         bool fwd, float alpha, float beta, cudaStream_t s, const uint8_t* lineflag, bool chained) {
@@ -1163,12 +1284,16 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
                      spec, P.y, (long long)nzp, nzh, ostr, nx, mode, K, slabflag, need);
   } else if (c == 1) {
     const dim3 g((unsigned)((nzh + 7) / 8), (unsigned)nx);
+    CUtensorMap map;
+    const int rows = spectrum_map(&map, spec, nx, ny, nzp, ny, 0);
     launch_dependent(chained, k_fft_strided<8, 4>, g, dim3(FFT_T), smem, s, spec, P.y, (long long)nzp, nzh, ostr, mode, K,
-                     slabflag, need);
+                     slabflag, need, map, rows, 0);
   } else {
     const dim3 g((unsigned)nzh, (unsigned)nx);
+    CUtensorMap none;
+    memset(&none, 0, sizeof(none));
     launch_dependent(chained, k_fft_strided<1, 1>, g, dim3(FFT_T), smem, s, spec, P.y, (long long)nzp, nzh, ostr, mode, K,
-                     slabflag, need);
+                     slabflag, need, none, 0, 0);
   }
 }
 
@@ -1187,12 +1312,16 @@ static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int m
                      spec, P.x, lstr, nzh, (long long)nzp, ny, mode, K, none, 0);
   } else if (c == 0) {
     const dim3 g((unsigned)((nzh + 7) / 8), (unsigned)ny);
+    CUtensorMap map;
+    const int rows = spectrum_map(&map, spec, nx, ny, nzp, nx, 1);
     launch_dependent(chained, k_fft_strided<8, 3>, g, dim3(FFT_T), smem, s, spec, P.x, lstr, nzh, (long long)nzp, mode, K, none,
-                     0);
+                     0, map, rows, 1);
   } else {
     const dim3 g((unsigned)nzh, (unsigned)ny);
+    CUtensorMap zero;
+    memset(&zero, 0, sizeof(zero));
     launch_dependent(chained, k_fft_strided<1, 1>, g, dim3(FFT_T), smem, s, spec, P.x, lstr, nzh, (long long)nzp, mode, K, none,
-                     0);
+                     0, zero, 0, 0);
   }
 }
 
@@ -1381,6 +1510,12 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
   launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag, c.z, ch);
   if (ev) cudaEventRecord(ev[5], s);
   return launch_status("svie_conv_apply_masked", 5);
+}
+
+unsigned int svie_conv_tma_timeouts(void) {
+  unsigned int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tma_timeouts, sizeof(v)) != cudaSuccess) return 0xFFFFFFFFu;
+  return v;
 }
 
 int svie_conv_get_choice(int nx, int ny, int nz, int* z, int* y, int* x) {

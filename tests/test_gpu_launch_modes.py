@@ -1,6 +1,7 @@
-"""Launch modes change timing only: the same solve with dependent launches off (SVIE_PDL=0) and with
-every grid shape's convolution forms tuned (SVIE_FFT_TUNE=all) gives the default run's results bit for
-bit.  Each mode runs in its own process, because both switches are read once per process."""
+"""Launch modes change timing only: the same solve with dependent launches off (SVIE_PDL=0), with every
+grid shape's convolution forms tuned (SVIE_FFT_TUNE=all) and with the TMA tile loads of the convolution
+passes replaced by cp.async (SVIE_TMA=0) gives the default run's results bit for bit.  Each mode runs in
+its own process, because the switches are read once per process."""
 
 import json
 import os
@@ -29,6 +30,8 @@ for law, kw in (("svi", dict(radius=0.08 * L, k=1, s=0, max_steps=12)), ("mean",
     phi = res.level_set.phi.cpu().numpy()
     out[law] = {"fractions": [r.fraction for r in res.history], "dt": [r.dt for r in res.history],
                 "phi": hashlib.sha256(phi.tobytes()).hexdigest()}
+from svierosion_gb300 import _native as nat
+out["tma_timeouts"] = int(nat.lib().svie_conv_tma_timeouts())
 print(json.dumps(out))
 """
 
@@ -44,5 +47,6 @@ def _run(env_extra):
 def test_dependent_launches_and_tuning_change_no_bits():
     base = _run({"SVIE_PDL": "1", "SVIE_FFT_TUNE": "1"})
     assert len(base["svi"]["fractions"]) == 12 and len(base["mean"]["fractions"]) == 30
-    for extra in ({"SVIE_PDL": "0"}, {"SVIE_FFT_TUNE": "all"}):
+    assert base["tma_timeouts"] == 0
+    for extra in ({"SVIE_PDL": "0"}, {"SVIE_FFT_TUNE": "all"}, {"SVIE_TMA": "0"}):
         assert _run(extra) == base, extra
