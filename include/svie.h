@@ -317,6 +317,19 @@ int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, flo
  * count could not be read. */
 unsigned int svie_conv_tma_timeouts(void);
 int svie_conv_get_choice(int nx, int ny, int nz, int* z, int* y, int* x);
+/* Passes compiled for the axis lengths: svie_conv_jit compiles (NVRTC) and
+ * loads, in the current context, the 8-line y and x passes for ny and nx with
+ * every stage's radix, column count and span as constants, and makes the
+ * shape's 8-line y and x forms run them (same bits; the y pass at n = 336
+ * measured 74 -> 64 us).  SVIE_OK, or SVIE_ERR_UNSUPPORTED when NVRTC or the
+ * driver functions are missing, the compilation failed or the 8-line forms do
+ * not fit.  Outside graph capture (it may synchronise for loading).
+ * svie_conv_jit_enabled reports whether a shape runs them;
+ * svie_conv_jit_source writes the generated source for an axis length into buf
+ * (no device needed).  Replace nothing in the reference. */
+int svie_conv_jit(int nx, int ny, int nz);
+int svie_conv_jit_enabled(int nx, int ny, int nz);
+int svie_conv_jit_source(int n, int minb, char* buf, size_t buf_bytes);
 int svie_conv_set_choice(int nx, int ny, int nz, int z, int y, int x);
 /* Full complex64 half spectrum K^ (rfftn of the wrapped kernel, svi.py:76-81). */
 int svie_conv_kernel_hat(const void* plan, int nx, int ny, int nz, void* out_c64, void* stream);

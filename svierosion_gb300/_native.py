@@ -142,6 +142,9 @@ _SIGS = {
     "svie_conv_tune": (I, [V, I, I, I, V, V, V, Z, I, V]),
     "svie_conv_get_choice": (I, [I, I, I, V, V, V]),
     "svie_conv_tma_timeouts": (ctypes.c_uint, []),
+    "svie_conv_jit": (I, [I, I, I]),
+    "svie_conv_jit_enabled": (I, [I, I, I]),
+    "svie_conv_jit_source": (I, [I, I, ctypes.c_char_p, Z]),
     "svie_conv_set_choice": (I, [I, I, I, I, I, I]),
     "svie_rfft3": (I, [V, I, I, I, V, V, V]),
     "svie_irfft3": (I, [V, I, I, I, V, V, D, D, V]),

@@ -27,22 +27,13 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "fft_dev.cuh"
+#include "fft_jit.h"
 
 namespace svie {
 
-constexpr int FFT_T = 256;      // threads per CTA
-constexpr int FFT_MAXST = 14;   // radix stages per axis
-constexpr int FFT_MAXN = 7168;  // longest supported axis (its one-line pass fits shared memory)
-
-struct AxisPlan {
-  int n;
-  int nst;
-  unsigned long long radices;  // radix of stage s in bits [4s, 4s+4) (no arrays: no local-memory copy)
-  const float2* tw;            // tw[k] = exp(-2 pi i k / n), k < n
-  const float2* stw;           // per-stage twiddles: stage with span p at p - 1 + k (R - 1) + q - 1 (n - 1 entries)
-  unsigned long long rradices; // the radices in reverse order (the inverse of the fused x pass)
-  const float2* rstw;          // stage twiddles of the reverse order (x axis only)
-};
+// FFT_T, AxisPlan, the radix butterflies, the tile stages and the pass epilogues are in fft_dev.cuh,
+// shared with the pass kernels compiled at run time for one axis length.
 
 // Radix order: the largest odd radix first, then the even radices
 // (descending), then the other odd ones.  With an odd first radix no stage of
@@ -79,326 +70,6 @@ static bool factor_axis(int n, AxisPlan* p) {
   p->rstw = nullptr;
   return true;
 }
-
-SVIE_DEV float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-SVIE_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-SVIE_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-SVIE_DEV float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
-SVIE_DEV float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // -i * a
-
-// cos / sin of 2 pi t / R for the odd radices (values of the trigonometric
-// functions at rational multiples of pi, to float precision).
-__constant__ float c_cos3[3] = {1.0f, -0.5f, -0.5f};
-__constant__ float c_sin3[3] = {0.0f, 0.86602540378443865f, -0.86602540378443865f};
-__constant__ float c_cos5[5] = {1.0f, 0.30901699437494742f, -0.80901699437494742f, -0.80901699437494742f,
-                                0.30901699437494742f};
-__constant__ float c_sin5[5] = {0.0f, 0.95105651629515357f, 0.58778525229247313f, -0.58778525229247313f,
-                                -0.95105651629515357f};
-__constant__ float c_cos7[7] = {1.0f, 0.62348980185873353f, -0.22252093395631440f, -0.90096886790241913f,
-                                -0.90096886790241913f, -0.22252093395631440f, 0.62348980185873353f};
-__constant__ float c_sin7[7] = {0.0f, 0.78183148246802981f, 0.97492791218182361f, 0.43388373911755812f,
-                                -0.43388373911755812f, -0.97492791218182361f, -0.78183148246802981f};
-
-// Forward DFT of R points in place: y_p = sum_q x_q exp(-2 pi i p q / R).
-template <int R>
-SVIE_DEV void dft(float2* x);
-
-template <>
-SVIE_DEV void dft<2>(float2* x) {
-  float2 a = x[0], b = x[1];
-  x[0] = cadd(a, b);
-  x[1] = csub(a, b);
-}
-
-template <>
-SVIE_DEV void dft<4>(float2* x) {
-  float2 t0 = cadd(x[0], x[2]), t1 = csub(x[0], x[2]);
-  float2 t2 = cadd(x[1], x[3]), t3 = csub(x[1], x[3]);
-  x[0] = cadd(t0, t2);
-  x[2] = csub(t0, t2);
-  x[1] = cadd(t1, mul_mi(t3));
-  x[3] = csub(t1, mul_mi(t3));
-}
-
-template <>
-SVIE_DEV void dft<8>(float2* x) {
-  float2 e[4] = {x[0], x[2], x[4], x[6]};
-  float2 o[4] = {x[1], x[3], x[5], x[7]};
-  dft<4>(e);
-  dft<4>(o);
-  const float r = 0.70710678118654752f;
-  float2 w1 = make_float2(r * (o[1].x + o[1].y), r * (o[1].y - o[1].x));    // o1 * (r - ir)
-  float2 w2 = mul_mi(o[2]);                                                  // o2 * (-i)
-  float2 w3 = make_float2(r * (o[3].y - o[3].x), -r * (o[3].x + o[3].y));   // o3 * (-r - ir)
-  x[0] = cadd(e[0], o[0]);
-  x[4] = csub(e[0], o[0]);
-  x[1] = cadd(e[1], w1);
-  x[5] = csub(e[1], w1);
-  x[2] = cadd(e[2], w2);
-  x[6] = csub(e[2], w2);
-  x[3] = cadd(e[3], w3);
-  x[7] = csub(e[3], w3);
-}
-
-// Odd radix with the symmetric pairing of q and R-q.
-template <int R>
-SVIE_DEV void dft_odd(float2* x, const float* C, const float* S) {
-  constexpr int H = (R - 1) / 2;
-  float2 a[H], b[H];
-#pragma unroll
-  for (int q = 1; q <= H; ++q) {
-    a[q - 1] = cadd(x[q], x[R - q]);
-    b[q - 1] = csub(x[q], x[R - q]);
-  }
-  float2 x0 = x[0];
-  float2 y0 = x0;
-#pragma unroll
-  for (int q = 0; q < H; ++q) y0 = cadd(y0, a[q]);
-#pragma unroll
-  for (int p = 1; p <= H; ++p) {
-    float2 re = x0, im = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int q = 1; q <= H; ++q) {
-      const int t = (p * q) % R;
-      re.x += a[q - 1].x * C[t];
-      re.y += a[q - 1].y * C[t];
-      im.x += b[q - 1].x * S[t];
-      im.y += b[q - 1].y * S[t];
-    }
-    // y_p = re - i*im ; y_{R-p} = re + i*im
-    x[p] = make_float2(re.x + im.y, re.y - im.x);
-    x[R - p] = make_float2(re.x - im.y, re.y + im.x);
-  }
-  x[0] = y0;
-}
-
-template <>
-SVIE_DEV void dft<3>(float2* x) { dft_odd<3>(x, c_cos3, c_sin3); }
-template <>
-SVIE_DEV void dft<5>(float2* x) { dft_odd<5>(x, c_cos5, c_sin5); }
-template <>
-SVIE_DEV void dft<7>(float2* x) { dft_odd<7>(x, c_cos7, c_sin7); }
-
-// 6 = 2 x 3: two 3-point DFTs on the even / odd samples, then twiddles
-// w6^k = exp(-2 pi i k / 6) and a final radix-2 combination.
-template <>
-SVIE_DEV void dft<6>(float2* x) {
-  float2 e[3] = {x[0], x[2], x[4]};
-  float2 o[3] = {x[1], x[3], x[5]};
-  dft<3>(e);
-  dft<3>(o);
-  const float h = 0.86602540378443865f;
-  const float2 o1 = make_float2(0.5f * o[1].x + h * o[1].y, 0.5f * o[1].y - h * o[1].x);    // o1 * (1/2 - i h)
-  const float2 o2 = make_float2(-0.5f * o[2].x + h * o[2].y, -0.5f * o[2].y - h * o[2].x);  // o2 * (-1/2 - i h)
-  x[0] = cadd(e[0], o[0]);
-  x[3] = csub(e[0], o[0]);
-  x[1] = cadd(e[1], o1);
-  x[4] = csub(e[1], o1);
-  x[2] = cadd(e[2], o2);
-  x[5] = csub(e[2], o2);
-}
-
-// ------------------------------------------------------------ tile layout
-// A tile holds LW lines of length n in shared memory, element (line l,
-// position x) at x * PS + l.  Butterfly j of a stage takes line j % LW and
-// column b = j / LW, so the 16 lanes of a half-warp (one wavefront of 8-byte
-// shared accesses) touch LW lines at 16 / LW consecutive columns:
-//  - LW = 16: every stage access is 16 consecutive slots, free of bank
-//    conflicts for any PS (the z passes use PS = 17 so that their loads and
-//    stores, lanes along a line, are conflict-free too);
-//  - LW = 8 (PS = 8): the two columns b, b + 1 (b even) land on different
-//    halves of the bank row whenever their positions differ in parity, which
-//    fails only where a run of k = b mod p wraps inside the pair (p odd, R
-//    even) and in a first stage of even radix; factor_axis puts one odd radix
-//    first so that only the wrap case remains (measured: about 1.5% extra
-//    wavefronts);
-//  - LW = 1 (PS = 1): one line per tile, for axes too long for the others.
-// Each stage is one Stockham radix-R pass from src to dst (ping-pong).
-template <int R, int LW, int PS, int NT = FFT_T>
-SVIE_DEV void tile_stage(const float2* __restrict__ src, float2* __restrict__ dst, int n, int p, unsigned int pmagic,
-                         const float2* __restrict__ stw, bool conj_in) {
-  const int m = n / R;
-  const int total = LW * m;
-  for (int j = threadIdx.x; j < total; j += NT) {
-    const int l = j % LW, b = j / LW;
-    // k = b mod p; umulhi(b, ceil(2^32 / p)) = b / p exactly for b * p < 2^32
-    const int k = (p == 1) ? 0 : b - (int)__umulhi((unsigned)b, pmagic) * p;
-    const float2* s = src + b * PS + l;
-    float2 v[R];
-#pragma unroll
-    for (int q = 0; q < R; ++q) v[q] = s[q * m * PS];
-    if (conj_in) {
-#pragma unroll
-      for (int q = 0; q < R; ++q) v[q].y = -v[q].y;
-    }
-    if (k) {
-      const float2* tk = stw + k * (R - 1);  // the stage's twiddles w^(q k n / (p R)), q = 1..R-1
-#pragma unroll
-      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tk[q - 1]);
-    }
-    dft<R>(v);
-    float2* d = dst + ((b - k) * R + k) * PS + l;
-#pragma unroll
-    for (int q = 0; q < R; ++q) d[q * p * PS] = v[q];
-  }
-  __syncthreads();
-}
-
-SVIE_DEV int radix_of(unsigned long long rad, int st) { return (int)((rad >> (4 * st)) & 15ULL); }
-
-// Stages [s0, s1) of the radix sequence `rad` (4 bits per stage) from a to b
-// and back; p is the span before stage s0 and is advanced past s1.  Returns
-// the buffer holding the result.  `stw` is the stage-twiddle table of that
-// sequence staged in shared memory; the stage with span p starts at entry
-// p - 1 (the earlier stages hold p - 1 entries).  conj_first: stage s0 reads
-// conj(a) (inverse transforms as conj(FFT(conj(x)))).
-template <int LW, int PS, int NT>
-SVIE_DEV float2* run_stages(float2* a, float2* b, int n, unsigned long long rad, int s0, int s1, const float2* stw,
-                            bool conj_first, int& p) {
-  for (int st = s0; st < s1; ++st) {
-    const int R = radix_of(rad, st);
-    const unsigned int mg = p > 1 ? 0xFFFFFFFFu / (unsigned)p + 1u : 0u;
-    const float2* sw = stw + (p - 1);
-    const bool cj = conj_first && st == s0;
-    switch (R) {
-      case 8: tile_stage<8, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
-      case 7: tile_stage<7, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
-      case 6: tile_stage<6, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
-      case 5: tile_stage<5, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
-      case 4: tile_stage<4, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
-      case 3: tile_stage<3, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
-      default: tile_stage<2, LW, PS, NT>(a, b, n, p, mg, sw, cj); break;
-    }
-    float2* t = a; a = b; b = t;
-    p *= R;
-  }
-  return a;
-}
-
-template <int LW, int PS, int NT = FFT_T>
-SVIE_DEV float2* run_tile_fft(float2* a, float2* b, const AxisPlan& P, const float2* stw, bool conj_first = false) {
-  int p = 1;
-  return run_stages<LW, PS, NT>(a, b, P.n, P.radices, 0, P.nst, stw, conj_first, p);
-}
-
-// The last stage of a transform (span p = m = n / R, so k = b): butterfly
-// (line l, column b) reads and writes the positions b + q m of line l, and its
-// outputs go to epi.apply(v, b, l, m) instead of back to shared memory.
-template <int R, int LW, int PS, int NT, class Epi>
-SVIE_DEV void last_stage(const float2* __restrict__ src, int n, const float2* __restrict__ stw, bool conj_in,
-                         const Epi& epi) {
-  const int m = n / R;
-  const int total = LW * m;
-  for (int j = threadIdx.x; j < total; j += NT) {
-    const int l = j % LW, b = j / LW;
-    const float2* s = src + b * PS + l;
-    float2 v[R];
-#pragma unroll
-    for (int q = 0; q < R; ++q) v[q] = s[q * m * PS];
-    if (conj_in) {
-#pragma unroll
-      for (int q = 0; q < R; ++q) v[q].y = -v[q].y;
-    }
-    if (b) {
-      const float2* tk = stw + (m - 1) + b * (R - 1);
-#pragma unroll
-      for (int q = 1; q < R; ++q) v[q] = cmul(v[q], tk[q - 1]);
-    }
-    dft<R>(v);
-    epi.template apply<R>(v, b, l, m);
-  }
-}
-
-template <int LW, int PS, int NT, class Epi>
-SVIE_DEV void run_last(const float2* src, int n, int R, const float2* stw, bool conj_in, const Epi& epi) {
-  const float2* sw = stw;
-  switch (R) {
-    case 8: last_stage<8, LW, PS, NT>(src, n, sw, conj_in, epi); break;
-    case 7: last_stage<7, LW, PS, NT>(src, n, sw, conj_in, epi); break;
-    case 6: last_stage<6, LW, PS, NT>(src, n, sw, conj_in, epi); break;
-    case 5: last_stage<5, LW, PS, NT>(src, n, sw, conj_in, epi); break;
-    case 4: last_stage<4, LW, PS, NT>(src, n, sw, conj_in, epi); break;
-    case 3: last_stage<3, LW, PS, NT>(src, n, sw, conj_in, epi); break;
-    default: last_stage<2, LW, PS, NT>(src, n, sw, conj_in, epi); break;
-  }
-}
-
-// Epilogue: store line l's outputs at base + l + position * stride (lines
-// l < nl only), conjugated for inverse transforms.
-struct StoreEpi {
-  float2* base;
-  long long stride;
-  int nl;
-  bool conj;
-  template <int R>
-  SVIE_DEV void apply(float2 (&v)[R], int b, int l, int m) const {
-    if (l >= nl) return;
-    float2* g = base + l + (long long)b * stride;
-    const long long ms = (long long)m * stride;
-#pragma unroll
-    for (int q = 0; q < R; ++q) {
-      float2 w = v[q];
-      if (conj) w.y = -w.y;
-      g[q * ms] = w;
-    }
-  }
-};
-
-// Epilogue of the x pass: multiply the forward outputs by K^ (real, even in
-// kx) and conjugate, then run the first stage of the inverse, whose radix
-// order is the forward's reversed: its first radix is this stage's R and it
-// reads exactly the positions b + q m this butterfly holds (span 1, no
-// twiddles); the results go to dst at positions b R + q.
-template <int PS>
-struct KEpi {
-  float2* dst;
-  const float* krow;  // K^ row of this slab and column block: + l + kr * kst
-  long long kst;
-  int n, nl;
-  template <int R>
-  SVIE_DEV void apply(float2 (&v)[R], int b, int l, int m) const {
-#pragma unroll
-    for (int q = 0; q < R; ++q) {
-      const int pos = b + q * m, kr = min(pos, n - pos);
-      const float kv = l < nl ? __ldg(krow + l + kr * kst) : 0.0f;
-      v[q] = make_float2(v[q].x * kv, -(v[q].y * kv));
-    }
-    dft<R>(v);
-    float2* d = dst + b * R * PS + l;
-#pragma unroll
-    for (int q = 0; q < R; ++q) d[q * PS] = v[q];
-  }
-};
-
-__host__ __device__ inline int padded_nzh(int nz) { return ((nz / 2 + 1) + 7) & ~7; }  // 64-byte rows
-// shared memory of a tile: two buffers of n positions and the stage-twiddle table (n entries)
-__host__ __device__ inline size_t tile_smem(int PS, int n) { return (2 * (size_t)PS + 1) * (size_t)n * sizeof(float2); }
-constexpr size_t TILE_SMEM_MAX = 227 * 1024;
-
-// Copy the axis' stage twiddles (n - 1 entries) into shared memory after the buffers.
-SVIE_DEV float2* stage_twiddles_to_smem(float2* sm, int PS, const AxisPlan& P) {
-  float2* stw = sm + 2 * PS * P.n;
-  for (int e = threadIdx.x; e < P.n - 1; e += blockDim.x) stw[e] = __ldg(P.stw + e);
-  return stw;
-}
-
-// 16-byte asynchronous global -> shared copies (L2 only), completed by groups.
-SVIE_DEV void cp_async16(void* smem, const void* gmem) {
-  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-// 8- and 4-byte forms (cached in L1 as well: the only forms for these sizes).
-SVIE_DEV void cp_async8(void* smem, const void* gmem) {
-  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-SVIE_DEV void cp_async4(void* smem, const void* gmem) {
-  const unsigned int sa = (unsigned int)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-SVIE_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-SVIE_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // ------------------------------------------------ TMA tile loads (mbarrier)
 // A tile of the 8-line passes is one box or a few boxes of a 3-D tensor map
@@ -624,10 +295,6 @@ __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ 
 // PS = LW), so thread t loads line t % LW of rows t / LW, + FFT_T / LW, ...
 // mode 0 = forward, 1 = inverse, 2 = forward * K^ then inverse (x axis only;
 // the outer index is y and the line index kz).
-struct KGeom {
-  const float* kred;  // [(nx/2+1)][(ny/2+1)][nzh]
-  int ny, nzh;
-};
 
 // Slab skipping: when `slabflag` is given, a CTA returns at once for an outer
 // slab whose flag lacks `need` (bit 0: the forward data of the slab is zero,
@@ -1091,6 +758,7 @@ static bool fits(size_t b) { return b <= TILE_SMEM_MAX; }
 
 struct FftChoice {
   int z, y, x;
+  int jit = 0;  // the 8-line y and x forms run as passes compiled for the axis lengths (svie_conv_jit)
 };
 
 // the fixed rule (above)
@@ -1271,7 +939,7 @@ static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, flo
 
 // y lines: outer index x, line index kz, element stride nzp.
 static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s,
-                     const uint8_t* slabflag, int c, bool chained) {
+                     const uint8_t* slabflag, int c, bool chained, bool jit = false) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const KGeom K{nullptr, ny, nzh};
   const int need = mode == 1 ? 2 : 1;
@@ -1284,6 +952,15 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
                      spec, P.y, (long long)nzp, nzh, ostr, nx, mode, K, slabflag, need);
   } else if (c == 1) {
     const dim3 g((unsigned)((nzh + 7) / 8), (unsigned)nx);
+    CUfunction jf = nullptr;
+    if (jit && jit_strided(ny, 4, P.y.radices, P.y.nst, &jf) == SVIE_OK) {
+      long long stride = nzp, ostr_ = ostr;
+      int ninner = nzh, mode_ = mode, need_ = need;
+      AxisPlan ax = P.y;
+      KGeom kg = K;
+      void* args[] = {&spec, &ax, &stride, &ninner, &ostr_, &mode_, &kg, &slabflag, &need_};
+      if (jit_launch(jf, g, dim3(FFT_T), smem, s, chained, args)) return;
+    }
     CUtensorMap map;
     const int rows = spectrum_map(&map, spec, nx, ny, nzp, ny, 0);
     launch_dependent(chained, k_fft_strided<8, 4>, g, dim3(FFT_T), smem, s, spec, P.y, (long long)nzp, nzh, ostr, mode, K,
@@ -1299,7 +976,7 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
 
 // x lines: outer index y, line index kz, element stride ny * nzp.
 static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int mode, cudaStream_t s, int c,
-                     bool chained) {
+                     bool chained, bool jit = false) {
   const int nzh = nz / 2 + 1, nzp = padded_nzh(nz);
   const KGeom K{P.kred, ny, nzh};
   const long long lstr = (long long)ny * nzp;
@@ -1312,6 +989,15 @@ static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int m
                      spec, P.x, lstr, nzh, (long long)nzp, ny, mode, K, none, 0);
   } else if (c == 0) {
     const dim3 g((unsigned)((nzh + 7) / 8), (unsigned)ny);
+    CUfunction jf = nullptr;
+    if (jit && jit_strided(nx, 3, P.x.radices, P.x.nst, &jf) == SVIE_OK) {
+      long long stride = lstr, ostr_ = nzp;
+      int ninner = nzh, mode_ = mode, need_ = 0;
+      AxisPlan ax = P.x;
+      KGeom kg = K;
+      void* args[] = {&spec, &ax, &stride, &ninner, &ostr_, &mode_, &kg, &none, &need_};
+      if (jit_launch(jf, g, dim3(FFT_T), smem, s, chained, args)) return;
+    }
     CUtensorMap map;
     const int rows = spectrum_map(&map, spec, nx, ny, nzp, nx, 1);
     launch_dependent(chained, k_fft_strided<8, 3>, g, dim3(FFT_T), smem, s, spec, P.x, lstr, nzh, (long long)nzp, mode, K, none,
@@ -1470,9 +1156,9 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
   float2* spec = (float2*)ws;
   const FftChoice c = choice_for(nx, ny, nz);
   launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z, false);
-  launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c.y, true);
-  launch_x(P, nx, ny, nz, spec, 2, s, c.x, true);
-  launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c.y, true);
+  launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c.y, true, c.jit);
+  launch_x(P, nx, ny, nz, spec, 2, s, c.x, true, c.jit);
+  launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c.y, true, c.jit);
   launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z, true);
   return launch_status("svie_conv_apply", 5);
 }
@@ -1501,11 +1187,11 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
   if (ev) cudaEventRecord(ev[0], s);
   launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, lineflag, c.z, false);
   if (ev) cudaEventRecord(ev[1], s);
-  launch_y(P, nx, ny, nz, spec, 0, s, slabflag, c.y, ch);
+  launch_y(P, nx, ny, nz, spec, 0, s, slabflag, c.y, ch, c.jit);
   if (ev) cudaEventRecord(ev[2], s);
-  launch_x(P, nx, ny, nz, spec, 2, s, c.x, ch);
+  launch_x(P, nx, ny, nz, spec, 2, s, c.x, ch, c.jit);
   if (ev) cudaEventRecord(ev[3], s);
-  launch_y(P, nx, ny, nz, spec, 1, s, slabflag, c.y, ch);
+  launch_y(P, nx, ny, nz, spec, 1, s, slabflag, c.y, ch, c.jit);
   if (ev) cudaEventRecord(ev[4], s);
   launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag, c.z, ch);
   if (ev) cudaEventRecord(ev[5], s);
@@ -1534,14 +1220,56 @@ int svie_conv_set_choice(int nx, int ny, int nz, int z, int y, int x) {
     g_choice.erase(k);
     return SVIE_OK;
   }
-  const FftChoice c{z, y, x};
+  FftChoice c{z, y, x};
   if (!choice_fits(c, nx, ny, nz)) {
     set_error("svie_conv_set_choice: forms (%d, %d, %d) do not exist or do not fit shared memory for %d x %d x %d",
               z, y, x, nx, ny, nz);
     return SVIE_ERR_ARG;
   }
   std::lock_guard<std::mutex> lock(g_choice_mu);
+  auto it = g_choice.find(k);
+  if (it != g_choice.end()) c.jit = it->second.jit;
   g_choice[k] = c;
+  return SVIE_OK;
+}
+
+int svie_conv_jit(int nx, int ny, int nz) {
+  AxisPlan ax, ay, az;
+  if (!factor_axis(nx, &ax) || !factor_axis(ny, &ay) || !factor_axis(nz, &az)) {
+    set_error("svie_conv_jit: axis sizes %d x %d x %d are not supported", nx, ny, nz);
+    return SVIE_ERR_UNSUPPORTED;
+  }
+  if (!fits(y_smem(1, ny)) || !fits(x_smem(0, nx))) {
+    set_error("svie_conv_jit: the 8-line passes do not fit shared memory on %d x %d x %d", nx, ny, nz);
+    return SVIE_ERR_UNSUPPORTED;
+  }
+  CUfunction fy = nullptr, fx = nullptr;
+  int st = jit_strided(ny, 4, ay.radices, ay.nst, &fy);
+  if (st == SVIE_OK) st = jit_strided(nx, 3, ax.radices, ax.nst, &fx);
+  if (st != SVIE_OK) return st;
+  const GridKey k = grid_key(nx, ny, nz);
+  std::lock_guard<std::mutex> lock(g_choice_mu);
+  auto it = g_choice.find(k);
+  FftChoice c = it != g_choice.end() ? it->second : default_choice(nx, ny, nz);
+  c.jit = 1;
+  g_choice[k] = c;
+  return SVIE_OK;
+}
+
+int svie_conv_jit_enabled(int nx, int ny, int nz) { return choice_for(nx, ny, nz).jit ? 1 : 0; }
+
+int svie_conv_jit_source(int n, int minb, char* buf, size_t buf_bytes) {
+  AxisPlan a;
+  if (!factor_axis(n, &a) || minb < 1 || minb > 8 || !buf) {
+    set_error("svie_conv_jit_source: bad arguments");
+    return SVIE_ERR_ARG;
+  }
+  const std::string src = jit_strided_source_for_test(n, minb, a.radices, a.nst);
+  if (src.size() + 1 > buf_bytes) {
+    set_error("svie_conv_jit_source: %zu bytes needed", src.size() + 1);
+    return SVIE_ERR_CAPACITY;
+  }
+  memcpy(buf, src.c_str(), src.size() + 1);
   return SVIE_OK;
 }
 
@@ -1573,6 +1301,7 @@ int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, flo
     return SVIE_ERR_LAUNCH;
   }
   FftChoice best = default_choice(nx, ny, nz);
+  best.jit = choice_for(nx, ny, nz).jit;  // the compiled passes, when the shape has them, are what is timed
   float tz = -1.f, ty = -1.f, tx = -1.f;
   bool failed = false;
   int launched = 1;
@@ -1591,8 +1320,8 @@ int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, flo
     }
     if (!failed && tunable_y(c, ny)) {  // forward and inverse y
       const float t = time_form([&] {
-        launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c, false);
-        launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c, false);
+        launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c, false, d.jit);
+        launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c, false, d.jit);
         launched += 2;
       }, reps, s, e0, e1);
       if (t < 0.f) failed = true;
@@ -1600,7 +1329,7 @@ int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, flo
     }
     if (!failed && tunable_x(c, nx)) {  // the fused x pass
       const float t = time_form([&] {
-        launch_x(P, nx, ny, nz, spec, 2, s, c, false);
+        launch_x(P, nx, ny, nz, spec, 2, s, c, false, d.jit);
         launched += 1;
       }, reps, s, e0, e1);
       if (t < 0.f) failed = true;
@@ -1658,8 +1387,8 @@ int svie_rfft3(const void* plan, int nx, int ny, int nz, const float* f, void* s
   cudaStream_t s = (cudaStream_t)stream;
   const FftChoice c = choice_for(nx, ny, nz);
   launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z, false);
-  launch_y(P, nx, ny, nz, (float2*)spec, 0, s, nullptr, c.y, true);
-  launch_x(P, nx, ny, nz, (float2*)spec, 0, s, c.x, true);
+  launch_y(P, nx, ny, nz, (float2*)spec, 0, s, nullptr, c.y, true, c.jit);
+  launch_x(P, nx, ny, nz, (float2*)spec, 0, s, c.x, true, c.jit);
   return launch_status("svie_rfft3", 3);
 }
 
@@ -1675,8 +1404,8 @@ int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const FftChoice c = choice_for(nx, ny, nz);
-  launch_x(P, nx, ny, nz, (float2*)spec, 1, s, c.x, false);
-  launch_y(P, nx, ny, nz, (float2*)spec, 1, s, nullptr, c.y, true);
+  launch_x(P, nx, ny, nz, (float2*)spec, 1, s, c.x, false, c.jit);
+  launch_y(P, nx, ny, nz, (float2*)spec, 1, s, nullptr, c.y, true, c.jit);
   launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z, true);
   return launch_status("svie_irfft3", 3);
 }

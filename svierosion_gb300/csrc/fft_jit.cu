@@ -1,0 +1,288 @@
+// Convolution pass kernels compiled at run time for one axis length.
+//
+// The 8-line y and x passes (k_fft_strided) take the axis length, and with it
+// every stage's radix, column count and span, as run-time values: each shared
+// memory access of a butterfly needs its address computed.  For a given axis
+// length this file generates the same pass with all of them as constants
+// (tile_stage_c / last_stage_c of fft_dev.cuh), compiles it with NVRTC for the
+// current device and loads it with the driver API.  Every butterfly performs the
+// same operations as in the library's own pass, so the results are the same
+// bits; on 448 x 336 x 245 the y pass measured 74 -> 64 us.
+//
+// NVRTC is opened with dlopen and the driver functions are reached through the
+// runtime's driver entry points, so the library links against neither.  When
+// either is missing or a compilation fails, no kernel is made and the caller
+// keeps the library's pass.  Kernels are kept per (CUDA context, axis length,
+// CTAs per SM) for the life of the process.
+#include <cuda.h>
+#include <dlfcn.h>
+#include <stdio.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+#include "fft_jit.h"
+
+namespace svie {
+namespace {
+
+typedef struct _nvrtcProgram* NvrtcProgram;
+struct Nvrtc {
+  int (*create)(NvrtcProgram*, const char*, const char*, int, const char* const*, const char* const*) = nullptr;
+  int (*compile)(NvrtcProgram, int, const char* const*) = nullptr;
+  int (*log_size)(NvrtcProgram, size_t*) = nullptr;
+  int (*log)(NvrtcProgram, char*) = nullptr;
+  int (*cubin_size)(NvrtcProgram, size_t*) = nullptr;
+  int (*cubin)(NvrtcProgram, char*) = nullptr;
+  int (*destroy)(NvrtcProgram*) = nullptr;
+  bool ok = false;
+};
+
+const Nvrtc& nvrtc() {
+  static Nvrtc n;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* h = nullptr;
+    for (const char* name : {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so"})
+      if ((h = dlopen(name, RTLD_NOW | RTLD_LOCAL))) break;
+    if (!h) return;
+    n.create = (decltype(n.create))dlsym(h, "nvrtcCreateProgram");
+    n.compile = (decltype(n.compile))dlsym(h, "nvrtcCompileProgram");
+    n.log_size = (decltype(n.log_size))dlsym(h, "nvrtcGetProgramLogSize");
+    n.log = (decltype(n.log))dlsym(h, "nvrtcGetProgramLog");
+    n.cubin_size = (decltype(n.cubin_size))dlsym(h, "nvrtcGetCUBINSize");
+    n.cubin = (decltype(n.cubin))dlsym(h, "nvrtcGetCUBIN");
+    n.destroy = (decltype(n.destroy))dlsym(h, "nvrtcDestroyProgram");
+    n.ok = n.create && n.compile && n.log_size && n.log && n.cubin_size && n.cubin && n.destroy;
+  });
+  return n;
+}
+
+struct Driver {
+  CUresult (*ctx_current)(CUcontext*) = nullptr;
+  CUresult (*load)(CUmodule*, const void*) = nullptr;
+  CUresult (*get_function)(CUfunction*, CUmodule, const char*) = nullptr;
+  CUresult (*set_attribute)(CUfunction, CUfunction_attribute, int) = nullptr;
+  CUresult (*launch)(const CUlaunchConfig*, CUfunction, void**, void**) = nullptr;
+  bool ok = false;
+};
+
+template <class F>
+void entry(const char* name, F* fn) {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    *fn = (F)f;
+}
+
+const Driver& driver() {
+  static Driver d;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    entry("cuCtxGetCurrent", &d.ctx_current);
+    entry("cuModuleLoadData", &d.load);
+    entry("cuModuleGetFunction", &d.get_function);
+    entry("cuFuncSetAttribute", &d.set_attribute);
+    entry("cuLaunchKernelEx", &d.launch);
+    d.ok = d.ctx_current && d.load && d.get_function && d.set_attribute && d.launch;
+  });
+  return d;
+}
+
+// The directory of fft_dev.cuh: csrc/ beside the loaded libsvie.so.
+std::string csrc_dir() {
+  Dl_info info;
+  if (!dladdr((const void*)&csrc_dir, &info) || !info.dli_fname) return "";
+  std::string p(info.dli_fname);
+  const size_t slash = p.rfind('/');
+  return (slash == std::string::npos ? std::string(".") : p.substr(0, slash)) + "/csrc";
+}
+
+// Source of the 8-line strided pass for an axis of n positions with the given
+// radix sequence (forward order): the body of k_fft_strided<8, MINB> on its
+// cp.async path, with each stage unrolled at compile time.
+std::string strided_source(int n, int minb, const std::vector<int>& r) {
+  const int nst = (int)r.size();
+  std::string s;
+  char buf[512];
+  auto add = [&](const char* fmt, auto... a) {
+    snprintf(buf, sizeof(buf), fmt, a...);
+    s += buf;
+  };
+  s += "#include \"fft_dev.cuh\"\nnamespace svie {\n";
+  add("extern \"C\" __global__ void __launch_bounds__(256, %d) svie_jit_strided(float2* __restrict__ data, AxisPlan P,\n",
+      minb);
+  s += "    long long stride, int ninner, long long outer_stride, int mode, KGeom K,\n"
+       "    const uint8_t* __restrict__ slabflag, int need) {\n"
+       "  pdl_wait();\n  pdl_release();\n"
+       "  if (slabflag && !(__ldg(slabflag + blockIdx.y) & need)) return;\n"
+       "  extern __shared__ __align__(16) float2 sm[];\n";
+  add("  constexpr int LW = 8, n = %d;\n", n);
+  s += "  float2* const sa = sm;\n  float2* const sb = sm + LW * n;\n"
+       "  const int c0 = blockIdx.x * LW;\n  const int nl = min(LW, ninner - c0);\n"
+       "  float2* base = data + (long long)blockIdx.y * outer_stride + c0;\n"
+       "  for (int e = threadIdx.x; e < 4 * n; e += 256) {\n"
+       "    const int row = e >> 2, part = 2 * (e & 3);\n"
+       "    cp_async16(sa + row * LW + part, base + row * stride + part);\n  }\n"
+       "  cp_async_commit();\n"
+       "  const float2* stw = stage_twiddles_to_smem(sm, LW, P);\n"
+       "  if (mode == 2)\n"
+       "    for (int e = threadIdx.x; e < n - 1; e += 256) sm[2 * LW * n + n + e] = __ldg(P.rstw + e);\n"
+       "  cp_async_wait<0>();\n  __syncthreads();\n";
+  const char* cur = "sa";
+  const char* oth = "sb";
+  int p = 1;
+  for (int st = 0; st + 1 < nst; ++st) {
+    add("  tile_stage_c<%d, %d, %d, 8, 8, 256>(%s, %s, stw, %s);\n", r[st], n / r[st], p, cur, oth,
+        st == 0 ? "mode == 1" : "false");
+    std::swap(cur, oth);
+    p *= r[st];
+  }
+  const int rl = r[nst - 1];
+  add("  if (mode != 2) {\n    last_stage_c<%d, %d, 8, 8, 256>(%s, stw, %s, StoreEpi{base, stride, nl, mode != 0});\n"
+      "    return;\n  }\n",
+      rl, n / rl, cur, nst == 1 ? "mode == 1" : "false");
+  s += "  const float2* rstw = stw + n;\n  const int nyh = K.ny / 2 + 1;\n"
+       "  const int y = blockIdx.y, yr = min(y, K.ny - y);\n";
+  add("  last_stage_c<%d, %d, 8, 8, 256>(%s, stw, false, KEpi<8>{%s, K.kred + (long long)yr * K.nzh + c0,\n"
+      "      (long long)nyh * K.nzh, n, nl});\n  __syncthreads();\n",
+      rl, n / rl, cur, oth);
+  if (nst == 1) {
+    add("  const int c = threadIdx.x %% LW, k0 = threadIdx.x / LW;\n  if (c < nl) {\n"
+        "    float2* g = base + (long long)k0 * stride + c;\n"
+        "    for (int k = k0; k < n; k += 256 / LW, g += (256 / LW) * stride) {\n"
+        "      const float2 v = %s[k * LW + c];\n      *g = make_float2(v.x, -v.y);\n    }\n  }\n",
+        oth);
+  } else {
+    // the inverse in reverse radix order: its first stage was the K^ epilogue
+    std::vector<int> rr(r.rbegin(), r.rend());
+    const char* c2 = oth;
+    const char* o2 = cur;
+    int p2 = rr[0];
+    for (int st = 1; st + 1 < nst; ++st) {
+      add("  tile_stage_c<%d, %d, %d, 8, 8, 256>(%s, %s, rstw, false);\n", rr[st], n / rr[st], p2, c2, o2);
+      std::swap(c2, o2);
+      p2 *= rr[st];
+    }
+    add("  last_stage_c<%d, %d, 8, 8, 256>(%s, rstw, false, StoreEpi{base, stride, nl, true});\n", rr[nst - 1],
+        n / rr[nst - 1], c2);
+  }
+  s += "}\n}  // namespace svie\n";
+  return s;
+}
+
+// Compiles a source for the current device; the cubin, or an empty vector
+// with the log in *err.
+std::vector<char> compile(const std::string& src, std::string* err) {
+  const Nvrtc& nv = nvrtc();
+  std::vector<char> out;
+  if (!nv.ok) {
+    *err = "NVRTC not found";
+    return out;
+  }
+  int dev = 0, major = 0, minor = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  const std::string arch = "-arch=sm_" + std::to_string(major * 10 + minor) + (major >= 9 ? "a" : "");
+  const std::string inc = "-I" + csrc_dir();
+  const char* opts[] = {arch.c_str(), "-std=c++17", inc.c_str()};
+  NvrtcProgram prog = nullptr;
+  if (nv.create(&prog, src.c_str(), "svie_jit_strided.cu", 0, nullptr, nullptr) != 0) {
+    *err = "nvrtcCreateProgram failed";
+    return out;
+  }
+  const int rc = nv.compile(prog, 3, opts);
+  size_t ls = 0;
+  nv.log_size(prog, &ls);
+  std::string log(ls, '\0');
+  if (ls) nv.log(prog, &log[0]);
+  size_t cs = 0;
+  if (rc == 0 && nv.cubin_size(prog, &cs) == 0 && cs > 0) {
+    out.resize(cs);
+    if (nv.cubin(prog, out.data()) != 0) out.clear();
+  }
+  if (out.empty()) *err = "compilation failed: " + log.substr(0, 400);
+  nv.destroy(&prog);
+  return out;
+}
+
+struct Key {
+  CUcontext ctx;
+  int n, minb;
+  bool operator<(const Key& o) const { return std::tie(ctx, n, minb) < std::tie(o.ctx, o.n, o.minb); }
+};
+std::mutex g_mu;
+std::map<Key, CUfunction> g_fn;  // nullptr: tried and failed
+
+}  // namespace
+
+int jit_strided(int n, int minb, unsigned long long radices, int nst, CUfunction* fn) {
+  *fn = nullptr;
+  const Driver& d = driver();
+  if (!d.ok) {
+    set_error("fft jit: driver entry points not found");
+    return SVIE_ERR_UNSUPPORTED;
+  }
+  CUcontext ctx = nullptr;
+  if (d.ctx_current(&ctx) != CUDA_SUCCESS || !ctx) {
+    set_error("fft jit: no current CUDA context");
+    return SVIE_ERR_LAUNCH;
+  }
+  const Key key{ctx, n, minb};
+  std::lock_guard<std::mutex> lock(g_mu);
+  auto it = g_fn.find(key);
+  if (it != g_fn.end()) {
+    *fn = it->second;
+    if (!*fn) set_error("fft jit: the pass for n = %d did not compile earlier", n);
+    return *fn ? SVIE_OK : SVIE_ERR_UNSUPPORTED;
+  }
+  std::vector<int> r;
+  for (int st = 0; st < nst; ++st) r.push_back((int)((radices >> (4 * st)) & 15ULL));
+  std::string err;
+  const std::vector<char> cubin = compile(strided_source(n, minb, r), &err);
+  CUfunction f = nullptr;
+  CUmodule mod = nullptr;
+  if (!cubin.empty() && d.load(&mod, cubin.data()) == CUDA_SUCCESS &&
+      d.get_function(&f, mod, "svie_jit_strided") == CUDA_SUCCESS &&
+      d.set_attribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 227 * 1024) == CUDA_SUCCESS) {
+    g_fn[key] = f;
+    *fn = f;
+    return SVIE_OK;
+  }
+  g_fn[key] = nullptr;
+  set_error("fft jit: no pass for n = %d: %s", n, err.empty() ? "module load failed" : err.c_str());
+  return SVIE_ERR_UNSUPPORTED;
+}
+
+bool jit_launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool chained, void** args) {
+  const Driver& d = driver();
+  CUlaunchAttribute attr[1];
+  attr[0].id = CU_LAUNCH_ATTRIBUTE_PROGRAMMATIC_STREAM_SERIALIZATION;
+  attr[0].value.programmaticStreamSerializationAllowed = 1;
+  CUlaunchConfig cfg = {};
+  cfg.gridDimX = grid.x;
+  cfg.gridDimY = grid.y;
+  cfg.gridDimZ = grid.z;
+  cfg.blockDimX = block.x;
+  cfg.blockDimY = block.y;
+  cfg.blockDimZ = block.z;
+  cfg.sharedMemBytes = (unsigned int)smem;
+  cfg.hStream = (CUstream)s;
+  cfg.attrs = attr;
+  cfg.numAttrs = chained && pdl_enabled() ? 1 : 0;
+  return d.ok && d.launch(&cfg, fn, args, nullptr) == CUDA_SUCCESS;
+}
+
+std::string jit_strided_source_for_test(int n, int minb, unsigned long long radices, int nst) {
+  std::vector<int> r;
+  for (int st = 0; st < nst; ++st) r.push_back((int)((radices >> (4 * st)) & 15ULL));
+  return strided_source(n, minb, r);
+}
+
+}  // namespace svie

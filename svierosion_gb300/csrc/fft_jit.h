@@ -1,0 +1,24 @@
+// Convolution pass kernels compiled at run time for one axis length (fft_jit.cu).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <string>
+
+namespace svie {
+
+// The 8-line strided pass (k_fft_strided<8, minb>) compiled for an axis of n
+// positions with the given radix sequence (4 bits per stage), in the current
+// context; kept for later calls.  SVIE_OK and *fn, or an error status (NVRTC
+// or the driver API missing, compilation or loading failed) with *fn = null.
+int jit_strided(int n, int minb, unsigned long long radices, int nst, CUfunction* fn);
+
+// Launches a compiled pass on `s` (a dependent launch when `chained`); false
+// when the launch failed (the caller then launches the library's pass).
+bool jit_launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool chained, void** args);
+
+// The generated source (for the CPU test that compiles it).
+std::string jit_strided_source_for_test(int n, int minb, unsigned long long radices, int nst);
+
+}  // namespace svie

@@ -76,6 +76,16 @@ def autotune_enabled(nodes: int | None = None) -> bool:
     return mode == "all" or nodes is None or nodes >= TUNE_MIN_NODES
 
 
+def jit_enabled(nodes: int | None = None) -> bool:
+    """Whether a grid of `nodes` nodes gets its y and x passes compiled for its axis lengths at its
+    first convolution (svie_conv_jit): SVIE_FFT_JIT=0 never, =all always, otherwise (default) from
+    TUNE_MIN_NODES nodes up (a compilation takes about a second per axis length)."""
+    mode = os.environ.get("SVIE_FFT_JIT", "1")
+    if mode == "0":
+        return False
+    return mode == "all" or nodes is None or nodes >= TUNE_MIN_NODES
+
+
 def _cache_path():
     """SVIE_FFT_TUNE_CACHE: a JSON file of tuned pass forms kept across processes (unset: none)."""
     p = os.environ.get("SVIE_FFT_TUNE_CACHE")
@@ -202,15 +212,22 @@ class BallConvolution:
         return out
 
     def _tune(self, f, out, ws) -> None:
-        """Time the pass forms on this grid shape once per process (not while a graph is captured), or
-        take them from the tuning cache file (SVIE_FFT_TUNE_CACHE) when it holds this GPU model and
-        shape; newly tuned forms are added to that file."""
+        """Once per grid shape and process (not while a graph is captured): compile the y and x
+        passes for the shape's axis lengths (jit_enabled), then time the pass forms, or take them
+        from the tuning cache file (SVIE_FFT_TUNE_CACHE) when it holds this GPU model and shape;
+        newly tuned forms are added to that file."""
         key = (self.device.index, tuple(self.grid.shape))
-        if key in _TUNED or not autotune_enabled(self.grid.size) or torch.cuda.is_current_stream_capturing():
+        if key in _TUNED or torch.cuda.is_current_stream_capturing():
+            return
+        nx, ny, nz = self.grid.shape
+        if jit_enabled(self.grid.size) and not nat.lib().svie_conv_jit_enabled(nx, ny, nz):
+            # the passes compiled for these axis lengths; on failure the library's own passes stay
+            nat.lib().svie_conv_jit(nx, ny, nz)
+        if not autotune_enabled(self.grid.size):
+            _TUNED.add(key)
             return
         if load_tuned_forms(self.device, self.grid.shape):
             return
-        nx, ny, nz = self.grid.shape
         nat.call("svie_conv_tune", nat.ptr(self.plan), nx, ny, nz, nat.ptr(f), nat.ptr(out.view(-1)), nat.ptr(ws),
                  ws.numel(), TUNE_REPS, nat.stream())
         _TUNED.add(key)

@@ -235,3 +235,38 @@ def test_tuned_forms_are_kept_in_the_cache_file(tmp_path, monkeypatch):
         assert svi.fft_choice(shape) == tuned
     finally:
         svi.set_fft_choice(shape, -1, -1, -1)
+
+
+@pytest.mark.parametrize("shape", [(40, 42, 36), (64, 48, 35), (90, 84, 60), (112, 98, 70)])
+def test_passes_compiled_for_the_axis_lengths_give_the_same_bits(shape):
+    """The y and x passes compiled at run time for the shape's axis lengths (svie_conv_jit) give the
+    library's own passes' bits for the convolution, the masked convolution and rfftn / irfftn."""
+    from svierosion_gb300 import _native as nat
+    rng = np.random.default_rng(sum(shape) + 1)
+    g = Grid((0.0, 0.0, 0.0), 1.0, shape)
+    f = torch.from_numpy(rng.random(shape, dtype=np.float32)).cuda()
+    conv = S.BallConvolution(g, 3.0)
+    nx, ny, nz = shape
+    lf = torch.from_numpy((rng.random(nx * ny) < 0.5).astype(np.uint8) * 3).cuda()
+    sf = torch.from_numpy(np.full(nx, 3, dtype=np.uint8)).cuda()
+
+    def run():
+        full = conv.exterior_fraction(f)
+        masked = torch.zeros(shape, device="cuda")
+        conv.exterior_fraction_into(f, masked, flags=(lf, sf))
+        spec = svi.rfftn(f, conv)
+        return [full, masked, torch.view_as_real(spec).clone(), svi.irfftn(spec, conv)]
+
+    lib = nat.lib()
+    try:
+        svi.set_fft_choice(shape, 0, 1, 0)
+        assert not lib.svie_conv_jit_enabled(nx, ny, nz)
+        ref = run()
+        nat.call("svie_conv_jit", nx, ny, nz)
+        assert lib.svie_conv_jit_enabled(nx, ny, nz)
+        got = run()
+        for a, b in zip(ref, got):
+            assert torch.equal(a, b)
+        assert lib.svie_conv_tma_timeouts() == 0
+    finally:
+        svi.set_fft_choice(shape, -1, -1, -1)

@@ -1,6 +1,7 @@
 """Launch modes change timing only: the same solve with dependent launches off (SVIE_PDL=0), with every
-grid shape's convolution forms tuned (SVIE_FFT_TUNE=all) and with the TMA tile loads of the convolution
-passes replaced by cp.async (SVIE_TMA=0) gives the default run's results bit for bit.  Each mode runs in
+grid shape's convolution forms tuned (SVIE_FFT_TUNE=all), with the TMA tile loads of the convolution
+passes replaced by cp.async (SVIE_TMA=0) and with the y and x passes compiled for every shape's axis
+lengths (SVIE_FFT_JIT=all) gives the default run's results bit for bit.  Each mode runs in
 its own process, because the switches are read once per process."""
 
 import json
@@ -48,5 +49,5 @@ def test_dependent_launches_and_tuning_change_no_bits():
     base = _run({"SVIE_PDL": "1", "SVIE_FFT_TUNE": "1"})
     assert len(base["svi"]["fractions"]) == 12 and len(base["mean"]["fractions"]) == 30
     assert base["tma_timeouts"] == 0
-    for extra in ({"SVIE_PDL": "0"}, {"SVIE_FFT_TUNE": "all"}, {"SVIE_TMA": "0"}):
+    for extra in ({"SVIE_PDL": "0"}, {"SVIE_FFT_TUNE": "all"}, {"SVIE_TMA": "0"}, {"SVIE_FFT_JIT": "all"}):
         assert _run(extra) == base, extra
