@@ -115,176 +115,23 @@ SVIE_DEV bool mbar_wait_bounded(uint64_t* bar, unsigned int phase) {
 }
 
 // ----------------------------------------------------------------- z passes
-// Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
-// A CTA takes 2 LW real lines, packed in pairs into LW complex lines (one
-// contiguous chunk of the input); a warp loads one pair, lanes along z.
-// `lineflag` (optional): lines whose flag lacks bit 0 hold no solid, so their
-// input is zero; a tile without any such line only writes zeros.
+// The bodies are z_r2c_body / z_c2r_body in fft_dev.cuh.
 template <int LW, int PS>
 __global__ void __launch_bounds__(FFT_T) k_fft_z_r2c(const float* __restrict__ in, float2* __restrict__ out,
                                                      AxisPlan P, long long nlines, int nzp,
                                                      const uint8_t* __restrict__ lineflag) {
   pdl_wait();
   pdl_release();
-  extern __shared__ float2 sm[];
-  const int n = P.n, nh = n / 2 + 1;
-  float2* sa = sm;
-  float2* sb = sm + PS * n;
-  const long long line0 = (long long)blockIdx.x * 2 * LW;
-  const int nl = (int)min((long long)2 * LW, nlines - line0);
-  const float* src = in + line0 * n;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int NW = FFT_T / 32;
-  if (lineflag) {
-    const int any = __syncthreads_or(threadIdx.x < nl ? (__ldg(lineflag + line0 + threadIdx.x) & 1) : 0);
-    if (!any) {
-      float2* dst = out + line0 * nzp;
-      for (int l = warp; l < nl; l += NW)
-        for (int k = lane; k < nh; k += 32) dst[(long long)l * nzp + k] = make_float2(0.f, 0.f);
-      return;
-    }
-  }
-  // the whole tile in flight at once: 4-byte asynchronous copies straight into
-  // the paired layout, lanes along (z, line of the pair) so that both the
-  // global reads (two 64-byte runs) and the shared writes are contiguous
-  float* sf = reinterpret_cast<float*>(sa);
-  for (int w = warp; w < LW; w += NW) {
-    const int par = lane & 1, l = 2 * w + par;
-    const bool ok = l < nl && (!lineflag || (__ldg(lineflag + line0 + l) & 1));
-    const float* g = src + (long long)l * n;
-    for (int z = lane >> 1; z < n; z += 16) {
-      float* d = sf + 2 * (z * PS + w) + par;
-      if (ok) cp_async4(d, g + z);
-      else *d = 0.0f;
-    }
-  }
-  cp_async_commit();
-  const float2* stw = stage_twiddles_to_smem(sm, PS, P);
-  cp_async_wait<0>();
-  __syncthreads();
-  const float2* r = run_tile_fft<LW, PS>(sa, sb, P, stw);
-  // untangle the two real spectra of each pair: X1 = (C_k + conj C_{n-k}) / 2,
-  // X2 = (C_k - conj C_{n-k}) / (2 i)
-  float2* dst = out + line0 * nzp;
-  for (int w = warp; 2 * w < nl; w += NW) {
-    const bool has2 = 2 * w + 1 < nl;
-    float2* d0 = dst + (long long)(2 * w) * nzp;
-    for (int k = lane; k < nh; k += 32) {
-      const float2 a = r[k * PS + w];
-      const float2 b = r[(k == 0 ? 0 : n - k) * PS + w];
-      d0[k] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
-      if (has2) d0[nzp + k] = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
-    }
-  }
+  z_r2c_body<LW, PS>(in, out, P, nlines, nzp, lineflag, PlanStages<LW, PS>{P});
 }
 
-// Real lines 2w (real parts) and 2w + 1 (imaginary parts, negated: the
-// inverse-by-forward transform) of the tile to dst = out + line0 * n,
-// out = beta + alpha * value; with `lineflag`, only lines with bit 1.
-template <int LW, int PS>
-SVIE_DEV void c2r_store(const float2* __restrict__ r, float* __restrict__ dst, int n, int nl, long long line0,
-                        float alpha, float beta, const uint8_t* __restrict__ lineflag) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int NW = FFT_T / 32;
-  for (int w = warp; 2 * w < nl; w += NW) {
-    const int l0 = 2 * w, l1 = 2 * w + 1;
-    const bool w0 = !lineflag || (__ldg(lineflag + line0 + l0) & 2);
-    const bool w1 = l1 < nl && (!lineflag || (__ldg(lineflag + line0 + l1) & 2));
-    if (!w0 && !w1) continue;
-    float* d0 = dst + (long long)l0 * n;
-    for (int z = lane; z < n; z += 32) {
-      const float2 v = r[z * PS + w];
-      if (w0) d0[z] = beta + alpha * v.x;
-      if (w1) d0[n + z] = beta + alpha * (-v.y);
-    }
-  }
-}
-
-// Inverse: half spectra -> real lines, out = beta + alpha * irfft_unnormalised.
-// `lineflag` (optional): only lines with bit 1 set are written (the others
-// are never read); a tile without such lines returns at once.
 template <int LW, int PS>
 __global__ void __launch_bounds__(FFT_T) k_fft_z_c2r(const float2* __restrict__ in, float* __restrict__ out,
                                                      AxisPlan P, long long nlines, int nzp, float alpha, float beta,
                                                      const uint8_t* __restrict__ lineflag) {
   pdl_wait();
   pdl_release();
-  extern __shared__ float2 sm[];
-  const int n = P.n;
-  float2* sa = sm;
-  float2* sb = sm + PS * n;
-  const long long line0 = (long long)blockIdx.x * 2 * LW;
-  const int nl = (int)min((long long)2 * LW, nlines - line0);
-  if (lineflag) {
-    const int any = __syncthreads_or(threadIdx.x < nl ? (__ldg(lineflag + line0 + threadIdx.x) & 2) : 0);
-    if (!any) return;
-  }
-  const float2* src = in + line0 * nzp;
-  const bool even = (n & 1) == 0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nzh = n / 2 + 1;
-  constexpr int NW = FFT_T / 32;
-  // C_k = X1_k + i X2_k over k = 0..n-1 (X_{n-k} = conj X_k), stored
-  // conjugated for the inverse-by-forward transform
-  auto combine = [&](float2 a, float2 b, int k, int kk) {
-    if (kk == 0 || (even && kk == n / 2)) { a.y = 0.f; b.y = 0.f; }
-    if (k > n / 2) { a.y = -a.y; b.y = -b.y; }
-    return make_float2(a.x - b.y, -(a.y + b.x));
-  };
-  if (2 * LW * nzh <= PS * n) {
-    // the 2 LW half spectra land in the idle second buffer with 8-byte
-    // asynchronous copies (all in flight at once), then C is built from there
-    for (int l = warp; l < 2 * LW; l += NW) {
-      float2* d = sb + l * nzh;
-      const float2* g = src + (long long)l * nzp;
-      for (int k = lane; k < nzh; k += 32) {
-        if (l < nl) cp_async8(d + k, g + k);
-        else d[k] = make_float2(0.f, 0.f);
-      }
-    }
-    cp_async_commit();
-    const float2* stw = stage_twiddles_to_smem(sm, PS, P);
-    cp_async_wait<0>();
-    __syncthreads();
-    for (int w = warp; w < LW; w += NW) {
-      const float2* x1 = sb + (2 * w) * nzh;
-      const float2* x2 = x1 + nzh;
-      for (int k = lane; k < n; k += 32) {
-        const int kk = k > n / 2 ? n - k : k;
-        sa[k * PS + w] = combine(x1[kk], x2[kk], k, kk);
-      }
-    }
-    __syncthreads();
-    const float2* r = run_tile_fft<LW, PS>(sa, sb, P, stw);
-    c2r_store<LW, PS>(r, out + line0 * n, n, nl, line0, alpha, beta, lineflag);
-    return;
-  }
-  const float2* stw = stage_twiddles_to_smem(sm, PS, P);
-  for (int w = warp; w < LW; w += NW) {
-    const bool has1 = 2 * w < nl, has2 = 2 * w + 1 < nl;
-    const float2* s1 = src + (long long)(2 * w) * nzp;
-    const float2* s2 = s1 + nzp;
-    // four positions of both half spectra in flight per thread before the stores
-    for (int k0 = lane; k0 < n; k0 += 4 * 32) {
-      float2 x1[4], x2[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int k = k0 + 32 * u;
-        const int kk = k > n / 2 ? n - k : k;
-        x1[u] = (has1 && k < n) ? __ldg(s1 + kk) : make_float2(0.f, 0.f);
-        x2[u] = (has2 && k < n) ? __ldg(s2 + kk) : make_float2(0.f, 0.f);
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int k = k0 + 32 * u;
-        if (k >= n) break;
-        const int kk = k > n / 2 ? n - k : k;
-        sa[k * PS + w] = combine(x1[u], x2[u], k, kk);
-      }
-    }
-  }
-  __syncthreads();
-  const float2* r = run_tile_fft<LW, PS>(sa, sb, P, stw);
-  c2r_store<LW, PS>(r, out + line0 * n, n, nl, line0, alpha, beta, lineflag);
+  z_c2r_body<LW, PS>(in, out, P, nlines, nzp, alpha, beta, lineflag, PlanStages<LW, PS>{P});
 }
 
 // ------------------------------------------------------------ strided passes
@@ -929,9 +776,23 @@ static void launch_z_as(const Plans& P, long long nlines, int nzp, const float* 
 }
 
 static void launch_z(const Plans& P, int nx, int ny, int nz, const float* f, float2* spec, float* out, bool fwd,
-                     float alpha, float beta, cudaStream_t s, const uint8_t* lineflag, int c, bool chained) {
+                     float alpha, float beta, cudaStream_t s, const uint8_t* lineflag, int c, bool chained,
+                     bool jit = false) {
   const long long nlines = (long long)nx * ny;
   const int nzp = padded_nzh(nz);
+  CUfunction r2c = nullptr, c2r = nullptr;
+  if (c == 0 && jit && jit_z(nz, P.z.radices, P.z.nst, &r2c, &c2r) == SVIE_OK) {
+    const dim3 grid((unsigned)((nlines + 31) / 32)), block(FFT_T);
+    AxisPlan az = P.z;
+    long long nl = nlines;
+    int nzp_ = nzp;
+    float a = alpha, b = beta;
+    const float* fin = f;
+    const float2* spec_in = spec;
+    void* fargs[] = {&fin, &spec, &az, &nl, &nzp_, &lineflag};
+    void* iargs[] = {&spec_in, &out, &az, &nl, &nzp_, &a, &b, &lineflag};
+    if (jit_launch(fwd ? r2c : c2r, grid, block, tile_smem(17, nz), s, chained, fwd ? fargs : iargs)) return;
+  }
   if (c == 0) launch_z_as<16, 17>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag, chained);
   else if (c == 1) launch_z_as<8, 9>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag, chained);
   else launch_z_as<1, 1>(P, nlines, nzp, f, spec, out, fwd, alpha, beta, s, lineflag, chained);
@@ -1155,11 +1016,11 @@ int svie_conv_apply(const void* plan, int nx, int ny, int nz, const float* f, fl
   cudaStream_t s = (cudaStream_t)stream;
   float2* spec = (float2*)ws;
   const FftChoice c = choice_for(nx, ny, nz);
-  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z, false);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z, false, c.jit);
   launch_y(P, nx, ny, nz, spec, 0, s, nullptr, c.y, true, c.jit);
   launch_x(P, nx, ny, nz, spec, 2, s, c.x, true, c.jit);
   launch_y(P, nx, ny, nz, spec, 1, s, nullptr, c.y, true, c.jit);
-  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z, true);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z, true, c.jit);
   return launch_status("svie_conv_apply", 5);
 }
 
@@ -1185,7 +1046,7 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
   // with timing events between the passes every pass is an ordinary launch
   const bool ch = ev == nullptr;
   if (ev) cudaEventRecord(ev[0], s);
-  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, lineflag, c.z, false);
+  launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, lineflag, c.z, false, c.jit);
   if (ev) cudaEventRecord(ev[1], s);
   launch_y(P, nx, ny, nz, spec, 0, s, slabflag, c.y, ch, c.jit);
   if (ev) cudaEventRecord(ev[2], s);
@@ -1193,7 +1054,7 @@ int svie_conv_apply_masked(const void* plan, int nx, int ny, int nz, const float
   if (ev) cudaEventRecord(ev[3], s);
   launch_y(P, nx, ny, nz, spec, 1, s, slabflag, c.y, ch, c.jit);
   if (ev) cudaEventRecord(ev[4], s);
-  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag, c.z, ch);
+  launch_z(P, nx, ny, nz, nullptr, spec, out, false, (float)alpha, (float)beta, s, lineflag, c.z, ch, c.jit);
   if (ev) cudaEventRecord(ev[5], s);
   return launch_status("svie_conv_apply_masked", 5);
 }
@@ -1243,9 +1104,10 @@ int svie_conv_jit(int nx, int ny, int nz) {
     set_error("svie_conv_jit: the 8-line passes do not fit shared memory on %d x %d x %d", nx, ny, nz);
     return SVIE_ERR_UNSUPPORTED;
   }
-  CUfunction fy = nullptr, fx = nullptr;
+  CUfunction fy = nullptr, fx = nullptr, zf = nullptr, zi = nullptr;
   int st = jit_strided(ny, 4, ay.radices, ay.nst, &fy);
   if (st == SVIE_OK) st = jit_strided(nx, 3, ax.radices, ax.nst, &fx);
+  if (st == SVIE_OK && fits(z_smem(0, nz))) st = jit_z(nz, az.radices, az.nst, &zf, &zi);
   if (st != SVIE_OK) return st;
   const GridKey k = grid_key(nx, ny, nz);
   std::lock_guard<std::mutex> lock(g_choice_mu);
@@ -1260,11 +1122,12 @@ int svie_conv_jit_enabled(int nx, int ny, int nz) { return choice_for(nx, ny, nz
 
 int svie_conv_jit_source(int n, int minb, char* buf, size_t buf_bytes) {
   AxisPlan a;
-  if (!factor_axis(n, &a) || minb < 1 || minb > 8 || !buf) {
+  if (!factor_axis(n, &a) || minb < 0 || minb > 8 || !buf) {
     set_error("svie_conv_jit_source: bad arguments");
     return SVIE_ERR_ARG;
   }
-  const std::string src = jit_strided_source_for_test(n, minb, a.radices, a.nst);
+  const std::string src = minb ? jit_strided_source_for_test(n, minb, a.radices, a.nst)
+                               : jit_z_source_for_test(n, a.radices, a.nst);
   if (src.size() + 1 > buf_bytes) {
     set_error("svie_conv_jit_source: %zu bytes needed", src.size() + 1);
     return SVIE_ERR_CAPACITY;
@@ -1311,8 +1174,8 @@ int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, flo
   for (int c = 0; c < FFT_NCHOICE && !failed; ++c) {
     if (tunable_z(c, nz)) {  // forward and inverse z
       const float t = time_form([&] {
-        launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c, false);
-        launch_z(P, nx, ny, nz, nullptr, spec, out, false, 1.f, 0.f, s, nullptr, c, false);
+        launch_z(P, nx, ny, nz, f, spec, nullptr, true, 0.f, 0.f, s, nullptr, c, false, d.jit);
+        launch_z(P, nx, ny, nz, nullptr, spec, out, false, 1.f, 0.f, s, nullptr, c, false, d.jit);
         launched += 2;
       }, reps, s, e0, e1);
       if (t < 0.f) failed = true;
@@ -1386,7 +1249,7 @@ int svie_rfft3(const void* plan, int nx, int ny, int nz, const float* f, void* s
   if ((st = ensure_smem_attr())) return st;
   cudaStream_t s = (cudaStream_t)stream;
   const FftChoice c = choice_for(nx, ny, nz);
-  launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z, false);
+  launch_z(P, nx, ny, nz, f, (float2*)spec, nullptr, true, 0.f, 0.f, s, nullptr, c.z, false, c.jit);
   launch_y(P, nx, ny, nz, (float2*)spec, 0, s, nullptr, c.y, true, c.jit);
   launch_x(P, nx, ny, nz, (float2*)spec, 0, s, c.x, true, c.jit);
   return launch_status("svie_rfft3", 3);
@@ -1406,7 +1269,8 @@ int svie_irfft3(const void* plan, int nx, int ny, int nz, void* spec, float* out
   const FftChoice c = choice_for(nx, ny, nz);
   launch_x(P, nx, ny, nz, (float2*)spec, 1, s, c.x, false, c.jit);
   launch_y(P, nx, ny, nz, (float2*)spec, 1, s, nullptr, c.y, true, c.jit);
-  launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z, true);
+  launch_z(P, nx, ny, nz, nullptr, (float2*)spec, out, false, (float)alpha, (float)beta, s, nullptr, c.z, true,
+           c.jit);
   return launch_status("svie_irfft3", 3);
 }
 

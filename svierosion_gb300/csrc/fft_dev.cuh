@@ -359,6 +359,183 @@ struct KGeom {
   int ny, nzh;
 };
 
+// ----------------------------------------------------------------- z passes
+// The stages of a whole tile transform, from buffer a, ping-ponging with b;
+// the buffer holding the result is returned.  PlanStages runs the plan's radix
+// sequence at run time (the z pass kernels of fft.cu); the z passes compiled
+// for one axis length pass a functor with the stages unrolled.
+template <int LW, int PS>
+struct PlanStages {
+  const AxisPlan& P;
+  SVIE_DEV float2* operator()(float2* a, float2* b, const float2* stw) const { return run_tile_fft<LW, PS>(a, b, P, stw); }
+};
+
+// Forward: real lines [nlines][n] -> half spectra at out[line * nzp + k].
+// A CTA takes 2 LW real lines, packed in pairs into LW complex lines (one
+// contiguous chunk of the input); a warp loads one pair, lanes along z.
+// `lineflag` (optional): lines whose flag lacks bit 0 hold no solid, so their
+// input is zero; a tile without any such line only writes zeros.
+template <int LW, int PS, class Stages>
+SVIE_DEV void z_r2c_body(const float* __restrict__ in, float2* __restrict__ out, const AxisPlan& P, long long nlines,
+                         int nzp, const uint8_t* __restrict__ lineflag, const Stages& stages) {
+  extern __shared__ float2 sm[];
+  const int n = P.n, nh = n / 2 + 1;
+  float2* sa = sm;
+  float2* sb = sm + PS * n;
+  const long long line0 = (long long)blockIdx.x * 2 * LW;
+  const int nl = (int)min((long long)2 * LW, nlines - line0);
+  const float* src = in + line0 * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = FFT_T / 32;
+  if (lineflag) {
+    const int any = __syncthreads_or(threadIdx.x < nl ? (__ldg(lineflag + line0 + threadIdx.x) & 1) : 0);
+    if (!any) {
+      float2* dst = out + line0 * nzp;
+      for (int l = warp; l < nl; l += NW)
+        for (int k = lane; k < nh; k += 32) dst[(long long)l * nzp + k] = make_float2(0.f, 0.f);
+      return;
+    }
+  }
+  // the whole tile in flight at once: 4-byte asynchronous copies straight into
+  // the paired layout, lanes along (z, line of the pair) so that both the
+  // global reads (two 64-byte runs) and the shared writes are contiguous
+  float* sf = reinterpret_cast<float*>(sa);
+  for (int w = warp; w < LW; w += NW) {
+    const int par = lane & 1, l = 2 * w + par;
+    const bool ok = l < nl && (!lineflag || (__ldg(lineflag + line0 + l) & 1));
+    const float* g = src + (long long)l * n;
+    for (int z = lane >> 1; z < n; z += 16) {
+      float* d = sf + 2 * (z * PS + w) + par;
+      if (ok) cp_async4(d, g + z);
+      else *d = 0.0f;
+    }
+  }
+  cp_async_commit();
+  const float2* stw = stage_twiddles_to_smem(sm, PS, P);
+  cp_async_wait<0>();
+  __syncthreads();
+  const float2* r = stages(sa, sb, stw);
+  // untangle the two real spectra of each pair: X1 = (C_k + conj C_{n-k}) / 2,
+  // X2 = (C_k - conj C_{n-k}) / (2 i)
+  float2* dst = out + line0 * nzp;
+  for (int w = warp; 2 * w < nl; w += NW) {
+    const bool has2 = 2 * w + 1 < nl;
+    float2* d0 = dst + (long long)(2 * w) * nzp;
+    for (int k = lane; k < nh; k += 32) {
+      const float2 a = r[k * PS + w];
+      const float2 b = r[(k == 0 ? 0 : n - k) * PS + w];
+      d0[k] = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+      if (has2) d0[nzp + k] = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
+    }
+  }
+}
+
+// Real lines 2w (real parts) and 2w + 1 (imaginary parts, negated: the
+// inverse-by-forward transform) of the tile to dst = out + line0 * n,
+// out = beta + alpha * value; with `lineflag`, only lines with bit 1.
+template <int LW, int PS>
+SVIE_DEV void c2r_store(const float2* __restrict__ r, float* __restrict__ dst, int n, int nl, long long line0,
+                        float alpha, float beta, const uint8_t* __restrict__ lineflag) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = FFT_T / 32;
+  for (int w = warp; 2 * w < nl; w += NW) {
+    const int l0 = 2 * w, l1 = 2 * w + 1;
+    const bool w0 = !lineflag || (__ldg(lineflag + line0 + l0) & 2);
+    const bool w1 = l1 < nl && (!lineflag || (__ldg(lineflag + line0 + l1) & 2));
+    if (!w0 && !w1) continue;
+    float* d0 = dst + (long long)l0 * n;
+    for (int z = lane; z < n; z += 32) {
+      const float2 v = r[z * PS + w];
+      if (w0) d0[z] = beta + alpha * v.x;
+      if (w1) d0[n + z] = beta + alpha * (-v.y);
+    }
+  }
+}
+
+// Inverse: half spectra -> real lines, out = beta + alpha * irfft_unnormalised.
+// `lineflag` (optional): only lines with bit 1 set are written (the others
+// are never read); a tile without such lines returns at once.
+template <int LW, int PS, class Stages>
+SVIE_DEV void z_c2r_body(const float2* __restrict__ in, float* __restrict__ out, const AxisPlan& P, long long nlines,
+                         int nzp, float alpha, float beta, const uint8_t* __restrict__ lineflag, const Stages& stages) {
+  extern __shared__ float2 sm[];
+  const int n = P.n;
+  float2* sa = sm;
+  float2* sb = sm + PS * n;
+  const long long line0 = (long long)blockIdx.x * 2 * LW;
+  const int nl = (int)min((long long)2 * LW, nlines - line0);
+  if (lineflag) {
+    const int any = __syncthreads_or(threadIdx.x < nl ? (__ldg(lineflag + line0 + threadIdx.x) & 2) : 0);
+    if (!any) return;
+  }
+  const float2* src = in + line0 * nzp;
+  const bool even = (n & 1) == 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nzh = n / 2 + 1;
+  constexpr int NW = FFT_T / 32;
+  // C_k = X1_k + i X2_k over k = 0..n-1 (X_{n-k} = conj X_k), stored
+  // conjugated for the inverse-by-forward transform
+  auto combine = [&](float2 a, float2 b, int k, int kk) {
+    if (kk == 0 || (even && kk == n / 2)) { a.y = 0.f; b.y = 0.f; }
+    if (k > n / 2) { a.y = -a.y; b.y = -b.y; }
+    return make_float2(a.x - b.y, -(a.y + b.x));
+  };
+  if (2 * LW * nzh <= PS * n) {
+    // the 2 LW half spectra land in the idle second buffer with 8-byte
+    // asynchronous copies (all in flight at once), then C is built from there
+    for (int l = warp; l < 2 * LW; l += NW) {
+      float2* d = sb + l * nzh;
+      const float2* g = src + (long long)l * nzp;
+      for (int k = lane; k < nzh; k += 32) {
+        if (l < nl) cp_async8(d + k, g + k);
+        else d[k] = make_float2(0.f, 0.f);
+      }
+    }
+    cp_async_commit();
+    const float2* stw = stage_twiddles_to_smem(sm, PS, P);
+    cp_async_wait<0>();
+    __syncthreads();
+    for (int w = warp; w < LW; w += NW) {
+      const float2* x1 = sb + (2 * w) * nzh;
+      const float2* x2 = x1 + nzh;
+      for (int k = lane; k < n; k += 32) {
+        const int kk = k > n / 2 ? n - k : k;
+        sa[k * PS + w] = combine(x1[kk], x2[kk], k, kk);
+      }
+    }
+    __syncthreads();
+    const float2* r = stages(sa, sb, stw);
+    c2r_store<LW, PS>(r, out + line0 * n, n, nl, line0, alpha, beta, lineflag);
+    return;
+  }
+  const float2* stw = stage_twiddles_to_smem(sm, PS, P);
+  for (int w = warp; w < LW; w += NW) {
+    const bool has1 = 2 * w < nl, has2 = 2 * w + 1 < nl;
+    const float2* s1 = src + (long long)(2 * w) * nzp;
+    const float2* s2 = s1 + nzp;
+    // four positions of both half spectra in flight per thread before the stores
+    for (int k0 = lane; k0 < n; k0 += 4 * 32) {
+      float2 x1[4], x2[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + 32 * u;
+        const int kk = k > n / 2 ? n - k : k;
+        x1[u] = (has1 && k < n) ? __ldg(s1 + kk) : make_float2(0.f, 0.f);
+        x2[u] = (has2 && k < n) ? __ldg(s2 + kk) : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + 32 * u;
+        if (k >= n) break;
+        const int kk = k > n / 2 ? n - k : k;
+        sa[k * PS + w] = combine(x1[u], x2[u], k, kk);
+      }
+    }
+  }
+  __syncthreads();
+  const float2* r = stages(sa, sb, stw);
+  c2r_store<LW, PS>(r, out + line0 * n, n, nl, line0, alpha, beta, lineflag);
+}
+
 // ------------------------------------------- stages with compile-time shape
 // tile_stage and last_stage with the radix R, the butterfly columns M = n / R
 // and the span P as constants (the pass kernels compiled for one axis length):

@@ -176,6 +176,39 @@ std::string strided_source(int n, int minb, const std::vector<int>& r) {
   return s;
 }
 
+// Source of the z passes (16 line pairs per CTA at position stride 17) for an
+// axis of n positions: z_r2c_body / z_c2r_body of fft_dev.cuh with the tile
+// transform's stages unrolled at compile time.
+std::string z_source(int n, const std::vector<int>& r) {
+  std::string s;
+  char buf[512];
+  s += "#include \"fft_dev.cuh\"\nnamespace svie {\nstruct JitStages {\n"
+       "  SVIE_DEV float2* operator()(float2* a, float2* b, const float2* stw) const {\n";
+  const char* cur = "a";
+  const char* oth = "b";
+  int p = 1;
+  for (int st = 0; st < (int)r.size(); ++st) {
+    snprintf(buf, sizeof(buf), "    tile_stage_c<%d, %d, %d, 16, 17, 256>(%s, %s, stw, false);\n", r[st], n / r[st], p,
+             cur, oth);
+    s += buf;
+    std::swap(cur, oth);
+    p *= r[st];
+  }
+  snprintf(buf, sizeof(buf), "    return %s;\n  }\n};\n", cur);
+  s += buf;
+  s += "extern \"C\" __global__ void __launch_bounds__(256) svie_jit_z_r2c(const float* __restrict__ in,\n"
+       "    float2* __restrict__ out, AxisPlan P, long long nlines, int nzp, const uint8_t* __restrict__ lineflag) {\n"
+       "  pdl_wait();\n  pdl_release();\n"
+       "  z_r2c_body<16, 17>(in, out, P, nlines, nzp, lineflag, JitStages{});\n}\n"
+       "extern \"C\" __global__ void __launch_bounds__(256) svie_jit_z_c2r(const float2* __restrict__ in,\n"
+       "    float* __restrict__ out, AxisPlan P, long long nlines, int nzp, float alpha, float beta,\n"
+       "    const uint8_t* __restrict__ lineflag) {\n"
+       "  pdl_wait();\n  pdl_release();\n"
+       "  z_c2r_body<16, 17>(in, out, P, nlines, nzp, alpha, beta, lineflag, JitStages{});\n}\n"
+       "}  // namespace svie\n";
+  return s;
+}
+
 // Compiles a source for the current device; the cubin, or an empty vector
 // with the log in *err.
 std::vector<char> compile(const std::string& src, std::string* err) {
@@ -212,52 +245,87 @@ std::vector<char> compile(const std::string& src, std::string* err) {
   return out;
 }
 
+// kind 0: the strided pass (minb CTAs per SM); kind 1: the z passes (minb 0)
 struct Key {
   CUcontext ctx;
-  int n, minb;
-  bool operator<(const Key& o) const { return std::tie(ctx, n, minb) < std::tie(o.ctx, o.n, o.minb); }
+  int kind, n, minb;
+  bool operator<(const Key& o) const {
+    return std::tie(ctx, kind, n, minb) < std::tie(o.ctx, o.kind, o.n, o.minb);
+  }
+};
+struct Fns {
+  CUfunction f[2] = {nullptr, nullptr};  // all null: tried and failed
 };
 std::mutex g_mu;
-std::map<Key, CUfunction> g_fn;  // nullptr: tried and failed
+std::map<Key, Fns> g_fn;
+
+// The kernels `names` of a generated source, compiled and loaded once per key.
+int jit_get(const Key& key, const std::string& src, const char* const* names, int count, CUfunction* out) {
+  const Driver& d = driver();
+  std::lock_guard<std::mutex> lock(g_mu);
+  auto it = g_fn.find(key);
+  if (it == g_fn.end()) {
+    Fns fns;
+    std::string err;
+    const std::vector<char> cubin = compile(src, &err);
+    CUmodule mod = nullptr;
+    bool ok = !cubin.empty() && d.load(&mod, cubin.data()) == CUDA_SUCCESS;
+    for (int k = 0; ok && k < count; ++k)
+      ok = d.get_function(&fns.f[k], mod, names[k]) == CUDA_SUCCESS &&
+           d.set_attribute(fns.f[k], CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 227 * 1024) == CUDA_SUCCESS;
+    if (!ok) {
+      fns = Fns();
+      set_error("fft jit: no pass for n = %d: %s", key.n, err.empty() ? "module load failed" : err.c_str());
+    }
+    it = g_fn.emplace(key, fns).first;
+  }
+  for (int k = 0; k < count; ++k) out[k] = it->second.f[k];
+  if (!out[0]) {
+    set_error("fft jit: the pass for n = %d did not compile", key.n);
+    return SVIE_ERR_UNSUPPORTED;
+  }
+  return SVIE_OK;
+}
+
+std::vector<int> radix_list(unsigned long long radices, int nst) {
+  std::vector<int> r;
+  for (int st = 0; st < nst; ++st) r.push_back((int)((radices >> (4 * st)) & 15ULL));
+  return r;
+}
+
+bool current_context(CUcontext* ctx) {
+  const Driver& d = driver();
+  if (!d.ok) {
+    set_error("fft jit: driver entry points not found");
+    return false;
+  }
+  if (d.ctx_current(ctx) != CUDA_SUCCESS || !*ctx) {
+    set_error("fft jit: no current CUDA context");
+    return false;
+  }
+  return true;
+}
 
 }  // namespace
 
 int jit_strided(int n, int minb, unsigned long long radices, int nst, CUfunction* fn) {
   *fn = nullptr;
-  const Driver& d = driver();
-  if (!d.ok) {
-    set_error("fft jit: driver entry points not found");
-    return SVIE_ERR_UNSUPPORTED;
-  }
   CUcontext ctx = nullptr;
-  if (d.ctx_current(&ctx) != CUDA_SUCCESS || !ctx) {
-    set_error("fft jit: no current CUDA context");
-    return SVIE_ERR_LAUNCH;
-  }
-  const Key key{ctx, n, minb};
-  std::lock_guard<std::mutex> lock(g_mu);
-  auto it = g_fn.find(key);
-  if (it != g_fn.end()) {
-    *fn = it->second;
-    if (!*fn) set_error("fft jit: the pass for n = %d did not compile earlier", n);
-    return *fn ? SVIE_OK : SVIE_ERR_UNSUPPORTED;
-  }
-  std::vector<int> r;
-  for (int st = 0; st < nst; ++st) r.push_back((int)((radices >> (4 * st)) & 15ULL));
-  std::string err;
-  const std::vector<char> cubin = compile(strided_source(n, minb, r), &err);
-  CUfunction f = nullptr;
-  CUmodule mod = nullptr;
-  if (!cubin.empty() && d.load(&mod, cubin.data()) == CUDA_SUCCESS &&
-      d.get_function(&f, mod, "svie_jit_strided") == CUDA_SUCCESS &&
-      d.set_attribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 227 * 1024) == CUDA_SUCCESS) {
-    g_fn[key] = f;
-    *fn = f;
-    return SVIE_OK;
-  }
-  g_fn[key] = nullptr;
-  set_error("fft jit: no pass for n = %d: %s", n, err.empty() ? "module load failed" : err.c_str());
-  return SVIE_ERR_UNSUPPORTED;
+  if (!current_context(&ctx)) return SVIE_ERR_UNSUPPORTED;
+  const char* names[] = {"svie_jit_strided"};
+  return jit_get(Key{ctx, 0, n, minb}, strided_source(n, minb, radix_list(radices, nst)), names, 1, fn);
+}
+
+int jit_z(int n, unsigned long long radices, int nst, CUfunction* r2c, CUfunction* c2r) {
+  *r2c = *c2r = nullptr;
+  CUcontext ctx = nullptr;
+  if (!current_context(&ctx)) return SVIE_ERR_UNSUPPORTED;
+  const char* names[] = {"svie_jit_z_r2c", "svie_jit_z_c2r"};
+  CUfunction f[2] = {nullptr, nullptr};
+  const int st = jit_get(Key{ctx, 1, n, 0}, z_source(n, radix_list(radices, nst)), names, 2, f);
+  *r2c = f[0];
+  *c2r = f[1];
+  return st;
 }
 
 bool jit_launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool chained, void** args) {
@@ -280,9 +348,11 @@ bool jit_launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, cudaStream_t 
 }
 
 std::string jit_strided_source_for_test(int n, int minb, unsigned long long radices, int nst) {
-  std::vector<int> r;
-  for (int st = 0; st < nst; ++st) r.push_back((int)((radices >> (4 * st)) & 15ULL));
-  return strided_source(n, minb, r);
+  return strided_source(n, minb, radix_list(radices, nst));
+}
+
+std::string jit_z_source_for_test(int n, unsigned long long radices, int nst) {
+  return z_source(n, radix_list(radices, nst));
 }
 
 }  // namespace svie

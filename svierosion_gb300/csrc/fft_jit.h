@@ -14,11 +14,16 @@ namespace svie {
 // or the driver API missing, compilation or loading failed) with *fn = null.
 int jit_strided(int n, int minb, unsigned long long radices, int nst, CUfunction* fn);
 
+// The z passes (16 line pairs per CTA) compiled for an axis of n positions:
+// the forward (R2C) and inverse (C2R) kernels of one module.
+int jit_z(int n, unsigned long long radices, int nst, CUfunction* r2c, CUfunction* c2r);
+
 // Launches a compiled pass on `s` (a dependent launch when `chained`); false
 // when the launch failed (the caller then launches the library's pass).
 bool jit_launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool chained, void** args);
 
 // The generated source (for the CPU test that compiles it).
 std::string jit_strided_source_for_test(int n, int minb, unsigned long long radices, int nst);
+std::string jit_z_source_for_test(int n, unsigned long long radices, int nst);
 
 }  // namespace svie

@@ -1,5 +1,6 @@
-"""The convolution passes compiled at run time for one axis length: the generated source for a
-range of axis lengths (one to four radix stages, odd and even) compiles with NVRTC for sm_103a.
+"""The convolution passes compiled at run time for one axis length: the generated sources of the
+strided and z passes for a range of axis lengths (one to four radix stages, odd and even) compile
+with NVRTC for sm_103a.
 No device is needed; skipped when NVRTC cannot be loaded."""
 
 import ctypes
@@ -37,13 +38,15 @@ def _compile(nv, src: bytes):
     return rc, log.value.decode(errors="replace"), cubin.value
 
 
-@pytest.mark.parametrize("n,minb", [(336, 4), (448, 3), (245, 4), (90, 4), (7, 3), (1792, 3)])
+# minb 0: the z passes (forward and inverse); else the 8-line strided pass for that many CTAs per SM
+@pytest.mark.parametrize("n,minb", [(336, 4), (448, 3), (245, 4), (90, 4), (7, 3), (1792, 3), (245, 0), (175, 0),
+                                    (128, 0), (7, 0)])
 def test_generated_pass_compiles(n, minb):
     lib = _native.lib()
     buf = ctypes.create_string_buffer(1 << 16)
     assert lib.svie_conv_jit_source(n, minb, buf, len(buf)) == 0
     src = buf.value
-    assert b"svie_jit_strided" in src and b"tile_stage_c<" in src or n == 7
+    assert (b"svie_jit_z_r2c" in src if minb == 0 else b"svie_jit_strided" in src) and b"_stage_c<" in src
     nv = _nvrtc()
     rc, log, cubin = _compile(nv, src)
     assert rc == 0 and cubin > 0, log[:2000]
