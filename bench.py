@@ -333,6 +333,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     t_setup = time.time() - t_setup
     band0 = ls.work32.numel()
     sim.run(target_fraction=None, max_steps=args.warmup)
+    # the convolution passes compiled for this grid's axis lengths start compiling at its first
+    # convolution (background threads): part of the warm-up, finished before the timed steps
+    nat.lib().svie_conv_jit_wait(120000)
     # timed region: events only around each reinitialisation's sweeps (the
     # dominant kernel, one pair per call); the full per-kernel breakdown comes
     # from a second pass below.  Events between the convolution passes would

@@ -317,18 +317,23 @@ int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, flo
  * count could not be read. */
 unsigned int svie_conv_tma_timeouts(void);
 int svie_conv_get_choice(int nx, int ny, int nz, int* z, int* y, int* x);
-/* Passes compiled for the axis lengths: svie_conv_jit compiles (NVRTC) and
- * loads, in the current context, the 8-line y and x passes for ny and nx with
- * every stage's radix, column count and span as constants, and makes the
- * shape's 8-line y and x forms run them (same bits; the y pass at n = 336
- * measured 74 -> 64 us).  SVIE_OK, or SVIE_ERR_UNSUPPORTED when NVRTC or the
- * driver functions are missing, the compilation failed or the 8-line forms do
- * not fit.  Outside graph capture (it may synchronise for loading).
- * svie_conv_jit_enabled reports whether a shape runs them;
- * svie_conv_jit_source writes the generated source for an axis length into buf
- * (no device needed).  Replace nothing in the reference. */
+/* Passes compiled for the axis lengths.  svie_conv_jit starts compiling
+ * (NVRTC, on background threads, in the current context) the 8-line y and x
+ * passes for ny and nx and the z passes for nz, with every stage's radix,
+ * column count and span as constants, and makes the shape use each of them as
+ * soon as it is loaded (the library's passes run until then; the bits are the
+ * same).  SVIE_OK, or SVIE_ERR_UNSUPPORTED when NVRTC or the driver functions
+ * are missing or the 8-line forms do not fit.  svie_conv_jit_enabled reports
+ * whether the shape is set to use them, svie_conv_jit_ready whether all three
+ * are loaded, svie_conv_jit_wait waits up to timeout_ms for every compilation
+ * started (SVIE_ERR_LAUNCH when some still run).  svie_conv_jit_source writes
+ * the generated source for an axis length into buf (minb 0: the z passes, else
+ * the strided pass for minb CTAs per SM; no device needed).  Replace nothing
+ * in the reference. */
 int svie_conv_jit(int nx, int ny, int nz);
 int svie_conv_jit_enabled(int nx, int ny, int nz);
+int svie_conv_jit_ready(int nx, int ny, int nz);
+int svie_conv_jit_wait(int timeout_ms);
 int svie_conv_jit_source(int n, int minb, char* buf, size_t buf_bytes);
 int svie_conv_set_choice(int nx, int ny, int nz, int z, int y, int x);
 /* Full complex64 half spectrum K^ (rfftn of the wrapped kernel, svi.py:76-81). */

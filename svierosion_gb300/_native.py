@@ -144,6 +144,8 @@ _SIGS = {
     "svie_conv_tma_timeouts": (ctypes.c_uint, []),
     "svie_conv_jit": (I, [I, I, I]),
     "svie_conv_jit_enabled": (I, [I, I, I]),
+    "svie_conv_jit_ready": (I, [I, I, I]),
+    "svie_conv_jit_wait": (I, [I]),
     "svie_conv_jit_source": (I, [I, I, ctypes.c_char_p, Z]),
     "svie_conv_set_choice": (I, [I, I, I, I, I, I]),
     "svie_rfft3": (I, [V, I, I, I, V, V, V]),

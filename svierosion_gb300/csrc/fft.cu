@@ -1104,11 +1104,15 @@ int svie_conv_jit(int nx, int ny, int nz) {
     set_error("svie_conv_jit: the 8-line passes do not fit shared memory on %d x %d x %d", nx, ny, nz);
     return SVIE_ERR_UNSUPPORTED;
   }
+  if (!jit_available()) {
+    set_error("svie_conv_jit: NVRTC or the CUDA driver functions were not found");
+    return SVIE_ERR_UNSUPPORTED;
+  }
+  // request the three passes (their compilations start on background threads)
   CUfunction fy = nullptr, fx = nullptr, zf = nullptr, zi = nullptr;
-  int st = jit_strided(ny, 4, ay.radices, ay.nst, &fy);
-  if (st == SVIE_OK) st = jit_strided(nx, 3, ax.radices, ax.nst, &fx);
-  if (st == SVIE_OK && fits(z_smem(0, nz))) st = jit_z(nz, az.radices, az.nst, &zf, &zi);
-  if (st != SVIE_OK) return st;
+  jit_strided(ny, 4, ay.radices, ay.nst, &fy);
+  jit_strided(nx, 3, ax.radices, ax.nst, &fx);
+  if (fits(z_smem(0, nz))) jit_z(nz, az.radices, az.nst, &zf, &zi);
   const GridKey k = grid_key(nx, ny, nz);
   std::lock_guard<std::mutex> lock(g_choice_mu);
   auto it = g_choice.find(k);
@@ -1119,6 +1123,25 @@ int svie_conv_jit(int nx, int ny, int nz) {
 }
 
 int svie_conv_jit_enabled(int nx, int ny, int nz) { return choice_for(nx, ny, nz).jit ? 1 : 0; }
+
+int svie_conv_jit_ready(int nx, int ny, int nz) {
+  AxisPlan ax, ay, az;
+  if (!factor_axis(nx, &ax) || !factor_axis(ny, &ay) || !factor_axis(nz, &az) || !jit_available()) return 0;
+  CUfunction f = nullptr, g = nullptr;
+  if (jit_strided(ny, 4, ay.radices, ay.nst, &f) != SVIE_OK || jit_strided(nx, 3, ax.radices, ax.nst, &f) != SVIE_OK)
+    return 0;
+  return !fits(z_smem(0, nz)) || jit_z(nz, az.radices, az.nst, &f, &g) == SVIE_OK;
+}
+
+int svie_conv_jit_wait(int timeout_ms) {
+  if (timeout_ms < 0) {
+    set_error("svie_conv_jit_wait: negative timeout");
+    return SVIE_ERR_ARG;
+  }
+  const int st = jit_wait(timeout_ms);
+  if (st) set_error("svie_conv_jit_wait: compilations still running after %d ms", timeout_ms);
+  return st;
+}
 
 int svie_conv_jit_source(int n, int minb, char* buf, size_t buf_bytes) {
   AxisPlan a;

@@ -10,17 +10,24 @@
 // bits; on 448 x 336 x 245 the y pass measured 74 -> 64 us.
 //
 // NVRTC is opened with dlopen and the driver functions are reached through the
-// runtime's driver entry points, so the library links against neither.  When
-// either is missing or a compilation fails, no kernel is made and the caller
-// keeps the library's pass.  Kernels are kept per (CUDA context, axis length,
-// CTAs per SM) for the life of the process.
+// runtime's driver entry points, so the library links against neither.  A pass
+// is compiled by a background worker thread after its first request (about a second):
+// until it is loaded, and for good when NVRTC or the driver functions are
+// missing or the compilation fails, the caller runs the library's pass, whose
+// bits are the same.  Kernels are kept per (CUDA context, axis length, CTAs per
+// SM) for the life of the process.
 #include <cuda.h>
 #include <dlfcn.h>
 #include <stdio.h>
+#include <stdlib.h>
 
+#include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -64,6 +71,7 @@ const Nvrtc& nvrtc() {
 
 struct Driver {
   CUresult (*ctx_current)(CUcontext*) = nullptr;
+  CUresult (*ctx_set)(CUcontext) = nullptr;
   CUresult (*load)(CUmodule*, const void*) = nullptr;
   CUresult (*get_function)(CUfunction*, CUmodule, const char*) = nullptr;
   CUresult (*set_attribute)(CUfunction, CUfunction_attribute, int) = nullptr;
@@ -85,6 +93,7 @@ const Driver& driver() {
   static std::once_flag once;
   std::call_once(once, [] {
     entry("cuCtxGetCurrent", &d.ctx_current);
+    entry("cuCtxSetCurrent", &d.ctx_set);
     entry("cuModuleLoadData", &d.load);
     entry("cuModuleGetFunction", &d.get_function);
     entry("cuFuncSetAttribute", &d.set_attribute);
@@ -254,36 +263,115 @@ struct Key {
   }
 };
 struct Fns {
-  CUfunction f[2] = {nullptr, nullptr};  // all null: tried and failed
+  CUfunction f[2] = {nullptr, nullptr};
+  int state = 0;  // 0: compiling, 1: ready, -1: failed
 };
-std::mutex g_mu;
-std::map<Key, Fns> g_fn;
+// Allocated once and never destroyed: the worker thread may still wait on them
+// while the process exits, and destroying a condition variable with a waiter
+// can block the exit.
+std::mutex& g_mu = *new std::mutex;
+std::condition_variable& g_cv = *new std::condition_variable;
+std::map<Key, Fns>& g_fn = *new std::map<Key, Fns>;
 
-// The kernels `names` of a generated source, compiled and loaded once per key.
-int jit_get(const Key& key, const std::string& src, const char* const* names, int count, CUfunction* out) {
+// Compiles and loads `src` in the key's context and records its kernels
+// `names` (run on a background thread).
+void build_module(Key key, std::string src, std::vector<std::string> names) {
   const Driver& d = driver();
-  std::lock_guard<std::mutex> lock(g_mu);
+  Fns fns;
+  std::string err;
+  bool ok = d.ctx_set && d.ctx_set(key.ctx) == CUDA_SUCCESS;
+  const std::vector<char> cubin = ok ? compile(src, &err) : std::vector<char>();
+  CUmodule mod = nullptr;
+  ok = ok && !cubin.empty() && d.load(&mod, cubin.data()) == CUDA_SUCCESS;
+  for (size_t k = 0; ok && k < names.size(); ++k)
+    ok = d.get_function(&fns.f[k], mod, names[k].c_str()) == CUDA_SUCCESS &&
+         d.set_attribute(fns.f[k], CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 227 * 1024) == CUDA_SUCCESS;
+  if (!ok) {
+    fns = Fns();
+    fprintf(stderr, "[svie] fft jit: no pass for n = %d (%s); the library's pass is used\n", key.n,
+            err.empty() ? "context or module load failed" : err.c_str());
+  }
+  fns.state = ok ? 1 : -1;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_fn[key] = fns;
+  }
+  g_cv.notify_all();
+}
+
+// One background worker compiles the requested modules in turn (a served
+// stream may request many axis lengths at once; one core compiles them).  It
+// exits when idle for a moment and the next request starts a new one.  At
+// process exit, stop_worker drops the queued jobs and waits (bounded) for the
+// compilation in progress, so that no thread is inside NVRTC while the
+// libraries are torn down.
+struct Job {
+  Key key;
+  std::string src;
+  std::vector<std::string> names;
+};
+std::deque<Job>& g_jobs = *new std::deque<Job>;
+bool g_worker = false;   // a worker thread exists (under g_mu)
+bool g_busy = false;     // it is compiling (under g_mu)
+bool g_stop = false;     // the process is exiting (under g_mu)
+
+void stop_worker() {
+  std::unique_lock<std::mutex> lock(g_mu);
+  g_stop = true;
+  g_jobs.clear();
+  g_cv.wait_for(lock, std::chrono::seconds(10), [] { return !g_busy; });
+}
+
+void worker() {
+  for (;;) {
+    Job job;
+    {
+      std::unique_lock<std::mutex> lock(g_mu);
+      if (!g_cv.wait_for(lock, std::chrono::milliseconds(200), [] { return g_stop || !g_jobs.empty(); }) || g_stop) {
+        g_worker = false;
+        return;
+      }
+      job = std::move(g_jobs.front());
+      g_jobs.pop_front();
+      g_busy = true;
+    }
+    build_module(job.key, std::move(job.src), std::move(job.names));
+    {
+      std::lock_guard<std::mutex> lock(g_mu);
+      g_busy = false;
+    }
+    g_cv.notify_all();
+  }
+}
+
+// The kernels of a key when they are ready (SVIE_OK).  The first request
+// queues their compilation for the background worker and, like every request
+// until it is loaded, returns SVIE_ERR_UNSUPPORTED at once (the caller runs the
+// library's pass meanwhile); a failed compilation stays failed.
+int jit_get(const Key& key, const std::string& src, const std::vector<std::string>& names, CUfunction* out) {
+  std::unique_lock<std::mutex> lock(g_mu);
   auto it = g_fn.find(key);
   if (it == g_fn.end()) {
-    Fns fns;
-    std::string err;
-    const std::vector<char> cubin = compile(src, &err);
-    CUmodule mod = nullptr;
-    bool ok = !cubin.empty() && d.load(&mod, cubin.data()) == CUDA_SUCCESS;
-    for (int k = 0; ok && k < count; ++k)
-      ok = d.get_function(&fns.f[k], mod, names[k]) == CUDA_SUCCESS &&
-           d.set_attribute(fns.f[k], CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 227 * 1024) == CUDA_SUCCESS;
-    if (!ok) {
-      fns = Fns();
-      set_error("fft jit: no pass for n = %d: %s", key.n, err.empty() ? "module load failed" : err.c_str());
+    if (g_stop) return SVIE_ERR_UNSUPPORTED;
+    g_fn.emplace(key, Fns());
+    g_jobs.push_back(Job{key, src, names});
+    if (!g_worker) {
+      static bool registered = false;
+      if (!registered) {
+        // NVRTC is opened first, so that this handler runs before its teardown
+        nvrtc();
+        std::atexit(stop_worker);
+        registered = true;
+      }
+      g_worker = true;
+      std::thread(worker).detach();
     }
-    it = g_fn.emplace(key, fns).first;
-  }
-  for (int k = 0; k < count; ++k) out[k] = it->second.f[k];
-  if (!out[0]) {
-    set_error("fft jit: the pass for n = %d did not compile", key.n);
+    lock.unlock();
+    g_cv.notify_all();
     return SVIE_ERR_UNSUPPORTED;
   }
+  if (it->second.state != 1) return SVIE_ERR_UNSUPPORTED;
+  for (size_t k = 0; k < names.size(); ++k) out[k] = it->second.f[k];
   return SVIE_OK;
 }
 
@@ -312,20 +400,55 @@ int jit_strided(int n, int minb, unsigned long long radices, int nst, CUfunction
   *fn = nullptr;
   CUcontext ctx = nullptr;
   if (!current_context(&ctx)) return SVIE_ERR_UNSUPPORTED;
-  const char* names[] = {"svie_jit_strided"};
-  return jit_get(Key{ctx, 0, n, minb}, strided_source(n, minb, radix_list(radices, nst)), names, 1, fn);
+  const Key key{ctx, 0, n, minb};
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_fn.find(key);
+    if (it != g_fn.end()) {
+      if (it->second.state != 1) return SVIE_ERR_UNSUPPORTED;
+      *fn = it->second.f[0];
+      return SVIE_OK;
+    }
+  }
+  return jit_get(key, strided_source(n, minb, radix_list(radices, nst)), {"svie_jit_strided"}, fn);
 }
 
 int jit_z(int n, unsigned long long radices, int nst, CUfunction* r2c, CUfunction* c2r) {
   *r2c = *c2r = nullptr;
   CUcontext ctx = nullptr;
   if (!current_context(&ctx)) return SVIE_ERR_UNSUPPORTED;
-  const char* names[] = {"svie_jit_z_r2c", "svie_jit_z_c2r"};
+  const Key key{ctx, 1, n, 0};
   CUfunction f[2] = {nullptr, nullptr};
-  const int st = jit_get(Key{ctx, 1, n, 0}, z_source(n, radix_list(radices, nst)), names, 2, f);
+  int st = SVIE_ERR_UNSUPPORTED;
+  bool known = false;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_fn.find(key);
+    if (it != g_fn.end()) {
+      known = true;
+      if (it->second.state == 1) {
+        f[0] = it->second.f[0];
+        f[1] = it->second.f[1];
+        st = SVIE_OK;
+      }
+    }
+  }
+  if (!known) st = jit_get(key, z_source(n, radix_list(radices, nst)), {"svie_jit_z_r2c", "svie_jit_z_c2r"}, f);
   *r2c = f[0];
   *c2r = f[1];
   return st;
+}
+
+bool jit_available() { return nvrtc().ok && driver().ok; }
+
+int jit_wait(int timeout_ms) {
+  std::unique_lock<std::mutex> lock(g_mu);
+  const bool done = g_cv.wait_for(lock, std::chrono::milliseconds(timeout_ms), [] {
+    for (const auto& kv : g_fn)
+      if (kv.second.state == 0) return false;
+    return true;
+  });
+  return done ? SVIE_OK : SVIE_ERR_LAUNCH;
 }
 
 bool jit_launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool chained, void** args) {

@@ -10,13 +10,21 @@ namespace svie {
 
 // The 8-line strided pass (k_fft_strided<8, minb>) compiled for an axis of n
 // positions with the given radix sequence (4 bits per stage), in the current
-// context; kept for later calls.  SVIE_OK and *fn, or an error status (NVRTC
-// or the driver API missing, compilation or loading failed) with *fn = null.
+// context.  SVIE_OK and *fn once it is loaded; until then (its compilation
+// starts on a background thread at the first request) and when it cannot be
+// made, an error status with *fn = null.
 int jit_strided(int n, int minb, unsigned long long radices, int nst, CUfunction* fn);
 
 // The z passes (16 line pairs per CTA) compiled for an axis of n positions:
 // the forward (R2C) and inverse (C2R) kernels of one module.
 int jit_z(int n, unsigned long long radices, int nst, CUfunction* r2c, CUfunction* c2r);
+
+// NVRTC and the driver functions were found.
+bool jit_available();
+
+// Waits up to timeout_ms for every compilation started so far (SVIE_OK when
+// none is still running).
+int jit_wait(int timeout_ms);
 
 // Launches a compiled pass on `s` (a dependent launch when `chained`); false
 // when the launch failed (the caller then launches the library's pass).

@@ -264,6 +264,8 @@ def test_passes_compiled_for_the_axis_lengths_give_the_same_bits(shape):
         ref = run()
         nat.call("svie_conv_jit", nx, ny, nz)
         assert lib.svie_conv_jit_enabled(nx, ny, nz)
+        nat.call("svie_conv_jit_wait", 120000)
+        assert lib.svie_conv_jit_ready(nx, ny, nz)
         got = run()
         for a, b in zip(ref, got):
             assert torch.equal(a, b)

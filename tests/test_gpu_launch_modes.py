@@ -24,14 +24,19 @@ import svierosion_gb300 as S
 from svierosion_gb300 import shapes
 frag = shapes.fragment(3, seed=5)
 L = float((frag.bounds[1] - frag.bounds[0]).max())
+from svierosion_gb300 import _native as nat
 out = {}
 for law, kw in (("svi", dict(radius=0.08 * L, k=1, s=0, max_steps=12)), ("mean", dict(alpha=1.0, max_steps=30))):
-    res = S.erode(frag, S.ErosionParams(law=law, resolution=40, target_fraction=0.1, **kw), extract_meshes=False,
-                  keep_state=True)
-    phi = res.level_set.phi.cpu().numpy()
-    out[law] = {"fractions": [r.fraction for r in res.history], "dt": [r.dt for r in res.history],
-                "phi": hashlib.sha256(phi.tobytes()).hexdigest()}
-from svierosion_gb300 import _native as nat
+    runs = []
+    for _ in range(2):  # the second solve finds the compiled passes loaded (SVIE_FFT_JIT=all)
+        res = S.erode(frag, S.ErosionParams(law=law, resolution=40, target_fraction=0.1, **kw),
+                      extract_meshes=False, keep_state=True)
+        phi = res.level_set.phi.cpu().numpy()
+        runs.append({"fractions": [r.fraction for r in res.history], "dt": [r.dt for r in res.history],
+                     "phi": hashlib.sha256(phi.tobytes()).hexdigest()})
+        nat.lib().svie_conv_jit_wait(120000)
+    assert runs[0] == runs[1]
+    out[law] = runs[1]
 out["tma_timeouts"] = int(nat.lib().svie_conv_tma_timeouts())
 print(json.dumps(out))
 """
@@ -40,7 +45,7 @@ print(json.dumps(out))
 def _run(env_extra):
     env = dict(os.environ, **env_extra)
     r = subprocess.run([sys.executable, "-c", SCRIPT, str(ROOT)], env=env, capture_output=True, text=True,
-                       timeout=600)
+                       timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     return json.loads(r.stdout.strip().splitlines()[-1])
 
