@@ -85,6 +85,8 @@ def main(argv=None) -> int:
     """Profiling driver for ncu captures of the step kernels on a synthetic level set.
 
         python -m svierosion_gb300.profiling --grid 448x336x245 --steps 2     # RK3 steps (FFT + stages)
+        python -m svierosion_gb300.profiling --grid 448x336x245 --steps 2 --jit-wait   # ... after the
+                                               # passes compiled for the axis lengths are loaded
         python -m svierosion_gb300.profiling --grid 448x336x245 --reinit 3    # reinitialisation calls
         python -m svierosion_gb300.profiling --job mean --resolution 160 --steps 30   # one served-mix job
     """
@@ -101,6 +103,9 @@ def main(argv=None) -> int:
     ap.add_argument("--job", choices=["svi", "mean", "gauss"], default=None,
                     help="erode one seeded fragment (subdivided 5x) with this law on the plain path, twice")
     ap.add_argument("--resolution", type=int, default=160)
+    ap.add_argument("--jit-wait", action="store_true",
+                    help="one untimed step first, then wait for the convolution passes compiled for the grid's "
+                         "axis lengths, so that the --steps steps run them")
     a = ap.parse_args(argv)
     if a.job:
         # one request of the served mix's kind, solved alone (a mid-size curvature or SVI job)
@@ -138,6 +143,10 @@ def main(argv=None) -> int:
         return 0
     law = S.SVIPowerLaw(0.05 * 2.078, 1, 1, 0.93)
     sim = S.ErosionSimulation(ls, law)
+    if a.jit_wait:
+        sim.run(target_fraction=None, max_steps=1)
+        ready = nat.lib().svie_conv_jit_wait(120000)
+        print("compiled passes ready" if ready == 0 else "compiled passes not ready (%d)" % ready, flush=True)
     t0 = time.time()
     res = sim.run(target_fraction=None, max_steps=a.steps)
     torch.cuda.synchronize()
