@@ -527,7 +527,9 @@ int svie_reinit_bits(const int32_t* band, int64_t m, int nx, int ny, int nz, int
  * svie_reinit_iterate / svie_reinit_rhs: dtau float[m], meta uint8[m] (bits
  * 0-5 crossing flags cp/cm per axis, bit 6 phi0 > 0, bit 7 phi0 < 0), per-warp
  * offsets and the subcell distances of the flagged crossings only (compact,
- * in work-set order).  geo: svie_reinit_geometry_bytes(m), 16-byte aligned. */
+ * in work-set order), and the two entry lists of the sweeps: the plain entries
+ * (no crossing, a sign) by grid index and sign, the others by entry.
+ * geo: svie_reinit_geometry_bytes(m), 16-byte aligned. */
 size_t svie_reinit_geometry_bytes(int64_t m);
 int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
                          int64_t sz, float h, float cfl, void* geo, void* stream);
@@ -547,7 +549,8 @@ int svie_reinit_geometry_arrays(const float* phi, const int32_t* idx, int64_t m,
                                 int64_t sz, float h, float cfl, float* sgn, float* dtau, uint8_t* flags,
                                 float* dist6, void* stream);
 /* Packed geometry from those arrays (kernels.reinit_rhs takes them from the
- * caller); dtau may be NULL. */
+ * caller) for svie_reinit_rhs; dtau may be NULL.  Without the grid indices
+ * every entry goes to the sweeps' general list. */
 int svie_reinit_geometry_pack(const float* sgn, const float* dtau, const uint8_t* flags, const float* dist6,
                               int64_t m, void* geo, void* stream);
 /* levelset.dilate (levelset.py:25-34); tmp is a same-size scratch grid. */

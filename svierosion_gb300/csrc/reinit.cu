@@ -45,17 +45,21 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
 //                       its first distance in `dist`; wbase[W] = the count
 //   dist  float [<= 6m] the subcell distances of the flagged crossings only,
 //                       in work-set order and flag-bit order within a node
-//   wx    int32 [W + 1] per warp: index of its first crossing node in xlist
-//   xlist int32 [<= m]  the entries with a flagged crossing (work-set order)
+//   wx    int32 [W + 1] per warp: index of its first general entry in xlist
+//   xlist int32 [<= m]  the general entries (work-set order): those with a
+//                       flagged crossing or without a sign (phi0 zero or NaN)
 //   xoff  int32 [<= m]  the index of each one's first distance in dist
+//   plist int32 [<= m]  the plain entries (every other one, work-set order) as
+//                       their grid index, complemented (~i) where phi0 < 0
 //   cfl   float
 //   sums  int32         scratch of the scan that makes wbase
-// A sweep streams 1 byte of geometry per node and reads distances only at
-// crossings, from an array a few per cent of the work set long: the sweep's
-// whole footprint (the band part of the two grids, the index list, flags and
-// distances) then stays in L2 across the 40 sweeps of a call.
+// A sweep streams 4 bytes of list per plain node (index and sign in one word,
+// every lane of a warp busy) and reads distances only at crossings, from an
+// array a few per cent of the work set long: the sweep's whole footprint (the
+// band part of the two grids, the lists and distances) then stays in L2
+// across the 40 sweeps of a call.
 struct GeoLayout {
-  long long m, W, meta, wbase, dist, wx, xlist, xoff, cfl, sums, nsums, total;
+  long long m, W, meta, wbase, dist, wx, xlist, xoff, plist, cfl, sums, nsums, total;
 };
 
 __host__ __device__ inline long long align16ll(long long b) { return (b + 15) & ~15LL; }
@@ -70,7 +74,8 @@ __host__ __device__ inline GeoLayout geo_layout(long long m) {
   L.wx = align16ll(L.dist + 24 * m);
   L.xlist = align16ll(L.wx + 4 * (L.W + 1));
   L.xoff = align16ll(L.xlist + 4 * m);
-  L.cfl = align16ll(L.xoff + 4 * m);
+  L.plist = align16ll(L.xoff + 4 * m);
+  L.cfl = align16ll(L.plist + 4 * m);
   L.sums = L.cfl + 16;
   L.nsums = (L.W + 1 + 1023) / 1024;
   L.total = L.sums + 4 * L.nsums + 256;
@@ -83,8 +88,9 @@ struct Geo {
   int* wbase;
   float* dist;
   int* wx;     // per warp: index of its first crossing node in xlist; wx[W] = the count
-  int* xlist;  // the work-set entries with a flagged crossing, in work-set order
+  int* xlist;  // the general work-set entries (crossing or no sign), in work-set order
   int* xoff;   // for each of them, the index of its first distance in dist
+  int* plist;  // the plain entries' grid indices, ~i where phi0 < 0
   float* cfl;
   long long m, W;
 };
@@ -102,6 +108,7 @@ inline Geo geo_view_host(void* base, long long m) {
   g.wx = (int*)(b + L.wx);
   g.xlist = (int*)(b + L.xlist);
   g.xoff = (int*)(b + L.xoff);
+  g.plist = (int*)(b + L.plist);
   g.cfl = (float*)(b + L.cfl);
   g.m = m;
   g.W = L.W;
@@ -119,6 +126,7 @@ SVIE_DEV Geo geo_view(void* base, long long m) {
   g.wx = (int*)(b + L.wx);
   g.xlist = (int*)(b + L.xlist);
   g.xoff = (int*)(b + L.xoff);
+  g.plist = (int*)(b + L.plist);
   g.cfl = (float*)(b + L.cfl);
   g.m = m;
   g.W = L.W;
@@ -176,6 +184,11 @@ SVIE_DEV uint32_t geometry_at(const float* __restrict__ f, int i, int sx, int sy
   return flags;
 }
 
+// A work-set entry with meta byte `meta` takes the general path (the compact
+// list xlist) when it has a flagged crossing or no sign bit; every other entry
+// is plain: no subcell branch and dtau = cfl max(h, 1e-3 h).
+SVIE_DEV bool general_entry(uint32_t meta) { return (meta & 63u) != 0u || (meta & 192u) == 0u; }
+
 // Exclusive prefix of v over the lanes of the warp (all lanes take part).
 SVIE_DEV int warp_exclusive(int v) {
   const int lane = threadIdx.x & 31;
@@ -190,7 +203,7 @@ SVIE_DEV int warp_exclusive(int v) {
 
 // Pass 1: flags and sign bits from the 7-point stencil, dtau of a node
 // without crossings (pass 3 writes the others); per-warp counts of the
-// flagged distances (wbase) and of the crossing nodes (wx).
+// flagged distances (wbase) and of the general entries (wx).
 __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
                                int sy, int sz, float h, float cfl, void* geo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -202,7 +215,7 @@ __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __res
     g.meta[t] = (uint8_t)flags;
   }
   const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags & 63u));
-  const int cx = __reduce_add_sync(0xffffffffu, (flags & 63u) ? 1 : 0);
+  const int cx = __reduce_add_sync(0xffffffffu, (t < m && general_entry(flags)) ? 1 : 0);
   const long long w = t >> 5;
   if ((threadIdx.x & 31) == 0 && w < g.W) {
     g.wbase[w] = cnt;
@@ -215,28 +228,40 @@ __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __res
   }
 }
 
-// Pass 3 (after the exclusive scans of wbase and wx): the flagged distances,
-// dtau, and the crossing list.  The flags come from pass 1; only warps
-// holding a crossing compute the geometry.
+// Pass 3 (after the exclusive scans of wbase and wx): the plain list, the
+// flagged distances, dtau, and the general list.  The flags come from pass 1;
+// only warps holding a crossing compute the geometry.  The warps before warp w
+// are full, so 32 w - wx[w] plain entries precede it.
 __global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
                               int sy, int sz, float h, float cfl, void* geo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   Geo g = geo_view(geo, m);
-  const uint32_t flags = t < m ? g.meta[t] & 63u : 0u;
-  if (!__ballot_sync(0xffffffffu, flags != 0u)) return;
+  const bool act = t < m;
+  const uint32_t meta = act ? g.meta[t] : 0u;
+  const uint32_t flags = meta & 63u;
+  const bool gen = act && general_entry(meta);
+  const long long w = t >> 5;
+  const int po = warp_exclusive(act && !gen ? 1 : 0);
+  if (act && !gen) {
+    const int i = idx[t];
+    g.plist[32 * w - g.wx[w] + po] = (meta & 64u) ? i : ~i;
+  }
+  if (!__ballot_sync(0xffffffffu, gen)) return;
   const int off = warp_exclusive(__popc(flags));
-  const int xo = warp_exclusive(flags ? 1 : 0);
-  if (!flags) return;
-  float d[6], dtau;
-  geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
-  g.dtau[t] = dtau;
-  const int doff = g.wbase[t >> 5] + off;
-  float* out = g.dist + doff;
-  int r = 0;
+  const int xo = warp_exclusive(gen ? 1 : 0);
+  if (!gen) return;
+  const int doff = g.wbase[w] + off;
+  if (flags) {
+    float d[6], dtau;
+    geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
+    g.dtau[t] = dtau;
+    float* out = g.dist + doff;
+    int r = 0;
 #pragma unroll
-  for (int b = 0; b < 6; ++b)
-    if ((flags >> b) & 1u) out[r++] = d[b];
-  const int k = g.wx[t >> 5] + xo;
+    for (int b = 0; b < 6; ++b)
+      if ((flags >> b) & 1u) out[r++] = d[b];
+  }
+  const int k = g.wx[w] + xo;
   g.xlist[k] = (int)t;
   g.xoff[k] = doff;
 }
@@ -259,7 +284,9 @@ __global__ void k_reinit_geometry_full(const float* __restrict__ f, const int32_
 }
 
 // Packed form from the 14 arrays (kernels.reinit_rhs takes them from the
-// caller): pass 1 counts, pass 2 (after the scan) writes the distances.
+// caller): pass 1 counts, pass 2 (after the scan) writes the distances.  The
+// grid indices are not known here, so every entry is general (the plain list
+// stays empty) and the sweeps take them all by the general path.
 __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __restrict__ dtau,
                               const uint8_t* __restrict__ flags6, const float* __restrict__ dist6, long long m,
                               void* geo, int pass) {
@@ -270,7 +297,7 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
     for (int a = 0; a < 6; ++a) flags |= (flags6[a * m + t] ? 1u : 0u) << a;
   if (pass == 0) {
     const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags));
-    const int cx = __reduce_add_sync(0xffffffffu, flags ? 1 : 0);
+    const int cx = __reduce_add_sync(0xffffffffu, t < m ? 1 : 0);
     const long long w = t >> 5;
     if ((threadIdx.x & 31) == 0 && w < g.W) {
       g.wbase[w] = cnt;
@@ -289,16 +316,14 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
     return;
   }
   const int off = warp_exclusive(__popc(flags));
-  const int xo = warp_exclusive(flags ? 1 : 0);
-  if (t >= m || !flags) return;
+  if (t >= m) return;
   const int doff = g.wbase[t >> 5] + off;
   float* out = g.dist + doff;
   int r = 0;
   for (int b = 0; b < 6; ++b)
     if ((flags >> b) & 1u) out[r++] = dist6[b * m + t];
-  const int k = g.wx[t >> 5] + xo;
-  g.xlist[k] = (int)t;
-  g.xoff[k] = doff;
+  g.xlist[t] = (int)t;
+  g.xoff[t] = doff;
 }
 
 SVIE_DEV float meta_sgn(uint32_t meta) { return (meta & 64u) ? 1.0f : ((meta & 128u) ? -1.0f : 0.0f); }
@@ -377,12 +402,13 @@ SVIE_DEV void sweep_update(const float* __restrict__ src, float* __restrict__ ds
   }
 }
 
-// One launch per half-step.  Blocks [0, nbm) take the entries without a
-// flagged crossing (about nine in ten): no subcell branch, no distance reads,
-// dtau = cfl max(h, 1e-3 h).  The blocks after them take the entries with a
-// crossing from the compact list (count wx[W]), grid-stride, so that no warp
-// runs the subcell branch for a few lanes; they are scheduled last and fill
-// the tail of the first part.
+// One launch per half-step.  Blocks [0, nbm) take the plain entries (about
+// nine in ten) from the plain list, whose word holds the grid index and the
+// sign: no subcell branch, no distance reads, dtau = cfl max(h, 1e-3 h), and
+// every lane of a warp busy.  The blocks after them take the general entries
+// from their compact list (count wx[W]), grid-stride, so that no warp runs the
+// subcell branch for a few lanes; they are scheduled last and fill the tail of
+// the first part.
 __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
                                                              const int32_t* __restrict__ idx, long long m, int sx,
                                                              int sy, int sz, float h, float rh, float rhh, Geo g,
@@ -390,23 +416,23 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
   pdl_wait();  // the previous half-step's writes (and the geometry) are visible from here on
   pdl_release();
   const float cfl = __ldg(g.cfl);
+  const int X = __ldg(g.wx + g.W);
   if ((int)blockIdx.x < nbm) {
-    // a contiguous run of the brick-ordered list per block: the bricks that follow one
+    // a contiguous run of the brick-ordered plain list per block: the bricks that follow one
     // another along z are swept by the same SM, whose L1 still holds their shared rows
-    const long long per = ((m + nbm - 1) / nbm + blockDim.x - 1) / blockDim.x * blockDim.x;
-    const long long t0 = (long long)blockIdx.x * per, t1 = min(t0 + per, m);
-    for (long long t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-      const uint32_t flags = __ldg(g.meta + t);
-      if (flags & 63u) continue;
-      const int i = __ldg(idx + t);
+    const long long P = m - X;
+    const long long per = ((P + nbm - 1) / nbm + blockDim.x - 1) / blockDim.x * blockDim.x;
+    const long long k0 = (long long)blockIdx.x * per, k1 = min(k0 + per, P);
+    for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+      const int e = __ldg(g.plist + k);
+      const int i = e >= 0 ? e : ~e;
       float hmin;
       // z stride 1 (C order) as a constant: the z neighbours become immediate offsets
-      const float r = reinit_rhs_at<false>(src, i, g, 0, flags, sx, sy, 1, h, rh, h * h, rhh, hmin);
+      const float r = reinit_rhs_at<false>(src, i, g, 0, e >= 0 ? 64u : 128u, sx, sy, 1, h, rh, h * h, rhh, hmin);
       sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
     }
     return;
   }
-  const int X = __ldg(g.wx + g.W);
   const int stride = (gridDim.x - nbm) * blockDim.x;
   for (int k = (blockIdx.x - nbm) * blockDim.x + threadIdx.x; k < X; k += stride) {
     const int t = __ldg(g.xlist + k);
