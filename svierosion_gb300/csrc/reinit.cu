@@ -47,11 +47,13 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
 //                       in work-set order and flag-bit order within a node
 //   wx    int32 [W + 1] per warp: index of its first general entry in xlist
 //   xlist int32 [<= m]  the general entries (work-set order): those with a
-//                       flagged crossing or without a sign (phi0 zero or NaN)
+//                       flagged crossing or without a sign (phi0 zero or NaN),
+//                       by grid index
 //   xoff  int32 [<= m]  the index of each one's first distance in dist
 //   plist int32 [<= m]  the plain entries (every other one, work-set order) as
 //                       their grid index, complemented (~i) where phi0 < 0
-//   cfl   float
+//   xmeta uint8 [<= m]  the meta byte of each general entry
+//   cfl   float, then np int32: the number of plain entries
 //   sums  int32         scratch of the scan that makes wbase
 // A sweep streams 4 bytes of list per plain node (index and sign in one word,
 // every lane of a warp busy) and reads distances only at crossings, from an
@@ -59,7 +61,7 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
 // band part of the two grids, the lists and distances) then stays in L2
 // across the 40 sweeps of a call.
 struct GeoLayout {
-  long long m, W, meta, wbase, dist, wx, xlist, xoff, plist, cfl, sums, nsums, total;
+  long long m, W, meta, wbase, dist, wx, xlist, xoff, plist, xmeta, cfl, sums, nsums, total;
 };
 
 __host__ __device__ inline long long align16ll(long long b) { return (b + 15) & ~15LL; }
@@ -75,7 +77,8 @@ __host__ __device__ inline GeoLayout geo_layout(long long m) {
   L.xlist = align16ll(L.wx + 4 * (L.W + 1));
   L.xoff = align16ll(L.xlist + 4 * m);
   L.plist = align16ll(L.xoff + 4 * m);
-  L.cfl = align16ll(L.plist + 4 * m);
+  L.xmeta = align16ll(L.plist + 4 * m);
+  L.cfl = align16ll(L.xmeta + m);
   L.sums = L.cfl + 16;
   L.nsums = (L.W + 1 + 1023) / 1024;
   L.total = L.sums + 4 * L.nsums + 256;
@@ -88,10 +91,12 @@ struct Geo {
   int* wbase;
   float* dist;
   int* wx;     // per warp: index of its first crossing node in xlist; wx[W] = the count
-  int* xlist;  // the general work-set entries (crossing or no sign), in work-set order
-  int* xoff;   // for each of them, the index of its first distance in dist
-  int* plist;  // the plain entries' grid indices, ~i where phi0 < 0
+  int* xlist;      // the general work-set entries (crossing or no sign) by grid index, in work-set order
+  int* xoff;       // for each of them, the index of its first distance in dist
+  int* plist;      // the plain entries' grid indices, ~i where phi0 < 0
+  uint8_t* xmeta;  // the general entries' meta bytes
   float* cfl;
+  int* np;         // the number of plain entries
   long long m, W;
 };
 
@@ -109,7 +114,9 @@ inline Geo geo_view_host(void* base, long long m) {
   g.xlist = (int*)(b + L.xlist);
   g.xoff = (int*)(b + L.xoff);
   g.plist = (int*)(b + L.plist);
+  g.xmeta = (uint8_t*)(b + L.xmeta);
   g.cfl = (float*)(b + L.cfl);
+  g.np = (int*)(b + L.cfl + 4);
   g.m = m;
   g.W = L.W;
   return g;
@@ -127,7 +134,9 @@ SVIE_DEV Geo geo_view(void* base, long long m) {
   g.xlist = (int*)(b + L.xlist);
   g.xoff = (int*)(b + L.xoff);
   g.plist = (int*)(b + L.plist);
+  g.xmeta = (uint8_t*)(b + L.xmeta);
   g.cfl = (float*)(b + L.cfl);
+  g.np = (int*)(b + L.cfl + 4);
   g.m = m;
   g.W = L.W;
   return g;
@@ -241,6 +250,7 @@ __global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __rest
   const uint32_t flags = meta & 63u;
   const bool gen = act && general_entry(meta);
   const long long w = t >> 5;
+  if (t == 0) *g.np = (int)(m - g.wx[g.W]);
   const int po = warp_exclusive(act && !gen ? 1 : 0);
   if (act && !gen) {
     const int i = idx[t];
@@ -251,9 +261,10 @@ __global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __rest
   const int xo = warp_exclusive(gen ? 1 : 0);
   if (!gen) return;
   const int doff = g.wbase[w] + off;
+  const int i = idx[t];
   if (flags) {
     float d[6], dtau;
-    geometry_at(f, idx[t], sx, sy, sz, h, cfl, d, dtau);
+    geometry_at(f, i, sx, sy, sz, h, cfl, d, dtau);
     g.dtau[t] = dtau;
     float* out = g.dist + doff;
     int r = 0;
@@ -262,7 +273,8 @@ __global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __rest
       if ((flags >> b) & 1u) out[r++] = d[b];
   }
   const int k = g.wx[w] + xo;
-  g.xlist[k] = (int)t;
+  g.xlist[k] = i;
+  g.xmeta[k] = (uint8_t)meta;
   g.xoff[k] = doff;
 }
 
@@ -285,8 +297,8 @@ __global__ void k_reinit_geometry_full(const float* __restrict__ f, const int32_
 
 // Packed form from the 14 arrays (kernels.reinit_rhs takes them from the
 // caller): pass 1 counts, pass 2 (after the scan) writes the distances.  The
-// grid indices are not known here, so every entry is general (the plain list
-// stays empty) and the sweeps take them all by the general path.
+// grid indices are not known here: both sweep lists stay empty (svie_reinit_rhs
+// reads the entries by position).
 __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __restrict__ dtau,
                               const uint8_t* __restrict__ flags6, const float* __restrict__ dist6, long long m,
                               void* geo, int pass) {
@@ -297,7 +309,7 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
     for (int a = 0; a < 6; ++a) flags |= (flags6[a * m + t] ? 1u : 0u) << a;
   if (pass == 0) {
     const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags));
-    const int cx = __reduce_add_sync(0xffffffffu, t < m ? 1 : 0);
+    const int cx = 0;
     const long long w = t >> 5;
     if ((threadIdx.x & 31) == 0 && w < g.W) {
       g.wbase[w] = cnt;
@@ -307,6 +319,7 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
       g.wbase[g.W] = 0;
       g.wx[g.W] = 0;
       *g.cfl = 0.0f;
+      *g.np = 0;
     }
     if (t < m) {
       const float s = sgn[t];
@@ -322,8 +335,6 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
   int r = 0;
   for (int b = 0; b < 6; ++b)
     if ((flags >> b) & 1u) out[r++] = dist6[b * m + t];
-  g.xlist[t] = (int)t;
-  g.xoff[t] = doff;
 }
 
 SVIE_DEV float meta_sgn(uint32_t meta) { return (meta & 64u) ? 1.0f : ((meta & 128u) ? -1.0f : 0.0f); }
@@ -410,17 +421,15 @@ SVIE_DEV void sweep_update(const float* __restrict__ src, float* __restrict__ ds
 // subcell branch for a few lanes; they are scheduled last and fill the tail of
 // the first part.
 __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __restrict__ src, float* __restrict__ dst,
-                                                             const int32_t* __restrict__ idx, long long m, int sx,
-                                                             int sy, int sz, float h, float rh, float rhh, Geo g,
-                                                             int second, int nbm) {
+                                                             int sx, int sy, int sz, float h, float rh, float rhh,
+                                                             Geo g, int second, int nbm) {
   pdl_wait();  // the previous half-step's writes (and the geometry) are visible from here on
   pdl_release();
   const float cfl = __ldg(g.cfl);
-  const int X = __ldg(g.wx + g.W);
   if ((int)blockIdx.x < nbm) {
     // a contiguous run of the brick-ordered plain list per block: the bricks that follow one
     // another along z are swept by the same SM, whose L1 still holds their shared rows
-    const long long P = m - X;
+    const long long P = __ldg(g.np);
     const long long per = ((P + nbm - 1) / nbm + blockDim.x - 1) / blockDim.x * blockDim.x;
     const long long k0 = (long long)blockIdx.x * per, k1 = min(k0 + per, P);
     for (long long k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
@@ -433,11 +442,11 @@ __global__ void __launch_bounds__(RI_THREADS, 8) k_reinit_sweep(const float* __r
     }
     return;
   }
+  const int X = __ldg(g.wx + g.W);
   const int stride = (gridDim.x - nbm) * blockDim.x;
   for (int k = (blockIdx.x - nbm) * blockDim.x + threadIdx.x; k < X; k += stride) {
-    const int t = __ldg(g.xlist + k);
-    const uint32_t flags = __ldg(g.meta + t);
-    const int i = __ldg(idx + t);
+    const int i = __ldg(g.xlist + k);
+    const uint32_t flags = __ldg(g.xmeta + k);
     float hmin;
     const float r = reinit_rhs_at<true>(src, i, g, __ldg(g.xoff + k), flags, sx, sy, 1, h, rh, h * h, rhh, hmin);
     sweep_update(src, dst, i, r, cfl * fmaxf(hmin, 1e-3f * h), second);
@@ -756,11 +765,11 @@ int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* id
   const dim3 grid(nb + nbx), block(RI_THREADS);
   cudaError_t e = cudaSuccess;
   for (int it = 0; it < iterations && e == cudaSuccess; ++it) {
-    e = launch_dependent(it > 0, k_reinit_sweep, grid, block, 0, s, (const float*)phi, phi_tmp, idx, (long long)m,
-                         (int)sx, (int)sy, (int)sz, h, rh, rhh, g, 0, nb);
+    e = launch_dependent(it > 0, k_reinit_sweep, grid, block, 0, s, (const float*)phi, phi_tmp, (int)sx, (int)sy,
+                         (int)sz, h, rh, rhh, g, 0, nb);
     if (e == cudaSuccess)
-      e = launch_dependent(true, k_reinit_sweep, grid, block, 0, s, (const float*)phi_tmp, phi, idx, (long long)m,
-                           (int)sx, (int)sy, (int)sz, h, rh, rhh, g, 1, nb);
+      e = launch_dependent(true, k_reinit_sweep, grid, block, 0, s, (const float*)phi_tmp, phi, (int)sx, (int)sy,
+                           (int)sz, h, rh, rhh, g, 1, nb);
   }
   if (e != cudaSuccess) {
     set_error("svie_reinit_iterate: launch failed: %s", cudaGetErrorString(e));
