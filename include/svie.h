@@ -524,12 +524,13 @@ size_t svie_reinit_bits_bytes(int nx, int ny, int nz);
 int svie_reinit_bits(const int32_t* band, int64_t m, int nx, int ny, int nz, int dilation, int margin,
                      uint32_t* bits, uint32_t* tmp, uint32_t* marked, void* stream);
 /* reinit_geometry (kernels.py:335-359) packed over the m work-set nodes for
- * svie_reinit_iterate / svie_reinit_rhs: dtau float[m], meta uint8[m] (bits
- * 0-5 crossing flags cp/cm per axis, bit 6 phi0 > 0, bit 7 phi0 < 0), per-warp
- * offsets and the subcell distances of the flagged crossings only (compact,
- * in work-set order), and the two entry lists of the sweeps: the plain entries
- * (no crossing, a sign) by grid index and sign, the others by grid index with
- * their flags and distance offsets.
+ * svie_reinit_iterate / svie_reinit_rhs: meta uint8[m] (bits 0-5 crossing
+ * flags cp/cm per axis, bit 6 phi0 > 0, bit 7 phi0 < 0), per-warp offsets and
+ * the subcell distances of the flagged crossings only (compact, in work-set
+ * order), and the two entry lists of the sweeps: the plain entries (no
+ * crossing, a sign) by grid index and sign, the others by grid index with
+ * their flags and distance offsets.  The pseudo-time step is not stored: it is
+ * rebuilt from the distances where it is used.
  * geo: svie_reinit_geometry_bytes(m), 16-byte aligned. */
 size_t svie_reinit_geometry_bytes(int64_t m);
 int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,
@@ -550,9 +551,9 @@ int svie_reinit_geometry_arrays(const float* phi, const int32_t* idx, int64_t m,
                                 int64_t sz, float h, float cfl, float* sgn, float* dtau, uint8_t* flags,
                                 float* dist6, void* stream);
 /* Packed geometry from those arrays (kernels.reinit_rhs takes them from the
- * caller) for svie_reinit_rhs; dtau may be NULL.  Without the grid indices
- * the sweep lists stay empty: svie_reinit_iterate takes the geometry of
- * svie_reinit_geometry. */
+ * caller) for svie_reinit_rhs; dtau is not used (may be NULL).  Without the
+ * grid indices the sweep lists stay empty: svie_reinit_iterate takes the
+ * geometry of svie_reinit_geometry. */
 int svie_reinit_geometry_pack(const float* sgn, const float* dtau, const uint8_t* flags, const float* dist6,
                               int64_t m, void* geo, void* stream);
 /* levelset.dilate (levelset.py:25-34); tmp is a same-size scratch grid. */

@@ -605,7 +605,8 @@ static bool fits(size_t b) { return b <= TILE_SMEM_MAX; }
 
 struct FftChoice {
   int z, y, x;
-  int jit = 0;  // the 8-line y and x forms run as passes compiled for the axis lengths (svie_conv_jit)
+  int jit = 0;   // the 8-line y and x forms run as passes compiled for the axis lengths (svie_conv_jit)
+  int kept = 0;  // the forms were tuned or set (svie_conv_tune, svie_conv_set_choice)
 };
 
 // the fixed rule (above)
@@ -651,7 +652,7 @@ static FftChoice choice_for(int nx, int ny, int nz, bool* tuned = nullptr) {
   const GridKey k = grid_key(nx, ny, nz);
   std::lock_guard<std::mutex> lock(g_choice_mu);
   auto it = g_choice.find(k);
-  if (tuned) *tuned = it != g_choice.end();
+  if (tuned) *tuned = it != g_choice.end() && it->second.kept;
   return it != g_choice.end() ? it->second : default_choice(nx, ny, nz);
 }
 
@@ -1082,6 +1083,7 @@ int svie_conv_set_choice(int nx, int ny, int nz, int z, int y, int x) {
     return SVIE_OK;
   }
   FftChoice c{z, y, x};
+  c.kept = 1;
   if (!choice_fits(c, nx, ny, nz)) {
     set_error("svie_conv_set_choice: forms (%d, %d, %d) do not exist or do not fit shared memory for %d x %d x %d",
               z, y, x, nx, ny, nz);
@@ -1225,6 +1227,7 @@ int svie_conv_tune(const void* plan, int nx, int ny, int nz, const float* f, flo
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (failed) return launch_status("svie_conv_tune", launched);
+  best.kept = 1;
   {
     std::lock_guard<std::mutex> lock(g_choice_mu);
     g_choice[grid_key(nx, ny, nz)] = best;

@@ -36,9 +36,9 @@ SVIE_DEV float interface_distance(float p0, float p1, float dd, float h) {
   return fminf(fmaxf(ok ? quad : lin, 0.0f), h);
 }
 
-// Geometry record over the m work-set nodes (byte offsets in GeoLayout):
-//   dtau  float [m]     local pseudo-time step (for the array form; the
-//                       sweeps rebuild it from the distances they read)
+// Geometry record over the m work-set nodes (byte offsets in GeoLayout; the
+// local pseudo-time step is not stored: the sweeps rebuild it from the
+// distances they read):
 //   meta  uint8 [m]     bits 0-5: crossing flags cp_x cm_x cp_y cm_y cp_z cm_z,
 //                       bit 6: phi0 > 0, bit 7: phi0 < 0
 //   wbase int32 [W + 1] per warp of 32 entries (W = ceil(m / 32)): index of
@@ -70,8 +70,8 @@ __host__ __device__ inline GeoLayout geo_layout(long long m) {
   GeoLayout L;
   L.m = m;
   L.W = (m + 31) / 32;
-  L.meta = 4 * m;
-  L.wbase = align16ll(5 * m);
+  L.meta = 0;
+  L.wbase = align16ll(m);
   L.dist = align16ll(L.wbase + 4 * (L.W + 1));
   L.wx = align16ll(L.dist + 24 * m);
   L.xlist = align16ll(L.wx + 4 * (L.W + 1));
@@ -86,7 +86,6 @@ __host__ __device__ inline GeoLayout geo_layout(long long m) {
 }
 
 struct Geo {
-  float* dtau;
   uint8_t* meta;
   int* wbase;
   float* dist;
@@ -106,7 +105,6 @@ inline Geo geo_view_host(void* base, long long m) {
   const GeoLayout L = geo_layout(m);
   char* b = (char*)base;
   Geo g;
-  g.dtau = (float*)b;
   g.meta = (uint8_t*)(b + L.meta);
   g.wbase = (int*)(b + L.wbase);
   g.dist = (float*)(b + L.dist);
@@ -126,7 +124,6 @@ SVIE_DEV Geo geo_view(void* base, long long m) {
   const GeoLayout L = geo_layout(m);
   char* b = (char*)base;
   Geo g;
-  g.dtau = (float*)b;
   g.meta = (uint8_t*)(b + L.meta);
   g.wbase = (int*)(b + L.wbase);
   g.dist = (float*)(b + L.dist);
@@ -210,9 +207,8 @@ SVIE_DEV int warp_exclusive(int v) {
   return s - v;
 }
 
-// Pass 1: flags and sign bits from the 7-point stencil, dtau of a node
-// without crossings (pass 3 writes the others); per-warp counts of the
-// flagged distances (wbase) and of the general entries (wx).
+// Pass 1: flags and sign bits from the 7-point stencil; per-warp counts of
+// the flagged distances (wbase) and of the general entries (wx).
 __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
                                int sy, int sz, float h, float cfl, void* geo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -220,7 +216,6 @@ __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __res
   uint32_t flags = 0;
   if (t < m) {
     flags = crossing_flags(f, idx[t], sx, sy, sz);
-    g.dtau[t] = cfl * fmaxf(h, 1e-3f * h);
     g.meta[t] = (uint8_t)flags;
   }
   const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags & 63u));
@@ -237,12 +232,11 @@ __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __res
   }
 }
 
-// Pass 3 (after the exclusive scans of wbase and wx): the plain list, the
-// flagged distances, dtau, and the general list.  The flags come from pass 1;
-// only warps holding a crossing compute the geometry.  The warps before warp w
-// are full, so 32 w - wx[w] plain entries precede it.
-__global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
-                              int sy, int sz, float h, float cfl, void* geo) {
+// Pass 3 (after the exclusive scans of wbase and wx): the plain and general
+// lists, with each general entry's flags and first distance.  The flags come
+// from pass 1.  The warps before warp w are full, so 32 w - wx[w] plain
+// entries precede it.
+__global__ void k_reinit_lists(const int32_t* __restrict__ idx, long long m, void* geo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   Geo g = geo_view(geo, m);
   const bool act = t < m;
@@ -260,22 +254,29 @@ __global__ void k_reinit_dist(const float* __restrict__ f, const int32_t* __rest
   const int off = warp_exclusive(__popc(flags));
   const int xo = warp_exclusive(gen ? 1 : 0);
   if (!gen) return;
-  const int doff = g.wbase[w] + off;
-  const int i = idx[t];
-  if (flags) {
+  const int k = g.wx[w] + xo;
+  g.xlist[k] = idx[t];
+  g.xmeta[k] = (uint8_t)meta;
+  g.xoff[k] = g.wbase[w] + off;
+}
+
+// Pass 4: the subcell distances of the flagged crossings, over the general
+// list (grid-stride; every lane of a warp holds a general entry).
+__global__ void k_reinit_dist(const float* __restrict__ f, long long m, int sx, int sy, int sz, float h, float cfl,
+                              void* geo) {
+  Geo g = geo_view(geo, m);
+  const int X = g.wx[g.W];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < X; k += gridDim.x * blockDim.x) {
+    const uint32_t flags = g.xmeta[k] & 63u;
+    if (!flags) continue;
     float d[6], dtau;
-    geometry_at(f, i, sx, sy, sz, h, cfl, d, dtau);
-    g.dtau[t] = dtau;
-    float* out = g.dist + doff;
+    geometry_at(f, g.xlist[k], sx, sy, sz, h, cfl, d, dtau);
+    float* out = g.dist + g.xoff[k];
     int r = 0;
 #pragma unroll
     for (int b = 0; b < 6; ++b)
       if ((flags >> b) & 1u) out[r++] = d[b];
   }
-  const int k = g.wx[w] + xo;
-  g.xlist[k] = i;
-  g.xmeta[k] = (uint8_t)meta;
-  g.xoff[k] = doff;
 }
 
 // Array form of the geometry for kernels.reinit_geometry: every node's
@@ -298,7 +299,7 @@ __global__ void k_reinit_geometry_full(const float* __restrict__ f, const int32_
 // Packed form from the 14 arrays (kernels.reinit_rhs takes them from the
 // caller): pass 1 counts, pass 2 (after the scan) writes the distances.  The
 // grid indices are not known here: both sweep lists stay empty (svie_reinit_rhs
-// reads the entries by position).
+// reads the entries by position).  dtau is not kept: the RHS does not use it.
 __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __restrict__ dtau,
                               const uint8_t* __restrict__ flags6, const float* __restrict__ dist6, long long m,
                               void* geo, int pass) {
@@ -309,11 +310,10 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
     for (int a = 0; a < 6; ++a) flags |= (flags6[a * m + t] ? 1u : 0u) << a;
   if (pass == 0) {
     const int cnt = __reduce_add_sync(0xffffffffu, __popc(flags));
-    const int cx = 0;
     const long long w = t >> 5;
     if ((threadIdx.x & 31) == 0 && w < g.W) {
       g.wbase[w] = cnt;
-      g.wx[w] = cx;
+      g.wx[w] = 0;
     }
     if (t == 0) {
       g.wbase[g.W] = 0;
@@ -324,7 +324,6 @@ __global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __rest
     if (t < m) {
       const float s = sgn[t];
       g.meta[t] = (uint8_t)(flags | (s > 0.0f ? 64u : 0u) | (s < 0.0f ? 128u : 0u));
-      g.dtau[t] = dtau ? dtau[t] : 0.0f;
     }
     return;
   }
@@ -736,8 +735,13 @@ int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_
   char* b = (char*)geo;
   int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
   ns += scan_exclusive_i32((int*)(b + L.wx), L.W + 1, (int*)(b + L.sums), s);
-  k_reinit_dist<<<nb, RI_THREADS, 0, s>>>(phi, idx, m, sx, sy, sz, h, cfl, geo);
-  return launch_status("svie_reinit_geometry", 2 + ns);
+  k_reinit_lists<<<nb, RI_THREADS, 0, s>>>(idx, m, geo);
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int nd = (int)std::min<long long>((long long)nb, 8LL * nsm);
+  k_reinit_dist<<<nd, RI_THREADS, 0, s>>>(phi, m, sx, sy, sz, h, cfl, geo);
+  return launch_status("svie_reinit_geometry", 3 + ns);
 }
 
 int svie_reinit_iterate(float* phi, float* phi_tmp, int64_t n, const int32_t* idx, int64_t m, int64_t sx, int64_t sy,

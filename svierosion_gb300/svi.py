@@ -212,17 +212,25 @@ class BallConvolution:
         return out
 
     def _tune(self, f, out, ws) -> None:
-        """Once per grid shape and process (not while a graph is captured): compile the y and x
-        passes for the shape's axis lengths (jit_enabled), then time the pass forms, or take them
-        from the tuning cache file (SVIE_FFT_TUNE_CACHE) when it holds this GPU model and shape;
-        newly tuned forms are added to that file."""
+        """Once per grid shape and process (not while a graph is captured): compile the passes for
+        the shape's axis lengths (jit_enabled) and keep the fixed rule's forms, the ones those
+        passes serve; without them, time the pass forms, or take them from the tuning cache file
+        (SVIE_FFT_TUNE_CACHE) when it holds this GPU model and shape; newly tuned forms are added
+        to that file."""
         key = (self.device.index, tuple(self.grid.shape))
         if key in _TUNED or torch.cuda.is_current_stream_capturing():
             return
         nx, ny, nz = self.grid.shape
-        if jit_enabled(self.grid.size) and not nat.lib().svie_conv_jit_enabled(nx, ny, nz):
-            # the passes compiled for these axis lengths; on failure the library's own passes stay
-            nat.lib().svie_conv_jit(nx, ny, nz)
+        lib = nat.lib()
+        if jit_enabled(self.grid.size):
+            if not lib.svie_conv_jit_enabled(nx, ny, nz):
+                # the passes compiled for these axis lengths; on failure the library's own passes stay
+                lib.svie_conv_jit(nx, ny, nz)
+            if lib.svie_conv_jit_enabled(nx, ny, nz) and not lib.svie_conv_get_choice(nx, ny, nz, None, None, None):
+                # timing now would measure the library's passes (the compiled ones are still being
+                # built) and could pick a form that has no compiled pass, a fifth slower
+                _TUNED.add(key)
+                return
         if not autotune_enabled(self.grid.size):
             _TUNED.add(key)
             return
