@@ -205,3 +205,42 @@ def test_sdf_slices_do_not_change_results():
         assert (keys[0] != np.iinfo(np.int64).max).any() and accs[0].any()
         for k, a in zip(keys[1:], accs[1:]):
             assert np.array_equal(k, keys[0]) and np.array_equal(a, accs[0])
+
+
+def test_reinit_sweep_lists_cover_every_entry():
+    """One pseudo-time iteration of svie_reinit_iterate, whose sweeps walk the plain and general entry
+    lists of the packed geometry, against the same iteration composed from reinit_rhs (the general
+    formula at every entry) and the array form's dtau: every work-set entry is updated once, with its
+    sign (entries with phi0 exactly 0 included), and nothing off the work set changes."""
+    shape = (40, 36, 44)
+    nx, ny, nz = shape
+    h = 0.05
+    ax = [np.arange(n) * h for n in shape]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    phi = (np.sqrt((X - 1.0) ** 2 + (Y - 0.9) ** 2 + (Z - 1.1) ** 2) - 0.62).astype(np.float32)
+    coords = np.stack(np.meshgrid(*[np.arange(n) for n in shape], indexing="ij"))
+    inner = np.all([(coords[a] >= 2) & (coords[a] <= shape[a] - 3) for a in range(3)], axis=0)
+    work = np.flatnonzero((np.abs(phi) < 4 * h) & inner)
+    planted = work[::97]
+    phi.reshape(-1)[planted] = 0.0              # sign-less entries: the general path
+    flat = _cuda(phi.reshape(-1))
+    idx = _cuda(work.astype(np.int32))
+    m, n = idx.numel(), flat.numel()
+    sx, sy = ny * nz, nz
+    geo = K.reinit_geometry(flat, idx, sx, sy, 1, h, 0.45)
+    sgn, dtau = geo[0], geo[1]
+    assert int((sgn == 0).sum()) >= len(planted)
+    a = flat.clone()
+    b = torch.empty_like(a)
+    nat.call("svie_reinit_iterate", nat.ptr(a), nat.ptr(b), n, nat.ptr(idx), m, sx, sy, 1, h, nat.ptr(geo.packed),
+             1, nat.stream())
+    i = idx.long()
+    a2, b2 = flat.clone(), flat.clone()
+    b2[i] = a2[i] + dtau * K.reinit_rhs(a2, idx, sx, sy, 1, h, sgn, *geo[2:])
+    a2[i] = 0.5 * (a2[i] + b2[i] + dtau * K.reinit_rhs(b2, idx, sx, sy, 1, h, sgn, *geo[2:]))
+    off = torch.ones(n, dtype=torch.bool, device="cuda")
+    off[i] = False
+    assert torch.equal(a[off], flat[off])
+    assert torch.equal(a[_cuda(planted)], flat[_cuda(planted)])
+    _close(a[i], a2[i].cpu().numpy(), 2e-6 * float(flat[i].abs().max()))
+    assert float((a[i] - flat[i]).abs().max()) > 1e-4   # the iteration moved the level set
