@@ -361,8 +361,19 @@ __global__ void __launch_bounds__(SUM_THREADS) k_stats_finalize(svie_stats* st, 
   stats_finalize_block(st, L, partial, nb, m);
 }
 
-// TVD-RK3 stage combinations (evolve.py:175-179) with the reference's float32
-// operation order; dt read from the device.
+// TVD-RK3 stage combinations (evolve.py:175-179): the new value from u0 (a),
+// L (l) and the current phi (p; stages 2 and 3), for stages 1-3.  Every
+// operation is rounded on its own, in the reference's float32 order (its
+// tensor arithmetic fuses no multiply-add), so that every kernel that calls
+// this gives the same bits whatever the compiler would contract.
+SVIE_DEV float rk_value(int stage, float a, float l, float p, float dt) {
+  const float dl = __fmul_rn(dt, l);
+  if (stage == 1) return __fadd_rn(a, dl);
+  if (stage == 2) return __fadd_rn(__fmul_rn(0.75f, a), __fmul_rn(0.25f, __fadd_rn(p, dl)));
+  return __fadd_rn(__fdiv_rn(a, 3.0f), __fmul_rn((float)(2.0 / 3.0), __fadd_rn(p, dl)));
+}
+
+// One entry (dt read from the device; stage 0 copies u0 back).
 SVIE_DEV void rk_at(long long t, float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
                     const float* __restrict__ u0, const float* __restrict__ L, const double* dtp, int stage) {
   if (t >= m) return;
@@ -373,20 +384,45 @@ SVIE_DEV void rk_at(long long t, float* __restrict__ phi, const int32_t* __restr
   }
   const double dtd = *dtp;
   if (!(dtd > 0.0) || !isfinite(dtd)) return;
-  const float dt = (float)dtd;
-  const float a = u0[t], dl = dt * L[t];
-  if (stage == 1) {
-    phi[i] = a + dl;
-  } else if (stage == 2) {
-    phi[i] = 0.75f * a + 0.25f * (phi[i] + dl);
-  } else {
-    phi[i] = a / 3.0f + (float)(2.0 / 3.0) * (phi[i] + dl);
-  }
+  phi[i] = rk_value(stage, u0[t], L[t], stage >= 2 ? phi[i] : 0.0f, (float)dtd);
 }
 
-__global__ void k_rk(float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
-                     const float* __restrict__ u0, const float* __restrict__ L, const double* dtp, int stage) {
-  rk_at((long long)blockIdx.x * blockDim.x + threadIdx.x, phi, band, m, u0, L, dtp, stage);
+// RK_PER entries per thread, at a stride of the block size (coalesced list
+// reads): every list read of the thread is issued before the dependent reads
+// of phi, so that RK_PER independent chains of two loads are in flight
+// instead of one.  The same values as rk_at.
+constexpr int RK_PER = 4;
+
+__global__ void __launch_bounds__(256) k_rk(float* __restrict__ phi, const int32_t* __restrict__ band, long long m,
+                                            const float* __restrict__ u0, const float* __restrict__ L,
+                                            const double* dtp, int stage) {
+  const long long t0 = (long long)blockIdx.x * blockDim.x * RK_PER + threadIdx.x;
+  if (stage == 0) {
+#pragma unroll
+    for (int u = 0; u < RK_PER; ++u) {
+      const long long t = t0 + (long long)u * blockDim.x;
+      if (t < m) phi[band[t]] = u0[t];
+    }
+    return;
+  }
+  const double dtd = *dtp;
+  if (!(dtd > 0.0) || !isfinite(dtd)) return;
+  const float dt = (float)dtd;
+  int i[RK_PER];
+  float a[RK_PER], l[RK_PER], p[RK_PER];
+#pragma unroll
+  for (int u = 0; u < RK_PER; ++u) {
+    const long long t = t0 + (long long)u * blockDim.x;
+    const bool in = t < m;
+    i[u] = in ? band[t] : -1;
+    a[u] = in ? u0[t] : 0.0f;
+    l[u] = in ? L[t] : 0.0f;
+  }
+#pragma unroll
+  for (int u = 0; u < RK_PER; ++u) p[u] = (stage >= 2 && i[u] >= 0) ? phi[i[u]] : 0.0f;
+#pragma unroll
+  for (int u = 0; u < RK_PER; ++u)
+    if (i[u] >= 0) phi[i[u]] = rk_value(stage, a[u], l[u], p[u], dt);
 }
 
 }  // namespace svie
@@ -480,7 +516,7 @@ int svie_rk_stage(float* phi, const int32_t* band, int64_t m, const float* u0, c
     return SVIE_ERR_ARG;
   }
   if (m == 0) return SVIE_OK;
-  k_rk<<<blocks_for(m, 256), 256, 0, (cudaStream_t)stream>>>(phi, band, m, u0, L, dt, stage);
+  k_rk<<<blocks_for((m + RK_PER - 1) / RK_PER, 256), 256, 0, (cudaStream_t)stream>>>(phi, band, m, u0, L, dt, stage);
   return launch_status("svie_rk_stage");
 }
 
