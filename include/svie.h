@@ -334,6 +334,13 @@ int svie_conv_jit(int nx, int ny, int nz);
 int svie_conv_jit_enabled(int nx, int ny, int nz);
 int svie_conv_jit_ready(int nx, int ny, int nz);
 int svie_conv_jit_wait(int timeout_ms);
+/* Stops the compile worker: drops the queued compilations, waits (at most
+ * 10 s) for the one in progress and joins the thread; later svie_conv_jit
+ * requests run the library's passes.  A host calls it on its exit path before
+ * the process tears its libraries down, so that no compilation runs inside
+ * NVRTC during that teardown (the Python package registers it at interpreter
+ * exit). */
+int svie_conv_jit_stop(void);
 int svie_conv_jit_source(int n, int minb, char* buf, size_t buf_bytes);
 int svie_conv_set_choice(int nx, int ny, int nz, int z, int y, int x);
 /* Full complex64 half spectrum K^ (rfftn of the wrapped kernel, svi.py:76-81). */

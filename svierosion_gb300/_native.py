@@ -8,6 +8,7 @@ non-zero status codes into Python exceptions.
 
 from __future__ import annotations
 
+import atexit
 import ctypes
 import math
 import os
@@ -146,6 +147,7 @@ _SIGS = {
     "svie_conv_jit_enabled": (I, [I, I, I]),
     "svie_conv_jit_ready": (I, [I, I, I]),
     "svie_conv_jit_wait": (I, [I]),
+    "svie_conv_jit_stop": (I, []),
     "svie_conv_jit_source": (I, [I, I, ctypes.c_char_p, Z]),
     "svie_conv_set_choice": (I, [I, I, I, I, I, I]),
     "svie_rfft3": (I, [V, I, I, I, V, V, V]),
@@ -239,6 +241,8 @@ def load(path: str | os.PathLike | None = None):
         fn.restype = res
         fn.argtypes = args
     _lib = lib
+    # the compile worker stops at interpreter exit, before the C-level teardown of NVRTC
+    atexit.register(lib.svie_conv_jit_stop)
     return lib
 
 

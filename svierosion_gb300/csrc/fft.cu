@@ -1135,6 +1135,11 @@ int svie_conv_jit_ready(int nx, int ny, int nz) {
   return !fits(z_smem(0, nz)) || jit_z(nz, az.radices, az.nst, &f, &g) == SVIE_OK;
 }
 
+int svie_conv_jit_stop(void) {
+  jit_stop();
+  return SVIE_OK;
+}
+
 int svie_conv_jit_wait(int timeout_ms) {
   if (timeout_ms < 0) {
     set_error("svie_conv_jit_wait: negative timeout");

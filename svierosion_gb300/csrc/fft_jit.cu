@@ -57,6 +57,12 @@ const Nvrtc& nvrtc() {
     for (const char* name : {"libnvrtc.so.13", "libnvrtc.so", "/usr/local/cuda/lib64/libnvrtc.so"})
       if ((h = dlopen(name, RTLD_NOW | RTLD_LOCAL))) break;
     if (!h) return;
+    // the builtins library NVRTC opens at its first compilation, opened here already: then it,
+    // like NVRTC, is loaded before the exit handler that stops the worker is registered, and is
+    // torn down after that handler has run
+    for (const char* name : {"libnvrtc-builtins.so.13.0", "libnvrtc-builtins.so",
+                             "/usr/local/cuda/lib64/libnvrtc-builtins.so"})
+      if (dlopen(name, RTLD_NOW | RTLD_LOCAL)) break;
     n.create = (decltype(n.create))dlsym(h, "nvrtcCreateProgram");
     n.compile = (decltype(n.compile))dlsym(h, "nvrtcCompileProgram");
     n.log_size = (decltype(n.log_size))dlsym(h, "nvrtcGetProgramLogSize");
@@ -301,17 +307,21 @@ void build_module(Key key, std::string src, std::vector<std::string> names) {
 
 // One background worker compiles the requested modules in turn (a served
 // stream may request many axis lengths at once; one core compiles them).  It
-// exits when idle for a moment and the next request starts a new one.  At
-// process exit, stop_worker drops the queued jobs and waits (bounded) for the
-// compilation in progress, so that no thread is inside NVRTC while the
-// libraries are torn down.
+// exits when idle for a moment and the next request starts a new one.
+// stop_worker drops the queued jobs, waits (bounded) for the compilation in
+// progress and joins the worker, so that no thread of this library runs while
+// the libraries are torn down.  It must run before NVRTC's own teardown: the
+// exit handler registered here runs after the handlers of everything NVRTC
+// initialises during its first compilation, so a host calls svie_conv_jit_stop
+// on its exit path first (the Python package does so at interpreter exit).
 struct Job {
   Key key;
   std::string src;
   std::vector<std::string> names;
 };
 std::deque<Job>& g_jobs = *new std::deque<Job>;
-bool g_worker = false;   // a worker thread exists (under g_mu)
+std::thread& g_thread = *new std::thread;  // the worker (never destroyed, like the objects above)
+bool g_worker = false;   // a worker thread runs its loop (under g_mu)
 bool g_busy = false;     // it is compiling (under g_mu)
 bool g_stop = false;     // the process is exiting (under g_mu)
 
@@ -319,7 +329,14 @@ void stop_worker() {
   std::unique_lock<std::mutex> lock(g_mu);
   g_stop = true;
   g_jobs.clear();
-  g_cv.wait_for(lock, std::chrono::seconds(10), [] { return !g_busy; });
+  g_cv.notify_all();
+  // the worker leaves its loop as soon as it is not compiling
+  const bool left = g_cv.wait_for(lock, std::chrono::seconds(10), [] { return !g_worker; });
+  lock.unlock();
+  if (g_thread.joinable()) {
+    if (left) g_thread.join();
+    else g_thread.detach();  // still inside a compilation after 10 s: left behind
+  }
 }
 
 void worker() {
@@ -329,6 +346,8 @@ void worker() {
       std::unique_lock<std::mutex> lock(g_mu);
       if (!g_cv.wait_for(lock, std::chrono::milliseconds(200), [] { return g_stop || !g_jobs.empty(); }) || g_stop) {
         g_worker = false;
+        lock.unlock();
+        g_cv.notify_all();
         return;
       }
       job = std::move(g_jobs.front());
@@ -363,8 +382,10 @@ int jit_get(const Key& key, const std::string& src, const std::vector<std::strin
         std::atexit(stop_worker);
         registered = true;
       }
+      // a worker that left its loop when idle has returned or is returning (it needs no lock)
+      if (g_thread.joinable()) g_thread.join();
       g_worker = true;
-      std::thread(worker).detach();
+      g_thread = std::thread(worker);
     }
     lock.unlock();
     g_cv.notify_all();
@@ -440,6 +461,8 @@ int jit_z(int n, unsigned long long radices, int nst, CUfunction* r2c, CUfunctio
 }
 
 bool jit_available() { return nvrtc().ok && driver().ok; }
+
+void jit_stop() { stop_worker(); }
 
 int jit_wait(int timeout_ms) {
   std::unique_lock<std::mutex> lock(g_mu);

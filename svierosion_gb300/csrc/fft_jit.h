@@ -26,6 +26,10 @@ bool jit_available();
 // none is still running).
 int jit_wait(int timeout_ms);
 
+// Drops the queued compilations, waits (at most 10 s) for the one in progress
+// and joins the worker; later requests are refused.  For a host's exit path.
+void jit_stop();
+
 // Launches a compiled pass on `s` (a dependent launch when `chained`); false
 // when the launch failed (the caller then launches the library's pass).
 bool jit_launch(CUfunction fn, dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool chained, void** args);

@@ -8,6 +8,7 @@ import json
 import os
 import subprocess
 import sys
+import time
 from pathlib import Path
 
 import pytest
@@ -56,3 +57,34 @@ def test_dependent_launches_and_tuning_change_no_bits():
     assert base["tma_timeouts"] == 0
     for extra in ({"SVIE_PDL": "0"}, {"SVIE_FFT_TUNE": "all"}, {"SVIE_TMA": "0"}, {"SVIE_FFT_JIT": "all"}):
         assert _run(extra) == base, extra
+
+
+EXIT_SCRIPT = r"""
+import sys, time
+sys.path.insert(0, sys.argv[1])
+import torch
+from svierosion_gb300 import _native as nat
+torch.cuda.init()
+torch.zeros(1, device="cuda")
+lib = nat.lib()
+mode = sys.argv[2]
+assert lib.svie_conv_jit(448, 336, 245) == 0
+if mode in ("idle", "gone"):
+    assert lib.svie_conv_jit_wait(120000) == 0 and lib.svie_conv_jit_ready(448, 336, 245)
+if mode == "gone":
+    time.sleep(0.5)
+print("exiting", mode, flush=True)
+"""
+
+
+@pytest.mark.parametrize("mode", ["compiling", "idle", "gone"])
+def test_process_exits_cleanly_around_the_compile_worker(mode):
+    """A process that requested the passes compiled for a shape exits with status 0, whether its
+    background worker is still compiling (the exit waits for that compilation and joins the
+    worker), idle in its loop, or already gone."""
+    t0 = time.time()
+    r = subprocess.run([sys.executable, "-c", EXIT_SCRIPT, str(ROOT), mode], capture_output=True, text=True,
+                       timeout=240)
+    assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
+    assert "exiting " + mode in r.stdout
+    assert time.time() - t0 < 200
