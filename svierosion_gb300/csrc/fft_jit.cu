@@ -377,7 +377,8 @@ int jit_get(const Key& key, const std::string& src, const std::vector<std::strin
     if (!g_worker) {
       static bool registered = false;
       if (!registered) {
-        // NVRTC is opened first, so that this handler runs before its teardown
+        // NVRTC and its builtins are opened first, so that this handler (the fallback of
+        // svie_conv_jit_stop) runs before those libraries are torn down
         nvrtc();
         std::atexit(stop_worker);
         registered = true;
