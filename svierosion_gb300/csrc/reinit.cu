@@ -210,7 +210,7 @@ SVIE_DEV int warp_exclusive(int v) {
 // Pass 1: flags and sign bits from the 7-point stencil; per-warp counts of
 // the flagged distances (wbase) and of the general entries (wx).
 __global__ void k_reinit_count(const float* __restrict__ f, const int32_t* __restrict__ idx, long long m, int sx,
-                               int sy, int sz, float h, float cfl, void* geo) {
+                               int sy, int sz, float cfl, void* geo) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   Geo g = geo_view(geo, m);
   uint32_t flags = 0;
@@ -300,9 +300,8 @@ __global__ void k_reinit_geometry_full(const float* __restrict__ f, const int32_
 // caller): pass 1 counts, pass 2 (after the scan) writes the distances.  The
 // grid indices are not known here: both sweep lists stay empty (svie_reinit_rhs
 // reads the entries by position).  dtau is not kept: the RHS does not use it.
-__global__ void k_reinit_pack(const float* __restrict__ sgn, const float* __restrict__ dtau,
-                              const uint8_t* __restrict__ flags6, const float* __restrict__ dist6, long long m,
-                              void* geo, int pass) {
+__global__ void k_reinit_pack(const float* __restrict__ sgn, const uint8_t* __restrict__ flags6,
+                              const float* __restrict__ dist6, long long m, void* geo, int pass) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   Geo g = geo_view(geo, m);
   uint32_t flags = 0;
@@ -731,7 +730,7 @@ int svie_reinit_geometry(const float* phi, const int32_t* idx, int64_t m, int64_
   cudaStream_t s = (cudaStream_t)stream;
   const GeoLayout L = geo_layout(m);
   const int nb = blocks_for(m, RI_THREADS);
-  k_reinit_count<<<nb, RI_THREADS, 0, s>>>(phi, idx, m, sx, sy, sz, h, cfl, geo);
+  k_reinit_count<<<nb, RI_THREADS, 0, s>>>(phi, idx, m, sx, sy, sz, cfl, geo);
   char* b = (char*)geo;
   int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
   ns += scan_exclusive_i32((int*)(b + L.wx), L.W + 1, (int*)(b + L.sums), s);
@@ -814,11 +813,11 @@ int svie_reinit_geometry_pack(const float* sgn, const float* dtau, const uint8_t
   cudaStream_t s = (cudaStream_t)stream;
   const GeoLayout L = geo_layout(m);
   const int nb = blocks_for(m, 256);
-  k_reinit_pack<<<nb, 256, 0, s>>>(sgn, dtau, flags, dist6, m, geo, 0);
+  k_reinit_pack<<<nb, 256, 0, s>>>(sgn, flags, dist6, m, geo, 0);
   char* b = (char*)geo;
   int ns = scan_exclusive_i32((int*)(b + L.wbase), L.W + 1, (int*)(b + L.sums), s);
   ns += scan_exclusive_i32((int*)(b + L.wx), L.W + 1, (int*)(b + L.sums), s);
-  k_reinit_pack<<<nb, 256, 0, s>>>(sgn, dtau, flags, dist6, m, geo, 1);
+  k_reinit_pack<<<nb, 256, 0, s>>>(sgn, flags, dist6, m, geo, 1);
   return launch_status("svie_reinit_geometry_pack", 2 + ns);
 }
 
