@@ -87,3 +87,58 @@ def test_mesh_bounds_without_a_device_copy():
     lo, hi = m.bounds
     top = np.asarray(g.origin) + g.spacing * (np.asarray(g.shape) - 1)
     assert np.all(np.asarray(g.origin) < lo) and np.all(top > hi)
+
+
+class _FakeConvLib:
+    """Stand-in for the library's convolution entry points the per-shape set-up calls."""
+
+    def __init__(self, jit_ok: bool):
+        self.jit_ok = jit_ok
+        self.jit_on = False
+        self.kept = False
+        self.calls = []
+
+    def svie_conv_jit_enabled(self, nx, ny, nz):
+        return int(self.jit_on)
+
+    def svie_conv_jit(self, nx, ny, nz):
+        self.calls.append("jit")
+        self.jit_on = self.jit_ok
+        return 0 if self.jit_ok else 5
+
+    def svie_conv_get_choice(self, nx, ny, nz, z, y, x):
+        return int(self.kept)
+
+
+@pytest.mark.parametrize("jit_ok", [True, False])
+def test_shape_setup_tunes_only_without_compiled_passes(monkeypatch, jit_ok):
+    """At a large shape's first convolution the passes compiled for its axis lengths are requested;
+    when that succeeds the fixed rule's forms stay (no timing of the library's passes while the
+    compiled ones build), otherwise the pass forms are tuned."""
+    import torch
+    from svierosion_gb300 import svi
+
+    fake = _FakeConvLib(jit_ok)
+    tuned = []
+    monkeypatch.setattr(svi.nat, "lib", lambda: fake)
+    monkeypatch.setattr(svi.nat, "call", lambda name, *a: tuned.append(name))
+    monkeypatch.setattr(svi.nat, "ptr", lambda t: None)
+    monkeypatch.setattr(svi.nat, "stream", lambda: None)
+    monkeypatch.setattr(torch.cuda, "is_current_stream_capturing", lambda: False)
+    monkeypatch.setattr(svi, "save_tuned_forms", lambda device, shape: None)
+    monkeypatch.setattr(svi, "load_tuned_forms", lambda device, shape: False)
+    monkeypatch.delenv("SVIE_FFT_JIT", raising=False)
+    monkeypatch.delenv("SVIE_FFT_TUNE", raising=False)
+    conv = object.__new__(svi.BallConvolution)
+    conv.device = torch.device("cuda", 0)
+    conv.grid = Grid((0.0, 0.0, 0.0), 1.0, (448, 336, 245))
+    conv.plan = None
+    key = (0, (448, 336, 245))
+    svi._TUNED.discard(key)
+    try:
+        conv._tune(torch.zeros(1), torch.zeros(1), torch.zeros(16, dtype=torch.uint8))
+        assert fake.calls == ["jit"]
+        assert tuned == ([] if jit_ok else ["svie_conv_tune"])
+        assert key in svi._TUNED
+    finally:
+        svi._TUNED.discard(key)
