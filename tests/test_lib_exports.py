@@ -70,6 +70,19 @@ def test_fft_form_table_without_gpu(lib):
     assert get(448, 336, 245) == (0, 0, 1, 0)
 
 
+def test_compile_worker_stop_without_gpu(lib):
+    """Stopping the compile worker when none was started returns at once (the interpreter-exit hook
+    runs it in every process that loaded the library), and may be repeated.  In a child process:
+    a stopped worker refuses later compilations for the rest of its process."""
+    import subprocess
+    import sys
+    code = ("import sys, time; sys.path.insert(0, sys.argv[1]); from svierosion_gb300 import _native as n; "
+            "l = n.load(); t0 = time.time(); assert l.svie_conv_jit_stop() == 0 and l.svie_conv_jit_stop() == 0; "
+            "assert time.time() - t0 < 1.0")
+    r = subprocess.run([sys.executable, "-c", code, str(ROOT)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+
+
 def test_no_cpu_fallback():
     import torch
     import svierosion_gb300 as S
