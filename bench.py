@@ -249,6 +249,20 @@ class ClockSampler:
                                          stdout=self.file, stderr=subprocess.DEVNULL)
         except (OSError, ValueError):
             self.proc = None
+        self.mark_at = 0
+
+    def wait_ready(self, timeout: float = 5.0) -> None:
+        """Wait for nvidia-smi's first sample, so that its start-up stays out of the timed steps."""
+        if self.proc is None:
+            return
+        t_end = time.time() + timeout
+        while time.time() < t_end and os.path.getsize(self.file.name) == 0:
+            time.sleep(0.01)
+
+    def mark(self) -> None:
+        """Samples written from here on are the timed region's."""
+        if self.proc is not None:
+            self.mark_at = os.path.getsize(self.file.name)
 
     def stop(self) -> dict:
         if self.proc is None:
@@ -260,8 +274,15 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.file.flush()
-        self.file.seek(0)
-        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.count(",") >= 8]
+        # read from the mark through a handle of our own (nvidia-smi shares the offset of self.file);
+        # a line cut by the mark is dropped
+        with open(self.file.name) as fh:
+            fh.seek(max(self.mark_at - 1, 0))
+            text = fh.read()
+        if self.mark_at > 0:
+            nl = text.find("\n")
+            text = text[nl + 1:] if nl >= 0 else ""
+        rows = [r.split(",") for r in text.strip().splitlines() if r.count(",") >= 8]
         os.unlink(self.file.name)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
@@ -332,10 +353,15 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     torch.cuda.synchronize()
     t_setup = time.time() - t_setup
     band0 = ls.work32.numel()
-    sim.run(target_fraction=None, max_steps=args.warmup)
     # the convolution passes compiled for this grid's axis lengths start compiling at its first
-    # convolution (background threads): part of the warm-up, finished before the timed steps
+    # convolution (a background thread): the first warm-up step, the wait for them, then the other
+    # warm-up steps, so that the compiled passes have run once before the timed steps
+    sim.run(target_fraction=None, max_steps=1)
     nat.lib().svie_conv_jit_wait(120000)
+    # nvidia-smi starts during the last warm-up steps; its samples count from the timed region's start
+    clocks = ClockSampler(local_rank)
+    sim.run(target_fraction=None, max_steps=args.warmup - 1)
+    clocks.wait_ready()
     # timed region: events only around each reinitialisation's sweeps (the
     # dominant kernel, one pair per call); the full per-kernel breakdown comes
     # from a second pass below.  Events between the convolution passes would
@@ -346,8 +372,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local_rank)
-    time.sleep(0.1)
+    clocks.mark()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     u0 = sim.band_updates

@@ -815,13 +815,15 @@ static void launch_y(const Plans& P, int nx, int ny, int nz, float2* spec, int m
   } else if (c == 1) {
     const dim3 g((unsigned)((nzh + 7) / 8), (unsigned)nx);
     CUfunction jf = nullptr;
-    if (jit && jit_strided(ny, 4, P.y.radices, P.y.nst, &jf) == SVIE_OK) {
+    if (jit && jit_strided(ny, JIT_Y_MINB, P.y.radices, P.y.nst, &jf) == SVIE_OK) {
       long long stride = nzp, ostr_ = ostr;
       int ninner = nzh, mode_ = mode, need_ = need;
       AxisPlan ax = P.y;
       KGeom kg = K;
       void* args[] = {&spec, &ax, &stride, &ninner, &ostr_, &mode_, &kg, &slabflag, &need_};
-      if (jit_launch(jf, g, dim3(FFT_T), smem, s, chained, args)) return;
+      // the two tile buffers only: this pass reads its stage twiddles from the plan
+      const size_t jsmem = 2 * 8 * (size_t)ny * sizeof(float2);
+      if (jit_launch(jf, g, dim3(FFT_T), jsmem, s, chained, args)) return;
     }
     CUtensorMap map;
     const int rows = spectrum_map(&map, spec, nx, ny, nzp, ny, 0);
@@ -1112,7 +1114,7 @@ int svie_conv_jit(int nx, int ny, int nz) {
   }
   // request the three passes (their compilations start on background threads)
   CUfunction fy = nullptr, fx = nullptr, zf = nullptr, zi = nullptr;
-  jit_strided(ny, 4, ay.radices, ay.nst, &fy);
+  jit_strided(ny, JIT_Y_MINB, ay.radices, ay.nst, &fy);
   jit_strided(nx, 3, ax.radices, ax.nst, &fx);
   if (fits(z_smem(0, nz))) jit_z(nz, az.radices, az.nst, &zf, &zi);
   const GridKey k = grid_key(nx, ny, nz);
@@ -1130,7 +1132,8 @@ int svie_conv_jit_ready(int nx, int ny, int nz) {
   AxisPlan ax, ay, az;
   if (!factor_axis(nx, &ax) || !factor_axis(ny, &ay) || !factor_axis(nz, &az) || !jit_available()) return 0;
   CUfunction f = nullptr, g = nullptr;
-  if (jit_strided(ny, 4, ay.radices, ay.nst, &f) != SVIE_OK || jit_strided(nx, 3, ax.radices, ax.nst, &f) != SVIE_OK)
+  if (jit_strided(ny, JIT_Y_MINB, ay.radices, ay.nst, &f) != SVIE_OK ||
+      jit_strided(nx, 3, ax.radices, ax.nst, &f) != SVIE_OK)
     return 0;
   return !fits(z_smem(0, nz)) || jit_z(nz, az.radices, az.nst, &f, &g) == SVIE_OK;
 }

@@ -120,7 +120,10 @@ std::string csrc_dir() {
 
 // Source of the 8-line strided pass for an axis of n positions with the given
 // radix sequence (forward order): the body of k_fft_strided<8, MINB> on its
-// cp.async path, with each stage unrolled at compile time.
+// cp.async path, with each stage unrolled at compile time.  With minb >= 5 (the
+// y passes) the stage twiddles are read from the plan in global memory, not
+// staged in shared memory: the tile buffers alone (16 n float2) then let five
+// CTAs share an SM.
 std::string strided_source(int n, int minb, const std::vector<int>& r) {
   const int nst = (int)r.size();
   std::string s;
@@ -144,11 +147,16 @@ std::string strided_source(int n, int minb, const std::vector<int>& r) {
        "  for (int e = threadIdx.x; e < 4 * n; e += 256) {\n"
        "    const int row = e >> 2, part = 2 * (e & 3);\n"
        "    cp_async16(sa + row * LW + part, base + row * stride + part);\n  }\n"
-       "  cp_async_commit();\n"
-       "  const float2* stw = stage_twiddles_to_smem(sm, LW, P);\n"
-       "  if (mode == 2)\n"
-       "    for (int e = threadIdx.x; e < n - 1; e += 256) sm[2 * LW * n + n + e] = __ldg(P.rstw + e);\n"
-       "  cp_async_wait<0>();\n  __syncthreads();\n";
+       "  cp_async_commit();\n";
+  const bool gtw = minb >= 5;  // stage twiddles (both orders) read from the plan
+  if (gtw) {
+    s += "  const float2* stw = P.stw;\n";
+  } else {
+    s += "  const float2* stw = stage_twiddles_to_smem(sm, LW, P);\n"
+         "  if (mode == 2)\n"
+         "    for (int e = threadIdx.x; e < n - 1; e += 256) sm[2 * LW * n + n + e] = __ldg(P.rstw + e);\n";
+  }
+  s += "  cp_async_wait<0>();\n  __syncthreads();\n";
   const char* cur = "sa";
   const char* oth = "sb";
   int p = 1;
@@ -162,7 +170,8 @@ std::string strided_source(int n, int minb, const std::vector<int>& r) {
   add("  if (mode != 2) {\n    last_stage_c<%d, %d, 8, 8, 256>(%s, stw, %s, StoreEpi{base, stride, nl, mode != 0});\n"
       "    return;\n  }\n",
       rl, n / rl, cur, nst == 1 ? "mode == 1" : "false");
-  s += "  const float2* rstw = stw + n;\n  const int nyh = K.ny / 2 + 1;\n"
+  s += gtw ? "  const float2* rstw = P.rstw;\n" : "  const float2* rstw = stw + n;\n";
+  s += "  const int nyh = K.ny / 2 + 1;\n"
        "  const int y = blockIdx.y, yr = min(y, K.ny - y);\n";
   add("  last_stage_c<%d, %d, 8, 8, 256>(%s, stw, false, KEpi<8>{%s, K.kred + (long long)yr * K.nzh + c0,\n"
       "      (long long)nyh * K.nzh, n, nl});\n  __syncthreads();\n",

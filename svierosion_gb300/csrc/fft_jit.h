@@ -15,6 +15,10 @@ namespace svie {
 // made, an error status with *fn = null.
 int jit_strided(int n, int minb, unsigned long long radices, int nst, CUfunction* fn);
 
+// CTAs per SM of the compiled y passes: from 5 up they read their stage
+// twiddles from the plan instead of shared memory, so that five tiles fit.
+constexpr int JIT_Y_MINB = 5;
+
 // The z passes (16 line pairs per CTA) compiled for an axis of n positions:
 // the forward (R2C) and inverse (C2R) kernels of one module.
 int jit_z(int n, unsigned long long radices, int nst, CUfunction* r2c, CUfunction* c2r);
