@@ -854,7 +854,7 @@ static void launch_x(const Plans& P, int nx, int ny, int nz, float2* spec, int m
   } else if (c == 0) {
     const dim3 g((unsigned)((nzh + 7) / 8), (unsigned)ny);
     CUfunction jf = nullptr;
-    if (jit && jit_strided(nx, 3, P.x.radices, P.x.nst, &jf) == SVIE_OK) {
+    if (jit && jit_strided(nx, JIT_X_MINB, P.x.radices, P.x.nst, &jf) == SVIE_OK) {
       long long stride = lstr, ostr_ = nzp;
       int ninner = nzh, mode_ = mode, need_ = 0;
       AxisPlan ax = P.x;
@@ -1115,7 +1115,7 @@ int svie_conv_jit(int nx, int ny, int nz) {
   // request the three passes (their compilations start on background threads)
   CUfunction fy = nullptr, fx = nullptr, zf = nullptr, zi = nullptr;
   jit_strided(ny, JIT_Y_MINB, ay.radices, ay.nst, &fy);
-  jit_strided(nx, 3, ax.radices, ax.nst, &fx);
+  jit_strided(nx, JIT_X_MINB, ax.radices, ax.nst, &fx);
   if (fits(z_smem(0, nz))) jit_z(nz, az.radices, az.nst, &zf, &zi);
   const GridKey k = grid_key(nx, ny, nz);
   std::lock_guard<std::mutex> lock(g_choice_mu);
@@ -1133,7 +1133,7 @@ int svie_conv_jit_ready(int nx, int ny, int nz) {
   if (!factor_axis(nx, &ax) || !factor_axis(ny, &ay) || !factor_axis(nz, &az) || !jit_available()) return 0;
   CUfunction f = nullptr, g = nullptr;
   if (jit_strided(ny, JIT_Y_MINB, ay.radices, ay.nst, &f) != SVIE_OK ||
-      jit_strided(nx, 3, ax.radices, ax.nst, &f) != SVIE_OK)
+      jit_strided(nx, JIT_X_MINB, ax.radices, ax.nst, &f) != SVIE_OK)
     return 0;
   return !fits(z_smem(0, nz)) || jit_z(nz, az.radices, az.nst, &f, &g) == SVIE_OK;
 }

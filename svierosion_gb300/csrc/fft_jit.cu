@@ -120,10 +120,10 @@ std::string csrc_dir() {
 
 // Source of the 8-line strided pass for an axis of n positions with the given
 // radix sequence (forward order): the body of k_fft_strided<8, MINB> on its
-// cp.async path, with each stage unrolled at compile time.  With minb >= 5 (the
-// y passes) the stage twiddles are read from the plan in global memory, not
-// staged in shared memory: the tile buffers alone (16 n float2) then let five
-// CTAs share an SM.
+// cp.async path, with each stage unrolled at compile time.  With minb >= 4 the
+// stage twiddles (both orders) are read from the plan in global memory, not
+// staged in shared memory: the tile buffers alone (16 n float2) then let more
+// CTAs share an SM (five y tiles of n = 336).
 std::string strided_source(int n, int minb, const std::vector<int>& r) {
   const int nst = (int)r.size();
   std::string s;
@@ -148,7 +148,7 @@ std::string strided_source(int n, int minb, const std::vector<int>& r) {
        "    const int row = e >> 2, part = 2 * (e & 3);\n"
        "    cp_async16(sa + row * LW + part, base + row * stride + part);\n  }\n"
        "  cp_async_commit();\n";
-  const bool gtw = minb >= 5;  // stage twiddles (both orders) read from the plan
+  const bool gtw = minb >= 4;  // stage twiddles (both orders) read from the plan
   if (gtw) {
     s += "  const float2* stw = P.stw;\n";
   } else {
@@ -298,9 +298,12 @@ void build_module(Key key, std::string src, std::vector<std::string> names) {
   const std::vector<char> cubin = ok ? compile(src, &err) : std::vector<char>();
   CUmodule mod = nullptr;
   ok = ok && !cubin.empty() && d.load(&mod, cubin.data()) == CUDA_SUCCESS;
-  for (size_t k = 0; ok && k < names.size(); ++k)
+  for (size_t k = 0; ok && k < names.size(); ++k) {
     ok = d.get_function(&fns.f[k], mod, names[k].c_str()) == CUDA_SUCCESS &&
          d.set_attribute(fns.f[k], CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 227 * 1024) == CUDA_SUCCESS;
+    // all of the unified L1/shared storage as shared memory, for as many resident tiles as fit
+    if (ok) d.set_attribute(fns.f[k], CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100);
+  }
   if (!ok) {
     fns = Fns();
     fprintf(stderr, "[svie] fft jit: no pass for n = %d (%s); the library's pass is used\n", key.n,

@@ -15,9 +15,12 @@ namespace svie {
 // made, an error status with *fn = null.
 int jit_strided(int n, int minb, unsigned long long radices, int nst, CUfunction* fn);
 
-// CTAs per SM of the compiled y passes: from 5 up they read their stage
-// twiddles from the plan instead of shared memory, so that five tiles fit.
-constexpr int JIT_Y_MINB = 5;
+// CTAs per SM of the compiled y and x passes.  From 4 up a compiled pass reads
+// its stage twiddles from the plan instead of shared memory (its tiles need 16 n
+// float2 only): five y tiles of n = 336 then fit.  The x passes keep theirs in
+// shared memory at three CTAs per SM (four, with the twiddles from the plan,
+// measured no faster).
+constexpr int JIT_Y_MINB = 5, JIT_X_MINB = 3;
 
 // The z passes (16 line pairs per CTA) compiled for an axis of n positions:
 // the forward (R2C) and inverse (C2R) kernels of one module.
