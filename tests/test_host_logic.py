@@ -142,3 +142,35 @@ def test_shape_setup_tunes_only_without_compiled_passes(monkeypatch, jit_ok):
         assert key in svi._TUNED
     finally:
         svi._TUNED.discard(key)
+
+
+class _FakeSampler:
+    def terminate(self):
+        pass
+
+    def wait(self, timeout=None):
+        return 0
+
+    def kill(self):
+        pass
+
+
+def test_clock_samples_count_from_the_timed_region(tmp_path):
+    """bench.py's nvidia-smi sampler starts during the warm-up; only the lines written after the timed
+    region's mark count, and a line cut by the mark is dropped."""
+    import bench
+    path = tmp_path / "clocks.csv"
+    warm = "0, 1800, 2070, 700.0, 0x0, Not Active, Not Active, Not Active, Not Active\n"
+    timed = "0, 2070, 2070, 900.0, 0x0, Not Active, Not Active, Not Active, Active\n"
+    path.write_text(warm * 3 + warm[:10])
+    s = object.__new__(bench.ClockSampler)
+    s.file = open(path, "a+")
+    s.proc = _FakeSampler()
+    s.mark_at = 0
+    s.mark()
+    with open(path, "a") as fh:
+        fh.write(warm[10:] + timed * 4)
+    out = s.stop()
+    assert out["samples"] == 4 and out["sm_mhz"] == 2070.0 and out["sm_max_mhz"] == 2070.0
+    assert out["reasons"] == ["sw_power_cap"]
+    assert not path.exists()
