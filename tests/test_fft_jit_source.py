@@ -39,8 +39,9 @@ def _compile(nv, src: bytes):
 
 
 # minb 0: the z passes (forward and inverse); else the 8-line strided pass for that many CTAs per SM
-@pytest.mark.parametrize("n,minb", [(336, 4), (336, 5), (448, 3), (448, 4), (245, 4), (90, 4), (7, 3), (1792, 3), (245, 0), (175, 0),
-                                    (128, 0), (7, 0)])
+# (from 4 CTAs per SM the strided pass reads its stage twiddles from the plan)
+@pytest.mark.parametrize("n,minb", [(336, 4), (336, 5), (448, 3), (448, 4), (245, 4), (90, 4), (7, 3), (1792, 3),
+                                    (245, 0), (175, 0), (128, 0), (7, 0)])
 def test_generated_pass_compiles(n, minb):
     lib = _native.lib()
     buf = ctypes.create_string_buffer(1 << 16)
